@@ -1,0 +1,464 @@
+"""ctypes wrapper of the FP64 CPU oracle (oracle/geostat_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline / reference arm of ``bench.py`` -- never by the
+product package.  The oracle restates the reference's CPU algorithms
+(geostat-rs crates/geostat-core) and is the parity checker for the CUDA path.
+
+Models are duck-typed: any object with ``nugget`` and ``structures`` (each
+with ``kind``, ``sill``, ``range``, optional ``param`` and optional ``anis``
+carrying ``azimuth_deg``, ``ratio``, ``ratio_z``, ``dip_deg``, ``rake_deg``)
+works, so the product's ``geostat_rs.VariogramModel`` can be passed directly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libgeostat_oracle.so")
+
+KINDS = {
+    "spherical": 0, "exponential": 1, "gaussian": 2, "matern15": 3, "matern25": 4,
+    "circular": 5, "stable": 6, "hole": 7, "wave": 8, "power": 9,
+}
+
+OK, INSUFFICIENT_DATA, DIMENSION_MISMATCH, SINGULAR_SYSTEM = 0, 1, 2, 3
+INVALID_PARAMETER, NO_NEIGHBORS, DUPLICATE_POINTS = 4, 5, 6
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"oracle error {code}: {msg}")
+        self.code = code
+
+
+class _Structure(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("has_anis", C.c_int32), ("param", C.c_double),
+                ("sill", C.c_double), ("range", C.c_double), ("azimuth_deg", C.c_double),
+                ("ratio", C.c_double), ("ratio_z", C.c_double), ("dip_deg", C.c_double),
+                ("rake_deg", C.c_double)]
+
+
+class _Model(C.Structure):
+    _fields_ = [("nugget", C.c_double), ("n_structures", C.c_int32), ("pad_", C.c_int32),
+                ("s", _Structure * 4)]
+
+
+class _Kcfg(C.Structure):
+    _fields_ = [("method", C.c_int64), ("sk_mean", C.c_double), ("uk_degree", C.c_int64),
+                ("ked_nvars", C.c_int64), ("max_neighbors", C.c_int64),
+                ("min_neighbors", C.c_int64), ("max_per_octant", C.c_int64),
+                ("has_search_radius", C.c_int64), ("search_radius", C.c_double),
+                ("has_anisotropic_search", C.c_int64), ("search_azimuth_deg", C.c_double),
+                ("search_ratio", C.c_double), ("search_ratio_z", C.c_double),
+                ("search_dip_deg", C.c_double), ("search_rake_deg", C.c_double)]
+
+
+def build(quiet: bool = True) -> str:
+    """Compiles the oracle with its Makefile (no-op when up to date)."""
+    out = subprocess.run(["make", "-C", _HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return _LIB_PATH
+
+
+_lib = None
+_OBJ = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int64, C.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        _lib = C.CDLL(_LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    """Argument types for every entry point (int64_t parameters must not be
+    passed as 32-bit C ints)."""
+    d, i32, i64, u64, vp = C.c_double, C.c_int32, C.c_int64, C.c_uint64, C.c_void_p
+    pd, pi8, pi32, pi64 = (C.POINTER(C.c_double), C.POINTER(C.c_int8), C.POINTER(C.c_int32),
+                           C.POINTER(C.c_int64))
+    pm, pk = C.POINTER(_Model), C.POINTER(_Kcfg)
+    sig = {
+        "or_last_error": (C.c_char_p, []),
+        "or_model_validate": (C.c_int, [pm]),
+        "or_gamma_dh": (d, [pm, C.c_int, pd]),
+        "or_lu_solve": (C.c_int, [i64, pd, pd, pd]),
+        "or_cholesky_solve": (C.c_int, [i64, pd, pd, pd]),
+        "or_kdtree_knn": (i64, [C.c_int, i64, pd, pd, i64, C.c_int, d, pi64]),
+        "or_knn_brute": (i64, [C.c_int, i64, pd, pd, i64, C.c_int, d, pi64]),
+        "or_bucketgrid_queries": (C.c_int, [C.c_int, i64, pd, pd, pd, i64, i64, pi64, pd, i64,
+                                            C.c_int, d, pi64, pi64, pi64]),
+        "or_duplicate_pair": (C.c_int, [C.c_int, i64, pd, pi64, pi64]),
+        "or_grid_centers": (C.c_int, [C.c_int, pd, pd, pi64, pd]),
+        "or_krige": (C.c_int, [C.c_int, i64, pd, pd, pd, pd, C.c_int, pm, pk, i64, pd, pd, pd,
+                               pd, pd, pi8, pi32, i64, pi32, pi64, C.c_int]),
+        "or_maxmin_order": (C.c_int, [C.c_int, i64, pd, pi64]),
+        "or_maxmin_order_brute": (C.c_int, [C.c_int, i64, pd, pi64]),
+        "or_vecchia_plan": (C.c_int, [C.c_int, i64, pd, i64, pi64, pi64, pi64, pi32]),
+        "or_vecchia_loglik_plan": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pi64, pi64, pi32,
+                                             pd, pd]),
+        "or_vecchia_loglik": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pi64, pd]),
+        "or_exact_loglik": (C.c_int, [C.c_int, i64, pd, pd, pm, pd]),
+        "or_vecchia_predict": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pd, i64, pd, pd]),
+        "or_vecchia_mle_objective": (C.c_int, [C.c_int, i64, pd, pd, i32, d, i64, pi64, pi64,
+                                               pi32, d, i64, pd, pd]),
+        "or_vecchia_mle_setup": (C.c_int, [C.c_int, i64, pd, pd, pd, pd]),
+        "or_vecchia_mle_nm": (C.c_int, [C.c_int, i64, pd, pd, i32, d, i64, pi64, i64, pd, d, i64,
+                                        pd, pd, pi64]),
+        "or_nelder_mead_multistart": (C.c_int, [_OBJ, vp, i64, i64, pd, d, i64, pd, pd]),
+        "or_rng_u64": (None, [u64, i64, C.POINTER(C.c_uint64)]),
+        "or_rng_uniform": (None, [u64, i64, pd]),
+        "or_rng_normal": (None, [u64, i64, pd]),
+        "or_test_field_2d": (None, [i64, u64, pd, pd]),
+        "or_test_field_3d": (None, [i64, u64, pd, pd]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def _p(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+def _check(rc):
+    if rc != 0:
+        raise OracleError(rc, lib().or_last_error().decode())
+
+
+def model_struct(model) -> _Model:
+    m = _Model()
+    m.nugget = float(model.nugget)
+    structs = list(model.structures)
+    if len(structs) > 4:
+        raise ValueError("at most 4 structures")
+    m.n_structures = len(structs)
+    for i, s in enumerate(structs):
+        kind = s.kind
+        m.s[i].kind = KINDS[kind] if isinstance(kind, str) else int(kind)
+        m.s[i].param = float(getattr(s, "param", 0.0) or 0.0)
+        m.s[i].sill = float(s.sill)
+        m.s[i].range = float(s.range)
+        a = getattr(s, "anis", None)
+        if a is not None:
+            m.s[i].has_anis = 1
+            m.s[i].azimuth_deg = a.azimuth_deg
+            m.s[i].ratio = a.ratio
+            m.s[i].ratio_z = getattr(a, "ratio_z", 1.0)
+            m.s[i].dip_deg = getattr(a, "dip_deg", 0.0)
+            m.s[i].rake_deg = getattr(a, "rake_deg", 0.0)
+        else:
+            m.s[i].ratio = m.s[i].ratio_z = 1.0
+    return m
+
+
+METHODS = {"simple": 0, "ordinary": 1, "universal": 2, "external_drift": 3}
+
+
+def kcfg_struct(method="ordinary", mean=None, degree=1, n_vars=0, max_neighbors=None,
+                min_neighbors=None, max_per_octant=None, radius=None, anisotropic_search=None):
+    c = _Kcfg()
+    c.method = METHODS[method]
+    c.sk_mean = float(mean) if mean is not None else 0.0
+    c.uk_degree = int(degree)
+    c.ked_nvars = int(n_vars)
+    c.max_neighbors = -1 if max_neighbors is None else int(max_neighbors)
+    c.min_neighbors = -1 if min_neighbors is None else int(min_neighbors)
+    c.max_per_octant = -1 if max_per_octant is None else int(max_per_octant)
+    c.has_search_radius = 0 if radius is None else 1
+    c.search_radius = float(radius) if radius is not None else 0.0
+    if anisotropic_search is not None:
+        a = anisotropic_search
+        c.has_anisotropic_search = 1
+        c.search_azimuth_deg = a.azimuth_deg
+        c.search_ratio = a.ratio
+        c.search_ratio_z = getattr(a, "ratio_z", 1.0)
+        c.search_dip_deg = getattr(a, "dip_deg", 0.0)
+        c.search_rake_deg = getattr(a, "rake_deg", 0.0)
+    return c
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def gamma_dh(model, dh):
+    dh = _f64(dh)
+    m = model_struct(model)
+    return lib().or_gamma_dh(C.byref(m), len(dh), _p(dh))
+
+
+def model_validate(model):
+    m = model_struct(model)
+    _check(lib().or_model_validate(C.byref(m)))
+
+
+def lu_solve(a, b):
+    a, b = _f64(a), _f64(b)
+    x = np.zeros_like(b)
+    _check(lib().or_lu_solve(len(b), _p(a), _p(b), _p(x)))
+    return x
+
+
+def cholesky_solve(a, b):
+    a, b = _f64(a), _f64(b)
+    x = np.zeros_like(b)
+    _check(lib().or_cholesky_solve(len(b), _p(a), _p(b), _p(x)))
+    return x
+
+
+def kdtree_knn(coords, target, k, radius=None):
+    coords, target = _f64(coords), _f64(target)
+    out = np.zeros(max(min(k, len(coords)), 1), dtype=np.int64)
+    cnt = lib().or_kdtree_knn(coords.shape[1], len(coords), _p(coords), _p(target), int(k),
+                              0 if radius is None else 1, C.c_double(radius or 0.0),
+                              _p(out, C.c_int64))
+    return out[:cnt].tolist()
+
+
+def knn_brute(coords, target, k, radius=None):
+    coords, target = _f64(coords), _f64(target)
+    out = np.zeros(max(min(k, len(coords)), 1), dtype=np.int64)
+    cnt = lib().or_knn_brute(coords.shape[1], len(coords), _p(coords), _p(target), int(k),
+                             0 if radius is None else 1, C.c_double(radius or 0.0),
+                             _p(out, C.c_int64))
+    return out[:cnt].tolist()
+
+
+def bucketgrid_queries(coords, bbox_min, bbox_max, expected, q_after, q_target, k, radius=None):
+    coords = _f64(coords)
+    dim = coords.shape[1]
+    q_after = np.ascontiguousarray(q_after, dtype=np.int64)
+    q_target = _f64(q_target).reshape(-1, dim)
+    nq = len(q_after)
+    out = np.full(nq * k, -1, dtype=np.int64)
+    cnt = np.zeros(nq, dtype=np.int64)
+    dims = np.zeros(3, dtype=np.int64)
+    _check(lib().or_bucketgrid_queries(dim, len(coords), _p(coords), _p(_f64(bbox_min)),
+                                       _p(_f64(bbox_max)), int(expected), nq,
+                                       _p(q_after, C.c_int64), _p(q_target), int(k),
+                                       0 if radius is None else 1, C.c_double(radius or 0.0),
+                                       _p(out, C.c_int64), _p(cnt, C.c_int64),
+                                       _p(dims, C.c_int64)))
+    res = [out[i * k:i * k + cnt[i]].tolist() for i in range(nq)]
+    return res, dims[:dim].tolist()
+
+
+def duplicate_pair(coords):
+    coords = _f64(coords)
+    i, j = C.c_int64(), C.c_int64()
+    found = lib().or_duplicate_pair(coords.shape[1], len(coords), _p(coords), C.byref(i),
+                                    C.byref(j))
+    return (i.value, j.value) if found else None
+
+
+def grid_centers(bmin, bmax, ncell):
+    dim = len(ncell)
+    nc = np.ascontiguousarray(ncell, dtype=np.int64)
+    out = np.zeros(int(np.prod(nc)) * dim)
+    _check(lib().or_grid_centers(dim, _p(_f64(bmin)), _p(_f64(bmax)), _p(nc, C.c_int64),
+                                 _p(out)))
+    return out.reshape(-1, dim)
+
+
+def krige(coords, values, model, targets, *, method="ordinary", mean=None, degree=1,
+          max_neighbors=None, min_neighbors=None, max_per_octant=None, radius=None,
+          anisotropic_search=None, drift=None, target_drift=None, measurement_error=None,
+          nthreads=None, kcap=0):
+    """Kriging::build + predict_many(_with_drift).  Returns a dict with
+    value, variance, lagrange, status, and (kcap > 0) neighbour indices."""
+    coords, values, targets = _f64(coords), _f64(values), _f64(targets)
+    dim = coords.shape[1]
+    nt = len(targets)
+    n_vars = 0 if drift is None else np.asarray(drift).reshape(len(coords), -1).shape[1]
+    if method == "external_drift":
+        ctor = 1
+    elif measurement_error is not None:
+        ctor = 2
+    else:
+        ctor = 0
+    cfg = kcfg_struct(method, mean, degree, n_vars, max_neighbors, min_neighbors,
+                      max_per_octant, radius, anisotropic_search)
+    m = model_struct(model)
+    value, var, lag = np.zeros(nt), np.zeros(nt), np.zeros(nt)
+    status = np.zeros(nt, dtype=np.int8)
+    nbo = np.zeros(max(nt * kcap, 1), dtype=np.int32) if kcap else None
+    nbc = np.zeros(max(nt, 1), dtype=np.int32)
+    ties = C.c_int64(0)
+    dr = _f64(drift).reshape(-1) if drift is not None else None
+    tdr = _f64(target_drift).reshape(-1) if target_drift is not None else None
+    me = _f64(measurement_error) if measurement_error is not None else None
+    if nthreads is None:
+        nthreads = os.cpu_count() or 1
+    _check(lib().or_krige(dim, len(coords), _p(coords), _p(values), _p(dr), _p(me), ctor,
+                          C.byref(m), C.byref(cfg), nt, _p(targets), _p(tdr), _p(value),
+                          _p(var), _p(lag), _p(status, C.c_int8),
+                          _p(nbo, C.c_int32) if nbo is not None else None, int(kcap),
+                          _p(nbc, C.c_int32), C.byref(ties), int(nthreads)))
+    out = dict(value=value, variance=var, lagrange=lag, status=status, nb_count=nbc[:nt],
+               boundary_ties=ties.value)
+    if kcap:
+        out["neighbors"] = nbo[:nt * kcap].reshape(nt, kcap)
+    return out
+
+
+def maxmin_order(coords):
+    coords = _f64(coords)
+    out = np.zeros(len(coords), dtype=np.int64)
+    _check(lib().or_maxmin_order(coords.shape[1], len(coords), _p(coords), _p(out, C.c_int64)))
+    return out
+
+
+def maxmin_order_brute(coords):
+    coords = _f64(coords)
+    out = np.zeros(len(coords), dtype=np.int64)
+    _check(lib().or_maxmin_order_brute(coords.shape[1], len(coords), _p(coords),
+                                       _p(out, C.c_int64)))
+    return out
+
+
+def vecchia_plan(coords, m, order=None):
+    coords = _f64(coords)
+    n = len(coords)
+    o_in = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    o_out = np.zeros(n, dtype=np.int64)
+    nb = np.zeros(n * m, dtype=np.int64)
+    cnt = np.zeros(n, dtype=np.int32)
+    _check(lib().or_vecchia_plan(coords.shape[1], n, _p(coords), int(m),
+                                 _p(o_in, C.c_int64) if o_in is not None else None,
+                                 _p(o_out, C.c_int64), _p(nb, C.c_int64), _p(cnt, C.c_int32)))
+    return o_out, nb.reshape(n, m), cnt
+
+
+def vecchia_loglik_plan(coords, values, model, order, nb, cnt, terms=False):
+    coords, values = _f64(coords), _f64(values)
+    n, m = nb.shape
+    ll = C.c_double()
+    t = np.zeros(n) if terms else None
+    mm = model_struct(model)
+    _check(lib().or_vecchia_loglik_plan(coords.shape[1], n, _p(coords), _p(values), C.byref(mm),
+                                        m, _p(np.ascontiguousarray(order, np.int64), C.c_int64),
+                                        _p(np.ascontiguousarray(nb, np.int64), C.c_int64),
+                                        _p(np.ascontiguousarray(cnt, np.int32), C.c_int32),
+                                        C.byref(ll), _p(t)))
+    return (ll.value, t) if terms else ll.value
+
+
+def vecchia_loglik(coords, values, model, m, order=None):
+    coords, values = _f64(coords), _f64(values)
+    ll = C.c_double()
+    mm = model_struct(model)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    _check(lib().or_vecchia_loglik(coords.shape[1], len(coords), _p(coords), _p(values),
+                                   C.byref(mm), int(m),
+                                   _p(o, C.c_int64) if o is not None else None, C.byref(ll)))
+    return ll.value
+
+
+def exact_loglik(coords, values, model):
+    coords, values = _f64(coords), _f64(values)
+    ll = C.c_double()
+    mm = model_struct(model)
+    _check(lib().or_exact_loglik(coords.shape[1], len(coords), _p(coords), _p(values),
+                                 C.byref(mm), C.byref(ll)))
+    return ll.value
+
+
+def vecchia_predict(coords, values, model, targets, m):
+    coords, values, targets = _f64(coords), _f64(values), _f64(targets)
+    nt = len(targets)
+    v, var = np.zeros(max(nt, 1)), np.zeros(max(nt, 1))
+    mm = model_struct(model)
+    _check(lib().or_vecchia_predict(coords.shape[1], len(coords), _p(coords), _p(values),
+                                    C.byref(mm), nt, _p(targets), int(m), _p(v), _p(var)))
+    return v[:nt], var[:nt]
+
+
+def vecchia_mle_setup(coords, values):
+    coords, values = _f64(coords), _f64(values)
+    s9 = np.zeros(9)
+    rmax = C.c_double()
+    _check(lib().or_vecchia_mle_setup(coords.shape[1], len(coords), _p(coords), _p(values),
+                                      _p(s9), C.byref(rmax)))
+    return s9.reshape(3, 3), rmax.value
+
+
+def vecchia_mle_objective(coords, values, kind, m, order, nb, cnt, range_max, xs, param=0.0):
+    coords, values = _f64(coords), _f64(values)
+    xs = _f64(xs).reshape(-1, 3)
+    fx = np.zeros(len(xs))
+    _check(lib().or_vecchia_mle_objective(
+        coords.shape[1], len(coords), _p(coords), _p(values),
+        KINDS[kind] if isinstance(kind, str) else int(kind), C.c_double(param), int(m),
+        _p(np.ascontiguousarray(order, np.int64), C.c_int64),
+        _p(np.ascontiguousarray(nb, np.int64), C.c_int64),
+        _p(np.ascontiguousarray(cnt, np.int32), C.c_int32), C.c_double(range_max), len(xs),
+        _p(xs), _p(fx)))
+    return fx
+
+
+def vecchia_mle_nm(coords, values, kind, m, starts, step=0.3, max_iter=2000, order=None,
+                   param=0.0):
+    coords, values = _f64(coords), _f64(values)
+    starts = _f64(starts).reshape(-1, 3)
+    x = np.zeros(3)
+    f = C.c_double()
+    ne = C.c_int64()
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    _check(lib().or_vecchia_mle_nm(
+        coords.shape[1], len(coords), _p(coords), _p(values),
+        KINDS[kind] if isinstance(kind, str) else int(kind), C.c_double(param), int(m),
+        _p(o, C.c_int64) if o is not None else None, len(starts), _p(starts), C.c_double(step),
+        int(max_iter), _p(x), C.byref(f), C.byref(ne)))
+    return x, f.value, ne.value
+
+
+def nelder_mead_multistart(fn, starts, step, max_iter):
+    starts = _f64(starts)
+    nstarts, n = starts.shape
+    cb = _OBJ(lambda xp, nn, ctx: float(fn(np.ctypeslib.as_array(xp, shape=(nn,)).copy())))
+    x = np.zeros(n)
+    f = C.c_double()
+    _check(lib().or_nelder_mead_multistart(cb, None, n, nstarts, _p(starts), C.c_double(step),
+                                           int(max_iter), _p(x), C.byref(f)))
+    return x, f.value
+
+
+def rng_u64(seed, count):
+    out = np.zeros(count, dtype=np.uint64)
+    lib().or_rng_u64(C.c_uint64(seed), count, _p(out, C.c_uint64))
+    return out
+
+
+def rng_uniform(seed, count):
+    out = np.zeros(count)
+    lib().or_rng_uniform(C.c_uint64(seed), count, _p(out))
+    return out
+
+
+def rng_normal(seed, count):
+    out = np.zeros(count)
+    lib().or_rng_normal(C.c_uint64(seed), count, _p(out))
+    return out
+
+
+def test_field_2d(n, seed):
+    c, v = np.zeros(n * 2), np.zeros(n)
+    lib().or_test_field_2d(n, C.c_uint64(seed), _p(c), _p(v))
+    return c.reshape(n, 2), v
+
+
+def test_field_3d(n, seed):
+    c, v = np.zeros(n * 3), np.zeros(n)
+    lib().or_test_field_3d(n, C.c_uint64(seed), _p(c), _p(v))
+    return c.reshape(n, 3), v

@@ -1,0 +1,422 @@
+"""Pins the FP64 CPU oracle to the reference's own known answers.
+
+Each test restates a test of geostat-rs (file:line given) against the oracle:
+gstat golden values where the reference has them, otherwise the reference's
+exactness / brute-force / closed-form identities.  These run on the CPU.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import pyoracle as O
+from geostat_rs.model import Anisotropy, Structure, VariogramModel
+
+
+def sph_model():
+    # kriging.rs:852-854 `model()`
+    return VariogramModel(0.05, [Structure("spherical", 0.95, 2.0)])
+
+
+def sample_data():
+    # kriging.rs:844-850 `sample_data()`
+    c = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0], [0.4, 0.6]])
+    v = np.array([1.0, 2.0, 1.5, 2.5, 1.7])
+    return c, v
+
+
+# ---------------------------------------------------------------- model.rs --
+def test_rotation_3d_matches_gstat_setrot():
+    # variogram/model.rs:906-952: gstat variogramLine with anis=c(30,20,40,.5,.3)
+    m = VariogramModel(0.0, [Structure.with_rotation("spherical", 1.0, 100.0, 30.0, 20.0, 40.0,
+                                                     0.5, 0.3)])
+    cases = [
+        ([1.0, 0.0, 0.0], 0.605458280770632),
+        ([0.0, 1.0, 0.0], 0.577390658041395),
+        ([0.0, 0.0, 1.0], 0.732990706603906),
+        ([0.577350269190, 0.577350269190, 0.577350269190], 0.432164835884142),
+        ([0.666666666667, -0.666666666667, 0.333333333333], 0.810043758779196),
+        ([-0.534522483825, 0.267261241912, 0.801783725737], 0.575462768274161),
+    ]
+    for d, expected in cases:
+        got = O.gamma_dh(m, [d[0] * 20.0, d[1] * 20.0, d[2] * 20.0])
+        assert abs(got - expected) < 1e-9, (d, got, expected)
+
+
+def test_gamma_boundary_and_closed_forms():
+    # model.rs gamma_boundary_behavior + the closed forms of ModelKind::g
+    m = VariogramModel(0.1, [Structure("spherical", 0.9, 100.0)])
+    assert O.gamma_dh(m, [0.0, 0.0]) == 0.0
+    assert O.gamma_dh(m, [1e-9, 0.0]) >= 0.1
+    assert O.gamma_dh(m, [100.0, 0.0]) == pytest.approx(1.0, abs=1e-15)
+    assert O.gamma_dh(m, [250.0, 0.0]) == pytest.approx(1.0, abs=1e-15)
+    for kind, fn in [
+        ("exponential", lambda d: 1 - math.exp(-d)),
+        ("gaussian", lambda d: 1 - math.exp(-d * d)),
+        ("matern15", lambda d: 1 - (1 + math.sqrt(3) * d) * math.exp(-math.sqrt(3) * d)),
+        ("matern25", lambda d: 1 - (1 + math.sqrt(5) * d + 5 * d * d / 3) * math.exp(-math.sqrt(5) * d)),
+    ]:
+        mm = VariogramModel(0.0, [Structure(kind, 1.0, 10.0)])
+        for h in (0.5, 3.0, 10.0, 40.0):
+            assert O.gamma_dh(mm, [h, 0.0]) == pytest.approx(fn(h / 10.0), rel=1e-14, abs=1e-15)
+
+
+def test_azimuth_mirror_symmetry_2d():
+    # model.rs:870-903: azimuth 90 with ratio 0.5 equals the rotated frame
+    m = VariogramModel(0.0, [Structure.with_anisotropy("spherical", 1.0, 100.0, 90.0, 0.5)])
+    # along azimuth 90 (x axis) the range is 100; along y it is 50
+    assert O.gamma_dh(m, [100.0, 0.0]) == pytest.approx(1.0, abs=1e-12)
+    assert O.gamma_dh(m, [0.0, 50.0]) == pytest.approx(1.0, abs=1e-12)
+    assert O.gamma_dh(m, [0.0, 25.0]) == pytest.approx(O.gamma_dh(m, [50.0, 0.0]), abs=1e-12)
+
+
+# --------------------------------------------------------------- linalg.rs --
+def test_lu_known_system_and_singular():
+    # linalg.rs:225-245
+    a = np.array([[2.0, 1.0, -1.0], [-3.0, -1.0, 2.0], [-2.0, 1.0, 2.0]])
+    x = O.lu_solve(a, [8.0, -11.0, -3.0])
+    assert np.max(np.abs(x - [2.0, 3.0, -1.0])) < 1e-12
+    with pytest.raises(O.OracleError) as e:
+        O.lu_solve([[1.0, 2.0], [2.0, 4.0]], [1.0, 2.0])
+    assert e.value.code == O.SINGULAR_SYSTEM
+
+
+def test_cholesky_matches_lu_and_rejects_non_pd():
+    # linalg.rs:248-268
+    a = np.array([4.0, 1.0, 0.5, 1.0, 3.0, 0.2, 0.5, 0.2, 2.0]).reshape(3, 3)
+    b = [1.0, 2.0, 3.0]
+    assert np.max(np.abs(O.cholesky_solve(a, b) - O.lu_solve(a, b))) < 1e-12
+    with pytest.raises(O.OracleError):
+        O.cholesky_solve([[1.0, 2.0], [2.0, 4.0]], [1.0, 2.0])
+
+
+def test_indefinite_kriging_like_system():
+    # linalg.rs:270-283
+    a = np.array([[1.0, 0.3, 1.0], [0.3, 1.0, 1.0], [1.0, 1.0, 0.0]])
+    b = np.array([0.7, 0.5, 1.0])
+    x = O.lu_solve(a, b)
+    assert np.max(np.abs(a @ x - b)) < 1e-12
+    assert abs(x[0] + x[1] - 1.0) < 1e-12
+
+
+# --------------------------------------------------------------- search.rs --
+def _random_points(n, seed):
+    u = O.rng_uniform(seed, 2 * n)
+    return (u * 100.0).reshape(n, 2)
+
+
+def test_kdtree_matches_brute_force():
+    # search.rs:364-377
+    pts = _random_points(500, 5)
+    u = O.rng_uniform(6, 400)
+    for t in range(200):
+        target = [u[2 * t] * 120.0 - 10.0, u[2 * t + 1] * 120.0 - 10.0]
+        for k, r in [(1, None), (8, None), (16, 15.0), (1000, 5.0)]:
+            assert O.kdtree_knn(pts, target, k, r) == O.knn_brute(pts, target, k, r)
+
+
+def test_bucket_grid_matches_brute_force_incrementally():
+    # search.rs:379-396
+    pts = _random_points(400, 9)
+    u = O.rng_uniform(10, 400)
+    after = [i for i in range(400) if i % 37 == 0]
+    targets = np.array([[u[2 * q] * 100.0, u[2 * q + 1] * 100.0] for q in range(len(after))])
+    for k, r in [(4, None), (16, 20.0)]:
+        res, _ = O.bucketgrid_queries(pts, [0, 0], [100, 100], 400, after, targets, k, r)
+        for q, i in enumerate(after):
+            assert res[q] == O.knn_brute(pts[:i + 1], targets[q], k, r)
+
+
+def test_bucket_grid_degenerate_axes():
+    # search.rs:410-445
+    pts = np.array([[i * 10.0, 5.0] for i in range(50)])
+    res, dims = O.bucketgrid_queries(pts, [0, 5], [500, 5], 50, [49], [[123.0, 5.0]], 5)
+    assert dims == [50, 1]
+    assert res[0] == O.knn_brute(pts, [123.0, 5.0], 5)
+    _, dims3 = O.bucketgrid_queries(np.zeros((1, 3)), [0, 0, 5], [500, 500, 5], 100, [], [], 1)
+    assert dims3[2] == 1 and dims3[0] * dims3[1] * dims3[2] <= 400
+    _, dims1 = O.bucketgrid_queries(np.zeros((1, 2)), [3, 3], [3, 3], 10, [], [], 1)
+    assert dims1 == [1, 1]
+
+
+def test_empty_and_single_point_search():
+    # search.rs:398-407
+    assert O.kdtree_knn(np.array([[1.0, 1.0]]), [0.0, 0.0], 5) == [0]
+    assert O.kdtree_knn(np.array([[1.0, 1.0]]), [0.0, 0.0], 5, 0.5) == []
+
+
+# ----------------------------------------------------------------- data.rs --
+def test_duplicate_pair_detection():
+    # data.rs:201-213
+    assert O.duplicate_pair(np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]])) is None
+    assert O.duplicate_pair(np.array([[0, 0], [1, 2], [1, 2], [3, 3]], float)) == (1, 2)
+    assert O.duplicate_pair(np.array([[0.0, 1.0], [-0.0, 1.0]])) == (0, 1)
+
+
+def test_grid_centers_order():
+    # grid.rs:99-109
+    c = O.grid_centers([0, 0], [4, 2], [4, 2])
+    assert c.shape == (8, 2)
+    assert c[0].tolist() == [0.5, 0.5] and c[1].tolist() == [1.5, 0.5]
+    assert c[4].tolist() == [0.5, 1.5] and c[7].tolist() == [3.5, 1.5]
+
+
+# ------------------------------------------------------------------ rng.rs --
+def _py_xoshiro(seed, count):
+    M = (1 << 64) - 1
+
+    def sm(st):
+        st = (st + 0x9E3779B97F4A7C15) & M
+        z = st
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        return st, z ^ (z >> 31)
+
+    st, s = seed, []
+    for _ in range(4):
+        st, v = sm(st)
+        s.append(v)
+    rotl = lambda x, k: ((x << k) | (x >> (64 - k))) & M
+    out = []
+    for _ in range(count):
+        out.append((rotl((s[0] + s[3]) & M, 23) + s[0]) & M)
+        t = (s[1] << 17) & M
+        s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3]; s[2] ^= t
+        s[3] = rotl(s[3], 45)
+    return out
+
+
+def test_rng_stream_matches_published_algorithm():
+    # rng.rs:7-48; splitmix64(0) first output is the published 0xE220A8397B1DCDAF
+    assert _py_xoshiro(0, 1)  # exercise
+    st = 0
+    st = (st + 0x9E3779B97F4A7C15) & ((1 << 64) - 1)
+    assert O.rng_u64(42, 100).tolist() == _py_xoshiro(42, 100)
+    assert O.rng_u64(0, 5).tolist() == _py_xoshiro(0, 5)
+    u = O.rng_uniform(1, 10000)
+    assert (u >= 0).all() and (u < 1).all()
+    z = O.rng_normal(7, 100000)
+    assert abs(z.mean()) < 0.02 and abs(z.var() - 1) < 0.05
+
+
+# -------------------------------------------------------------- kriging.rs --
+def test_ordinary_kriging_exact_at_data():
+    # kriging.rs:1205-1220
+    c, v = sample_data()
+    r = O.krige(c, v, sph_model(), c)
+    assert np.max(np.abs(r["value"] - v)) < 1e-8
+    assert np.max(r["variance"]) < 1e-8
+
+
+def test_power_model_matches_gstat_ordinary_kriging():
+    # kriging.rs:1222-1268 (gstat krige with vgm(2.0,"Pow",1.2))
+    c = np.array([[0, 0], [10, 0], [0, 10], [10, 10], [5, 5]], float)
+    v = np.array([1.0, 2.0, 1.5, 2.5, 1.8])
+    m = VariogramModel(0.0, [Structure("power", 2.0, 1.0, param=1.2)])
+    r = O.krige(c, v, m, np.array([[3.0, 4.0], [7.0, 8.0], [5.0, 5.0]]))
+    assert abs(r["value"][0] - 1.5252052569) < 1e-6
+    assert abs(r["variance"][0] - 6.4437897810) < 1e-5
+    assert abs(r["value"][1] - 2.1366210000) < 1e-6
+    assert abs(r["variance"][1] - 7.7780140000) < 1e-5
+    assert abs(r["value"][2] - 1.8) < 1e-6 and r["variance"][2] < 1e-6
+
+
+def test_far_field_simple_and_ordinary():
+    # kriging.rs:1360-1383
+    c, v = sample_data()
+    m = sph_model()
+    ok = O.krige(c, v, m, np.array([[1e6, 1e6]]))
+    assert ok["variance"][0] >= 0.99 * m.total_sill() and np.isfinite(ok["value"][0])
+    sk = O.krige(c, v, m, np.array([[1e6, 1e6]]), method="simple", mean=1.74)
+    assert abs(sk["value"][0] - 1.74) < 1e-9
+    assert abs(sk["variance"][0] - m.total_sill()) < 1e-9
+    assert np.isnan(sk["lagrange"][0]) and np.isfinite(ok["lagrange"][0])
+
+
+def test_universal_kriging_reproduces_exact_drift():
+    # kriging.rs:1385-1413
+    c = np.array([[i, j] for i in range(4) for j in range(4)], float)
+    v = 2.0 + 3.0 * c[:, 0] - c[:, 1]
+    t = np.array([[1.5, 1.5], [5.0, 2.0]])
+    r = O.krige(c, v, sph_model(), t, method="universal", degree=1)
+    assert np.max(np.abs(r["value"] - (2 + 3 * t[:, 0] - t[:, 1]))) < 1e-7
+
+
+def test_external_drift_reproduces_linear_relation():
+    # kriging.rs:1415-1445
+    xs = [(i * 10.0, j * 10.0) for i in range(5) for j in range(5)]
+    c = np.array(xs)
+    d = np.sin(c[:, 0] * 0.13 + c[:, 1] * 0.07)
+    v = 2.0 + 3.0 * d
+    t = np.array([[12.0, 33.0], [45.0, 5.0]])
+    td = np.array([[0.4], [-0.7]])
+    r = O.krige(c, v, sph_model(), t, method="external_drift", drift=d.reshape(-1, 1),
+                target_drift=td)
+    assert np.max(np.abs(r["value"] - (2 + 3 * td[:, 0]))) < 1e-7
+
+
+def test_octant_search_balances_clustered_neighbors():
+    # kriging.rs:960-1011
+    c = np.array([[1.0, 0.1], [1.1, -0.1], [1.2, 0.2], [1.3, -0.2], [1.4, 0.05],
+                  [-2.0, 0.5], [-2.0, -0.5], [0.5, -2.0], [0.5, 2.0]])
+    v = np.array([10.0] * 5 + [0.0] * 4)
+    t = np.array([[0.0, 0.0]])
+    near = O.krige(c, v, sph_model(), t, max_neighbors=4)["value"][0]
+    octn = O.krige(c, v, sph_model(), t, max_neighbors=4, max_per_octant=1)["value"][0]
+    assert near > 9.0 and octn < near - 2.0
+
+
+def test_min_neighbors_and_invalid_configs():
+    # kriging.rs:913-958
+    c, v = sample_data()
+    r = O.krige(c, v, sph_model(), np.array([[0.5, 0.5], [1.5, 1.5]]), radius=0.75,
+                min_neighbors=3)
+    assert r["status"][0] == 0 and r["status"][1] == O.NO_NEIGHBORS
+    assert np.isnan(r["value"][1])
+    with pytest.raises(O.OracleError):
+        O.krige(c, v, sph_model(), c, min_neighbors=0)
+    with pytest.raises(O.OracleError):
+        O.krige(c, v, sph_model(), c, max_neighbors=2, min_neighbors=3)
+
+
+def test_duplicate_points_rejected_up_front():
+    # kriging.rs:1191-1203
+    c = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 0.0], [0.0, 1.0]])
+    with pytest.raises(O.OracleError) as e:
+        O.krige(c, np.array([1.0, 2.0, 2.1, 1.5]), sph_model(), c)
+    assert e.value.code == O.DUPLICATE_POINTS and "1 and 2" in str(e.value)
+
+
+def test_kdtree_neighborhood_matches_global_at_full_k():
+    # kriging.rs:1570-1592
+    c, v = sample_data()
+    t = np.array([[0.3, 0.3], [0.9, 0.1], [2.0, 2.0]])
+    g = O.krige(c, v, sph_model(), t)
+    loc = O.krige(c, v, sph_model(), t, max_neighbors=len(c))
+    assert np.max(np.abs(g["value"] - loc["value"])) < 1e-12
+    assert np.max(np.abs(g["variance"] - loc["variance"])) < 1e-12
+
+
+def test_measurement_error_smooths():
+    # kriging.rs:856-911
+    c, v = sample_data()
+    ex = O.krige(c, v, sph_model(), c)
+    nz = O.krige(c, v, sph_model(), c, measurement_error=np.full(5, 0.5))
+    assert np.max(np.abs(ex["value"] - v)) < 1e-8
+    assert np.min(np.abs(nz["value"] - v)) > 1e-3 and np.min(nz["variance"]) > 1e-3
+    z = O.krige(c, v, sph_model(), np.array([[0.3, 0.7]]), measurement_error=np.zeros(5))
+    e2 = O.krige(c, v, sph_model(), np.array([[0.3, 0.7]]))
+    assert abs(z["value"][0] - e2["value"][0]) < 1e-14
+
+
+def test_anisotropic_search_prefers_major_axis():
+    # kriging.rs:1013-1066 (shape of the test: the ellipse admits the far
+    # major-axis point over a nearer minor-axis one)
+    c = np.array([[3.0, 0.0], [0.0, 2.0], [10.0, 10.0], [-10.0, 10.0]])
+    v = np.array([5.0, -5.0, 0.0, 0.0])
+    t = np.array([[0.0, 0.0]])
+    eu = O.krige(c, v, sph_model(), t, max_neighbors=1, kcap=1)
+    an = O.krige(c, v, sph_model(), t, max_neighbors=1, kcap=1,
+                 anisotropic_search=Anisotropy(90.0, 0.25))
+    assert eu["neighbors"][0, 0] == 1 and an["neighbors"][0, 0] == 0
+
+
+def test_kriging_3d_exact_and_far_field():
+    # tests/three_d.rs:48-76
+    c, v = O.test_field_3d(150, 5)
+    m = VariogramModel(0.01, [Structure("spherical", 1.0, 40.0)])
+    idx = list(range(0, 150, 30))
+    r = O.krige(c, v, m, c[idx])
+    assert np.max(np.abs(r["value"] - v[idx])) < 1e-7 and np.max(r["variance"]) < 1e-7
+    far = O.krige(c, v, m, np.array([[1e5, 1e5, 1e5]]))
+    assert far["variance"][0] >= 0.99 * m.total_sill()
+
+
+# -------------------------------------------------------------- vecchia.rs --
+def exp_model(nug, sill, rng_):
+    return VariogramModel(nug, [Structure("exponential", sill, rng_)])
+
+
+def test_vecchia_full_conditioning_equals_exact():
+    # vecchia.rs:1998-2010
+    c, v = O.test_field_2d(14, 3)
+    m = exp_model(0.05, 1.0, 40.0)
+    assert abs(O.vecchia_loglik(c, v, m, 13) - O.exact_loglik(c, v, m)) < 1e-9
+
+
+def test_vecchia_approximation_is_close_with_maxmin():
+    # vecchia.rs:2012-2026
+    c, v = O.test_field_2d(90, 11)
+    m = exp_model(0.05, 1.0, 30.0)
+    ex = O.exact_loglik(c, v, m)
+    assert abs(O.vecchia_loglik(c, v, m, 12) - ex) / abs(ex) < 0.02
+
+
+def test_vecchia_predict_full_conditioning_equals_simple_kriging():
+    # vecchia.rs:2131-2167
+    c, v = O.test_field_2d(60, 5)
+    m = exp_model(0.1, 0.9, 30.0)
+    t = np.array([[12.0, 33.0], [55.0, 71.0], [80.0, 20.0], [40.0, 40.0]])
+    pv, pvar = O.vecchia_predict(c, v, m, t, 1000)
+    sk = O.krige(c, v, m, t, method="simple", mean=float(np.sum(v) / len(v)))
+    assert np.max(np.abs(pv - sk["value"])) < 1e-8
+    assert np.max(np.abs(pvar - sk["variance"])) < 1e-8
+
+
+def test_vecchia_predict_small_m_tracks_and_is_deterministic():
+    # vecchia.rs:2169-2240
+    c, v = O.test_field_2d(150, 9)
+    m = exp_model(0.05, 0.95, 25.0)
+    t = np.array([[2.5 * i + 1.0, 97.0 - 2.3 * i] for i in range(40)])
+    pv, pvar = O.vecchia_predict(c, v, m, t, 25)
+    sk = O.krige(c, v, m, t, method="simple", mean=float(np.mean(v)))
+    assert np.max(np.abs(pv - sk["value"])) < 0.02
+    assert np.max(np.abs(pvar - sk["variance"])) < 0.02
+    c2, v2 = O.test_field_2d(150, 11)
+    t2 = np.array([[1.7 * i + 3.0, 96.0 - 1.6 * i] for i in range(60)])
+    a = O.vecchia_predict(c2, v2, m, t2, 8)
+    b = O.vecchia_predict(c2, v2, m, t2, 8)
+    assert a[0].tobytes() == b[0].tobytes() and a[1].tobytes() == b[1].tobytes()
+
+
+def test_lazy_maxmin_matches_exact_traversal():
+    # vecchia.rs:2276-2289
+    for seed in (3, 11, 29):
+        c, _ = O.test_field_2d(400, seed)
+        assert O.maxmin_order(c).tolist() == O.maxmin_order_brute(c).tolist()
+    c, _ = O.test_field_2d(50, 7)
+    assert sorted(O.maxmin_order(c).tolist()) == list(range(50))
+
+
+def test_incremental_predecessors_match_brute_force():
+    # vecchia.rs:2290-2310
+    c, _ = O.test_field_2d(300, 13)
+    m = 8
+    order, nb, cnt = O.vecchia_plan(c, m)
+    for k in range(len(c)):
+        t = order[k]
+        prev = sorted(((float(np.sum((c[t] - c[j]) ** 2)), j) for j in order[:k]))[:m]
+        assert sorted(j for _, j in prev) == sorted(nb[k, :cnt[k]].tolist())
+
+
+def test_vecchia_rejects_bad_args():
+    # vecchia.rs:2312-2319
+    c, v = O.test_field_2d(10, 1)
+    m = VariogramModel(0.1, [Structure("spherical", 1.0, 20.0)])
+    with pytest.raises(O.OracleError):
+        O.vecchia_loglik(c, v, m, 0)
+    with pytest.raises(O.OracleError):
+        O.vecchia_loglik(c, v, VariogramModel(0.0, [Structure("power", 1.0, 1.0, param=1.0)]), 5)
+
+
+# ---------------------------------------------------------------- optim.rs --
+def test_nelder_mead_rosenbrock_and_multistart():
+    # optim.rs:294-324
+    rosen = lambda x: (1 - x[0]) ** 2 + 100 * (x[1] - x[0] ** 2) ** 2
+    x, fx = O.nelder_mead_multistart(rosen, [[-1.2, 1.0]], 0.1, 5000)
+    assert abs(x[0] - 1) < 1e-3 and abs(x[1] - 1) < 1e-3 and fx < 1e-6
+    wells = lambda x: -2 * math.exp(-0.5 * (x[0] + 3) ** 2) - 3 * math.exp(-0.5 * (x[0] - 3) ** 2)
+    _, single = O.nelder_mead_multistart(wells, [[-3.0]], 0.1, 500)
+    assert single > -2.5
+    x, fx = O.nelder_mead_multistart(wells, [[-3.0], [3.0], [0.0]], 0.1, 500)
+    assert abs(x[0] - 3.0) < 1e-2 and fx < -2.9
