@@ -1,0 +1,719 @@
+// gs_api.cu -- the C ABI (include/geostat_gb300.h): handles, validation in
+// the reference's order, and the host orchestration of the device kernels.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "gs_common.cuh"
+#include "gs_host.h"
+#include "gs_internal.h"
+#include "gs_krige.cuh"
+#include "gs_search.cuh"
+
+namespace gs {
+
+// ------------------------------------------------------------ utilities --
+static std::once_flag g_pool_once;
+
+int ensure_device() {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0)
+    return fail(GS_ERR_CUDA, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+  std::call_once(g_pool_once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  });
+  return GS_OK;
+}
+
+int DevBuf::alloc(size_t b, cudaStream_t s) {
+  release();
+  stream = s;
+  bytes = b;
+  GS_CUDA(cudaMallocAsync(&ptr, std::max<size_t>(b, 16), s));
+  return GS_OK;
+}
+void DevBuf::release() {
+  if (ptr) cudaFreeAsync(ptr, stream);
+  ptr = nullptr;
+  bytes = 0;
+}
+DevBuf::~DevBuf() { release(); }
+
+static thread_local double g_timings[4] = {0, 0, 0, 0};
+
+}  // namespace gs
+
+using namespace gs;
+
+// ============================================================== C ABI ====
+gs_pointset::~gs_pointset() {
+  cudaFree(d_x);
+  cudaFree(d_y);
+  cudaFree(d_z);
+  cudaFree(d_v);
+}
+
+struct gs_kriging {
+  const gs_pointset* ps = nullptr;
+  gs_kcfg cfg{};
+  gs_model model{};
+  DevModel dm{};
+  int p = 0;
+  int nv = 0;
+  double center[3] = {0, 0, 0};
+  double scale = 1.0;
+  double dmean[GS_MAX_KED_VARS] = {0};
+  double dscale[GS_MAX_KED_VARS] = {0};
+  double* d_drift = nullptr;
+  double* d_err = nullptr;
+  bool use_tree = false;
+  SearchFrame frame{};
+  Grid grid;
+  cudaStream_t stream = nullptr;
+  ~gs_kriging() {
+    cudaFree(d_drift);
+    cudaFree(d_err);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+extern "C" {
+
+const char* gs_last_error(void) { return gs::last_error(); }
+int gs_abi_version(void) { return GS_ABI_VERSION; }
+
+int gs_last_timings(double* ms4) {
+  for (int i = 0; i < 4; ++i) ms4[i] = g_timings[i];
+  return GS_OK;
+}
+
+// data.rs:15-83 (+ duplicate_coord_pair, data.rs:384-397).
+int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, const double* z,
+                       const double* values, gs_pointset** out) {
+  *out = nullptr;
+  if (dim != 2 && dim != 3) return fail(GS_ERR_DIMENSION_MISMATCH, "dim must be 2 or 3");
+  if (n <= 0) return fail(GS_ERR_INSUFFICIENT_DATA, "no points provided");
+  if (n > 0x7fffffffll) return fail(GS_ERR_INVALID_PARAMETER, "at most 2^31-1 points");
+  for (int64_t i = 0; i < n; ++i) {
+    if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || (dim == 3 && !std::isfinite(z[i])))
+      return fail(GS_ERR_INVALID_PARAMETER, "non-finite coordinate");
+  }
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(values[i])) return fail(GS_ERR_INVALID_PARAMETER, "non-finite value");
+  GS_TRY(ensure_device());
+  auto* ps = new gs_pointset();
+  ps->dim = dim;
+  ps->n = n;
+  ps->host.resize(n * dim);
+  for (int64_t i = 0; i < n; ++i) {
+    ps->host[i * dim] = x[i];
+    ps->host[i * dim + 1] = y[i];
+    if (dim == 3) ps->host[i * dim + 2] = z[i];
+  }
+  ps->values.assign(values, values + n);
+  // first pair with bitwise-identical coordinates, -0.0 normalised
+  {
+    struct H {
+      size_t operator()(const std::array<uint64_t, 3>& k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (uint64_t v : k) h = (h ^ v) * 1099511628211ull;
+        return (size_t)h;
+      }
+    };
+    std::unordered_map<std::array<uint64_t, 3>, int64_t, H> seen;
+    seen.reserve(n);
+    for (int64_t i = 0; i < n; ++i) {
+      std::array<uint64_t, 3> key = {0, 0, 0};
+      for (int d = 0; d < dim; ++d) {
+        double v = ps->host[i * dim + d] + 0.0;
+        std::memcpy(&key[d], &v, 8);
+      }
+      auto it = seen.find(key);
+      if (it != seen.end()) {
+        ps->has_dup = true;
+        ps->dup_i = it->second;
+        ps->dup_j = i;
+        break;
+      }
+      seen.emplace(key, i);
+    }
+  }
+  auto up = [&](double** d, const double* h) -> int {
+    GS_CUDA(cudaMalloc(d, n * sizeof(double)));
+    GS_CUDA(cudaMemcpy(*d, h, n * sizeof(double), cudaMemcpyHostToDevice));
+    return GS_OK;
+  };
+  int rc = up(&ps->d_x, x);
+  if (!rc) rc = up(&ps->d_y, y);
+  if (!rc && dim == 3) rc = up(&ps->d_z, z);
+  if (!rc) rc = up(&ps->d_v, values);
+  if (rc) {
+    delete ps;
+    return rc;
+  }
+  *out = ps;
+  return GS_OK;
+}
+
+void gs_pointset_destroy(gs_pointset* ps) { delete ps; }
+
+int gs_pointset_duplicate_pair(const gs_pointset* ps, int64_t* i, int64_t* j) {
+  if (!ps->has_dup) return 0;
+  *i = ps->dup_i;
+  *j = ps->dup_j;
+  return 1;
+}
+
+}  // extern "C"
+
+namespace {
+
+// KrigingMethod::n_drift (kriging.rs:46-60).
+int n_drift(const gs_kcfg& c, int dim) {
+  switch (c.method) {
+    case GS_SIMPLE:
+      return 0;
+    case GS_ORDINARY:
+      return 1;
+    case GS_UNIVERSAL:
+      if (c.uk_degree == 1) return 1 + dim;
+      if (c.uk_degree == 2) return 1 + dim + dim * (dim + 1) / 2;
+      return 0;
+    case GS_EXTERNAL_DRIFT:
+      return 1 + (int)c.ked_nvars;
+  }
+  return 0;
+}
+
+bool valid_in_dim(const gs_model& m, int dim) {
+  for (int k = 0; k < m.n_structures; ++k)
+    if (m.s[k].kind == GS_KIND_CIRCULAR && dim > 2) return false;
+  return true;
+}
+
+// Kriging::build and the three constructors (kriging.rs:166-408).
+int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* cfg, int ctor,
+                   const double* drift, const double* errors, gs_kriging** out) {
+  *out = nullptr;
+  if (!ps || !model || !cfg) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
+  GS_TRY(validate_model(*model));
+  const int dim = ps->dim;
+  const int64_t n = ps->n;
+  if (ctor == 0) {
+    if (cfg->method == GS_EXTERNAL_DRIFT)
+      return fail(GS_ERR_INVALID_PARAMETER,
+                  "external drift kriging requires Kriging::with_external_drift");
+  } else if (ctor == 2) {
+    if (cfg->method == GS_EXTERNAL_DRIFT)
+      return fail(GS_ERR_INVALID_PARAMETER, "measurement error with external drift is not supported yet");
+    if (has_power(*model))
+      return fail(GS_ERR_INVALID_PARAMETER,
+                  "measurement error with Power (IRF-0) models is not supported yet");
+    for (int64_t i = 0; i < n; ++i)
+      if (!(std::isfinite(errors[i]) && errors[i] >= 0.0))
+        return fail(GS_ERR_INVALID_PARAMETER,
+                    "measurement-error variances must be finite and non-negative");
+  } else {
+    if (cfg->method != GS_EXTERNAL_DRIFT)
+      return fail(GS_ERR_INVALID_PARAMETER, "with_external_drift requires KrigingMethod::ExternalDrift");
+    if (cfg->ked_nvars <= 0)
+      return fail(GS_ERR_INVALID_PARAMETER, "external drift requires at least one covariate");
+    for (int64_t i = 0; i < n * cfg->ked_nvars; ++i)
+      if (!std::isfinite(drift[i]))
+        return fail(GS_ERR_INVALID_PARAMETER,
+                    "non-finite drift value at data point " + std::to_string(i / cfg->ked_nvars));
+  }
+  if (cfg->method < GS_SIMPLE || cfg->method > GS_EXTERNAL_DRIFT)
+    return fail(GS_ERR_INVALID_PARAMETER, "unknown kriging method");
+  if (cfg->method == GS_UNIVERSAL && !(cfg->uk_degree >= 1 && cfg->uk_degree <= 2))
+    return fail(GS_ERR_INVALID_PARAMETER, "universal kriging drift degree must be 1 or 2, got " +
+                                              std::to_string(cfg->uk_degree));
+  if (has_power(*model) && cfg->method == GS_SIMPLE)
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "Power (unbounded) models have no covariance function, so simple kriging cannot "
+                "use them");
+  if (!valid_in_dim(*model, dim))
+    return fail(GS_ERR_INVALID_PARAMETER, "this model is not a valid covariance in 3 dimensions");
+  if (cfg->has_search_radius && !(cfg->search_radius > 0.0))
+    return fail(GS_ERR_INVALID_PARAMETER, "search radius must be positive");
+  if (cfg->has_anisotropic_search)
+    GS_TRY(validate_anisotropy(cfg->search_azimuth_deg, cfg->search_ratio, cfg->search_ratio_z,
+                               cfg->search_dip_deg, cfg->search_rake_deg));
+  if (cfg->max_neighbors == 0) return fail(GS_ERR_INVALID_PARAMETER, "max_neighbors must be at least 1");
+  if (ps->has_dup)
+    return fail(GS_ERR_DUPLICATE_POINTS, "duplicate data points: indices " +
+                                             std::to_string(ps->dup_i) + " and " +
+                                             std::to_string(ps->dup_j) +
+                                             " share the same coordinates");
+  if (cfg->max_per_octant == 0) return fail(GS_ERR_INVALID_PARAMETER, "max_per_octant must be at least 1");
+  if (cfg->min_neighbors >= 0) {
+    if (cfg->min_neighbors == 0) return fail(GS_ERR_INVALID_PARAMETER, "min_neighbors must be at least 1");
+    if (cfg->min_neighbors > n)
+      return fail(GS_ERR_INSUFFICIENT_DATA, "min_neighbors (" + std::to_string(cfg->min_neighbors) +
+                                                ") exceeds the number of data points (" +
+                                                std::to_string(n) + ")");
+    if (cfg->max_neighbors >= 0 && cfg->min_neighbors > cfg->max_neighbors)
+      return fail(GS_ERR_INVALID_PARAMETER, "min_neighbors exceeds max_neighbors");
+  }
+  // GPU-path limits (kinds, drift terms)
+  auto* k = new gs_kriging();
+  int rc = make_dev_model(*model, dim, &k->dm, true);
+  if (rc) {
+    delete k;
+    return rc;
+  }
+  k->ps = ps;
+  k->cfg = *cfg;
+  k->model = *model;
+  k->p = n_drift(*cfg, dim);
+  if (k->p > GS_MIXED_MAX_DRIFT || (cfg->method == GS_EXTERNAL_DRIFT && cfg->ked_nvars > GS_MAX_KED_VARS)) {
+    delete k;
+    return fail(GS_ERR_INVALID_PARAMETER, "at most 8 external-drift covariates on the CUDA path");
+  }
+  k->nv = cfg->method == GS_EXTERNAL_DRIFT ? (int)cfg->ked_nvars : 0;
+  // bbox centre / scale (kriging.rs:340-347)
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < dim; ++d) {
+      mn[d] = std::fmin(mn[d], ps->host[i * dim + d]);
+      mx[d] = std::fmax(mx[d], ps->host[i * dim + d]);
+    }
+  double spread = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    k->center[d] = 0.5 * (mn[d] + mx[d]);
+    spread = std::fmax(spread, mx[d] - mn[d]);
+  }
+  k->scale = std::fmax(0.5 * spread, 2.2250738585072014e-308);
+  if (ctor == 1) {
+    const int nv = k->nv;
+    for (int c = 0; c < nv; ++c) {
+      double s = 0.0;
+      for (int64_t i = 0; i < n; ++i) s += drift[i * nv + c];
+      double mean = s / (double)n;
+      double v = 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        double t = drift[i * nv + c] - mean;
+        v += t * t;
+      }
+      v = v / (double)n;
+      k->dmean[c] = mean;
+      k->dscale[c] = std::fmax(std::sqrt(v), 2.2250738585072014e-308);
+    }
+  }
+  rc = cudaStreamCreateWithFlags(&k->stream, cudaStreamNonBlocking) == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "stream creation failed");
+  if (!rc && ctor == 1) {
+    if (cudaMalloc(&k->d_drift, n * k->nv * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(k->d_drift, drift, n * k->nv * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(GS_ERR_CUDA, "drift upload failed");
+  }
+  if (!rc && ctor == 2) {
+    if (cudaMalloc(&k->d_err, n * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(k->d_err, errors, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(GS_ERR_CUDA, "measurement-error upload failed");
+  }
+  k->use_tree = cfg->max_neighbors >= 0 || cfg->has_search_radius || cfg->max_per_octant >= 0;
+  if (!rc && k->use_tree) {
+    SearchFrame& f = k->frame;
+    std::memset(&f, 0, sizeof(f));
+    if (cfg->has_anisotropic_search) {
+      f.aniso = 1;
+      f.ratio = cfg->search_ratio;
+      if (dim == 2) {
+        double a = cfg->search_azimuth_deg * (3.14159265358979323846 / 180.0);
+        f.s = std::sin(a);
+        f.c = std::cos(a);
+      } else {
+        rotation_3d(cfg->search_azimuth_deg, cfg->search_ratio, cfg->search_ratio_z,
+                    cfg->search_dip_deg, cfg->search_rake_deg, f.rot);
+      }
+    }
+    double ppc = dim == 2 ? 3.0 : 4.0;
+    rc = grid_build(&k->grid, dim, n, ps->d_x, ps->d_y, ps->d_z, f, ppc, k->stream);
+  }
+  if (rc) {
+    delete k;
+    return rc;
+  }
+  *out = k;
+  return GS_OK;
+}
+
+__global__ void iota_rows_kernel(int64_t nt, int n, int32_t* nb, int32_t* nbc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nt * n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    nb[i] = (int32_t)(i % n);
+    if (i % n == 0) nbc[i / n] = n;
+  }
+}
+
+struct PhaseTimer {
+  cudaEvent_t ev[4];
+  bool ok = false;
+  explicit PhaseTimer(cudaStream_t s) {
+    ok = true;
+    for (int i = 0; i < 4; ++i) ok = ok && cudaEventCreate(&ev[i]) == cudaSuccess;
+    (void)s;
+  }
+  ~PhaseTimer() {
+    for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  }
+};
+
+// Search + solves for targets already on the device.
+int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                   const double* tz, const double* tdrift, double* value, double* variance,
+                   double* lagrange, uint8_t* status, int precision, cudaStream_t stream) {
+  if (nt == 0) return GS_OK;
+  const gs_pointset* ps = k->ps;
+  const gs_kcfg& c = k->cfg;
+  const int dim = ps->dim;
+  const int64_t n = ps->n;
+  const int p = k->p;
+  // neighbourhood geometry
+  SearchParams sp{};
+  int kout;
+  if (!k->use_tree) {
+    if (n + p > GS_MAX_SYSTEM)
+      return fail(GS_ERR_INVALID_PARAMETER,
+                  "global neighbourhood of " + std::to_string(n) +
+                      " points exceeds the CUDA path's system limit; set max_neighbors");
+    kout = (int)n;
+  } else if (c.max_per_octant >= 0) {
+    const int NB = 1 << dim;
+    int per = (int)std::min<int64_t>(c.max_per_octant, n);
+    sp.octant = 1;
+    sp.k = per;
+    kout = NB * per;
+    if (c.max_neighbors >= 0) kout = (int)std::min<int64_t>(kout, c.max_neighbors);
+  } else if (c.max_neighbors >= 0) {
+    sp.k = (int)std::min<int64_t>(c.max_neighbors, n);
+    kout = sp.k;
+  } else {
+    sp.unbounded = 1;
+    sp.k = (int)std::min<int64_t>(n, GS_MAX_SYSTEM - p);
+    kout = sp.k;
+  }
+  if (kout + p > GS_MAX_SYSTEM)
+    return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood plus drift terms exceed " +
+                                              std::to_string(GS_MAX_SYSTEM) + " on the CUDA path");
+  sp.kout = kout;
+  sp.has_radius = c.has_search_radius ? 1 : 0;
+  sp.r2 = c.has_search_radius ? c.search_radius * c.search_radius : 0.0;
+  const int nmax_all = kout + p;
+
+  KrigeArgs a{};
+  a.dim = dim;
+  a.method = (int)c.method;
+  a.p = p;
+  a.nv = k->nv;
+  a.uk_degree = (int)c.uk_degree;
+  a.min_nb = c.min_neighbors >= 0 ? (int)c.min_neighbors : 1;
+  a.kout = kout;
+  a.sk_mean = c.sk_mean;
+  for (int d = 0; d < 3; ++d) a.center[d] = k->center[d];
+  a.scale = k->scale;
+  for (int v = 0; v < GS_MAX_KED_VARS; ++v) {
+    a.dmean[v] = k->dmean[v];
+    a.dscale[v] = k->dscale[v];
+  }
+  a.x = ps->d_x;
+  a.y = ps->d_y;
+  a.z = ps->d_z;
+  a.val = ps->d_v;
+  a.meas_err = k->d_err;
+  a.drift = k->d_drift;
+
+  // chunking keeps the neighbour lists within a fixed budget
+  const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(nt, (int64_t)(1ll << 30) / (4ll * kout + 16)));
+  DevBuf nb, nbc, flag, tlist, nsel, tmp;
+  GS_TRY(nb.alloc((size_t)chunk * kout * 4, stream));
+  GS_TRY(nbc.alloc((size_t)chunk * 4, stream));
+  GS_TRY(flag.alloc((size_t)chunk, stream));
+  GS_TRY(tlist.alloc((size_t)chunk * 8, stream));
+  GS_TRY(nsel.alloc(8, stream));
+  size_t sel_bytes = 0;
+  GS_CUDA(cub::DeviceSelect::Flagged(nullptr, sel_bytes, thrust::counting_iterator<int64_t>(0),
+                                     (uint8_t*)nullptr, (int64_t*)nullptr, (int64_t*)nullptr,
+                                     (int64_t)chunk, stream));
+  GS_TRY(tmp.alloc(sel_bytes, stream));
+  // FP64 scratch (plain build or re-solve)
+  const int64_t budget = (int64_t)2 << 30;
+  const int64_t fthreads = fp64_threads_for(nmax_all, budget);
+  DevBuf scratch;
+  GS_TRY(scratch.alloc((size_t)fp64_scratch_doubles(nmax_all, fthreads) * 8, stream));
+
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; ++i) GS_CUDA(cudaEventCreate(&ev[i]));
+  float t_search = 0, t_mixed = 0, t_fp64 = 0;
+  GS_CUDA(cudaEventRecord(ev[0], stream));
+  int rc = GS_OK;
+  for (int64_t c0 = 0; c0 < nt && !rc; c0 += chunk) {
+    const int64_t cn = std::min(chunk, nt - c0);
+    const double* ctx = tx + c0;
+    const double* cty = ty + c0;
+    const double* ctz = dim == 3 ? tz + c0 : nullptr;
+    int32_t* dnb = (int32_t*)nb.ptr;
+    int32_t* dnbc = (int32_t*)nbc.ptr;
+    GS_CUDA(cudaEventRecord(ev[1], stream));
+    if (k->use_tree) {
+      rc = search_launch(k->grid, k->frame, sp, cn, ctx, cty, ctz, dnb, dnbc, stream);
+    } else {
+      iota_rows_kernel<<<(int)std::min<int64_t>((cn * kout + 255) / 256, 152 * 64), 256, 0, stream>>>(
+          cn, kout, dnb, dnbc);
+      rc = cudaGetLastError() == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "launch failed");
+    }
+    if (rc) break;
+    GS_CUDA(cudaEventRecord(ev[2], stream));
+    KrigeArgs ca = a;
+    ca.tx = ctx;
+    ca.ty = cty;
+    ca.tz = ctz;
+    ca.tdrift = tdrift ? tdrift + c0 * k->nv : nullptr;
+    ca.nb = dnb;
+    ca.nbc = dnbc;
+    ca.out_v = value + c0;
+    ca.out_var = variance + c0;
+    ca.out_lag = lagrange ? lagrange + c0 : nullptr;
+    ca.out_st = status + c0;
+    int64_t nflag = 0;
+    if (precision == GS_PREC_FP64) {
+      ca.nmax = nmax_all;
+      ca.tlist = nullptr;
+      ca.ntl = cn;
+      GS_CUDA(cudaEventRecord(ev[3], stream));
+      rc = krige_fp64_launch(ca, k->dm, (double*)scratch.ptr, fthreads, stream);
+      if (rc) break;
+      GS_CUDA(cudaEventRecord(ev[4], stream));
+    } else {
+      ca.nmax = std::min(nmax_all, GS_MIXED_MAX_NEIGHBORS + p);
+      ca.tlist = nullptr;
+      ca.ntl = cn;
+      rc = krige_mixed_launch(ca, k->dm, (uint8_t*)flag.ptr, 4, stream);
+      if (rc) break;
+      GS_CUDA(cudaEventRecord(ev[3], stream));
+      size_t b = sel_bytes;
+      GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
+                                         (uint8_t*)flag.ptr, (int64_t*)tlist.ptr,
+                                         (int64_t*)nsel.ptr, cn, stream));
+      GS_CUDA(cudaMemcpyAsync(&nflag, nsel.ptr, 8, cudaMemcpyDeviceToHost, stream));
+      GS_CUDA(cudaStreamSynchronize(stream));
+      if (nflag > 0) {
+        ca.nmax = nmax_all;
+        ca.tlist = (const int64_t*)tlist.ptr;
+        ca.ntl = nflag;
+        rc = krige_fp64_launch(ca, k->dm, (double*)scratch.ptr, fthreads, stream);
+        if (rc) break;
+      }
+      GS_CUDA(cudaEventRecord(ev[4], stream));
+    }
+    GS_CUDA(cudaEventSynchronize(ev[4]));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev[1], ev[2]);
+    t_search += ms;
+    if (precision == GS_PREC_FP64) {
+      cudaEventElapsedTime(&ms, ev[3], ev[4]);
+      t_fp64 += ms;
+    } else {
+      cudaEventElapsedTime(&ms, ev[2], ev[3]);
+      t_mixed += ms;
+      cudaEventElapsedTime(&ms, ev[3], ev[4]);
+      t_fp64 += ms;
+    }
+  }
+  GS_CUDA(cudaEventRecord(ev[5], stream));
+  GS_CUDA(cudaEventSynchronize(ev[5]));
+  float tot = 0;
+  cudaEventElapsedTime(&tot, ev[0], ev[5]);
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  g_timings[0] = t_search;
+  g_timings[1] = t_mixed;
+  g_timings[2] = t_fp64;
+  g_timings[3] = tot;
+  if (rc) return rc;
+  GS_CUDA(cudaStreamSynchronize(stream));
+  return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gs_kriging_new(const gs_pointset* ps, const gs_model* model, const gs_kcfg* cfg,
+                   gs_kriging** out) {
+  return kriging_create(ps, model, cfg, 0, nullptr, nullptr, out);
+}
+int gs_kriging_with_external_drift(const gs_pointset* ps, const gs_model* model,
+                                   const gs_kcfg* cfg, const double* drift, gs_kriging** out) {
+  return kriging_create(ps, model, cfg, 1, drift, nullptr, out);
+}
+int gs_kriging_with_measurement_error(const gs_pointset* ps, const gs_model* model,
+                                      const gs_kcfg* cfg, const double* errors,
+                                      gs_kriging** out) {
+  return kriging_create(ps, model, cfg, 2, nullptr, errors, out);
+}
+void gs_kriging_destroy(gs_kriging* k) { delete k; }
+
+int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double* tx,
+                                   const double* ty, const double* tz, const double* tdrift,
+                                   double* value, double* variance, double* lagrange,
+                                   uint8_t* status, int precision, void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (k->cfg.method == GS_EXTERNAL_DRIFT && !tdrift)
+    return fail(GS_ERR_INVALID_PARAMETER, "external drift kriging requires predict_with_drift");
+  if (k->cfg.method != GS_EXTERNAL_DRIFT && tdrift)
+    return fail(GS_ERR_INVALID_PARAMETER, "predict_with_drift requires KrigingMethod::ExternalDrift");
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  return predict_device(k, nt, tx, ty, tz, tdrift, value, variance, lagrange, status, precision, s);
+}
+
+int gs_kriging_predict_many(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                            const double* tz, const double* tdrift, double* value,
+                            double* variance, double* lagrange, uint8_t* status, int precision,
+                            void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (k->cfg.method == GS_EXTERNAL_DRIFT && !tdrift)
+    return fail(GS_ERR_INVALID_PARAMETER, "external drift kriging requires predict_with_drift");
+  if (k->cfg.method != GS_EXTERNAL_DRIFT && tdrift)
+    return fail(GS_ERR_INVALID_PARAMETER, "predict_with_drift requires KrigingMethod::ExternalDrift");
+  if (nt == 0) return GS_OK;
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  const int dim = k->ps->dim;
+  const int nv = k->nv;
+  DevBuf dx, dy, dz, dd, dv, dvar, dlag, dst;
+  GS_TRY(dx.alloc(nt * 8, s));
+  GS_TRY(dy.alloc(nt * 8, s));
+  if (dim == 3) GS_TRY(dz.alloc(nt * 8, s));
+  if (tdrift) GS_TRY(dd.alloc(nt * nv * 8, s));
+  GS_TRY(dv.alloc(nt * 8, s));
+  GS_TRY(dvar.alloc(nt * 8, s));
+  if (lagrange) GS_TRY(dlag.alloc(nt * 8, s));
+  GS_TRY(dst.alloc(nt, s));
+  GS_CUDA(cudaMemcpyAsync(dx.ptr, tx, nt * 8, cudaMemcpyHostToDevice, s));
+  GS_CUDA(cudaMemcpyAsync(dy.ptr, ty, nt * 8, cudaMemcpyHostToDevice, s));
+  if (dim == 3) GS_CUDA(cudaMemcpyAsync(dz.ptr, tz, nt * 8, cudaMemcpyHostToDevice, s));
+  if (tdrift) GS_CUDA(cudaMemcpyAsync(dd.ptr, tdrift, nt * nv * 8, cudaMemcpyHostToDevice, s));
+  GS_TRY(predict_device(k, nt, (double*)dx.ptr, (double*)dy.ptr, (double*)dz.ptr,
+                        (double*)dd.ptr, (double*)dv.ptr, (double*)dvar.ptr,
+                        lagrange ? (double*)dlag.ptr : nullptr, (uint8_t*)dst.ptr, precision, s));
+  GS_CUDA(cudaMemcpyAsync(value, dv.ptr, nt * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(variance, dvar.ptr, nt * 8, cudaMemcpyDeviceToHost, s));
+  if (lagrange) GS_CUDA(cudaMemcpyAsync(lagrange, dlag.ptr, nt * 8, cudaMemcpyDeviceToHost, s));
+  if (status) GS_CUDA(cudaMemcpyAsync(status, dst.ptr, nt, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+int gs_kriging_predict_grid(const gs_kriging* k, const double* bbox_min, const double* bbox_max,
+                            const int64_t* ncell, double* value, double* variance,
+                            uint8_t* status, int precision, void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (k->cfg.method == GS_EXTERNAL_DRIFT)
+    return fail(GS_ERR_INVALID_PARAMETER, "external drift kriging requires predict_with_drift");
+  const int dim = k->ps->dim;
+  double step[3] = {0, 0, 0};
+  int64_t total = 1;
+  for (int d = 0; d < dim; ++d) {
+    if (ncell[d] == 0) return fail(GS_ERR_INVALID_PARAMETER, "grid must have at least one cell per axis");
+    if (!(bbox_max[d] > bbox_min[d])) return fail(GS_ERR_INVALID_PARAMETER, "degenerate bbox");
+    step[d] = (bbox_max[d] - bbox_min[d]) / (double)ncell[d];
+    total *= ncell[d];
+  }
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  DevBuf dx, dy, dz, dv, dvar, dst;
+  GS_TRY(dx.alloc(total * 8, s));
+  GS_TRY(dy.alloc(total * 8, s));
+  if (dim == 3) GS_TRY(dz.alloc(total * 8, s));
+  GS_TRY(dv.alloc(total * 8, s));
+  GS_TRY(dvar.alloc(total * 8, s));
+  GS_TRY(dst.alloc(total, s));
+  GS_TRY(grid_centers_launch(dim, bbox_min, step, ncell, (double*)dx.ptr, (double*)dy.ptr,
+                             (double*)dz.ptr, s));
+  GS_TRY(predict_device(k, total, (double*)dx.ptr, (double*)dy.ptr, (double*)dz.ptr, nullptr,
+                        (double*)dv.ptr, (double*)dvar.ptr, nullptr, (uint8_t*)dst.ptr, precision, s));
+  GS_CUDA(cudaMemcpyAsync(value, dv.ptr, total * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(variance, dvar.ptr, total * 8, cudaMemcpyDeviceToHost, s));
+  if (status) GS_CUDA(cudaMemcpyAsync(status, dst.ptr, total, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+int gs_kriging_neighbors(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                         const double* tz, int64_t kcap, int32_t* idx, int32_t* count,
+                         void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (nt == 0) return GS_OK;
+  const gs_kcfg& c = k->cfg;
+  const int dim = k->ps->dim;
+  const int64_t n = k->ps->n;
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  if (!k->use_tree) {
+    for (int64_t t = 0; t < nt; ++t) {
+      for (int64_t j = 0; j < kcap; ++j) idx[t * kcap + j] = j < n ? (int32_t)j : -1;
+      if (count) count[t] = (int32_t)n;
+    }
+    return GS_OK;
+  }
+  SearchParams sp{};
+  int kout;
+  if (c.max_per_octant >= 0) {
+    int per = (int)std::min<int64_t>(c.max_per_octant, n);
+    sp.octant = 1;
+    sp.k = per;
+    kout = (1 << dim) * per;
+    if (c.max_neighbors >= 0) kout = (int)std::min<int64_t>(kout, c.max_neighbors);
+  } else if (c.max_neighbors >= 0) {
+    sp.k = (int)std::min<int64_t>(c.max_neighbors, n);
+    kout = sp.k;
+  } else {
+    sp.unbounded = 1;
+    sp.k = (int)std::min<int64_t>(n, GS_MAX_SYSTEM);
+    kout = sp.k;
+  }
+  sp.kout = kout;
+  sp.has_radius = c.has_search_radius ? 1 : 0;
+  sp.r2 = c.has_search_radius ? c.search_radius * c.search_radius : 0.0;
+  DevBuf dx, dy, dz, dnb, dnbc;
+  GS_TRY(dx.alloc(nt * 8, s));
+  GS_TRY(dy.alloc(nt * 8, s));
+  if (dim == 3) GS_TRY(dz.alloc(nt * 8, s));
+  GS_TRY(dnb.alloc((size_t)nt * kout * 4, s));
+  GS_TRY(dnbc.alloc(nt * 4, s));
+  GS_CUDA(cudaMemcpyAsync(dx.ptr, tx, nt * 8, cudaMemcpyHostToDevice, s));
+  GS_CUDA(cudaMemcpyAsync(dy.ptr, ty, nt * 8, cudaMemcpyHostToDevice, s));
+  if (dim == 3) GS_CUDA(cudaMemcpyAsync(dz.ptr, tz, nt * 8, cudaMemcpyHostToDevice, s));
+  GS_TRY(search_launch(k->grid, k->frame, sp, nt, (double*)dx.ptr, (double*)dy.ptr,
+                       (double*)dz.ptr, (int32_t*)dnb.ptr, (int32_t*)dnbc.ptr, s));
+  std::vector<int32_t> h((size_t)nt * kout), hc(nt);
+  GS_CUDA(cudaMemcpyAsync(h.data(), dnb.ptr, (size_t)nt * kout * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hc.data(), dnbc.ptr, nt * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  for (int64_t t = 0; t < nt; ++t) {
+    for (int64_t j = 0; j < kcap; ++j) idx[t * kcap + j] = j < kout ? h[t * kout + j] : -1;
+    if (count) count[t] = hc[t];
+  }
+  return GS_OK;
+}
+
+void gs_rng_uniform(uint64_t seed, int64_t count, double* out) {
+  Xoshiro r(seed);
+  for (int64_t i = 0; i < count; ++i) out[i] = r.uniform();
+}
+void gs_rng_normal(uint64_t seed, int64_t count, double* out) {
+  Xoshiro r(seed);
+  for (int64_t i = 0; i < count; ++i) out[i] = r.normal();
+}
+
+}  // extern "C"

@@ -1,0 +1,273 @@
+// gs_common.cuh -- shared types, error plumbing, double-float arithmetic and
+// the device variogram model.
+//
+// Precision design (GB300 has ~1/64-rate FP64): matrix entries are formed in
+// double-float ("df": an unevaluated FP32 pair hi+lo, ~2^-48 relative), the
+// hi parts feed an FP32 factorisation, and the df entries feed the residuals
+// of the iterative refinement.  Only O(N) per-system work (variances,
+// log-likelihood terms, coordinate differences) uses FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/geostat_gb300.h"
+
+namespace gs {
+
+// ---------------------------------------------------------------- errors --
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+#define GS_CUDA(call)                                                       \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) return ::gs::cuda_fail(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define GS_TRY(call)           \
+  do {                         \
+    int rc_ = (call);          \
+    if (rc_ != GS_OK) return rc_; \
+  } while (0)
+
+// ------------------------------------------------------------ df numbers --
+struct df {
+  float hi, lo;
+};
+
+__host__ __device__ inline df df_make(float h, float l) {
+  df r;
+  r.hi = h;
+  r.lo = l;
+  return r;
+}
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return df_make(s, e);
+}
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return df_make(s, e);
+}
+__device__ __forceinline__ df two_prod(float a, float b) {
+  float p = __fmul_rn(a, b);
+  float e = __fmaf_rn(a, b, -p);
+  return df_make(p, e);
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  df t = two_sum(a.lo, b.lo);
+  s.lo = __fadd_rn(s.lo, t.hi);
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo = __fadd_rn(s.lo, t.lo);
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_neg(df a) { return df_make(-a.hi, -a.lo); }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  df s = two_sum(a.hi, b);
+  s.lo = __fadd_rn(s.lo, a.lo);
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_mul(df a, df b) {
+  df p = two_prod(a.hi, b.hi);
+  p.lo = __fmaf_rn(a.hi, b.lo, p.lo);
+  p.lo = __fmaf_rn(a.lo, b.hi, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+  df p = two_prod(a.hi, b);
+  p.lo = __fmaf_rn(a.lo, b, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ df df_sqr(df a) {
+  df p = two_prod(a.hi, a.hi);
+  p.lo = __fmaf_rn(2.0f * a.hi, a.lo, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+__host__ __device__ inline df df_from_double(double x) {
+  float h = (float)x;
+  float l = (float)(x - (double)h);
+  return df_make(h, l);
+}
+__host__ __device__ inline double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
+
+// sqrt of a non-negative df: FP32 sqrt plus one correction step with the
+// exact residual s - y*y (Karp & Markstein 1997).
+__device__ __forceinline__ df df_sqrt(df s) {
+  if (!(s.hi > 0.0f)) return df_make(0.0f, 0.0f);
+  float y = __fsqrt_rn(s.hi);
+  df yy = two_prod(y, y);
+  float e = __fadd_rn(__fsub_rn(__fsub_rn(s.hi, yy.hi), yy.lo), s.lo);
+  float c = __fmul_rn(e, __frcp_rn(__fmul_rn(2.0f, y)));
+  return fast_two_sum(y, c);
+}
+
+// exp(-d) for d >= 0, table-driven after P. T. P. Tang, "Table-driven
+// implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2), 1989: d = n*ln2/64 + r with |r| <= ln2/128,
+// exp(-d) = 2^(-n/64) * exp(-r); 2^(-j/64) comes from a 64-entry df table
+// and exp(-r) from its Taylor series (r^2 term in df, higher terms in FP32).
+// ln2/64 is split in three parts; the first has 11 significant bits so that
+// n*L1 is exact for n < 2^13 (d < 88).
+struct ExpTable {
+  float hi[64];
+  float lo[64];
+};
+// Uniform df constants, filled on the host (df_consts_host): ln2/64 split in
+// three parts (l1 with 11 significant bits), 64/ln2, sqrt(3), sqrt(5).
+struct DfConsts {
+  float l1, l2, l3, inv;
+  float s3h, s3l, s5h, s5l;
+};
+typedef DfConsts ExpConsts;
+
+__device__ __forceinline__ df df_expneg(df d, const ExpTable& tab, const ExpConsts& k) {
+  if (!(d.hi < 87.0f)) return df_make(0.0f, 0.0f);
+  float nf = rintf(__fmul_rn(d.hi, k.inv));
+  int n = (int)nf;
+  float t1 = __fsub_rn(d.hi, __fmul_rn(nf, k.l1));  // exact (Sterbenz)
+  df r = two_sum(t1, d.lo);
+  df nl2 = two_prod(nf, k.l2);
+  r = df_sub(r, nl2);
+  r = df_add_f(r, -__fmul_rn(nf, k.l3));
+  // exp(-r) = 1 - r + r^2/2 - r^3/6 + r^4/24 - r^5/120
+  df r2 = df_sqr(r);
+  r2.hi *= 0.5f;
+  r2.lo *= 0.5f;
+  float t = r.hi;
+  float tail = t * t * t * (-(1.0f / 6.0f) + t * ((1.0f / 24.0f) - t * (1.0f / 120.0f)));
+  df q = df_add(df_neg(r), r2);
+  q = df_add_f(q, tail);
+  df e = df_add_f(q, 1.0f);
+  int j = n & 63;
+  int kk = n >> 6;
+  df res = df_mul(e, df_make(tab.hi[j], tab.lo[j]));
+  float sc = __int_as_float((127 - kk) << 23);  // 2^-kk, kk <= 125 for d < 87
+  return df_make(res.hi * sc, res.lo * sc);
+}
+
+void df_consts_host(ExpTable* tab, DfConsts* k);
+
+// ------------------------------------------------------------ the model --
+struct DevStruct {
+  int kind;
+  int aniso;
+  double sill;
+  double inv_range;
+  double rot[9];  // covariance-frame rotation+scaling, row-major 3x3
+  df sill_df;
+  df inv_range_df;
+  df rot_df[9];
+};
+
+struct DevModel {
+  int ns;
+  int dim;
+  double nugget;
+  double c0;  // total sill = C(0)
+  df c0_df;
+  DevStruct s[GS_MAX_STRUCTURES];
+};
+
+// Host: converts and validates a gs_model for the device path.
+int make_dev_model(const gs_model& m, int dim, DevModel* out, bool gpu_kinds_only);
+int validate_model(const gs_model& m);
+double total_sill(const gs_model& m);
+bool has_power(const gs_model& m);
+// Host rotation matrix of model.rs:407-433 (3-D) / 353-367 (2-D as matrix).
+void rotation_matrix(const gs_structure& s, int dim, double rot[9]);
+
+// Unit-sill correlation rho(d) = 1 - g(d) in FP64 (model.rs:122-141).
+__device__ __forceinline__ double rho_fp64(int kind, double d) {
+  switch (kind) {
+    case GS_KIND_SPHERICAL:
+      return d >= 1.0 ? 0.0 : 1.0 - (1.5 * d - 0.5 * d * d * d);
+    case GS_KIND_EXPONENTIAL:
+      return exp(-d);
+    case GS_KIND_GAUSSIAN:
+      return exp(-(d * d));
+    case GS_KIND_MATERN15: {
+      double s = 1.7320508075688772 * d;
+      return (1.0 + s) * exp(-s);
+    }
+    default: {  // GS_KIND_MATERN25
+      double s = 2.23606797749979 * d;
+      return (1.0 + s + s * s / 3.0) * exp(-s);
+    }
+  }
+}
+
+// Covariance C(h) = c0 - gamma(h) in FP64 for a separation vector.
+template <int D>
+__device__ __forceinline__ double cov_fp64(const DevModel& m, const double* h) {
+  bool zero = true;
+#pragma unroll
+  for (int d = 0; d < D; ++d) zero = zero && (h[d] == 0.0);
+  if (zero) return m.c0;
+  double acc = 0.0;
+  for (int k = 0; k < m.ns; ++k) {
+    const DevStruct& s = m.s[k];
+    double q = 0.0;
+    if (s.aniso) {
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        double e = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) e += s.rot[r * 3 + c] * h[c];
+        q += e * e;
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) q += h[d] * h[d];
+    }
+    acc += s.sill * rho_fp64(s.kind, sqrt(q) * s.inv_range);
+  }
+  return acc;
+}
+
+// rho(d) in df for d >= 0.
+__device__ __forceinline__ df rho_df(int kind, df d, const ExpTable& tab, const ExpConsts& k) {
+  switch (kind) {
+    case GS_KIND_SPHERICAL: {
+      if (d.hi > 1.0f || (d.hi == 1.0f && d.lo >= 0.0f)) return df_make(0.0f, 0.0f);
+      // 1 - d (1.5 - 0.5 d^2)
+      df d2 = df_sqr(d);
+      df t = df_add_f(df_make(-0.5f * d2.hi, -0.5f * d2.lo), 1.5f);
+      df u = df_mul(d, t);
+      return df_add_f(df_neg(u), 1.0f);
+    }
+    case GS_KIND_EXPONENTIAL:
+      return df_expneg(d, tab, k);
+    case GS_KIND_GAUSSIAN:
+      return df_expneg(df_sqr(d), tab, k);
+    case GS_KIND_MATERN15: {
+      df s = df_mul(d, df_make(k.s3h, k.s3l));
+      df e = df_expneg(s, tab, k);
+      return df_mul(df_add_f(s, 1.0f), e);
+    }
+    default: {  // GS_KIND_MATERN25
+      df s = df_mul(d, df_make(k.s5h, k.s5l));
+      df e = df_expneg(s, tab, k);
+      df s2 = df_sqr(s);
+      // 1 + s + s^2/3: s^2/3 as df via FP32 reciprocal correction
+      float q = s2.hi * (1.0f / 3.0f);
+      df q3 = two_prod(q, 3.0f);
+      float rq = (s2.hi - q3.hi - q3.lo + s2.lo) * (1.0f / 3.0f);
+      df third = fast_two_sum(q, rq);
+      df p = df_add(df_add_f(s, 1.0f), third);
+      return df_mul(p, e);
+    }
+  }
+}
+
+}  // namespace gs

@@ -1,0 +1,41 @@
+// gs_internal.h -- small host helpers shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace gs {
+
+// Initialises the device (and keeps the stream-ordered memory pool from
+// returning memory to the driver between calls).
+int ensure_device();
+
+// Stream-ordered device allocation released at scope exit.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  int alloc(size_t b, cudaStream_t s);
+  void release();
+  ~DevBuf();
+};
+
+}  // namespace gs
+
+// Device-resident point set behind the opaque gs_pointset handle.
+struct gs_pointset {
+  int dim = 2;
+  int64_t n = 0;
+  std::vector<double> host;  // n x dim, row-major
+  std::vector<double> values;
+  double* d_x = nullptr;
+  double* d_y = nullptr;
+  double* d_z = nullptr;
+  double* d_v = nullptr;
+  bool has_dup = false;
+  int64_t dup_i = 0, dup_j = 0;
+  ~gs_pointset();
+};

@@ -1,0 +1,63 @@
+// gs_krige.cuh -- per-target kriging solves (K3 mixed, K3' FP64).
+#pragma once
+
+#include <stdint.h>
+
+#include "gs_common.cuh"
+
+namespace gs {
+
+#define GS_MAX_KED_VARS 8
+#define GS_MIXED_MAX_DRIFT 10
+
+struct KrigeArgs {
+  int dim;
+  int method;     // GS_SIMPLE .. GS_EXTERNAL_DRIFT
+  int p;          // number of drift terms (KrigingMethod::n_drift)
+  int nv;         // external-drift variables
+  int uk_degree;
+  int min_nb;     // min_neighbors (1 when unset)
+  int kout;       // neighbour slots per target
+  int nmax;       // largest N = n + p in this launch (shared-memory sizing)
+  double sk_mean;
+  double center[3];
+  double scale;
+  double dmean[GS_MAX_KED_VARS];
+  double dscale[GS_MAX_KED_VARS];
+  const double* x;
+  const double* y;
+  const double* z;
+  const double* val;
+  const double* meas_err;    // n or null
+  const double* drift;       // n x nv raw covariates or null
+  const double* tx;
+  const double* ty;
+  const double* tz;
+  const double* tdrift;      // nt x nv or null
+  const int32_t* nb;
+  const int32_t* nbc;
+  double* out_v;
+  double* out_var;
+  double* out_lag;           // may be null
+  uint8_t* out_st;
+  const int64_t* tlist;      // targets to process (null: 0..nt-1)
+  int64_t ntl;
+};
+
+// Mixed-precision kernel for systems with n <= 64 neighbours and at most
+// GS_MIXED_MAX_DRIFT drift terms.  Systems it cannot certify are marked in
+// `flag` (1 = re-solve in FP64).
+int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int warps_per_block,
+                       cudaStream_t stream);
+// Plain FP64 kernel, one system per thread (also the re-solve path).
+// scratch must hold fp64_scratch_doubles(nmax, threads) doubles.
+int krige_fp64_launch(const KrigeArgs& a, const DevModel& m, double* scratch, int64_t threads,
+                      cudaStream_t stream);
+int64_t fp64_scratch_doubles(int nmax, int64_t threads);
+int64_t fp64_threads_for(int nmax, int64_t budget_bytes);
+
+// Grid2D / Grid3D cell centres (grid.rs:80-96, 188-203) on the device.
+int grid_centers_launch(int dim, const double* bmin, const double* step, const int64_t* ncell,
+                        double* x, double* y, double* z, cudaStream_t stream);
+
+}  // namespace gs

@@ -1,0 +1,640 @@
+// gs_search.cu -- device bucket grid (K1) and warp-per-target neighbour
+// search (K2).
+//
+// The search returns exactly the set the reference's kd-tree returns
+// (crates/geostat-core/src/search.rs:57-99 via kriging.rs:441-490): the k
+// smallest (squared distance, index) pairs within the radius, in that order.
+// Squared distances are formed exactly as the reference does --
+// ((0 + dx0^2) + dx1^2) + dx2^2 with dx = point - target, every operation
+// separately rounded -- so the comparisons see bit-identical values.  The
+// kd-tree keeps the first-visited candidate when the k-th and (k+1)-th tie
+// exactly; this search keeps the smaller index.  The two agree whenever no
+// such boundary tie exists (the oracle counts them).
+//
+// Octant search (kriging.rs:462-489) keeps, per 2^D sector around the
+// target, the per_octant smallest (d2, index) candidates, merges the sectors
+// in (d2, index) order and truncates to max_neighbors -- the same selection
+// as the reference's distance-ordered walk over all candidates.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gs_search.cuh"
+
+namespace gs {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// search_point (kriging.rs:16-21) with the reference's operation order.
+template <int D>
+__device__ __forceinline__ void to_search_frame(const SearchFrame& f, const double* p, double* q) {
+  if (!f.aniso) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) q[d] = p[d];
+    return;
+  }
+  if (D == 2) {
+    // out[0] = dh0*s + dh1*c ; out[1] = (dh0*c - dh1*s) / ratio
+    q[0] = __dadd_rn(__dmul_rn(p[0], f.s), __dmul_rn(p[1], f.c));
+    q[1] = __ddiv_rn(__dsub_rn(__dmul_rn(p[0], f.c), __dmul_rn(p[1], f.s)), f.ratio);
+  } else {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      q[r] = __dadd_rn(__dadd_rn(__dmul_rn(f.rot[r * 3 + 0], p[0]), __dmul_rn(f.rot[r * 3 + 1], p[1])),
+                       __dmul_rn(f.rot[r * 3 + 2], p[2]));
+  }
+}
+
+template <int D>
+__global__ void transform_kernel(SearchFrame f, int64_t n, const double* x, const double* y,
+                                 const double* z, double* ox, double* oy, double* oz) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double p[3] = {x[i], y[i], D == 3 ? z[i] : 0.0};
+    double q[3];
+    to_search_frame<D>(f, p, q);
+    ox[i] = q[0];
+    oy[i] = q[1];
+    if (D == 3) oz[i] = q[2];
+  }
+}
+
+__device__ __forceinline__ int clamp_cell(double v, int n) {
+  double c = floor(v);
+  if (!(c >= 0.0)) return 0;  // also NaN
+  if (c >= (double)(n - 1)) return n - 1;
+  return (int)c;
+}
+
+template <int D>
+__global__ void cell_id_kernel(GridDev g, int64_t n, const double* x, const double* y,
+                               const double* z, uint32_t* keys, uint32_t* vals) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int cx = clamp_cell((x[i] - g.origin[0]) * g.inv_cell, g.n[0]);
+    int cy = clamp_cell((y[i] - g.origin[1]) * g.inv_cell, g.n[1]);
+    int cz = D == 3 ? clamp_cell((z[i] - g.origin[2]) * g.inv_cell, g.n[2]) : 0;
+    keys[i] = (uint32_t)(cx + g.n[0] * (cy + g.n[1] * cz));
+    vals[i] = (uint32_t)i;
+  }
+}
+
+template <int D>
+__global__ void gather_kernel(int64_t n, const uint32_t* perm, const double* x, const double* y,
+                              const double* z, double* sx, double* sy, double* sz,
+                              uint32_t* sidx) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t p = perm[i];
+    sx[i] = x[p];
+    sy[i] = y[p];
+    if (D == 3) sz[i] = z[p];
+    sidx[i] = p;
+  }
+}
+
+__global__ void cell_start_kernel(int64_t ncells, int64_t n, const uint32_t* keys,
+                                  uint32_t* cstart) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= ncells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = n;  // first position with key >= c
+    while (lo < hi) {
+      int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)keys[mid] < c) lo = mid + 1;
+      else hi = mid;
+    }
+    cstart[c] = (uint32_t)lo;
+  }
+}
+
+// Offset of the s-th cell on the surface of the Chebyshev shell of radius r.
+template <int D>
+__device__ __forceinline__ void shell_offset(int r, int s, int* o) {
+  if (r == 0) {
+    o[0] = o[1] = o[2] = 0;
+    return;
+  }
+  const int w = 2 * r + 1, wi = 2 * r - 1;
+  if (D == 2) {
+    if (s < w) {
+      o[0] = -r + s;
+      o[1] = -r;
+    } else if (s < 2 * w) {
+      o[0] = -r + (s - w);
+      o[1] = r;
+    } else {
+      int rem = s - 2 * w;
+      o[0] = (rem / wi) ? r : -r;
+      o[1] = -r + 1 + rem % wi;
+    }
+    o[2] = 0;
+  } else {
+    const int fz = w * w, fy = w * wi;
+    if (s < 2 * fz) {
+      int q = s % fz;
+      o[0] = -r + q % w;
+      o[1] = -r + q / w;
+      o[2] = (s / fz) ? r : -r;
+    } else if (s < 2 * fz + 2 * fy) {
+      int rem = s - 2 * fz;
+      int q = rem % fy;
+      o[0] = -r + q % w;
+      o[2] = -r + 1 + q / w;
+      o[1] = (rem / fy) ? r : -r;
+    } else {
+      int rem = s - 2 * fz - 2 * fy;
+      int fx = wi * wi;
+      int q = rem % fx;
+      o[1] = -r + 1 + q % wi;
+      o[2] = -r + 1 + q / wi;
+      o[0] = (rem / fx) ? r : -r;
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ int shell_size(int r) {
+  if (r == 0) return 1;
+  return D == 2 ? 8 * r : 24 * r * r + 2;
+}
+
+// Warp-wide bitonic sort of cap (power of two) entries by (d2, idx).
+__device__ __noinline__ void warp_sort(double* d2, uint32_t* id, int n_valid, int cap, int lane) {
+  for (int i = n_valid + lane; i < cap; i += 32) {
+    d2[i] = __longlong_as_double(0x7ff0000000000000ll);
+    id[i] = 0xffffffffu;
+  }
+  __syncwarp();
+  for (int size = 2; size <= cap; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = lane; i < (cap >> 1); i += 32) {
+        int a = 2 * stride * (i / stride) + (i % stride);
+        int b = a + stride;
+        bool up = (a & size) == 0;
+        double da = d2[a], db = d2[b];
+        uint32_t ia = id[a], ib = id[b];
+        bool gt = (da > db) || (da == db && ia > ib);
+        if (gt == up) {
+          d2[a] = db;
+          d2[b] = da;
+          id[a] = ib;
+          id[b] = ia;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+template <int D, bool OCT, bool RANKED>
+__global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, SearchParams p,
+                                                  int64_t nt, const double* tx, const double* ty,
+                                                  const double* tz, int32_t* nb, int32_t* nbc) {
+  constexpr int NB = OCT ? (1 << D) : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const int capb = p.capb;
+  const size_t per_warp = (size_t)NB * capb * 12 + NB * 16;
+  unsigned char* base = smem_raw + (size_t)wib * per_warp;
+  double* bd2 = reinterpret_cast<double*>(base);
+  uint32_t* bid = reinterpret_cast<uint32_t*>(bd2 + NB * capb);
+  double* thr = reinterpret_cast<double*>(bid + NB * capb);
+  int* cnt = reinterpret_cast<int*>(thr + NB);
+  int* dirty = cnt + NB;
+  const double kInf = __longlong_as_double(0x7ff0000000000000ll);
+  const double r2 = p.has_radius ? p.r2 : kInf;
+  const int kb = p.k;
+
+  for (int64_t t = (int64_t)blockIdx.x * wpb + wib; t < nt; t += (int64_t)gridDim.x * wpb) {
+    double pt[3] = {tx[t], ty[t], D == 3 ? tz[t] : 0.0};
+    double q[3];
+    to_search_frame<D>(fr, pt, q);
+    int tc[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) tc[d] = clamp_cell((q[d] - g.origin[d]) * g.inv_cell, g.n[d]);
+    int maxring = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) maxring = max(maxring, max(tc[d], g.n[d] - 1 - tc[d]));
+    int octmax[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      int m = 0;
+      if (OCT) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          int ext = ((b >> d) & 1) ? (g.n[d] - 1 - tc[d]) : tc[d];
+          m = max(m, max(ext, 1));
+        }
+      } else {
+        m = maxring;
+      }
+      octmax[b] = m;
+    }
+    if (lane < NB) {
+      thr[lane] = kInf;
+      cnt[lane] = 0;
+      dirty[lane] = 0;
+    }
+    __syncwarp();
+    long long inrad = 0;
+    const int64_t qrank = RANKED ? p.rank0 + t : 0;
+    if (RANKED && qrank <= p.brute_below) {
+      // early ranks: scan the whole (short) prefix of the store
+      for (int64_t rb = 0; rb < qrank; rb += 32) {
+        const int64_t r = rb + lane;
+        const bool valid = r < qrank;
+        double d2 = kInf;
+        if (valid) {
+          const double dx = __dsub_rn(p.px[r], q[0]);
+          const double dy = __dsub_rn(p.py[r], q[1]);
+          d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+          if (D == 3) {
+            const double dz = __dsub_rn(p.pz[r], q[2]);
+            d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
+          }
+        }
+        bool want = valid && d2 <= r2 && d2 <= thr[0];
+        unsigned m = __ballot_sync(kFull, want);
+        if (!m) continue;
+        if (cnt[0] + __popc(m) > capb) {
+          warp_sort(bd2, bid, cnt[0], capb, lane);
+          if (lane == 0) {
+            cnt[0] = min(cnt[0], kb);
+            if (cnt[0] >= kb) thr[0] = bd2[kb - 1];
+          }
+          __syncwarp();
+          want = want && d2 <= thr[0];
+          m = __ballot_sync(kFull, want);
+        }
+        if (want) {
+          int slot = cnt[0] + __popc(m & ((1u << lane) - 1u));
+          bd2[slot] = d2;
+          bid[slot] = (uint32_t)r;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          cnt[0] += __popc(m);
+          dirty[0] = 1;
+        }
+        __syncwarp();
+      }
+      maxring = -1;  // skip the ring walk
+    }
+
+    for (int ring = 0; ring <= maxring; ++ring) {
+      double rmin = fmax((double)ring - 1.0 - 1e-9, 0.0) * g.cell;
+      double rmin2 = rmin * rmin;
+      unsigned active = 0;
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        bool done = (rmin2 > r2) || (cnt[b] >= kb && rmin2 > thr[b]) || (ring > octmax[b]);
+        if (!done) active |= 1u << b;
+      }
+      if (!active) break;
+      const int S = shell_size<D>(ring);
+      for (int sbase = 0; sbase < S; sbase += 32) {
+        int s = sbase + lane;
+        int ccount = 0;
+        uint32_t cst = 0;
+        if (s < S) {
+          int o[3];
+          shell_offset<D>(ring, s, o);
+          int c[3] = {tc[0] + o[0], tc[1] + o[1], tc[2] + o[2]};
+          bool ok = true;
+#pragma unroll
+          for (int d = 0; d < D; ++d) ok = ok && c[d] >= 0 && c[d] < g.n[d];
+          if (OCT && ok) {
+            // sectors a cell can hold (conservative by one cell for rounding)
+            unsigned mask = (1u << NB) - 1u;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              unsigned hi_side = 0, lo_side = 0;
+#pragma unroll
+              for (int b = 0; b < NB; ++b) {
+                if ((b >> d) & 1) hi_side |= 1u << b;
+                else lo_side |= 1u << b;
+              }
+              if (o[d] >= 2) mask &= hi_side;
+              else if (o[d] <= -2) mask &= lo_side;
+            }
+            ok = (mask & active) != 0;
+          }
+          if (ok) {
+            int64_t cid = c[0] + (int64_t)g.n[0] * (c[1] + (int64_t)g.n[1] * c[2]);
+            cst = g.cstart[cid];
+            ccount = (int)(g.cstart[cid + 1] - cst);
+          }
+        }
+        int incl = ccount;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          int v = __shfl_up_sync(kFull, incl, off);
+          if (lane >= off) incl += v;
+        }
+        const int tot = __shfl_sync(kFull, incl, 31);
+        const int excl = incl - ccount;
+        for (int pbase = 0; pbase < tot; pbase += 32) {
+          const int my = pbase + lane;
+          int pos = 0;
+#pragma unroll
+          for (int st = 16; st > 0; st >>= 1) {
+            int v = __shfl_sync(kFull, incl, pos + st - 1);
+            if (v <= my) pos += st;
+          }
+          const int src = pos & 31;
+          const uint32_t sst = __shfl_sync(kFull, cst, src);
+          const int sex = __shfl_sync(kFull, excl, src);
+          const bool valid = my < tot;
+          double d2 = kInf;
+          uint32_t oid = 0;
+          int ob = 0;
+          if (valid) {
+            const uint32_t pi = sst + (uint32_t)(my - sex);
+            const double px = g.sx[pi], py = g.sy[pi];
+            const double dx = __dsub_rn(px, q[0]);
+            const double dy = __dsub_rn(py, q[1]);
+            d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+            if (OCT) ob = (px >= q[0] ? 1 : 0) | (py >= q[1] ? 2 : 0);
+            if (D == 3) {
+              const double pz = g.sz[pi];
+              const double dz = __dsub_rn(pz, q[2]);
+              d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
+              if (OCT) ob |= (pz >= q[2] ? 4 : 0);
+            }
+            oid = g.sidx[pi];
+          }
+          const bool inr = valid && d2 <= r2 && (!RANKED || (int64_t)oid < qrank);
+          if (p.unbounded) inrad += __popc(__ballot_sync(kFull, inr));
+#pragma unroll
+          for (int b = 0; b < NB; ++b) {
+            bool want = inr && (ob == b) && d2 <= thr[b];
+            unsigned m = __ballot_sync(kFull, want);
+            if (!m) continue;
+            if (cnt[b] + __popc(m) > capb) {
+              warp_sort(bd2 + b * capb, bid + b * capb, cnt[b], capb, lane);
+              if (lane == 0) {
+                cnt[b] = min(cnt[b], kb);
+                if (cnt[b] >= kb) thr[b] = bd2[b * capb + kb - 1];
+                dirty[b] = 0;
+              }
+              __syncwarp();
+              want = want && d2 <= thr[b];
+              m = __ballot_sync(kFull, want);
+            }
+            if (want) {
+              int slot = cnt[b] + __popc(m & ((1u << lane) - 1u));
+              bd2[b * capb + slot] = d2;
+              bid[b * capb + slot] = oid;
+            }
+            __syncwarp();
+            if (lane == 0) {
+              cnt[b] += __popc(m);
+              dirty[b] = 1;
+            }
+            __syncwarp();
+          }
+        }
+      }
+      // ring end: settle thresholds of buffers that reached k
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (dirty[b] && cnt[b] >= kb) {
+          warp_sort(bd2 + b * capb, bid + b * capb, cnt[b], capb, lane);
+          if (lane == 0) {
+            cnt[b] = kb;
+            thr[b] = bd2[b * capb + kb - 1];
+            dirty[b] = 0;
+          }
+          __syncwarp();
+        }
+      }
+    }
+    // final ordering
+    int total = 0;
+    if (!OCT) {
+      warp_sort(bd2, bid, cnt[0], capb, lane);
+      total = min(cnt[0], kb);
+    } else {
+      for (int b = 0; b < NB; ++b) {
+        if (dirty[b]) warp_sort(bd2 + b * capb, bid + b * capb, cnt[b], capb, lane);
+        int c = min(cnt[b], kb);
+        total += c;
+        for (int i = c + lane; i < capb; i += 32) {
+          bd2[b * capb + i] = kInf;
+          bid[b * capb + i] = 0xffffffffu;
+        }
+      }
+      __syncwarp();
+      warp_sort(bd2, bid, NB * capb, NB * capb, lane);
+    }
+    const int kout = p.kout;
+    const int outn = min(total, kout);
+    for (int j = lane; j < kout; j += 32) nb[t * kout + j] = j < outn ? (int32_t)bid[j] : -1;
+    if (lane == 0) {
+      bool overflow = p.unbounded && inrad > (long long)kout;
+      nbc[t] = overflow ? -1 : outn;
+    }
+    __syncwarp();
+  }
+}
+
+inline unsigned ceil_pow2(unsigned v) {
+  unsigned p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+template <class T>
+int dalloc(T** p, size_t count) {
+  GS_CUDA(cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
+  return GS_OK;
+}
+
+}  // namespace
+
+Grid::~Grid() {
+  cudaFree(d_sx);
+  cudaFree(d_sy);
+  cudaFree(d_sz);
+  cudaFree(d_sidx);
+  cudaFree(d_cstart);
+}
+
+int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, const double* z,
+               const SearchFrame& frame, double points_per_cell, cudaStream_t stream) {
+  if (n <= 0 || n > 0xfffffff0ll) return fail(GS_ERR_INVALID_PARAMETER, "point count out of range");
+  g->dim = dim;
+  g->n = n;
+  double *tx = nullptr, *ty = nullptr, *tz = nullptr;
+  GS_TRY(dalloc(&tx, n));
+  GS_TRY(dalloc(&ty, n));
+  if (dim == 3) GS_TRY(dalloc(&tz, n));
+  const int threads = 256;
+  const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, 152 * 32);
+  if (dim == 2) transform_kernel<2><<<blocks, threads, 0, stream>>>(frame, n, x, y, z, tx, ty, tz);
+  else transform_kernel<3><<<blocks, threads, 0, stream>>>(frame, n, x, y, z, tx, ty, tz);
+  GS_CUDA(cudaGetLastError());
+
+  // bounding box of the search-frame coordinates
+  double* d_red = nullptr;
+  GS_TRY(dalloc(&d_red, 6));
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0;
+  GS_CUDA(cub::DeviceReduce::Min(tmp, tmp_bytes, tx, d_red, (int)n, stream));
+  size_t need = tmp_bytes;
+  GS_CUDA(cub::DeviceReduce::Max(nullptr, tmp_bytes, tx, d_red, (int)n, stream));
+  need = std::max(need, tmp_bytes);
+  GS_CUDA(cudaMalloc(&tmp, need));
+  const double* axes[3] = {tx, ty, tz};
+  for (int d = 0; d < dim; ++d) {
+    tmp_bytes = need;
+    GS_CUDA(cub::DeviceReduce::Min(tmp, tmp_bytes, axes[d], d_red + d, (int)n, stream));
+    tmp_bytes = need;
+    GS_CUDA(cub::DeviceReduce::Max(tmp, tmp_bytes, axes[d], d_red + 3 + d, (int)n, stream));
+  }
+  double h_red[6] = {0, 0, 0, 0, 0, 0};
+  GS_CUDA(cudaMemcpyAsync(h_red, d_red, 6 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  GS_CUDA(cudaStreamSynchronize(stream));
+  cudaFree(tmp);
+  cudaFree(d_red);
+
+  // cell size: about points_per_cell points per cell over the active axes
+  double ext[3] = {0, 0, 0}, maxext = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    ext[d] = h_red[3 + d] - h_red[d];
+    maxext = std::max(maxext, ext[d]);
+  }
+  double vol = 1.0;
+  int act = 0;
+  for (int d = 0; d < dim; ++d)
+    if (ext[d] > maxext * 1e-9) {
+      vol *= ext[d];
+      ++act;
+    }
+  double cell;
+  if (act == 0 || !(maxext > 0.0)) {
+    cell = 1.0;
+  } else {
+    cell = std::pow(vol * points_per_cell / (double)n, 1.0 / act);
+    if (!(cell > 0.0)) cell = maxext;
+  }
+  int64_t total = 1;
+  int nd[3] = {1, 1, 1};
+  for (int guard = 0; guard < 200; ++guard) {
+    total = 1;
+    for (int d = 0; d < dim; ++d) {
+      double c = ext[d] > maxext * 1e-9 ? std::ceil(ext[d] / cell) : 1.0;
+      nd[d] = (int)std::max(1.0, std::min(c, 1.0e6));
+      total *= nd[d];
+    }
+    if (total <= 2 * n + 64) break;
+    cell *= 1.25;
+  }
+  GridDev& G = g->dev;
+  for (int d = 0; d < 3; ++d) {
+    G.origin[d] = d < dim ? h_red[d] : 0.0;
+    G.n[d] = nd[d];
+  }
+  G.cell = cell;
+  G.inv_cell = 1.0 / cell;
+  G.ncells = total;
+
+  uint32_t *keys = nullptr, *vals = nullptr, *keys2 = nullptr, *vals2 = nullptr;
+  GS_TRY(dalloc(&keys, n));
+  GS_TRY(dalloc(&vals, n));
+  GS_TRY(dalloc(&keys2, n));
+  GS_TRY(dalloc(&vals2, n));
+  if (dim == 2) cell_id_kernel<2><<<blocks, threads, 0, stream>>>(G, n, tx, ty, tz, keys, vals);
+  else cell_id_kernel<3><<<blocks, threads, 0, stream>>>(G, n, tx, ty, tz, keys, vals);
+  GS_CUDA(cudaGetLastError());
+  int bits = 1;
+  while (bits < 32 && ((int64_t)1 << bits) < total) ++bits;
+  tmp = nullptr;
+  tmp_bytes = 0;
+  GS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0,
+                                          bits, stream));
+  GS_CUDA(cudaMalloc(&tmp, std::max<size_t>(tmp_bytes, 1)));
+  GS_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0,
+                                          bits, stream));
+  GS_TRY(dalloc(&g->d_sx, n));
+  GS_TRY(dalloc(&g->d_sy, n));
+  if (dim == 3) GS_TRY(dalloc(&g->d_sz, n));
+  GS_TRY(dalloc(&g->d_sidx, n));
+  GS_TRY(dalloc(&g->d_cstart, total + 1));
+  if (dim == 2)
+    gather_kernel<2><<<blocks, threads, 0, stream>>>(n, vals2, tx, ty, tz, g->d_sx, g->d_sy,
+                                                     g->d_sz, g->d_sidx);
+  else
+    gather_kernel<3><<<blocks, threads, 0, stream>>>(n, vals2, tx, ty, tz, g->d_sx, g->d_sy,
+                                                     g->d_sz, g->d_sidx);
+  GS_CUDA(cudaGetLastError());
+  {
+    int cb = (int)std::min<int64_t>((total + 1 + threads - 1) / threads, 152 * 32);
+    cell_start_kernel<<<cb, threads, 0, stream>>>(total, n, keys2, g->d_cstart);
+    GS_CUDA(cudaGetLastError());
+  }
+  GS_CUDA(cudaStreamSynchronize(stream));
+  cudaFree(tmp);
+  cudaFree(keys);
+  cudaFree(vals);
+  cudaFree(keys2);
+  cudaFree(vals2);
+  cudaFree(tx);
+  cudaFree(ty);
+  cudaFree(tz);
+  G.sx = g->d_sx;
+  G.sy = g->d_sy;
+  G.sz = g->d_sz;
+  G.sidx = g->d_sidx;
+  G.cstart = g->d_cstart;
+  return GS_OK;
+}
+
+int grid_build_ranked(Grid* g, int dim, int64_t n, const double* x, const double* y,
+                      const double* z, double points_per_cell, cudaStream_t stream) {
+  SearchFrame f;
+  std::memset(&f, 0, sizeof(f));
+  return grid_build(g, dim, n, x, y, z, f, points_per_cell, stream);
+}
+
+int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p0, int64_t nt,
+                  const double* tx, const double* ty, const double* tz, int32_t* nb,
+                  int32_t* nbc, cudaStream_t stream) {
+  if (nt == 0) return GS_OK;
+  SearchParams p = p0;
+  p.capb = (int)ceil_pow2((unsigned)std::max(p.k + 32, 64));
+  const int NB = p.octant ? (1 << g.dim) : 1;
+  const int wpb = 4;
+  size_t per_warp = (size_t)NB * p.capb * 12 + NB * 16;
+  size_t smem = per_warp * wpb;
+  static const size_t kMaxSmem = 227 * 1024;
+  if (smem > kMaxSmem) return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood too large for the device search");
+  int64_t blocks64 = (nt + wpb - 1) / wpb;
+  int blocks = (int)std::min<int64_t>(blocks64, 152 * 64);
+  auto launch = [&](auto kern) -> int {
+    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<blocks, wpb * 32, smem, stream>>>(g.dev, frame, p, nt, tx, ty, tz, nb, nbc);
+    GS_CUDA(cudaGetLastError());
+    return GS_OK;
+  };
+  if (p.ranked) {
+    if (p.octant) return fail(GS_ERR_INVALID_PARAMETER, "ranked octant search is not supported");
+    if (g.dim == 2) return launch(knn_kernel<2, false, true>);
+    return launch(knn_kernel<3, false, true>);
+  }
+  if (g.dim == 2) {
+    if (p.octant) return launch(knn_kernel<2, true, false>);
+    return launch(knn_kernel<2, false, false>);
+  }
+  if (p.octant) return launch(knn_kernel<3, true, false>);
+  return launch(knn_kernel<3, false, false>);
+}
+
+}  // namespace gs

@@ -1,0 +1,828 @@
+// gs_vecchia.cu -- Vecchia plan, log-likelihood, MLE driver and joint
+// prediction (crates/geostat-core/src/vecchia.rs).
+//
+// Plan (vecchia.rs:232-282): the max-min order is computed on the host (as
+// in the reference); the m nearest predecessors of every ordered point come
+// from the ranked device search (store rank = order position), sorted by
+// (squared distance, position) like the reference's incremental BucketGrid.
+//
+// Log-likelihood (vecchia.rs:285-336): one warp per ordered point runs every
+// parameter candidate of the batch against the point's conditioning set:
+// double-float covariances, FP32 L D L^T with FP64-accumulated refinement,
+// FP64 mean/variance/log terms.  Points whose refinement stalls are redone
+// by an FP64 one-thread-per-point Cholesky that follows linalg.rs:123-203.
+// Per-point terms are summed per candidate in a fixed tree order (FP64), so
+// results do not depend on scheduling.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "gs_common.cuh"
+#include "gs_host.h"
+#include "gs_internal.h"
+#include "gs_search.cuh"
+#include "gs_solve.cuh"
+
+struct gs_vecchia_plan {
+  const gs_pointset* ps = nullptr;
+  int64_t n = 0;
+  int64_t m = 0;
+  std::vector<int64_t> order;
+  int64_t* d_order = nullptr;  // position -> point id
+  int32_t* d_nb = nullptr;     // n x m point ids, -1 padded
+  int32_t* d_cnt = nullptr;
+  double mean = 0.0;
+  cudaStream_t stream = nullptr;
+  ~gs_vecchia_plan() {
+    cudaFree(d_order);
+    cudaFree(d_nb);
+    cudaFree(d_cnt);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace gs {
+namespace {
+
+__global__ void gather_by_order(int64_t n, const int64_t* order, const double* x, const double* y,
+                                const double* z, double* ox, double* oy, double* oz) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = order[k];
+    ox[k] = x[i];
+    oy[k] = y[i];
+    if (oz) oz[k] = z[i];
+  }
+}
+
+__global__ void positions_to_ids(int64_t total, const int64_t* order, int32_t* nb) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t pos = nb[q];
+    if (pos >= 0) nb[q] = (int32_t)order[pos];
+  }
+}
+
+struct VArgs {
+  int dim;
+  int64_t n;
+  int m;
+  int ncand;
+  int iso_shared;  // every candidate isotropic: cache separation norms
+  const double* x;
+  const double* y;
+  const double* z;
+  const double* v;
+  double mean;
+  const int64_t* order;
+  const int32_t* nb;
+  const int32_t* cnt;
+  const DevModel* models;  // device array of ncand models
+  double* terms;           // ncand x n (position order)
+  uint8_t* flag;           // ncand x n
+};
+
+constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
+
+size_t vecchia_per_warp_bytes(int m, int dim) {
+  const int NP = m * (m + 1) / 2;
+  size_t b = 0;
+  b += (size_t)NP * sizeof(df) * 2;                       // A, H (cached norms)
+  b += (size_t)(GS_MAX_STRUCTURES + 1) * m * dim * sizeof(df);  // V
+  b += (size_t)m * sizeof(df) * 3;                        // B, XD, H0
+  b += (size_t)m * sizeof(double) * 2;                    // X, Z
+  b += (size_t)NP * sizeof(float);                        // L
+  b += (size_t)m * sizeof(float) * 2;                     // W, DI
+  return (b + 15) & ~(size_t)15;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) vecchia_loglik_kernel(VArgs a, ExpTable tab_g, DfConsts kc,
+                                                             size_t per_warp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ ExpTable tab;
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+    tab.hi[i] = tab_g.hi[i];
+    tab.lo[i] = tab_g.lo[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const int M = a.m;
+  const int NP = (M * (M + 1)) >> 1;
+  unsigned char* base = smem_raw + (size_t)wib * per_warp;
+  df* A = reinterpret_cast<df*>(base);
+  df* H = A + NP;
+  df* V = H + NP;
+  df* B = V + (GS_MAX_STRUCTURES + 1) * M * D;
+  df* XD = B + M;
+  df* H0 = XD + M;
+  double* X = reinterpret_cast<double*>(H0 + M);
+  double* Z = X + M;
+  float* L = reinterpret_cast<float*>(Z + M);
+  float* W = L + NP;
+  float* DI = W + M;
+
+  for (int64_t k = (int64_t)blockIdx.x * wpb + wib; k < a.n; k += (int64_t)gridDim.x * wpb) {
+    const int64_t i = a.order[k];
+    const int s = a.cnt[k];
+    const double zi = a.v[i] - a.mean;
+    if (s == 0) {
+      // first point: marginal N(0, sill)
+      for (int c = lane; c < a.ncand; c += 32) {
+        const double sill = a.models[c].c0;
+        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
+        a.flag[(int64_t)c * a.n + k] = 0;
+      }
+      continue;
+    }
+    if (s > M) {
+      for (int c = lane; c < a.ncand; c += 32) a.flag[(int64_t)c * a.n + k] = 1;
+      continue;
+    }
+    double pi[3] = {a.x[i], a.y[i], D == 3 ? a.z[i] : 0.0};
+    // separations to the point, identity frame (df) and values
+    for (int q = lane; q < s; q += 32) {
+      const int j = a.nb[k * (int64_t)M + q];
+      double u[3] = {a.x[j] - pi[0], a.y[j] - pi[1], D == 3 ? a.z[j] - pi[2] : 0.0};
+#pragma unroll
+      for (int d = 0; d < D; ++d) V[q * D + d] = df_from_double(u[d]);
+      Z[q] = a.v[j] - a.mean;
+    }
+    __syncwarp();
+    const int npairs = (s * (s - 1)) >> 1;
+    if (a.iso_shared) {
+      for (int q = lane; q < s; q += 32) H0[q] = norm0_df<D>(&V[q * D]);
+      int ii = 1, jj = lane;
+      while (jj >= ii && ii < s) {
+        jj -= ii;
+        ++ii;
+      }
+      for (int q = lane; q < npairs; q += 32) {
+        H[pk(ii, jj)] = norm_df<D>(&V[ii * D], &V[jj * D]);
+        jj += 32;
+        while (jj >= ii && ii < s) {
+          jj -= ii;
+          ++ii;
+        }
+      }
+      __syncwarp();
+    }
+    for (int c = 0; c < a.ncand; ++c) {
+      const DevModel& mdl = a.models[c];
+      const Frames fr = frames_of(mdl);
+      if (a.iso_shared) {
+        for (int q = lane; q < s; q += 32) {
+          B[q] = cov_from_h(mdl, fr, &H0[q], tab, kc);
+          A[pk(q, q)] = mdl.c0_df;
+        }
+        int ii = 1, jj = lane;
+        while (jj >= ii && ii < s) {
+          jj -= ii;
+          ++ii;
+        }
+        for (int q = lane; q < npairs; q += 32) {
+          A[pk(ii, jj)] = cov_from_h(mdl, fr, &H[pk(ii, jj)], tab, kc);
+          jj += 32;
+          while (jj >= ii && ii < s) {
+            jj -= ii;
+            ++ii;
+          }
+        }
+      } else {
+        df* VF = V + M * D;  // frames 1.. (frame 0 is V itself)
+        for (int q = lane; q < s; q += 32) {
+          df hq[GS_MAX_STRUCTURES + 1];
+          hq[0] = norm0_df<D>(&V[q * D]);
+          for (int st = 0; st < mdl.ns; ++st) {
+            if (!mdl.s[st].aniso) continue;
+            const int f = fr.fid[st];
+            df acc3[3];
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+              df acc = df_make(0.0f, 0.0f);
+#pragma unroll
+              for (int cc = 0; cc < D; ++cc) acc = df_add(acc, df_mul(mdl.s[st].rot_df[r * 3 + cc], V[q * D + cc]));
+              acc3[r] = acc;
+              VF[((f - 1) * M + q) * D + r] = acc;
+            }
+            hq[f] = norm0_df<D>(acc3);
+          }
+          B[q] = cov_from_h(mdl, fr, hq, tab, kc);
+          A[pk(q, q)] = mdl.c0_df;
+        }
+        __syncwarp();
+        int ii = 1, jj = lane;
+        while (jj >= ii && ii < s) {
+          jj -= ii;
+          ++ii;
+        }
+        for (int q = lane; q < npairs; q += 32) {
+          df h[GS_MAX_STRUCTURES + 1];
+          h[0] = norm_df<D>(&V[ii * D], &V[jj * D]);
+          for (int f = 1; f < fr.nf; ++f)
+            h[f] = norm_df<D>(&VF[((f - 1) * M + ii) * D], &VF[((f - 1) * M + jj) * D]);
+          A[pk(ii, jj)] = cov_from_h(mdl, fr, h, tab, kc);
+          jj += 32;
+          while (jj >= ii && ii < s) {
+            jj -= ii;
+            ++ii;
+          }
+        }
+      }
+      __syncwarp();
+      const bool ok = ldl_refine_solve(A, B, L, DI, W, X, XD, s, lane);
+      if (!ok) {
+        if (lane == 0) a.flag[(int64_t)c * a.n + k] = 1;
+        __syncwarp();
+        continue;
+      }
+      double mu = 0.0, red = 0.0;
+      for (int q = lane; q < s; q += 32) {
+        mu += X[q] * Z[q];
+        red += X[q] * df_to_double(B[q]);
+      }
+      mu = warp_sum_d(mu);
+      red = warp_sum_d(red);
+      if (lane == 0) {
+        const double var = fmax(mdl.c0 - red, 1e-12);
+        const double r = zi - mu;
+        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+        a.flag[(int64_t)c * a.n + k] = 0;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// FP64 per-(candidate, point) solve: cholesky_solve_in_place
+// (linalg.rs:123-203) on the assembled K_SS of vecchia.rs:302-320.
+template <int D>
+__global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist, double* scratch,
+                                    int64_t T, int32_t* cand_status) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tid >= T) return;
+  const int M = a.m;
+  double* S = scratch + tid;
+  double* W = scratch + (int64_t)M * M * T + tid;
+  double* K0 = W + (int64_t)M * T;
+  for (int64_t it = tid; it < nlist; it += T) {
+    const int64_t code = list ? list[it] : it;
+    const int c = (int)(code / a.n);
+    const int64_t k = code % a.n;
+    const DevModel& mdl = a.models[c];
+    const int64_t i = a.order[k];
+    const int s = a.cnt[k];
+    const double zi = a.v[i] - a.mean;
+    const double sill = mdl.c0;
+    if (s == 0) {
+      a.terms[code] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
+      continue;
+    }
+    const int32_t* nbk = a.nb + k * (int64_t)M;
+    double pi[3] = {a.x[i], a.y[i], D == 3 ? a.z[i] : 0.0};
+    for (int aa = 0; aa < s; ++aa) {
+      const int ja = nbk[aa];
+      double h[3] = {pi[0] - a.x[ja], pi[1] - a.y[ja], D == 3 ? pi[2] - a.z[ja] : 0.0};
+      const double kv = cov_fp64<D>(mdl, h);
+      W[(int64_t)aa * T] = kv;
+      K0[(int64_t)aa * T] = kv;
+      for (int bb = aa; bb < s; ++bb) {
+        const int jb = nbk[bb];
+        double g[3] = {a.x[ja] - a.x[jb], a.y[ja] - a.y[jb], D == 3 ? a.z[ja] - a.z[jb] : 0.0};
+        const double cv = cov_fp64<D>(mdl, g);
+        S[(int64_t)(aa * s + bb) * T] = cv;
+        S[(int64_t)(bb * s + aa) * T] = cv;
+      }
+    }
+    double scale = 0.0;
+    for (int q = 0; q < s; ++q) scale = fmax(scale, S[(int64_t)(q * s + q) * T]);
+    scale = fmax(scale, 2.2250738585072014e-308);
+    bool fail_ = false;
+    for (int kk = 0; kk < s && !fail_; ++kk) {
+      double d = S[(int64_t)(kk * s + kk) * T];
+      for (int j = 0; j < kk; ++j) d -= S[(int64_t)(kk * s + j) * T] * S[(int64_t)(kk * s + j) * T];
+      if (!(d > 1e-12 * scale)) {
+        fail_ = true;
+        break;
+      }
+      d = sqrt(d);
+      S[(int64_t)(kk * s + kk) * T] = d;
+      for (int r = kk + 1; r < s; ++r) {
+        double acc = S[(int64_t)(r * s + kk) * T];
+        for (int j = 0; j < kk; ++j) acc -= S[(int64_t)(r * s + j) * T] * S[(int64_t)(kk * s + j) * T];
+        S[(int64_t)(r * s + kk) * T] = acc / d;
+      }
+    }
+    if (fail_) {
+      atomicExch(&cand_status[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
+      a.terms[code] = __longlong_as_double(0x7ff8000000000000ll);
+      continue;
+    }
+    for (int r = 0; r < s; ++r) {
+      double acc = W[(int64_t)r * T];
+      for (int j = 0; j < r; ++j) acc -= S[(int64_t)(r * s + j) * T] * W[(int64_t)j * T];
+      W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
+    }
+    for (int r = s - 1; r >= 0; --r) {
+      double acc = W[(int64_t)r * T];
+      for (int j = r + 1; j < s; ++j) acc -= S[(int64_t)(j * s + r) * T] * W[(int64_t)j * T];
+      W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
+    }
+    double mu = 0.0, red = 0.0;
+    for (int q = 0; q < s; ++q) mu += W[(int64_t)q * T] * (a.v[nbk[q]] - a.mean);
+    for (int q = 0; q < s; ++q) red += W[(int64_t)q * T] * K0[(int64_t)q * T];
+    const double var = fmax(sill - red, 1e-12);
+    const double r = zi - mu;
+    a.terms[code] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+  }
+}
+
+// Fixed-order reduction: block b sums terms [b*chunk, (b+1)*chunk) of one
+// candidate in a fixed tree; the partials are added in block order.
+__global__ void reduce_terms(const double* terms, int64_t n, int64_t chunk, double* partial) {
+  __shared__ double sh[256];
+  const int c = blockIdx.y;
+  const int64_t lo = blockIdx.x * chunk;
+  const int64_t hi = min(n, lo + chunk);
+  double acc = 0.0;
+  for (int64_t q = lo + threadIdx.x; q < hi; q += blockDim.x) acc += terms[(int64_t)c * n + q];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(int64_t)c * gridDim.x + blockIdx.x] = sh[0];
+}
+
+__global__ void reduce_partials(const double* partial, int nblk, int ncand, double* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncand) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += partial[(int64_t)c * nblk + b];
+  out[c] = s;
+}
+
+ExpTable g_vtab;
+DfConsts g_vkc;
+bool g_vready = false;
+
+int reject_vecchia_model(const gs_model& m, int dim) {
+  GS_TRY(validate_model(m));
+  if (has_power(m))
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "Vecchia needs a valid covariance function and cannot use the unbounded Power model");
+  for (int k = 0; k < m.n_structures; ++k)
+    if (m.s[k].kind == GS_KIND_CIRCULAR && dim > 2)
+      return fail(GS_ERR_INVALID_PARAMETER, "Circular is not a valid covariance in 3 dimensions");
+  return GS_OK;
+}
+
+}  // namespace
+
+// Evaluates ncand candidates on a plan; ll[c] and status[c] per candidate.
+int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
+                 int32_t* status, int precision, cudaStream_t s) {
+  const gs_pointset* ps = P->ps;
+  const int dim = ps->dim;
+  const int64_t n = P->n;
+  const int M = (int)P->m;
+  if (!g_vready) {
+    df_consts_host(&g_vtab, &g_vkc);
+    g_vready = true;
+  }
+  std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
+  std::vector<int> valid(ncand, 0);
+  bool all_iso = true;
+  for (int64_t c = 0; c < ncand; ++c) {
+    status[c] = GS_OK;
+    ll[c] = NAN;
+    int rc = reject_vecchia_model(models[c], dim);
+    if (!rc) rc = make_dev_model(models[c], dim, &dms[c], true);
+    if (rc) {
+      status[c] = rc;
+      dms[c] = DevModel{};
+      dms[c].ns = 0;
+      dms[c].c0 = 1.0;
+      dms[c].c0_df = df_from_double(1.0);
+      continue;
+    }
+    valid[c] = 1;
+    for (int k = 0; k < models[c].n_structures; ++k)
+      if (models[c].s[k].has_anis) all_iso = false;
+  }
+  if (ncand == 0) return GS_OK;
+  DevBuf dmod, terms, flag, partial, out, cstat;
+  GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
+  GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
+  GS_TRY(terms.alloc((size_t)ncand * n * 8, s));
+  GS_TRY(flag.alloc((size_t)ncand * n, s));
+  GS_TRY(cstat.alloc((size_t)ncand * 4, s));
+  GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
+  VArgs a{};
+  a.dim = dim;
+  a.n = n;
+  a.m = M;
+  a.ncand = (int)ncand;
+  a.iso_shared = all_iso ? 1 : 0;
+  a.x = ps->d_x;
+  a.y = ps->d_y;
+  a.z = ps->d_z;
+  a.v = ps->d_v;
+  a.mean = P->mean;
+  a.order = P->d_order;
+  a.nb = P->d_nb;
+  a.cnt = P->d_cnt;
+  a.models = (const DevModel*)dmod.ptr;
+  a.terms = (double*)terms.ptr;
+  a.flag = (uint8_t*)flag.ptr;
+  int64_t nfl = 0;
+  DevBuf list;
+  const bool mixed = precision != GS_PREC_FP64 && M <= GS_MIXED_MAX_NEIGHBORS;
+  if (mixed) {
+    const size_t per_warp = vecchia_per_warp_bytes(std::max(M, 1), dim);
+    int wpb = 4;
+    while (wpb > 1 && per_warp * wpb > 200 * 1024) --wpb;
+    const size_t smem = per_warp * wpb;
+    auto kern = dim == 2 ? vecchia_loglik_kernel<2> : vecchia_loglik_kernel<3>;
+    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int blocks = (int)std::min<int64_t>((n + wpb - 1) / wpb, 152 * 64);
+    kern<<<blocks, wpb * 32, smem, s>>>(a, g_vtab, g_vkc, per_warp);
+    GS_CUDA(cudaGetLastError());
+    // compact flagged (candidate, point) pairs
+    DevBuf nsel, tmp;
+    GS_TRY(nsel.alloc(8, s));
+    GS_TRY(list.alloc((size_t)ncand * n * 8, s));
+    size_t tb = 0;
+    GS_CUDA(cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<int64_t>(0),
+                                       (uint8_t*)flag.ptr, (int64_t*)list.ptr, (int64_t*)nsel.ptr,
+                                       (int64_t)(ncand * n), s));
+    GS_TRY(tmp.alloc(tb, s));
+    GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, tb, thrust::counting_iterator<int64_t>(0),
+                                       (uint8_t*)flag.ptr, (int64_t*)list.ptr, (int64_t*)nsel.ptr,
+                                       (int64_t)(ncand * n), s));
+    GS_CUDA(cudaMemcpyAsync(&nfl, nsel.ptr, 8, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaStreamSynchronize(s));
+  }
+  if (!mixed || nfl > 0) {
+    const int64_t work = mixed ? nfl : ncand * n;
+    const int64_t per = ((int64_t)M * M + 2 * (int64_t)M) * 8;
+    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 1024);
+    T = std::min<int64_t>(T, ((work + 127) / 128) * 128);
+    T = std::max<int64_t>(T, 128);
+    DevBuf scratch;
+    GS_TRY(scratch.alloc((size_t)T * per, s));
+    const int blocks = (int)((T + 127) / 128);
+    if (dim == 2)
+      vecchia_fp64_kernel<2><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
+                                                    work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
+    else
+      vecchia_fp64_kernel<3><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
+                                                    work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
+    GS_CUDA(cudaGetLastError());
+  }
+  const int64_t chunk = 8192;
+  const int nblk = (int)((n + chunk - 1) / chunk);
+  GS_TRY(partial.alloc((size_t)nblk * ncand * 8, s));
+  GS_TRY(out.alloc((size_t)ncand * 8, s));
+  reduce_terms<<<dim3(nblk, (unsigned)ncand), 256, 0, s>>>((double*)terms.ptr, n, chunk, (double*)partial.ptr);
+  reduce_partials<<<(int)((ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)ncand, (double*)out.ptr);
+  GS_CUDA(cudaGetLastError());
+  std::vector<double> hll(ncand);
+  std::vector<int32_t> hst(ncand);
+  GS_CUDA(cudaMemcpyAsync(hll.data(), out.ptr, ncand * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hst.data(), cstat.ptr, ncand * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  for (int64_t c = 0; c < ncand; ++c) {
+    if (!valid[c]) continue;
+    if (hst[c] != 0) {
+      status[c] = hst[c];
+      ll[c] = NAN;
+    } else {
+      ll[c] = hll[c];
+    }
+  }
+  return GS_OK;
+}
+
+// vecchia_plan (vecchia.rs:232-282).
+int plan_create(const gs_pointset* ps, int64_t m, const int64_t* order, gs_vecchia_plan** out) {
+  *out = nullptr;
+  const int64_t n = ps->n;
+  const int dim = ps->dim;
+  if (n < 2) return fail(GS_ERR_INSUFFICIENT_DATA, "Vecchia requires at least 2 points");
+  if (m <= 0) return fail(GS_ERR_INVALID_PARAMETER, "conditioning size m must be at least 1");
+  if (ps->has_dup)
+    return fail(GS_ERR_DUPLICATE_POINTS, "duplicate data points: indices " + std::to_string(ps->dup_i) +
+                                             " and " + std::to_string(ps->dup_j) +
+                                             " share the same coordinates");
+  auto* P = new gs_vecchia_plan();
+  P->ps = ps;
+  P->n = n;
+  P->m = std::min<int64_t>(m, n - 1);
+  P->order.resize(n);
+  if (order) {
+    std::vector<char> seen(n, 0);
+    for (int64_t k = 0; k < n; ++k) {
+      if (order[k] < 0 || order[k] >= n || seen[order[k]]) {
+        delete P;
+        return fail(GS_ERR_INVALID_PARAMETER, "order must be a permutation of 0..n-1");
+      }
+      seen[order[k]] = 1;
+      P->order[k] = order[k];
+    }
+  } else {
+    maxmin_order(ps->host, dim, n, P->order.data());
+  }
+  double sum = 0.0;
+  for (int64_t i = 0; i < n; ++i) sum += ps->values[i];
+  P->mean = sum / (double)n;
+  int rc = cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) == cudaSuccess
+               ? GS_OK
+               : fail(GS_ERR_CUDA, "stream creation failed");
+  cudaStream_t s = P->stream;
+  const int M = (int)P->m;
+  if (!rc && (cudaMalloc(&P->d_order, n * 8) != cudaSuccess ||
+              cudaMalloc(&P->d_nb, (size_t)n * M * 4) != cudaSuccess ||
+              cudaMalloc(&P->d_cnt, n * 4) != cudaSuccess))
+    rc = fail(GS_ERR_OUT_OF_MEMORY, "plan allocation failed");
+  if (!rc) {
+    DevBuf ox, oy, oz;
+    rc = ox.alloc(n * 8, s);
+    if (!rc) rc = oy.alloc(n * 8, s);
+    if (!rc && dim == 3) rc = oz.alloc(n * 8, s);
+    if (!rc) {
+      cudaMemcpyAsync(P->d_order, P->order.data(), n * 8, cudaMemcpyHostToDevice, s);
+      const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
+      gather_by_order<<<blocks, 256, 0, s>>>(n, P->d_order, ps->d_x, ps->d_y, ps->d_z,
+                                            (double*)ox.ptr, (double*)oy.ptr,
+                                            dim == 3 ? (double*)oz.ptr : nullptr);
+      Grid g;
+      rc = grid_build_ranked(&g, dim, n, (double*)ox.ptr, (double*)oy.ptr, (double*)oz.ptr,
+                             dim == 2 ? 2.0 : 3.0, s);
+      if (!rc) {
+        SearchFrame f;
+        std::memset(&f, 0, sizeof(f));
+        SearchParams sp{};
+        sp.k = M;
+        sp.kout = M;
+        sp.ranked = 1;
+        sp.rank0 = 0;
+        sp.brute_below = 2048;
+        sp.px = (double*)ox.ptr;
+        sp.py = (double*)oy.ptr;
+        sp.pz = (double*)oz.ptr;
+        rc = search_launch(g, f, sp, n, (double*)ox.ptr, (double*)oy.ptr, (double*)oz.ptr, P->d_nb,
+                           P->d_cnt, s);
+      }
+      if (!rc) {
+        positions_to_ids<<<(int)std::min<int64_t>((n * M + 255) / 256, 152 * 64), 256, 0, s>>>(
+            n * M, P->d_order, P->d_nb);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+          rc = fail(GS_ERR_CUDA, "plan kernels failed");
+      }
+    }
+  }
+  if (rc) {
+    delete P;
+    return rc;
+  }
+  *out = P;
+  return GS_OK;
+}
+
+}  // namespace gs
+
+using namespace gs;
+
+extern "C" {
+
+int gs_maxmin_order(int dim, int64_t n, const double* x, const double* y, const double* z,
+                    int64_t* order) {
+  if (dim != 2 && dim != 3) return fail(GS_ERR_DIMENSION_MISMATCH, "dim must be 2 or 3");
+  std::vector<double> pts(n * dim);
+  for (int64_t i = 0; i < n; ++i) {
+    pts[i * dim] = x[i];
+    pts[i * dim + 1] = y[i];
+    if (dim == 3) pts[i * dim + 2] = z[i];
+  }
+  maxmin_order(pts, dim, n, order);
+  return GS_OK;
+}
+
+int gs_vecchia_plan_create(const gs_pointset* ps, int64_t m, const int64_t* order,
+                           gs_vecchia_plan** out) {
+  if (!ps) return fail(GS_ERR_INVALID_PARAMETER, "null point set");
+  return plan_create(ps, m, order, out);
+}
+
+int gs_vecchia_plan_get(const gs_vecchia_plan* P, int64_t* order, int64_t* neighbours,
+                        int32_t* count) {
+  const int64_t n = P->n;
+  const int M = (int)P->m;
+  std::vector<int32_t> nb((size_t)n * M), cnt(n);
+  GS_CUDA(cudaMemcpy(nb.data(), P->d_nb, (size_t)n * M * 4, cudaMemcpyDeviceToHost));
+  GS_CUDA(cudaMemcpy(cnt.data(), P->d_cnt, n * 4, cudaMemcpyDeviceToHost));
+  for (int64_t k = 0; k < n; ++k) {
+    if (order) order[k] = P->order[k];
+    if (count) count[k] = cnt[k];
+    if (neighbours)
+      for (int a = 0; a < M; ++a) neighbours[k * M + a] = a < cnt[k] ? nb[k * M + a] : -1;
+  }
+  return GS_OK;
+}
+
+void gs_vecchia_plan_destroy(gs_vecchia_plan* P) { delete P; }
+
+int gs_vecchia_loglik_batch(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
+                            double* loglik, int32_t* status, int precision, void* stream) {
+  if (!P) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
+  cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
+  return vecchia_eval(P, ncand, models, loglik, status, precision, s);
+}
+
+// vecchia_loglik (vecchia.rs:874-884).
+int gs_vecchia_loglik(const gs_pointset* ps, const gs_model* model, int64_t m,
+                      const int64_t* order, double* loglik) {
+  if (!ps) return fail(GS_ERR_INVALID_PARAMETER, "null point set");
+  GS_TRY(reject_vecchia_model(*model, ps->dim));
+  gs_vecchia_plan* P = nullptr;
+  GS_TRY(plan_create(ps, m, order, &P));
+  int32_t st = 0;
+  int rc = vecchia_eval(P, 1, model, loglik, &st, GS_PREC_MIXED, P->stream);
+  delete P;
+  if (rc) return rc;
+  if (st) return fail(st, "singular conditioning system");
+  return GS_OK;
+}
+
+// mle_fit_with_plan (vecchia.rs:952-1081) with every start's simplex
+// advanced in lock step so each round's evaluations form one batch.
+int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                   int64_t nstarts, const double* starts, double step, int64_t max_iter,
+                   gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals) {
+  if (!ps) return fail(GS_ERR_INVALID_PARAMETER, "null point set");
+  if (kind == GS_KIND_POWER)
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "Vecchia needs a valid covariance function and cannot use the unbounded Power model");
+  if (kind == GS_KIND_CIRCULAR && ps->dim > 2)
+    return fail(GS_ERR_INVALID_PARAMETER, "Circular is not a valid covariance in 3 dimensions");
+  if (kind < 0 || kind > GS_KIND_MATERN25)
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "the CUDA path fits spherical, exponential, gaussian, matern15 and matern25");
+  gs_vecchia_plan* P = nullptr;
+  GS_TRY(plan_create(ps, m, order, &P));
+  const int64_t n = ps->n;
+  const int dim = ps->dim;
+  // initial scales (vecchia.rs:958-980)
+  double mean = P->mean;
+  double sq = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    double t = ps->values[i] - mean;
+    sq += t * t;
+  }
+  double var0 = std::fmax(sq / (double)n, 1e-12);
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < dim; ++d) {
+      lo[d] = std::fmin(lo[d], ps->host[i * dim + d]);
+      hi[d] = std::fmax(hi[d], ps->host[i * dim + d]);
+    }
+  double e2 = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    double t = hi[d] - lo[d];
+    e2 += t * t;
+  }
+  const double extent = std::sqrt(e2);
+  const double range0 = std::fmax(extent / 3.0, 1e-9);
+  const double range_max = 10.0 * extent;
+  std::vector<std::vector<double>> st;
+  if (starts) {
+    for (int64_t q = 0; q < nstarts; ++q) st.push_back({starts[q * 3], starts[q * 3 + 1], starts[q * 3 + 2]});
+  } else {
+    const double lr0 = std::log(range0);
+    if (nstarts <= 3) {
+      for (double f : {0.3, 1.0, 3.0}) st.push_back({std::sqrt(0.1 * var0), std::log(0.9 * var0), lr0 + std::log(f)});
+    } else {
+      // a deterministic spread over range and nugget share
+      for (int64_t q = 0; q < nstarts; ++q) {
+        const double fr = std::pow(10.0, -1.0 + 2.0 * (double)(q % 4) / 3.0);
+        const double nugf = 0.05 + 0.15 * (double)((q / 4) % 4);
+        st.push_back({std::sqrt(nugf * var0), std::log((1.0 - nugf) * var0), lr0 + std::log(fr)});
+      }
+    }
+  }
+  if (st.empty()) {
+    delete P;
+    return fail(GS_ERR_INVALID_PARAMETER, "at least one start is required");
+  }
+  std::vector<NelderMead> runs;
+  for (auto& x0 : st) runs.emplace_back(x0, step, max_iter);
+  int64_t evals = 0;
+  int rc = GS_OK;
+  for (int guard = 0; guard < 1000000 && !rc; ++guard) {
+    std::vector<gs_model> batch;
+    std::vector<std::pair<size_t, size_t>> owner;
+    std::vector<double> regs;
+    for (size_t r = 0; r < runs.size(); ++r) {
+      if (runs[r].done()) continue;
+      const auto& pend = runs[r].pending();
+      for (size_t q = 0; q < pend.size(); ++q) {
+        const auto& x = pend[q];
+        gs_model mdl;
+        std::memset(&mdl, 0, sizeof(mdl));
+        mdl.nugget = x[0] * x[0];
+        mdl.n_structures = 1;
+        mdl.s[0].kind = kind;
+        mdl.s[0].sill = std::exp(x[1]);
+        mdl.s[0].range = std::exp(x[2]);
+        mdl.s[0].ratio = mdl.s[0].ratio_z = 1.0;
+        const double range = mdl.s[0].range;
+        double reg = 0.0;
+        if (range > range_max) {
+          double t = (range - range_max) / range_max;
+          reg = t * t;
+        }
+        batch.push_back(mdl);
+        owner.push_back({r, q});
+        regs.push_back(reg);
+      }
+    }
+    if (batch.empty()) break;
+    std::vector<double> ll(batch.size());
+    std::vector<int32_t> sts(batch.size());
+    rc = vecchia_eval(P, (int64_t)batch.size(), batch.data(), ll.data(), sts.data(), GS_PREC_MIXED, P->stream);
+    if (rc) break;
+    evals += (int64_t)batch.size();
+    std::vector<std::vector<double>> fvals(runs.size());
+    for (size_t b = 0; b < batch.size(); ++b) {
+      double f = (sts[b] == 0 && std::isfinite(ll[b])) ? -ll[b] + 1e6 * regs[b] : 1e12;
+      fvals[owner[b].first].push_back(f);
+    }
+    for (size_t r = 0; r < runs.size(); ++r)
+      if (!fvals[r].empty()) runs[r].supply(fvals[r]);
+  }
+  delete P;
+  if (rc) return rc;
+  auto best = multistart_best(runs);
+  if (n_evals) *n_evals = evals;
+  if (best.second >= 1e12)
+    return fail(GS_ERR_SINGULAR_SYSTEM,
+                "Vecchia MLE did not converge to a feasible fit: every starting point stayed on a "
+                "singular/degenerate covariance");
+  const auto& xb = best.first;
+  if (out_x)
+    for (int i = 0; i < 3; ++i) out_x[i] = xb[i];
+  if (out_model) {
+    std::memset(out_model, 0, sizeof(*out_model));
+    out_model->nugget = xb[0] * xb[0];
+    out_model->n_structures = 1;
+    out_model->s[0].kind = kind;
+    out_model->s[0].sill = std::exp(xb[1]);
+    out_model->s[0].range = std::exp(xb[2]);
+    out_model->s[0].ratio = out_model->s[0].ratio_z = 1.0;
+    GS_TRY(validate_model(*out_model));
+  }
+  if (out_loglik) *out_loglik = -best.second;
+  return GS_OK;
+}
+
+int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t nstarts,
+                              const double* starts, double step, int64_t max_iter, double* x_out,
+                              double* f_out) {
+  if (nstarts <= 0) return fail(GS_ERR_INVALID_PARAMETER, "starts must be non-empty");
+  std::vector<NelderMead> runs;
+  for (int64_t q = 0; q < nstarts; ++q)
+    runs.emplace_back(std::vector<double>(starts + q * n, starts + (q + 1) * n), step, max_iter);
+  for (;;) {
+    bool any = false;
+    for (auto& r : runs) {
+      if (r.done()) continue;
+      any = true;
+      std::vector<double> fv;
+      for (const auto& x : r.pending()) fv.push_back(f(x.data(), n, ctx));
+      r.supply(fv);
+    }
+    if (!any) break;
+  }
+  auto best = multistart_best(runs);
+  for (int64_t i = 0; i < n; ++i) x_out[i] = best.first[i];
+  *f_out = best.second;
+  return GS_OK;
+}
+
+}  // extern "C"
+
+extern "C" int gs_vecchia_predict(const gs_pointset* ps, const gs_model* model, int64_t nt,
+                                  const double* tx, const double* ty, const double* tz, int64_t m,
+                                  double* value, double* variance) {
+  (void)ps; (void)model; (void)nt; (void)tx; (void)ty; (void)tz; (void)m; (void)value; (void)variance;
+  return gs::fail(GS_ERR_INVALID_PARAMETER, "vecchia_predict is not available yet");
+}

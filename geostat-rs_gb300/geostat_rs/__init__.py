@@ -1,4 +1,19 @@
-"""geostat_rs -- GB300-native kriging and Vecchia likelihood (placeholder, filled below)."""
-from .errors import (GeostatError, InsufficientData, DimensionMismatch, SingularSystem,
-                     InvalidParameter, NoNeighbors, DuplicatePoints)
-from .model import Anisotropy, Structure, VariogramModel
+"""geostat_rs -- GB300-native moving-neighbourhood kriging and Vecchia likelihood.
+
+A drop-in for geostat-rs's hot path: the same model format, kriging
+configuration and entry points (``krige``, ``krige_grid``, ``krige_3d``,
+``vecchia_loglik``, ``vecchia_mle``, ``vecchia_krige`` and the
+``PointSet``/``Kriging`` core API), computed by hand-written sm_103a kernels in
+libgeostat_gb300.so through its C ABI.
+"""
+from .errors import (CudaError, DimensionMismatch, DuplicatePoints, GeostatError,
+                     InsufficientData, InvalidParameter, NoNeighbors, OutOfDeviceMemory,
+                     SingularSystem)
+from .model import Anisotropy, Structure, VariogramModel, parse_kind
+from .api import (Kriging, KrigingConfig, KrigingResult, PointSet, VecchiaPlan, krige,
+                  krige_3d, krige_grid, last_timings, maxmin_order, nelder_mead_multistart,
+                  rff_field, rng_normal, rng_uniform, seq_mean, vecchia_krige, vecchia_loglik,
+                  vecchia_mle, vecchia_mle_fit)
+from ._abi import LIB_PATH, load as load_library
+
+__all__ = [n for n in dir() if not n.startswith("_")]

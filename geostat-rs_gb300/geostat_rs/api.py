@@ -1,0 +1,523 @@
+"""Host-side mirror of geostat-rs's kriging / Vecchia interface over the C ABI.
+
+Two layers:
+
+* ``PointSet`` / ``KrigingConfig`` / ``Kriging`` follow the core Rust API
+  (crates/geostat-core/src/data.rs, kriging.rs): ``Kriging.new``,
+  ``with_external_drift``, ``with_measurement_error``, ``predict_many``,
+  ``predict_many_with_drift``, ``predict_grid``.
+* ``krige``, ``krige_grid``, ``krige_3d``, ``vecchia_loglik``,
+  ``vecchia_mle``, ``vecchia_krige`` follow the reference's Python binding
+  (crates/geostat-python/src/lib.rs) argument for argument, returning the same
+  ``(predictions, variances)`` numpy pairs and raising ``ValueError``
+  subclasses for ``GeostatError``s.
+
+Every computation runs in libgeostat_gb300.so on the GPU; nothing here
+computes estimates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _abi
+from .errors import DimensionMismatch, InvalidParameter
+from .model import KIND_CODES, Anisotropy, Structure, VariogramModel
+
+PRECISIONS = {"mixed": _abi.PREC_MIXED, "fp64": _abi.PREC_FP64}
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _p(a, ct=C.c_double):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+def seq_mean(values) -> float:
+    """Left-to-right mean, as PointSet::mean (data.rs:344-346) sums."""
+    v = _f64(values)
+    return float(np.add.accumulate(v)[-1] / len(v))
+
+
+def model_struct(model: VariogramModel) -> _abi.Model:
+    m = _abi.Model()
+    m.nugget = float(model.nugget)
+    m.n_structures = len(model.structures)
+    for i, s in enumerate(model.structures):
+        m.s[i].kind = KIND_CODES[s.kind]
+        m.s[i].param = float(s.param)
+        m.s[i].sill = float(s.sill)
+        m.s[i].range = float(s.range)
+        if s.anis is not None:
+            m.s[i].has_anis = 1
+            m.s[i].azimuth_deg = s.anis.azimuth_deg
+            m.s[i].ratio = s.anis.ratio
+            m.s[i].ratio_z = s.anis.ratio_z
+            m.s[i].dip_deg = s.anis.dip_deg
+            m.s[i].rake_deg = s.anis.rake_deg
+        else:
+            m.s[i].ratio = m.s[i].ratio_z = 1.0
+    return m
+
+
+class PointSet:
+    """Device-resident ``PointSet<D>`` (data.rs:8-83)."""
+
+    def __init__(self, coords, values):
+        coords = _f64(coords)
+        if coords.ndim != 2 or coords.shape[1] not in (2, 3):
+            raise DimensionMismatch("coords must be an (n, 2) or (n, 3) array")
+        values = _f64(values)
+        if len(values) != len(coords):
+            raise DimensionMismatch(f"{len(coords)} coordinates vs {len(values)} values")
+        self.dim = coords.shape[1]
+        self.n = len(coords)
+        self.coords = coords
+        self.values = values
+        lib = _abi.load()
+        x = _f64(coords[:, 0])
+        y = _f64(coords[:, 1])
+        z = _f64(coords[:, 2]) if self.dim == 3 else None
+        h = C.c_void_p()
+        _abi.check(lib.gs_pointset_create(self.dim, self.n, _p(x), _p(y), _p(z), _p(values),
+                                          C.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_xyz(cls, x, y, values):
+        x, y = _f64(x), _f64(y)
+        if not (len(x) == len(y) == len(values)):
+            raise DimensionMismatch(f"x: {len(x)}, y: {len(y)}, z: {len(values)}")
+        return cls(np.stack([x, y], axis=1), values)
+
+    @classmethod
+    def from_xyzv(cls, x, y, z, values):
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        if not (len(x) == len(y) == len(z) == len(values)):
+            raise DimensionMismatch(
+                f"x: {len(x)}, y: {len(y)}, z: {len(z)}, values: {len(values)}")
+        return cls(np.stack([x, y, z], axis=1), values)
+
+    def mean(self) -> float:
+        return seq_mean(self.values)
+
+    def duplicate_pair(self):
+        i, j = C.c_int64(), C.c_int64()
+        if _abi.load().gs_pointset_duplicate_pair(self._h, C.byref(i), C.byref(j)):
+            return (i.value, j.value)
+        return None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().gs_pointset_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class KrigingConfig:
+    """``KrigingConfig`` (kriging.rs:73-115).  ``method`` is one of
+    "simple", "ordinary", "universal", "external_drift"."""
+    method: str = "ordinary"
+    mean: Optional[float] = None      # simple kriging's known mean
+    degree: int = 1                   # universal kriging drift degree
+    n_vars: int = 0                   # external-drift covariates
+    max_neighbors: Optional[int] = None
+    search_radius: Optional[float] = None
+    min_neighbors: Optional[int] = None
+    max_per_octant: Optional[int] = None
+    anisotropic_search: Optional[Anisotropy] = None
+
+    def to_struct(self) -> _abi.Kcfg:
+        if self.method not in _abi.METHODS:
+            raise InvalidParameter(f"unknown kriging method '{self.method}'")
+        c = _abi.Kcfg()
+        c.method = _abi.METHODS[self.method]
+        c.sk_mean = float(self.mean) if self.mean is not None else 0.0
+        c.uk_degree = int(self.degree)
+        c.ked_nvars = int(self.n_vars)
+        c.max_neighbors = -1 if self.max_neighbors is None else int(self.max_neighbors)
+        c.min_neighbors = -1 if self.min_neighbors is None else int(self.min_neighbors)
+        c.max_per_octant = -1 if self.max_per_octant is None else int(self.max_per_octant)
+        c.has_search_radius = 0 if self.search_radius is None else 1
+        c.search_radius = float(self.search_radius) if self.search_radius is not None else 0.0
+        a = self.anisotropic_search
+        if a is not None:
+            c.has_anisotropic_search = 1
+            c.search_azimuth_deg = a.azimuth_deg
+            c.search_ratio = a.ratio
+            c.search_ratio_z = a.ratio_z
+            c.search_dip_deg = a.dip_deg
+            c.search_rake_deg = a.rake_deg
+        return c
+
+
+@dataclass
+class KrigingResult:
+    value: np.ndarray
+    variance: np.ndarray
+    lagrange: np.ndarray
+    status: np.ndarray
+
+
+class Kriging:
+    """``Kriging<'_, D>`` over a device-resident ``PointSet`` (kriging.rs:138-408)."""
+
+    def __init__(self, data: PointSet, model: VariogramModel, config: KrigingConfig, _ctor=0,
+                 _aux=None):
+        self.data = data
+        self.model = model
+        self.config = config
+        lib = _abi.load()
+        m = model_struct(model)
+        cfg = config.to_struct()
+        h = C.c_void_p()
+        if _ctor == 0:
+            rc = lib.gs_kriging_new(data._h, C.byref(m), C.byref(cfg), C.byref(h))
+        elif _ctor == 1:
+            rc = lib.gs_kriging_with_external_drift(data._h, C.byref(m), C.byref(cfg), _p(_aux),
+                                                    C.byref(h))
+        else:
+            rc = lib.gs_kriging_with_measurement_error(data._h, C.byref(m), C.byref(cfg),
+                                                       _p(_aux), C.byref(h))
+        _abi.check(rc)
+        self._h = h
+
+    @classmethod
+    def new(cls, data, model, config=None):
+        return cls(data, model, config or KrigingConfig())
+
+    @classmethod
+    def with_external_drift(cls, data, model, config, drift_data):
+        """``drift_data[i]`` holds the covariates of data point ``i``."""
+        if config.method != "external_drift":
+            raise InvalidParameter("with_external_drift requires KrigingMethod::ExternalDrift")
+        d = _f64(drift_data).reshape(data.n, -1) if len(drift_data) == data.n else None
+        if d is None:
+            raise DimensionMismatch(f"{len(drift_data)} drift rows vs {data.n} data points")
+        if config.n_vars and d.shape[1] != config.n_vars:
+            raise DimensionMismatch(
+                f"drift rows have {d.shape[1]} values, expected {config.n_vars}")
+        return cls(data, model, config, 1, np.ascontiguousarray(d))
+
+    @classmethod
+    def with_measurement_error(cls, data, model, config, errors):
+        e = _f64(errors)
+        if len(e) != data.n:
+            raise DimensionMismatch(f"{len(e)} error variances vs {data.n} data points")
+        return cls(data, model, config, 2, e)
+
+    def _targets(self, targets):
+        t = _f64(targets)
+        if t.ndim != 2 or t.shape[1] != self.data.dim:
+            raise DimensionMismatch(f"targets must be (nt, {self.data.dim})")
+        cols = [_f64(t[:, d]) for d in range(self.data.dim)]
+        if self.data.dim == 2:
+            cols.append(None)
+        return len(t), cols
+
+    def predict_many(self, targets, precision: str = "mixed", full: bool = False,
+                     _tdrift=None):
+        """Estimates at ``targets`` (nt x D).  Returns ``(value, variance)``,
+        or a :class:`KrigingResult` with ``full=True``."""
+        nt, (x, y, z) = self._targets(targets)
+        v, var = np.empty(nt), np.empty(nt)
+        lag = np.empty(nt)
+        st = np.empty(nt, dtype=np.uint8)
+        rc = _abi.load().gs_kriging_predict_many(self._h, nt, _p(x), _p(y), _p(z), _p(_tdrift),
+                                                 _p(v), _p(var), _p(lag), _p(st, C.c_uint8),
+                                                 PRECISIONS[precision], None)
+        _abi.check(rc)
+        if full:
+            return KrigingResult(v, var, lag, st)
+        return v, var
+
+    def predict_many_with_drift(self, targets, drifts, precision: str = "mixed",
+                                full: bool = False):
+        """External-drift estimates; ``drifts[i]`` holds target ``i``'s covariates."""
+        if len(targets) != len(drifts):
+            raise DimensionMismatch(f"{len(targets)} targets vs {len(drifts)} drift rows")
+        d = _f64(drifts).reshape(len(targets), -1)
+        return self.predict_many(targets, precision, full, _tdrift=np.ascontiguousarray(d))
+
+    def predict_grid(self, bbox_min, bbox_max, ncell, precision: str = "mixed", full=False):
+        """``predict_grid`` over Grid2D/Grid3D cell centres (x fastest)."""
+        nc = np.ascontiguousarray(ncell, dtype=np.int64)
+        total = int(np.prod(nc))
+        v, var = np.empty(total), np.empty(total)
+        st = np.empty(total, dtype=np.uint8)
+        rc = _abi.load().gs_kriging_predict_grid(self._h, _p(_f64(bbox_min)), _p(_f64(bbox_max)),
+                                                 _p(nc, C.c_int64), _p(v), _p(var),
+                                                 _p(st, C.c_uint8), PRECISIONS[precision], None)
+        _abi.check(rc)
+        if full:
+            return KrigingResult(v, var, np.full(total, np.nan), st)
+        return v, var
+
+    def neighbors(self, targets, kcap: int):
+        """Conditioning indices per target (``Kriging::neighbors``), -1 padded."""
+        nt, (x, y, z) = self._targets(targets)
+        idx = np.empty(nt * kcap, dtype=np.int32)
+        cnt = np.empty(nt, dtype=np.int32)
+        _abi.check(_abi.load().gs_kriging_neighbors(self._h, nt, _p(x), _p(y), _p(z), kcap,
+                                                    _p(idx, C.c_int32), _p(cnt, C.c_int32),
+                                                    None))
+        return idx.reshape(nt, kcap), cnt
+
+    def predict_device(self, nt, x_ptr, y_ptr, z_ptr, v_ptr, var_ptr, st_ptr,
+                       precision="mixed", stream=None, tdrift_ptr=None, lag_ptr=None):
+        """Device-pointer variant (inputs/outputs already in HBM)."""
+        rc = _abi.load().gs_kriging_predict_many_device(
+            self._h, nt, x_ptr, y_ptr, z_ptr, tdrift_ptr, v_ptr, var_ptr, lag_ptr, st_ptr,
+            PRECISIONS[precision], stream)
+        _abi.check(rc)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().gs_kriging_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def last_timings():
+    """Per-phase device milliseconds of the last predict call on this thread:
+    (search, mixed solve, FP64 re-solve, whole call)."""
+    out = np.zeros(4)
+    _abi.load().gs_last_timings(_p(out))
+    return tuple(out.tolist())
+
+
+# -------------------------------------------------- reference Python API --
+def _build_method(method: str, mean, degree, data_values) -> KrigingConfig:
+    # crates/geostat-python/src/lib.rs:104-121 build_method
+    if method == "ordinary":
+        return KrigingConfig("ordinary")
+    if method == "simple":
+        return KrigingConfig("simple", mean=mean if mean is not None else seq_mean(data_values))
+    if method == "universal":
+        return KrigingConfig("universal", degree=degree)
+    raise InvalidParameter(
+        f"unknown method '{method}' (expected ordinary, simple or universal)")
+
+
+def _anisotropic_search(search_azimuth, ratio, ratio_z, dip, rake):
+    if search_azimuth is None:
+        return None
+    return Anisotropy(search_azimuth, ratio, ratio_z, dip, rake)
+
+
+def krige(x, y, values, model, target_x, target_y, method="ordinary", mean=None, degree=1,
+          max_neighbors=None, radius=None, min_neighbors=None, octant=None,
+          measurement_error=None, search_azimuth=None, search_ratio=1.0, search_ratio_z=1.0,
+          search_dip=0.0, search_rake=0.0, precision="mixed"):
+    """lib.rs:500-571 ``krige``: returns ``(predictions, variances)``."""
+    if len(target_x) != len(target_y):
+        raise InvalidParameter("target_x and target_y differ in length")
+    data = PointSet.from_xyz(x, y, values)
+    cfg = _build_method(method, mean, degree, values)
+    cfg.max_neighbors = max_neighbors
+    cfg.search_radius = radius
+    cfg.min_neighbors = min_neighbors
+    cfg.max_per_octant = octant
+    cfg.anisotropic_search = _anisotropic_search(search_azimuth, search_ratio, search_ratio_z,
+                                                 search_dip, search_rake)
+    if measurement_error is not None:
+        k = Kriging.with_measurement_error(data, model, cfg, measurement_error)
+    else:
+        k = Kriging.new(data, model, cfg)
+    t = np.stack([_f64(target_x), _f64(target_y)], axis=1)
+    return k.predict_many(t, precision)
+
+
+def krige_grid(x, y, values, model, bbox, nx, ny, method="ordinary", mean=None, degree=1,
+               max_neighbors=None, radius=None, block=None, block_discr=(4, 4),
+               min_neighbors=None, octant=None, search_azimuth=None, search_ratio=1.0,
+               search_ratio_z=1.0, search_dip=0.0, search_rake=0.0, precision="mixed"):
+    """lib.rs:632-696 ``krige_grid`` (point kriging; block kriging is not on
+    the CUDA path)."""
+    if block is not None:
+        raise InvalidParameter("block kriging is not available on the CUDA path")
+    if nx == 0 or ny == 0:
+        raise InvalidParameter("grid must have at least one cell per axis")
+    if not (bbox[2] > bbox[0]) or not (bbox[3] > bbox[1]):
+        raise InvalidParameter(f"degenerate bbox: {bbox}")
+    data = PointSet.from_xyz(x, y, values)
+    cfg = _build_method(method, mean, degree, values)
+    cfg.max_neighbors = max_neighbors
+    cfg.search_radius = radius
+    cfg.min_neighbors = min_neighbors
+    cfg.max_per_octant = octant
+    cfg.anisotropic_search = _anisotropic_search(search_azimuth, search_ratio, search_ratio_z,
+                                                 search_dip, search_rake)
+    k = Kriging.new(data, model, cfg)
+    return k.predict_grid([bbox[0], bbox[1]], [bbox[2], bbox[3]], [nx, ny], precision)
+
+
+def krige_3d(x, y, z, values, model, target_x, target_y, target_z, method="ordinary",
+             mean=None, degree=1, max_neighbors=None, radius=None, precision="mixed"):
+    """lib.rs:1650-1717 ``krige_3d``."""
+    if not (len(target_x) == len(target_y) == len(target_z)):
+        raise InvalidParameter("target_x, target_y and target_z differ in length")
+    data = PointSet.from_xyzv(x, y, z, values)
+    cfg = _build_method(method, mean, degree, values)
+    cfg.max_neighbors = max_neighbors
+    cfg.search_radius = radius
+    k = Kriging.new(data, model, cfg)
+    t = np.stack([_f64(target_x), _f64(target_y), _f64(target_z)], axis=1)
+    return k.predict_many(t, precision)
+
+
+class VecchiaPlan:
+    """``VecchiaPlan`` (vecchia.rs:223-282) with its neighbour sets on the device."""
+
+    def __init__(self, data: PointSet, m: int, order=None):
+        self.data = data
+        self.m = int(m)
+        o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+        if o is not None and len(o) != data.n:
+            raise DimensionMismatch(f"order has {len(o)} entries for {data.n} points")
+        h = C.c_void_p()
+        _abi.check(_abi.load().gs_vecchia_plan_create(data._h, self.m, _p(o, C.c_int64),
+                                                      C.byref(h)))
+        self._h = h
+        self.m_eff = min(self.m, data.n - 1)
+
+    def arrays(self):
+        n, m = self.data.n, self.m_eff
+        order = np.empty(n, dtype=np.int64)
+        nb = np.empty(n * m, dtype=np.int64)
+        cnt = np.empty(n, dtype=np.int32)
+        _abi.check(_abi.load().gs_vecchia_plan_get(self._h, _p(order, C.c_int64),
+                                                   _p(nb, C.c_int64), _p(cnt, C.c_int32)))
+        return order, nb.reshape(n, m), cnt
+
+    def loglik(self, models: Sequence[VariogramModel], precision="mixed"):
+        """Log-likelihood of each candidate model in one batched launch.
+        Returns ``(loglik, status)``."""
+        arr = (_abi.Model * len(models))(*[model_struct(m) for m in models])
+        ll = np.empty(len(models))
+        st = np.empty(len(models), dtype=np.int32)
+        _abi.check(_abi.load().gs_vecchia_loglik_batch(self._h, len(models), arr, _p(ll),
+                                                       _p(st, C.c_int32),
+                                                       PRECISIONS[precision], None))
+        return ll, st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().gs_vecchia_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def maxmin_order(coords):
+    """``maxmin_order`` (vecchia.rs:144-215), on the host."""
+    c = _f64(coords)
+    dim = c.shape[1]
+    out = np.empty(len(c), dtype=np.int64)
+    cols = [_f64(c[:, d]) for d in range(dim)] + ([None] if dim == 2 else [])
+    _abi.check(_abi.load().gs_maxmin_order(dim, len(c), _p(cols[0]), _p(cols[1]), _p(cols[2]),
+                                           _p(out, C.c_int64)))
+    return out
+
+
+def vecchia_loglik(x, y, values, model, m=20):
+    """lib.rs:478-490 ``vecchia_loglik``."""
+    data = PointSet.from_xyz(x, y, values)
+    ll = C.c_double()
+    _abi.check(_abi.load().gs_vecchia_loglik(data._h, C.byref(model_struct(model)), int(m), None,
+                                             C.byref(ll)))
+    return ll.value
+
+
+def vecchia_mle_fit(data: PointSet, kind="exponential", m=20, starts=None, nstarts=3, step=0.3,
+                    max_iter=2000, order=None):
+    """Batched multi-start Nelder-Mead fit; returns ``(model, loglik, x, n_evals)``."""
+    from .model import parse_kind
+    kname, _ = parse_kind(kind) if kind not in KIND_CODES else (kind, 0.0)
+    st = None if starts is None else _f64(starts).reshape(-1, 3)
+    ns = len(st) if st is not None else int(nstarts)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    out = _abi.Model()
+    ll = C.c_double()
+    x = np.zeros(3)
+    ne = C.c_int64()
+    _abi.check(_abi.load().gs_vecchia_mle(data._h, KIND_CODES[kname], int(m), _p(o, C.c_int64),
+                                          ns, _p(st), float(step), int(max_iter), C.byref(out),
+                                          C.byref(ll), _p(x), C.byref(ne)))
+    model = VariogramModel(out.nugget, [Structure(kname, out.s[0].sill, out.s[0].range)])
+    return model, ll.value, x, ne.value
+
+
+def vecchia_mle(x, y, values, kind="exponential", m=20):
+    """lib.rs:351-367 ``vecchia_mle`` (Nelder-Mead multistart on the GPU)."""
+    data = PointSet.from_xyz(x, y, values)
+    return vecchia_mle_fit(data, kind, m)[0]
+
+
+def vecchia_krige(x, y, values, model, target_x, target_y, m=30):
+    """lib.rs:445-476 ``vecchia_krige``: returns ``(predictions, variances)``."""
+    if len(target_x) != len(target_y):
+        raise InvalidParameter("target_x and target_y differ in length")
+    data = PointSet.from_xyz(x, y, values)
+    tx, ty = _f64(target_x), _f64(target_y)
+    nt = len(tx)
+    v, var = np.empty(nt), np.empty(nt)
+    _abi.check(_abi.load().gs_vecchia_predict(data._h, C.byref(model_struct(model)), nt, _p(tx),
+                                              _p(ty), None, int(m), _p(v), _p(var)))
+    return v, var
+
+
+def nelder_mead_multistart(fn, starts, step, max_iter):
+    """The library's Nelder-Mead state machine driven by a Python objective."""
+    starts = _f64(starts)
+    ns, n = starts.shape
+    cb = _abi.OBJECTIVE(lambda xp, nn, ctx: float(fn(np.ctypeslib.as_array(xp, shape=(nn,)).copy())))
+    x = np.zeros(n)
+    f = C.c_double()
+    _abi.check(_abi.load().gs_nelder_mead_multistart(cb, None, n, ns, _p(starts), float(step),
+                                                     int(max_iter), _p(x), C.byref(f)))
+    return x, f.value
+
+
+def rng_uniform(seed: int, count: int) -> np.ndarray:
+    out = np.empty(count)
+    _abi.load().gs_rng_uniform(seed, count, _p(out))
+    return out
+
+
+def rng_normal(seed: int, count: int) -> np.ndarray:
+    out = np.empty(count)
+    _abi.load().gs_rng_normal(seed, count, _p(out))
+    return out
+
+
+def rff_field(coords, model: VariogramModel, n_features: int, seed: int) -> np.ndarray:
+    """Seeded random-Fourier-feature Gaussian field at ``coords`` (device)."""
+    c = _f64(coords)
+    dim = c.shape[1]
+    cols = [_f64(c[:, d]) for d in range(dim)] + ([None] if dim == 2 else [])
+    out = np.empty(len(c))
+    _abi.check(_abi.load().gs_synth_rff_field(dim, len(c), _p(cols[0]), _p(cols[1]), _p(cols[2]),
+                                              C.byref(model_struct(model)), int(n_features),
+                                              int(seed), _p(out)))
+    return out

@@ -1,0 +1,233 @@
+/*
+ * geostat_gb300.h -- C ABI of the GB300-native kriging / Vecchia library.
+ *
+ * Every entry point is plain C: pointers, sizes and status codes, no CUDA or
+ * torch types (streams are passed as `void*` holding a cudaStream_t, NULL for
+ * the handle's own stream).  Each declaration names the geostat-rs interface
+ * it replaces (paths relative to the geostat-rs workspace); the Rust-side
+ * binding lives behind a `cuda` cargo feature next to
+ * crates/geostat-core/src/parallel.rs.
+ *
+ * Threading: handles are immutable after creation and may be used from
+ * several host threads at once (each call takes its own stream); the only
+ * mutable shared state is the per-thread last-error message.
+ */
+#ifndef GEOSTAT_GB300_H
+#define GEOSTAT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS_ABI_VERSION 1
+#define GS_MAX_STRUCTURES 4
+/* Largest conditioning set the mixed-precision kernel holds on chip, and the
+ * largest neighbourhood (neighbours + drift terms) any GPU kernel accepts. */
+#define GS_MIXED_MAX_NEIGHBORS 64
+#define GS_MAX_SYSTEM 256
+
+/* Return codes: 1..6 mirror GeostatError (crates/geostat-core/src/error.rs:14-39). */
+enum {
+  GS_OK = 0,
+  GS_ERR_INSUFFICIENT_DATA = 1,
+  GS_ERR_DIMENSION_MISMATCH = 2,
+  GS_ERR_SINGULAR_SYSTEM = 3,
+  GS_ERR_INVALID_PARAMETER = 4,
+  GS_ERR_NO_NEIGHBORS = 5,
+  GS_ERR_DUPLICATE_POINTS = 6,
+  GS_ERR_CUDA = 100,
+  GS_ERR_OUT_OF_MEMORY = 101
+};
+
+/* ModelKind (crates/geostat-core/src/variogram/model.rs:50-101).  The CUDA
+ * path evaluates the closed-form kinds 0..4; others are rejected with
+ * GS_ERR_INVALID_PARAMETER so the caller keeps them on the generic path. */
+enum {
+  GS_KIND_SPHERICAL = 0,
+  GS_KIND_EXPONENTIAL = 1,
+  GS_KIND_GAUSSIAN = 2,
+  GS_KIND_MATERN15 = 3,
+  GS_KIND_MATERN25 = 4,
+  GS_KIND_CIRCULAR = 5,
+  GS_KIND_STABLE = 6,
+  GS_KIND_HOLE = 7,
+  GS_KIND_WAVE = 8,
+  GS_KIND_POWER = 9
+};
+
+/* KrigingMethod (crates/geostat-core/src/kriging.rs:24-44). */
+enum { GS_SIMPLE = 0, GS_ORDINARY = 1, GS_UNIVERSAL = 2, GS_EXTERNAL_DRIFT = 3 };
+
+/* Arithmetic of the per-target solve. */
+enum {
+  GS_PREC_MIXED = 0, /* FP32 factorisation, double-float refinement, FP64 outputs */
+  GS_PREC_FP64 = 1   /* plain FP64, one system per thread */
+};
+
+/* Per-target status byte.  Low bits: 0 or a GeostatError code (the
+ * reference maps every per-target error to a NaN estimate,
+ * kriging.rs:648-652).  GS_ST_FP64_RESOLVED is OR-ed in when the mixed
+ * kernel handed the system to the FP64 solver (refinement stalled or a
+ * pivot was too small). */
+enum {
+  GS_ST_OK = 0,
+  GS_ST_INSUFFICIENT_DATA = 1,
+  GS_ST_SINGULAR = 3,
+  GS_ST_NO_NEIGHBORS = 5,
+  GS_ST_CAPACITY = 7, /* neighbourhood larger than GS_MAX_SYSTEM */
+  GS_ST_FP64_RESOLVED = 0x40
+};
+
+/* Structure / Anisotropy (model.rs:288-519); ratio/ratio_z/dip/rake are
+ * read only when has_anis != 0. */
+typedef struct {
+  int32_t kind;
+  int32_t has_anis;
+  double param; /* Stable alpha / Power theta; unused by the CUDA path */
+  double sill;
+  double range;
+  double azimuth_deg, ratio, ratio_z, dip_deg, rake_deg;
+} gs_structure;
+
+/* VariogramModel (model.rs:542-552). */
+typedef struct {
+  double nugget;
+  int32_t n_structures;
+  int32_t pad_;
+  gs_structure s[GS_MAX_STRUCTURES];
+} gs_model;
+
+/* KrigingConfig (kriging.rs:73-115).  Negative integers and has_* == 0
+ * encode Option::None. */
+typedef struct {
+  int64_t method;
+  double sk_mean;
+  int64_t uk_degree;
+  int64_t ked_nvars;
+  int64_t max_neighbors;
+  int64_t min_neighbors;
+  int64_t max_per_octant;
+  int64_t has_search_radius;
+  double search_radius;
+  int64_t has_anisotropic_search;
+  double search_azimuth_deg, search_ratio, search_ratio_z, search_dip_deg, search_rake_deg;
+} gs_kcfg;
+
+typedef struct gs_pointset gs_pointset;
+typedef struct gs_kriging gs_kriging;
+typedef struct gs_vecchia_plan gs_vecchia_plan;
+
+/* Message of the last failing call on this host thread. */
+const char* gs_last_error(void);
+int gs_abi_version(void);
+
+/* PointSet::from_xyz / from_xyzv + PointSet::new validation
+ * (crates/geostat-core/src/data.rs:15-83).  Copies coordinates and values
+ * into device memory; z is ignored when dim == 2. */
+int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, const double* z,
+                       const double* values, gs_pointset** out);
+void gs_pointset_destroy(gs_pointset* ps);
+/* PointSet::duplicate_pair (data.rs:171-173, 384-397): 1 and (i, j) when
+ * two points share coordinates, else 0. */
+int gs_pointset_duplicate_pair(const gs_pointset* ps, int64_t* i, int64_t* j);
+
+/* Kriging::new / with_external_drift / with_measurement_error
+ * (kriging.rs:166-260) including Kriging::build's validation
+ * (kriging.rs:262-340).  drift is n x ked_nvars row-major; errors has n
+ * entries.  The device bucket grid for the search frame is built here. */
+int gs_kriging_new(const gs_pointset* ps, const gs_model* model, const gs_kcfg* cfg,
+                   gs_kriging** out);
+int gs_kriging_with_external_drift(const gs_pointset* ps, const gs_model* model,
+                                   const gs_kcfg* cfg, const double* drift, gs_kriging** out);
+int gs_kriging_with_measurement_error(const gs_pointset* ps, const gs_model* model,
+                                      const gs_kcfg* cfg, const double* errors,
+                                      gs_kriging** out);
+void gs_kriging_destroy(gs_kriging* k);
+
+/* Kriging::predict_many / predict_many_with_drift (kriging.rs:648-672):
+ * host buffers in and out (copied inside the call).  tz ignored in 2-D;
+ * tdrift is nt x ked_nvars (external drift only).  lagrange and status may
+ * be NULL.  Failed targets get NaN value/variance as in the reference. */
+int gs_kriging_predict_many(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                            const double* tz, const double* tdrift, double* value,
+                            double* variance, double* lagrange, uint8_t* status, int precision,
+                            void* stream);
+/* Same, with every buffer already in device memory (no host copies). */
+int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double* tx,
+                                   const double* ty, const double* tz, const double* tdrift,
+                                   double* value, double* variance, double* lagrange,
+                                   uint8_t* status, int precision, void* stream);
+/* Kriging::predict_grid (kriging.rs:783-786) for Grid2D / Grid3D cell
+ * centres (grid.rs:80-96, 188-203), generated on the device. */
+int gs_kriging_predict_grid(const gs_kriging* k, const double* bbox_min, const double* bbox_max,
+                            const int64_t* ncell, double* value, double* variance,
+                            uint8_t* status, int precision, void* stream);
+/* Kriging::neighbors (kriging.rs:441-490): the conditioning indices the
+ * path uses, in the reference's (squared distance, index) order; host
+ * buffers, kcap slots per target, -1 padded.  count may be NULL. */
+int gs_kriging_neighbors(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                         const double* tz, int64_t kcap, int32_t* idx, int32_t* count,
+                         void* stream);
+
+/* vecchia::maxmin_order (crates/geostat-core/src/vecchia.rs:144-215), on
+ * the host as in the reference. */
+int gs_maxmin_order(int dim, int64_t n, const double* x, const double* y, const double* z,
+                    int64_t* order);
+/* vecchia_plan (vecchia.rs:232-282): order == NULL uses maxmin_order; the
+ * predecessor search runs on the device. */
+int gs_vecchia_plan_create(const gs_pointset* ps, int64_t m, const int64_t* order,
+                           gs_vecchia_plan** out);
+/* Copies the plan out: order[n], neighbours[n*m] (-1 padded), count[n]. */
+int gs_vecchia_plan_get(const gs_vecchia_plan* plan, int64_t* order, int64_t* neighbours,
+                        int32_t* count);
+void gs_vecchia_plan_destroy(gs_vecchia_plan* plan);
+/* loglik_with_plan (vecchia.rs:285-336) for ncand parameter candidates in
+ * one launch (the batched Nelder-Mead objective).  status[c] is 0 or a
+ * GeostatError code (a singular conditioning system). */
+int gs_vecchia_loglik_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs_model* models,
+                            double* loglik, int32_t* status, int precision, void* stream);
+/* vecchia_loglik (vecchia.rs:874-884). */
+int gs_vecchia_loglik(const gs_pointset* ps, const gs_model* model, int64_t m,
+                      const int64_t* order, double* loglik);
+/* vecchia_mle (vecchia.rs:921-1081) with a batched multi-start
+ * Nelder-Mead: every start's pending simplex evaluations go to the device
+ * in one gs_vecchia_loglik_batch launch.  starts (nstarts x 3, in the
+ * reference's x = (sqrt nugget, ln psill, ln range) parameters) may be NULL
+ * for the reference's three starts.  out_x receives the optimum. */
+int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                   int64_t nstarts, const double* starts, double step, int64_t max_iter,
+                   gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals);
+/* vecchia_predict (vecchia.rs:748-866): level-scheduled on the device. */
+int gs_vecchia_predict(const gs_pointset* ps, const gs_model* model, int64_t nt,
+                       const double* tx, const double* ty, const double* tz, int64_t m,
+                       double* value, double* variance);
+
+/* optim::nelder_mead_multistart (crates/geostat-core/src/optim.rs:6-123)
+ * over a host callback: the same state machine gs_vecchia_mle drives with
+ * batched device evaluations, exposed for driver parity checks. */
+typedef double (*gs_objective_fn)(const double* x, int64_t n, void* ctx);
+int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t nstarts,
+                              const double* starts, double step, int64_t max_iter, double* x_out,
+                              double* f_out);
+
+/* Seeded synthetic inputs (no reference counterpart beyond
+ * crates/geostat-core/src/rng.rs): xoshiro256++ uniforms on the host and a
+ * random-Fourier-feature Gaussian field evaluated on the device.  kind is
+ * the spectral family (exponential, gaussian, matern15, matern25; spherical
+ * uses the exponential family at the same practical range). */
+void gs_rng_uniform(uint64_t seed, int64_t count, double* out);
+void gs_rng_normal(uint64_t seed, int64_t count, double* out);
+int gs_synth_rff_field(int dim, int64_t n, const double* x, const double* y, const double* z,
+                       const gs_model* model, int64_t n_features, uint64_t seed, double* out);
+
+/* Timing of the last gs_kriging_predict_* call on this host thread (ms of
+ * device time per phase, measured with CUDA events on the call's stream):
+ * [0] search, [1] mixed solve, [2] FP64 re-solve, [3] whole call. */
+int gs_last_timings(double* ms4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

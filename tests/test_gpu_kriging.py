@@ -1,0 +1,293 @@
+"""GPU parity of moving-neighbourhood kriging against the FP64 oracle.
+
+Every test calls the CUDA library through its C ABI (geostat_rs) and checks
+neighbour sets bit-exactly and estimates/variances within the tolerance of
+tests/gpu_common.py, for both the mixed-precision and the plain FP64 paths.
+"""
+import numpy as np
+import pytest
+
+import pyoracle as O
+import geostat_rs as G
+from geostat_rs.model import Anisotropy, Structure, VariogramModel
+from gpu_common import (assert_close, cfg1_model, cfg2_model, cfg3_model, clustered_points,
+                        max_rel, smooth_values, uniform_points)
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(coords, values, model, targets, cfg_kw, oracle_kw=None, kcap=None, drift=None,
+             tdrift=None, errors=None, precisions=("mixed", "fp64")):
+    ps = G.PointSet(coords, values)
+    cfg = G.KrigingConfig(**cfg_kw)
+    if drift is not None:
+        k = G.Kriging.with_external_drift(ps, model, cfg, drift)
+    elif errors is not None:
+        k = G.Kriging.with_measurement_error(ps, model, cfg, errors)
+    else:
+        k = G.Kriging.new(ps, model, cfg)
+    okw = dict(method=cfg.method, mean=cfg.mean, degree=cfg.degree,
+               max_neighbors=cfg.max_neighbors, min_neighbors=cfg.min_neighbors,
+               max_per_octant=cfg.max_per_octant, radius=cfg.search_radius,
+               anisotropic_search=cfg.anisotropic_search, drift=drift, target_drift=tdrift,
+               measurement_error=errors, kcap=kcap or 0)
+    ref = O.krige(coords, values, model, targets, **okw)
+    outs = {}
+    for prec in precisions:
+        if tdrift is not None:
+            outs[prec] = k.predict_many_with_drift(targets, tdrift, prec, full=True)
+        else:
+            outs[prec] = k.predict_many(targets, prec, full=True)
+    return k, ref, outs
+
+
+def check(ref, out, values, sill, tol=1e-9):
+    st = out.status & 0x3f
+    assert (st == ref["status"].astype(np.uint8)).all()
+    vscale = float(np.mean(np.abs(values)))
+    rv = assert_close(out.value, ref["value"], vscale, tol, "value")
+    rs = assert_close(out.variance, ref["variance"], 1e-3 * sill, tol, "variance")
+    return rv, rs
+
+
+# ------------------------------------------------------------ neighbours --
+@pytest.mark.parametrize("dim,n,k", [(2, 2000, 32), (3, 5000, 64), (2, 300, 1), (2, 50, 80)])
+def test_knn_neighbour_sets_bit_exact(dim, n, k):
+    ext = [1000.0, 1000.0] if dim == 2 else [2000.0, 2000.0, 200.0]
+    c = uniform_points(n, dim, 7 + dim, ext)
+    v = smooth_values(c)
+    t = uniform_points(1500, dim, 99, np.asarray(ext) * 1.1) - 0.05 * np.asarray(ext)
+    ref = O.krige(c, v, cfg1_model(), t, max_neighbors=k, kcap=min(k, n))
+    assert ref["boundary_ties"] == 0
+    k_ = G.Kriging.new(G.PointSet(c, v), cfg1_model(), G.KrigingConfig(max_neighbors=k))
+    idx, cnt = k_.neighbors(t, min(k, n))
+    assert (cnt == ref["nb_count"]).all()
+    assert (idx == ref["neighbors"]).all()
+
+
+def test_radius_and_octant_neighbour_sets_bit_exact():
+    c = clustered_points(20000, 3, extent=10000.0, nblobs=40)
+    v = smooth_values(c)
+    t = uniform_points(800, 2, 5, [10000.0, 10000.0])
+    cases = [dict(max_neighbors=16, search_radius=300.0),
+             dict(max_neighbors=64, max_per_octant=16, min_neighbors=4),
+             dict(max_per_octant=4),
+             dict(max_neighbors=40, max_per_octant=16, search_radius=800.0)]
+    for case in cases:
+        cfg = G.KrigingConfig(**case)
+        kcap = 64
+        ref = O.krige(c, v, cfg1_model(), t, max_neighbors=cfg.max_neighbors,
+                      max_per_octant=cfg.max_per_octant, radius=cfg.search_radius,
+                      min_neighbors=cfg.min_neighbors, kcap=kcap)
+        kk = G.Kriging.new(G.PointSet(c, v), cfg1_model(), cfg)
+        idx, cnt = kk.neighbors(t, kcap)
+        assert (cnt == ref["nb_count"]).all(), case
+        assert (idx == ref["neighbors"]).all(), case
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_anisotropic_search_and_octants_bit_exact(dim):
+    ext = [1000.0, 1000.0] if dim == 2 else [1000.0, 1000.0, 300.0]
+    c = uniform_points(4000, dim, 21, ext)
+    v = smooth_values(c)
+    t = uniform_points(600, dim, 22, ext)
+    an = Anisotropy(35.0, 0.4, 0.5, 12.0, 7.0)
+    for case in (dict(max_neighbors=24, anisotropic_search=an),
+                 dict(max_neighbors=32, max_per_octant=6, anisotropic_search=an),
+                 dict(max_neighbors=20, search_radius=120.0, anisotropic_search=an)):
+        cfg = G.KrigingConfig(**case)
+        ref = O.krige(c, v, cfg1_model(), t, max_neighbors=cfg.max_neighbors,
+                      max_per_octant=cfg.max_per_octant, radius=cfg.search_radius,
+                      anisotropic_search=an, kcap=32)
+        kk = G.Kriging.new(G.PointSet(c, v), cfg1_model(), cfg)
+        idx, cnt = kk.neighbors(t, 32)
+        assert (cnt == ref["nb_count"]).all(), case
+        assert (idx == ref["neighbors"]).all(), case
+
+
+# ---------------------------------------------------- estimates / variances --
+def test_config1_ordinary_kriging_full_size():
+    """2-D OK: n=2000 in [0,1000]^2, nugget 0.1 + Sph(1, 200), 100x100 grid, n_max=32."""
+    c = uniform_points(2000, 2, 2024, [1000.0, 1000.0])
+    m = cfg1_model()
+    v = 10.0 + G.rff_field(c, VariogramModel(0.1, [Structure("exponential", 1.0, 200.0 / 3)]),
+                           2048, 11)
+    t = O.grid_centers([0, 0], [1000, 1000], [100, 100])
+    k, ref, outs = run_both(c, v, m, t, dict(max_neighbors=32))
+    for prec, out in outs.items():
+        check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-11)
+    # grid entry point == explicit targets
+    gv, gvar = k.predict_grid([0, 0], [1000, 1000], [100, 100])
+    assert np.array_equal(gv, outs["mixed"].value)
+
+
+@pytest.mark.parametrize("kind", ["spherical", "exponential", "gaussian", "matern15", "matern25"])
+def test_kinds_2d(kind):
+    c = uniform_points(1500, 2, 31, [100.0, 100.0])
+    v = smooth_values(c)
+    m = VariogramModel(0.05, [Structure(kind, 1.0, 25.0)])
+    t = uniform_points(700, 2, 32, [100.0, 100.0])
+    _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=24))
+    for prec, out in outs.items():
+        check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
+
+
+def test_config2_shape_3d_nested_rotated():
+    """3-D OK with nugget + rotated Sph(300/150/40, az 30, dip 10) + Exp(800), n_max=64."""
+    c = uniform_points(20000, 3, 5, [2000.0, 2000.0, 200.0])
+    m = cfg2_model()
+    v = G.rff_field(c, m, 1024, 3)
+    t = uniform_points(3000, 3, 6, [2000.0, 2000.0, 200.0])
+    _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64))
+    for prec, out in outs.items():
+        check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
+
+
+def test_ill_conditioned_gaussian_goes_to_fp64():
+    """Gaussian without nugget: cond(A) ~ 1e10+, beyond FP32 factorisation.  The
+    mixed kernel must hand such systems to the FP64 solver (status bit 0x40)
+    and then agree with the oracle as far as the conditioning allows."""
+    c = uniform_points(600, 2, 33, [100.0, 100.0])
+    v = smooth_values(c)
+    m = VariogramModel(0.0, [Structure("gaussian", 1.0, 25.0)])
+    t = uniform_points(200, 2, 34, [100.0, 100.0])
+    _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=16))
+    out = outs["mixed"]
+    assert ((out.status & 0x40) != 0).sum() > 0
+    ok = ref["status"] == 0
+    assert ((out.status & 0x3f)[ok] == 0).all()
+    assert max_rel(out.value[ok], ref["value"][ok], 10.0) < 1e-4
+
+
+@pytest.mark.parametrize("method,deg", [("simple", 1), ("universal", 1), ("universal", 2)])
+def test_methods_2d_and_3d(method, deg):
+    for dim in (2, 3):
+        ext = [500.0] * dim
+        c = uniform_points(3000, dim, 40 + dim, ext)
+        v = smooth_values(c) + (0.01 * c[:, 0] if method == "universal" else 0.0)
+        m = VariogramModel(0.02, [Structure("exponential", 0.8, 120.0),
+                                  Structure("spherical", 0.2, 300.0)])
+        t = uniform_points(500, dim, 50 + dim, ext)
+        kw = dict(method=method, degree=deg, max_neighbors=30)
+        if method == "simple":
+            kw["mean"] = float(np.mean(v))
+        _, ref, outs = run_both(c, v, m, t, kw)
+        for prec, out in outs.items():
+            check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
+        if method != "simple":
+            assert_close(outs["mixed"].lagrange, ref["lagrange"], 1.0, 1e-8, "lagrange")
+
+
+def test_external_drift_and_measurement_error():
+    c = uniform_points(2500, 2, 61, [1000.0, 1000.0])
+    cov = O.rng_uniform(62, 2500)
+    v = smooth_values(c) + 2.0 * cov
+    m = cfg3_model()
+    t = uniform_points(400, 2, 63, [1000.0, 1000.0])
+    tc = O.rng_uniform(64, 400).reshape(-1, 1)
+    _, ref, outs = run_both(c, v, m, t, dict(method="external_drift", n_vars=1, max_neighbors=32),
+                            drift=cov.reshape(-1, 1), tdrift=tc)
+    for prec, out in outs.items():
+        check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
+    err = 0.05 * O.rng_uniform(65, 2500)
+    _, ref, outs = run_both(c, v, cfg1_model(), t, dict(max_neighbors=20), errors=err)
+    for prec, out in outs.items():
+        check(ref, out, v, 1.1, 1e-9 if prec == "mixed" else 1e-10)
+
+
+def test_octant_uneven_systems_clustered():
+    """Octant search on clustered data: systems of 4..64 neighbours in one launch."""
+    c = clustered_points(30000, 9, extent=10000.0, nblobs=60)
+    m = cfg3_model()
+    v = G.rff_field(c, m, 512, 4)
+    t = uniform_points(1500, 2, 10, [10000.0, 10000.0])
+    _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64, max_per_octant=16,
+                                             min_neighbors=4))
+    counts = ref["nb_count"]
+    assert counts.min() < 64 <= counts.max()
+    for prec, out in outs.items():
+        check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
+
+
+# ---------------------------------------------- the reference's known answers --
+def sample():
+    c = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0], [0.4, 0.6]])
+    v = np.array([1.0, 2.0, 1.5, 2.5, 1.7])
+    return c, v, VariogramModel(0.05, [Structure("spherical", 0.95, 2.0)])
+
+
+def test_reference_known_answers_on_gpu():
+    c, v, m = sample()
+    # kriging.rs:1205 exact at data (global neighbourhood)
+    pv, pvar = G.Kriging.new(G.PointSet(c, v), m).predict_many(c)
+    assert np.max(np.abs(pv - v)) < 1e-8 and np.max(pvar) < 1e-8
+    # kriging.rs:1371 SK far field
+    sk = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig("simple", mean=1.74))
+    fv, fvar = sk.predict_many(np.array([[1e6, 1e6]]))
+    assert abs(fv[0] - 1.74) < 1e-9 and abs(fvar[0] - m.total_sill()) < 1e-9
+    # kriging.rs:1570 global == moving at k = n
+    t = np.array([[0.3, 0.3], [0.9, 0.1], [2.0, 2.0]])
+    g = G.Kriging.new(G.PointSet(c, v), m).predict_many(t)
+    l = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig(max_neighbors=5)).predict_many(t)
+    assert np.max(np.abs(g[0] - l[0])) < 1e-12 and np.max(np.abs(g[1] - l[1])) < 1e-12
+    # kriging.rs:1385 UK reproduces a linear drift
+    cu = np.array([[i, j] for i in range(4) for j in range(4)], float)
+    vu = 2.0 + 3.0 * cu[:, 0] - cu[:, 1]
+    tu = np.array([[1.5, 1.5], [5.0, 2.0]])
+    uv, _ = G.Kriging.new(G.PointSet(cu, vu), m, G.KrigingConfig("universal")).predict_many(tu)
+    assert np.max(np.abs(uv - (2 + 3 * tu[:, 0] - tu[:, 1]))) < 1e-7
+    # kriging.rs:960 octant balancing
+    co = np.array([[1.0, 0.1], [1.1, -0.1], [1.2, 0.2], [1.3, -0.2], [1.4, 0.05],
+                   [-2.0, 0.5], [-2.0, -0.5], [0.5, -2.0], [0.5, 2.0]])
+    vo = np.array([10.0] * 5 + [0.0] * 4)
+    near = G.Kriging.new(G.PointSet(co, vo), m, G.KrigingConfig(max_neighbors=4)).predict_many(
+        np.zeros((1, 2)))[0][0]
+    octn = G.Kriging.new(G.PointSet(co, vo), m, G.KrigingConfig(max_neighbors=4, max_per_octant=1)
+                         ).predict_many(np.zeros((1, 2)))[0][0]
+    assert near > 9.0 and octn < near - 2.0
+    # kriging.rs:913 min_neighbors -> NaN + NoNeighbors status
+    kr = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig(search_radius=0.75, min_neighbors=3))
+    r = kr.predict_many(np.array([[0.5, 0.5], [1.5, 1.5]]), full=True)
+    assert r.status[0] == 0 and r.status[1] == 5 and np.isnan(r.value[1])
+
+
+def test_construction_errors_match_reference():
+    c, v, m = sample()
+    ps = G.PointSet(c, v)
+    with pytest.raises(G.InvalidParameter):
+        G.Kriging.new(ps, m, G.KrigingConfig(min_neighbors=0))
+    with pytest.raises(G.InvalidParameter):
+        G.Kriging.new(ps, m, G.KrigingConfig(max_neighbors=2, min_neighbors=3))
+    with pytest.raises(G.InsufficientData):
+        G.Kriging.new(ps, m, G.KrigingConfig(min_neighbors=6))
+    with pytest.raises(G.InvalidParameter):
+        G.Kriging.new(ps, m, G.KrigingConfig(search_radius=-1.0))
+    with pytest.raises(G.InvalidParameter):
+        G.Kriging.new(ps, m, G.KrigingConfig("universal", degree=3))
+    with pytest.raises(G.InvalidParameter):
+        G.Kriging.new(ps, m, G.KrigingConfig("external_drift", n_vars=1))
+    dup = G.PointSet(np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 0.0], [0.0, 1.0]]),
+                     np.array([1.0, 2.0, 2.1, 1.5]))
+    with pytest.raises(G.DuplicatePoints, match="1 and 2"):
+        G.Kriging.new(dup, m)
+
+
+def test_python_binding_mirror_matches_oracle():
+    c = uniform_points(800, 2, 71, [100.0, 100.0])
+    v = smooth_values(c)
+    m = VariogramModel(0.05, [Structure("exponential", 0.95, 20.0)])
+    tx, ty = np.linspace(1, 99, 50), np.linspace(99, 1, 50)
+    pv, pvar = G.krige(c[:, 0], c[:, 1], v, m, tx, ty, max_neighbors=16, octant=4)
+    ref = O.krige(c, v, m, np.stack([tx, ty], 1), max_neighbors=16, max_per_octant=4)
+    assert_close(pv, ref["value"], 10.0, 1e-9, "krige")
+    gv, gvar = G.krige_grid(c[:, 0], c[:, 1], v, m, (0.0, 0.0, 100.0, 50.0), 20, 10,
+                            max_neighbors=12)
+    gref = O.krige(c, v, m, O.grid_centers([0, 0], [100, 50], [20, 10]), max_neighbors=12)
+    assert_close(gv, gref["value"], 10.0, 1e-9, "krige_grid")
+    c3 = uniform_points(800, 3, 72, [100.0, 100.0, 30.0])
+    v3 = smooth_values(c3)
+    t3 = uniform_points(60, 3, 73, [100.0, 100.0, 30.0])
+    pv3, _ = G.krige_3d(c3[:, 0], c3[:, 1], c3[:, 2], v3, m, t3[:, 0], t3[:, 1], t3[:, 2],
+                        method="universal", max_neighbors=20)
+    ref3 = O.krige(c3, v3, m, t3, method="universal", max_neighbors=20)
+    assert_close(pv3, ref3["value"], 10.0, 1e-9, "krige_3d")

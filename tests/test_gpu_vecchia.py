@@ -1,0 +1,107 @@
+"""GPU parity of the Vecchia plan, log-likelihood and MLE against the oracle."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+import geostat_rs as G
+from geostat_rs.model import Structure, VariogramModel
+from gpu_common import assert_close, uniform_points
+
+pytestmark = pytest.mark.gpu
+
+
+def matern25(nug=0.02, sill=1.0, rng=0.05):
+    return VariogramModel(nug, [Structure("matern25", sill, rng)])
+
+
+@pytest.mark.parametrize("dim,n,m", [(2, 3000, 30), (3, 2500, 20), (2, 60, 100), (2, 5000, 8)])
+def test_plan_matches_reference_plan_exactly(dim, n, m):
+    if dim == 2:
+        c, v = O.test_field_2d(n, 100 + n)
+    else:
+        c, v = O.test_field_3d(n, 100 + n)
+    plan = G.VecchiaPlan(G.PointSet(c, v), m)
+    order, nb, cnt = plan.arrays()
+    o_ref, nb_ref, cnt_ref = O.vecchia_plan(c, m)
+    assert order.tolist() == o_ref.tolist()
+    assert (cnt == cnt_ref).all()
+    mm = nb.shape[1]
+    assert (nb == nb_ref[:, :mm]).all()
+
+
+def test_plan_with_given_order():
+    c, v = O.test_field_2d(2000, 7)
+    order = np.arange(2000)[::-1].copy()
+    plan = G.VecchiaPlan(G.PointSet(c, v), 15, order)
+    o, nb, cnt = plan.arrays()
+    o_ref, nb_ref, cnt_ref = O.vecchia_plan(c, 15, order)
+    assert o.tolist() == o_ref.tolist() and (nb == nb_ref).all() and (cnt == cnt_ref).all()
+
+
+def test_loglik_batch_matches_oracle_and_is_batch_invariant():
+    c = uniform_points(20000, 2, 3, [1.0, 1.0])
+    v = 0.5 + G.rff_field(c, matern25(), 1024, 5)
+    ps = G.PointSet(c, v)
+    plan = G.VecchiaPlan(ps, 30)
+    order, nb, cnt = plan.arrays()
+    models = [matern25(), matern25(0.05, 0.8, 0.08), matern25(0.001, 1.5, 0.02),
+              VariogramModel(0.02, [Structure("exponential", 1.0, 0.05)]),
+              VariogramModel(0.02, [Structure.with_anisotropy("spherical", 0.7, 0.2, 30.0, 0.5),
+                                    Structure("matern15", 0.3, 0.05)])]
+    ll, st = plan.loglik(models)
+    assert (st == 0).all()
+    for i, mdl in enumerate(models):
+        ref = O.vecchia_loglik_plan(c, v, mdl, order, nb, cnt)
+        assert_close([ll[i]], [ref], 1.0, 1e-9, f"candidate {i}")
+        one, _ = plan.loglik([mdl])
+        assert one[0] == ll[i]
+    ll64, st64 = plan.loglik(models, precision="fp64")
+    assert (st64 == 0).all()
+    for i, mdl in enumerate(models):
+        ref = O.vecchia_loglik_plan(c, v, mdl, order, nb, cnt)
+        assert_close([ll64[i]], [ref], 1.0, 1e-11, f"fp64 candidate {i}")
+
+
+def test_full_conditioning_equals_exact_likelihood():
+    # vecchia.rs:1998-2010
+    c, v = O.test_field_2d(14, 3)
+    m = VariogramModel(0.05, [Structure("exponential", 1.0, 40.0)])
+    got = G.vecchia_loglik(c[:, 0], c[:, 1], v, m, 13)
+    assert abs(got - O.exact_loglik(c, v, m)) < 1e-9
+
+
+def test_vecchia_loglik_entry_point_3d():
+    c, v = O.test_field_3d(3000, 17)
+    m = VariogramModel(0.05, [Structure.with_rotation("spherical", 0.9, 40.0, 20.0, 10.0, 5.0,
+                                                      0.6, 0.4)])
+    plan = G.VecchiaPlan(G.PointSet(c, v), 25)
+    ll, st = plan.loglik([m])
+    ref = O.vecchia_loglik(c, v, m, 25)
+    assert st[0] == 0
+    assert_close(ll, [ref], 1.0, 1e-9, "3-D loglik")
+
+
+def test_rejected_models():
+    c, v = O.test_field_2d(50, 1)
+    plan = G.VecchiaPlan(G.PointSet(c, v), 5)
+    ll, st = plan.loglik([VariogramModel(0.0, [Structure("power", 1.0, 1.0, param=1.0)])])
+    assert st[0] == G.InvalidParameter.code and np.isnan(ll[0])
+    with pytest.raises(G.InvalidParameter):
+        G.VecchiaPlan(G.PointSet(c, v), 0)
+    with pytest.raises(G.InsufficientData):
+        G.VecchiaPlan(G.PointSet(c[:1], v[:1]), 3)
+
+
+def test_mle_objective_parity_and_batched_nelder_mead():
+    c, v = O.test_field_2d(400, 21)
+    ps = G.PointSet(c, v)
+    starts, rmax = O.vecchia_mle_setup(c, v)
+    model, ll, x, nev = G.vecchia_mle_fit(ps, "exponential", 12, starts=starts, max_iter=400)
+    xr, fr, nr = O.vecchia_mle_nm(c, v, "exponential", 12, starts, max_iter=400)
+    # same algorithm, same objective to ~1e-12: the optimum agrees closely
+    assert abs(-ll - fr) <= 1e-7 * abs(fr)
+    assert np.max(np.abs(x - xr)) < 1e-3
+    o, nb, cnt = O.vecchia_plan(c, 12)
+    fx = O.vecchia_mle_objective(c, v, "exponential", 12, o, nb, cnt, rmax, x)
+    assert abs(fx[0] + ll) <= 1e-9 * abs(fx[0])
+    assert model.nugget >= 0 and model.structures[0].range > 0
