@@ -1,0 +1,485 @@
+#!/usr/bin/env python
+"""Benchmark: kriged targets/s (and Vecchia points/s) on one GB300.
+
+Workload (one step = one pass of the hot path over one batch):
+  3-D ordinary kriging, n = 200,000 data points uniform in a 2000 x 2000 x 200 m
+  box; values from a 4,096-feature random-Fourier-feature field of the nested
+  model nugget 0.05 + Sph(0.6; ranges 300/150/40 m, azimuth 30, dip 10) +
+  Exp(0.35, 800 m); targets = the 256 x 256 x 64 grid (4,194,304 cells); the
+  64 nearest Euclidean neighbours per target; FP32 factorisation with
+  double-float refinement and FP64 outputs.
+
+`value` is measured with inputs resident in HBM (the device entry point), L2
+flushed between steps; `e2e` goes through the host-buffer C-ABI call with the
+host<->device copies inside the timed region.  The plain FP64 GPU build and a
+Vecchia log-likelihood batch (2,000,000 points, m = 30, 16 candidates) are
+timed beside it, and the CPU oracle is timed on a bounded sample of the same
+workload on the host's cores.
+
+--impl reference times the reference algorithm on the CPU (the oracle, all
+host threads) on the same workload and prints the same JSON line.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "geostat-rs_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "kriged targets/s & Vecchia points/s, mixed-prec vs FP64 GPU @1e-9; p99 latency"
+WORKLOAD = ("3-D ordinary kriging: n=200,000 points in 2000x2000x200 m, RFF field (4,096 "
+            "features) of nugget 0.05 + Sph(0.6; 300/150/40 m; az 30, dip 10) + Exp(0.35, 800 m); "
+            "targets 256x256x64 grid (4,194,304); n_max=64 Euclidean nearest")
+N_DATA = 200_000
+GRID = (256, 256, 64)
+BOX = (2000.0, 2000.0, 200.0)
+K_NEIGH = 64
+SEED = 20260
+
+
+def algorithmic_flops_per_target(n, p=1):
+    """N^3/3 + 2N^2 + 4N for a system of N = n + p unknowns."""
+    N = n + p
+    return N ** 3 / 3.0 + 2.0 * N ** 2 + 4.0 * N
+
+
+def make_model():
+    from geostat_rs.model import Structure, VariogramModel
+    return VariogramModel(0.05, [Structure.with_rotation("spherical", 0.6, 300.0, 30.0, 10.0, 0.0,
+                                                         0.5, 40.0 / 300.0),
+                                 Structure("exponential", 0.35, 800.0)])
+
+
+def make_coords():
+    import geostat_rs as G
+    u = G.rng_uniform(SEED, 3 * N_DATA).reshape(N_DATA, 3)
+    return u * np.asarray(BOX)
+
+
+def grid_targets():
+    nx, ny, nz = GRID
+    ix = (np.arange(nx) + 0.5) * (BOX[0] / nx)
+    iy = (np.arange(ny) + 0.5) * (BOX[1] / ny)
+    iz = (np.arange(nz) + 0.5) * (BOX[2] / nz)
+    z, y, x = np.meshgrid(iz, iy, ix, indexing="ij")
+    return np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_profile_traffic():
+    """Per-launch DRAM traffic of the mixed kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "krige_mixed_kernel_cfg2.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------------ ours --
+def run_ours(args, rank, world):
+    import torch
+    import geostat_rs as G
+    from geostat_rs import _abi
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda")
+    log = (lambda *a: print(*a, file=sys.stderr, flush=True)) if rank == 0 else (lambda *a: None)
+    t0 = time.time()
+    coords = make_coords()
+    model = make_model()
+    values = G.rff_field(coords, model, 4096, SEED + 1)
+    ps = G.PointSet(coords, values)
+    kr = G.Kriging.new(ps, model, G.KrigingConfig(max_neighbors=K_NEIGH))
+    tg = grid_targets()
+    nt = len(tg)
+    log(f"[bench] data + grid build {time.time() - t0:.1f}s, nt={nt}")
+
+    cols = [torch.from_numpy(np.ascontiguousarray(tg[:, d])).to(dev) for d in range(3)]
+    out_v = torch.empty(nt, dtype=torch.float64, device=dev)
+    out_var = torch.empty(nt, dtype=torch.float64, device=dev)
+    out_st = torch.empty(nt, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def step(prec):
+        kr.predict_device(nt, cols[0].data_ptr(), cols[1].data_ptr(), cols[2].data_ptr(),
+                          out_v.data_ptr(), out_var.data_ptr(), out_st.data_ptr(), prec, sptr)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(prec, steps, warmup, collect=None):
+        for _ in range(warmup):
+            step(prec)
+        torch.cuda.synchronize()
+        barrier()
+        times, phases, launches = [], [], 0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = _abi.load().gs_launch_count()
+            e0.record(stream)
+            step(prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            launches += _abi.load().gs_launch_count() - l0
+            times.append(e0.elapsed_time(e1))
+            phases.append(G.last_timings())
+        barrier()
+        mx = max(times)
+        tot = sum(times)
+        if world > 1:
+            t = torch.tensor([tot], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot = float(t.item())
+        return tot / steps, times, phases, launches
+
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ms_mixed, times, phases, launches = timed("mixed", args.steps, args.warmup)
+    clk = clocks.stop()
+    value = world * nt / (ms_mixed * 1e-3)
+    mixed_ms = statistics.mean(p[1] for p in phases)
+    search_ms = statistics.mean(p[0] for p in phases)
+    resolve_ms = statistics.mean(p[2] for p in phases)
+    st = out_st.cpu().numpy()
+    n_fallback = int(((st & 0x40) != 0).sum())
+    n_fail = int(((st & 0x3f) != 0).sum())
+    log(f"[bench] mixed: {ms_mixed:.1f} ms/step (search {search_ms:.1f}, solve {mixed_ms:.1f}, "
+        f"fp64 re-solve {resolve_ms:.1f}), fallback {n_fallback}, failed {n_fail}")
+    mixed_value = out_v.cpu().numpy()
+    mixed_var = out_var.cpu().numpy()
+
+    # plain FP64 GPU build on the same workload
+    ms_fp64, _, ph64, _ = timed("fp64", max(1, min(2, args.steps)), 1)
+    fp64_value = world * nt / (ms_fp64 * 1e-3)
+    fp64_v = out_v.cpu().numpy()
+    log(f"[bench] fp64 plain build: {ms_fp64:.1f} ms/step")
+
+    # end to end through the host-buffer call (pinned host memory)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    hx, hy, hz = pin(tg[:, 0]), pin(tg[:, 1]), pin(tg[:, 2])
+    hv = torch.empty(nt, dtype=torch.float64).pin_memory().numpy()
+    hvar = torch.empty(nt, dtype=torch.float64).pin_memory().numpy()
+    hlag = torch.empty(nt, dtype=torch.float64).pin_memory().numpy()
+    hst = torch.empty(nt, dtype=torch.uint8).pin_memory().numpy()
+    import ctypes as C
+    P = lambda a, ct=C.c_double: a.ctypes.data_as(C.POINTER(ct))
+    lib = _abi.load()
+
+    def e2e_step():
+        _abi.check(lib.gs_kriging_predict_many(kr._h, nt, P(hx), P(hy), P(hz), None, P(hv), P(hvar),
+                                               P(hlag), P(hst, C.c_uint8), 0, None))
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t1)
+    barrier()
+    e2e_ms = statistics.mean(e2e_times) * 1e3
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * nt / (e2e_ms * 1e-3)
+    h2d = 3 * 8 * nt
+    d2h = (8 + 8 + 8 + 1) * nt
+    assert np.array_equal(hv, mixed_value, equal_nan=True)
+    log(f"[bench] e2e: {e2e_ms:.1f} ms/step")
+
+    result = None
+    if rank == 0:
+        # roofline: algorithmic FP32 flops of the dominant (mixed) kernel
+        fpt = algorithmic_flops_per_target(K_NEIGH, 1)
+        flops_per_launch_set = fpt * nt
+        achieved = flops_per_launch_set / (mixed_ms * 1e-3) / 1e12
+        peak_fp32 = C.c_double()
+        peak_fp64 = C.c_double()
+        _abi.check(lib.gs_probe_fma_tflops(0, C.byref(peak_fp32)))
+        _abi.check(lib.gs_probe_fma_tflops(1, C.byref(peak_fp64)))
+        traffic = read_profile_traffic()
+        # accuracy and CPU baseline on a bounded sample
+        acc, cpu = cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var,
+                                           fp64_v, kr, log)
+        vec = vecchia_bench(args, log) if not args.no_vecchia else None
+        peaks = measured_peaks()
+        result = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "kriged targets/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_mixed,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 factor + df64 refinement + f64 outputs",
+            "data": "synthetic: seeded xoshiro256++ coordinates, random-Fourier-feature field",
+            "config": {"workload": WORKLOAD, "n_data": N_DATA, "n_targets": nt,
+                       "max_neighbors": K_NEIGH, "dim": 3,
+                       "l2": "flushed between steps (256 MiB write); neighbour lists 1 GiB > L2",
+                       "parallelism": f"replicas x{world} (targets independent)"},
+            "phases_ms": {"search": search_ms, "mixed_solve": mixed_ms, "fp64_resolve": resolve_ms,
+                          "fp64_resolved_targets": n_fallback, "failed_targets": n_fail},
+            "fp64_gpu_build": {"value": fp64_value, "unit": "kriged targets/s",
+                               "ms_per_step": ms_fp64,
+                               "mixed_over_fp64": value / fp64_value},
+            "accuracy": acc,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32.value,
+                         "unit": "TFLOP/s", "frac": achieved / peak_fp32.value,
+                         "traffic": traffic,
+                         "kernel": "krige_mixed_kernel",
+                         "peak_source": "measured FP32 FMA probe (gs_probe_fma_tflops); "
+                                        "MEASURED_PEAKS.json has no CUDA-core number",
+                         "fp64_peak_tflops": peak_fp64.value,
+                         "algorithmic_flops_per_target": fpt,
+                         "hbm_peak_gbs": peaks.get("hbm_gbs")},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "kriged targets/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        if vec is not None:
+            result["vecchia"] = vec
+    return result
+
+
+def cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var, fp64_v, kr,
+                            log):
+    """Oracle on a bounded sample: CPU throughput and max rel error of both GPU paths."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    rng = np.random.RandomState(7)
+    probe = rng.choice(len(tg), 2000, replace=False)
+    t0 = time.perf_counter()
+    O.krige(coords, values, model, tg[probe], max_neighbors=K_NEIGH, nthreads=cores)
+    per = (time.perf_counter() - t0) / len(probe)
+    ns = int(min(len(tg), max(2000, args.cpu_seconds / max(per, 1e-9))))
+    idx = np.sort(rng.choice(len(tg), ns, replace=False))
+    t0 = time.perf_counter()
+    ref = O.krige(coords, values, model, tg[idx], max_neighbors=K_NEIGH, nthreads=cores,
+                  kcap=K_NEIGH)
+    dt = time.perf_counter() - t0
+    log(f"[bench] oracle: {ns} targets in {dt:.1f}s on {cores} threads")
+    vs = float(np.mean(np.abs(values)))
+    sill = model.total_sill()
+
+    def rel(a, b, floor):
+        return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+    nbr_idx, _ = kr.neighbors(tg[idx[:5000]], K_NEIGH)
+    mism = int((nbr_idx != ref["neighbors"][:5000]).any(axis=1).sum())
+    acc = {"sample_targets": ns,
+           "mixed_max_rel_value": rel(mixed_value[idx], ref["value"], vs),
+           "mixed_max_rel_variance": rel(mixed_var[idx], ref["variance"], 1e-3 * sill),
+           "fp64_max_rel_value": rel(fp64_v[idx], ref["value"], vs),
+           "tolerance": "|a-b| <= 1e-9 max(|b|, floor); floor = mean|z| (values), 1e-3 sill (variances)",
+           "neighbour_set_mismatches": mism, "neighbour_sample": min(5000, ns),
+           "oracle_boundary_ties": ref["boundary_ties"]}
+    cpu = {"value": ns / dt, "unit": "kriged targets/s", "cores": cores, "kind": "port",
+           "sample": f"{ns} random targets of the 4,194,304-cell grid (same data, model, n_max=64)"}
+    return acc, cpu
+
+
+def vecchia_bench(args, log):
+    """Vecchia log-likelihood: n = 2,000,000 points in [0,1]^2, m = 30, 16 candidates."""
+    import geostat_rs as G
+    from geostat_rs.model import Structure, VariogramModel
+    n = args.vecchia_n
+    t0 = time.time()
+    c = G.rng_uniform(SEED + 5, 2 * n).reshape(n, 2)
+    base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
+    v = 0.5 + G.rff_field(c, base, 8192, SEED + 6)
+    ps = G.PointSet(c, v)
+    t1 = time.time()
+    plan = G.VecchiaPlan(ps, 30)
+    t_plan = time.time() - t1
+    log(f"[bench] vecchia data {t1 - t0:.1f}s, plan (host maxmin + device kNN) {t_plan:.1f}s")
+    cands = [VariogramModel(0.02 * (1 + 0.05 * i), [Structure("matern25", 1.0 - 0.01 * i,
+                                                              0.05 * (1 + 0.03 * i))])
+             for i in range(16)]
+    plan.loglik(cands)
+    ts = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        ll, st = plan.loglik(cands)
+        ts.append(time.perf_counter() - t1)
+    dt = statistics.median(ts)
+    ll64, _ = plan.loglik(cands[:1], precision="fp64")
+    t1 = time.perf_counter()
+    plan.loglik(cands[:1], precision="fp64")
+    dt64 = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    ll1, _ = plan.loglik(cands[:1])
+    dt1 = time.perf_counter() - t1
+    return {"points_per_s": n * len(cands) / dt, "unit": "Vecchia points/s",
+            "n": n, "m": 30, "candidates_per_batch": len(cands), "batch_ms": dt * 1e3,
+            "fp64_gpu_points_per_s": n / dt64, "single_candidate_points_per_s": n / dt1,
+            "mixed_vs_fp64_rel_diff": abs(ll1[0] - ll64[0]) / abs(ll64[0]),
+            "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
+
+
+# ------------------------------------------------------------- reference --
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    from geostat_rs.model import Structure, VariogramModel  # pure-Python model description
+    cores = os.cpu_count() or 1
+    u = O.rng_uniform(SEED, 3 * N_DATA).reshape(N_DATA, 3) * np.asarray(BOX)
+    model = VariogramModel(0.05, [Structure.with_rotation("spherical", 0.6, 300.0, 30.0, 10.0, 0.0,
+                                                          0.5, 40.0 / 300.0),
+                                  Structure("exponential", 0.35, 800.0)])
+    # field values from a CPU random-Fourier-feature sum (the oracle's cost does
+    # not depend on the values)
+    rs = np.random.RandomState(SEED)
+    w = rs.standard_normal((3, 512)) / 300.0
+    ph = rs.uniform(0, 2 * np.pi, 512)
+    vals = np.cos(u @ w + ph).sum(axis=1) * np.sqrt(2.0 / 512)
+    tg = grid_targets()
+    rng = np.random.RandomState(11)
+    probe = rng.choice(len(tg), 1000, replace=False)
+    t0 = time.perf_counter()
+    O.krige(u, vals, model, tg[probe], max_neighbors=K_NEIGH, nthreads=cores)
+    per = (time.perf_counter() - t0) / len(probe)
+    ns = int(min(len(tg), max(1000, args.ref_step_seconds / max(per, 1e-9))))
+    for _ in range(args.warmup):
+        idx = rng.choice(len(tg), min(ns, 2000), replace=False)
+        O.krige(u, vals, model, tg[idx], max_neighbors=K_NEIGH, nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        idx = np.sort(rng.choice(len(tg), ns, replace=False))
+        t0 = time.perf_counter()
+        O.krige(u, vals, model, tg[idx], max_neighbors=K_NEIGH, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    mean = statistics.mean(times)
+    value = ns / mean
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "kriged targets/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": mean * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_data": N_DATA, "n_targets": len(tg),
+                       "max_neighbors": K_NEIGH, "dim": 3},
+            "cpu_baseline": {"value": value, "unit": "kriged targets/s", "cores": cores,
+                             "kind": "port",
+                             "sample": f"{ns} random grid targets per step (same data size, model, "
+                                       "n_max=64); the reference's Rust crate cannot be built "
+                                       "without cargo, so its FP64 C++ restatement runs"},
+            "e2e": {"value": value, "unit": "kriged targets/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--vecchia-n", type=int, default=2_000_000)
+    ap.add_argument("--no-vecchia", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

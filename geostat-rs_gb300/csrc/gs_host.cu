@@ -253,6 +253,11 @@ struct KeyLess {
   }
 };
 
+// Multi-resolution grid over the selected points.  Level l has cells 2^l
+// times wider than level 0 (about one point per cell when all n points are
+// selected).  A query uses the finest level whose cells hold about one
+// selected point each, so the exact nearest neighbour is found within a
+// couple of rings whatever the current selected count.
 class SelectedGrid {
  public:
   SelectedGrid(const std::vector<double>& pts, int dim, int64_t n) : dim_(dim) {
@@ -268,8 +273,6 @@ class SelectedGrid {
     double ext = 0.0;
     for (int d = 0; d < dim; ++d) ext = std::max(ext, hi_[d] - lo_[d]);
     if (!(ext > 0.0)) ext = 1.0;
-    // About one point per cell at the end of the ordering; axes with no
-    // extent get a single cell.
     double vol = 1.0;
     int act = 0;
     for (int d = 0; d < dim; ++d)
@@ -278,42 +281,51 @@ class SelectedGrid {
         ++act;
       }
     if (act == 0) act = 1;
-    cell_ = pow(vol / (double)std::max<int64_t>(n, 1), 1.0 / act);
-    if (!(cell_ > 0.0)) cell_ = ext;
-    int64_t total = 1;
-    for (;;) {
-      total = 1;
+    double cell = pow(vol / (double)std::max<int64_t>(n, 1), 1.0 / act);
+    if (!(cell > 0.0)) cell = ext;
+    for (int guard = 0; guard < 64; ++guard) {
+      Level L;
+      L.cell = cell;
+      int64_t total = 1;
       for (int d = 0; d < dim; ++d) {
-        double c = ceil((hi_[d] - lo_[d]) / cell_);
-        n_[d] = std::max<int64_t>(1, (int64_t)std::min(c, 1e9));
-        total *= n_[d];
+        double c = (hi_[d] - lo_[d] > ext * 1e-9) ? ceil((hi_[d] - lo_[d]) / cell) : 1.0;
+        L.n[d] = std::max<int64_t>(1, (int64_t)std::min(c, 1e9));
+        total *= L.n[d];
       }
-      if (total <= 4 * std::max<int64_t>(n, 16)) break;
-      cell_ *= 1.5;
+      if (total <= 4 * std::max<int64_t>(n, 16) || levels_.size() > 0) {
+        L.head.assign(total, -1);
+        levels_.push_back(std::move(L));
+      }
+      if (total <= 4) break;
+      cell *= 2.0;
     }
-    head_.assign(total, -1);
-    next_.reserve(n);
     pts_.reserve(n * dim);
   }
   void insert(const double* p) {
-    int64_t c = cell_of(p);
-    int64_t id = (int64_t)next_.size();
-    next_.push_back(head_[c]);
-    head_[c] = id;
+    const int64_t id = (int64_t)(pts_.size() / dim_);
     for (int d = 0; d < dim_; ++d) pts_.push_back(p[d]);
+    for (auto& L : levels_) {
+      int64_t c = cell_of(L, p);
+      L.next.push_back(L.head[c]);
+      L.head[c] = id;
+    }
   }
   // Exact squared distance to the nearest inserted point.
   double nearest_d2(const double* p) const {
+    const int64_t nsel = (int64_t)(pts_.size() / dim_);
+    size_t lv = 0;
+    while (lv + 1 < levels_.size() && (int64_t)levels_[lv].head.size() > 2 * nsel) ++lv;
+    const Level& L = levels_[lv];
     int64_t tc[3] = {0, 0, 0};
-    cell_coords(p, tc);
+    cell_coords(L, p, tc);
     double best = std::numeric_limits<double>::infinity();
     int64_t maxring = 0;
-    for (int d = 0; d < dim_; ++d) maxring = std::max(maxring, n_[d]);
+    for (int d = 0; d < dim_; ++d) maxring = std::max(maxring, L.n[d]);
     for (int64_t ring = 0; ring <= maxring; ++ring) {
-      double rmin = std::max((double)ring - 1.0 - 1e-9, 0.0) * cell_;
+      double rmin = std::max((double)ring - 1.0 - 1e-9, 0.0) * L.cell;
       if (rmin * rmin > best) break;
-      visit_shell(tc, ring, [&](int64_t cell) {
-        for (int64_t q = head_[cell]; q >= 0; q = next_[q]) {
+      visit_shell(L, tc, ring, [&](int64_t cell) {
+        for (int64_t q = L.head[cell]; q >= 0; q = L.next[q]) {
           double s = 0.0;
           for (int d = 0; d < dim_; ++d) {
             double dd = pts_[q * dim_ + d] - p[d];
@@ -327,64 +339,55 @@ class SelectedGrid {
   }
 
  private:
-  void cell_coords(const double* p, int64_t* c) const {
+  struct Level {
+    double cell = 1.0;
+    int64_t n[3] = {1, 1, 1};
+    std::vector<int64_t> head, next;
+  };
+  void cell_coords(const Level& L, const double* p, int64_t* c) const {
     for (int d = 0; d < dim_; ++d) {
-      double q = floor((p[d] - lo_[d]) / cell_);
-      int64_t v = q < 0 ? 0 : (q >= (double)n_[d] ? n_[d] - 1 : (int64_t)q);
-      c[d] = v;
+      double q = floor((p[d] - lo_[d]) / L.cell);
+      c[d] = q < 0 ? 0 : (q >= (double)L.n[d] ? L.n[d] - 1 : (int64_t)q);
     }
   }
-  int64_t cell_of(const double* p) const {
+  int64_t cell_of(const Level& L, const double* p) const {
     int64_t c[3] = {0, 0, 0};
-    cell_coords(p, c);
+    cell_coords(L, p, c);
     int64_t id = 0, stride = 1;
     for (int d = 0; d < dim_; ++d) {
       id += c[d] * stride;
-      stride *= n_[d];
+      stride *= L.n[d];
     }
     return id;
   }
   template <class F>
-  void visit_shell(const int64_t* tc, int64_t r, F&& f) const {
+  void visit_shell(const Level& L, const int64_t* tc, int64_t r, F&& f) const {
     int64_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     for (int d = 0; d < dim_; ++d) {
       lo[d] = tc[d] - r;
       hi[d] = tc[d] + r;
     }
-    // Walk the (2r+1)^D cube, visiting only cells on its surface.
-    int64_t cur[3];
-    for (int d = 0; d < dim_; ++d) cur[d] = std::max<int64_t>(lo[d], 0);
-    if (dim_ < 3) cur[2] = 0;
-    auto inside = [&](const int64_t* c) {
-      for (int d = 0; d < dim_; ++d)
-        if (c[d] < 0 || c[d] >= n_[d]) return false;
-      return true;
-    };
+    const int64_t* n = L.n;
     int64_t zlo = dim_ == 3 ? std::max<int64_t>(lo[2], 0) : 0;
-    int64_t zhi = dim_ == 3 ? std::min<int64_t>(hi[2], n_[2] - 1) : 0;
-    int64_t ylo = std::max<int64_t>(lo[1], 0), yhi = std::min<int64_t>(hi[1], n_[1] - 1);
-    int64_t xlo = std::max<int64_t>(lo[0], 0), xhi = std::min<int64_t>(hi[0], n_[0] - 1);
+    int64_t zhi = dim_ == 3 ? std::min<int64_t>(hi[2], n[2] - 1) : 0;
+    int64_t ylo = std::max<int64_t>(lo[1], 0), yhi = std::min<int64_t>(hi[1], n[1] - 1);
+    int64_t xlo = std::max<int64_t>(lo[0], 0), xhi = std::min<int64_t>(hi[0], n[0] - 1);
     for (int64_t z = zlo; z <= zhi; ++z) {
       bool zface = dim_ == 3 && (z == lo[2] || z == hi[2]);
       for (int64_t y = ylo; y <= yhi; ++y) {
         bool yface = (y == lo[1] || y == hi[1]);
         if (zface || yface || r == 0) {
-          for (int64_t x = xlo; x <= xhi; ++x) {
-            int64_t c[3] = {x, y, z};
-            if (inside(c)) f(x + n_[0] * (y + n_[1] * z));
-          }
+          for (int64_t x = xlo; x <= xhi; ++x) f(x + n[0] * (y + n[1] * z));
         } else {
-          if (lo[0] >= 0) f(lo[0] + n_[0] * (y + n_[1] * z));
-          if (hi[0] < n_[0] && hi[0] != lo[0]) f(hi[0] + n_[0] * (y + n_[1] * z));
+          if (lo[0] >= 0) f(lo[0] + n[0] * (y + n[1] * z));
+          if (hi[0] < n[0] && hi[0] != lo[0]) f(hi[0] + n[0] * (y + n[1] * z));
         }
       }
     }
   }
   int dim_;
   double lo_[3], hi_[3];
-  double cell_ = 1.0;
-  int64_t n_[3] = {1, 1, 1};
-  std::vector<int64_t> head_, next_;
+  std::vector<Level> levels_;
   std::vector<double> pts_;
 };
 

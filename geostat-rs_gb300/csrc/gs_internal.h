@@ -9,6 +9,9 @@
 
 namespace gs {
 
+// Counts kernels this library launched (reported by gs_launch_count).
+void count_launch(int n);
+
 // Initialises the device (and keeps the stream-ordered memory pool from
 // returning memory to the driver between calls).
 int ensure_device();

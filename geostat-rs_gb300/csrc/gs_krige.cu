@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "gs_internal.h"
 #include "gs_krige.cuh"
 #include "gs_solve.cuh"
 
@@ -422,6 +423,7 @@ int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   const int blocks = (int)std::min<int64_t>(want, (int64_t)sms * per_sm * 8);
   kern<<<blocks, wpb * 32, smem, stream>>>(a, m, g_tab, g_kc, flag, per_warp);
   GS_CUDA(cudaGetLastError());
+  count_launch(1);
   return GS_OK;
 }
 
@@ -447,6 +449,7 @@ int krige_fp64_launch(const KrigeArgs& a, const DevModel& m, double* scratch, in
   if (a.dim == 2) krige_fp64_kernel<2><<<blocks, tpb, 0, stream>>>(a, m, scratch, Tl);
   else krige_fp64_kernel<3><<<blocks, tpb, 0, stream>>>(a, m, scratch, Tl);
   GS_CUDA(cudaGetLastError());
+  count_launch(1);
   return GS_OK;
 }
 

@@ -1,0 +1,70 @@
+// gs_probe.cu -- measurement helpers: CUDA-core FMA throughput (the roofline
+// denominator of the per-system kernels, which run on the FP32 pipe with a
+// little FP64) and the count of this library's kernel launches.
+#include <algorithm>
+#include <atomic>
+
+#include "gs_common.cuh"
+#include "gs_internal.h"
+
+namespace gs {
+
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches += n; }
+
+namespace {
+
+// Eight independent FMA chains per thread; the result is stored so the
+// chains cannot be removed.
+template <class T>
+__global__ void fma_probe(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+  T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+    x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <class T>
+int probe(double* tflops, int iters) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 256, blocks = sms * 8;
+  T* out = nullptr;
+  GS_CUDA(cudaMalloc(&out, sizeof(T) * threads * blocks));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0);
+    fma_probe<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaError_t err = cudaGetLastError();
+  cudaFree(out);
+  if (err != cudaSuccess) return cuda_fail(err, "fma probe", __FILE__, __LINE__);
+  const double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return GS_OK;
+}
+
+}  // namespace
+}  // namespace gs
+
+extern "C" int gs_probe_fma_tflops(int precision, double* tflops) {
+  GS_TRY(gs::ensure_device());
+  if (precision == GS_PREC_FP64) return gs::probe<double>(tflops, 1 << 13);
+  return gs::probe<float>(tflops, 1 << 16);
+}
+
+extern "C" int64_t gs_launch_count(void) { return gs::g_launches.load(); }

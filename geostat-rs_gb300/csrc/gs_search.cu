@@ -22,6 +22,7 @@
 #include <cstring>
 #include <vector>
 
+#include "gs_internal.h"
 #include "gs_search.cuh"
 
 namespace gs {
@@ -622,6 +623,7 @@ int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p
     GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<blocks, wpb * 32, smem, stream>>>(g.dev, frame, p, nt, tx, ty, tz, nb, nbc);
     GS_CUDA(cudaGetLastError());
+    count_launch(1);
     return GS_OK;
   };
   if (p.ranked) {

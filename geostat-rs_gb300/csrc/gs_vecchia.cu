@@ -456,6 +456,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     const int blocks = (int)std::min<int64_t>((n + wpb - 1) / wpb, 152 * 64);
     kern<<<blocks, wpb * 32, smem, s>>>(a, g_vtab, g_vkc, per_warp);
     GS_CUDA(cudaGetLastError());
+    count_launch(1);
     // compact flagged (candidate, point) pairs
     DevBuf nsel, tmp;
     GS_TRY(nsel.alloc(8, s));
@@ -487,6 +488,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
       vecchia_fp64_kernel<3><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
                                                     work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
     GS_CUDA(cudaGetLastError());
+    count_launch(1);
   }
   const int64_t chunk = 8192;
   const int nblk = (int)((n + chunk - 1) / chunk);
@@ -495,6 +497,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   reduce_terms<<<dim3(nblk, (unsigned)ncand), 256, 0, s>>>((double*)terms.ptr, n, chunk, (double*)partial.ptr);
   reduce_partials<<<(int)((ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)ncand, (double*)out.ptr);
   GS_CUDA(cudaGetLastError());
+  count_launch(2);
   std::vector<double> hll(ncand);
   std::vector<int32_t> hst(ncand);
   GS_CUDA(cudaMemcpyAsync(hll.data(), out.ptr, ncand * 8, cudaMemcpyDeviceToHost, s));

@@ -84,6 +84,8 @@ SIGNATURES = {
     "gs_rng_normal": (None, [_u64, _i64, _pd]),
     "gs_synth_rff_field": (_int, [_int, _i64, _pd, _pd, _pd, _pm, _i64, _u64, _pd]),
     "gs_last_timings": (_int, [_pd]),
+    "gs_probe_fma_tflops": (_int, [_int, _pd]),
+    "gs_launch_count": (_i64, []),
 }
 
 _lib = None

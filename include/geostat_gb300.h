@@ -227,6 +227,13 @@ int gs_synth_rff_field(int dim, int64_t n, const double* x, const double* y, con
  * [0] search, [1] mixed solve, [2] FP64 re-solve, [3] whole call. */
 int gs_last_timings(double* ms4);
 
+/* Measurement helpers (no reference counterpart): sustained CUDA-core FMA
+ * throughput in TFLOP/s for FP32 (precision 0) or FP64 (1) -- the roofline
+ * denominator of the per-system kernels -- and the number of kernels this
+ * library has launched since it was loaded. */
+int gs_probe_fma_tflops(int precision, double* tflops);
+int64_t gs_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif
