@@ -453,6 +453,34 @@ def run_reference(args, rank, world):
                     "d2h_bytes_per_step": 0}}
 
 
+def profile_case(args):
+    """Small fixed case for ncu: the benchmark's data, a prefix of its targets."""
+    import torch
+    import geostat_rs as G
+    if args.profile_case:
+        coords = make_coords()
+        model = make_model()
+        values = G.rff_field(coords, model, 4096, SEED + 1)
+        kr = G.Kriging.new(G.PointSet(coords, values), model, G.KrigingConfig(max_neighbors=K_NEIGH))
+        tg = grid_targets()[:args.profile_case]
+        for _ in range(2):
+            v, var = kr.predict_many(tg)
+        torch.cuda.synchronize()
+        print(f"profile case: {len(tg)} targets, mean estimate {np.nanmean(v):.6f}")
+    if args.profile_vecchia:
+        from geostat_rs.model import Structure, VariogramModel
+        n = args.profile_vecchia
+        c = G.rng_uniform(SEED + 5, 2 * n).reshape(n, 2)
+        base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
+        v = 0.5 + G.rff_field(c, base, 1024, SEED + 6)
+        plan = G.VecchiaPlan(G.PointSet(c, v), 30)
+        cands = [VariogramModel(0.02 * (1 + 0.05 * i), [Structure("matern25", 1.0, 0.05)])
+                 for i in range(16)]
+        for _ in range(2):
+            ll, st = plan.loglik(cands)
+        print(f"profile vecchia: {n} points, loglik[0] {ll[0]:.6f}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -463,6 +491,11 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--vecchia-n", type=int, default=2_000_000)
     ap.add_argument("--no-vecchia", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0,
+                    help="run one mixed-precision pass over the first N grid targets and exit "
+                         "(the small case for ncu captures)")
+    ap.add_argument("--profile-vecchia", type=int, default=0,
+                    help="run one 16-candidate Vecchia batch on N points and exit")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -470,6 +503,9 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
+    if args.profile_case or args.profile_vecchia:
+        profile_case(args)
+        return
     if args.impl == "reference":
         res = run_reference(args, rank, world)
     else:

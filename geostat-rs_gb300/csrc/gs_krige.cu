@@ -22,6 +22,7 @@
 
 #include "gs_internal.h"
 #include "gs_krige.cuh"
+#include "gs_cta.cuh"
 #include "gs_solve.cuh"
 
 namespace gs {
@@ -61,36 +62,68 @@ __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
   }
 }
 
-template <int D>
-__global__ void __launch_bounds__(128) krige_mixed_kernel(KrigeArgs a, DevModel m, ExpTable tab_g,
-                                                          DfConsts kc, uint8_t* flag,
-                                                          size_t per_warp) {
+// Shared-memory layout of one system (see mixed_smem_bytes).
+struct MixedLayout {
+  int np, nbr;
+  size_t off_a, off_v, off_b, off_xd, off_x, off_z, off_red, off_l, off_w, off_di, off_col,
+      off_flag, total;
+};
+
+__host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
+  MixedLayout L;
+  L.np = nmax * (nmax + 1) / 2;
+  L.nbr = (nmax + 3) / 4;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = o;
+    o += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  L.off_a = take((size_t)L.np * sizeof(df));
+  L.off_v = take((size_t)nf * GS_MIXED_MAX_NEIGHBORS * dim * sizeof(df));
+  L.off_b = take((size_t)nmax * sizeof(df));
+  L.off_xd = take((size_t)nmax * sizeof(df));
+  L.off_x = take((size_t)nmax * sizeof(double));
+  L.off_z = take((size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(double));
+  L.off_red = take(16 * sizeof(double));
+  L.off_l = take((size_t)L.np * sizeof(float));
+  L.off_w = take((size_t)nmax * sizeof(float));
+  L.off_di = take((size_t)nmax * sizeof(float));
+  L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
+  L.off_flag = take(16);
+  L.total = o;
+  return L;
+}
+
+template <int D, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevModel m, ExpTable tab_g,
+                                                            DfConsts kc, uint8_t* flag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+  for (int i = threadIdx.x; i < 64; i += BLOCK) {
     tab.hi[i] = tab_g.hi[i];
     tab.lo[i] = tab_g.lo[i];
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
-  const int NMAX = a.nmax;
-  const int NP = (NMAX * (NMAX + 1)) >> 1;
+  const int tid = threadIdx.x;
   const Frames fr = frames_of(m);
   const int NBMAX = GS_MIXED_MAX_NEIGHBORS;
-  unsigned char* base = smem_raw + (size_t)wib * per_warp;
-  df* A = reinterpret_cast<df*>(base);
-  df* V = A + NP;                                   // [frame][i][d]
-  df* B = V + fr.nf * NBMAX * D;                    // rhs
-  df* XD = B + NMAX;                                // x as df
-  double* X = reinterpret_cast<double*>(XD + NMAX); // FP64 solution
-  double* Z = X + NMAX;                             // neighbour values
-  float* L = reinterpret_cast<float*>(Z + NBMAX);
-  float* W = L + NP;
-  float* DI = W + NMAX;
+  const MixedLayout lay = mixed_layout(a.nmax, fr.nf, D);
+  df* A = reinterpret_cast<df*>(smem_raw + lay.off_a);
+  df* V = reinterpret_cast<df*>(smem_raw + lay.off_v);
+  df* B = reinterpret_cast<df*>(smem_raw + lay.off_b);
+  CtaScratch S;
+  S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
+  S.X = reinterpret_cast<double*>(smem_raw + lay.off_x);
+  double* Z = reinterpret_cast<double*>(smem_raw + lay.off_z);
+  S.red = reinterpret_cast<double*>(smem_raw + lay.off_red);
+  S.L = reinterpret_cast<float*>(smem_raw + lay.off_l);
+  S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
+  S.DI = reinterpret_cast<float*>(smem_raw + lay.off_di);
+  S.colU = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
+  __syncthreads();
 
-  for (int64_t it = (int64_t)blockIdx.x * wpb + wib; it < a.ntl; it += (int64_t)gridDim.x * wpb) {
+  for (int64_t it = blockIdx.x; it < a.ntl; it += gridDim.x) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
     const int n = a.nbc[t];
     const int p = a.p;
@@ -99,7 +132,7 @@ __global__ void __launch_bounds__(128) krige_mixed_kernel(KrigeArgs a, DevModel 
     else if (n < a.min_nb) st = GS_ST_NO_NEIGHBORS;
     else if (n < p) st = GS_ST_INSUFFICIENT_DATA;
     if (st != GS_ST_OK) {
-      if (lane == 0) {
+      if (tid == 0) {
         a.out_v[t] = __longlong_as_double(0x7ff8000000000000ll);
         a.out_var[t] = __longlong_as_double(0x7ff8000000000000ll);
         if (a.out_lag) a.out_lag[t] = __longlong_as_double(0x7ff8000000000000ll);
@@ -109,16 +142,15 @@ __global__ void __launch_bounds__(128) krige_mixed_kernel(KrigeArgs a, DevModel 
       continue;
     }
     if (n > NBMAX) {
-      if (lane == 0) flag[t] = 1;
-      __syncwarp();
+      if (tid == 0) flag[t] = 1;
       continue;
     }
     const int N = n + p;
-    double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
-    // --- per-neighbour data: frames, values, rhs, drift rows -----------
-    for (int i = lane; i < n; i += 32) {
+    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+    // --- per-neighbour data: frames, values, rhs, diagonal, drift rows ---
+    for (int i = tid; i < n; i += BLOCK) {
       const int idx = a.nb[t * (int64_t)a.kout + i];
-      double pp[3] = {a.x[idx], a.y[idx], D == 3 ? a.z[idx] : 0.0};
+      const double pp[3] = {a.x[idx], a.y[idx], D == 3 ? a.z[idx] : 0.0};
       double u[3];
       bool zero = true;
 #pragma unroll
@@ -133,7 +165,6 @@ __global__ void __launch_bounds__(128) krige_mixed_kernel(KrigeArgs a, DevModel 
       frame_coords<D>(m, fr, ud, V, NBMAX, i, h);
       B[i] = zero ? m.c0_df : cov_from_h(m, fr, h, tab, kc);
       Z[i] = a.val[idx];
-      // diagonal and drift entries of row i
       df diag = m.c0_df;
       if (a.meas_err) diag = df_add(diag, df_from_double(a.meas_err[idx]));
       A[pk(i, i)] = diag;
@@ -143,70 +174,72 @@ __global__ void __launch_bounds__(128) krige_mixed_kernel(KrigeArgs a, DevModel 
         for (int k = 0; k < p; ++k) A[pk(n + k, i)] = df_from_double(f[k]);
       }
     }
-    if (lane < p) {
+    if (tid < p) {
       double f[GS_MIXED_MAX_DRIFT];
       fill_basis<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, f);
-      B[n + lane] = df_from_double(f[lane]);
+      B[n + tid] = df_from_double(f[tid]);
     }
-    for (int q = lane; q < p * (p + 1) / 2; q += 32) {
+    for (int q = tid; q < p * (p + 1) / 2; q += BLOCK) {
       int r = 0;
       while ((r + 1) * (r + 2) / 2 <= q) ++r;
-      int c = q - r * (r + 1) / 2;
+      const int c = q - r * (r + 1) / 2;
       A[pk(n + r, n + c)] = df_make(0.0f, 0.0f);
     }
-    __syncwarp();
-    // --- covariance block, strictly lower part -------------------------
+    __syncthreads();
+    // --- covariance block, strictly lower part ---------------------------
     {
       const int npairs = (n * (n - 1)) >> 1;
-      int i = 1, j = lane;
+      int i = 1, j = tid;
       while (j >= i && i < n) {
         j -= i;
         ++i;
       }
-      for (int q = lane; q < npairs; q += 32) {
+      for (int q = tid; q < npairs; q += BLOCK) {
         df h[GS_MAX_STRUCTURES + 1];
         for (int f = 0; f < fr.nf; ++f)
           h[f] = norm_df<D>(&V[(f * NBMAX + i) * D], &V[(f * NBMAX + j) * D]);
         A[pk(i, j)] = cov_from_h(m, fr, h, tab, kc);
-        j += 32;
+        j += BLOCK;
         while (j >= i && i < n) {
           j -= i;
           ++i;
         }
       }
     }
-    __syncwarp();
-    // --- FP32 L D L^T, FP64-accumulated refinement --------------------
-    const bool bad = !ldl_refine_solve(A, B, L, DI, W, X, XD, N, lane);
-    if (bad) {
-      if (lane == 0) flag[t] = 1;
-      __syncwarp();
+    __syncthreads();
+    // --- FP32 L D L^T, FP64-accumulated refinement -----------------------
+    bool ok = cta_ldl<BLOCK>(A, N, S);
+    if (ok) ok = cta_refine<BLOCK>(A, B, N, S);
+    if (!ok) {
+      if (tid == 0) flag[t] = 1;
+      __syncthreads();
       continue;
     }
-    // --- outputs (FP64) ------------------------------------------------
-    double sv = 0.0, sr = 0.0;
-    if (a.method == GS_SIMPLE) {
-      for (int i = lane; i < n; i += 32) {
-        sv += X[i] * (Z[i] - a.sk_mean);
-        sr += X[i] * df_to_double(B[i]);
+    // --- outputs (FP64) ---------------------------------------------------
+    if (tid < 32) {
+      double sv = 0.0, sr = 0.0;
+      if (a.method == GS_SIMPLE) {
+        for (int i = tid; i < n; i += 32) {
+          sv += S.X[i] * (Z[i] - a.sk_mean);
+          sr += S.X[i] * df_to_double(B[i]);
+        }
+      } else {
+        for (int i = tid; i < n; i += 32) sv += S.X[i] * Z[i];
+        for (int i = tid; i < N; i += 32) sr += S.X[i] * df_to_double(B[i]);
       }
-    } else {
-      for (int i = lane; i < n; i += 32) sv += X[i] * Z[i];
-      for (int i = lane; i < N; i += 32) sr += X[i] * df_to_double(B[i]);
+      sv = warp_sum_d(sv);
+      sr = warp_sum_d(sr);
+      if (tid == 0) {
+        const double val = a.method == GS_SIMPLE ? a.sk_mean + sv : sv;
+        a.out_v[t] = val;
+        a.out_var[t] = fmax(m.c0 - sr, 0.0);
+        if (a.out_lag)
+          a.out_lag[t] = a.method == GS_SIMPLE ? __longlong_as_double(0x7ff8000000000000ll) : S.X[n];
+        a.out_st[t] = GS_ST_OK;
+        flag[t] = 0;
+      }
     }
-    sv = warp_sum_d(sv);
-    sr = warp_sum_d(sr);
-    if (lane == 0) {
-      const double val = a.method == GS_SIMPLE ? a.sk_mean + sv : sv;
-      const double var = fmax(m.c0 - sr, 0.0);
-      a.out_v[t] = val;
-      a.out_var[t] = var;
-      if (a.out_lag)
-        a.out_lag[t] = a.method == GS_SIMPLE ? __longlong_as_double(0x7ff8000000000000ll) : X[n];
-      a.out_st[t] = GS_ST_OK;
-      flag[t] = 0;
-    }
-    __syncwarp();
+    __syncthreads();
   }
 }
 
@@ -387,44 +420,39 @@ static void ensure_tables() {
   }
 }
 
-size_t mixed_per_warp_bytes(int nmax, int nf, int dim) {
-  const int NP = nmax * (nmax + 1) / 2;
-  size_t bytes = 0;
-  bytes += (size_t)NP * sizeof(df);                                 // A
-  bytes += (size_t)nf * GS_MIXED_MAX_NEIGHBORS * dim * sizeof(df);  // V
-  bytes += (size_t)nmax * sizeof(df) * 2;                           // B, XD
-  bytes += (size_t)nmax * sizeof(double);                           // X
-  bytes += (size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(double);         // Z
-  bytes += (size_t)NP * sizeof(float);                              // L
-  bytes += (size_t)nmax * sizeof(float) * 2;                        // W, DI
-  return (bytes + 15) & ~(size_t)15;
-}
-
-int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int warps_per_block,
+int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int /*unused*/,
                        cudaStream_t stream) {
   if (a.ntl == 0) return GS_OK;
   ensure_tables();
   int nf = 1;
   for (int s = 0; s < m.ns; ++s) nf += m.s[s].aniso ? 1 : 0;
-  const size_t per_warp = mixed_per_warp_bytes(a.nmax, nf, a.dim);
-  int wpb = std::max(1, warps_per_block);
-  while (wpb > 1 && per_warp * wpb > 200 * 1024) --wpb;
-  const size_t smem = per_warp * wpb;
-  if (smem > 220 * 1024) return fail(GS_ERR_INVALID_PARAMETER, "system too large for the mixed kernel");
+  const MixedLayout lay = mixed_layout(a.nmax, nf, a.dim);
+  const size_t smem = lay.total;
+  if (smem > 200 * 1024) return fail(GS_ERR_INVALID_PARAMETER, "system too large for the mixed kernel");
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  auto kern = a.dim == 2 ? krige_mixed_kernel<2> : krige_mixed_kernel<3>;
-  GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * 32, smem));
-  per_sm = std::max(per_sm, 1);
-  const int64_t want = (a.ntl + wpb - 1) / wpb;
-  const int blocks = (int)std::min<int64_t>(want, (int64_t)sms * per_sm * 8);
-  kern<<<blocks, wpb * 32, smem, stream>>>(a, m, g_tab, g_kc, flag, per_warp);
-  GS_CUDA(cudaGetLastError());
-  count_launch(1);
-  return GS_OK;
+  const int nbr = lay.nbr;
+  const int tiles = nbr * (nbr + 1) / 2;
+  auto go = [&](auto kern, int block) -> int {
+    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+    per_sm = std::max(per_sm, 1);
+    const int blocks = (int)std::min<int64_t>(a.ntl, (int64_t)sms * per_sm);
+    kern<<<blocks, block, smem, stream>>>(a, m, g_tab, g_kc, flag);
+    GS_CUDA(cudaGetLastError());
+    count_launch(1);
+    return GS_OK;
+  };
+  if (a.dim == 2) {
+    if (tiles <= 64) return go(krige_mixed_kernel<2, 64>, 64);
+    if (tiles <= 128) return go(krige_mixed_kernel<2, 128>, 128);
+    return go(krige_mixed_kernel<2, 256>, 256);
+  }
+  if (tiles <= 64) return go(krige_mixed_kernel<3, 64>, 64);
+  if (tiles <= 128) return go(krige_mixed_kernel<3, 128>, 128);
+  return go(krige_mixed_kernel<3, 256>, 256);
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {

@@ -119,96 +119,4 @@ __device__ __forceinline__ void ldl_solve(const float* L, const float* DI, float
   }
 }
 
-// Factors hi(A) into L/DI and solves A X = B with refinement.  Returns false
-// when a pivot is too small for FP32 or the refinement does not contract to
-// ~1e-13 relative within four sweeps (the caller re-solves in FP64).
-__device__ __noinline__ static bool ldl_refine_solve(const df* A, const df* B, float* L, float* DI, float* W,
-                                 double* X, df* XD, int N, int lane) {
-  float amax = 0.0f;
-  const int NP = (N * (N + 1)) >> 1;
-  for (int q = lane; q < NP; q += 32) {
-    const float v = A[q].hi;
-    L[q] = v;
-    amax = fmaxf(amax, fabsf(v));
-  }
-  amax = warp_max_f(amax);
-  __syncwarp();
-  const float tol = 1e-6f * amax;
-  for (int k = 0; k < N; ++k) {
-    const float d = L[pk(k, k)];
-    if (!(fabsf(d) > tol)) return false;
-    const float id = 1.0f / d;
-    if (lane == 0) DI[k] = id;
-    const int mrows = N - 1 - k;
-    // rows q and 63-q pair up so every lane does a similar amount of work
-    for (int pass = 0; pass < 2; ++pass) {
-      for (int qq = pass == 0 ? lane : 63 - lane; qq < mrows; qq += 64) {
-        const int i = k + 1 + qq;
-        const float lik = L[pk(i, k)] * id;
-        float* Li = L + pk(i, 0);
-        for (int jj = k + 1; jj <= i; ++jj) Li[jj] = fmaf(-lik, L[pk(jj, k)], Li[jj]);
-      }
-    }
-    __syncwarp();
-    for (int i = k + 1 + lane; i < N; i += 32) L[pk(i, k)] *= id;
-    __syncwarp();
-  }
-  for (int i = lane; i < N; i += 32) W[i] = B[i].hi;
-  __syncwarp();
-  ldl_solve(L, DI, W, N, lane);
-  double nx = 0.0;
-  for (int i = lane; i < N; i += 32) {
-    const double xi = (double)W[i];
-    X[i] = xi;
-    XD[i] = df_from_double(xi);
-    nx = fmax(nx, fabs(xi));
-  }
-  nx = warp_max_d(nx);
-  __syncwarp();
-  double nd_prev = nx;
-  for (int sweep = 1; sweep <= 4; ++sweep) {
-    for (int i = lane; i < N; i += 32) {
-      float s = B[i].hi, c = B[i].lo;
-      for (int jj = 0; jj < N; ++jj) {
-        const df aij = jj <= i ? A[pk(i, jj)] : A[pk(jj, i)];
-        const df xj = XD[jj];
-        // TwoProduct / TwoSum written with explicit roundings so the
-        // compiler cannot contract them into FMAs
-        const float ph = __fmul_rn(-aij.hi, xj.hi);
-        float pe = __fmaf_rn(-aij.hi, xj.hi, -ph);
-        pe = __fmaf_rn(-aij.hi, xj.lo, pe);
-        pe = __fmaf_rn(-aij.lo, xj.hi, pe);
-        const float tsum = __fadd_rn(s, ph);
-        const float bb = __fsub_rn(tsum, s);
-        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
-        s = tsum;
-        c += e + pe;
-      }
-      W[i] = s + c;
-    }
-    __syncwarp();
-    ldl_solve(L, DI, W, N, lane);
-    double nd = 0.0;
-    nx = 0.0;
-    for (int i = lane; i < N; i += 32) {
-      const double dlt = (double)W[i];
-      const double xi = X[i] + dlt;
-      X[i] = xi;
-      XD[i] = df_from_double(xi);
-      nd = fmax(nd, fabs(dlt));
-      nx = fmax(nx, fabs(xi));
-    }
-    nd = warp_max_d(nd);
-    nx = warp_max_d(nx);
-    __syncwarp();
-    if (nd <= 1e-15 * nx) return true;
-    if (sweep >= 2) {
-      const double rho = nd / nd_prev;
-      if (rho < 0.5 && rho * nd <= 1e-13 * nx) return true;
-    }
-    nd_prev = nd;
-  }
-  return false;
-}
-
 }  // namespace gs

@@ -26,6 +26,7 @@
 #include "gs_host.h"
 #include "gs_internal.h"
 #include "gs_search.cuh"
+#include "gs_cta.cuh"
 #include "gs_solve.cuh"
 
 struct gs_vecchia_plan {
@@ -89,107 +90,125 @@ struct VArgs {
 
 constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
 
-size_t vecchia_per_warp_bytes(int m, int dim) {
-  const int NP = m * (m + 1) / 2;
-  size_t b = 0;
-  b += (size_t)NP * sizeof(df) * 2;                       // A, H (cached norms)
-  b += (size_t)(GS_MAX_STRUCTURES + 1) * m * dim * sizeof(df);  // V
-  b += (size_t)m * sizeof(df) * 3;                        // B, XD, H0
-  b += (size_t)m * sizeof(double) * 2;                    // X, Z
-  b += (size_t)NP * sizeof(float);                        // L
-  b += (size_t)m * sizeof(float) * 2;                     // W, DI
-  return (b + 15) & ~(size_t)15;
+struct VLayout {
+  int np, nbr;
+  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_x, off_z, off_red, off_l, off_w, off_di,
+      off_col, off_flag, total;
+};
+
+__host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
+  VLayout L;
+  L.np = m * (m + 1) / 2;
+  L.nbr = (m + 3) / 4;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = o;
+    o += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  L.off_a = take((size_t)L.np * sizeof(df));
+  L.off_h = take((size_t)L.np * sizeof(df));
+  L.off_v = take((size_t)(GS_MAX_STRUCTURES + 1) * m * dim * sizeof(df));
+  L.off_b = take((size_t)m * sizeof(df));
+  L.off_xd = take((size_t)m * sizeof(df));
+  L.off_h0 = take((size_t)m * sizeof(df));
+  L.off_x = take((size_t)m * sizeof(double));
+  L.off_z = take((size_t)m * sizeof(double));
+  L.off_red = take(16 * sizeof(double));
+  L.off_l = take((size_t)L.np * sizeof(float));
+  L.off_w = take((size_t)m * sizeof(float));
+  L.off_di = take((size_t)m * sizeof(float));
+  L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
+  L.off_flag = take(16);
+  L.total = o;
+  return L;
 }
 
-template <int D>
-__global__ void __launch_bounds__(128) vecchia_loglik_kernel(VArgs a, ExpTable tab_g, DfConsts kc,
-                                                             size_t per_warp) {
+template <int D, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable tab_g,
+                                                               DfConsts kc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+  for (int i = threadIdx.x; i < 64; i += BLOCK) {
     tab.hi[i] = tab_g.hi[i];
     tab.lo[i] = tab_g.lo[i];
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
+  const int tid = threadIdx.x;
   const int M = a.m;
-  const int NP = (M * (M + 1)) >> 1;
-  unsigned char* base = smem_raw + (size_t)wib * per_warp;
-  df* A = reinterpret_cast<df*>(base);
-  df* H = A + NP;
-  df* V = H + NP;
-  df* B = V + (GS_MAX_STRUCTURES + 1) * M * D;
-  df* XD = B + M;
-  df* H0 = XD + M;
-  double* X = reinterpret_cast<double*>(H0 + M);
-  double* Z = X + M;
-  float* L = reinterpret_cast<float*>(Z + M);
-  float* W = L + NP;
-  float* DI = W + M;
+  const VLayout lay = vecchia_layout(M, D);
+  df* A = reinterpret_cast<df*>(smem_raw + lay.off_a);
+  df* H = reinterpret_cast<df*>(smem_raw + lay.off_h);
+  df* V = reinterpret_cast<df*>(smem_raw + lay.off_v);
+  df* B = reinterpret_cast<df*>(smem_raw + lay.off_b);
+  df* H0 = reinterpret_cast<df*>(smem_raw + lay.off_h0);
+  double* Z = reinterpret_cast<double*>(smem_raw + lay.off_z);
+  CtaScratch S;
+  S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
+  S.X = reinterpret_cast<double*>(smem_raw + lay.off_x);
+  S.red = reinterpret_cast<double*>(smem_raw + lay.off_red);
+  S.L = reinterpret_cast<float*>(smem_raw + lay.off_l);
+  S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
+  S.DI = reinterpret_cast<float*>(smem_raw + lay.off_di);
+  S.colU = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
+  __syncthreads();
 
-  for (int64_t k = (int64_t)blockIdx.x * wpb + wib; k < a.n; k += (int64_t)gridDim.x * wpb) {
+  for (int64_t k = blockIdx.x; k < a.n; k += gridDim.x) {
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
     const double zi = a.v[i] - a.mean;
     if (s == 0) {
       // first point: marginal N(0, sill)
-      for (int c = lane; c < a.ncand; c += 32) {
+      for (int c = tid; c < a.ncand; c += BLOCK) {
         const double sill = a.models[c].c0;
         a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
         a.flag[(int64_t)c * a.n + k] = 0;
       }
       continue;
     }
-    if (s > M) {
-      for (int c = lane; c < a.ncand; c += 32) a.flag[(int64_t)c * a.n + k] = 1;
-      continue;
-    }
-    double pi[3] = {a.x[i], a.y[i], D == 3 ? a.z[i] : 0.0};
-    // separations to the point, identity frame (df) and values
-    for (int q = lane; q < s; q += 32) {
+    const double pi[3] = {a.x[i], a.y[i], D == 3 ? a.z[i] : 0.0};
+    for (int q = tid; q < s; q += BLOCK) {
       const int j = a.nb[k * (int64_t)M + q];
-      double u[3] = {a.x[j] - pi[0], a.y[j] - pi[1], D == 3 ? a.z[j] - pi[2] : 0.0};
+      const double u[3] = {a.x[j] - pi[0], a.y[j] - pi[1], D == 3 ? a.z[j] - pi[2] : 0.0};
 #pragma unroll
       for (int d = 0; d < D; ++d) V[q * D + d] = df_from_double(u[d]);
       Z[q] = a.v[j] - a.mean;
     }
-    __syncwarp();
+    __syncthreads();
     const int npairs = (s * (s - 1)) >> 1;
     if (a.iso_shared) {
-      for (int q = lane; q < s; q += 32) H0[q] = norm0_df<D>(&V[q * D]);
-      int ii = 1, jj = lane;
+      for (int q = tid; q < s; q += BLOCK) H0[q] = norm0_df<D>(&V[q * D]);
+      int ii = 1, jj = tid;
       while (jj >= ii && ii < s) {
         jj -= ii;
         ++ii;
       }
-      for (int q = lane; q < npairs; q += 32) {
+      for (int q = tid; q < npairs; q += BLOCK) {
         H[pk(ii, jj)] = norm_df<D>(&V[ii * D], &V[jj * D]);
-        jj += 32;
+        jj += BLOCK;
         while (jj >= ii && ii < s) {
           jj -= ii;
           ++ii;
         }
       }
-      __syncwarp();
+      __syncthreads();
     }
     for (int c = 0; c < a.ncand; ++c) {
       const DevModel& mdl = a.models[c];
       const Frames fr = frames_of(mdl);
       if (a.iso_shared) {
-        for (int q = lane; q < s; q += 32) {
+        for (int q = tid; q < s; q += BLOCK) {
           B[q] = cov_from_h(mdl, fr, &H0[q], tab, kc);
           A[pk(q, q)] = mdl.c0_df;
         }
-        int ii = 1, jj = lane;
+        int ii = 1, jj = tid;
         while (jj >= ii && ii < s) {
           jj -= ii;
           ++ii;
         }
-        for (int q = lane; q < npairs; q += 32) {
+        for (int q = tid; q < npairs; q += BLOCK) {
           A[pk(ii, jj)] = cov_from_h(mdl, fr, &H[pk(ii, jj)], tab, kc);
-          jj += 32;
+          jj += BLOCK;
           while (jj >= ii && ii < s) {
             jj -= ii;
             ++ii;
@@ -197,7 +216,7 @@ __global__ void __launch_bounds__(128) vecchia_loglik_kernel(VArgs a, ExpTable t
         }
       } else {
         df* VF = V + M * D;  // frames 1.. (frame 0 is V itself)
-        for (int q = lane; q < s; q += 32) {
+        for (int q = tid; q < s; q += BLOCK) {
           df hq[GS_MAX_STRUCTURES + 1];
           hq[0] = norm0_df<D>(&V[q * D]);
           for (int st = 0; st < mdl.ns; ++st) {
@@ -208,7 +227,8 @@ __global__ void __launch_bounds__(128) vecchia_loglik_kernel(VArgs a, ExpTable t
             for (int r = 0; r < D; ++r) {
               df acc = df_make(0.0f, 0.0f);
 #pragma unroll
-              for (int cc = 0; cc < D; ++cc) acc = df_add(acc, df_mul(mdl.s[st].rot_df[r * 3 + cc], V[q * D + cc]));
+              for (int cc = 0; cc < D; ++cc)
+                acc = df_add(acc, df_mul(mdl.s[st].rot_df[r * 3 + cc], V[q * D + cc]));
               acc3[r] = acc;
               VF[((f - 1) * M + q) * D + r] = acc;
             }
@@ -217,46 +237,49 @@ __global__ void __launch_bounds__(128) vecchia_loglik_kernel(VArgs a, ExpTable t
           B[q] = cov_from_h(mdl, fr, hq, tab, kc);
           A[pk(q, q)] = mdl.c0_df;
         }
-        __syncwarp();
-        int ii = 1, jj = lane;
+        __syncthreads();
+        int ii = 1, jj = tid;
         while (jj >= ii && ii < s) {
           jj -= ii;
           ++ii;
         }
-        for (int q = lane; q < npairs; q += 32) {
+        for (int q = tid; q < npairs; q += BLOCK) {
           df h[GS_MAX_STRUCTURES + 1];
           h[0] = norm_df<D>(&V[ii * D], &V[jj * D]);
           for (int f = 1; f < fr.nf; ++f)
             h[f] = norm_df<D>(&VF[((f - 1) * M + ii) * D], &VF[((f - 1) * M + jj) * D]);
           A[pk(ii, jj)] = cov_from_h(mdl, fr, h, tab, kc);
-          jj += 32;
+          jj += BLOCK;
           while (jj >= ii && ii < s) {
             jj -= ii;
             ++ii;
           }
         }
       }
-      __syncwarp();
-      const bool ok = ldl_refine_solve(A, B, L, DI, W, X, XD, s, lane);
+      __syncthreads();
+      bool ok = cta_ldl<BLOCK>(A, s, S);
+      if (ok) ok = cta_refine<BLOCK>(A, B, s, S);
       if (!ok) {
-        if (lane == 0) a.flag[(int64_t)c * a.n + k] = 1;
-        __syncwarp();
+        if (tid == 0) a.flag[(int64_t)c * a.n + k] = 1;
+        __syncthreads();
         continue;
       }
-      double mu = 0.0, red = 0.0;
-      for (int q = lane; q < s; q += 32) {
-        mu += X[q] * Z[q];
-        red += X[q] * df_to_double(B[q]);
+      if (tid < 32) {
+        double mu = 0.0, red = 0.0;
+        for (int q = tid; q < s; q += 32) {
+          mu += S.X[q] * Z[q];
+          red += S.X[q] * df_to_double(B[q]);
+        }
+        mu = warp_sum_d(mu);
+        red = warp_sum_d(red);
+        if (tid == 0) {
+          const double var = fmax(mdl.c0 - red, 1e-12);
+          const double r = zi - mu;
+          a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+          a.flag[(int64_t)c * a.n + k] = 0;
+        }
       }
-      mu = warp_sum_d(mu);
-      red = warp_sum_d(red);
-      if (lane == 0) {
-        const double var = fmax(mdl.c0 - red, 1e-12);
-        const double r = zi - mu;
-        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
-        a.flag[(int64_t)c * a.n + k] = 0;
-      }
-      __syncwarp();
+      __syncthreads();
     }
   }
 }
@@ -447,16 +470,33 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   DevBuf list;
   const bool mixed = precision != GS_PREC_FP64 && M <= GS_MIXED_MAX_NEIGHBORS;
   if (mixed) {
-    const size_t per_warp = vecchia_per_warp_bytes(std::max(M, 1), dim);
-    int wpb = 4;
-    while (wpb > 1 && per_warp * wpb > 200 * 1024) --wpb;
-    const size_t smem = per_warp * wpb;
-    auto kern = dim == 2 ? vecchia_loglik_kernel<2> : vecchia_loglik_kernel<3>;
-    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int blocks = (int)std::min<int64_t>((n + wpb - 1) / wpb, 152 * 64);
-    kern<<<blocks, wpb * 32, smem, s>>>(a, g_vtab, g_vkc, per_warp);
-    GS_CUDA(cudaGetLastError());
-    count_launch(1);
+    const VLayout lay = vecchia_layout(std::max(M, 1), dim);
+    const size_t smem = lay.total;
+    const int tiles = lay.nbr * (lay.nbr + 1) / 2;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto go = [&](auto kern, int block) -> int {
+      GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int per_sm = 0;
+      GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+      per_sm = std::max(per_sm, 1);
+      const int blocks = (int)std::min<int64_t>(n, (int64_t)sms * per_sm);
+      kern<<<blocks, block, smem, s>>>(a, g_vtab, g_vkc);
+      GS_CUDA(cudaGetLastError());
+      count_launch(1);
+      return GS_OK;
+    };
+    int rc2;
+    if (dim == 2)
+      rc2 = tiles <= 64 ? go(vecchia_loglik_kernel<2, 64>, 64)
+                        : (tiles <= 128 ? go(vecchia_loglik_kernel<2, 128>, 128)
+                                        : go(vecchia_loglik_kernel<2, 256>, 256));
+    else
+      rc2 = tiles <= 64 ? go(vecchia_loglik_kernel<3, 64>, 64)
+                        : (tiles <= 128 ? go(vecchia_loglik_kernel<3, 128>, 128)
+                                        : go(vecchia_loglik_kernel<3, 256>, 256));
+    GS_TRY(rc2);
     // compact flagged (candidate, point) pairs
     DevBuf nsel, tmp;
     GS_TRY(nsel.alloc(8, s));
