@@ -1,16 +1,23 @@
 // gs_cta.cuh -- one small symmetric system per thread block: register-tiled
-// L D L^T factorisation, triangular solves and double-float refinement.
+// FP32 inversion and double-float iterative refinement.
 //
 // The packed lower-triangular double-float matrix A (entry (i, j), j <= i, at
-// i(i+1)/2 + j) lives in shared memory.  For the factorisation each thread
-// owns one 4x4 tile of the lower triangle in registers (tile (ib, jb),
-// ib >= jb, numbered row by row); step k reads column k from a small shared
-// buffer, applies the rank-1 update A_ij -= (A_ik / d_k) A_jk to its tile and
-// the owners of column k+1 publish it -- one barrier per column.  The unit-
-// lower factor is written packed (FP32) for the solves, which one warp runs
-// while the others wait; refinement residuals b - A x are formed from the
-// double-float entries in compensated FP32 (Ogita, Rump & Oishi 2005), two
-// threads per row, and the solution is accumulated in FP64.
+// i(i+1)/2 + j) lives in shared memory.  Each thread owns one 4x4 tile of the
+// lower triangle (tile (ib, jb), ib >= jb, numbered row by row) in registers.
+// The FP32 hi parts are inverted in place with the symmetric sweep operator
+// (Gauss-Jordan elimination without pivoting: for pivot k, a_ij -= a_ik a_kj /
+// a_kk off row/column k, a_ik /= a_kk, a_kk = -1/a_kk; after all N pivots the
+// tiles hold -A^{-1}).  No pivoting is needed for a positive-definite
+// covariance block bordered by drift rows: the pivots are those of A = L D L^T,
+// positive for the covariance block and negative for the drift block.  Every
+// step reads column k from a shared buffer written by its owners -- one
+// barrier per pivot, every tile busy.
+//
+// The solution and its corrections are tile-parallel matrix-vector products
+// from the registers, reduced in a fixed order (deterministic).  Refinement
+// residuals b - A x use the double-float entries in compensated FP32
+// (Ogita, Rump & Oishi, "Accurate sum and dot product", 2005), two threads per
+// row; the solution accumulates in FP64.
 #pragma once
 
 #include "gs_solve.cuh"
@@ -18,10 +25,9 @@
 namespace gs {
 
 struct CtaScratch {
-  float* L;      // packed unit-lower factor
-  float* DI;     // inverse pivots
-  float* W;      // FP32 work vector
-  float* colU;   // 2 x (4 * nbr) column buffers
+  float* W;      // FP32 work vector (residual)
+  float* col;    // 2 x stride column buffers
+  float* P;      // nbr x nbr x 4 partial products
   double* X;     // FP64 solution
   df* XD;        // solution as df
   double* red;   // block reduction scratch (>= 2 * warps doubles)
@@ -50,29 +56,65 @@ __device__ __forceinline__ float sel4(const float* row, int c) {
 }
 
 template <int BLOCK>
-__device__ __forceinline__ float block_max_f(float v, double* red) {
-  v = warp_max_f(v);
+__device__ __forceinline__ void block_max2(double& a, double& b, double* red) {
+  a = warp_max_d(a);
+  b = warp_max_d(b);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
-  if (lane == 0) red[w] = (double)v;
+  if (lane == 0) {
+    red[2 * w] = a;
+    red[2 * w + 1] = b;
+  }
   __syncthreads();
-  float r = 0.0f;
+  a = 0.0;
+  b = 0.0;
 #pragma unroll
-  for (int i = 0; i < BLOCK / 32; ++i) r = fmaxf(r, (float)red[i]);
-  return r;
+  for (int i = 0; i < BLOCK / 32; ++i) {
+    a = fmax(a, red[2 * i]);
+    b = fmax(b, red[2 * i + 1]);
+  }
 }
 
-// Factors hi(A) (N x N) into S.L / S.DI.  Returns false (uniformly) when a
-// pivot is too small for FP32.
+// Writes this tile's share of y = T_full r (T symmetric, lower tiles) to P.
+__device__ __forceinline__ void tile_gemv_partial(const float (&T)[4][4], bool own, int ib, int jb,
+                                                  int nbr, const float* r, float* P) {
+  if (!own) return;
+  float rc[4], rr[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) rc[b] = r[4 * jb + b];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) rr[a] = r[4 * ib + a];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    float s = 0.0f;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) s = fmaf(T[a][b], rc[b], s);
+    P[(ib * nbr + jb) * 4 + a] = s;
+  }
+  if (ib != jb) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      float s = 0.0f;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) s = fmaf(T[a][b], rr[a], s);
+      P[(jb * nbr + ib) * 4 + b] = s;
+    }
+  }
+}
+
+// Solves A X = B (N unknowns) and refines to ~1e-13 relative.  Returns false
+// (uniformly) when a pivot is too small for FP32 or the refinement stalls;
+// the caller then re-solves in FP64.  S.col needs 2 * 4 * nbr floats,
+// S.P nbr * nbr * 4 floats, S.W 4 * nbr floats.
 template <int BLOCK>
-__device__ bool cta_ldl(const df* A, int N, const CtaScratch& S) {
+__device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) {
   const int tid = threadIdx.x;
   const int nbr = (N + 3) >> 2;
   const int stride = nbr * 4;
   int ib = 0, jb = 0;
   const bool own = tile_of(tid, nbr, ib, jb);
   float T[4][4];
-  float amax = 0.0f;
+  double amax_d = 0.0, dummy = 0.0;
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -81,85 +123,89 @@ __device__ bool cta_ldl(const df* A, int N, const CtaScratch& S) {
       float v = 0.0f;
       if (own) {
         if (i < N && j < N) v = i >= j ? A[pk(i, j)].hi : A[pk(j, i)].hi;
-        else if (i == j) v = 1.0f;
+        else if (i == j) v = 1.0f;  // padding: decoupled unit pivots
       }
       T[a][b] = v;
-      amax = fmaxf(amax, fabsf(v));
+      amax_d = fmax(amax_d, (double)fabsf(v));
     }
-  amax = block_max_f<BLOCK>(amax, S.red);
-  const float tol = 1e-6f * amax;
+  block_max2<BLOCK>(amax_d, dummy, S.red);
+  const float tol = 1e-6f * (float)amax_d;
+  // publish column 0: rows of block column 0 (tiles (ib, 0))
   if (own && jb == 0) {
 #pragma unroll
-    for (int a = 0; a < 4; ++a) S.colU[4 * ib + a] = T[a][0];
+    for (int a = 0; a < 4; ++a) S.col[4 * ib + a] = T[a][0];
   }
   __syncthreads();
   for (int k = 0; k < N; ++k) {
-    const float* cu = S.colU + (k & 1) * stride;
-    const float d = cu[k];
-    if (!(fabsf(d) > tol)) return false;  // same value for every thread
-    const float invd = 1.0f / d;
-    const int kb = k >> 2, kc = k & 3;
-    if (own && jb >= kb) {
-      if (jb == kb) {
-        // column k is final: publish the scaled multipliers of this tile
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const int i = 4 * ib + a;
-          if (i > k && i < N) S.L[pk(i, k)] = sel4(T[a], kc) * invd;
-        }
-        if (ib == kb && tid == (kb * (kb + 1) / 2 + kb)) S.DI[k] = invd;
-      }
+    const float* u = S.col + (k & 1) * stride;
+    const float d = u[k];
+    if (!(fabsf(d) > tol)) return false;  // the same value in every thread
+    const float invd = __fdividef(1.0f, d);
+    const int kb = k >> 2;
+    if (own) {
       float lr[4], cc[4];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) lr[a] = cu[4 * ib + a] * invd;
+      for (int a = 0; a < 4; ++a) lr[a] = u[4 * ib + a] * invd;
 #pragma unroll
-      for (int b = 0; b < 4; ++b) cc[b] = cu[4 * jb + b];
-      const bool edge = (ib == kb) || (jb == kb);
+      for (int b = 0; b < 4; ++b) cc[b] = u[4 * jb + b];
+      if (ib != kb && jb != kb) {
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) T[a][b] = fmaf(-lr[a], cc[b], T[a][b]);
+      } else {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const bool rk = (4 * ib + a) == k, ck = (4 * jb + b) == k;
+            const float gen = fmaf(-lr[a], cc[b], T[a][b]);
+            const float edge = T[a][b] * invd;
+            T[a][b] = (rk && ck) ? -invd : ((rk || ck) ? edge : gen);
+          }
+      }
+    }
+    // publish column k+1 of the updated matrix: block column (tiles (ib, kbn),
+    // rows >= 4 kbn) and block row (tiles (kbn, jb), rows < 4 kbn)
+    const int kn = k + 1;
+    if (own && kn < N) {
+      const int kbn = kn >> 2, kcn = kn & 3;
+      float* cn = S.col + (kn & 1) * stride;
+      if (jb == kbn) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) cn[4 * ib + a] = sel4(T[a], kcn);
+      } else if (ib == kbn) {
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-          const bool upd = !edge || ((4 * ib + a) > k && (4 * jb + b) > k);
-          if (upd) T[a][b] = fmaf(-lr[a], cc[b], T[a][b]);
+          float v = T[0][b];
+          v = kcn == 1 ? T[1][b] : v;
+          v = kcn == 2 ? T[2][b] : v;
+          v = kcn == 3 ? T[3][b] : v;
+          cn[4 * jb + b] = v;
         }
-    }
-    const int kn = k + 1;
-    if (own && kn < N && jb == (kn >> 2)) {
-      float* cn = S.colU + (kn & 1) * stride;
-      const int kcn = kn & 3;
-#pragma unroll
-      for (int a = 0; a < 4; ++a) cn[4 * ib + a] = sel4(T[a], kcn);
+      }
     }
     __syncthreads();
   }
-  return true;
-}
-
-// Solves A X = B with the factor from cta_ldl and refines; returns false
-// (uniformly) when the refinement does not contract to ~1e-13 relative.
-template <int BLOCK>
-__device__ bool cta_refine(const df* A, const df* B, int N, const CtaScratch& S) {
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const bool w0 = tid < 32;
-  if (w0) {
-    for (int i = lane; i < N; i += 32) S.W[i] = B[i].hi;
-    __syncwarp();
-    ldl_solve(S.L, S.DI, S.W, N, lane);
-    double nx = 0.0;
-    for (int i = lane; i < N; i += 32) {
-      const double xi = (double)S.W[i];
-      S.X[i] = xi;
-      S.XD[i] = df_from_double(xi);
-      nx = fmax(nx, fabs(xi));
-    }
-    nx = warp_max_d(nx);
-    if (lane == 0) S.red[0] = nx;
-  }
+  // T now holds -A^{-1}.  x0 = A^{-1} b_hi
+  float* w = S.W;
+  for (int i = tid; i < stride; i += BLOCK) w[i] = i < N ? B[i].hi : 0.0f;
   __syncthreads();
-  double nd_prev = S.red[0];
+  tile_gemv_partial(T, own, ib, jb, nbr, w, S.P);
+  __syncthreads();
+  double nx = 0.0;
+  for (int i = tid; i < N; i += BLOCK) {
+    float s = 0.0f;
+    for (int q = 0; q < nbr; ++q) s += S.P[((i >> 2) * nbr + q) * 4 + (i & 3)];
+    const double xi = -(double)s;
+    S.X[i] = xi;
+    S.XD[i] = df_from_double(xi);
+    nx = fmax(nx, fabs(xi));
+  }
+  block_max2<BLOCK>(nx, dummy, S.red);
+  double nd_prev = nx;
   for (int sweep = 1; sweep <= 4; ++sweep) {
-    // residual: two threads per row, each over half the columns
+    // residual r = b - A x: two threads per row, each over half the columns
     for (int rbase = 0; rbase < N; rbase += BLOCK / 2) {
       const int row = rbase + (tid >> 1), half = tid & 1;
       float s = 0.0f, c = 0.0f;
@@ -172,6 +218,7 @@ __device__ bool cta_refine(const df* A, const df* B, int N, const CtaScratch& S)
         for (int jj = j0; jj < j1; ++jj) {
           const df aij = jj <= row ? A[pk(row, jj)] : A[pk(jj, row)];
           const df xj = S.XD[jj];
+          // TwoProduct / TwoSum with explicit roundings (no contraction)
           const float ph = __fmul_rn(-aij.hi, xj.hi);
           float pe = __fmaf_rn(-aij.hi, xj.hi, -ph);
           pe = __fmaf_rn(-aij.hi, xj.lo, pe);
@@ -183,46 +230,37 @@ __device__ bool cta_refine(const df* A, const df* B, int N, const CtaScratch& S)
           c += e + pe;
         }
       }
-      // combine the two halves (same pairing and order every time)
       const float s2 = __shfl_down_sync(0xffffffffu, s, 1);
       const float c2 = __shfl_down_sync(0xffffffffu, c, 1);
       if (row < N && !half) {
         const float tsum = __fadd_rn(s, s2);
         const float bb = __fsub_rn(tsum, s);
         const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(s2, bb));
-        S.W[row] = tsum + (c + c2 + e);
+        w[row] = tsum + (c + c2 + e);
       }
     }
     __syncthreads();
-    if (w0) {
-      ldl_solve(S.L, S.DI, S.W, N, lane);
-      double nd = 0.0, nx = 0.0;
-      for (int i = lane; i < N; i += 32) {
-        const double dlt = (double)S.W[i];
-        const double xi = S.X[i] + dlt;
-        S.X[i] = xi;
-        S.XD[i] = df_from_double(xi);
-        nd = fmax(nd, fabs(dlt));
-        nx = fmax(nx, fabs(xi));
-      }
-      nd = warp_max_d(nd);
-      nx = warp_max_d(nx);
-      if (lane == 0) {
-        int dec = 0;  // 0 continue, 1 converged
-        if (nd <= 1e-15 * nx) dec = 1;
-        else if (sweep >= 2) {
-          const double rho = nd / nd_prev;
-          if (rho < 0.5 && rho * nd <= 1e-13 * nx) dec = 1;
-        }
-        S.flag[0] = dec;
-        S.red[1] = nd;
-      }
+    tile_gemv_partial(T, own, ib, jb, nbr, w, S.P);
+    __syncthreads();
+    double nd = 0.0;
+    nx = 0.0;
+    for (int i = tid; i < N; i += BLOCK) {
+      float s = 0.0f;
+      for (int q = 0; q < nbr; ++q) s += S.P[((i >> 2) * nbr + q) * 4 + (i & 3)];
+      const double dlt = -(double)s;
+      const double xi = S.X[i] + dlt;
+      S.X[i] = xi;
+      S.XD[i] = df_from_double(xi);
+      nd = fmax(nd, fabs(dlt));
+      nx = fmax(nx, fabs(xi));
     }
-    __syncthreads();
-    const int dec = S.flag[0];
-    nd_prev = S.red[1];
-    __syncthreads();
-    if (dec) return true;
+    block_max2<BLOCK>(nd, nx, S.red);
+    if (nd <= 1e-15 * nx) return true;
+    if (sweep >= 2) {
+      const double rho = nd / nd_prev;
+      if (rho < 0.5 && rho * nd <= 1e-13 * nx) return true;
+    }
+    nd_prev = nd;
   }
   return false;
 }

@@ -65,8 +65,8 @@ __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
 // Shared-memory layout of one system (see mixed_smem_bytes).
 struct MixedLayout {
   int np, nbr;
-  size_t off_a, off_v, off_b, off_xd, off_x, off_z, off_red, off_l, off_w, off_di, off_col,
-      off_flag, total;
+  size_t off_a, off_v, off_b, off_xd, off_x, off_z, off_red, off_w, off_col, off_p, off_flag,
+      total;
 };
 
 __host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
@@ -86,10 +86,9 @@ __host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
   L.off_x = take((size_t)nmax * sizeof(double));
   L.off_z = take((size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(double));
   L.off_red = take(16 * sizeof(double));
-  L.off_l = take((size_t)L.np * sizeof(float));
-  L.off_w = take((size_t)nmax * sizeof(float));
-  L.off_di = take((size_t)nmax * sizeof(float));
+  L.off_w = take((size_t)4 * L.nbr * sizeof(float));
   L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
+  L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
   L.off_flag = take(16);
   L.total = o;
   return L;
@@ -116,10 +115,9 @@ __global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevMode
   S.X = reinterpret_cast<double*>(smem_raw + lay.off_x);
   double* Z = reinterpret_cast<double*>(smem_raw + lay.off_z);
   S.red = reinterpret_cast<double*>(smem_raw + lay.off_red);
-  S.L = reinterpret_cast<float*>(smem_raw + lay.off_l);
   S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
-  S.DI = reinterpret_cast<float*>(smem_raw + lay.off_di);
-  S.colU = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.col = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
   S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
   __syncthreads();
 
@@ -208,8 +206,7 @@ __global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevMode
     }
     __syncthreads();
     // --- FP32 L D L^T, FP64-accumulated refinement -----------------------
-    bool ok = cta_ldl<BLOCK>(A, N, S);
-    if (ok) ok = cta_refine<BLOCK>(A, B, N, S);
+    const bool ok = cta_solve<BLOCK>(A, B, N, S);
     if (!ok) {
       if (tid == 0) flag[t] = 1;
       __syncthreads();

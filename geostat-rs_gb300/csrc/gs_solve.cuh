@@ -1,15 +1,8 @@
-// gs_solve.cuh -- in-warp factor / solve / refine of one small symmetric
-// system held in shared memory, shared by the kriging and Vecchia kernels.
-//
-// The matrix is packed lower-triangular (entry (i, j), j <= i, at
-// i(i+1)/2 + j) in double-float.  Its FP32 hi parts are factored
-// A = L D L^T without pivoting -- valid for a positive-definite covariance
-// block bordered by drift rows (the Schur complement is negative definite) --
-// and the solution is refined with residuals b - A x taken against the
-// double-float entries in compensated FP32 (Ogita, Rump & Oishi, "Accurate
-// sum and dot product", SIAM J. Sci. Comput. 26(6), 2005), accumulated in
-// FP64.  Triangular numbers modulo 32 form a permutation of 0..31, so the
-// column accesses of the packed layout are free of bank conflicts.
+// gs_solve.cuh -- device helpers shared by the per-system kernels: packed
+// lower-triangular indexing (entry (i, j), j <= i, at i(i+1)/2 + j), warp
+// reductions, coordinate frames and double-float covariances.  Triangular
+// numbers modulo 32 form a permutation of 0..31, so column accesses of the
+// packed layout are free of shared-memory bank conflicts.
 #pragma once
 
 #include "gs_common.cuh"
@@ -99,23 +92,6 @@ __device__ __forceinline__ void frame_coords(const DevModel& m, const Frames& fr
       V[(f * stride + i) * D + r] = acc;
     }
     h[f] = norm0_df<D>(vv);
-  }
-}
-
-// L D L^T w = w in place (unit-lower packed L, inverse pivots DI).
-__device__ __forceinline__ void ldl_solve(const float* L, const float* DI, float* w, int N,
-                                          int lane) {
-  for (int k = 0; k < N - 1; ++k) {
-    const float wk = w[k];
-    for (int i = k + 1 + lane; i < N; i += 32) w[i] = fmaf(-L[pk(i, k)], wk, w[i]);
-    __syncwarp();
-  }
-  for (int i = lane; i < N; i += 32) w[i] *= DI[i];
-  __syncwarp();
-  for (int k = N - 1; k > 0; --k) {
-    const float wk = w[k];
-    for (int i = lane; i < k; i += 32) w[i] = fmaf(-L[pk(k, i)], wk, w[i]);
-    __syncwarp();
   }
 }
 

@@ -92,8 +92,8 @@ constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
 
 struct VLayout {
   int np, nbr;
-  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_x, off_z, off_red, off_l, off_w, off_di,
-      off_col, off_flag, total;
+  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_x, off_z, off_red, off_w, off_col, off_p,
+      off_flag, total;
 };
 
 __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
@@ -115,10 +115,9 @@ __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
   L.off_x = take((size_t)m * sizeof(double));
   L.off_z = take((size_t)m * sizeof(double));
   L.off_red = take(16 * sizeof(double));
-  L.off_l = take((size_t)L.np * sizeof(float));
-  L.off_w = take((size_t)m * sizeof(float));
-  L.off_di = take((size_t)m * sizeof(float));
+  L.off_w = take((size_t)4 * L.nbr * sizeof(float));
   L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
+  L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
   L.off_flag = take(16);
   L.total = o;
   return L;
@@ -146,10 +145,9 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
   S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
   S.X = reinterpret_cast<double*>(smem_raw + lay.off_x);
   S.red = reinterpret_cast<double*>(smem_raw + lay.off_red);
-  S.L = reinterpret_cast<float*>(smem_raw + lay.off_l);
   S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
-  S.DI = reinterpret_cast<float*>(smem_raw + lay.off_di);
-  S.colU = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.col = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
   S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
   __syncthreads();
 
@@ -257,8 +255,7 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
         }
       }
       __syncthreads();
-      bool ok = cta_ldl<BLOCK>(A, s, S);
-      if (ok) ok = cta_refine<BLOCK>(A, B, s, S);
+      const bool ok = cta_solve<BLOCK>(A, B, s, S);
       if (!ok) {
         if (tid == 0) a.flag[(int64_t)c * a.n + k] = 1;
         __syncthreads();
