@@ -100,7 +100,11 @@ def test_mle_objective_parity_and_batched_nelder_mead():
     xr, fr, nr = O.vecchia_mle_nm(c, v, "exponential", 12, starts, max_iter=400)
     # same algorithm, same objective to ~1e-12: the optimum agrees closely
     assert abs(-ll - fr) <= 1e-7 * abs(fr)
-    assert np.max(np.abs(x - xr)) < 1e-3
+    # x = (sqrt nugget, ln psill, ln range): the objective is even in x[0], so
+    # simplices that part ways on ~1e-12 objective differences may end on
+    # mirror images; the fitted model (nugget = x0^2) is what must agree
+    assert abs(x[0] ** 2 - xr[0] ** 2) < 1e-3 * max(xr[0] ** 2, 1e-3)
+    assert np.max(np.abs(x[1:] - xr[1:])) < 1e-3
     o, nb, cnt = O.vecchia_plan(c, 12)
     fx = O.vecchia_mle_objective(c, v, "exponential", 12, o, nb, cnt, rmax, x)
     assert abs(fx[0] + ll) <= 1e-9 * abs(fx[0])
