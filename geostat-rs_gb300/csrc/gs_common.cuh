@@ -71,6 +71,14 @@ __device__ __forceinline__ df df_add(df a, df b) {
   s.lo = __fadd_rn(s.lo, t.lo);
   return fast_two_sum(s.hi, s.lo);
 }
+// Double-float sum without the second renormalisation: error <= ~2^-46
+// (|a| + |b|); used for sums of same-sign terms (no cancellation) and for
+// differences of nearby coordinates whose magnitudes bound the error.
+__device__ __forceinline__ df df_add_fast(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  const float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, e);
+}
 __device__ __forceinline__ df df_neg(df a) { return df_make(-a.hi, -a.lo); }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
 __device__ __forceinline__ df df_add_f(df a, float b) {
@@ -101,58 +109,53 @@ __host__ __device__ inline df df_from_double(double x) {
 }
 __host__ __device__ inline double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
 
-// sqrt of a non-negative df: FP32 sqrt plus one correction step with the
-// exact residual s - y*y (Karp & Markstein 1997).
+// sqrt of a non-negative df: an FP32 reciprocal square root refined by one
+// Newton step, then one correction with the exact residual s - y*y
+// (Karp & Markstein, ACM TOMS 23(4), 1997): relative error ~2^-47.
 __device__ __forceinline__ df df_sqrt(df s) {
   if (!(s.hi > 0.0f)) return df_make(0.0f, 0.0f);
-  float y = __fsqrt_rn(s.hi);
-  df yy = two_prod(y, y);
-  float e = __fadd_rn(__fsub_rn(__fsub_rn(s.hi, yy.hi), yy.lo), s.lo);
-  float c = __fmul_rn(e, __frcp_rn(__fmul_rn(2.0f, y)));
-  return fast_two_sum(y, c);
+  float r = rsqrtf(s.hi);
+  r = r * fmaf(-0.5f * s.hi * r, r, 1.5f);
+  const float y = s.hi * r;
+  const df yy = two_prod(y, y);
+  const float e = __fadd_rn(__fsub_rn(__fsub_rn(s.hi, yy.hi), yy.lo), s.lo);
+  return fast_two_sum(y, e * (0.5f * r));
 }
 
 // exp(-d) for d >= 0, table-driven after P. T. P. Tang, "Table-driven
 // implementation of the exponential function in IEEE floating-point
-// arithmetic", ACM TOMS 15(2), 1989: d = n*ln2/64 + r with |r| <= ln2/128,
-// exp(-d) = 2^(-n/64) * exp(-r); 2^(-j/64) comes from a 64-entry df table
-// and exp(-r) from its Taylor series (r^2 term in df, higher terms in FP32).
-// ln2/64 is split in three parts; the first has 11 significant bits so that
-// n*L1 is exact for n < 2^13 (d < 88).
+// arithmetic", ACM TOMS 15(2), 1989: d = n*ln2/256 + r with |r| <= ln2/512,
+// exp(-d) = 2^(-n/256) * exp(-r).  2^(-j/256) comes from a 256-entry df table;
+// exp(-r) = 1 - r + r^2 (1/2 - r/6 + r^2/24) with the polynomial part in FP32
+// (its terms are below 1e-6).  ln2/256 is split as l1 (9 significant bits, so
+// n*l1 is exact for n < 2^15, i.e. d < 88) + l2 + l3; n*l2 is formed exactly.
 struct ExpTable {
-  float hi[64];
-  float lo[64];
+  float hi[256];
+  float lo[256];
 };
-// Uniform df constants, filled on the host (df_consts_host): ln2/64 split in
-// three parts (l1 with 11 significant bits), 64/ln2, sqrt(3), sqrt(5).
+// Uniform df constants, filled on the host (df_consts_host).
 struct DfConsts {
-  float l1, l2, l3, inv;
-  float s3h, s3l, s5h, s5l;
+  float l1, l2, l3, inv;  // ln2/256 in three parts, 256/ln2
+  float s3h, s3l, s5h, s5l;  // sqrt(3), sqrt(5) as df
 };
 typedef DfConsts ExpConsts;
 
 __device__ __forceinline__ df df_expneg(df d, const ExpTable& tab, const ExpConsts& k) {
   if (!(d.hi < 87.0f)) return df_make(0.0f, 0.0f);
-  float nf = rintf(__fmul_rn(d.hi, k.inv));
-  int n = (int)nf;
-  float t1 = __fsub_rn(d.hi, __fmul_rn(nf, k.l1));  // exact (Sterbenz)
-  df r = two_sum(t1, d.lo);
-  df nl2 = two_prod(nf, k.l2);
-  r = df_sub(r, nl2);
-  r = df_add_f(r, -__fmul_rn(nf, k.l3));
-  // exp(-r) = 1 - r + r^2/2 - r^3/6 + r^4/24 - r^5/120
-  df r2 = df_sqr(r);
-  r2.hi *= 0.5f;
-  r2.lo *= 0.5f;
-  float t = r.hi;
-  float tail = t * t * t * (-(1.0f / 6.0f) + t * ((1.0f / 24.0f) - t * (1.0f / 120.0f)));
-  df q = df_add(df_neg(r), r2);
-  q = df_add_f(q, tail);
-  df e = df_add_f(q, 1.0f);
-  int j = n & 63;
-  int kk = n >> 6;
-  df res = df_mul(e, df_make(tab.hi[j], tab.lo[j]));
-  float sc = __int_as_float((127 - kk) << 23);  // 2^-kk, kk <= 125 for d < 87
+  const float nf = rintf(__fmul_rn(d.hi, k.inv));
+  const int n = (int)nf;
+  const float t1 = __fsub_rn(d.hi, __fmul_rn(nf, k.l1));  // exact (Sterbenz)
+  const df nl2 = two_prod(nf, k.l2);
+  df r = two_sum(t1, -nl2.hi);
+  r = fast_two_sum(r.hi, __fadd_rn(r.lo, __fsub_rn(__fsub_rn(d.lo, nl2.lo), __fmul_rn(nf, k.l3))));
+  const float t = r.hi;
+  const float poly = t * t * (0.5f + t * (-(1.0f / 6.0f) + t * (1.0f / 24.0f)));
+  const df q = df_add_f(df_neg(r), poly);
+  const df e = df_add_f(q, 1.0f);
+  const int j = n & 255;
+  const int kk = n >> 8;
+  const df res = df_mul(e, df_make(tab.hi[j], tab.lo[j]));
+  const float sc = __int_as_float((127 - kk) << 23);  // 2^-kk, kk <= 126 for d < 88
   return df_make(res.hi * sc, res.lo * sc);
 }
 
@@ -242,7 +245,7 @@ __device__ __forceinline__ df rho_df(int kind, df d, const ExpTable& tab, const 
       if (d.hi > 1.0f || (d.hi == 1.0f && d.lo >= 0.0f)) return df_make(0.0f, 0.0f);
       // 1 - d (1.5 - 0.5 d^2)
       df d2 = df_sqr(d);
-      df t = df_add_f(df_make(-0.5f * d2.hi, -0.5f * d2.lo), 1.5f);
+      const df t = df_add_f(df_make(-0.5f * d2.hi, -0.5f * d2.lo), 1.5f);
       df u = df_mul(d, t);
       return df_add_f(df_neg(u), 1.0f);
     }

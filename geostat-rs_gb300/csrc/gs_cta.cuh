@@ -55,7 +55,6 @@ __device__ __forceinline__ float sel4(const float* row, int c) {
   return v;
 }
 
-template <int BLOCK>
 __device__ __forceinline__ void block_max2(double& a, double& b, double* red) {
   a = warp_max_d(a);
   b = warp_max_d(b);
@@ -68,8 +67,8 @@ __device__ __forceinline__ void block_max2(double& a, double& b, double* red) {
   __syncthreads();
   a = 0.0;
   b = 0.0;
-#pragma unroll
-  for (int i = 0; i < BLOCK / 32; ++i) {
+  const int nw = blockDim.x >> 5;
+  for (int i = 0; i < nw; ++i) {
     a = fmax(a, red[2 * i]);
     b = fmax(b, red[2 * i + 1]);
   }
@@ -106,9 +105,9 @@ __device__ __forceinline__ void tile_gemv_partial(const float (&T)[4][4], bool o
 // (uniformly) when a pivot is too small for FP32 or the refinement stalls;
 // the caller then re-solves in FP64.  S.col needs 2 * 4 * nbr floats,
 // S.P nbr * nbr * 4 floats, S.W 4 * nbr floats.
-template <int BLOCK>
-__device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) {
+static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) {
   const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
   const int nbr = (N + 3) >> 2;
   const int stride = nbr * 4;
   int ib = 0, jb = 0;
@@ -128,7 +127,7 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
       T[a][b] = v;
       amax_d = fmax(amax_d, (double)fabsf(v));
     }
-  block_max2<BLOCK>(amax_d, dummy, S.red);
+  block_max2(amax_d, dummy, S.red);
   const float tol = 1e-6f * (float)amax_d;
   // publish column 0: rows of block column 0 (tiles (ib, 0))
   if (own && jb == 0) {
@@ -143,11 +142,10 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
     const float invd = __fdividef(1.0f, d);
     const int kb = k >> 2;
     if (own) {
-      float lr[4], cc[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) lr[a] = u[4 * ib + a] * invd;
-#pragma unroll
-      for (int b = 0; b < 4; ++b) cc[b] = u[4 * jb + b];
+      const float4 ur = *reinterpret_cast<const float4*>(u + 4 * ib);
+      const float4 uc = *reinterpret_cast<const float4*>(u + 4 * jb);
+      const float lr[4] = {ur.x * invd, ur.y * invd, ur.z * invd, ur.w * invd};
+      const float cc[4] = {uc.x, uc.y, uc.z, uc.w};
       if (ib != kb && jb != kb) {
 #pragma unroll
         for (int a = 0; a < 4; ++a)
@@ -189,12 +187,12 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
   }
   // T now holds -A^{-1}.  x0 = A^{-1} b_hi
   float* w = S.W;
-  for (int i = tid; i < stride; i += BLOCK) w[i] = i < N ? B[i].hi : 0.0f;
+  for (int i = tid; i < stride; i += nthr) w[i] = i < N ? B[i].hi : 0.0f;
   __syncthreads();
   tile_gemv_partial(T, own, ib, jb, nbr, w, S.P);
   __syncthreads();
   double nx = 0.0;
-  for (int i = tid; i < N; i += BLOCK) {
+  for (int i = tid; i < N; i += nthr) {
     float s = 0.0f;
     for (int q = 0; q < nbr; ++q) s += S.P[((i >> 2) * nbr + q) * 4 + (i & 3)];
     const double xi = -(double)s;
@@ -202,11 +200,11 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
     S.XD[i] = df_from_double(xi);
     nx = fmax(nx, fabs(xi));
   }
-  block_max2<BLOCK>(nx, dummy, S.red);
+  block_max2(nx, dummy, S.red);
   double nd_prev = nx;
   for (int sweep = 1; sweep <= 4; ++sweep) {
     // residual r = b - A x: two threads per row, each over half the columns
-    for (int rbase = 0; rbase < N; rbase += BLOCK / 2) {
+    for (int rbase = 0; rbase < N; rbase += nthr / 2) {
       const int row = rbase + (tid >> 1), half = tid & 1;
       float s = 0.0f, c = 0.0f;
       if (row < N) {
@@ -215,8 +213,15 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
           s = B[row].hi;
           c = B[row].lo;
         }
+        // entries (row, jj): packed row for jj <= row, packed column after
+        const int jmid = min(j1, row + 1);
+        int idx = pk(row, 0) + j0;
+        int idx2 = pk(max(j0, row + 1), row);
         for (int jj = j0; jj < j1; ++jj) {
-          const df aij = jj <= row ? A[pk(row, jj)] : A[pk(jj, row)];
+          const bool lower = jj < jmid;
+          const df aij = A[lower ? idx : idx2];
+          if (lower) ++idx;
+          else idx2 += jj + 1;
           const df xj = S.XD[jj];
           // TwoProduct / TwoSum with explicit roundings (no contraction)
           const float ph = __fmul_rn(-aij.hi, xj.hi);
@@ -244,7 +249,7 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
     __syncthreads();
     double nd = 0.0;
     nx = 0.0;
-    for (int i = tid; i < N; i += BLOCK) {
+    for (int i = tid; i < N; i += nthr) {
       float s = 0.0f;
       for (int q = 0; q < nbr; ++q) s += S.P[((i >> 2) * nbr + q) * 4 + (i & 3)];
       const double dlt = -(double)s;
@@ -254,7 +259,7 @@ __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) 
       nd = fmax(nd, fabs(dlt));
       nx = fmax(nx, fabs(xi));
     }
-    block_max2<BLOCK>(nd, nx, S.red);
+    block_max2(nd, nx, S.red);
     if (nd <= 1e-15 * nx) return true;
     if (sweep >= 2) {
       const double rho = nd / nd_prev;

@@ -46,23 +46,22 @@ static float round_to_bits(long double v, int bits) {
 
 void df_consts_host(ExpTable* tab, DfConsts* k) {
   const long double ln2 = 0.693147180559945309417232121458176568L;
-  long double L = ln2 / 64.0L;
-  float l1 = round_to_bits(L, 11);
-  long double rem = L - (long double)l1;
-  float l2 = (float)rem;
-  long double rem2 = rem - (long double)l2;
-  float l3 = (float)rem2;
+  const long double L = ln2 / 256.0L;
+  const float l1 = round_to_bits(L, 9);
+  const long double rem = L - (long double)l1;
+  const float l2 = (float)rem;
+  const float l3 = (float)(rem - (long double)l2);
   k->l1 = l1;
   k->l2 = l2;
   k->l3 = l3;
-  k->inv = (float)(64.0L / ln2);
-  long double s3 = sqrtl(3.0L), s5 = sqrtl(5.0L);
+  k->inv = (float)(256.0L / ln2);
+  const long double s3 = sqrtl(3.0L), s5 = sqrtl(5.0L);
   k->s3h = (float)s3;
   k->s3l = (float)(s3 - (long double)k->s3h);
   k->s5h = (float)s5;
   k->s5l = (float)(s5 - (long double)k->s5h);
-  for (int j = 0; j < 64; ++j) {
-    long double v = exp2l(-(long double)j / 64.0L);
+  for (int j = 0; j < 256; ++j) {
+    const long double v = exp2l(-(long double)j / 256.0L);
     tab->hi[j] = (float)v;
     tab->lo[j] = (float)(v - (long double)tab->hi[j]);
   }

@@ -95,15 +95,16 @@ __host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
 }
 
 template <int D, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevModel m, ExpTable tab_g,
+__global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevModel m, ExpTable tab_g,
                                                             DfConsts kc, uint8_t* flag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
-  for (int i = threadIdx.x; i < 64; i += BLOCK) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     tab.hi[i] = tab_g.hi[i];
     tab.lo[i] = tab_g.lo[i];
   }
   const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
   const Frames fr = frames_of(m);
   const int NBMAX = GS_MIXED_MAX_NEIGHBORS;
   const MixedLayout lay = mixed_layout(a.nmax, fr.nf, D);
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevMode
     const int N = n + p;
     const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
     // --- per-neighbour data: frames, values, rhs, diagonal, drift rows ---
-    for (int i = tid; i < n; i += BLOCK) {
+    for (int i = tid; i < n; i += nthr) {
       const int idx = a.nb[t * (int64_t)a.kout + i];
       const double pp[3] = {a.x[idx], a.y[idx], D == 3 ? a.z[idx] : 0.0};
       double u[3];
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevMode
       fill_basis<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, f);
       B[n + tid] = df_from_double(f[tid]);
     }
-    for (int q = tid; q < p * (p + 1) / 2; q += BLOCK) {
+    for (int q = tid; q < p * (p + 1) / 2; q += nthr) {
       int r = 0;
       while ((r + 1) * (r + 2) / 2 <= q) ++r;
       const int c = q - r * (r + 1) / 2;
@@ -192,12 +193,12 @@ __global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevMode
         j -= i;
         ++i;
       }
-      for (int q = tid; q < npairs; q += BLOCK) {
+      for (int q = tid; q < npairs; q += nthr) {
         df h[GS_MAX_STRUCTURES + 1];
         for (int f = 0; f < fr.nf; ++f)
           h[f] = norm_df<D>(&V[(f * NBMAX + i) * D], &V[(f * NBMAX + j) * D]);
         A[pk(i, j)] = cov_from_h(m, fr, h, tab, kc);
-        j += BLOCK;
+        j += nthr;
         while (j >= i && i < n) {
           j -= i;
           ++i;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(BLOCK) krige_mixed_kernel(KrigeArgs a, DevMode
     }
     __syncthreads();
     // --- FP32 L D L^T, FP64-accumulated refinement -----------------------
-    const bool ok = cta_solve<BLOCK>(A, B, N, S);
+    const bool ok = cta_solve(A, B, N, S);
     if (!ok) {
       if (tid == 0) flag[t] = 1;
       __syncthreads();
@@ -431,25 +432,17 @@ int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int nbr = lay.nbr;
   const int tiles = nbr * (nbr + 1) / 2;
-  auto go = [&](auto kern, int block) -> int {
-    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
-    per_sm = std::max(per_sm, 1);
-    const int blocks = (int)std::min<int64_t>(a.ntl, (int64_t)sms * per_sm);
-    kern<<<blocks, block, smem, stream>>>(a, m, g_tab, g_kc, flag);
-    GS_CUDA(cudaGetLastError());
-    count_launch(1);
-    return GS_OK;
-  };
-  if (a.dim == 2) {
-    if (tiles <= 64) return go(krige_mixed_kernel<2, 64>, 64);
-    if (tiles <= 128) return go(krige_mixed_kernel<2, 128>, 128);
-    return go(krige_mixed_kernel<2, 256>, 256);
-  }
-  if (tiles <= 64) return go(krige_mixed_kernel<3, 64>, 64);
-  if (tiles <= 128) return go(krige_mixed_kernel<3, 128>, 128);
-  return go(krige_mixed_kernel<3, 256>, 256);
+  const int block = std::min(256, std::max(64, ((tiles + 31) / 32) * 32));
+  auto kern = a.dim == 2 ? krige_mixed_kernel<2, 256> : krige_mixed_kernel<3, 256>;
+  GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+  per_sm = std::max(per_sm, 1);
+  const int blocks = (int)std::min<int64_t>(a.ntl, (int64_t)sms * per_sm);
+  kern<<<blocks, block, smem, stream>>>(a, m, g_tab, g_kc, flag);
+  GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  return GS_OK;
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {

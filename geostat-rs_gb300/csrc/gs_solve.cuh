@@ -49,24 +49,27 @@ __device__ __forceinline__ df cov_from_h(const DevModel& m, const Frames& fr, co
     const DevStruct& st = m.s[s];
     df d = df_mul(h[fr.fid[s]], st.inv_range_df);
     df r = rho_df(st.kind, d, tab, k);
-    c = df_add(c, df_mul(r, st.sill_df));
+    c = df_add_fast(c, df_mul(r, st.sill_df));  // non-negative terms
   }
   return c;
 }
 
+// |a - b| in df.  Coordinates are target-relative (a few ranges at most), so
+// the fast difference keeps ~2^-46 relative accuracy on the separation; the
+// squares are non-negative, so their sum needs no extra renormalisation.
 template <int D>
 __device__ __forceinline__ df norm_df(const df* a, const df* b) {
-  df q = df_make(0.0f, 0.0f);
+  df q = df_sqr(df_add_fast(a[0], df_neg(b[0])));
 #pragma unroll
-  for (int d = 0; d < D; ++d) q = df_add(q, df_sqr(df_sub(a[d], b[d])));
+  for (int d = 1; d < D; ++d) q = df_add_fast(q, df_sqr(df_add_fast(a[d], df_neg(b[d]))));
   return df_sqrt(q);
 }
 
 template <int D>
 __device__ __forceinline__ df norm0_df(const df* a) {
-  df q = df_make(0.0f, 0.0f);
+  df q = df_sqr(a[0]);
 #pragma unroll
-  for (int d = 0; d < D; ++d) q = df_add(q, df_sqr(a[d]));
+  for (int d = 1; d < D; ++d) q = df_add_fast(q, df_sqr(a[d]));
   return df_sqrt(q);
 }
 

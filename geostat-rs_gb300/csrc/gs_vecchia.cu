@@ -124,15 +124,16 @@ __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
 }
 
 template <int D, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable tab_g,
+__global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTable tab_g,
                                                                DfConsts kc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
-  for (int i = threadIdx.x; i < 64; i += BLOCK) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     tab.hi[i] = tab_g.hi[i];
     tab.lo[i] = tab_g.lo[i];
   }
   const int tid = threadIdx.x;
+  const int nthr = blockDim.x;
   const int M = a.m;
   const VLayout lay = vecchia_layout(M, D);
   df* A = reinterpret_cast<df*>(smem_raw + lay.off_a);
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
     const double zi = a.v[i] - a.mean;
     if (s == 0) {
       // first point: marginal N(0, sill)
-      for (int c = tid; c < a.ncand; c += BLOCK) {
+      for (int c = tid; c < a.ncand; c += nthr) {
         const double sill = a.models[c].c0;
         a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
         a.flag[(int64_t)c * a.n + k] = 0;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
       continue;
     }
     const double pi[3] = {a.x[i], a.y[i], D == 3 ? a.z[i] : 0.0};
-    for (int q = tid; q < s; q += BLOCK) {
+    for (int q = tid; q < s; q += nthr) {
       const int j = a.nb[k * (int64_t)M + q];
       const double u[3] = {a.x[j] - pi[0], a.y[j] - pi[1], D == 3 ? a.z[j] - pi[2] : 0.0};
 #pragma unroll
@@ -175,15 +176,15 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
     __syncthreads();
     const int npairs = (s * (s - 1)) >> 1;
     if (a.iso_shared) {
-      for (int q = tid; q < s; q += BLOCK) H0[q] = norm0_df<D>(&V[q * D]);
+      for (int q = tid; q < s; q += nthr) H0[q] = norm0_df<D>(&V[q * D]);
       int ii = 1, jj = tid;
       while (jj >= ii && ii < s) {
         jj -= ii;
         ++ii;
       }
-      for (int q = tid; q < npairs; q += BLOCK) {
+      for (int q = tid; q < npairs; q += nthr) {
         H[pk(ii, jj)] = norm_df<D>(&V[ii * D], &V[jj * D]);
-        jj += BLOCK;
+        jj += nthr;
         while (jj >= ii && ii < s) {
           jj -= ii;
           ++ii;
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
       const DevModel& mdl = a.models[c];
       const Frames fr = frames_of(mdl);
       if (a.iso_shared) {
-        for (int q = tid; q < s; q += BLOCK) {
+        for (int q = tid; q < s; q += nthr) {
           B[q] = cov_from_h(mdl, fr, &H0[q], tab, kc);
           A[pk(q, q)] = mdl.c0_df;
         }
@@ -204,9 +205,9 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
           jj -= ii;
           ++ii;
         }
-        for (int q = tid; q < npairs; q += BLOCK) {
+        for (int q = tid; q < npairs; q += nthr) {
           A[pk(ii, jj)] = cov_from_h(mdl, fr, &H[pk(ii, jj)], tab, kc);
-          jj += BLOCK;
+          jj += nthr;
           while (jj >= ii && ii < s) {
             jj -= ii;
             ++ii;
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
         }
       } else {
         df* VF = V + M * D;  // frames 1.. (frame 0 is V itself)
-        for (int q = tid; q < s; q += BLOCK) {
+        for (int q = tid; q < s; q += nthr) {
           df hq[GS_MAX_STRUCTURES + 1];
           hq[0] = norm0_df<D>(&V[q * D]);
           for (int st = 0; st < mdl.ns; ++st) {
@@ -241,13 +242,13 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
           jj -= ii;
           ++ii;
         }
-        for (int q = tid; q < npairs; q += BLOCK) {
+        for (int q = tid; q < npairs; q += nthr) {
           df h[GS_MAX_STRUCTURES + 1];
           h[0] = norm_df<D>(&V[ii * D], &V[jj * D]);
           for (int f = 1; f < fr.nf; ++f)
             h[f] = norm_df<D>(&VF[((f - 1) * M + ii) * D], &VF[((f - 1) * M + jj) * D]);
           A[pk(ii, jj)] = cov_from_h(mdl, fr, h, tab, kc);
-          jj += BLOCK;
+          jj += nthr;
           while (jj >= ii && ii < s) {
             jj -= ii;
             ++ii;
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(BLOCK) vecchia_loglik_kernel(VArgs a, ExpTable
         }
       }
       __syncthreads();
-      const bool ok = cta_solve<BLOCK>(A, B, s, S);
+      const bool ok = cta_solve(A, B, s, S);
       if (!ok) {
         if (tid == 0) a.flag[(int64_t)c * a.n + k] = 1;
         __syncthreads();
@@ -473,27 +474,16 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    auto go = [&](auto kern, int block) -> int {
-      GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      int per_sm = 0;
-      GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
-      per_sm = std::max(per_sm, 1);
-      const int blocks = (int)std::min<int64_t>(n, (int64_t)sms * per_sm);
-      kern<<<blocks, block, smem, s>>>(a, g_vtab, g_vkc);
-      GS_CUDA(cudaGetLastError());
-      count_launch(1);
-      return GS_OK;
-    };
-    int rc2;
-    if (dim == 2)
-      rc2 = tiles <= 64 ? go(vecchia_loglik_kernel<2, 64>, 64)
-                        : (tiles <= 128 ? go(vecchia_loglik_kernel<2, 128>, 128)
-                                        : go(vecchia_loglik_kernel<2, 256>, 256));
-    else
-      rc2 = tiles <= 64 ? go(vecchia_loglik_kernel<3, 64>, 64)
-                        : (tiles <= 128 ? go(vecchia_loglik_kernel<3, 128>, 128)
-                                        : go(vecchia_loglik_kernel<3, 256>, 256));
-    GS_TRY(rc2);
+    const int block = std::min(256, std::max(64, ((tiles + 31) / 32) * 32));
+    auto kern = dim == 2 ? vecchia_loglik_kernel<2, 256> : vecchia_loglik_kernel<3, 256>;
+    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+    per_sm = std::max(per_sm, 1);
+    const int blocks = (int)std::min<int64_t>(n, (int64_t)sms * per_sm);
+    kern<<<blocks, block, smem, s>>>(a, g_vtab, g_vkc);
+    GS_CUDA(cudaGetLastError());
+    count_launch(1);
     // compact flagged (candidate, point) pairs
     DevBuf nsel, tmp;
     GS_TRY(nsel.alloc(8, s));
