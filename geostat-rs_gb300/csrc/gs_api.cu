@@ -64,7 +64,25 @@ gs_pointset::~gs_pointset() {
   cudaFree(d_y);
   cudaFree(d_z);
   cudaFree(d_v);
+  cudaFree(d_cdf);
+  cudaFree(d_vdf);
 }
+
+namespace {
+
+// Splits FP64 coordinates and values into double-float copies (once per set).
+__global__ void split_df_kernel(int dim, int64_t n, const double* x, const double* y,
+                                const double* z, const double* v, gs::df* cdf, gs::df* vdf) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    cdf[i] = gs::df_from_double(x[i]);
+    cdf[n + i] = gs::df_from_double(y[i]);
+    if (dim == 3) cdf[2 * n + i] = gs::df_from_double(z[i]);
+    vdf[i] = gs::df_from_double(v[i]);
+  }
+}
+
+}  // namespace
 
 struct gs_kriging {
   const gs_pointset* ps = nullptr;
@@ -79,6 +97,8 @@ struct gs_kriging {
   double dscale[GS_MAX_KED_VARS] = {0};
   double* d_drift = nullptr;
   double* d_err = nullptr;
+  df* d_basis_df = nullptr;  // p x n drift basis of the data points
+  df* d_err_df = nullptr;    // measurement errors as df
   bool use_tree = false;
   SearchFrame frame{};
   Grid grid;
@@ -86,6 +106,8 @@ struct gs_kriging {
   ~gs_kriging() {
     cudaFree(d_drift);
     cudaFree(d_err);
+    cudaFree(d_basis_df);
+    cudaFree(d_err_df);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -160,6 +182,17 @@ int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, con
   if (!rc) rc = up(&ps->d_y, y);
   if (!rc && dim == 3) rc = up(&ps->d_z, z);
   if (!rc) rc = up(&ps->d_v, values);
+  if (!rc) {
+    if (cudaMalloc(&ps->d_cdf, (size_t)dim * n * sizeof(df)) != cudaSuccess ||
+        cudaMalloc(&ps->d_vdf, (size_t)n * sizeof(df)) != cudaSuccess) {
+      rc = fail(GS_ERR_OUT_OF_MEMORY, "point set allocation failed");
+    } else {
+      split_df_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256>>>(
+          dim, n, ps->d_x, ps->d_y, ps->d_z, ps->d_v, (df*)ps->d_cdf, (df*)ps->d_vdf);
+      if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+        rc = fail(GS_ERR_CUDA, "point set split failed");
+    }
+  }
   if (rc) {
     delete ps;
     return rc;
@@ -324,6 +357,44 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
         cudaMemcpy(k->d_err, errors, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
       rc = fail(GS_ERR_CUDA, "measurement-error upload failed");
   }
+  // drift basis of every data point (fill_basis, kriging.rs:410-439) and the
+  // measurement errors, as double-float device arrays for the mixed kernel
+  if (!rc && k->p > 0) {
+    const int p = k->p;
+    std::vector<df> basis((size_t)p * n);
+    for (int64_t i = 0; i < n; ++i) {
+      const double* pi = &ps->host[i * dim];
+      double xn[3] = {0, 0, 0};
+      for (int d = 0; d < dim; ++d) xn[d] = (pi[d] - k->center[d]) / k->scale;
+      for (int q = 0; q < p; ++q) {
+        double f = 0.0;
+        if (q == 0) f = 1.0;
+        else if (cfg->method == GS_EXTERNAL_DRIFT)
+          f = (drift[i * k->nv + (q - 1)] - k->dmean[q - 1]) / k->dscale[q - 1];
+        else if (q <= dim) f = xn[q - 1];
+        else {
+          int idx = 1 + dim;
+          for (int u = 0; u < dim; ++u)
+            for (int v = u; v < dim; ++v) {
+              if (idx == q) f = xn[u] * xn[v];
+              ++idx;
+            }
+        }
+        basis[(size_t)q * n + i] = df_from_double(f);
+      }
+    }
+    if (cudaMalloc(&k->d_basis_df, basis.size() * sizeof(df)) != cudaSuccess ||
+        cudaMemcpy(k->d_basis_df, basis.data(), basis.size() * sizeof(df),
+                   cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(GS_ERR_OUT_OF_MEMORY, "drift basis upload failed");
+  }
+  if (!rc && ctor == 2) {
+    std::vector<df> e(n);
+    for (int64_t i = 0; i < n; ++i) e[i] = df_from_double(errors[i]);
+    if (cudaMalloc(&k->d_err_df, n * sizeof(df)) != cudaSuccess ||
+        cudaMemcpy(k->d_err_df, e.data(), n * sizeof(df), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(GS_ERR_OUT_OF_MEMORY, "measurement-error upload failed");
+  }
   k->use_tree = cfg->max_neighbors >= 0 || cfg->has_search_radius || cfg->max_per_octant >= 0;
   if (!rc && k->use_tree) {
     SearchFrame& f = k->frame;
@@ -435,6 +506,11 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   a.val = ps->d_v;
   a.meas_err = k->d_err;
   a.drift = k->d_drift;
+  a.cdf = (const df*)ps->d_cdf;
+  a.vdf = (const df*)ps->d_vdf;
+  a.basis_df = k->d_basis_df;
+  a.err_df = k->d_err_df;
+  a.n = n;
 
   // chunking keeps the neighbour lists within a fixed budget
   const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(nt, (int64_t)(1ll << 30) / (4ll * kout + 16)));

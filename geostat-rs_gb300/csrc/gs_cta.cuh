@@ -28,9 +28,8 @@ struct CtaScratch {
   float* W;      // FP32 work vector (residual)
   float* col;    // 2 x stride column buffers
   float* P;      // nbr x nbr x 4 partial products
-  double* X;     // FP64 solution
-  df* XD;        // solution as df
-  double* red;   // block reduction scratch (>= 2 * warps doubles)
+  df* XD;        // solution (double-float)
+  float* red;    // block reduction scratch (>= 2 * warps floats)
   int* flag;     // shared decision word
 };
 
@@ -55,9 +54,9 @@ __device__ __forceinline__ float sel4(const float* row, int c) {
   return v;
 }
 
-__device__ __forceinline__ void block_max2(double& a, double& b, double* red) {
-  a = warp_max_d(a);
-  b = warp_max_d(b);
+__device__ __forceinline__ void block_max2(float& a, float& b, float* red) {
+  a = warp_max_f(a);
+  b = warp_max_f(b);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();
   if (lane == 0) {
@@ -65,12 +64,12 @@ __device__ __forceinline__ void block_max2(double& a, double& b, double* red) {
     red[2 * w + 1] = b;
   }
   __syncthreads();
-  a = 0.0;
-  b = 0.0;
+  a = 0.0f;
+  b = 0.0f;
   const int nw = blockDim.x >> 5;
   for (int i = 0; i < nw; ++i) {
-    a = fmax(a, red[2 * i]);
-    b = fmax(b, red[2 * i + 1]);
+    a = fmaxf(a, red[2 * i]);
+    b = fmaxf(b, red[2 * i + 1]);
   }
 }
 
@@ -113,7 +112,7 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
   int ib = 0, jb = 0;
   const bool own = tile_of(tid, nbr, ib, jb);
   float T[4][4];
-  double amax_d = 0.0, dummy = 0.0;
+  float amax = 0.0f, dummy = 0.0f;
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -125,10 +124,10 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
         else if (i == j) v = 1.0f;  // padding: decoupled unit pivots
       }
       T[a][b] = v;
-      amax_d = fmax(amax_d, (double)fabsf(v));
+      amax = fmaxf(amax, fabsf(v));
     }
-  block_max2(amax_d, dummy, S.red);
-  const float tol = 1e-6f * (float)amax_d;
+  block_max2(amax, dummy, S.red);
+  const float tol = 1e-6f * amax;
   // publish column 0: rows of block column 0 (tiles (ib, 0))
   if (own && jb == 0) {
 #pragma unroll
@@ -191,17 +190,16 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
   __syncthreads();
   tile_gemv_partial(T, own, ib, jb, nbr, w, S.P);
   __syncthreads();
-  double nx = 0.0;
+  // |x| from the FP32 first solution; refinement moves x by ~1e-4 relative
+  float nx = 0.0f;
   for (int i = tid; i < N; i += nthr) {
     float s = 0.0f;
     for (int q = 0; q < nbr; ++q) s += S.P[((i >> 2) * nbr + q) * 4 + (i & 3)];
-    const double xi = -(double)s;
-    S.X[i] = xi;
-    S.XD[i] = df_from_double(xi);
-    nx = fmax(nx, fabs(xi));
+    S.XD[i] = df_make(-s, 0.0f);
+    nx = fmaxf(nx, fabsf(s));
   }
   block_max2(nx, dummy, S.red);
-  double nd_prev = nx;
+  float nd_prev = nx;
   for (int sweep = 1; sweep <= 4; ++sweep) {
     // residual r = b - A x: two threads per row, each over half the columns
     for (int rbase = 0; rbase < N; rbase += nthr / 2) {
@@ -247,23 +245,18 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
     __syncthreads();
     tile_gemv_partial(T, own, ib, jb, nbr, w, S.P);
     __syncthreads();
-    double nd = 0.0;
-    nx = 0.0;
+    float nd = 0.0f;
     for (int i = tid; i < N; i += nthr) {
       float s = 0.0f;
       for (int q = 0; q < nbr; ++q) s += S.P[((i >> 2) * nbr + q) * 4 + (i & 3)];
-      const double dlt = -(double)s;
-      const double xi = S.X[i] + dlt;
-      S.X[i] = xi;
-      S.XD[i] = df_from_double(xi);
-      nd = fmax(nd, fabs(dlt));
-      nx = fmax(nx, fabs(xi));
+      S.XD[i] = df_add_f(S.XD[i], -s);
+      nd = fmaxf(nd, fabsf(s));
     }
-    block_max2(nd, nx, S.red);
-    if (nd <= 1e-15 * nx) return true;
+    block_max2(nd, dummy, S.red);
+    if (nd <= 1e-15f * nx) return true;
     if (sweep >= 2) {
-      const double rho = nd / nd_prev;
-      if (rho < 0.5 && rho * nd <= 1e-13 * nx) return true;
+      const float rho = nd / nd_prev;
+      if (rho < 0.5f && rho * nd <= 1e-13f * nx) return true;
     }
     nd_prev = nd;
   }

@@ -38,6 +38,8 @@ struct gs_pointset {
   double* d_y = nullptr;
   double* d_z = nullptr;
   double* d_v = nullptr;
+  void* d_cdf = nullptr;  // gs::df[dim][n]: coordinates as double-float, axis-major
+  void* d_vdf = nullptr;  // gs::df[n]: values as double-float
   bool has_dup = false;
   int64_t dup_i = 0, dup_j = 0;
   ~gs_pointset();

@@ -29,6 +29,24 @@ namespace gs {
 
 namespace {
 
+// Basis function k of fill_basis (kriging.rs:410-439) at point pt, FP64.
+template <int D>
+__device__ __forceinline__ double basis_at(const KrigeArgs& a, const double* pt,
+                                           const double* drow, int k) {
+  if (k == 0) return 1.0;
+  if (a.method == GS_EXTERNAL_DRIFT) return (drow[k - 1] - a.dmean[k - 1]) / a.dscale[k - 1];
+  // universal: normalised coordinates, then their degree-2 monomials
+  if (k <= D) return (pt[k - 1] - a.center[k - 1]) / a.scale;
+  int idx = 1 + D;
+  for (int u = 0; u < D; ++u)
+    for (int v = u; v < D; ++v) {
+      if (idx == k)
+        return ((pt[u] - a.center[u]) / a.scale) * ((pt[v] - a.center[v]) / a.scale);
+      ++idx;
+    }
+  return 0.0;
+}
+
 // fill_basis (kriging.rs:410-439) in FP64.
 template <int D>
 __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
@@ -62,10 +80,10 @@ __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
   }
 }
 
-// Shared-memory layout of one system (see mixed_smem_bytes).
+// Shared-memory layout of one system.
 struct MixedLayout {
   int np, nbr;
-  size_t off_a, off_v, off_b, off_xd, off_x, off_z, off_red, off_w, off_col, off_p, off_flag,
+  size_t off_a, off_v, off_b, off_xd, off_z, off_red, off_w, off_col, off_p, off_t, off_flag,
       total;
 };
 
@@ -80,23 +98,31 @@ __host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
     return r;
   };
   L.off_a = take((size_t)L.np * sizeof(df));
-  L.off_v = take((size_t)nf * GS_MIXED_MAX_NEIGHBORS * dim * sizeof(df));
+  L.off_v = take((size_t)nf * dim * GS_MIXED_MAX_NEIGHBORS * sizeof(df));
   L.off_b = take((size_t)nmax * sizeof(df));
-  L.off_xd = take((size_t)nmax * sizeof(df));
-  L.off_x = take((size_t)nmax * sizeof(double));
-  L.off_z = take((size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(double));
-  L.off_red = take(16 * sizeof(double));
+  L.off_xd = take((size_t)4 * L.nbr * sizeof(df));
+  L.off_z = take((size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(df));
+  L.off_red = take(32 * sizeof(float));
   L.off_w = take((size_t)4 * L.nbr * sizeof(float));
   L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
   L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
+  L.off_t = take(8 * sizeof(df));
   L.off_flag = take(16);
   L.total = o;
   return L;
 }
 
+// Exact coordinate coincidence (reference: gamma(0) = 0 only when every
+// separation component is exactly zero, -0 == +0), on the 64-bit patterns.
+__device__ __forceinline__ bool same_double(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+  return x == y || ((x | y) << 1) == 0ull;
+}
+
 template <int D, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevModel m, ExpTable tab_g,
-                                                            DfConsts kc, uint8_t* flag) {
+                                                               DfConsts kc, uint8_t* flag) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
@@ -106,20 +132,21 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
   const Frames fr = frames_of(m);
-  const int NBMAX = GS_MIXED_MAX_NEIGHBORS;
+  const int NB = GS_MIXED_MAX_NEIGHBORS;
   const MixedLayout lay = mixed_layout(a.nmax, fr.nf, D);
   df* A = reinterpret_cast<df*>(smem_raw + lay.off_a);
   df* V = reinterpret_cast<df*>(smem_raw + lay.off_v);
   df* B = reinterpret_cast<df*>(smem_raw + lay.off_b);
+  df* ZV = reinterpret_cast<df*>(smem_raw + lay.off_z);
+  df* TD = reinterpret_cast<df*>(smem_raw + lay.off_t);  // target coordinates, sk mean
   CtaScratch S;
   S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
-  S.X = reinterpret_cast<double*>(smem_raw + lay.off_x);
-  double* Z = reinterpret_cast<double*>(smem_raw + lay.off_z);
-  S.red = reinterpret_cast<double*>(smem_raw + lay.off_red);
+  S.red = reinterpret_cast<float*>(smem_raw + lay.off_red);
   S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
   S.col = reinterpret_cast<float*>(smem_raw + lay.off_col);
   S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
   S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
+  const double* coord[3] = {a.x, a.y, a.z};
   __syncthreads();
 
   for (int64_t it = blockIdx.x; it < a.ntl; it += gridDim.x) {
@@ -140,43 +167,36 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
       }
       continue;
     }
-    if (n > NBMAX) {
+    if (n > NB) {
       if (tid == 0) flag[t] = 1;
       continue;
     }
     const int N = n + p;
     const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+    // target coordinates (and the simple-kriging mean) as df, once per system
+    if (tid < D) TD[tid] = df_from_double(tp[tid]);
+    if (tid == 3) TD[3] = df_from_double(a.sk_mean);
+    // drift basis of the target: one basis function per thread
+    if (tid >= 32 && tid - 32 < p) {
+      const int k = tid - 32;
+      B[n + k] = df_from_double(basis_at<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, k));
+    }
+    __syncthreads();
     // --- per-neighbour data: frames, values, rhs, diagonal, drift rows ---
     for (int i = tid; i < n; i += nthr) {
       const int idx = a.nb[t * (int64_t)a.kout + i];
-      const double pp[3] = {a.x[idx], a.y[idx], D == 3 ? a.z[idx] : 0.0};
-      double u[3];
+      df ud[3];
       bool zero = true;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        u[d] = pp[d] - tp[d];
-        zero = zero && (u[d] == 0.0);
+        ud[d] = df_sub(a.cdf[(int64_t)d * a.n + idx], TD[d]);
+        zero = zero && same_double(coord[d][idx], tp[d]);
       }
-      df ud[3];
-#pragma unroll
-      for (int d = 0; d < D; ++d) ud[d] = df_from_double(u[d]);
-      df h[GS_MAX_STRUCTURES + 1];
-      frame_coords<D>(m, fr, ud, V, NBMAX, i, h);
-      B[i] = zero ? m.c0_df : cov_from_h(m, fr, h, tab, kc);
-      Z[i] = a.val[idx];
-      df diag = m.c0_df;
-      if (a.meas_err) diag = df_add(diag, df_from_double(a.meas_err[idx]));
-      A[pk(i, i)] = diag;
-      if (p > 0) {
-        double f[GS_MIXED_MAX_DRIFT];
-        fill_basis<D>(a, pp, a.drift ? a.drift + (int64_t)idx * a.nv : nullptr, f);
-        for (int k = 0; k < p; ++k) A[pk(n + k, i)] = df_from_double(f[k]);
-      }
-    }
-    if (tid < p) {
-      double f[GS_MIXED_MAX_DRIFT];
-      fill_basis<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, f);
-      B[n + tid] = df_from_double(f[tid]);
+      frame_coords<D>(m, fr, ud, V, NB, i);
+      B[i] = zero ? m.c0_df : cov_origin<D>(m, fr, V, NB, i, tab, kc);
+      ZV[i] = a.vdf[idx];
+      A[pk(i, i)] = a.err_df ? df_add(m.c0_df, a.err_df[idx]) : m.c0_df;
+      for (int k = 0; k < p; ++k) A[pk(n + k, i)] = a.basis_df[(int64_t)k * a.n + idx];
     }
     for (int q = tid; q < p * (p + 1) / 2; q += nthr) {
       int r = 0;
@@ -194,10 +214,7 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
         ++i;
       }
       for (int q = tid; q < npairs; q += nthr) {
-        df h[GS_MAX_STRUCTURES + 1];
-        for (int f = 0; f < fr.nf; ++f)
-          h[f] = norm_df<D>(&V[(f * NBMAX + i) * D], &V[(f * NBMAX + j) * D]);
-        A[pk(i, j)] = cov_from_h(m, fr, h, tab, kc);
+        A[pk(i, j)] = cov_pair<D>(m, fr, V, NB, i, j, tab, kc);
         j += nthr;
         while (j >= i && i < n) {
           j -= i;
@@ -206,33 +223,35 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
       }
     }
     __syncthreads();
-    // --- FP32 L D L^T, FP64-accumulated refinement -----------------------
+    // --- FP32 inverse, double-float refinement ----------------------------
     const bool ok = cta_solve(A, B, N, S);
     if (!ok) {
       if (tid == 0) flag[t] = 1;
       __syncthreads();
       continue;
     }
-    // --- outputs (FP64) ---------------------------------------------------
+    // --- outputs: double-float dot products, FP64 at the end -------------
     if (tid < 32) {
-      double sv = 0.0, sr = 0.0;
+      df sv = df_make(0.0f, 0.0f), sr = df_make(0.0f, 0.0f);
       if (a.method == GS_SIMPLE) {
+        const df mean = TD[3];
         for (int i = tid; i < n; i += 32) {
-          sv += S.X[i] * (Z[i] - a.sk_mean);
-          sr += S.X[i] * df_to_double(B[i]);
+          sv = df_fma_acc(sv, S.XD[i], df_sub(ZV[i], mean));
+          sr = df_fma_acc(sr, S.XD[i], B[i]);
         }
       } else {
-        for (int i = tid; i < n; i += 32) sv += S.X[i] * Z[i];
-        for (int i = tid; i < N; i += 32) sr += S.X[i] * df_to_double(B[i]);
+        for (int i = tid; i < n; i += 32) sv = df_fma_acc(sv, S.XD[i], ZV[i]);
+        for (int i = tid; i < N; i += 32) sr = df_fma_acc(sr, S.XD[i], B[i]);
       }
-      sv = warp_sum_d(sv);
-      sr = warp_sum_d(sr);
+      sv = warp_sum_df(sv);
+      sr = warp_sum_df(sr);
       if (tid == 0) {
-        const double val = a.method == GS_SIMPLE ? a.sk_mean + sv : sv;
+        const double val = a.method == GS_SIMPLE ? a.sk_mean + df_to_double(sv) : df_to_double(sv);
         a.out_v[t] = val;
-        a.out_var[t] = fmax(m.c0 - sr, 0.0);
+        a.out_var[t] = fmax(df_to_double(df_sub(m.c0_df, sr)), 0.0);
         if (a.out_lag)
-          a.out_lag[t] = a.method == GS_SIMPLE ? __longlong_as_double(0x7ff8000000000000ll) : S.X[n];
+          a.out_lag[t] = a.method == GS_SIMPLE ? __longlong_as_double(0x7ff8000000000000ll)
+                                               : df_to_double(S.XD[n]);
         a.out_st[t] = GS_ST_OK;
         flag[t] = 0;
       }

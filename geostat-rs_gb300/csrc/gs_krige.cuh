@@ -28,6 +28,11 @@ struct KrigeArgs {
   const double* y;
   const double* z;
   const double* val;
+  const df* cdf;             // coordinates as df, axis-major (dim x n)
+  const df* vdf;             // values as df
+  const df* basis_df;        // p x n drift basis of the data points (df), or null
+  const df* err_df;          // n measurement-error variances (df), or null
+  int64_t n;                 // data points
   const double* meas_err;    // n or null
   const double* drift;       // n x nv raw covariates or null
   const double* tx;

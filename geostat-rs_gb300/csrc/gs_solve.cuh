@@ -41,61 +41,129 @@ __device__ __forceinline__ Frames frames_of(const DevModel& m) {
   return f;
 }
 
-// Covariance in df from per-frame separation norms h[frame] (all > 0).
-__device__ __forceinline__ df cov_from_h(const DevModel& m, const Frames& fr, const df* h,
-                                         const ExpTable& tab, const DfConsts& k) {
+// Covariance of one structure at separation norm h (> 0), df.
+__device__ __forceinline__ df cov_struct(const DevStruct& st, df h, const ExpTable& tab,
+                                         const DfConsts& k) {
+  const df d = df_mul(h, st.inv_range_df);
+  return df_mul(rho_df(st.kind, d, tab, k), st.sill_df);
+}
+
+// Covariance from a single norm shared by every (isotropic) structure.
+__device__ __forceinline__ df cov_from_norm(const DevModel& m, df h, const ExpTable& tab,
+                                            const DfConsts& k) {
   df c = df_make(0.0f, 0.0f);
-  for (int s = 0; s < m.ns; ++s) {
-    const DevStruct& st = m.s[s];
-    df d = df_mul(h[fr.fid[s]], st.inv_range_df);
-    df r = rho_df(st.kind, d, tab, k);
-    c = df_add_fast(c, df_mul(r, st.sill_df));  // non-negative terms
+#pragma unroll
+  for (int s = 0; s < GS_MAX_STRUCTURES; ++s)
+    if (s < m.ns) c = df_add_fast(c, cov_struct(m.s[s], h, tab, k));  // non-negative terms
+  return c;
+}
+
+// Frame coordinates are stored structure-of-arrays: coordinate d of point i in
+// frame f at V[(f * D + d) * stride + i].
+template <int D>
+__device__ __forceinline__ df vget(const df* V, int stride, int f, int d, int i) {
+  return V[(f * D + d) * stride + i];
+}
+
+// |a - b| in df for points i, j of frame f.  Coordinates are target-relative
+// (a few ranges at most), so the fast difference keeps ~2^-46 relative
+// accuracy on the separation; the squares are non-negative, so their sum needs
+// no extra renormalisation.
+template <int D>
+__device__ __forceinline__ df norm_pair(const df* V, int stride, int f, int i, int j) {
+  df q = df_sqr(df_add_fast(vget<D>(V, stride, f, 0, i), df_neg(vget<D>(V, stride, f, 0, j))));
+#pragma unroll
+  for (int d = 1; d < D; ++d)
+    q = df_add_fast(q, df_sqr(df_add_fast(vget<D>(V, stride, f, d, i),
+                                          df_neg(vget<D>(V, stride, f, d, j)))));
+  return df_sqrt(q);
+}
+
+template <int D>
+__device__ __forceinline__ df norm_origin(const df* V, int stride, int f, int i) {
+  df q = df_sqr(vget<D>(V, stride, f, 0, i));
+#pragma unroll
+  for (int d = 1; d < D; ++d) q = df_add_fast(q, df_sqr(vget<D>(V, stride, f, d, i)));
+  return df_sqrt(q);
+}
+
+// Writes point i's coordinates (identity frame ud) in every frame of the
+// model: frame 0 = identity, frame fr.fid[s] = anisotropic structure s.
+template <int D>
+__device__ __forceinline__ void frame_coords(const DevModel& m, const Frames& fr, const df* ud,
+                                             df* V, int stride, int i) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) V[(0 * D + d) * stride + i] = ud[d];
+#pragma unroll
+  for (int s = 0; s < GS_MAX_STRUCTURES; ++s) {
+    if (s >= m.ns || !m.s[s].aniso) continue;
+    const int f = fr.fid[s];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      df acc = df_mul(m.s[s].rot_df[r * 3 + 0], ud[0]);
+#pragma unroll
+      for (int c = 1; c < D; ++c) acc = df_add(acc, df_mul(m.s[s].rot_df[r * 3 + c], ud[c]));
+      V[(f * D + r) * stride + i] = acc;
+    }
+  }
+}
+
+// Covariance between stored points i and j (all frames of the model).
+template <int D>
+__device__ __forceinline__ df cov_pair(const DevModel& m, const Frames& fr, const df* V,
+                                       int stride, int i, int j, const ExpTable& tab,
+                                       const DfConsts& k) {
+  df c = df_make(0.0f, 0.0f);
+  df hiso = df_make(-1.0f, 0.0f);
+#pragma unroll
+  for (int s = 0; s < GS_MAX_STRUCTURES; ++s) {
+    if (s >= m.ns) break;
+    df h;
+    if (m.s[s].aniso) {
+      h = norm_pair<D>(V, stride, fr.fid[s], i, j);
+    } else {
+      if (hiso.hi < 0.0f) hiso = norm_pair<D>(V, stride, 0, i, j);
+      h = hiso;
+    }
+    c = df_add_fast(c, cov_struct(m.s[s], h, tab, k));
   }
   return c;
 }
 
-// |a - b| in df.  Coordinates are target-relative (a few ranges at most), so
-// the fast difference keeps ~2^-46 relative accuracy on the separation; the
-// squares are non-negative, so their sum needs no extra renormalisation.
+// Covariance between stored point i and the frame origin (the target).
 template <int D>
-__device__ __forceinline__ df norm_df(const df* a, const df* b) {
-  df q = df_sqr(df_add_fast(a[0], df_neg(b[0])));
+__device__ __forceinline__ df cov_origin(const DevModel& m, const Frames& fr, const df* V,
+                                         int stride, int i, const ExpTable& tab,
+                                         const DfConsts& k) {
+  df c = df_make(0.0f, 0.0f);
+  df hiso = df_make(-1.0f, 0.0f);
 #pragma unroll
-  for (int d = 1; d < D; ++d) q = df_add_fast(q, df_sqr(df_add_fast(a[d], df_neg(b[d]))));
-  return df_sqrt(q);
-}
-
-template <int D>
-__device__ __forceinline__ df norm0_df(const df* a) {
-  df q = df_sqr(a[0]);
-#pragma unroll
-  for (int d = 1; d < D; ++d) q = df_add_fast(q, df_sqr(a[d]));
-  return df_sqrt(q);
-}
-
-// Frame coordinates of one point (identity frame in ud already): writes the
-// transformed coordinates of every anisotropic structure's frame to
-// V[(f * stride + i) * D + r] and the norms to h[f].
-template <int D>
-__device__ __forceinline__ void frame_coords(const DevModel& m, const Frames& fr, const df* ud,
-                                             df* V, int stride, int i, df* h) {
-#pragma unroll
-  for (int d = 0; d < D; ++d) V[(0 * stride + i) * D + d] = ud[d];
-  h[0] = norm0_df<D>(ud);
-  for (int s = 0; s < m.ns; ++s) {
-    if (!m.s[s].aniso) continue;
-    const int f = fr.fid[s];
-    df vv[3];
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-      df acc = df_make(0.0f, 0.0f);
-#pragma unroll
-      for (int c = 0; c < D; ++c) acc = df_add(acc, df_mul(m.s[s].rot_df[r * 3 + c], ud[c]));
-      vv[r] = acc;
-      V[(f * stride + i) * D + r] = acc;
+  for (int s = 0; s < GS_MAX_STRUCTURES; ++s) {
+    if (s >= m.ns) break;
+    df h;
+    if (m.s[s].aniso) {
+      h = norm_origin<D>(V, stride, fr.fid[s], i);
+    } else {
+      if (hiso.hi < 0.0f) hiso = norm_origin<D>(V, stride, 0, i);
+      h = hiso;
     }
-    h[f] = norm0_df<D>(vv);
+    c = df_add_fast(c, cov_struct(m.s[s], h, tab, k));
   }
+  return c;
+}
+
+// Compensated accumulation of df products: acc += a * b.
+__device__ __forceinline__ df df_fma_acc(df acc, df a, df b) { return df_add(acc, df_mul(a, b)); }
+
+__device__ __forceinline__ df warp_sum_df(df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    df w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = df_add(v, w);
+  }
+  return v;
 }
 
 }  // namespace gs

@@ -80,6 +80,9 @@ struct VArgs {
   const double* z;
   const double* v;
   double mean;
+  const df* cdf;   // coordinates as df, axis-major
+  const df* vdf;   // values as df
+  df mean_df;
   const int64_t* order;
   const int32_t* nb;
   const int32_t* cnt;
@@ -92,7 +95,7 @@ constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
 
 struct VLayout {
   int np, nbr;
-  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_x, off_z, off_red, off_w, off_col, off_p,
+  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_z, off_red, off_w, off_col, off_p,
       off_flag, total;
 };
 
@@ -108,13 +111,12 @@ __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
   };
   L.off_a = take((size_t)L.np * sizeof(df));
   L.off_h = take((size_t)L.np * sizeof(df));
-  L.off_v = take((size_t)(GS_MAX_STRUCTURES + 1) * m * dim * sizeof(df));
+  L.off_v = take((size_t)(GS_MAX_STRUCTURES + 1) * dim * m * sizeof(df));
   L.off_b = take((size_t)m * sizeof(df));
-  L.off_xd = take((size_t)m * sizeof(df));
+  L.off_xd = take((size_t)4 * L.nbr * sizeof(df));
   L.off_h0 = take((size_t)m * sizeof(df));
-  L.off_x = take((size_t)m * sizeof(double));
-  L.off_z = take((size_t)m * sizeof(double));
-  L.off_red = take(16 * sizeof(double));
+  L.off_z = take((size_t)m * sizeof(df));
+  L.off_red = take(32 * sizeof(float));
   L.off_w = take((size_t)4 * L.nbr * sizeof(float));
   L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
   L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
@@ -125,7 +127,7 @@ __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
 
 template <int D, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTable tab_g,
-                                                               DfConsts kc) {
+                                                                  DfConsts kc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
@@ -141,11 +143,10 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
   df* V = reinterpret_cast<df*>(smem_raw + lay.off_v);
   df* B = reinterpret_cast<df*>(smem_raw + lay.off_b);
   df* H0 = reinterpret_cast<df*>(smem_raw + lay.off_h0);
-  double* Z = reinterpret_cast<double*>(smem_raw + lay.off_z);
+  df* ZV = reinterpret_cast<df*>(smem_raw + lay.off_z);
   CtaScratch S;
   S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
-  S.X = reinterpret_cast<double*>(smem_raw + lay.off_x);
-  S.red = reinterpret_cast<double*>(smem_raw + lay.off_red);
+  S.red = reinterpret_cast<float*>(smem_raw + lay.off_red);
   S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
   S.col = reinterpret_cast<float*>(smem_raw + lay.off_col);
   S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
@@ -155,35 +156,35 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
   for (int64_t k = blockIdx.x; k < a.n; k += gridDim.x) {
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
-    const double zi = a.v[i] - a.mean;
+    const df zi = df_sub(a.vdf[i], a.mean_df);
     if (s == 0) {
       // first point: marginal N(0, sill)
+      const double z = df_to_double(zi);
       for (int c = tid; c < a.ncand; c += nthr) {
         const double sill = a.models[c].c0;
-        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
+        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + z * z / sill);
         a.flag[(int64_t)c * a.n + k] = 0;
       }
       continue;
     }
-    const double pi[3] = {a.x[i], a.y[i], D == 3 ? a.z[i] : 0.0};
     for (int q = tid; q < s; q += nthr) {
       const int j = a.nb[k * (int64_t)M + q];
-      const double u[3] = {a.x[j] - pi[0], a.y[j] - pi[1], D == 3 ? a.z[j] - pi[2] : 0.0};
 #pragma unroll
-      for (int d = 0; d < D; ++d) V[q * D + d] = df_from_double(u[d]);
-      Z[q] = a.v[j] - a.mean;
+      for (int d = 0; d < D; ++d)
+        V[d * M + q] = df_sub(a.cdf[(int64_t)d * a.n + j], a.cdf[(int64_t)d * a.n + i]);
+      ZV[q] = df_sub(a.vdf[j], a.mean_df);
     }
     __syncthreads();
     const int npairs = (s * (s - 1)) >> 1;
     if (a.iso_shared) {
-      for (int q = tid; q < s; q += nthr) H0[q] = norm0_df<D>(&V[q * D]);
+      for (int q = tid; q < s; q += nthr) H0[q] = norm_origin<D>(V, M, 0, q);
       int ii = 1, jj = tid;
       while (jj >= ii && ii < s) {
         jj -= ii;
         ++ii;
       }
       for (int q = tid; q < npairs; q += nthr) {
-        H[pk(ii, jj)] = norm_df<D>(&V[ii * D], &V[jj * D]);
+        H[pk(ii, jj)] = norm_pair<D>(V, M, 0, ii, jj);
         jj += nthr;
         while (jj >= ii && ii < s) {
           jj -= ii;
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
       const Frames fr = frames_of(mdl);
       if (a.iso_shared) {
         for (int q = tid; q < s; q += nthr) {
-          B[q] = cov_from_h(mdl, fr, &H0[q], tab, kc);
+          B[q] = cov_from_norm(mdl, H0[q], tab, kc);
           A[pk(q, q)] = mdl.c0_df;
         }
         int ii = 1, jj = tid;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
           ++ii;
         }
         for (int q = tid; q < npairs; q += nthr) {
-          A[pk(ii, jj)] = cov_from_h(mdl, fr, &H[pk(ii, jj)], tab, kc);
+          A[pk(ii, jj)] = cov_from_norm(mdl, H[pk(ii, jj)], tab, kc);
           jj += nthr;
           while (jj >= ii && ii < s) {
             jj -= ii;
@@ -214,26 +215,12 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
           }
         }
       } else {
-        df* VF = V + M * D;  // frames 1.. (frame 0 is V itself)
         for (int q = tid; q < s; q += nthr) {
-          df hq[GS_MAX_STRUCTURES + 1];
-          hq[0] = norm0_df<D>(&V[q * D]);
-          for (int st = 0; st < mdl.ns; ++st) {
-            if (!mdl.s[st].aniso) continue;
-            const int f = fr.fid[st];
-            df acc3[3];
+          df ud[3];
 #pragma unroll
-            for (int r = 0; r < D; ++r) {
-              df acc = df_make(0.0f, 0.0f);
-#pragma unroll
-              for (int cc = 0; cc < D; ++cc)
-                acc = df_add(acc, df_mul(mdl.s[st].rot_df[r * 3 + cc], V[q * D + cc]));
-              acc3[r] = acc;
-              VF[((f - 1) * M + q) * D + r] = acc;
-            }
-            hq[f] = norm0_df<D>(acc3);
-          }
-          B[q] = cov_from_h(mdl, fr, hq, tab, kc);
+          for (int d = 0; d < D; ++d) ud[d] = V[d * M + q];
+          frame_coords<D>(mdl, fr, ud, V, M, q);
+          B[q] = cov_origin<D>(mdl, fr, V, M, q, tab, kc);
           A[pk(q, q)] = mdl.c0_df;
         }
         __syncthreads();
@@ -243,11 +230,7 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
           ++ii;
         }
         for (int q = tid; q < npairs; q += nthr) {
-          df h[GS_MAX_STRUCTURES + 1];
-          h[0] = norm_df<D>(&V[ii * D], &V[jj * D]);
-          for (int f = 1; f < fr.nf; ++f)
-            h[f] = norm_df<D>(&VF[((f - 1) * M + ii) * D], &VF[((f - 1) * M + jj) * D]);
-          A[pk(ii, jj)] = cov_from_h(mdl, fr, h, tab, kc);
+          A[pk(ii, jj)] = cov_pair<D>(mdl, fr, V, M, ii, jj, tab, kc);
           jj += nthr;
           while (jj >= ii && ii < s) {
             jj -= ii;
@@ -263,16 +246,16 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
         continue;
       }
       if (tid < 32) {
-        double mu = 0.0, red = 0.0;
+        df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
         for (int q = tid; q < s; q += 32) {
-          mu += S.X[q] * Z[q];
-          red += S.X[q] * df_to_double(B[q]);
+          mu = df_fma_acc(mu, S.XD[q], ZV[q]);
+          red = df_fma_acc(red, S.XD[q], B[q]);
         }
-        mu = warp_sum_d(mu);
-        red = warp_sum_d(red);
+        mu = warp_sum_df(mu);
+        red = warp_sum_df(red);
         if (tid == 0) {
-          const double var = fmax(mdl.c0 - red, 1e-12);
-          const double r = zi - mu;
+          const double var = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
+          const double r = df_to_double(df_sub(zi, mu));
           a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
           a.flag[(int64_t)c * a.n + k] = 0;
         }
@@ -458,6 +441,9 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   a.z = ps->d_z;
   a.v = ps->d_v;
   a.mean = P->mean;
+  a.cdf = (const df*)ps->d_cdf;
+  a.vdf = (const df*)ps->d_vdf;
+  a.mean_df = df_from_double(P->mean);
   a.order = P->d_order;
   a.nb = P->d_nb;
   a.cnt = P->d_cnt;
