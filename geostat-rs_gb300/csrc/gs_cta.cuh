@@ -5,13 +5,15 @@
 // i(i+1)/2 + j) lives in shared memory.  Each thread owns one 4x4 tile of the
 // lower triangle (tile (ib, jb), ib >= jb, numbered row by row) in registers.
 // The FP32 hi parts are inverted in place with the symmetric sweep operator
-// (Gauss-Jordan elimination without pivoting: for pivot k, a_ij -= a_ik a_kj /
-// a_kk off row/column k, a_ik /= a_kk, a_kk = -1/a_kk; after all N pivots the
-// tiles hold -A^{-1}).  No pivoting is needed for a positive-definite
-// covariance block bordered by drift rows: the pivots are those of A = L D L^T,
-// positive for the covariance block and negative for the drift block.  Every
-// step reads column k from a shared buffer written by its owners -- one
-// barrier per pivot, every tile busy.
+// applied one 4x4 block at a time (block Gauss-Jordan without pivoting: for
+// pivot block K with P = A_KK, A_IJ -= A_IK P^{-1} A_KJ off block row/column
+// K, A_IK = A_IK P^{-1}, A_KK = -P^{-1}; after every block the tiles hold
+// -A^{-1}).  No pivoting is needed for a positive-definite covariance block
+// bordered by drift rows: the pivots are those of A = L D L^T, positive for
+// the covariance block and negative for the drift block.  Per block step the
+// diagonal-tile owner inverts P in registers, the panel owners publish A_IK
+// and A_IK P^{-1}, and every other tile applies a 64-FMA update -- two
+// barriers per four pivots.
 //
 // The solution and its corrections are tile-parallel matrix-vector products
 // from the registers, reduced in a fixed order (deterministic).  Refinement
@@ -26,7 +28,9 @@ namespace gs {
 
 struct CtaScratch {
   float* W;      // FP32 work vector (residual)
-  float* col;    // 2 x stride column buffers
+  float* pan;    // 2 x nbr x 16: panel blocks A_IK, by block-step parity
+  float* lp;     // 2 x nbr x 16: A_IK P^{-1}, by parity
+  float* pinv;   // 2 x 16: P^{-1}, by parity
   float* P;      // nbr x nbr x 4 partial products
   df* XD;        // solution (double-float)
   float* red;    // block reduction scratch (>= 2 * warps floats)
@@ -73,6 +77,31 @@ __device__ __forceinline__ void block_max2(float& a, float& b, float* red) {
   }
 }
 
+// In-register sweep of a symmetric 4x4 block: P -> -P^{-1}.  Returns false
+// when a pivot is not larger than tol in magnitude.
+__device__ __forceinline__ bool inv4_sweep(float (&P)[4][4], float tol) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float d = P[k][k];
+    ok = ok && (fabsf(d) > tol);
+    const float invd = __fdividef(1.0f, d);
+    float u[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) u[i] = P[i][k];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (i == k && j == k) P[i][j] = -invd;
+        else if (i == k) P[i][j] = u[j] * invd;
+        else if (j == k) P[i][j] = u[i] * invd;
+        else P[i][j] = fmaf(-u[i] * invd, u[j], P[i][j]);
+      }
+  }
+  return ok;
+}
+
 // Writes this tile's share of y = T_full r (T symmetric, lower tiles) to P.
 __device__ __forceinline__ void tile_gemv_partial(const float (&T)[4][4], bool own, int ib, int jb,
                                                   int nbr, const float* r, float* P) {
@@ -102,8 +131,8 @@ __device__ __forceinline__ void tile_gemv_partial(const float (&T)[4][4], bool o
 
 // Solves A X = B (N unknowns) and refines to ~1e-13 relative.  Returns false
 // (uniformly) when a pivot is too small for FP32 or the refinement stalls;
-// the caller then re-solves in FP64.  S.col needs 2 * 4 * nbr floats,
-// S.P nbr * nbr * 4 floats, S.W 4 * nbr floats.
+// the caller then re-solves in FP64.  S.pan and S.lp need 2 * nbr * 16
+// floats, S.pinv 32, S.P nbr * nbr * 4, S.W 4 * nbr; S.flag[0] must be 0.
 static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) {
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
@@ -113,6 +142,7 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
   const bool own = tile_of(tid, nbr, ib, jb);
   float T[4][4];
   float amax = 0.0f, dummy = 0.0f;
+  if (tid == 0) S.flag[0] = 0;
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -128,61 +158,94 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
     }
   block_max2(amax, dummy, S.red);
   const float tol = 1e-6f * amax;
-  // publish column 0: rows of block column 0 (tiles (ib, 0))
-  if (own && jb == 0) {
-#pragma unroll
-    for (int a = 0; a < 4; ++a) S.col[4 * ib + a] = T[a][0];
-  }
-  __syncthreads();
-  for (int k = 0; k < N; ++k) {
-    const float* u = S.col + (k & 1) * stride;
-    const float d = u[k];
-    if (!(fabsf(d) > tol)) return false;  // the same value in every thread
-    const float invd = __fdividef(1.0f, d);
-    const int kb = k >> 2;
+  for (int K = 0; K < nbr; ++K) {
+    const int par = K & 1;
+    float* pan = S.pan + par * nbr * 16;
+    float* lp = S.lp + par * nbr * 16;
+    float* pinv = S.pinv + par * 16;
+    // A: invert the diagonal block; publish the panel blocks A_IK (I != K)
     if (own) {
-      const float4 ur = *reinterpret_cast<const float4*>(u + 4 * ib);
-      const float4 uc = *reinterpret_cast<const float4*>(u + 4 * jb);
-      const float lr[4] = {ur.x * invd, ur.y * invd, ur.z * invd, ur.w * invd};
-      const float cc[4] = {uc.x, uc.y, uc.z, uc.w};
-      if (ib != kb && jb != kb) {
+      if (ib == K && jb == K) {
+        const bool ok = inv4_sweep(T, tol);
+        if (!ok) S.flag[0] = 1;
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 4; ++b) T[a][b] = fmaf(-lr[a], cc[b], T[a][b]);
+          for (int b = 0; b < 4; ++b) pinv[a * 4 + b] = -T[a][b];
+      } else if (jb == K) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+          *reinterpret_cast<float4*>(pan + ib * 16 + a * 4) =
+              make_float4(T[a][0], T[a][1], T[a][2], T[a][3]);
+      } else if (ib == K) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          *reinterpret_cast<float4*>(pan + jb * 16 + b * 4) =
+              make_float4(T[0][b], T[1][b], T[2][b], T[3][b]);
+      }
+    }
+    __syncthreads();
+    if (S.flag[0]) return false;  // the same value in every thread
+    // B: panel owners form A_IK P^{-1}
+    if (own && (jb == K || ib == K) && !(ib == K && jb == K)) {
+      const int I = jb == K ? ib : jb;
+      float pv[4][4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float4 r = *reinterpret_cast<const float4*>(pinv + c * 4);
+        pv[c][0] = r.x; pv[c][1] = r.y; pv[c][2] = r.z; pv[c][3] = r.w;
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const float4 r = *reinterpret_cast<const float4*>(pan + I * 16 + a * 4);
+        const float ra[4] = {r.x, r.y, r.z, r.w};
+        float o[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc = fmaf(ra[c], pv[c][b], acc);
+          o[b] = acc;
+        }
+        *reinterpret_cast<float4*>(lp + I * 16 + a * 4) = make_float4(o[0], o[1], o[2], o[3]);
+      }
+    }
+    __syncthreads();
+    // C: update every tile
+    if (own && !(ib == K && jb == K)) {
+      if (jb == K) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const float4 r = *reinterpret_cast<const float4*>(lp + ib * 16 + a * 4);
+          T[a][0] = r.x; T[a][1] = r.y; T[a][2] = r.z; T[a][3] = r.w;
+        }
+      } else if (ib == K) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const float4 r = *reinterpret_cast<const float4*>(lp + jb * 16 + b * 4);
+          T[0][b] = r.x; T[1][b] = r.y; T[2][b] = r.z; T[3][b] = r.w;
+        }
       } else {
+        // T -= (A_IK P^{-1}) A_JK^T
+        float li[4][4], pj[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const float4 r = *reinterpret_cast<const float4*>(lp + ib * 16 + a * 4);
+          li[a][0] = r.x; li[a][1] = r.y; li[a][2] = r.z; li[a][3] = r.w;
+          const float4 q = *reinterpret_cast<const float4*>(pan + jb * 16 + a * 4);
+          pj[a][0] = q.x; pj[a][1] = q.y; pj[a][2] = q.z; pj[a][3] = q.w;
+        }
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const bool rk = (4 * ib + a) == k, ck = (4 * jb + b) == k;
-            const float gen = fmaf(-lr[a], cc[b], T[a][b]);
-            const float edge = T[a][b] * invd;
-            T[a][b] = (rk && ck) ? -invd : ((rk || ck) ? edge : gen);
+            float acc = T[a][b];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc = fmaf(-li[a][c], pj[b][c], acc);
+            T[a][b] = acc;
           }
       }
     }
-    // publish column k+1 of the updated matrix: block column (tiles (ib, kbn),
-    // rows >= 4 kbn) and block row (tiles (kbn, jb), rows < 4 kbn)
-    const int kn = k + 1;
-    if (own && kn < N) {
-      const int kbn = kn >> 2, kcn = kn & 3;
-      float* cn = S.col + (kn & 1) * stride;
-      if (jb == kbn) {
-#pragma unroll
-        for (int a = 0; a < 4; ++a) cn[4 * ib + a] = sel4(T[a], kcn);
-      } else if (ib == kbn) {
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          float v = T[0][b];
-          v = kcn == 1 ? T[1][b] : v;
-          v = kcn == 2 ? T[2][b] : v;
-          v = kcn == 3 ? T[3][b] : v;
-          cn[4 * jb + b] = v;
-        }
-      }
-    }
-    __syncthreads();
   }
   // T now holds -A^{-1}.  x0 = A^{-1} b_hi
   float* w = S.W;

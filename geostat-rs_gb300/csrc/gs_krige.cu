@@ -83,7 +83,7 @@ __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
 // Shared-memory layout of one system.
 struct MixedLayout {
   int np, nbr;
-  size_t off_a, off_v, off_b, off_xd, off_z, off_red, off_w, off_col, off_p, off_t, off_flag,
+  size_t off_a, off_v, off_b, off_xd, off_z, off_red, off_w, off_pan, off_lp, off_pinv, off_p, off_t, off_flag,
       total;
 };
 
@@ -104,7 +104,9 @@ __host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
   L.off_z = take((size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(df));
   L.off_red = take(32 * sizeof(float));
   L.off_w = take((size_t)4 * L.nbr * sizeof(float));
-  L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
+  L.off_pan = take((size_t)2 * L.nbr * 16 * sizeof(float));
+  L.off_lp = take((size_t)2 * L.nbr * 16 * sizeof(float));
+  L.off_pinv = take(32 * sizeof(float));
   L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
   L.off_t = take(8 * sizeof(df));
   L.off_flag = take(16);
@@ -143,7 +145,9 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
   S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
   S.red = reinterpret_cast<float*>(smem_raw + lay.off_red);
   S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
-  S.col = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.pan = reinterpret_cast<float*>(smem_raw + lay.off_pan);
+  S.lp = reinterpret_cast<float*>(smem_raw + lay.off_lp);
+  S.pinv = reinterpret_cast<float*>(smem_raw + lay.off_pinv);
   S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
   S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
   const double* coord[3] = {a.x, a.y, a.z};

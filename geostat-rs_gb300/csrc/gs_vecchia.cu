@@ -95,7 +95,7 @@ constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
 
 struct VLayout {
   int np, nbr;
-  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_z, off_red, off_w, off_col, off_p,
+  size_t off_a, off_h, off_v, off_b, off_xd, off_h0, off_z, off_red, off_w, off_pan, off_lp, off_pinv, off_p,
       off_flag, total;
 };
 
@@ -118,7 +118,9 @@ __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
   L.off_z = take((size_t)m * sizeof(df));
   L.off_red = take(32 * sizeof(float));
   L.off_w = take((size_t)4 * L.nbr * sizeof(float));
-  L.off_col = take((size_t)2 * 4 * L.nbr * sizeof(float));
+  L.off_pan = take((size_t)2 * L.nbr * 16 * sizeof(float));
+  L.off_lp = take((size_t)2 * L.nbr * 16 * sizeof(float));
+  L.off_pinv = take(32 * sizeof(float));
   L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
   L.off_flag = take(16);
   L.total = o;
@@ -148,7 +150,9 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
   S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
   S.red = reinterpret_cast<float*>(smem_raw + lay.off_red);
   S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
-  S.col = reinterpret_cast<float*>(smem_raw + lay.off_col);
+  S.pan = reinterpret_cast<float*>(smem_raw + lay.off_pan);
+  S.lp = reinterpret_cast<float*>(smem_raw + lay.off_lp);
+  S.pinv = reinterpret_cast<float*>(smem_raw + lay.off_pinv);
   S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
   S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
   __syncthreads();
