@@ -130,8 +130,7 @@ __device__ __forceinline__ df df_sqrt(df s) {
 // (its terms are below 1e-6).  ln2/256 is split as l1 (9 significant bits, so
 // n*l1 is exact for n < 2^15, i.e. d < 88) + l2 + l3; n*l2 is formed exactly.
 struct ExpTable {
-  float hi[256];
-  float lo[256];
+  df v[256];  // 2^(-j/256) as (hi, lo) pairs: one 8-byte load per lookup
 };
 // Uniform df constants, filled on the host (df_consts_host).
 struct DfConsts {
@@ -154,7 +153,7 @@ __device__ __forceinline__ df df_expneg(df d, const ExpTable& tab, const ExpCons
   const df e = df_add_f(q, 1.0f);
   const int j = n & 255;
   const int kk = n >> 8;
-  const df res = df_mul(e, df_make(tab.hi[j], tab.lo[j]));
+  const df res = df_mul(e, tab.v[j]);
   const float sc = __int_as_float((127 - kk) << 23);  // 2^-kk, kk <= 126 for d < 88
   return df_make(res.hi * sc, res.lo * sc);
 }

@@ -26,10 +26,14 @@
 
 namespace gs {
 
+// Panel blocks are 4x4 floats padded to a 20-float stride, so the float4 rows
+// of blocks read by one warp fall on distinct banks.
+#define GS_PB 20
+
 struct CtaScratch {
   float* W;      // FP32 work vector (residual)
-  float* pan;    // 2 x nbr x 16: panel blocks A_IK, by block-step parity
-  float* lp;     // 2 x nbr x 16: A_IK P^{-1}, by parity
+  float* pan;    // 2 x nbr x PB: panel blocks A_IK, by block-step parity
+  float* lp;     // 2 x nbr x PB: A_IK P^{-1}, by parity
   float* pinv;   // 2 x 16: P^{-1}, by parity
   float* P;      // nbr x nbr x 4 partial products
   df* XD;        // solution (double-float)
@@ -131,8 +135,8 @@ __device__ __forceinline__ void tile_gemv_partial(const float (&T)[4][4], bool o
 
 // Solves A X = B (N unknowns) and refines to ~1e-13 relative.  Returns false
 // (uniformly) when a pivot is too small for FP32 or the refinement stalls;
-// the caller then re-solves in FP64.  S.pan and S.lp need 2 * nbr * 16
-// floats, S.pinv 32, S.P nbr * nbr * 4, S.W 4 * nbr; S.flag[0] must be 0.
+// the caller then re-solves in FP64.  S.pan and S.lp need 2 * nbr * GS_PB
+// floats (GS_PB = 20), S.pinv 32, S.P nbr * nbr * 4, S.W 4 * nbr.
 static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScratch& S) {
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
@@ -160,8 +164,8 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
   const float tol = 1e-6f * amax;
   for (int K = 0; K < nbr; ++K) {
     const int par = K & 1;
-    float* pan = S.pan + par * nbr * 16;
-    float* lp = S.lp + par * nbr * 16;
+    float* pan = S.pan + par * nbr * GS_PB;
+    float* lp = S.lp + par * nbr * GS_PB;
     float* pinv = S.pinv + par * 16;
     // A: invert the diagonal block; publish the panel blocks A_IK (I != K)
     if (own) {
@@ -175,12 +179,12 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
       } else if (jb == K) {
 #pragma unroll
         for (int a = 0; a < 4; ++a)
-          *reinterpret_cast<float4*>(pan + ib * 16 + a * 4) =
+          *reinterpret_cast<float4*>(pan + ib * GS_PB + a * 4) =
               make_float4(T[a][0], T[a][1], T[a][2], T[a][3]);
       } else if (ib == K) {
 #pragma unroll
         for (int b = 0; b < 4; ++b)
-          *reinterpret_cast<float4*>(pan + jb * 16 + b * 4) =
+          *reinterpret_cast<float4*>(pan + jb * GS_PB + b * 4) =
               make_float4(T[0][b], T[1][b], T[2][b], T[3][b]);
       }
     }
@@ -197,7 +201,7 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
       }
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        const float4 r = *reinterpret_cast<const float4*>(pan + I * 16 + a * 4);
+        const float4 r = *reinterpret_cast<const float4*>(pan + I * GS_PB + a * 4);
         const float ra[4] = {r.x, r.y, r.z, r.w};
         float o[4];
 #pragma unroll
@@ -207,7 +211,7 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
           for (int c = 0; c < 4; ++c) acc = fmaf(ra[c], pv[c][b], acc);
           o[b] = acc;
         }
-        *reinterpret_cast<float4*>(lp + I * 16 + a * 4) = make_float4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<float4*>(lp + I * GS_PB + a * 4) = make_float4(o[0], o[1], o[2], o[3]);
       }
     }
     __syncthreads();
@@ -216,13 +220,13 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
       if (jb == K) {
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-          const float4 r = *reinterpret_cast<const float4*>(lp + ib * 16 + a * 4);
+          const float4 r = *reinterpret_cast<const float4*>(lp + ib * GS_PB + a * 4);
           T[a][0] = r.x; T[a][1] = r.y; T[a][2] = r.z; T[a][3] = r.w;
         }
       } else if (ib == K) {
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-          const float4 r = *reinterpret_cast<const float4*>(lp + jb * 16 + b * 4);
+          const float4 r = *reinterpret_cast<const float4*>(lp + jb * GS_PB + b * 4);
           T[0][b] = r.x; T[1][b] = r.y; T[2][b] = r.z; T[3][b] = r.w;
         }
       } else {
@@ -230,9 +234,9 @@ static __device__ bool cta_solve(const df* A, const df* B, int N, const CtaScrat
         float li[4][4], pj[4][4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-          const float4 r = *reinterpret_cast<const float4*>(lp + ib * 16 + a * 4);
+          const float4 r = *reinterpret_cast<const float4*>(lp + ib * GS_PB + a * 4);
           li[a][0] = r.x; li[a][1] = r.y; li[a][2] = r.z; li[a][3] = r.w;
-          const float4 q = *reinterpret_cast<const float4*>(pan + jb * 16 + a * 4);
+          const float4 q = *reinterpret_cast<const float4*>(pan + jb * GS_PB + a * 4);
           pj[a][0] = q.x; pj[a][1] = q.y; pj[a][2] = q.z; pj[a][3] = q.w;
         }
 #pragma unroll

@@ -62,8 +62,8 @@ void df_consts_host(ExpTable* tab, DfConsts* k) {
   k->s5l = (float)(s5 - (long double)k->s5h);
   for (int j = 0; j < 256; ++j) {
     const long double v = exp2l(-(long double)j / 256.0L);
-    tab->hi[j] = (float)v;
-    tab->lo[j] = (float)(v - (long double)tab->hi[j]);
+    tab->v[j].hi = (float)v;
+    tab->v[j].lo = (float)(v - (long double)tab->v[j].hi);
   }
 }
 

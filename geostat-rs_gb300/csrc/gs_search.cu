@@ -88,7 +88,7 @@ __global__ void cell_id_kernel(GridDev g, int64_t n, const double* x, const doub
 template <int D>
 __global__ void gather_kernel(int64_t n, const uint32_t* perm, const double* x, const double* y,
                               const double* z, double* sx, double* sy, double* sz,
-                              uint32_t* sidx) {
+                              uint32_t* sidx, GridDev g, float* f) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     uint32_t p = perm[i];
@@ -96,6 +96,9 @@ __global__ void gather_kernel(int64_t n, const uint32_t* perm, const double* x, 
     sy[i] = y[p];
     if (D == 3) sz[i] = z[p];
     sidx[i] = p;
+    f[i] = (float)(x[p] - g.origin[0]);
+    f[n + i] = (float)(y[p] - g.origin[1]);
+    if (D == 3) f[2 * n + i] = (float)(z[p] - g.origin[2]);
   }
 }
 
@@ -164,6 +167,28 @@ __device__ __forceinline__ int shell_size(int r) {
   return D == 2 ? 8 * r : 24 * r * r + 2;
 }
 
+// FP32 bound for the prefilter: every candidate whose exact squared distance
+// is <= T has an FP32 squared distance (from origin-relative FP32
+// coordinates) <= the returned value.  delta bounds the per-axis FP32
+// coordinate error (both roundings); the FP32 sum adds a relative 4 ulp.
+__device__ __forceinline__ float prefilter_bound(double T, double delta, int D) {
+  if (!(T < 1e300)) return __int_as_float(0x7f800000);  // +inf
+  const double sT = sqrt(T);
+  const double b = T * (1.0 + 1.0 / 1048576.0) + 2.0 * D * sT * delta + D * delta * delta +
+                   4.0 * D * 5.96e-8 * sT * delta;
+  return __double2float_ru(b * (1.0 + 1e-6));
+}
+
+// Lane 0: refreshes the cached prefilter bound after a threshold changed.
+template <int NB>
+__device__ __forceinline__ void refresh_bound(const double* thr, float* tfs, double delta, int D,
+                                              float r2f) {
+  double tmax = thr[0];
+#pragma unroll
+  for (int b = 1; b < NB; ++b) tmax = fmax(tmax, thr[b]);
+  tfs[0] = fminf(prefilter_bound(tmax, delta, D), r2f);
+}
+
 // Warp-wide bitonic sort of cap (power of two) entries by (d2, idx).
 __device__ __noinline__ void warp_sort(double* d2, uint32_t* id, int n_valid, int cap, int lane) {
   for (int i = n_valid + lane; i < cap; i += 32) {
@@ -202,13 +227,14 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const int capb = p.capb;
-  const size_t per_warp = (size_t)NB * capb * 12 + NB * 16;
+  const size_t per_warp = (size_t)NB * capb * 12 + NB * 16 + 16;
   unsigned char* base = smem_raw + (size_t)wib * per_warp;
   double* bd2 = reinterpret_cast<double*>(base);
   uint32_t* bid = reinterpret_cast<uint32_t*>(bd2 + NB * capb);
   double* thr = reinterpret_cast<double*>(bid + NB * capb);
   int* cnt = reinterpret_cast<int*>(thr + NB);
   int* dirty = cnt + NB;
+  float* tfs = reinterpret_cast<float*>(dirty + NB);  // cached prefilter bound
   const double kInf = __longlong_as_double(0x7ff0000000000000ll);
   const double r2 = p.has_radius ? p.r2 : kInf;
   const int kb = p.k;
@@ -220,6 +246,16 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
     int tc[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d) tc[d] = clamp_cell((q[d] - g.origin[d]) * g.inv_cell, g.n[d]);
+    // prefilter: FP32 target coordinates and the per-axis error bound
+    float qf[3] = {0.0f, 0.0f, 0.0f};
+    double delta = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double rel = q[d] - g.origin[d];
+      qf[d] = (float)rel;
+      delta = fmax(delta, (g.ext[d] + fabs(rel)) * (1.0 / 8388608.0) + 1e-30);
+    }
+    const float r2f = prefilter_bound(r2, delta, D);
     int maxring = 0;
 #pragma unroll
     for (int d = 0; d < D; ++d) maxring = max(maxring, max(tc[d], g.n[d] - 1 - tc[d]));
@@ -243,6 +279,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
       cnt[lane] = 0;
       dirty[lane] = 0;
     }
+    if (lane == 0) tfs[0] = r2f;
     __syncwarp();
     long long inrad = 0;
     const int64_t qrank = RANKED ? p.rank0 + t : 0;
@@ -352,12 +389,25 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
           const int src = pos & 31;
           const uint32_t sst = __shfl_sync(kFull, cst, src);
           const int sex = __shfl_sync(kFull, excl, src);
-          const bool valid = my < tot;
+          bool valid = my < tot;
           double d2 = kInf;
           uint32_t oid = 0;
           int ob = 0;
+          const uint32_t pi = sst + (uint32_t)(my - sex);
           if (valid) {
-            const uint32_t pi = sst + (uint32_t)(my - sex);
+            // FP32 prefilter against the loosest live threshold
+            const float tf = tfs[0];
+            float e = g.fx[pi] - qf[0];
+            float d2f = e * e;
+            e = g.fy[pi] - qf[1];
+            d2f = fmaf(e, e, d2f);
+            if (D == 3) {
+              e = g.fz[pi] - qf[2];
+              d2f = fmaf(e, e, d2f);
+            }
+            valid = d2f <= tf;
+          }
+          if (valid) {
             const double px = g.sx[pi], py = g.sy[pi];
             const double dx = __dsub_rn(px, q[0]);
             const double dy = __dsub_rn(py, q[1]);
@@ -384,6 +434,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
                 cnt[b] = min(cnt[b], kb);
                 if (cnt[b] >= kb) thr[b] = bd2[b * capb + kb - 1];
                 dirty[b] = 0;
+                refresh_bound<NB>(thr, tfs, delta, D, r2f);
               }
               __syncwarp();
               want = want && d2 <= thr[b];
@@ -412,6 +463,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
             cnt[b] = kb;
             thr[b] = bd2[b * capb + kb - 1];
             dirty[b] = 0;
+            refresh_bound<NB>(thr, tfs, delta, D, r2f);
           }
           __syncwarp();
         }
@@ -466,6 +518,7 @@ Grid::~Grid() {
   cudaFree(d_sz);
   cudaFree(d_sidx);
   cudaFree(d_cstart);
+  cudaFree(d_f);
 }
 
 int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, const double* z,
@@ -569,12 +622,14 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
   if (dim == 3) GS_TRY(dalloc(&g->d_sz, n));
   GS_TRY(dalloc(&g->d_sidx, n));
   GS_TRY(dalloc(&g->d_cstart, total + 1));
+  GS_TRY(dalloc(&g->d_f, 3 * n));
+  for (int d = 0; d < 3; ++d) G.ext[d] = d < dim ? ext[d] : 0.0;
   if (dim == 2)
     gather_kernel<2><<<blocks, threads, 0, stream>>>(n, vals2, tx, ty, tz, g->d_sx, g->d_sy,
-                                                     g->d_sz, g->d_sidx);
+                                                     g->d_sz, g->d_sidx, G, g->d_f);
   else
     gather_kernel<3><<<blocks, threads, 0, stream>>>(n, vals2, tx, ty, tz, g->d_sx, g->d_sy,
-                                                     g->d_sz, g->d_sidx);
+                                                     g->d_sz, g->d_sidx, G, g->d_f);
   GS_CUDA(cudaGetLastError());
   {
     int cb = (int)std::min<int64_t>((total + 1 + threads - 1) / threads, 152 * 32);
@@ -593,6 +648,9 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
   G.sx = g->d_sx;
   G.sy = g->d_sy;
   G.sz = g->d_sz;
+  G.fx = g->d_f;
+  G.fy = g->d_f + n;
+  G.fz = g->d_f + 2 * n;
   G.sidx = g->d_sidx;
   G.cstart = g->d_cstart;
   return GS_OK;

@@ -28,6 +28,12 @@ struct GridDev {
   const double* sz;
   const uint32_t* sidx;    // original index of each sorted point
   const uint32_t* cstart;  // ncells + 1 offsets
+  // FP32 copies of the sorted coordinates relative to the origin, for the
+  // distance prefilter; ext[d] bounds |coordinate - origin| per axis.
+  const float* fx;
+  const float* fy;
+  const float* fz;
+  double ext[3];
 };
 
 struct SearchParams {
@@ -59,6 +65,7 @@ struct Grid {
   double* d_sz = nullptr;
   uint32_t* d_sidx = nullptr;
   uint32_t* d_cstart = nullptr;
+  float* d_f = nullptr;  // 3 x n FP32 prefilter coordinates
   ~Grid();
 };
 

@@ -52,9 +52,8 @@ __device__ __forceinline__ df cov_struct(const DevStruct& st, df h, const ExpTab
 __device__ __forceinline__ df cov_from_norm(const DevModel& m, df h, const ExpTable& tab,
                                             const DfConsts& k) {
   df c = df_make(0.0f, 0.0f);
-#pragma unroll
-  for (int s = 0; s < GS_MAX_STRUCTURES; ++s)
-    if (s < m.ns) c = df_add_fast(c, cov_struct(m.s[s], h, tab, k));  // non-negative terms
+#pragma unroll 1
+  for (int s = 0; s < m.ns; ++s) c = df_add_fast(c, cov_struct(m.s[s], h, tab, k));  // >= 0 terms
   return c;
 }
 
@@ -115,9 +114,8 @@ __device__ __forceinline__ df cov_pair(const DevModel& m, const Frames& fr, cons
                                        const DfConsts& k) {
   df c = df_make(0.0f, 0.0f);
   df hiso = df_make(-1.0f, 0.0f);
-#pragma unroll
-  for (int s = 0; s < GS_MAX_STRUCTURES; ++s) {
-    if (s >= m.ns) break;
+#pragma unroll 1
+  for (int s = 0; s < m.ns; ++s) {
     df h;
     if (m.s[s].aniso) {
       h = norm_pair<D>(V, stride, fr.fid[s], i, j);
@@ -137,9 +135,8 @@ __device__ __forceinline__ df cov_origin(const DevModel& m, const Frames& fr, co
                                          const DfConsts& k) {
   df c = df_make(0.0f, 0.0f);
   df hiso = df_make(-1.0f, 0.0f);
-#pragma unroll
-  for (int s = 0; s < GS_MAX_STRUCTURES; ++s) {
-    if (s >= m.ns) break;
+#pragma unroll 1
+  for (int s = 0; s < m.ns; ++s) {
     df h;
     if (m.s[s].aniso) {
       h = norm_origin<D>(V, stride, fr.fid[s], i);

@@ -118,8 +118,8 @@ __host__ __device__ inline VLayout vecchia_layout(int m, int dim) {
   L.off_z = take((size_t)m * sizeof(df));
   L.off_red = take(32 * sizeof(float));
   L.off_w = take((size_t)4 * L.nbr * sizeof(float));
-  L.off_pan = take((size_t)2 * L.nbr * 16 * sizeof(float));
-  L.off_lp = take((size_t)2 * L.nbr * 16 * sizeof(float));
+  L.off_pan = take((size_t)2 * L.nbr * GS_PB * sizeof(float));
+  L.off_lp = take((size_t)2 * L.nbr * GS_PB * sizeof(float));
   L.off_pinv = take(32 * sizeof(float));
   L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
   L.off_flag = take(16);
@@ -133,8 +133,7 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-    tab.hi[i] = tab_g.hi[i];
-    tab.lo[i] = tab_g.lo[i];
+    tab.v[i] = tab_g.v[i];
   }
   const int tid = threadIdx.x;
   const int nthr = blockDim.x;
