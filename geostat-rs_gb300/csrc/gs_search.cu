@@ -179,6 +179,13 @@ __device__ __forceinline__ float prefilter_bound(double T, double delta, int D) 
   return __double2float_ru(b * (1.0 + 1e-6));
 }
 
+// Shared memory of one warp of knn_kernel: NB buffers of capb (d2, idx)
+// entries, then NB thresholds, counts and dirty flags, then the cached
+// prefilter bound.  Used by both the kernel and its launch.
+__host__ __device__ inline size_t knn_per_warp(int NB, int capb) {
+  return (size_t)NB * capb * 12 + (size_t)NB * 16 + 16;
+}
+
 // Lane 0: refreshes the cached prefilter bound after a threshold changed.
 template <int NB>
 __device__ __forceinline__ void refresh_bound(const double* thr, float* tfs, double delta, int D,
@@ -227,7 +234,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const int capb = p.capb;
-  const size_t per_warp = (size_t)NB * capb * 12 + NB * 16 + 16;
+  const size_t per_warp = knn_per_warp(NB, capb);
   unsigned char* base = smem_raw + (size_t)wib * per_warp;
   double* bd2 = reinterpret_cast<double*>(base);
   uint32_t* bid = reinterpret_cast<uint32_t*>(bd2 + NB * capb);
@@ -671,7 +678,7 @@ int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p
   p.capb = (int)ceil_pow2((unsigned)std::max(p.k + 32, 64));
   const int NB = p.octant ? (1 << g.dim) : 1;
   const int wpb = 4;
-  size_t per_warp = (size_t)NB * p.capb * 12 + NB * 16;
+  const size_t per_warp = knn_per_warp(NB, p.capb);
   size_t smem = per_warp * wpb;
   static const size_t kMaxSmem = 227 * 1024;
   if (smem > kMaxSmem) return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood too large for the device search");
