@@ -186,35 +186,53 @@ __host__ __device__ inline size_t knn_per_warp(int NB, int capb) {
   return (size_t)NB * capb * 12 + (size_t)NB * 16 + 16;
 }
 
-// Lane 0: refreshes the cached prefilter bound after a threshold changed.
-template <int NB>
-__device__ __forceinline__ void refresh_bound(const double* thr, float* tfs, double delta, int D,
-                                              float r2f) {
-  double tmax = thr[0];
-#pragma unroll
-  for (int b = 1; b < NB; ++b) tmax = fmax(tmax, thr[b]);
-  tfs[0] = fminf(prefilter_bound(tmax, delta, D), r2f);
+// Squared distances are never negative (and never -0: they are sums of
+// squares), so the IEEE bit pattern of a squared distance, read as an
+// unsigned integer, orders exactly like the value; +inf is the largest key.
+// The search compares these keys on the integer pipes: an FP64 compare costs
+// as much issue time as dozens of integer instructions on this GPU.
+typedef unsigned long long dkey;
+constexpr dkey kInfKey = 0x7ff0000000000000ull;
+
+__device__ __forceinline__ dkey d2key(double d2) { return (dkey)__double_as_longlong(d2); }
+
+// True when a >= b for doubles given a - b (IEEE: a - b is +/-0 only when
+// a == b, and its sign is that of a - b otherwise).
+__device__ __forceinline__ bool diff_nonneg(double diff) {
+  const dkey u = (dkey)__double_as_longlong(diff);
+  return (u >> 63) == 0 || (u << 1) == 0;
 }
 
-// Warp-wide bitonic sort of cap (power of two) entries by (d2, idx).
-__device__ __noinline__ void warp_sort(double* d2, uint32_t* id, int n_valid, int cap, int lane) {
+// Lane 0: refreshes the cached prefilter bound after a threshold changed.
+template <int NB>
+__device__ __forceinline__ void refresh_bound(const dkey* thr, float* tfs, double delta, int D,
+                                              float r2f) {
+  dkey tmax = thr[0];
+#pragma unroll
+  for (int b = 1; b < NB; ++b) tmax = tmax > thr[b] ? tmax : thr[b];
+  tfs[0] = fminf(prefilter_bound(__longlong_as_double((long long)tmax), delta, D), r2f);
+}
+
+// Warp-wide bitonic sort of cap (power of two) entries by (d2, idx), keys as
+// in d2key.
+__device__ __noinline__ void warp_sort(dkey* key, uint32_t* id, int n_valid, int cap, int lane) {
   for (int i = n_valid + lane; i < cap; i += 32) {
-    d2[i] = __longlong_as_double(0x7ff0000000000000ll);
+    key[i] = kInfKey;
     id[i] = 0xffffffffu;
   }
   __syncwarp();
   for (int size = 2; size <= cap; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
       for (int i = lane; i < (cap >> 1); i += 32) {
-        int a = 2 * stride * (i / stride) + (i % stride);
-        int b = a + stride;
-        bool up = (a & size) == 0;
-        double da = d2[a], db = d2[b];
-        uint32_t ia = id[a], ib = id[b];
-        bool gt = (da > db) || (da == db && ia > ib);
+        const int a = 2 * stride * (i / stride) + (i % stride);
+        const int b = a + stride;
+        const bool up = (a & size) == 0;
+        const dkey ka = key[a], kb = key[b];
+        const uint32_t ia = id[a], ib = id[b];
+        const bool gt = (ka > kb) || (ka == kb && ia > ib);
         if (gt == up) {
-          d2[a] = db;
-          d2[b] = da;
+          key[a] = kb;
+          key[b] = ka;
           id[a] = ib;
           id[b] = ia;
         }
@@ -236,14 +254,15 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
   const int capb = p.capb;
   const size_t per_warp = knn_per_warp(NB, capb);
   unsigned char* base = smem_raw + (size_t)wib * per_warp;
-  double* bd2 = reinterpret_cast<double*>(base);
+  dkey* bd2 = reinterpret_cast<dkey*>(base);
   uint32_t* bid = reinterpret_cast<uint32_t*>(bd2 + NB * capb);
-  double* thr = reinterpret_cast<double*>(bid + NB * capb);
+  dkey* thr = reinterpret_cast<dkey*>(bid + NB * capb);
   int* cnt = reinterpret_cast<int*>(thr + NB);
   int* dirty = cnt + NB;
   float* tfs = reinterpret_cast<float*>(dirty + NB);  // cached prefilter bound
   const double kInf = __longlong_as_double(0x7ff0000000000000ll);
   const double r2 = p.has_radius ? p.r2 : kInf;
+  const dkey r2k = d2key(r2);
   const int kb = p.k;
 
   for (int64_t t = (int64_t)blockIdx.x * wpb + wib; t < nt; t += (int64_t)gridDim.x * wpb) {
@@ -282,7 +301,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
       octmax[b] = m;
     }
     if (lane < NB) {
-      thr[lane] = kInf;
+      thr[lane] = kInfKey;
       cnt[lane] = 0;
       dirty[lane] = 0;
     }
@@ -305,7 +324,8 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
             d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
           }
         }
-        bool want = valid && d2 <= r2 && d2 <= thr[0];
+        const dkey k2 = d2key(d2);
+        bool want = valid && k2 <= r2k && k2 <= thr[0];
         unsigned m = __ballot_sync(kFull, want);
         if (!m) continue;
         if (cnt[0] + __popc(m) > capb) {
@@ -315,12 +335,12 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
             if (cnt[0] >= kb) thr[0] = bd2[kb - 1];
           }
           __syncwarp();
-          want = want && d2 <= thr[0];
+          want = want && k2 <= thr[0];
           m = __ballot_sync(kFull, want);
         }
         if (want) {
           int slot = cnt[0] + __popc(m & ((1u << lane) - 1u));
-          bd2[slot] = d2;
+          bd2[slot] = k2;
           bid[slot] = (uint32_t)r;
         }
         __syncwarp();
@@ -335,11 +355,11 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
 
     for (int ring = 0; ring <= maxring; ++ring) {
       double rmin = fmax((double)ring - 1.0 - 1e-9, 0.0) * g.cell;
-      double rmin2 = rmin * rmin;
+      const dkey rmin2k = d2key(rmin * rmin);
       unsigned active = 0;
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
-        bool done = (rmin2 > r2) || (cnt[b] >= kb && rmin2 > thr[b]) || (ring > octmax[b]);
+        bool done = (rmin2k > r2k) || (cnt[b] >= kb && rmin2k > thr[b]) || (ring > octmax[b]);
         if (!done) active |= 1u << b;
       }
       if (!active) break;
@@ -419,20 +439,21 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
             const double dx = __dsub_rn(px, q[0]);
             const double dy = __dsub_rn(py, q[1]);
             d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-            if (OCT) ob = (px >= q[0] ? 1 : 0) | (py >= q[1] ? 2 : 0);
+            if (OCT) ob = (diff_nonneg(dx) ? 1 : 0) | (diff_nonneg(dy) ? 2 : 0);
             if (D == 3) {
               const double pz = g.sz[pi];
               const double dz = __dsub_rn(pz, q[2]);
               d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
-              if (OCT) ob |= (pz >= q[2] ? 4 : 0);
+              if (OCT) ob |= (diff_nonneg(dz) ? 4 : 0);
             }
             oid = g.sidx[pi];
           }
-          const bool inr = valid && d2 <= r2 && (!RANKED || (int64_t)oid < qrank);
+          const dkey k2 = d2key(d2);
+          const bool inr = valid && k2 <= r2k && (!RANKED || (int64_t)oid < qrank);
           if (p.unbounded) inrad += __popc(__ballot_sync(kFull, inr));
 #pragma unroll
           for (int b = 0; b < NB; ++b) {
-            bool want = inr && (ob == b) && d2 <= thr[b];
+            bool want = inr && (ob == b) && k2 <= thr[b];
             unsigned m = __ballot_sync(kFull, want);
             if (!m) continue;
             if (cnt[b] + __popc(m) > capb) {
@@ -444,12 +465,12 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
                 refresh_bound<NB>(thr, tfs, delta, D, r2f);
               }
               __syncwarp();
-              want = want && d2 <= thr[b];
+              want = want && k2 <= thr[b];
               m = __ballot_sync(kFull, want);
             }
             if (want) {
               int slot = cnt[b] + __popc(m & ((1u << lane) - 1u));
-              bd2[b * capb + slot] = d2;
+              bd2[b * capb + slot] = k2;
               bid[b * capb + slot] = oid;
             }
             __syncwarp();
@@ -487,7 +508,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
         int c = min(cnt[b], kb);
         total += c;
         for (int i = c + lane; i < capb; i += 32) {
-          bd2[b * capb + i] = kInf;
+          bd2[b * capb + i] = kInfKey;
           bid[b * capb + i] = 0xffffffffu;
         }
       }

@@ -28,6 +28,7 @@
 #include "gs_search.cuh"
 #include "gs_cta.cuh"
 #include "gs_solve.cuh"
+#include "gs_warp.cuh"
 
 struct gs_vecchia_plan {
   const gs_pointset* ps = nullptr;
@@ -268,6 +269,166 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
   }
 }
 
+// Per-warp shared-memory layout of vecchia_warp_kernel (conditioning sets of
+// at most 32 points).
+struct VWLayout {
+  size_t off_a, off_h, off_v, off_b, off_h0, off_z, off_row, off_vec, off_xd, total;
+};
+
+__host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim) {
+  VWLayout L;
+  const int np = m * (m + 1) / 2;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = o;
+    o += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  L.off_a = take((size_t)np * sizeof(df));
+  L.off_h = take((size_t)np * sizeof(df));
+  L.off_v = take((size_t)(GS_MAX_STRUCTURES + 1) * dim * m * sizeof(df));
+  L.off_b = take((size_t)m * sizeof(df));
+  L.off_h0 = take((size_t)m * sizeof(df));
+  L.off_z = take((size_t)m * sizeof(df));
+  L.off_row = take(kWarpN * sizeof(float));
+  L.off_vec = take(kWarpN * sizeof(float));
+  L.off_xd = take(kWarpN * sizeof(df));
+  L.total = o;
+  return L;
+}
+
+constexpr int kVWarps = 4;  // warps (ordered points in flight) per block
+
+// One warp per ordered point for conditioning sets of at most 32 points: the
+// same assembly and certification as vecchia_loglik_kernel, with the
+// register-row solver of gs_warp.cuh (no block barriers).
+template <int D>
+__global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, ExpTable tab_g,
+                                                                   DfConsts kc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ ExpTable tab;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tab.v[i] = tab_g.v[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int M = a.m;
+  const VWLayout lay = vecchia_warp_layout(M, D);
+  unsigned char* base = smem_raw + (size_t)wib * lay.total;
+  df* A = reinterpret_cast<df*>(base + lay.off_a);
+  df* H = reinterpret_cast<df*>(base + lay.off_h);
+  df* V = reinterpret_cast<df*>(base + lay.off_v);
+  df* B = reinterpret_cast<df*>(base + lay.off_b);
+  df* H0 = reinterpret_cast<df*>(base + lay.off_h0);
+  df* ZV = reinterpret_cast<df*>(base + lay.off_z);
+  WarpScratch W;
+  W.row = reinterpret_cast<float*>(base + lay.off_row);
+  W.vec = reinterpret_cast<float*>(base + lay.off_vec);
+  W.xd = reinterpret_cast<df*>(base + lay.off_xd);
+  const int64_t nwarps = (int64_t)gridDim.x * kVWarps;
+  for (int64_t k = (int64_t)blockIdx.x * kVWarps + wib; k < a.n; k += nwarps) {
+    const int64_t i = a.order[k];
+    const int s = a.cnt[k];
+    const df zi = df_sub(a.vdf[i], a.mean_df);
+    if (s == 0) {
+      const double z = df_to_double(zi);
+      for (int c = lane; c < a.ncand; c += 32) {
+        const double sill = a.models[c].c0;
+        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + z * z / sill);
+        a.flag[(int64_t)c * a.n + k] = 0;
+      }
+      continue;
+    }
+    __syncwarp();
+    if (lane < s) {
+      const int j = a.nb[k * (int64_t)M + lane];
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        V[d * M + lane] = df_sub(a.cdf[(int64_t)d * a.n + j], a.cdf[(int64_t)d * a.n + i]);
+      ZV[lane] = df_sub(a.vdf[j], a.mean_df);
+    }
+    __syncwarp();
+    const int npairs = (s * (s - 1)) >> 1;
+    // first pair (ii, jj) of this lane in the packed strict lower triangle
+    int ii0 = 1, jj0 = lane;
+    while (jj0 >= ii0 && ii0 < s) {
+      jj0 -= ii0;
+      ++ii0;
+    }
+    if (a.iso_shared) {
+      if (lane < s) H0[lane] = norm_origin<D>(V, M, 0, lane);
+      int ii = ii0, jj = jj0;
+      for (int q = lane; q < npairs; q += 32) {
+        H[pk(ii, jj)] = norm_pair<D>(V, M, 0, ii, jj);
+        jj += 32;
+        while (jj >= ii && ii < s) {
+          jj -= ii;
+          ++ii;
+        }
+      }
+      __syncwarp();
+    }
+    for (int c = 0; c < a.ncand; ++c) {
+      const DevModel& mdl = a.models[c];
+      const Frames fr = frames_of(mdl);
+      if (a.iso_shared) {
+        if (lane < s) {
+          B[lane] = cov_from_norm(mdl, H0[lane], tab, kc);
+          A[pk(lane, lane)] = mdl.c0_df;
+        }
+        int ii = ii0, jj = jj0;
+        for (int q = lane; q < npairs; q += 32) {
+          A[pk(ii, jj)] = cov_from_norm(mdl, H[pk(ii, jj)], tab, kc);
+          jj += 32;
+          while (jj >= ii && ii < s) {
+            jj -= ii;
+            ++ii;
+          }
+        }
+      } else {
+        if (lane < s) {
+          df ud[3];
+#pragma unroll
+          for (int d = 0; d < D; ++d) ud[d] = V[d * M + lane];
+          frame_coords<D>(mdl, fr, ud, V, M, lane);
+          B[lane] = cov_origin<D>(mdl, fr, V, M, lane, tab, kc);
+          A[pk(lane, lane)] = mdl.c0_df;
+        }
+        __syncwarp();
+        int ii = ii0, jj = jj0;
+        for (int q = lane; q < npairs; q += 32) {
+          A[pk(ii, jj)] = cov_pair<D>(mdl, fr, V, M, ii, jj, tab, kc);
+          jj += 32;
+          while (jj >= ii && ii < s) {
+            jj -= ii;
+            ++ii;
+          }
+        }
+      }
+      __syncwarp();
+      const bool ok = warp_solve(A, B, s, lane, W);
+      if (!ok) {
+        if (lane == 0) a.flag[(int64_t)c * a.n + k] = 1;
+        __syncwarp();
+        continue;
+      }
+      df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
+      if (lane < s) {
+        mu = df_fma_acc(mu, W.xd[lane], ZV[lane]);
+        red = df_fma_acc(red, W.xd[lane], B[lane]);
+      }
+      mu = warp_sum_df(mu);
+      red = warp_sum_df(red);
+      if (lane == 0) {
+        const double var = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
+        const double r = df_to_double(df_sub(zi, mu));
+        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+        a.flag[(int64_t)c * a.n + k] = 0;
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // FP64 per-(candidate, point) solve: cholesky_solve_in_place
 // (linalg.rs:123-203) on the assembled K_SS of vecchia.rs:302-320.
 template <int D>
@@ -457,20 +618,32 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   DevBuf list;
   const bool mixed = precision != GS_PREC_FP64 && M <= GS_MIXED_MAX_NEIGHBORS;
   if (mixed) {
-    const VLayout lay = vecchia_layout(std::max(M, 1), dim);
-    const size_t smem = lay.total;
-    const int tiles = lay.nbr * (lay.nbr + 1) / 2;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int block = std::min(256, std::max(64, ((tiles + 31) / 32) * 32));
-    auto kern = dim == 2 ? vecchia_loglik_kernel<2, 256> : vecchia_loglik_kernel<3, 256>;
-    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
-    per_sm = std::max(per_sm, 1);
-    const int blocks = (int)std::min<int64_t>(n, (int64_t)sms * per_sm);
-    kern<<<blocks, block, smem, s>>>(a, g_vtab, g_vkc);
+    if (M <= kWarpN) {
+      const size_t smem = vecchia_warp_layout(std::max(M, 1), dim).total * kVWarps;
+      auto kern = dim == 2 ? vecchia_warp_kernel<2> : vecchia_warp_kernel<3>;
+      GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int per_sm = 0;
+      GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kVWarps, smem));
+      per_sm = std::max(per_sm, 1);
+      const int blocks =
+          (int)std::min<int64_t>((n + kVWarps - 1) / kVWarps, (int64_t)sms * per_sm);
+      kern<<<blocks, 32 * kVWarps, smem, s>>>(a, g_vtab, g_vkc);
+    } else {
+      const VLayout lay = vecchia_layout(std::max(M, 1), dim);
+      const size_t smem = lay.total;
+      const int tiles = lay.nbr * (lay.nbr + 1) / 2;
+      const int block = std::min(256, std::max(64, ((tiles + 31) / 32) * 32));
+      auto kern = dim == 2 ? vecchia_loglik_kernel<2, 256> : vecchia_loglik_kernel<3, 256>;
+      GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int per_sm = 0;
+      GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+      per_sm = std::max(per_sm, 1);
+      const int blocks = (int)std::min<int64_t>(n, (int64_t)sms * per_sm);
+      kern<<<blocks, block, smem, s>>>(a, g_vtab, g_vkc);
+    }
     GS_CUDA(cudaGetLastError());
     count_launch(1);
     // compact flagged (candidate, point) pairs

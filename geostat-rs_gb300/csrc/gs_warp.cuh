@@ -1,0 +1,152 @@
+// gs_warp.cuh -- one small symmetric system (N <= 32) per warp, rows in
+// registers: FP32 inversion by the sweep operator and double-float refinement.
+//
+// Lane i holds row i of the working matrix in registers.  Pivot k: lane k
+// publishes its row through shared memory, with its pivot entry replaced by
+// d - 1 (d = a_kk); every lane then applies the same update
+//     t[j] -= l * row_k[j]   for all j,
+// with l = a_ik / d on lane i != k and l = 1 - 1/d on lane k.  This single
+// uniform update is the sweep operator (a_ij -= a_ik a_kj / d, a_ik = a_ik/d,
+// a_kj = a_kj/d) except on lane k's own diagonal, which ends at 2 - 1/d instead
+// of -1/d.  Later pivots change that entry linearly, so after all N pivots
+// every lane's diagonal is exactly 2 too large and the rows hold -A^{-1}
+// (diagonal corrected once).  No per-element selects and no register-array
+// indexing are needed.  Symmetry gives a_ik as row_k[i].
+//
+// Refinement residuals b - A x use the double-float entries held in registers
+// (compensated FP32 dot products, Ogita, Rump & Oishi 2005); corrections are
+// register GEMVs with -A^{-1}.
+#pragma once
+
+#include "gs_solve.cuh"
+
+namespace gs {
+
+constexpr int kWarpN = 32;
+
+struct WarpScratch {
+  float* row;  // 32 (+1 for d) floats: the published pivot row
+  float* vec;  // 32 floats: broadcast vector
+  df* xd;      // 32 df: solution
+};
+
+// Loads row `lane` of the packed df matrix A (N x N) into registers; rows and
+// columns beyond N hold the identity.
+__device__ __forceinline__ void warp_load_rows(const df* A, int N, int lane, float (&ah)[kWarpN],
+                                               float (&al)[kWarpN]) {
+#pragma unroll
+  for (int j = 0; j < kWarpN; ++j) {
+    df v = df_make(j == lane ? 1.0f : 0.0f, 0.0f);
+    if (lane < N && j < N) v = lane >= j ? A[pk(lane, j)] : A[pk(j, lane)];
+    ah[j] = v.hi;
+    al[j] = v.lo;
+  }
+}
+
+__device__ __forceinline__ void warp_gemv_neg_inv(const float (&t)[kWarpN], const float* vec,
+                                                  int lane, float& y) {
+  // y = (-A^{-1}) v with the +2 diagonal offset removed
+  float s = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kWarpN; j += 4) {
+    const float4 v = *reinterpret_cast<const float4*>(vec + j);
+    s = fmaf(t[j], v.x, s);
+    s = fmaf(t[j + 1], v.y, s);
+    s = fmaf(t[j + 2], v.z, s);
+    s = fmaf(t[j + 3], v.w, s);
+  }
+  y = fmaf(-2.0f, vec[lane], s);
+}
+
+// Solves A x = B (N <= 32 unknowns) and refines to ~1e-13 relative; on
+// success W.xd[i] holds x_i.  Returns false (uniformly in the warp) when a
+// pivot is too small for FP32 or the refinement stalls.
+__device__ bool warp_solve(const df* A, const df* B, int N, int lane, const WarpScratch& W) {
+  float ah[kWarpN], al[kWarpN], t[kWarpN];
+  warp_load_rows(A, N, lane, ah, al);
+  float amax = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kWarpN; ++j) {
+    t[j] = ah[j];
+    amax = fmaxf(amax, fabsf(ah[j]));
+  }
+  amax = warp_max_f(amax);
+  const float tol = 1e-6f * amax;
+  for (int k = 0; k < N; ++k) {
+    if (lane == k) {
+#pragma unroll
+      for (int j = 0; j < kWarpN; j += 4)
+        *reinterpret_cast<float4*>(W.row + j) = make_float4(t[j], t[j + 1], t[j + 2], t[j + 3]);
+    }
+    __syncwarp();
+    const float d = W.row[k];
+    __syncwarp();
+    if (lane == k) W.row[k] = d - 1.0f;
+    __syncwarp();
+    if (!(fabsf(d) > tol)) return false;  // the same value in every lane
+    const float invd = __frcp_rn(d);
+    const float l = lane == k ? 1.0f - invd : W.row[lane] * invd;
+#pragma unroll
+    for (int j = 0; j < kWarpN; j += 4) {
+      const float4 r = *reinterpret_cast<const float4*>(W.row + j);
+      t[j] = fmaf(-l, r.x, t[j]);
+      t[j + 1] = fmaf(-l, r.y, t[j + 1]);
+      t[j + 2] = fmaf(-l, r.z, t[j + 2]);
+      t[j + 3] = fmaf(-l, r.w, t[j + 3]);
+    }
+    __syncwarp();
+  }
+  // x0 = A^{-1} b_hi = -(-A^{-1}) b_hi
+  W.vec[lane] = lane < N ? B[lane].hi : 0.0f;
+  __syncwarp();
+  float y;
+  warp_gemv_neg_inv(t, W.vec, lane, y);
+  df x = df_make(lane < N ? -y : 0.0f, 0.0f);
+  const float nx = warp_max_f(fabsf(x.hi));
+  float nd_prev = nx;
+  for (int sweep = 1; sweep <= 4; ++sweep) {
+    // residual of row `lane`: b - A x, compensated, x broadcast as df
+    __syncwarp();
+    W.xd[lane] = x;
+    __syncwarp();
+    float s = lane < N ? B[lane].hi : 0.0f, c = lane < N ? B[lane].lo : 0.0f;
+#pragma unroll
+    for (int j = 0; j < kWarpN; ++j) {
+      const df xj = W.xd[j];
+      const float ph = __fmul_rn(-ah[j], xj.hi);
+      float pe = __fmaf_rn(-ah[j], xj.hi, -ph);
+      pe = __fmaf_rn(-ah[j], xj.lo, pe);
+      pe = __fmaf_rn(-al[j], xj.hi, pe);
+      const float tsum = __fadd_rn(s, ph);
+      const float bb = __fsub_rn(tsum, s);
+      const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
+      s = tsum;
+      c += e + pe;
+    }
+    const float r = lane < N ? s + c : 0.0f;
+    __syncwarp();
+    W.vec[lane] = r;
+    __syncwarp();
+    warp_gemv_neg_inv(t, W.vec, lane, y);
+    if (lane < N) x = df_add_f(x, -y);
+    const float nd = warp_max_f(lane < N ? fabsf(y) : 0.0f);
+    if (nd <= 1e-15f * nx) {
+      W.xd[lane] = x;
+      __syncwarp();
+      return true;
+    }
+    if (sweep >= 2) {
+      const float rho = nd / nd_prev;
+      if (rho < 0.5f && rho * nd <= 1e-13f * nx) {
+        __syncwarp();
+        W.xd[lane] = x;
+        __syncwarp();
+        return true;
+      }
+    }
+    nd_prev = nd;
+  }
+  return false;
+}
+
+}  // namespace gs
