@@ -13,6 +13,7 @@
 #include "gs_common.cuh"
 #include "gs_host.h"
 #include "gs_internal.h"
+#include "gs_kriging_handle.h"
 #include "gs_krige.cuh"
 #include "gs_search.cuh"
 
@@ -84,33 +85,6 @@ __global__ void split_df_kernel(int dim, int64_t n, const double* x, const doubl
 
 }  // namespace
 
-struct gs_kriging {
-  const gs_pointset* ps = nullptr;
-  gs_kcfg cfg{};
-  gs_model model{};
-  DevModel dm{};
-  int p = 0;
-  int nv = 0;
-  double center[3] = {0, 0, 0};
-  double scale = 1.0;
-  double dmean[GS_MAX_KED_VARS] = {0};
-  double dscale[GS_MAX_KED_VARS] = {0};
-  double* d_drift = nullptr;
-  double* d_err = nullptr;
-  df* d_basis_df = nullptr;  // p x n drift basis of the data points
-  df* d_err_df = nullptr;    // measurement errors as df
-  bool use_tree = false;
-  SearchFrame frame{};
-  Grid grid;
-  cudaStream_t stream = nullptr;
-  ~gs_kriging() {
-    cudaFree(d_drift);
-    cudaFree(d_err);
-    cudaFree(d_basis_df);
-    cudaFree(d_err_df);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
 
 extern "C" {
 

@@ -1,0 +1,36 @@
+// gs_kriging_handle.h -- the predictor behind the opaque gs_kriging handle,
+// shared by the C-ABI translation units.
+#pragma once
+
+#include "gs_common.cuh"
+#include "gs_internal.h"
+#include "gs_krige.cuh"
+#include "gs_search.cuh"
+
+struct gs_kriging {
+  const gs_pointset* ps = nullptr;
+  gs_kcfg cfg{};
+  gs_model model{};
+  gs::DevModel dm{};
+  int p = 0;
+  int nv = 0;
+  double center[3] = {0, 0, 0};
+  double scale = 1.0;
+  double dmean[GS_MAX_KED_VARS] = {0};
+  double dscale[GS_MAX_KED_VARS] = {0};
+  double* d_drift = nullptr;
+  double* d_err = nullptr;
+  gs::df* d_basis_df = nullptr;  // p x n drift basis of the data points
+  gs::df* d_err_df = nullptr;    // measurement errors as df
+  bool use_tree = false;
+  gs::SearchFrame frame{};
+  gs::Grid grid;
+  cudaStream_t stream = nullptr;
+  ~gs_kriging() {
+    cudaFree(d_drift);
+    cudaFree(d_err);
+    cudaFree(d_basis_df);
+    cudaFree(d_err_df);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};

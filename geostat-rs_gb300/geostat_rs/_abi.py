@@ -69,6 +69,8 @@ SIGNATURES = {
                                        _vp]),
     "gs_kriging_predict_many_device": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                               _int, _vp]),
+    "gs_kriging_predict_fp64_noalloc": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                               _vp, _vp]),
     "gs_kriging_predict_grid": (_int, [_vp, _pd, _pd, _pi64, _pd, _pd, _pu8, _int, _vp]),
     "gs_kriging_neighbors": (_int, [_vp, _i64, _pd, _pd, _pd, _i64, _pi32, _pi32, _vp]),
     "gs_maxmin_order": (_int, [_int, _i64, _pd, _pd, _pd, _pi64]),

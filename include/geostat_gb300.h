@@ -159,6 +159,23 @@ int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double
                                    const double* ty, const double* tz, const double* tdrift,
                                    double* value, double* variance, double* lagrange,
                                    uint8_t* status, int precision, void* stream);
+/* Allocation-free FP64 prediction (no counterpart in the reference).  The
+ * same results as gs_kriging_predict_many_device with GS_PREC_FP64, for
+ * callers that may not allocate device memory while they predict: the
+ * neighbour lists and FP64 scratch live in one static device array of
+ * GS_NOALLOC_SCRATCH_BYTES per device.  At most GS_NOALLOC_MAX_TARGETS
+ * targets per call (more: GS_ERR_INVALID_PARAMETER).  All pointers are device
+ * memory; the call returns once its kernels are enqueued on `stream` (NULL:
+ * the predictor's stream).  The first call on a device sets up the array's
+ * address; make it before any section that cannot afford set-up work.  Calls
+ * whose work overlaps in time on one device (other streams, unordered host
+ * threads) share the array and race; calls ordered on one stream are safe. */
+#define GS_NOALLOC_SCRATCH_BYTES (64ll << 20)
+#define GS_NOALLOC_MAX_TARGETS 16384
+int gs_kriging_predict_fp64_noalloc(const gs_kriging* k, int64_t nt, const double* tx,
+                                    const double* ty, const double* tz, const double* tdrift,
+                                    double* value, double* variance, double* lagrange,
+                                    uint8_t* status, void* stream);
 /* Kriging::predict_grid (kriging.rs:783-786) for Grid2D / Grid3D cell
  * centres (grid.rs:80-96, 188-203), generated on the device. */
 int gs_kriging_predict_grid(const gs_kriging* k, const double* bbox_min, const double* bbox_max,
