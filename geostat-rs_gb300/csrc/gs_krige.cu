@@ -1,16 +1,18 @@
 // gs_krige.cu -- per-target kriging solves.
 //
-// K3 (krige_mixed_kernel): one warp per target system.  The system
-// (kriging.rs:527-567 build_lhs + the right-hand side of predict_inner,
-// kriging.rs:569-612) is assembled in shared memory as packed lower-triangular
-// double-float entries; the FP32 hi parts are factored A = L D L^T without
-// pivoting (the covariance block is positive definite, the drift block's
-// Schur complement negative definite); the solution is refined with
-// residuals b - A x formed from the double-float entries in compensated FP32
-// (Ogita-Rump-Oishi Dot2) and accumulated in FP64; the outputs
-// (kriging.rs:614-643) are FP64 sums.  A system whose refinement does not
-// contract to ~1e-13 relative, or whose pivot is too small for FP32, is
-// flagged for the FP64 solver.
+// K3 (krige_rows_kernel): one system per block of 32 or 64 threads, thread
+// i owning neighbour i.  The system (kriging.rs:527-567 build_lhs + the
+// right-hand side of predict_inner, kriging.rs:569-612) is assembled in shared
+// memory as packed lower-triangular double-float entries.  The FP32 hi parts
+// of the covariance block are inverted by a sweep with each thread's row in
+// registers; drift terms enter through the Schur complement F^T C^{-1} F
+// (the covariance block is positive definite, so no pivoting is needed).  The
+// solution is refined with residuals b - A x formed from the double-float
+// entries in compensated FP32 (Ogita-Rump-Oishi Dot2) and accumulated in
+// double-float; the outputs (kriging.rs:614-643) are double-float sums
+// converted to FP64 once.  A system whose refinement does not contract to
+// ~1e-13 relative, or whose pivot is too small for FP32, is flagged for the
+// FP64 solver.
 //
 // K3' (krige_fp64_kernel): one system per thread, the reference's own
 // algorithm in FP64 -- build_lhs, LU with partial pivoting and its singular
@@ -22,7 +24,7 @@
 
 #include "gs_internal.h"
 #include "gs_krige.cuh"
-#include "gs_cta.cuh"
+#include "gs_rows.cuh"
 #include "gs_solve.cuh"
 
 namespace gs {
@@ -80,35 +82,34 @@ __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
   }
 }
 
-// Shared-memory layout of one system.
-struct MixedLayout {
-  int np, nbr;
-  size_t off_a, off_v, off_b, off_xd, off_z, off_red, off_w, off_pan, off_lp, off_pinv, off_p, off_t, off_flag,
-      total;
+// Shared-memory layout of one system of krige_rows_kernel (R rows, PC drift
+// columns, nf coordinate frames).
+struct RowsLayout {
+  size_t off_a, off_f, off_v, off_b, off_z, off_x, off_row, off_vec, off_red, off_redd, off_s,
+      off_td, off_flag, total;
 };
 
-__host__ __device__ inline MixedLayout mixed_layout(int nmax, int nf, int dim) {
-  MixedLayout L;
-  L.np = nmax * (nmax + 1) / 2;
-  L.nbr = (nmax + 3) / 4;
+__host__ __device__ inline RowsLayout rows_layout(int R, int PC, int nf, int dim) {
+  RowsLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t r = o;
     o += (bytes + 15) & ~(size_t)15;
     return r;
   };
-  L.off_a = take((size_t)L.np * sizeof(df));
-  L.off_v = take((size_t)nf * dim * GS_MIXED_MAX_NEIGHBORS * sizeof(df));
-  L.off_b = take((size_t)nmax * sizeof(df));
-  L.off_xd = take((size_t)4 * L.nbr * sizeof(df));
-  L.off_z = take((size_t)GS_MIXED_MAX_NEIGHBORS * sizeof(df));
-  L.off_red = take(32 * sizeof(float));
-  L.off_w = take((size_t)4 * L.nbr * sizeof(float));
-  L.off_pan = take((size_t)2 * L.nbr * GS_PB * sizeof(float));
-  L.off_lp = take((size_t)2 * L.nbr * GS_PB * sizeof(float));
-  L.off_pinv = take(32 * sizeof(float));
-  L.off_p = take((size_t)L.nbr * L.nbr * 4 * sizeof(float));
-  L.off_t = take(8 * sizeof(df));
+  const int W = R + PC;
+  L.off_a = take((size_t)(R * (R + 1) / 2) * sizeof(df));
+  L.off_f = take((size_t)PC * R * sizeof(df));
+  L.off_v = take((size_t)nf * dim * R * sizeof(df));
+  L.off_b = take((size_t)W * sizeof(df));
+  L.off_z = take((size_t)R * sizeof(df));
+  L.off_x = take((size_t)R * sizeof(df));
+  L.off_row = take((size_t)2 * (W + 4) * sizeof(float));
+  L.off_vec = take((size_t)W * sizeof(float));
+  L.off_red = take((size_t)2 * (R / 32) * PC * sizeof(float));
+  L.off_redd = take((size_t)2 * (R / 32) * 2 * sizeof(df));
+  L.off_s = take((size_t)PC * PC * sizeof(float));
+  L.off_td = take(8 * sizeof(df));
   L.off_flag = take(16);
   L.total = o;
   return L;
@@ -122,34 +123,40 @@ __device__ __forceinline__ bool same_double(double a, double b) {
   return x == y || ((x | y) << 1) == 0ull;
 }
 
-template <int D, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevModel m, ExpTable tab_g,
-                                                               DfConsts kc, uint8_t* flag) {
+// K3: one system per block of R threads (n <= R neighbours, p <= PC drift
+// terms); thread i owns neighbour i.  The system [C F; F^T 0] [w; mu] =
+// [c; f] is solved through the covariance block: the sweep gives -C^{-1} and
+// G = C^{-1} F in registers, S = F^T G (p x p) is inverted in FP32, and a
+// correction for a residual (r1, r2) is
+//     y = C^{-1} r1,  dmu = S^{-1} (F^T y - r2),  dw = y - G dmu.
+// Residuals come from the double-float system (compensated FP32 products),
+// the solution is accumulated in double-float, and the outputs are
+// double-float sums converted to FP64 once.
+template <int D, int R, int PC>
+__global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
+    krige_rows_kernel(KrigeArgs a, DevModel m, ExpTable tab_g, DfConsts kc, uint8_t* flag) {
+  constexpr int W = R + PC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-    tab.v[i] = tab_g.v[i];
-  }
-  const int tid = threadIdx.x;
-  const int nthr = blockDim.x;
+  for (int q = threadIdx.x; q < 256; q += R) tab.v[q] = tab_g.v[q];
+  const int i = threadIdx.x;
   const Frames fr = frames_of(m);
-  const int NB = GS_MIXED_MAX_NEIGHBORS;
-  const MixedLayout lay = mixed_layout(a.nmax, fr.nf, D);
-  df* A = reinterpret_cast<df*>(smem_raw + lay.off_a);
-  df* V = reinterpret_cast<df*>(smem_raw + lay.off_v);
-  df* B = reinterpret_cast<df*>(smem_raw + lay.off_b);
-  df* ZV = reinterpret_cast<df*>(smem_raw + lay.off_z);
-  df* TD = reinterpret_cast<df*>(smem_raw + lay.off_t);  // target coordinates, sk mean
-  CtaScratch S;
-  S.XD = reinterpret_cast<df*>(smem_raw + lay.off_xd);
-  S.red = reinterpret_cast<float*>(smem_raw + lay.off_red);
-  S.W = reinterpret_cast<float*>(smem_raw + lay.off_w);
-  S.pan = reinterpret_cast<float*>(smem_raw + lay.off_pan);
-  S.lp = reinterpret_cast<float*>(smem_raw + lay.off_lp);
-  S.pinv = reinterpret_cast<float*>(smem_raw + lay.off_pinv);
-  S.P = reinterpret_cast<float*>(smem_raw + lay.off_p);
-  S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
+  const RowsLayout L = rows_layout(R, PC, fr.nf, D);
+  df* A = reinterpret_cast<df*>(smem_raw + L.off_a);     // packed covariance block
+  df* F = reinterpret_cast<df*>(smem_raw + L.off_f);     // F[q * R + i]: drift q at neighbour i
+  df* V = reinterpret_cast<df*>(smem_raw + L.off_v);     // frame coordinates
+  df* B = reinterpret_cast<df*>(smem_raw + L.off_b);     // c (0..n-1), f (R..R+p-1)
+  df* Z = reinterpret_cast<df*>(smem_raw + L.off_z);     // neighbour values
+  df* X = reinterpret_cast<df*>(smem_raw + L.off_x);     // current w, broadcast
+  float* rowbuf = reinterpret_cast<float*>(smem_raw + L.off_row);
+  float* vec = reinterpret_cast<float*>(smem_raw + L.off_vec);
+  float* red = reinterpret_cast<float*>(smem_raw + L.off_red);
+  df* redd = reinterpret_cast<df*>(smem_raw + L.off_redd);
+  float* Sinv = reinterpret_cast<float*>(smem_raw + L.off_s);
+  df* TD = reinterpret_cast<df*>(smem_raw + L.off_td);  // target coordinates, sk mean
+  int* sflag = reinterpret_cast<int*>(smem_raw + L.off_flag);
   const double* coord[3] = {a.x, a.y, a.z};
+  int slot = 0;
   __syncthreads();
 
   for (int64_t it = blockIdx.x; it < a.ntl; it += gridDim.x) {
@@ -161,7 +168,7 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
     else if (n < a.min_nb) st = GS_ST_NO_NEIGHBORS;
     else if (n < p) st = GS_ST_INSUFFICIENT_DATA;
     if (st != GS_ST_OK) {
-      if (tid == 0) {
+      if (i == 0) {
         a.out_v[t] = __longlong_as_double(0x7ff8000000000000ll);
         a.out_var[t] = __longlong_as_double(0x7ff8000000000000ll);
         if (a.out_lag) a.out_lag[t] = __longlong_as_double(0x7ff8000000000000ll);
@@ -170,23 +177,17 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
       }
       continue;
     }
-    if (n > NB) {
-      if (tid == 0) flag[t] = 1;
+    if (n > R || p > PC) {
+      if (i == 0) flag[t] = 1;
       continue;
     }
-    const int N = n + p;
     const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
-    // target coordinates (and the simple-kriging mean) as df, once per system
-    if (tid < D) TD[tid] = df_from_double(tp[tid]);
-    if (tid == 3) TD[3] = df_from_double(a.sk_mean);
-    // drift basis of the target: one basis function per thread
-    if (tid >= 32 && tid - 32 < p) {
-      const int k = tid - 32;
-      B[n + k] = df_from_double(basis_at<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, k));
-    }
-    __syncthreads();
-    // --- per-neighbour data: frames, values, rhs, diagonal, drift rows ---
-    for (int i = tid; i < n; i += nthr) {
+    if (i < D) TD[i] = df_from_double(tp[i]);
+    if (i == 3) TD[3] = df_from_double(a.sk_mean);
+    if (i < p) B[R + i] = df_from_double(basis_at<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, i));
+    rows_bar<R>();
+    // --- neighbour i: frames, value, covariance with the target, drift row
+    if (i < n) {
       const int idx = a.nb[t * (int64_t)a.kout + i];
       df ud[3];
       bool zero = true;
@@ -195,71 +196,231 @@ __global__ void __launch_bounds__(BLOCK, 4) krige_mixed_kernel(KrigeArgs a, DevM
         ud[d] = df_sub(a.cdf[(int64_t)d * a.n + idx], TD[d]);
         zero = zero && same_double(coord[d][idx], tp[d]);
       }
-      frame_coords<D>(m, fr, ud, V, NB, i);
-      B[i] = zero ? m.c0_df : cov_origin<D>(m, fr, V, NB, i, tab, kc);
-      ZV[i] = a.vdf[idx];
+      frame_coords<D>(m, fr, ud, V, R, i);
+      B[i] = zero ? m.c0_df : cov_origin<D>(m, fr, V, R, i, tab, kc);
+      Z[i] = a.vdf[idx];
       A[pk(i, i)] = a.err_df ? df_add(m.c0_df, a.err_df[idx]) : m.c0_df;
-      for (int k = 0; k < p; ++k) A[pk(n + k, i)] = a.basis_df[(int64_t)k * a.n + idx];
+#pragma unroll
+      for (int q = 0; q < PC; ++q)
+        if (q < p) F[q * R + i] = a.basis_df[(int64_t)q * a.n + idx];
     }
-    for (int q = tid; q < p * (p + 1) / 2; q += nthr) {
-      int r = 0;
-      while ((r + 1) * (r + 2) / 2 <= q) ++r;
-      const int c = q - r * (r + 1) / 2;
-      A[pk(n + r, n + c)] = df_make(0.0f, 0.0f);
-    }
-    __syncthreads();
-    // --- covariance block, strictly lower part ---------------------------
+    rows_bar<R>();
+    // --- covariance block, strictly lower part
     {
       const int npairs = (n * (n - 1)) >> 1;
-      int i = 1, j = tid;
-      while (j >= i && i < n) {
-        j -= i;
-        ++i;
+      int ii = 1, jj = i;
+      while (jj >= ii && ii < n) {
+        jj -= ii;
+        ++ii;
       }
-      for (int q = tid; q < npairs; q += nthr) {
-        A[pk(i, j)] = cov_pair<D>(m, fr, V, NB, i, j, tab, kc);
-        j += nthr;
-        while (j >= i && i < n) {
-          j -= i;
-          ++i;
+      for (int q = i; q < npairs; q += R) {
+        A[pk(ii, jj)] = cov_pair<D>(m, fr, V, R, ii, jj, tab, kc);
+        jj += R;
+        while (jj >= ii && ii < n) {
+          jj -= ii;
+          ++ii;
         }
       }
     }
-    __syncthreads();
-    // --- FP32 inverse, double-float refinement ----------------------------
-    const bool ok = cta_solve(A, B, N, S);
+    rows_bar<R>();
+    // --- FP32 rows: covariance block (identity padding) and drift block
+    float tr[W];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      float v = i == j ? 1.0f : 0.0f;
+      if (i < n && j < n) v = i >= j ? A[pk(i, j)].hi : A[pk(j, i)].hi;
+      tr[j] = v;
+    }
+#pragma unroll
+    for (int q = 0; q < PC; ++q) tr[R + q] = (i < n && q < p) ? F[q * R + i].hi : 0.0f;
+    float amax = 0.0f;
+#pragma unroll
+    for (int j = 0; j < R; ++j) amax = fmaxf(amax, fabsf(tr[j]));
+    amax = rows_max<R>(amax, red, slot);
+    bool ok = rows_sweep<R, W>(tr, n, 1e-6f * amax, rowbuf);
+    // --- Schur complement S = F^T G and its FP32 inverse (thread 0)
+    if (ok && p > 0) {
+      for (int q = 0; q < p; ++q) {
+        float v[PC];
+        const float fq = i < n ? F[q * R + i].hi : 0.0f;
+#pragma unroll
+        for (int r = 0; r < PC; ++r) v[r] = fq * tr[R + r];
+        rows_sum<R, PC>(v, red, slot);
+        if (i == 0) {
+#pragma unroll
+          for (int r = 0; r < PC; ++r) Sinv[q * PC + r] = v[r];
+        }
+      }
+      if (i == 0) {
+        // Gauss-Jordan without pivoting (S is positive definite for full-rank drift)
+        float smax = 0.0f;
+        for (int q = 0; q < p; ++q) smax = fmaxf(smax, fabsf(Sinv[q * PC + q]));
+        int good = 1;
+        for (int k = 0; k < p && good; ++k) {
+          const float d = Sinv[k * PC + k];
+          if (!(fabsf(d) > 1e-6f * smax)) {
+            good = 0;
+            break;
+          }
+          const float inv = 1.0f / d;
+          for (int r = 0; r < p; ++r) {
+            if (r == k) continue;
+            const float lr = Sinv[r * PC + k] * inv;
+            for (int c = 0; c < p; ++c)
+              if (c != k) Sinv[r * PC + c] -= lr * Sinv[k * PC + c];
+            Sinv[r * PC + k] = -lr;
+          }
+          for (int c = 0; c < p; ++c)
+            if (c != k) Sinv[k * PC + c] *= inv;
+          Sinv[k * PC + k] = inv;
+        }
+        sflag[0] = good;
+      }
+      rows_bar<R>();
+      ok = sflag[0] != 0;
+    }
     if (!ok) {
-      if (tid == 0) flag[t] = 1;
-      __syncthreads();
+      if (i == 0) flag[t] = 1;
+      rows_bar<R>();
       continue;
     }
-    // --- outputs: double-float dot products, FP64 at the end -------------
-    if (tid < 32) {
-      df sv = df_make(0.0f, 0.0f), sr = df_make(0.0f, 0.0f);
-      if (a.method == GS_SIMPLE) {
-        const df mean = TD[3];
-        for (int i = tid; i < n; i += 32) {
-          sv = df_fma_acc(sv, S.XD[i], df_sub(ZV[i], mean));
-          sr = df_fma_acc(sr, S.XD[i], B[i]);
+    // --- correction operator: (r1 in vec[0..R), r2 in vec[R..R+p)) -> (d1, d2)
+    auto apply = [&](float& d1, float (&d2)[PC]) {
+      const float y = rows_cinv_apply<R, W>(tr, vec, n);
+      d1 = y;
+#pragma unroll
+      for (int q = 0; q < PC; ++q) d2[q] = 0.0f;
+      if (p > 0) {
+        float u[PC];
+#pragma unroll
+        for (int q = 0; q < PC; ++q) u[q] = (i < n && q < p) ? F[q * R + i].hi * y : 0.0f;
+        rows_sum<R, PC>(u, red, slot);
+#pragma unroll
+        for (int q = 0; q < PC; ++q) u[q] = q < p ? u[q] - vec[R + q] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < PC; ++q) {
+          float s = 0.0f;
+#pragma unroll
+          for (int r = 0; r < PC; ++r) s = fmaf(q < p && r < p ? Sinv[q * PC + r] : 0.0f, u[r], s);
+          d2[q] = s;
         }
-      } else {
-        for (int i = tid; i < n; i += 32) sv = df_fma_acc(sv, S.XD[i], ZV[i]);
-        for (int i = tid; i < N; i += 32) sr = df_fma_acc(sr, S.XD[i], B[i]);
+        float g = 0.0f;
+#pragma unroll
+        for (int q = 0; q < PC; ++q) g = fmaf(tr[R + q], d2[q], g);
+        d1 = i < n ? y - g : 0.0f;
       }
-      sv = warp_sum_df(sv);
-      sr = warp_sum_df(sr);
-      if (tid == 0) {
-        const double val = a.method == GS_SIMPLE ? a.sk_mean + df_to_double(sv) : df_to_double(sv);
-        a.out_v[t] = val;
-        a.out_var[t] = fmax(df_to_double(df_sub(m.c0_df, sr)), 0.0);
-        if (a.out_lag)
-          a.out_lag[t] = a.method == GS_SIMPLE ? __longlong_as_double(0x7ff8000000000000ll)
-                                               : df_to_double(S.XD[n]);
-        a.out_st[t] = GS_ST_OK;
-        flag[t] = 0;
+    };
+    // x0 from the hi parts of the right-hand side
+    vec[i] = i < n ? B[i].hi : 0.0f;
+    if (i < p) vec[R + i] = B[R + i].hi;
+    rows_bar<R>();
+    float d1, d2[PC];
+    apply(d1, d2);
+    df x1 = df_make(d1, 0.0f);
+    df x2[PC];
+#pragma unroll
+    for (int q = 0; q < PC; ++q) x2[q] = df_make(d2[q], 0.0f);
+    float mx = fabsf(d1);
+#pragma unroll
+    for (int q = 0; q < PC; ++q) mx = fmaxf(mx, fabsf(d2[q]));
+    const float nx = rows_max<R>(mx, red, slot);
+    float nd_prev = nx;
+    bool conv = false;
+    for (int sweep = 1; sweep <= 4 && !conv; ++sweep) {
+      X[i] = x1;
+      rows_bar<R>();
+      // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q (compensated)
+      float s = 0.0f, c = 0.0f;
+      auto acc = [&](df aij, df xj) {
+        const float ph = __fmul_rn(-aij.hi, xj.hi);
+        float pe = __fmaf_rn(-aij.hi, xj.hi, -ph);
+        pe = __fmaf_rn(-aij.hi, xj.lo, pe);
+        pe = __fmaf_rn(-aij.lo, xj.hi, pe);
+        const float tsum = __fadd_rn(s, ph);
+        const float bb = __fsub_rn(tsum, s);
+        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
+        s = tsum;
+        c += e + pe;
+      };
+      if (i < n) {
+        s = B[i].hi;
+        c = B[i].lo;
+        int idx = pk(i, 0);
+        int idx2 = pk(i + 1, i);
+        for (int j = 0; j < n; ++j) {
+          const bool lower = j <= i;
+          acc(A[lower ? idx : idx2], X[j]);
+          if (lower) ++idx;
+          else idx2 += j + 1;
+        }
+#pragma unroll
+        for (int q = 0; q < PC; ++q)
+          if (q < p) acc(F[q * R + i], x2[q]);
       }
+      // r2_q = f_q - sum_i F_iq w_i, as double-float block sums
+      float r2[PC];
+#pragma unroll
+      for (int q = 0; q < PC; ++q) r2[q] = 0.0f;
+      for (int q = 0; q < p; ++q) {
+        df v[1] = {i < n ? df_mul(F[q * R + i], x1) : df_make(0.0f, 0.0f)};
+        rows_sum_df<R, 1>(v, redd, slot);
+        const df rq = df_sub(B[R + q], v[0]);
+#pragma unroll
+        for (int r = 0; r < PC; ++r)
+          if (r == q) r2[r] = rq.hi + rq.lo;
+      }
+      vec[i] = i < n ? s + c : 0.0f;
+      if (i == 0) {
+#pragma unroll
+        for (int q = 0; q < PC; ++q)
+          if (q < p) vec[R + q] = r2[q];
+      }
+      rows_bar<R>();
+      apply(d1, d2);
+      if (i < n) x1 = df_add_f(x1, d1);
+      mx = fabsf(d1);
+#pragma unroll
+      for (int q = 0; q < PC; ++q) {
+        x2[q] = df_add_f(x2[q], d2[q]);
+        mx = fmaxf(mx, fabsf(d2[q]));
+      }
+      const float nd = rows_max<R>(mx, red, slot);
+      if (nd <= 1e-15f * nx) conv = true;
+      else if (sweep >= 2) {
+        const float rho = nd / nd_prev;
+        if (rho < 0.5f && rho * nd <= 1e-13f * nx) conv = true;
+      }
+      nd_prev = nd;
     }
-    __syncthreads();
+    if (!conv) {
+      if (i == 0) flag[t] = 1;
+      rows_bar<R>();
+      continue;
+    }
+    // --- outputs: double-float sums, FP64 at the end
+    df o[2];
+    if (a.method == GS_SIMPLE) {
+      o[0] = i < n ? df_mul(x1, df_sub(Z[i], TD[3])) : df_make(0.0f, 0.0f);
+    } else {
+      o[0] = i < n ? df_mul(x1, Z[i]) : df_make(0.0f, 0.0f);
+    }
+    o[1] = i < n ? df_mul(x1, B[i]) : df_make(0.0f, 0.0f);
+    rows_sum_df<R, 2>(o, redd, slot);
+    if (i == 0) {
+      df sr = o[1];
+#pragma unroll
+      for (int q = 0; q < PC; ++q)
+        if (q < p) sr = df_add(sr, df_mul(x2[q], B[R + q]));
+      const double val = a.method == GS_SIMPLE ? a.sk_mean + df_to_double(o[0]) : df_to_double(o[0]);
+      a.out_v[t] = val;
+      a.out_var[t] = fmax(df_to_double(df_sub(m.c0_df, sr)), 0.0);
+      if (a.out_lag)
+        a.out_lag[t] = a.method == GS_SIMPLE ? __longlong_as_double(0x7ff8000000000000ll)
+                                             : df_to_double(x2[0]);
+      a.out_st[t] = GS_ST_OK;
+      flag[t] = 0;
+    }
+    rows_bar<R>();
   }
 }
 
@@ -440,31 +601,45 @@ static void ensure_tables() {
   }
 }
 
+template <int D, int R, int PC>
+static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int nf,
+                       cudaStream_t stream) {
+  const RowsLayout lay = rows_layout(R, PC, nf, D);
+  const size_t smem = lay.total;
+  auto kern = krige_rows_kernel<D, R, PC>;
+  GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per_sm = 0;
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R, smem));
+  per_sm = std::max(per_sm, 1);
+  const int blocks = (int)std::min<int64_t>(a.ntl, (int64_t)sms * per_sm);
+  kern<<<blocks, R, smem, stream>>>(a, m, g_tab, g_kc, flag);
+  GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  return GS_OK;
+}
+
 int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int /*unused*/,
                        cudaStream_t stream) {
   if (a.ntl == 0) return GS_OK;
   ensure_tables();
   int nf = 1;
   for (int s = 0; s < m.ns; ++s) nf += m.s[s].aniso ? 1 : 0;
-  const MixedLayout lay = mixed_layout(a.nmax, nf, a.dim);
-  const size_t smem = lay.total;
-  if (smem > 200 * 1024) return fail(GS_ERR_INVALID_PARAMETER, "system too large for the mixed kernel");
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int nbr = lay.nbr;
-  const int tiles = nbr * (nbr + 1) / 2;
-  const int block = std::min(256, std::max(64, ((tiles + 31) / 32) * 32));
-  auto kern = a.dim == 2 ? krige_mixed_kernel<2, 256> : krige_mixed_kernel<3, 256>;
-  GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
-  per_sm = std::max(per_sm, 1);
-  const int blocks = (int)std::min<int64_t>(a.ntl, (int64_t)sms * per_sm);
-  kern<<<blocks, block, smem, stream>>>(a, m, g_tab, g_kc, flag);
-  GS_CUDA(cudaGetLastError());
-  count_launch(1);
-  return GS_OK;
+  const int nb = a.nmax - a.p;  // neighbour slots
+  const bool small = nb <= 32;
+  const bool wide = a.p > 4;
+  if (a.dim == 2) {
+    if (small) return wide ? launch_rows<2, 32, 12>(a, m, flag, nf, stream)
+                           : launch_rows<2, 32, 4>(a, m, flag, nf, stream);
+    return wide ? launch_rows<2, 64, 12>(a, m, flag, nf, stream)
+                : launch_rows<2, 64, 4>(a, m, flag, nf, stream);
+  }
+  if (small) return wide ? launch_rows<3, 32, 12>(a, m, flag, nf, stream)
+                         : launch_rows<3, 32, 4>(a, m, flag, nf, stream);
+  return wide ? launch_rows<3, 64, 12>(a, m, flag, nf, stream)
+              : launch_rows<3, 64, 4>(a, m, flag, nf, stream);
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {
