@@ -111,15 +111,18 @@ __host__ __device__ inline double df_to_double(df a) { return (double)a.hi + (do
 
 // sqrt of a non-negative df: an FP32 reciprocal square root refined by one
 // Newton step, then one correction with the exact residual s - y*y
-// (Karp & Markstein, ACM TOMS 23(4), 1997): relative error ~2^-47.
+// (Karp & Markstein, ACM TOMS 23(4), 1997): relative error ~2^-47.  Branch
+// free (0 for s <= 0), so independent evaluations interleave.
 __device__ __forceinline__ df df_sqrt(df s) {
-  if (!(s.hi > 0.0f)) return df_make(0.0f, 0.0f);
-  float r = rsqrtf(s.hi);
-  r = r * fmaf(-0.5f * s.hi * r, r, 1.5f);
-  const float y = s.hi * r;
+  const bool pos = s.hi > 0.0f;
+  const float sh = pos ? s.hi : 1.0f;
+  float r = rsqrtf(sh);
+  r = r * fmaf(-0.5f * sh * r, r, 1.5f);
+  const float y = sh * r;
   const df yy = two_prod(y, y);
-  const float e = __fadd_rn(__fsub_rn(__fsub_rn(s.hi, yy.hi), yy.lo), s.lo);
-  return fast_two_sum(y, e * (0.5f * r));
+  const float e = __fadd_rn(__fsub_rn(__fsub_rn(sh, yy.hi), yy.lo), pos ? s.lo : 0.0f);
+  const df res = fast_two_sum(y, e * (0.5f * r));
+  return pos ? res : df_make(0.0f, 0.0f);
 }
 
 // exp(-d) for d >= 0, table-driven after P. T. P. Tang, "Table-driven
@@ -139,8 +142,11 @@ struct DfConsts {
 };
 typedef DfConsts ExpConsts;
 
-__device__ __forceinline__ df df_expneg(df d, const ExpTable& tab, const ExpConsts& k) {
-  if (!(d.hi < 87.0f)) return df_make(0.0f, 0.0f);
+__device__ __forceinline__ df df_expneg(df din, const ExpTable& tab, const ExpConsts& k) {
+  // branch free: out-of-range (or NaN) arguments are evaluated at 0 and
+  // replaced by 0 at the end
+  const bool in = din.hi < 87.0f;
+  const df d = in ? din : df_make(0.0f, 0.0f);
   const float nf = rintf(__fmul_rn(d.hi, k.inv));
   const int n = (int)nf;
   const float t1 = __fsub_rn(d.hi, __fmul_rn(nf, k.l1));  // exact (Sterbenz)
@@ -155,7 +161,7 @@ __device__ __forceinline__ df df_expneg(df d, const ExpTable& tab, const ExpCons
   const int kk = n >> 8;
   const df res = df_mul(e, tab.v[j]);
   const float sc = __int_as_float((127 - kk) << 23);  // 2^-kk, kk <= 126 for d < 88
-  return df_make(res.hi * sc, res.lo * sc);
+  return in ? df_make(res.hi * sc, res.lo * sc) : df_make(0.0f, 0.0f);
 }
 
 void df_consts_host(ExpTable* tab, DfConsts* k);
@@ -237,38 +243,75 @@ __device__ __forceinline__ double cov_fp64(const DevModel& m, const double* h) {
   return acc;
 }
 
+// Unit-sill correlations in df for d >= 0, branch free.
+__device__ __forceinline__ df rho_sph_df(df d) {
+  // 1 - d (1.5 - 0.5 d^2) for d < 1, else 0
+  const bool inside = !(d.hi > 1.0f || (d.hi == 1.0f && d.lo >= 0.0f));
+  const df d2 = df_sqr(d);
+  const df t = df_add_f(df_make(-0.5f * d2.hi, -0.5f * d2.lo), 1.5f);
+  const df u = df_mul(d, t);
+  const df r = df_add_f(df_neg(u), 1.0f);
+  return inside ? r : df_make(0.0f, 0.0f);
+}
+__device__ __forceinline__ df rho_mat15_df(df d, const ExpTable& tab, const ExpConsts& k) {
+  const df s = df_mul(d, df_make(k.s3h, k.s3l));
+  const df e = df_expneg(s, tab, k);
+  return df_mul(df_add_f(s, 1.0f), e);
+}
+__device__ __forceinline__ df rho_mat25_df(df d, const ExpTable& tab, const ExpConsts& k) {
+  const df s = df_mul(d, df_make(k.s5h, k.s5l));
+  const df e = df_expneg(s, tab, k);
+  const df s2 = df_sqr(s);
+  // 1 + s + s^2/3: s^2/3 as df via FP32 reciprocal correction
+  const float q = s2.hi * (1.0f / 3.0f);
+  const df q3 = two_prod(q, 3.0f);
+  const float rq = (s2.hi - q3.hi - q3.lo + s2.lo) * (1.0f / 3.0f);
+  const df third = fast_two_sum(q, rq);
+  const df p = df_add(df_add_f(s, 1.0f), third);
+  return df_mul(p, e);
+}
+
 // rho(d) in df for d >= 0.
 __device__ __forceinline__ df rho_df(int kind, df d, const ExpTable& tab, const ExpConsts& k) {
   switch (kind) {
-    case GS_KIND_SPHERICAL: {
-      if (d.hi > 1.0f || (d.hi == 1.0f && d.lo >= 0.0f)) return df_make(0.0f, 0.0f);
-      // 1 - d (1.5 - 0.5 d^2)
-      df d2 = df_sqr(d);
-      const df t = df_add_f(df_make(-0.5f * d2.hi, -0.5f * d2.lo), 1.5f);
-      df u = df_mul(d, t);
-      return df_add_f(df_neg(u), 1.0f);
-    }
+    case GS_KIND_SPHERICAL:
+      return rho_sph_df(d);
     case GS_KIND_EXPONENTIAL:
       return df_expneg(d, tab, k);
     case GS_KIND_GAUSSIAN:
       return df_expneg(df_sqr(d), tab, k);
-    case GS_KIND_MATERN15: {
-      df s = df_mul(d, df_make(k.s3h, k.s3l));
-      df e = df_expneg(s, tab, k);
-      return df_mul(df_add_f(s, 1.0f), e);
-    }
-    default: {  // GS_KIND_MATERN25
-      df s = df_mul(d, df_make(k.s5h, k.s5l));
-      df e = df_expneg(s, tab, k);
-      df s2 = df_sqr(s);
-      // 1 + s + s^2/3: s^2/3 as df via FP32 reciprocal correction
-      float q = s2.hi * (1.0f / 3.0f);
-      df q3 = two_prod(q, 3.0f);
-      float rq = (s2.hi - q3.hi - q3.lo + s2.lo) * (1.0f / 3.0f);
-      df third = fast_two_sum(q, rq);
-      df p = df_add(df_add_f(s, 1.0f), third);
-      return df_mul(p, e);
-    }
+    case GS_KIND_MATERN15:
+      return rho_mat15_df(d, tab, k);
+    default:  // GS_KIND_MATERN25
+      return rho_mat25_df(d, tab, k);
+  }
+}
+
+// rho at two arguments under one (uniform) branch on the kind: the two
+// evaluations are independent and interleave.
+__device__ __forceinline__ void rho_df2(int kind, df d0, df d1, const ExpTable& tab,
+                                        const ExpConsts& k, df& r0, df& r1) {
+  switch (kind) {
+    case GS_KIND_SPHERICAL:
+      r0 = rho_sph_df(d0);
+      r1 = rho_sph_df(d1);
+      break;
+    case GS_KIND_EXPONENTIAL:
+      r0 = df_expneg(d0, tab, k);
+      r1 = df_expneg(d1, tab, k);
+      break;
+    case GS_KIND_GAUSSIAN:
+      r0 = df_expneg(df_sqr(d0), tab, k);
+      r1 = df_expneg(df_sqr(d1), tab, k);
+      break;
+    case GS_KIND_MATERN15:
+      r0 = rho_mat15_df(d0, tab, k);
+      r1 = rho_mat15_df(d1, tab, k);
+      break;
+    default:
+      r0 = rho_mat25_df(d0, tab, k);
+      r1 = rho_mat25_df(d1, tab, k);
+      break;
   }
 }
 

@@ -86,8 +86,12 @@ __device__ __forceinline__ void fill_basis(const KrigeArgs& a, const double* pt,
 // columns, nf coordinate frames).
 struct RowsLayout {
   size_t off_a, off_f, off_v, off_b, off_z, off_x, off_row, off_vec, off_red, off_redd, off_s,
-      off_td, off_flag, total;
+      off_td, off_flag, off_slots, total;
 };
+
+// Targets per run: a block solves consecutive targets of its run one after
+// another and keeps the matrix entries of the neighbours they share.
+constexpr int kRowsRun = 64;
 
 __host__ __device__ inline RowsLayout rows_layout(int R, int PC, int nf, int dim) {
   RowsLayout L;
@@ -111,6 +115,7 @@ __host__ __device__ inline RowsLayout rows_layout(int R, int PC, int nf, int dim
   L.off_s = take((size_t)PC * PC * sizeof(float));
   L.off_td = take(8 * sizeof(df));
   L.off_flag = take(16);
+  L.off_slots = take((size_t)5 * R * sizeof(int) + 8 * sizeof(unsigned));
   L.total = o;
   return L;
 }
@@ -124,14 +129,22 @@ __device__ __forceinline__ bool same_double(double a, double b) {
 }
 
 // K3: one system per block of R threads (n <= R neighbours, p <= PC drift
-// terms); thread i owns neighbour i.  The system [C F; F^T 0] [w; mu] =
-// [c; f] is solved through the covariance block: the sweep gives -C^{-1} and
-// G = C^{-1} F in registers, S = F^T G (p x p) is inverted in FP32, and a
-// correction for a residual (r1, r2) is
+// terms).  The system [C F; F^T 0] [w; mu] = [c; f] is solved through the
+// covariance block: the sweep gives -C^{-1} and G = C^{-1} F in registers,
+// S = F^T G (p x p) is inverted in FP32, and a correction for a residual
+// (r1, r2) is
 //     y = C^{-1} r1,  dmu = S^{-1} (F^T y - r2),  dw = y - G dmu.
 // Residuals come from the double-float system (compensated FP32 products),
 // the solution is accumulated in double-float, and the outputs are
 // double-float sums converted to FP64 once.
+//
+// Slots: thread s owns slot s, which holds one neighbour (a data point id) or
+// nothing.  A block walks a run of consecutive targets; neighbours that the
+// next target shares with the previous one keep their slot, so the
+// covariances between kept neighbours (target independent) stay in the
+// packed matrix, and only pairs with a newly placed neighbour are evaluated.
+// Solving in slot order instead of neighbour order changes only the order of
+// roundings.
 template <int D, int R, int PC>
 __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     krige_rows_kernel(KrigeArgs a, DevModel m, ExpTable tab_g, DfConsts kc, uint8_t* flag) {
@@ -142,11 +155,11 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
   const int i = threadIdx.x;
   const Frames fr = frames_of(m);
   const RowsLayout L = rows_layout(R, PC, fr.nf, D);
-  df* A = reinterpret_cast<df*>(smem_raw + L.off_a);     // packed covariance block
-  df* F = reinterpret_cast<df*>(smem_raw + L.off_f);     // F[q * R + i]: drift q at neighbour i
-  df* V = reinterpret_cast<df*>(smem_raw + L.off_v);     // frame coordinates
-  df* B = reinterpret_cast<df*>(smem_raw + L.off_b);     // c (0..n-1), f (R..R+p-1)
-  df* Z = reinterpret_cast<df*>(smem_raw + L.off_z);     // neighbour values
+  df* A = reinterpret_cast<df*>(smem_raw + L.off_a);     // packed covariance block (slots)
+  df* F = reinterpret_cast<df*>(smem_raw + L.off_f);     // F[q * R + s]: drift q at slot s
+  df* V = reinterpret_cast<df*>(smem_raw + L.off_v);     // frame coordinates (slots)
+  df* B = reinterpret_cast<df*>(smem_raw + L.off_b);     // c (slots), f (R..R+p-1)
+  df* Z = reinterpret_cast<df*>(smem_raw + L.off_z);     // values (slots)
   df* X = reinterpret_cast<df*>(smem_raw + L.off_x);     // current w, broadcast
   float* rowbuf = reinterpret_cast<float*>(smem_raw + L.off_row);
   float* vec = reinterpret_cast<float*>(smem_raw + L.off_vec);
@@ -155,11 +168,20 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
   float* Sinv = reinterpret_cast<float*>(smem_raw + L.off_s);
   df* TD = reinterpret_cast<df*>(smem_raw + L.off_td);  // target coordinates, sk mean
   int* sflag = reinterpret_cast<int*>(smem_raw + L.off_flag);
+  int* new_idx = reinterpret_cast<int*>(smem_raw + L.off_slots);  // this target's neighbours
+  int* matched = new_idx + R;     // neighbour already in a slot
+  int* umap = matched + R;        // k-th unplaced neighbour
+  int* act_list = umap + R;       // occupied slots, ascending (the pivot order)
+  int* fresh_list = act_list + R; // newly placed slots, ascending
+  unsigned* bal = reinterpret_cast<unsigned*>(fresh_list + R);  // 2 x 4 ballot words
   const double* coord[3] = {a.x, a.y, a.z};
   int slot = 0;
+  int my_idx = -1;  // data point in this thread's slot
   __syncthreads();
 
-  for (int64_t it = blockIdx.x; it < a.ntl; it += gridDim.x) {
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowsRun; r0 < a.ntl; r0 += (int64_t)gridDim.x * kRowsRun) {
+  const int64_t r1 = r0 + kRowsRun < a.ntl ? r0 + kRowsRun : a.ntl;
+  for (int64_t it = r0; it < r1; ++it) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
     const int n = a.nbc[t];
     const int p = a.p;
@@ -185,10 +207,35 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     if (i < D) TD[i] = df_from_double(tp[i]);
     if (i == 3) TD[3] = df_from_double(a.sk_mean);
     if (i < p) B[R + i] = df_from_double(basis_at<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, i));
+    // --- slots: keep shared neighbours, place new ones in free slots
+    if (i < n) new_idx[i] = a.nb[t * (int64_t)a.kout + i];
+    matched[i] = 0;
     rows_bar<R>();
-    // --- neighbour i: frames, value, covariance with the target, drift row
-    if (i < n) {
-      const int idx = a.nb[t * (int64_t)a.kout + i];
+    int pos = -1;
+    if (my_idx >= 0) {
+      for (int q = 0; q < n; ++q) pos = new_idx[q] == my_idx ? q : pos;
+    }
+    const bool keep = pos >= 0;
+    if (keep) matched[pos] = 1;
+    rows_bar<R>();
+    unsigned long long m_un, m_free;
+    rows_ballot2<R>(i < n && !matched[i], !keep, m_un, m_free, bal);
+    const int n_un = __popcll(m_un);
+    if ((m_un >> i) & 1ull) umap[rank_below(m_un, i)] = i;
+    rows_bar<R>();
+    const int rf = rank_below(m_free, i);
+    const bool fresh = !keep && rf < n_un;
+    my_idx = keep ? my_idx : (fresh ? new_idx[umap[rf]] : -1);
+    const bool act = my_idx >= 0;
+    unsigned long long m_act, m_fresh;
+    rows_ballot2<R>(act, fresh, m_act, m_fresh, bal + 4);
+    const int nact = __popcll(m_act);  // == n
+    const int nfresh = __popcll(m_fresh);
+    if (act) act_list[rank_below(m_act, i)] = i;
+    if (fresh) fresh_list[rank_below(m_fresh, i)] = i;
+    // --- this slot's point: frames, value, covariance with the target, drift row
+    if (act) {
+      const int idx = my_idx;
       df ud[3];
       bool zero = true;
 #pragma unroll
@@ -205,46 +252,90 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         if (q < p) F[q * R + i] = a.basis_df[(int64_t)q * a.n + idx];
     }
     rows_bar<R>();
-    // --- covariance block, strictly lower part
-    {
-      const int npairs = (n * (n - 1)) >> 1;
-      int ii = 1, jj = i;
-      while (jj >= ii && ii < n) {
-        jj -= ii;
-        ++ii;
+    // --- covariances of pairs with a newly placed point, two at a time
+    auto put2 = [&](int s0, int u0, int s1, int u1, bool two) {
+      df c0, c1;
+      cov_pair2<D>(m, fr, V, R, s0, u0, s1, u1, tab, kc, c0, c1);
+      A[s0 >= u0 ? pk(s0, u0) : pk(u0, s0)] = c0;
+      if (two) A[s1 >= u1 ? pk(s1, u1) : pk(u1, s1)] = c1;
+    };
+    if (2 * nfresh >= nact) {
+      // most slots are new: the whole triangle over occupied slots
+      for_pairs2(nact, i, R, [&](int i0, int j0, int i1, int j1, bool two) {
+        put2(act_list[i0], act_list[j0], act_list[i1], act_list[j1], two);
+      });
+    } else {
+      // (new slot, occupied slot) pairs; a pair of two new slots once
+      const int P = nfresh * nact;
+      int fr0 = 0, c0 = i;
+      while (c0 >= nact) {
+        c0 -= nact;
+        ++fr0;
       }
-      for (int q = i; q < npairs; q += R) {
-        A[pk(ii, jj)] = cov_pair<D>(m, fr, V, R, ii, jj, tab, kc);
-        jj += R;
-        while (jj >= ii && ii < n) {
-          jj -= ii;
-          ++ii;
+      for (int q = i; q < P; q += 2 * R) {
+        int fr1 = fr0, c1 = c0 + R;
+        while (c1 >= nact) {
+          c1 -= nact;
+          ++fr1;
+        }
+        const bool has1 = q + R < P;
+        const int s0 = fresh_list[fr0], u0 = act_list[c0];
+        const int s1 = has1 ? fresh_list[fr1] : s0, u1 = has1 ? act_list[c1] : u0;
+        const bool v0 = u0 != s0 && (!((m_fresh >> u0) & 1ull) || u0 < s0);
+        const bool v1 = has1 && u1 != s1 && (!((m_fresh >> u1) & 1ull) || u1 < s1);
+        if (v0 || v1) {
+          df e0, e1;
+          cov_pair2<D>(m, fr, V, R, s0, u0, s1, u1, tab, kc, e0, e1);
+          if (v0) A[s0 >= u0 ? pk(s0, u0) : pk(u0, s0)] = e0;
+          if (v1) A[s1 >= u1 ? pk(s1, u1) : pk(u1, s1)] = e1;
+        }
+        fr0 = fr1;
+        c0 = c1 + R;
+        while (c0 >= nact) {
+          c0 -= nact;
+          ++fr0;
         }
       }
     }
     rows_bar<R>();
-    // --- FP32 rows: covariance block (identity padding) and drift block
-    float tr[W];
-#pragma unroll
-    for (int j = 0; j < R; ++j) {
+    // --- FP32 rows: covariance block (identity off the occupied slots), drift block
+    float2 tr[W / 2];
+    auto cov_hi = [&](int j) {
       float v = i == j ? 1.0f : 0.0f;
-      if (i < n && j < n) v = i >= j ? A[pk(i, j)].hi : A[pk(j, i)].hi;
-      tr[j] = v;
-    }
+      if (act && ((m_act >> j) & 1ull)) v = i >= j ? A[pk(i, j)].hi : A[pk(j, i)].hi;
+      return v;
+    };
 #pragma unroll
-    for (int q = 0; q < PC; ++q) tr[R + q] = (i < n && q < p) ? F[q * R + i].hi : 0.0f;
+    for (int j2 = 0; j2 < R / 2; ++j2) tr[j2] = make_float2(cov_hi(2 * j2), cov_hi(2 * j2 + 1));
     float amax = 0.0f;
 #pragma unroll
-    for (int j = 0; j < R; ++j) amax = fmaxf(amax, fabsf(tr[j]));
+    for (int j2 = 0; j2 < R / 2; ++j2)
+      amax = fmaxf(amax, act ? fmaxf(fabsf(tr[j2].x), fabsf(tr[j2].y)) : 0.0f);
     amax = rows_max<R>(amax, red, slot);
-    bool ok = rows_sweep<R, W>(tr, n, 1e-6f * amax, rowbuf);
+    // power-of-two scale sc with sc * max|C| in [0.5, 1): every pivot is then
+    // <= 1, so the pivot thread's multiplier 1 - 1/d never cancels.  The
+    // covariance rows and the drift columns are both scaled, so the drift
+    // block ends as C^{-1} F unscaled; C^{-1} itself comes out divided by sc.
+    int ex = 0;
+    frexpf(amax, &ex);
+    const float sc = ldexpf(1.0f, -ex);
+#pragma unroll
+    for (int j2 = 0; j2 < R / 2; ++j2) {
+      if (act && ((m_act >> (2 * j2)) & 1ull)) tr[j2].x *= sc;
+      if (act && ((m_act >> (2 * j2 + 1)) & 1ull)) tr[j2].y *= sc;
+    }
+    auto drift_hi = [&](int q) { return (act && q < p) ? F[q * R + i].hi * sc : 0.0f; };
+#pragma unroll
+    for (int q2 = 0; q2 < PC / 2; ++q2) tr[R / 2 + q2] = make_float2(drift_hi(2 * q2), drift_hi(2 * q2 + 1));
+    // (an empty simple-kriging system has nothing to invert: w = 0)
+    bool ok = nact == 0 || (amax > 0.0f && rows_sweep<R, W / 2>(tr, act_list, nact, 1e-6f * amax * sc, rowbuf));
     // --- Schur complement S = F^T G and its FP32 inverse (thread 0)
     if (ok && p > 0) {
       for (int q = 0; q < p; ++q) {
         float v[PC];
-        const float fq = i < n ? F[q * R + i].hi : 0.0f;
+        const float fq = act ? F[q * R + i].hi : 0.0f;
 #pragma unroll
-        for (int r = 0; r < PC; ++r) v[r] = fq * tr[R + r];
+        for (int r = 0; r < PC; ++r) v[r] = fq * row_elt(tr, R + r);
         rows_sum<R, PC>(v, red, slot);
         if (i == 0) {
 #pragma unroll
@@ -286,14 +377,14 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     }
     // --- correction operator: (r1 in vec[0..R), r2 in vec[R..R+p)) -> (d1, d2)
     auto apply = [&](float& d1, float (&d2)[PC]) {
-      const float y = rows_cinv_apply<R, W>(tr, vec, n);
+      const float y = sc * rows_cinv_apply<R, W / 2>(tr, vec, act);
       d1 = y;
 #pragma unroll
       for (int q = 0; q < PC; ++q) d2[q] = 0.0f;
       if (p > 0) {
         float u[PC];
 #pragma unroll
-        for (int q = 0; q < PC; ++q) u[q] = (i < n && q < p) ? F[q * R + i].hi * y : 0.0f;
+        for (int q = 0; q < PC; ++q) u[q] = (act && q < p) ? F[q * R + i].hi * y : 0.0f;
         rows_sum<R, PC>(u, red, slot);
 #pragma unroll
         for (int q = 0; q < PC; ++q) u[q] = q < p ? u[q] - vec[R + q] : 0.0f;
@@ -306,12 +397,12 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         }
         float g = 0.0f;
 #pragma unroll
-        for (int q = 0; q < PC; ++q) g = fmaf(tr[R + q], d2[q], g);
-        d1 = i < n ? y - g : 0.0f;
+        for (int q = 0; q < PC; ++q) g = fmaf(row_elt(tr, R + q), d2[q], g);
+        d1 = act ? y - g : 0.0f;
       }
     };
     // x0 from the hi parts of the right-hand side
-    vec[i] = i < n ? B[i].hi : 0.0f;
+    vec[i] = act ? B[i].hi : 0.0f;
     if (i < p) vec[R + i] = B[R + i].hi;
     rows_bar<R>();
     float d1, d2[PC];
@@ -329,47 +420,53 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     for (int sweep = 1; sweep <= 4 && !conv; ++sweep) {
       X[i] = x1;
       rows_bar<R>();
-      // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q (compensated)
-      float s = 0.0f, c = 0.0f;
-      auto acc = [&](df aij, df xj) {
+      // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q over occupied slots,
+      // two compensated accumulators for ILP
+      float s = 0.0f, c = 0.0f, s1 = 0.0f, c1 = 0.0f;
+      auto acc = [](float& sa, float& ca, df aij, df xj) {
         const float ph = __fmul_rn(-aij.hi, xj.hi);
         float pe = __fmaf_rn(-aij.hi, xj.hi, -ph);
         pe = __fmaf_rn(-aij.hi, xj.lo, pe);
         pe = __fmaf_rn(-aij.lo, xj.hi, pe);
-        const float tsum = __fadd_rn(s, ph);
-        const float bb = __fsub_rn(tsum, s);
-        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
-        s = tsum;
-        c += e + pe;
+        const float tsum = __fadd_rn(sa, ph);
+        const float bb = __fsub_rn(tsum, sa);
+        const float e = __fadd_rn(__fsub_rn(sa, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
+        sa = tsum;
+        ca += e + pe;
       };
-      if (i < n) {
+      if (act) {
         s = B[i].hi;
         c = B[i].lo;
-        int idx = pk(i, 0);
-        int idx2 = pk(i + 1, i);
-        for (int j = 0; j < n; ++j) {
-          const bool lower = j <= i;
-          acc(A[lower ? idx : idx2], X[j]);
-          if (lower) ++idx;
-          else idx2 += j + 1;
+        int jj = 0;
+        for (; jj + 1 < nact; jj += 2) {
+          const int j0 = act_list[jj], j1 = act_list[jj + 1];
+          acc(s, c, A[j0 <= i ? pk(i, j0) : pk(j0, i)], X[j0]);
+          acc(s1, c1, A[j1 <= i ? pk(i, j1) : pk(j1, i)], X[j1]);
+        }
+        if (jj < nact) {
+          const int j0 = act_list[jj];
+          acc(s, c, A[j0 <= i ? pk(i, j0) : pk(j0, i)], X[j0]);
         }
 #pragma unroll
         for (int q = 0; q < PC; ++q)
-          if (q < p) acc(F[q * R + i], x2[q]);
+          if (q < p) acc(s1, c1, F[q * R + i], x2[q]);
+        const df st2 = two_sum(s, s1);
+        s = st2.hi;
+        c = c + c1 + st2.lo;
       }
       // r2_q = f_q - sum_i F_iq w_i, as double-float block sums
       float r2[PC];
 #pragma unroll
       for (int q = 0; q < PC; ++q) r2[q] = 0.0f;
       for (int q = 0; q < p; ++q) {
-        df v[1] = {i < n ? df_mul(F[q * R + i], x1) : df_make(0.0f, 0.0f)};
+        df v[1] = {act ? df_mul(F[q * R + i], x1) : df_make(0.0f, 0.0f)};
         rows_sum_df<R, 1>(v, redd, slot);
         const df rq = df_sub(B[R + q], v[0]);
 #pragma unroll
         for (int r = 0; r < PC; ++r)
           if (r == q) r2[r] = rq.hi + rq.lo;
       }
-      vec[i] = i < n ? s + c : 0.0f;
+      vec[i] = act ? s + c : 0.0f;
       if (i == 0) {
 #pragma unroll
         for (int q = 0; q < PC; ++q)
@@ -377,7 +474,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       }
       rows_bar<R>();
       apply(d1, d2);
-      if (i < n) x1 = df_add_f(x1, d1);
+      if (act) x1 = df_add_f(x1, d1);
       mx = fabsf(d1);
 #pragma unroll
       for (int q = 0; q < PC; ++q) {
@@ -400,11 +497,11 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     // --- outputs: double-float sums, FP64 at the end
     df o[2];
     if (a.method == GS_SIMPLE) {
-      o[0] = i < n ? df_mul(x1, df_sub(Z[i], TD[3])) : df_make(0.0f, 0.0f);
+      o[0] = act ? df_mul(x1, df_sub(Z[i], TD[3])) : df_make(0.0f, 0.0f);
     } else {
-      o[0] = i < n ? df_mul(x1, Z[i]) : df_make(0.0f, 0.0f);
+      o[0] = act ? df_mul(x1, Z[i]) : df_make(0.0f, 0.0f);
     }
-    o[1] = i < n ? df_mul(x1, B[i]) : df_make(0.0f, 0.0f);
+    o[1] = act ? df_mul(x1, B[i]) : df_make(0.0f, 0.0f);
     rows_sum_df<R, 2>(o, redd, slot);
     if (i == 0) {
       df sr = o[1];
@@ -421,6 +518,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       flag[t] = 0;
     }
     rows_bar<R>();
+  }
   }
 }
 
@@ -614,7 +712,7 @@ static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   int per_sm = 0;
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R, smem));
   per_sm = std::max(per_sm, 1);
-  const int blocks = (int)std::min<int64_t>(a.ntl, (int64_t)sms * per_sm);
+  const int blocks = (int)std::min<int64_t>((a.ntl + kRowsRun - 1) / kRowsRun, (int64_t)sms * per_sm);
   kern<<<blocks, R, smem, stream>>>(a, m, g_tab, g_kc, flag);
   GS_CUDA(cudaGetLastError());
   count_launch(1);

@@ -95,9 +95,17 @@ __device__ __forceinline__ void rows_sum_df(df (&v)[K], df* red, int& slot) {
   }
 }
 
-// In-place sweep inverse of the register rows: after pivots 0..n-1 the
-// covariance block holds -C^{-1} with +2 on its diagonal (rows < n) and the
-// drift block holds C^{-1} F.
+// Element j of a register row stored as float2 pairs (j compile-time after
+// unrolling).
+template <int W2>
+__device__ __forceinline__ float row_elt(const float2 (&t)[W2], int j) {
+  return (j & 1) ? t[j >> 1].y : t[j >> 1].x;
+}
+
+// In-place sweep inverse of the register rows (2 * W2 columns as packed
+// pairs) over the pivots piv[0..npiv): afterwards the covariance block holds
+// -C^{-1} with +2 on its diagonal (pivot rows) and the drift block holds
+// C^{-1} F.
 //
 // Pivot k: thread k publishes its row with the pivot entry replaced by d - 1
 // (d = a_kk, also stored after the row); every thread then applies
@@ -107,18 +115,24 @@ __device__ __forceinline__ void rows_sum_df(df (&v)[K], df* red, int& slot) {
 // (a_ij -= a_ik a_kj / d, a_ik /= d, a_kj /= d) except on the pivot's own
 // diagonal, which becomes 2 - 1/d instead of -1/d; later pivots change that
 // entry linearly, so every swept diagonal ends exactly 2 too large.  Rows
-// beyond n are identity rows and never change (their published columns are
-// zero).  The row buffer is double-buffered, so one barrier per pivot
+// that are not pivots are identity rows and never change (their published
+// columns are zero).  The update runs as packed FP32x2 FMAs (two columns per
+// instruction).  The row buffer is double-buffered, so one barrier per pivot
 // suffices.  Returns false (uniformly) when a pivot is not above tol.
-template <int R, int W>
-__device__ __forceinline__ bool rows_sweep(float (&t)[W], int n, float tol, float* rowbuf) {
+template <int R, int W2>
+__device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int npiv, float tol,
+                                           float* rowbuf) {
+  constexpr int W = 2 * W2;
+  static_assert(W2 % 2 == 0, "rows are published as float4");
   const int i = threadIdx.x;
-  for (int k = 0; k < n; ++k) {
-    float* rb = rowbuf + (k & 1) * (W + 4);
+  for (int kk = 0; kk < npiv; ++kk) {
+    const int k = piv[kk];
+    float* rb = rowbuf + (kk & 1) * (W + 4);
     if (i == k) {
 #pragma unroll
-      for (int j = 0; j < W; j += 4)
-        *reinterpret_cast<float4*>(rb + j) = make_float4(t[j], t[j + 1], t[j + 2], t[j + 3]);
+      for (int j2 = 0; j2 < W2; j2 += 2)
+        *reinterpret_cast<float4*>(rb + 2 * j2) =
+            make_float4(t[j2].x, t[j2].y, t[j2 + 1].x, t[j2 + 1].y);
       const float d = rb[k];  // this thread's own store
       rb[k] = d - 1.0f;
       rb[W] = d;
@@ -126,35 +140,62 @@ __device__ __forceinline__ bool rows_sweep(float (&t)[W], int n, float tol, floa
     rows_bar<R>();
     const float d = rb[W];
     if (!(fabsf(d) > tol)) return false;
-    const float invd = __frcp_rn(d);
+    const float invd = __fdividef(1.0f, d);  // an approximate inverse suffices
     const float l = i == k ? 1.0f - invd : rb[i] * invd;
+    const float2 nl = make_float2(-l, -l);
 #pragma unroll
-    for (int j = 0; j < W; j += 4) {
-      const float4 r = *reinterpret_cast<const float4*>(rb + j);
-      t[j] = fmaf(-l, r.x, t[j]);
-      t[j + 1] = fmaf(-l, r.y, t[j + 1]);
-      t[j + 2] = fmaf(-l, r.z, t[j + 2]);
-      t[j + 3] = fmaf(-l, r.w, t[j + 3]);
+    for (int j2 = 0; j2 < W2; j2 += 2) {
+      const float4 r = *reinterpret_cast<const float4*>(rb + 2 * j2);
+      t[j2] = __ffma2_rn(nl, make_float2(r.x, r.y), t[j2]);
+      t[j2 + 1] = __ffma2_rn(nl, make_float2(r.z, r.w), t[j2 + 1]);
     }
   }
   return true;
 }
 
-// y_i = (C^{-1} v)_i for row i < n from the swept rows (v broadcast through
-// shared memory, zero beyond n).
-template <int R, int W>
-__device__ __forceinline__ float rows_cinv_apply(const float (&t)[W], const float* v, int n) {
+// y_i = (M^{-1} v)_i for a pivot row i (act) from the rows swept on M (v
+// broadcast through shared memory, zero off the pivots); packed FP32x2
+// products.
+template <int R, int W2>
+__device__ __forceinline__ float rows_cinv_apply(const float2 (&t)[W2], const float* v, bool act) {
   const int i = threadIdx.x;
-  float s = 0.0f;
+  float2 a0 = make_float2(0.0f, 0.0f), a1 = make_float2(0.0f, 0.0f);
 #pragma unroll
-  for (int j = 0; j < R; j += 4) {
-    const float4 q = *reinterpret_cast<const float4*>(v + j);
-    s = fmaf(t[j], q.x, s);
-    s = fmaf(t[j + 1], q.y, s);
-    s = fmaf(t[j + 2], q.z, s);
-    s = fmaf(t[j + 3], q.w, s);
+  for (int j2 = 0; j2 < R / 2; j2 += 2) {
+    const float4 q = *reinterpret_cast<const float4*>(v + 2 * j2);
+    a0 = __ffma2_rn(t[j2], make_float2(q.x, q.y), a0);
+    a1 = __ffma2_rn(t[j2 + 1], make_float2(q.z, q.w), a1);
   }
-  return i < n ? fmaf(2.0f, v[i], -s) : 0.0f;
+  const float s = (a0.x + a1.x) + (a0.y + a1.y);
+  return act ? fmaf(2.0f, v[i], -s) : 0.0f;
+}
+
+// 64-bit masks of two predicates over the block's threads (bit i = thread
+// i), identical in every thread.  sh: 4 words of shared scratch not read by
+// anyone else until the next barrier after this call.
+template <int R>
+__device__ __forceinline__ void rows_ballot2(bool p0, bool p1, unsigned long long& m0,
+                                             unsigned long long& m1, unsigned* sh) {
+  const unsigned b0 = __ballot_sync(0xffffffffu, p0), b1 = __ballot_sync(0xffffffffu, p1);
+  if constexpr (R == 32) {
+    m0 = b0;
+    m1 = b1;
+  } else {
+    static_assert(R == 64, "one or two warps");
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      sh[2 * w] = b0;
+      sh[2 * w + 1] = b1;
+    }
+    __syncthreads();
+    m0 = (unsigned long long)sh[0] | ((unsigned long long)sh[2] << 32);
+    m1 = (unsigned long long)sh[1] | ((unsigned long long)sh[3] << 32);
+  }
+}
+
+// Number of set bits of m below bit i.
+__device__ __forceinline__ int rank_below(unsigned long long m, int i) {
+  return __popcll(m & ((1ull << i) - 1ull));
 }
 
 }  // namespace gs

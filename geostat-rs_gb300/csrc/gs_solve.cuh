@@ -128,6 +128,87 @@ __device__ __forceinline__ df cov_pair(const DevModel& m, const Frames& fr, cons
   return c;
 }
 
+// Covariances at two separation norms (isotropic models), side by side.
+__device__ __forceinline__ void cov_from_norm2(const DevModel& m, df h0, df h1,
+                                               const ExpTable& tab, const DfConsts& k, df& c0,
+                                               df& c1) {
+  c0 = df_make(0.0f, 0.0f);
+  c1 = df_make(0.0f, 0.0f);
+#pragma unroll 1
+  for (int s = 0; s < m.ns; ++s) {
+    const DevStruct& st = m.s[s];
+    df r0, r1;
+    rho_df2(st.kind, df_mul(h0, st.inv_range_df), df_mul(h1, st.inv_range_df), tab, k, r0, r1);
+    c0 = df_add_fast(c0, df_mul(r0, st.sill_df));
+    c1 = df_add_fast(c1, df_mul(r1, st.sill_df));
+  }
+}
+
+// Visits this thread's pairs (i, j), i > j, of the strict lower triangle of
+// an n x n matrix -- pair numbers first, first + stride, first + 2 stride,
+// ... in packed order -- two at a time: fn(i0, j0, i1, j1, two).  When the
+// second pair does not exist, (i1, j1) repeats the first and two is false.
+template <class Fn>
+__device__ __forceinline__ void for_pairs2(int n, int first, int stride, Fn&& fn) {
+  const int npairs = (n * (n - 1)) >> 1;
+  int ii = 1, jj = first;
+  while (jj >= ii && ii < n) {
+    jj -= ii;
+    ++ii;
+  }
+  for (int q = first; q < npairs; q += 2 * stride) {
+    int ii2 = ii, jj2 = jj + stride;
+    while (jj2 >= ii2 && ii2 < n) {
+      jj2 -= ii2;
+      ++ii2;
+    }
+    const bool two = q + stride < npairs;
+    if (!two) {
+      ii2 = ii;
+      jj2 = jj;
+    }
+    fn(ii, jj, ii2, jj2, two);
+    ii = ii2;
+    jj = jj2 + stride;
+    while (jj >= ii && ii < n) {
+      jj -= ii;
+      ++ii;
+    }
+  }
+}
+
+// Covariances of two pairs (i0, j0) and (i1, j1) of stored points, evaluated
+// side by side so the two independent double-float chains interleave.
+template <int D>
+__device__ __forceinline__ void cov_pair2(const DevModel& m, const Frames& fr, const df* V,
+                                          int stride, int i0, int j0, int i1, int j1,
+                                          const ExpTable& tab, const DfConsts& k, df& c0,
+                                          df& c1) {
+  c0 = df_make(0.0f, 0.0f);
+  c1 = df_make(0.0f, 0.0f);
+  df h0iso = df_make(-1.0f, 0.0f), h1iso = df_make(-1.0f, 0.0f);
+#pragma unroll 1
+  for (int s = 0; s < m.ns; ++s) {
+    const DevStruct& st = m.s[s];
+    df h0, h1;
+    if (st.aniso) {
+      h0 = norm_pair<D>(V, stride, fr.fid[s], i0, j0);
+      h1 = norm_pair<D>(V, stride, fr.fid[s], i1, j1);
+    } else {
+      if (h0iso.hi < 0.0f) {
+        h0iso = norm_pair<D>(V, stride, 0, i0, j0);
+        h1iso = norm_pair<D>(V, stride, 0, i1, j1);
+      }
+      h0 = h0iso;
+      h1 = h1iso;
+    }
+    df r0, r1;
+    rho_df2(st.kind, df_mul(h0, st.inv_range_df), df_mul(h1, st.inv_range_df), tab, k, r0, r1);
+    c0 = df_add_fast(c0, df_mul(r0, st.sill_df));
+    c1 = df_add_fast(c1, df_mul(r1, st.sill_df));
+  }
+}
+
 // Covariance between stored point i and the frame origin (the target).
 template <int D>
 __device__ __forceinline__ df cov_origin(const DevModel& m, const Frames& fr, const df* V,

@@ -347,24 +347,14 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
       ZV[lane] = df_sub(a.vdf[j], a.mean_df);
     }
     __syncwarp();
-    const int npairs = (s * (s - 1)) >> 1;
-    // first pair (ii, jj) of this lane in the packed strict lower triangle
-    int ii0 = 1, jj0 = lane;
-    while (jj0 >= ii0 && ii0 < s) {
-      jj0 -= ii0;
-      ++ii0;
-    }
     if (a.iso_shared) {
       if (lane < s) H0[lane] = norm_origin<D>(V, M, 0, lane);
-      int ii = ii0, jj = jj0;
-      for (int q = lane; q < npairs; q += 32) {
-        H[pk(ii, jj)] = norm_pair<D>(V, M, 0, ii, jj);
-        jj += 32;
-        while (jj >= ii && ii < s) {
-          jj -= ii;
-          ++ii;
-        }
-      }
+      for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+        const df h0 = norm_pair<D>(V, M, 0, i0, j0);
+        const df h1 = norm_pair<D>(V, M, 0, i1, j1);
+        H[pk(i0, j0)] = h0;
+        if (two) H[pk(i1, j1)] = h1;
+      });
       __syncwarp();
     }
     for (int c = 0; c < a.ncand; ++c) {
@@ -375,15 +365,12 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
           B[lane] = cov_from_norm(mdl, H0[lane], tab, kc);
           A[pk(lane, lane)] = mdl.c0_df;
         }
-        int ii = ii0, jj = jj0;
-        for (int q = lane; q < npairs; q += 32) {
-          A[pk(ii, jj)] = cov_from_norm(mdl, H[pk(ii, jj)], tab, kc);
-          jj += 32;
-          while (jj >= ii && ii < s) {
-            jj -= ii;
-            ++ii;
-          }
-        }
+        for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+          df c0, c1;
+          cov_from_norm2(mdl, H[pk(i0, j0)], H[pk(i1, j1)], tab, kc, c0, c1);
+          A[pk(i0, j0)] = c0;
+          if (two) A[pk(i1, j1)] = c1;
+        });
       } else {
         if (lane < s) {
           df ud[3];
@@ -394,15 +381,12 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
           A[pk(lane, lane)] = mdl.c0_df;
         }
         __syncwarp();
-        int ii = ii0, jj = jj0;
-        for (int q = lane; q < npairs; q += 32) {
-          A[pk(ii, jj)] = cov_pair<D>(mdl, fr, V, M, ii, jj, tab, kc);
-          jj += 32;
-          while (jj >= ii && ii < s) {
-            jj -= ii;
-            ++ii;
-          }
-        }
+        for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+          df c0, c1;
+          cov_pair2<D>(mdl, fr, V, M, i0, j0, i1, j1, tab, kc, c0, c1);
+          A[pk(i0, j0)] = c0;
+          if (two) A[pk(i1, j1)] = c1;
+        });
       }
       __syncwarp();
       const bool ok = warp_solve(A, B, s, lane, W);

@@ -66,12 +66,18 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
   warp_load_rows(A, N, lane, ah, al);
   float amax = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kWarpN; ++j) {
-    t[j] = ah[j];
-    amax = fmaxf(amax, fabsf(ah[j]));
-  }
+  for (int j = 0; j < kWarpN; ++j) amax = fmaxf(amax, lane < N ? fabsf(ah[j]) : 0.0f);
   amax = warp_max_f(amax);
-  const float tol = 1e-6f * amax;
+  if (!(amax > 0.0f)) return false;
+  // power-of-two scale: sc * max|A| in [0.5, 1), so every pivot is <= 1 and
+  // the pivot lane's multiplier 1 - 1/d never cancels; the swept rows then
+  // hold -(sc A)^{-1}, i.e. -A^{-1} / sc
+  int ex = 0;
+  frexpf(amax, &ex);
+  const float sc = ldexpf(1.0f, -ex);
+#pragma unroll
+  for (int j = 0; j < kWarpN; ++j) t[j] = (lane < N && j < N) ? ah[j] * sc : ah[j];
+  const float tol = 1e-6f * amax * sc;
   for (int k = 0; k < N; ++k) {
     if (lane == k) {
 #pragma unroll
@@ -84,7 +90,7 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
     if (lane == k) W.row[k] = d - 1.0f;
     __syncwarp();
     if (!(fabsf(d) > tol)) return false;  // the same value in every lane
-    const float invd = __frcp_rn(d);
+    const float invd = __fdividef(1.0f, d);  // an approximate inverse suffices
     const float l = lane == k ? 1.0f - invd : W.row[lane] * invd;
 #pragma unroll
     for (int j = 0; j < kWarpN; j += 4) {
@@ -101,6 +107,7 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
   __syncwarp();
   float y;
   warp_gemv_neg_inv(t, W.vec, lane, y);
+  y *= sc;
   df x = df_make(lane < N ? -y : 0.0f, 0.0f);
   const float nx = warp_max_f(fabsf(x.hi));
   float nd_prev = nx;
@@ -128,6 +135,7 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
     W.vec[lane] = r;
     __syncwarp();
     warp_gemv_neg_inv(t, W.vec, lane, y);
+    y *= sc;
     if (lane < N) x = df_add_f(x, -y);
     const float nd = warp_max_f(lane < N ? fabsf(y) : 0.0f);
     if (nd <= 1e-15f * nx) {

@@ -245,9 +245,9 @@ int gs_synth_rff_field(int dim, int64_t n, const double* x, const double* y, con
 int gs_last_timings(double* ms4);
 
 /* Measurement helpers (no reference counterpart): sustained CUDA-core FMA
- * throughput in TFLOP/s for FP32 (precision 0) or FP64 (1) -- the roofline
- * denominator of the per-system kernels -- and the number of kernels this
- * library has launched since it was loaded. */
+ * throughput in TFLOP/s for FP32 (precision 0), FP64 (1) or packed FP32x2
+ * FMAs (2) -- the roofline denominator of the per-system kernels -- and the
+ * number of kernels this library has launched since it was loaded. */
 int gs_probe_fma_tflops(int precision, double* tflops);
 int64_t gs_launch_count(void);
 

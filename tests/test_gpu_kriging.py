@@ -291,3 +291,45 @@ def test_python_binding_mirror_matches_oracle():
                         method="universal", max_neighbors=20)
     ref3 = O.krige(c3, v3, m, t3, method="universal", max_neighbors=20)
     assert_close(pv3, ref3["value"], 10.0, 1e-9, "krige_3d")
+
+
+# ------------------------------------------------ consecutive grid targets --
+# A block solves consecutive targets and keeps the matrix entries of the
+# neighbours they share; grid targets (x fastest) exercise that reuse with
+# neighbour sets that change by a few points per step, and octant / radius
+# searches make the neighbour count vary from target to target.
+@pytest.mark.parametrize("case", [
+    dict(max_neighbors=64),
+    dict(max_neighbors=24, method="universal", degree=1),
+    dict(max_neighbors=48, method="universal", degree=2),
+    dict(max_neighbors=64, max_per_octant=16, min_neighbors=4),
+    dict(max_neighbors=40, search_radius=45.0, min_neighbors=2),
+    dict(max_neighbors=30, method="simple", mean=10.0),
+])
+def test_grid_targets_reuse_shared_neighbours(case):
+    c = uniform_points(6000, 2, 404, [1000.0, 1000.0])
+    m = VariogramModel(0.05, [Structure.with_anisotropy("spherical", 0.7, 150.0, 30.0, 0.5),
+                              Structure("exponential", 0.25, 400.0)])
+    v = 10.0 + G.rff_field(c, m, 1024, 12)
+    t = O.grid_centers([100, 100], [900, 900], [120, 40])
+    k, ref, outs = run_both(c, v, m, t, case, precisions=("mixed",))
+    check(ref, outs["mixed"], v, m.total_sill())
+
+
+def test_grid_targets_reuse_3d_and_external_drift():
+    c = uniform_points(8000, 3, 405, [600.0, 600.0, 60.0])
+    m = cfg2_model()
+    v = G.rff_field(c, m, 1024, 13)
+    t = O.grid_centers([50, 50, 5], [550, 550, 55], [64, 8, 4])
+    k, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64), precisions=("mixed",))
+    check(ref, outs["mixed"], v, m.total_sill())
+    c2 = uniform_points(5000, 2, 406, [1000.0, 1000.0])
+    m2 = cfg1_model()
+    drift = 0.01 * c2[:, 0:1] + O.rng_uniform(407, 5000).reshape(-1, 1)
+    v2 = 3.0 * drift[:, 0] + smooth_values(c2)
+    t2 = O.grid_centers([100, 100], [900, 900], [100, 20])
+    tdrift = 0.01 * t2[:, 0:1] + 0.5
+    k2, ref2, outs2 = run_both(c2, v2, m2, t2, dict(max_neighbors=32, method="external_drift",
+                                                    n_vars=1),
+                               drift=drift, tdrift=tdrift, precisions=("mixed",))
+    check(ref2, outs2["mixed"], v2, m2.total_sill())
