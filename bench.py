@@ -127,13 +127,15 @@ class ClockSampler:
 
 
 def read_profile_traffic():
-    """Per-launch DRAM traffic of the mixed kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "krige_mixed_kernel_cfg2.md")
+    """DRAM bytes per target of the kriging kernel from the committed ncu summary
+    (dram__bytes_read.sum + dram__bytes_write.sum of one captured launch divided by
+    the targets it solved)."""
+    path = os.path.join(ROOT, "profiles", "krige_rows_kernel_3d_ok64.md")
     try:
         text = open(path).read()
     except OSError:
         return None
-    m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", text)
+    m = re.search(r"dram_bytes_per_target:\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
 
 
@@ -273,9 +275,13 @@ def run_ours(args, rank, world):
         achieved = flops_per_launch_set / (mixed_ms * 1e-3) / 1e12
         peak_fp32 = C.c_double()
         peak_fp64 = C.c_double()
+        peak_x2 = C.c_double()
         _abi.check(lib.gs_probe_fma_tflops(0, C.byref(peak_fp32)))
         _abi.check(lib.gs_probe_fma_tflops(1, C.byref(peak_fp64)))
-        traffic = read_profile_traffic()
+        _abi.check(lib.gs_probe_fma_tflops(2, C.byref(peak_x2)))
+        bpt = read_profile_traffic()
+        # one launch of the kriging kernel per step (the neighbour lists fit one chunk)
+        traffic = bpt * nt if bpt is not None else None
         # accuracy and CPU baseline on a bounded sample
         acc, cpu = cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var,
                                            fp64_v, kr, log)
@@ -307,10 +313,12 @@ def run_ours(args, rank, world):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32.value,
                          "unit": "TFLOP/s", "frac": achieved / peak_fp32.value,
                          "traffic": traffic,
-                         "kernel": "krige_mixed_kernel",
+                         "kernel": "krige_rows_kernel",
                          "peak_source": "measured FP32 FMA probe (gs_probe_fma_tflops); "
                                         "MEASURED_PEAKS.json has no CUDA-core number",
+                         "fp32x2_peak_tflops": peak_x2.value,
                          "fp64_peak_tflops": peak_fp64.value,
+                         "traffic_bytes_per_target": bpt,
                          "algorithmic_flops_per_target": fpt,
                          "hbm_peak_gbs": peaks.get("hbm_gbs")},
             "cpu_baseline": cpu,

@@ -486,8 +486,9 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   a.err_df = k->d_err_df;
   a.n = n;
 
-  // chunking keeps the neighbour lists within a fixed budget
-  const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(nt, (int64_t)(1ll << 30) / (4ll * kout + 16)));
+  // chunking keeps the neighbour lists within a fixed budget (4 GiB: a
+  // 4.19 M-target grid with 64 neighbours is one chunk)
+  const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(nt, (int64_t)(4ll << 30) / (4ll * kout + 16)));
   DevBuf nb, nbc, flag, tlist, nsel, tmp;
   GS_TRY(nb.alloc((size_t)chunk * kout * 4, stream));
   GS_TRY(nbc.alloc((size_t)chunk * 4, stream));
