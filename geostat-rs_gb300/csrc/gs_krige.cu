@@ -120,14 +120,6 @@ __host__ __device__ inline RowsLayout rows_layout(int R, int PC, int nf, int dim
   return L;
 }
 
-// Exact coordinate coincidence (reference: gamma(0) = 0 only when every
-// separation component is exactly zero, -0 == +0), on the 64-bit patterns.
-__device__ __forceinline__ bool same_double(double a, double b) {
-  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
-  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
-  return x == y || ((x | y) << 1) == 0ull;
-}
-
 // K3: one system per block of R threads (n <= R neighbours, p <= PC drift
 // terms).  The system [C F; F^T 0] [w; mu] = [c; f] is solved through the
 // covariance block: the sweep gives -C^{-1} and G = C^{-1} F in registers,

@@ -11,6 +11,14 @@ namespace gs {
 
 __device__ __forceinline__ int pk(int i, int j) { return ((i * (i + 1)) >> 1) + j; }
 
+// Exact coordinate coincidence (reference: gamma(0) = 0 only when every
+// separation component is exactly zero, -0 == +0), on the 64-bit patterns.
+__device__ __forceinline__ bool same_double(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+  return x == y || ((x | y) << 1) == 0ull;
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -413,6 +413,39 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
   }
 }
 
+// cholesky_solve_in_place (linalg.rs:123-203) on an s x s row-major matrix
+// whose element e lives at S[e * T] (one slab per thread, interleaved): the
+// unpivoted factor with the reference's failure test !(d > 1e-12 max diag),
+// then the forward and back substitutions of W in place.
+__device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
+  double scale = 0.0;
+  for (int q = 0; q < s; ++q) scale = fmax(scale, S[(int64_t)(q * s + q) * T]);
+  scale = fmax(scale, 2.2250738585072014e-308);
+  for (int kk = 0; kk < s; ++kk) {
+    double d = S[(int64_t)(kk * s + kk) * T];
+    for (int j = 0; j < kk; ++j) d -= S[(int64_t)(kk * s + j) * T] * S[(int64_t)(kk * s + j) * T];
+    if (!(d > 1e-12 * scale)) return false;
+    d = sqrt(d);
+    S[(int64_t)(kk * s + kk) * T] = d;
+    for (int r = kk + 1; r < s; ++r) {
+      double acc = S[(int64_t)(r * s + kk) * T];
+      for (int j = 0; j < kk; ++j) acc -= S[(int64_t)(r * s + j) * T] * S[(int64_t)(kk * s + j) * T];
+      S[(int64_t)(r * s + kk) * T] = acc / d;
+    }
+  }
+  for (int r = 0; r < s; ++r) {
+    double acc = W[(int64_t)r * T];
+    for (int j = 0; j < r; ++j) acc -= S[(int64_t)(r * s + j) * T] * W[(int64_t)j * T];
+    W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
+  }
+  for (int r = s - 1; r >= 0; --r) {
+    double acc = W[(int64_t)r * T];
+    for (int j = r + 1; j < s; ++j) acc -= S[(int64_t)(j * s + r) * T] * W[(int64_t)j * T];
+    W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
+  }
+  return true;
+}
+
 // FP64 per-(candidate, point) solve: cholesky_solve_in_place
 // (linalg.rs:123-203) on the assembled K_SS of vecchia.rs:302-320.
 template <int D>
@@ -453,39 +486,10 @@ __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
         S[(int64_t)(bb * s + aa) * T] = cv;
       }
     }
-    double scale = 0.0;
-    for (int q = 0; q < s; ++q) scale = fmax(scale, S[(int64_t)(q * s + q) * T]);
-    scale = fmax(scale, 2.2250738585072014e-308);
-    bool fail_ = false;
-    for (int kk = 0; kk < s && !fail_; ++kk) {
-      double d = S[(int64_t)(kk * s + kk) * T];
-      for (int j = 0; j < kk; ++j) d -= S[(int64_t)(kk * s + j) * T] * S[(int64_t)(kk * s + j) * T];
-      if (!(d > 1e-12 * scale)) {
-        fail_ = true;
-        break;
-      }
-      d = sqrt(d);
-      S[(int64_t)(kk * s + kk) * T] = d;
-      for (int r = kk + 1; r < s; ++r) {
-        double acc = S[(int64_t)(r * s + kk) * T];
-        for (int j = 0; j < kk; ++j) acc -= S[(int64_t)(r * s + j) * T] * S[(int64_t)(kk * s + j) * T];
-        S[(int64_t)(r * s + kk) * T] = acc / d;
-      }
-    }
-    if (fail_) {
+    if (!chol_solve_strided(S, W, s, T)) {
       atomicExch(&cand_status[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
       a.terms[code] = __longlong_as_double(0x7ff8000000000000ll);
       continue;
-    }
-    for (int r = 0; r < s; ++r) {
-      double acc = W[(int64_t)r * T];
-      for (int j = 0; j < r; ++j) acc -= S[(int64_t)(r * s + j) * T] * W[(int64_t)j * T];
-      W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
-    }
-    for (int r = s - 1; r >= 0; --r) {
-      double acc = W[(int64_t)r * T];
-      for (int j = r + 1; j < s; ++j) acc -= S[(int64_t)(j * s + r) * T] * W[(int64_t)j * T];
-      W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
     }
     double mu = 0.0, red = 0.0;
     for (int q = 0; q < s; ++q) mu += W[(int64_t)q * T] * (a.v[nbk[q]] - a.mean);
@@ -774,6 +778,537 @@ int plan_create(const gs_pointset* ps, int64_t m, const int64_t* order, gs_vecch
   return GS_OK;
 }
 
+// ------------------------------------------------------ joint prediction --
+// vecchia_predict (vecchia.rs:748-866).  The conditioning store holds the
+// data (store index i = data index) followed by the targets in max-min
+// processing order (store index n + k for position k).  Target k conditions
+// on its m nearest store points of smaller index -- the ranked device search,
+// ties by store index like the reference's incremental BucketGrid.  A target
+// depends only on the targets in its conditioning set, so the targets are
+// solved level by level: level 0 conditions on data alone, level L on
+// targets of lower levels.  Per level, one warp per target solves its
+// conditional system (double-float assembly, FP32 inverse, refinement; the
+// reference's FP64 Cholesky for systems the refinement cannot certify) and
+// writes its weights, conditional mean and innovation variance; then one warp
+// per target merges the innovation rows of its conditioning targets.
+
+struct VPArgs {
+  int64_t n;            // data points
+  int64_t ns;           // store size n + nt
+  int kout;             // neighbour slots per target
+  const int32_t* nb;    // nt x kout store indices, nearest first
+  const int32_t* cnt;
+  const df* cdf;        // store coordinates as df, [dim][ns]
+  const double* sx;
+  const double* sy;
+  const double* sz;
+  double* smean64;      // conditional means: data z_i, then targets
+  df* smean_df;
+  double* w64;          // nt x kout conditioning weights
+  double* d64;          // innovation variances
+  uint8_t* flag;        // 1: solve in FP64
+  const int64_t* list;  // the level's targets
+  int64_t nlist;
+  int32_t* err;         // GS_ERR_SINGULAR_SYSTEM after an FP64 Cholesky failure
+};
+
+constexpr int kVPWarps = 4;
+
+// Store coordinates as double-float and the data's centred values.
+__global__ void vp_store_kernel(int dim, int64_t n, int64_t ns, const double* sx, const double* sy,
+                                const double* sz, const double* v, double mean, df* cdf,
+                                double* smean64, df* smean_df) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < ns;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    cdf[j] = df_from_double(sx[j]);
+    cdf[ns + j] = df_from_double(sy[j]);
+    if (dim == 3) cdf[2 * ns + j] = df_from_double(sz[j]);
+    if (j < n) {
+      const double z = v[j] - mean;
+      smean64[j] = z;
+      smean_df[j] = df_from_double(z);
+    }
+  }
+}
+
+// One warp per target of a level (conditioning sets of at most 32 points).
+template <int D>
+__global__ void __launch_bounds__(32 * kVPWarps) vp_solve_kernel(VPArgs a, DevModel m, ExpTable tab_g,
+                                                                DfConsts kc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ ExpTable tab;
+  for (int q = threadIdx.x; q < 256; q += blockDim.x) tab.v[q] = tab_g.v[q];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int M = a.kout;
+  const VWLayout lay = vecchia_warp_layout(M, D);
+  unsigned char* base = smem_raw + (size_t)wib * lay.total;
+  df* A = reinterpret_cast<df*>(base + lay.off_a);
+  df* V = reinterpret_cast<df*>(base + lay.off_v);
+  df* B = reinterpret_cast<df*>(base + lay.off_b);
+  WarpScratch W;
+  W.row = reinterpret_cast<float*>(base + lay.off_row);
+  W.vec = reinterpret_cast<float*>(base + lay.off_vec);
+  W.xd = reinterpret_cast<df*>(base + lay.off_xd);
+  const Frames fr = frames_of(m);
+  const double* sc[3] = {a.sx, a.sy, a.sz};
+  for (int64_t it = (int64_t)blockIdx.x * kVPWarps + wib; it < a.nlist;
+       it += (int64_t)gridDim.x * kVPWarps) {
+    const int64_t k = a.list[it];
+    const int s = a.cnt[k];
+    const int32_t* nbk = a.nb + k * (int64_t)M;
+    const int64_t tix = a.n + k;
+    __syncwarp();
+    if (s == 0) {
+      if (lane == 0) {
+        a.smean64[tix] = 0.0;
+        a.smean_df[tix] = df_make(0.0f, 0.0f);
+        a.d64[k] = m.c0;
+        a.flag[k] = 0;
+      }
+      continue;
+    }
+    if (lane < s) {
+      const int j = nbk[lane];
+      df ud[3];
+      bool zero = true;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        ud[d] = df_sub(a.cdf[(int64_t)d * a.ns + j], a.cdf[(int64_t)d * a.ns + tix]);
+        zero = zero && same_double(sc[d][j], sc[d][tix]);
+      }
+      frame_coords<D>(m, fr, ud, V, M, lane);
+      B[lane] = zero ? m.c0_df : cov_origin<D>(m, fr, V, M, lane, tab, kc);
+      A[pk(lane, lane)] = m.c0_df;
+    }
+    __syncwarp();
+    for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+      df c0, c1;
+      cov_pair2<D>(m, fr, V, M, i0, j0, i1, j1, tab, kc, c0, c1);
+      A[pk(i0, j0)] = c0;
+      if (two) A[pk(i1, j1)] = c1;
+    });
+    __syncwarp();
+    const bool ok = warp_solve(A, B, s, lane, W);
+    if (!ok) {
+      if (lane == 0) a.flag[k] = 1;
+      __syncwarp();
+      continue;
+    }
+    const df w = lane < s ? W.xd[lane] : df_make(0.0f, 0.0f);
+    df mu = lane < s ? df_mul(w, a.smean_df[nbk[lane]]) : df_make(0.0f, 0.0f);
+    df red = lane < s ? df_mul(w, B[lane]) : df_make(0.0f, 0.0f);
+    mu = warp_sum_df(mu);
+    red = warp_sum_df(red);
+    if (lane < s) a.w64[k * (int64_t)M + lane] = df_to_double(w);
+    if (lane == 0) {
+      a.smean64[tix] = df_to_double(mu);
+      a.smean_df[tix] = mu;
+      a.d64[k] = fmax(df_to_double(df_sub(m.c0_df, red)), 0.0);
+      a.flag[k] = 0;
+    }
+    __syncwarp();
+  }
+}
+
+// One thread per target of a level in FP64, the reference's algorithm:
+// K_SS and k_i from c0 - gamma (vecchia.rs:808-817), cholesky_solve_in_place,
+// mu and d in conditioning order.  all = 0: only flagged targets.
+template <int D>
+__global__ void vp_fp64_kernel(VPArgs a, DevModel m, double* scratch, int64_t T, int all) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tid >= T) return;
+  const int M = a.kout;
+  double* S = scratch + tid;
+  double* W = scratch + (int64_t)M * M * T + tid;
+  double* K0 = W + (int64_t)M * T;
+  for (int64_t it = tid; it < a.nlist; it += T) {
+    const int64_t k = a.list[it];
+    if (!all && !a.flag[k]) continue;
+    const int s = a.cnt[k];
+    const int64_t tix = a.n + k;
+    if (s == 0) {
+      a.smean64[tix] = 0.0;
+      a.smean_df[tix] = df_make(0.0f, 0.0f);
+      a.d64[k] = m.c0;
+      a.flag[k] = 0;
+      continue;
+    }
+    const int32_t* nbk = a.nb + k * (int64_t)M;
+    const double pt[3] = {a.sx[tix], a.sy[tix], D == 3 ? a.sz[tix] : 0.0};
+    for (int aa = 0; aa < s; ++aa) {
+      const int ja = nbk[aa];
+      const double h[3] = {pt[0] - a.sx[ja], pt[1] - a.sy[ja], D == 3 ? pt[2] - a.sz[ja] : 0.0};
+      const double kv = cov_fp64<D>(m, h);
+      W[(int64_t)aa * T] = kv;
+      K0[(int64_t)aa * T] = kv;
+      for (int bb = aa; bb < s; ++bb) {
+        const int jb = nbk[bb];
+        const double g[3] = {a.sx[ja] - a.sx[jb], a.sy[ja] - a.sy[jb],
+                             D == 3 ? a.sz[ja] - a.sz[jb] : 0.0};
+        const double cv = cov_fp64<D>(m, g);
+        S[(int64_t)(aa * s + bb) * T] = cv;
+        S[(int64_t)(bb * s + aa) * T] = cv;
+      }
+    }
+    if (!chol_solve_strided(S, W, s, T)) {
+      atomicExch(a.err, (int32_t)GS_ERR_SINGULAR_SYSTEM);
+      a.flag[k] = 0;
+      continue;
+    }
+    double mu = 0.0, red = 0.0;
+    for (int q = 0; q < s; ++q) mu += W[(int64_t)q * T] * a.smean64[nbk[q]];
+    for (int q = 0; q < s; ++q) red += W[(int64_t)q * T] * K0[(int64_t)q * T];
+    for (int q = 0; q < s; ++q) a.w64[k * (int64_t)M + q] = W[(int64_t)q * T];
+    a.smean64[tix] = mu;
+    a.smean_df[tix] = df_from_double(mu);
+    a.d64[k] = fmax(m.c0 - red, 0.0);
+    a.flag[k] = 0;
+  }
+}
+
+// Upper bound of each merged innovation row: 1 + the parents' row lengths.
+__global__ void vp_bound_kernel(const int64_t* list, int64_t nlist, int64_t n, int kout,
+                                const int32_t* nb, const int32_t* cnt, const int32_t* row_len,
+                                int64_t* bound) {
+  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < nlist;
+       it += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = list[it];
+    int64_t b = 1;
+    for (int q = 0; q < cnt[k]; ++q) {
+      const int j = nb[k * (int64_t)kout + q];
+      if (j >= n) b += row_len[j - n];
+    }
+    bound[it] = b;
+  }
+}
+
+__device__ __forceinline__ int warp_min_i(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Innovation rows (vecchia.rs:830-849): one warp per target; lane l follows
+// the rows of conditioning points l, l + 32, ... (rows are sorted by
+// innovation id); every step takes the smallest pending id, sums w_q * coef
+// over the rows holding it, keeps the sum when |sum| > tol, and finally
+// appends the target's own innovation sqrt(d).  var = sum of the squared
+// kept coefficients in id order.
+constexpr int kVPParentsPerLane = (GS_MAX_SYSTEM + 31) / 32;
+
+__global__ void vp_merge_kernel(const int64_t* list, int64_t nlist, int64_t n, int kout,
+                                const int32_t* nb, const int32_t* cnt, const double* w64,
+                                const double* d64, const int64_t* off, int64_t base,
+                                int64_t* row_off, int32_t* row_len, int32_t* pool_i,
+                                double* pool_c, double* var64, double tol) {
+  constexpr int PL = kVPParentsPerLane;
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t it = wid; it < nlist; it += nw) {
+    const int64_t k = list[it];
+    const int s = cnt[k];
+    int64_t poff[PL];
+    int plen[PL], cur[PL];
+    double w[PL];
+#pragma unroll
+    for (int u = 0; u < PL; ++u) {
+      poff[u] = 0;
+      plen[u] = 0;
+      cur[u] = 0;
+      w[u] = 0.0;
+      const int q = lane + 32 * u;
+      if (q < s) {
+        const int j = nb[k * (int64_t)kout + q];
+        if (j >= n) {
+          poff[u] = row_off[j - n];
+          plen[u] = row_len[j - n];
+          w[u] = w64[k * (int64_t)kout + q];
+        }
+      }
+    }
+    const int64_t out = base + off[it];
+    int count = 0;
+    double var = 0.0;
+    while (true) {
+      int head = 0x7fffffff;
+#pragma unroll
+      for (int u = 0; u < PL; ++u)
+        if (cur[u] < plen[u]) head = min(head, pool_i[poff[u] + cur[u]]);
+      const int mn = warp_min_i(head);
+      if (mn == 0x7fffffff) break;
+      double contrib = 0.0;
+#pragma unroll
+      for (int u = 0; u < PL; ++u) {
+        if (cur[u] < plen[u] && pool_i[poff[u] + cur[u]] == mn) {
+          contrib += w[u] * pool_c[poff[u] + cur[u]];
+          ++cur[u];
+        }
+      }
+      const double acc = warp_sum_d(contrib);
+      if (fabs(acc) > tol) {
+        if (lane == 0) {
+          pool_i[out + count] = mn;
+          pool_c[out + count] = acc;
+        }
+        ++count;
+        var += acc * acc;
+      }
+    }
+    const double own = sqrt(d64[k]);
+    if (lane == 0) {
+      pool_i[out + count] = (int)k;
+      pool_c[out + count] = own;
+      row_off[k] = out;
+      row_len[k] = count + 1;
+      var64[k] = var + own * own;
+    }
+  }
+}
+
+int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t nt, const double* tx,
+                         const double* ty, const double* tz, int64_t m, double* value,
+                         double* variance) {
+  const int dim = ps->dim;
+  GS_TRY(reject_vecchia_model(*model, dim));
+  DevModel dm;
+  GS_TRY(make_dev_model(*model, dim, &dm, true));
+  if (m <= 0) return fail(GS_ERR_INVALID_PARAMETER, "conditioning size m must be at least 1");
+  if (nt == 0) return GS_OK;
+  if (ps->has_dup)
+    return fail(GS_ERR_DUPLICATE_POINTS, "duplicate data points: indices " + std::to_string(ps->dup_i) +
+                                             " and " + std::to_string(ps->dup_j) +
+                                             " share the same coordinates");
+  const int64_t n = ps->n;
+  const int64_t ns = n + nt;
+  const int kout = (int)std::min<int64_t>(m, ns - 1);
+  if (kout > GS_MAX_SYSTEM)
+    return fail(GS_ERR_INVALID_PARAMETER, "the CUDA path conditions on at most " +
+                                              std::to_string(GS_MAX_SYSTEM) + " points");
+  if (!g_vready) {
+    df_consts_host(&g_vtab, &g_vkc);
+    g_vready = true;
+  }
+  double sum = 0.0;
+  for (int64_t i = 0; i < n; ++i) sum += ps->values[i];
+  const double mean = sum / (double)n;
+  // targets in max-min order (vecchia.rs:792)
+  std::vector<double> tp((size_t)nt * dim);
+  for (int64_t i = 0; i < nt; ++i) {
+    tp[i * dim] = tx[i];
+    tp[i * dim + 1] = ty[i];
+    if (dim == 3) tp[i * dim + 2] = tz[i];
+  }
+  std::vector<int64_t> order(nt);
+  maxmin_order(tp, dim, nt, order.data());
+  std::vector<double> ox(nt), oy(nt), oz(dim == 3 ? nt : 0);
+  for (int64_t k = 0; k < nt; ++k) {
+    ox[k] = tx[order[k]];
+    oy[k] = ty[order[k]];
+    if (dim == 3) oz[k] = tz[order[k]];
+  }
+  cudaStream_t s = nullptr;
+  GS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  } guard{s};
+  DevBuf sx, sy, sz, cdf, sm64, smdf, nb, cnt, w64, d64, var64, flag, roff, rlen, err, list, bound,
+      offs, scan_tmp, pool_i, pool_c;
+  GS_TRY(sx.alloc(ns * 8, s));
+  GS_TRY(sy.alloc(ns * 8, s));
+  if (dim == 3) GS_TRY(sz.alloc(ns * 8, s));
+  GS_CUDA(cudaMemcpyAsync(sx.ptr, ps->d_x, n * 8, cudaMemcpyDeviceToDevice, s));
+  GS_CUDA(cudaMemcpyAsync(sy.ptr, ps->d_y, n * 8, cudaMemcpyDeviceToDevice, s));
+  if (dim == 3) GS_CUDA(cudaMemcpyAsync(sz.ptr, ps->d_z, n * 8, cudaMemcpyDeviceToDevice, s));
+  GS_CUDA(cudaMemcpyAsync((double*)sx.ptr + n, ox.data(), nt * 8, cudaMemcpyHostToDevice, s));
+  GS_CUDA(cudaMemcpyAsync((double*)sy.ptr + n, oy.data(), nt * 8, cudaMemcpyHostToDevice, s));
+  if (dim == 3)
+    GS_CUDA(cudaMemcpyAsync((double*)sz.ptr + n, oz.data(), nt * 8, cudaMemcpyHostToDevice, s));
+  GS_TRY(cdf.alloc((size_t)dim * ns * sizeof(df), s));
+  GS_TRY(sm64.alloc(ns * 8, s));
+  GS_TRY(smdf.alloc(ns * sizeof(df), s));
+  vp_store_kernel<<<(int)std::min<int64_t>((ns + 255) / 256, 152 * 32), 256, 0, s>>>(
+      dim, n, ns, (double*)sx.ptr, (double*)sy.ptr, (double*)sz.ptr, ps->d_v, mean, (df*)cdf.ptr,
+      (double*)sm64.ptr, (df*)smdf.ptr);
+  GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  // conditioning sets: ranked search over the store (rank = store index)
+  GS_TRY(nb.alloc((size_t)nt * kout * 4, s));
+  GS_TRY(cnt.alloc(nt * 4, s));
+  {
+    Grid g;
+    GS_TRY(grid_build_ranked(&g, dim, ns, (double*)sx.ptr, (double*)sy.ptr, (double*)sz.ptr,
+                             dim == 2 ? 2.0 : 3.0, s));
+    SearchFrame f;
+    std::memset(&f, 0, sizeof(f));
+    SearchParams sp{};
+    sp.k = kout;
+    sp.kout = kout;
+    sp.ranked = 1;
+    sp.rank0 = n;
+    sp.brute_below = 2048;
+    sp.px = (double*)sx.ptr;
+    sp.py = (double*)sy.ptr;
+    sp.pz = (double*)sz.ptr;
+    GS_TRY(search_launch(g, f, sp, nt, (double*)sx.ptr + n, (double*)sy.ptr + n,
+                         dim == 3 ? (double*)sz.ptr + n : nullptr, (int32_t*)nb.ptr,
+                         (int32_t*)cnt.ptr, s));
+  }
+  // dependency levels (host): level k = 1 + the highest level among its
+  // conditioning targets, 0 when it conditions on data alone
+  std::vector<int32_t> hnb((size_t)nt * kout), hcnt(nt);
+  GS_CUDA(cudaMemcpyAsync(hnb.data(), nb.ptr, (size_t)nt * kout * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hcnt.data(), cnt.ptr, nt * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  std::vector<int32_t> level(nt, 0);
+  int nlev = 0;
+  for (int64_t k = 0; k < nt; ++k) {
+    int lv = 0;
+    for (int q = 0; q < hcnt[k]; ++q) {
+      const int64_t j = hnb[(size_t)k * kout + q];
+      if (j >= n) lv = std::max(lv, level[j - n] + 1);
+    }
+    level[k] = lv;
+    nlev = std::max(nlev, lv + 1);
+  }
+  std::vector<int64_t> lstart(nlev + 1, 0), hlist(nt);
+  for (int64_t k = 0; k < nt; ++k) ++lstart[level[k] + 1];
+  for (int l = 0; l < nlev; ++l) lstart[l + 1] += lstart[l];
+  {
+    std::vector<int64_t> fill(lstart.begin(), lstart.end() - 1);
+    for (int64_t k = 0; k < nt; ++k) hlist[fill[level[k]]++] = k;
+  }
+  GS_TRY(list.alloc(nt * 8, s));
+  GS_CUDA(cudaMemcpyAsync(list.ptr, hlist.data(), nt * 8, cudaMemcpyHostToDevice, s));
+  GS_TRY(w64.alloc((size_t)nt * kout * 8, s));
+  GS_TRY(d64.alloc(nt * 8, s));
+  GS_TRY(var64.alloc(nt * 8, s));
+  GS_TRY(flag.alloc(nt, s));
+  GS_TRY(roff.alloc(nt * 8, s));
+  GS_TRY(rlen.alloc(nt * 4, s));
+  GS_TRY(err.alloc(4, s));
+  GS_TRY(bound.alloc(nt * 8, s));
+  GS_TRY(offs.alloc(nt * 8, s));
+  GS_CUDA(cudaMemsetAsync(err.ptr, 0, 4, s));
+  GS_CUDA(cudaMemsetAsync(flag.ptr, 1, nt, s));
+  size_t scan_bytes = 0;
+  GS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (int64_t*)nullptr, (int64_t*)nullptr,
+                                        (int64_t)nt, s));
+  GS_TRY(scan_tmp.alloc(scan_bytes, s));
+  int64_t cap = std::max<int64_t>(nt * 8, 1024), used = 0;
+  GS_TRY(pool_i.alloc(cap * 4, s));
+  GS_TRY(pool_c.alloc(cap * 8, s));
+  VPArgs a{};
+  a.n = n;
+  a.ns = ns;
+  a.kout = kout;
+  a.nb = (const int32_t*)nb.ptr;
+  a.cnt = (const int32_t*)cnt.ptr;
+  a.cdf = (const df*)cdf.ptr;
+  a.sx = (const double*)sx.ptr;
+  a.sy = (const double*)sy.ptr;
+  a.sz = (const double*)sz.ptr;
+  a.smean64 = (double*)sm64.ptr;
+  a.smean_df = (df*)smdf.ptr;
+  a.w64 = (double*)w64.ptr;
+  a.d64 = (double*)d64.ptr;
+  a.flag = (uint8_t*)flag.ptr;
+  a.err = (int32_t*)err.ptr;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const bool mixed = kout <= kWarpN;
+  size_t vsmem = 0;
+  if (mixed) {
+    vsmem = vecchia_warp_layout(kout, dim).total * kVPWarps;
+    auto kern = dim == 2 ? vp_solve_kernel<2> : vp_solve_kernel<3>;
+    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+  }
+  // FP64 slabs: up to 2 GiB, at least one block of threads
+  const int64_t per = ((int64_t)kout * kout + 2 * (int64_t)kout) * 8;
+  int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / per, 128), 152 * 1024);
+  T = std::max<int64_t>((T / 128) * 128, 128);
+  DevBuf slab;
+  GS_TRY(slab.alloc((size_t)T * per, s));
+  const double tol = 1e-8 * std::sqrt(dm.c0);
+  for (int l = 0; l < nlev; ++l) {
+    const int64_t l0 = lstart[l], ln = lstart[l + 1] - l0;
+    a.list = (const int64_t*)list.ptr + l0;
+    a.nlist = ln;
+    if (mixed) {
+      const int blocks = (int)std::min<int64_t>((ln + kVPWarps - 1) / kVPWarps, (int64_t)sms * 8);
+      if (dim == 2) vp_solve_kernel<2><<<blocks, 32 * kVPWarps, vsmem, s>>>(a, dm, g_vtab, g_vkc);
+      else vp_solve_kernel<3><<<blocks, 32 * kVPWarps, vsmem, s>>>(a, dm, g_vtab, g_vkc);
+      GS_CUDA(cudaGetLastError());
+      count_launch(1);
+    }
+    {
+      const int64_t Tl = std::min<int64_t>(T, ((ln + 127) / 128) * 128);
+      const int blocks = (int)((Tl + 127) / 128);
+      if (dim == 2) vp_fp64_kernel<2><<<blocks, 128, 0, s>>>(a, dm, (double*)slab.ptr, Tl, mixed ? 0 : 1);
+      else vp_fp64_kernel<3><<<blocks, 128, 0, s>>>(a, dm, (double*)slab.ptr, Tl, mixed ? 0 : 1);
+      GS_CUDA(cudaGetLastError());
+      count_launch(1);
+    }
+    const int gb = (int)std::min<int64_t>((ln + 255) / 256, 152 * 32);
+    vp_bound_kernel<<<gb, 256, 0, s>>>(a.list, ln, n, kout, a.nb, a.cnt, (const int32_t*)rlen.ptr,
+                                      (int64_t*)bound.ptr);
+    GS_CUDA(cudaGetLastError());
+    size_t b = scan_bytes;
+    GS_CUDA(cub::DeviceScan::ExclusiveSum(scan_tmp.ptr, b, (int64_t*)bound.ptr, (int64_t*)offs.ptr,
+                                          ln, s));
+    count_launch(2);
+    int64_t last[2] = {0, 0};
+    GS_CUDA(cudaMemcpyAsync(&last[0], (int64_t*)offs.ptr + ln - 1, 8, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaMemcpyAsync(&last[1], (int64_t*)bound.ptr + ln - 1, 8, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaStreamSynchronize(s));
+    const int64_t need = used + last[0] + last[1];
+    if (need > cap) {
+      const int64_t ncap = std::max<int64_t>(need, cap * 2);
+      DevBuf ni, nc;
+      GS_TRY(ni.alloc(ncap * 4, s));
+      GS_TRY(nc.alloc(ncap * 8, s));
+      if (used > 0) {
+        GS_CUDA(cudaMemcpyAsync(ni.ptr, pool_i.ptr, used * 4, cudaMemcpyDeviceToDevice, s));
+        GS_CUDA(cudaMemcpyAsync(nc.ptr, pool_c.ptr, used * 8, cudaMemcpyDeviceToDevice, s));
+      }
+      std::swap(ni.ptr, pool_i.ptr);
+      std::swap(ni.bytes, pool_i.bytes);
+      std::swap(nc.ptr, pool_c.ptr);
+      std::swap(nc.bytes, pool_c.bytes);
+      cap = ncap;
+    }
+    const int mb = (int)std::min<int64_t>((ln * 32 + 255) / 256, 152 * 32);
+    vp_merge_kernel<<<mb, 256, 0, s>>>(a.list, ln, n, kout, a.nb, a.cnt, a.w64, a.d64,
+                                       (const int64_t*)offs.ptr, used, (int64_t*)roff.ptr,
+                                       (int32_t*)rlen.ptr, (int32_t*)pool_i.ptr,
+                                       (double*)pool_c.ptr, (double*)var64.ptr, tol);
+    GS_CUDA(cudaGetLastError());
+    count_launch(1);
+    used = need;
+  }
+  int32_t herr = 0;
+  std::vector<double> hmu(nt), hvar(nt);
+  GS_CUDA(cudaMemcpyAsync(&herr, err.ptr, 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hmu.data(), (double*)sm64.ptr + n, nt * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hvar.data(), var64.ptr, nt * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  if (herr)
+    return fail(GS_ERR_SINGULAR_SYSTEM,
+                "non-positive Cholesky pivot in a Vecchia prediction conditioning system");
+  for (int64_t k = 0; k < nt; ++k) {
+    value[order[k]] = mean + hmu[k];
+    variance[order[k]] = hvar[k];
+  }
+  return GS_OK;
+}
+
 }  // namespace gs
 
 using namespace gs;
@@ -999,6 +1534,10 @@ int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t n
 extern "C" int gs_vecchia_predict(const gs_pointset* ps, const gs_model* model, int64_t nt,
                                   const double* tx, const double* ty, const double* tz, int64_t m,
                                   double* value, double* variance) {
-  (void)ps; (void)model; (void)nt; (void)tx; (void)ty; (void)tz; (void)m; (void)value; (void)variance;
-  return gs::fail(GS_ERR_INVALID_PARAMETER, "vecchia_predict is not available yet");
+  if (!ps || !model) return gs::fail(GS_ERR_INVALID_PARAMETER, "null point set or model");
+  if (nt < 0) return gs::fail(GS_ERR_INVALID_PARAMETER, "negative target count");
+  if (nt > 0 && (!tx || !ty || (ps->dim == 3 && !tz) || !value || !variance))
+    return gs::fail(GS_ERR_INVALID_PARAMETER, "null target or output buffer");
+  GS_TRY(gs::ensure_device());
+  return gs::vecchia_predict_impl(ps, model, nt, tx, ty, tz, m, value, variance);
 }

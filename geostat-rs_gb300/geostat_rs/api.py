@@ -487,6 +487,23 @@ def vecchia_krige(x, y, values, model, target_x, target_y, m=30):
     return v, var
 
 
+def vecchia_predict(coords, values, model, targets, m=30):
+    """``vecchia_predict`` (vecchia.rs:748-866) in 2-D or 3-D: joint Vecchia
+    prediction at ``targets``; returns ``(values, variances)``."""
+    data = PointSet(coords, values)
+    targets = np.ascontiguousarray(np.asarray(targets, dtype=np.float64))
+    if targets.ndim != 2 or targets.shape[1] != data.dim:
+        raise DimensionMismatch("targets must be an (nt, dim) array matching the data")
+    nt = len(targets)
+    cols = [np.ascontiguousarray(targets[:, d]) for d in range(data.dim)]
+    v, var = np.empty(nt), np.empty(nt)
+    _abi.check(_abi.load().gs_vecchia_predict(data._h, C.byref(model_struct(model)), nt,
+                                              _p(cols[0]), _p(cols[1]),
+                                              _p(cols[2]) if data.dim == 3 else None, int(m),
+                                              _p(v), _p(var)))
+    return v, var
+
+
 def nelder_mead_multistart(fn, starts, step, max_iter):
     """The library's Nelder-Mead state machine driven by a Python objective."""
     starts = _f64(starts)

@@ -109,3 +109,65 @@ def test_mle_objective_parity_and_batched_nelder_mead():
     fx = O.vecchia_mle_objective(c, v, "exponential", 12, o, nb, cnt, rmax, x)
     assert abs(fx[0] + ll) <= 1e-9 * abs(fx[0])
     assert model.nugget >= 0 and model.structures[0].range > 0
+
+
+# ------------------------------------------------------- joint prediction --
+@pytest.mark.parametrize("dim,n,nt,m", [(2, 3000, 800, 30), (2, 2000, 600, 8), (3, 2000, 500, 20),
+                                        (2, 1200, 300, 40)])
+def test_vecchia_predict_matches_oracle(dim, n, nt, m):
+    """vecchia.rs:748-866: targets appended after the data in max-min order,
+    each conditioning on its m nearest earlier store points; m > 32 runs the
+    FP64 Cholesky path for every target."""
+    if dim == 2:
+        c, v = O.test_field_2d(n, 300 + n)
+        t = uniform_points(nt, 2, 301, [100.0, 100.0])
+        mdl = VariogramModel(0.05, [Structure("exponential", 0.95, 25.0)])
+    else:
+        c, v = O.test_field_3d(n, 302)
+        t = uniform_points(nt, 3, 303, [100.0, 100.0, 100.0])
+        mdl = VariogramModel(0.05, [Structure.with_rotation("spherical", 0.9, 40.0, 20.0, 10.0, 5.0,
+                                                            0.6, 0.4)])
+    gv, gvar = G.vecchia_predict(c, v, mdl, t, m)
+    rv, rvar = O.vecchia_predict(c, v, mdl, t, m)
+    assert_close(gv, rv, float(np.mean(np.abs(v))), 1e-9, "value")
+    assert_close(gvar, rvar, mdl.total_sill(), 1e-9, "variance")
+
+
+def test_vecchia_predict_full_conditioning_equals_simple_kriging():
+    # vecchia.rs:2131-2167: m >= n + targets gives global simple kriging
+    c, v = O.test_field_2d(60, 5)
+    mdl = VariogramModel(0.1, [Structure("exponential", 0.9, 30.0)])
+    t = np.array([[12.0, 33.0], [55.0, 71.0], [80.0, 20.0], [40.0, 40.0]])
+    gv, gvar = G.vecchia_predict(c, v, mdl, t, 1000)
+    sk = O.krige(c, v, mdl, t, method="simple", mean=float(np.sum(v) / len(v)))
+    assert np.max(np.abs(gv - sk["value"])) < 1e-8
+    assert np.max(np.abs(gvar - sk["variance"])) < 1e-8
+
+
+def test_vecchia_predict_deterministic_and_edge_cases():
+    # vecchia.rs:2203-2240: bit-identical on repeat
+    c, v = O.test_field_2d(150, 11)
+    mdl = VariogramModel(0.05, [Structure("exponential", 0.95, 25.0)])
+    t = np.array([[1.7 * i + 3.0, 96.0 - 1.6 * i] for i in range(60)])
+    a = G.vecchia_predict(c, v, mdl, t, 8)
+    b = G.vecchia_predict(c, v, mdl, t, 8)
+    assert a[0].tobytes() == b[0].tobytes() and a[1].tobytes() == b[1].tobytes()
+    r = O.vecchia_predict(c, v, mdl, t, 8)
+    assert_close(a[0], r[0], float(np.mean(np.abs(v))), 1e-9, "value")
+    assert_close(a[1], r[1], 1.0, 1e-9, "variance")
+    # a target on a data point, and a single target
+    t1 = np.array([c[17]])
+    g1 = G.vecchia_predict(c, v, mdl, t1, 12)
+    r1 = O.vecchia_predict(c, v, mdl, t1, 12)
+    assert_close(g1[0], r1[0], 1.0, 1e-9, "value at a datum")
+    assert_close(g1[1], r1[1], 1.0, 1e-9, "variance at a datum")
+    # empty target set, and the reference's rejections
+    e = G.vecchia_predict(c, v, mdl, np.zeros((0, 2)), 8)
+    assert len(e[0]) == 0 and len(e[1]) == 0
+    with pytest.raises(G.InvalidParameter):
+        G.vecchia_predict(c, v, mdl, t, 0)
+    with pytest.raises(G.InvalidParameter):
+        G.vecchia_predict(c, v, VariogramModel(0.0, [Structure("power", 1.0, 1.0, param=1.0)]), t, 8)
+    dup = np.vstack([c, c[:1]])
+    with pytest.raises(G.DuplicatePoints):
+        G.vecchia_predict(dup, np.append(v, 1.0), mdl, t, 8)
