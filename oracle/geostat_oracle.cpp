@@ -1508,6 +1508,305 @@ void mle_setup(const double* coords, const double* values, size_t n, int dim, do
   }
 }
 
+// vecchia.rs:353-389 g_and_dg: unit-sill variogram g(d) and dg/dd for the
+// kinds with a closed-form range derivative.
+bool g_and_dg(int kind, double d, double* g, double* dg) {
+  switch (kind) {
+    case OR_SPHERICAL:
+      if (d >= 1.0) {
+        *g = 1.0;
+        *dg = 0.0;
+      } else {
+        *g = 1.5 * d - 0.5 * d * d * d;
+        *dg = 1.5 - 1.5 * d * d;
+      }
+      return true;
+    case OR_EXPONENTIAL: {
+      double e = std::exp(-d);
+      *g = 1.0 - e;
+      *dg = e;
+      return true;
+    }
+    case OR_GAUSSIAN: {
+      double e = std::exp(-(d * d));
+      *g = 1.0 - e;
+      *dg = 2.0 * d * e;
+      return true;
+    }
+    case OR_MATERN15: {
+      double s = std::sqrt(3.0) * d;
+      double e = std::exp(-s);
+      *g = 1.0 - (1.0 + s) * e;
+      *dg = 3.0 * d * e;
+      return true;
+    }
+    case OR_MATERN25: {
+      double s = std::sqrt(5.0) * d;
+      double e = std::exp(-s);
+      *g = 1.0 - (1.0 + s + s * s / 3.0) * e;
+      *dg = 5.0 * d * (1.0 + s) / 3.0 * e;
+      return true;
+    }
+    default:
+      return false;
+  }
+}
+
+// vecchia.rs:93-100 dist2.
+double dist2_(const double* a, const double* b, int dim) {
+  double s = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    double v = a[d] - b[d];
+    s += v * v;
+  }
+  return s;
+}
+
+// vecchia.rs:428-530 loglik_grad_inner: the log-likelihood and its gradient
+// with respect to (nugget, psill, range) of a single isotropic structure.
+int loglik_grad(const double* coords, const double* values, size_t n, int dim, int kind,
+                double nugget, double psill, double range, const Plan& plan, double* ll_out,
+                double* grad_out) {
+  double gg, dgg;
+  if (!g_and_dg(kind, 0.5, &gg, &dgg)) return fail(OR_INVALID_PARAMETER, "no closed-form gradient");
+  double mean = mean_of(values, n);
+  std::vector<double> z(n);
+  for (size_t i = 0; i < n; ++i) z[i] = values[i] - mean;
+  const double sill = nugget + psill;
+  const double ln2pi = std::log(2.0 * kPi);
+  std::vector<double> kss, ki, w, dk_psill, dk_range, dki_psill, dki_range, rhs, dw;
+  double loglik = 0.0;
+  double grad[3] = {0.0, 0.0, 0.0};
+  for (size_t k = 0; k < plan.order.size(); ++k) {
+    size_t i = plan.order[k];
+    const std::vector<size_t>& nb = plan.nb[k];
+    if (nb.empty()) {
+      double var = sill;
+      double r = z[i];
+      loglik += -0.5 * (ln2pi + std::log(var) + r * r / var);
+      double common = -0.5 / var + 0.5 * r * r / (var * var);
+      grad[0] += common;
+      grad[1] += common;
+      continue;
+    }
+    size_t s = nb.size();
+    kss.assign(s * s, 0.0);
+    ki.assign(s, 0.0);
+    dk_psill.assign(s * s, 0.0);
+    dk_range.assign(s * s, 0.0);
+    dki_psill.assign(s, 0.0);
+    dki_range.assign(s, 0.0);
+    for (size_t a = 0; a < s; ++a) {
+      double h_ia = std::sqrt(dist2_(&coords[i * dim], &coords[nb[a] * dim], dim));
+      double g_ia, dg_ia;
+      g_and_dg(kind, h_ia / range, &g_ia, &dg_ia);
+      ki[a] = sill - (nugget + psill * g_ia);
+      dki_psill[a] = 1.0 - g_ia;
+      dki_range[a] = psill * dg_ia * h_ia / (range * range);
+      kss[a * s + a] = sill;
+      dk_psill[a * s + a] = 1.0;
+      for (size_t b = a + 1; b < s; ++b) {
+        double h_ab = std::sqrt(dist2_(&coords[nb[a] * dim], &coords[nb[b] * dim], dim));
+        double g_ab, dg_ab;
+        g_and_dg(kind, h_ab / range, &g_ab, &dg_ab);
+        double c = sill - (nugget + psill * g_ab);
+        kss[a * s + b] = c;
+        kss[b * s + a] = c;
+        double dp = 1.0 - g_ab;
+        dk_psill[a * s + b] = dp;
+        dk_psill[b * s + a] = dp;
+        double dr = psill * dg_ab * h_ab / (range * range);
+        dk_range[a * s + b] = dr;
+        dk_range[b * s + a] = dr;
+      }
+    }
+    int rc = cholesky_factor(kss.data(), s);
+    if (rc) return rc;
+    w = ki;
+    cholesky_forward(kss.data(), s, w.data());
+    cholesky_back(kss.data(), s, w.data());
+    double mu = 0.0;
+    for (size_t a = 0; a < s; ++a) mu += w[a] * z[nb[a]];
+    double reduction = 0.0;
+    for (size_t a = 0; a < s; ++a) reduction += w[a] * ki[a];
+    double raw_var = sill - reduction;
+    double var = fmax_(raw_var, 1e-12);
+    bool clamped = raw_var <= 1e-12;
+    double r = z[i] - mu;
+    loglik += -0.5 * (ln2pi + std::log(var) + r * r / var);
+    auto solve_param = [&](double dsill_dp, const double* dk, const double* dki) {
+      rhs.assign(s, 0.0);
+      if (dk) {
+        // vecchia.rs:391-398 matvec
+        dw.assign(s, 0.0);
+        for (size_t row = 0; row < s; ++row) {
+          double acc = 0.0;
+          for (size_t j = 0; j < s; ++j) acc += dk[row * s + j] * w[j];
+          dw[row] = acc;
+        }
+        for (size_t a = 0; a < s; ++a) rhs[a] = dki[a] - dw[a];
+      } else {
+        for (size_t a = 0; a < s; ++a) rhs[a] = -w[a];
+      }
+      dw = rhs;
+      cholesky_forward(kss.data(), s, dw.data());
+      cholesky_back(kss.data(), s, dw.data());
+      double dmu = 0.0;
+      for (size_t a = 0; a < s; ++a) dmu += dw[a] * z[nb[a]];
+      double d1 = 0.0, d2 = 0.0;
+      for (size_t a = 0; a < s; ++a) d1 += dw[a] * ki[a];
+      for (size_t a = 0; a < s; ++a) d2 += w[a] * dki[a];
+      double dreduction = d1 + d2;
+      double dvar = clamped ? 0.0 : dsill_dp - dreduction;
+      return -0.5 * dvar / var + r * dmu / var + 0.5 * r * r / (var * var) * dvar;
+    };
+    std::vector<double> zeros(s, 0.0);
+    grad[0] += solve_param(1.0, nullptr, zeros.data());
+    grad[1] += solve_param(1.0, dk_psill.data(), dki_psill.data());
+    grad[2] += solve_param(0.0, dk_range.data(), dki_range.data());
+  }
+  *ll_out = loglik;
+  for (int q = 0; q < 3; ++q) grad_out[q] = grad[q];
+  return OR_OK;
+}
+
+// optim.rs:125-182 helpers and the BFGS inverse-Hessian update.
+double dot_(const std::vector<double>& a, const std::vector<double>& b) {
+  double s = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+std::vector<double> identity_flat(size_t n) {
+  std::vector<double> m(n * n, 0.0);
+  for (size_t i = 0; i < n * n; ++i) m[i] = (i % (n + 1) == 0) ? 1.0 : 0.0;
+  return m;
+}
+std::vector<double> neg_mat_vec(const std::vector<double>& h, const std::vector<double>& v, size_t n) {
+  std::vector<double> out(n);
+  for (size_t i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (size_t j = 0; j < n; ++j) s += h[i * n + j] * v[j];
+    out[i] = -s;
+  }
+  return out;
+}
+std::vector<double> outer_(const std::vector<double>& u, const std::vector<double>& v, size_t n) {
+  std::vector<double> m(n * n, 0.0);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j < n; ++j) m[i * n + j] = u[i] * v[j];
+  return m;
+}
+std::vector<double> mat_mat(const std::vector<double>& a, const std::vector<double>& b, size_t n) {
+  std::vector<double> c(n * n, 0.0);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (size_t k = 0; k < n; ++k) s += a[i * n + k] * b[k * n + j];
+      c[i * n + j] = s;
+    }
+  return c;
+}
+std::vector<double> bfgs_update(const std::vector<double>& h, const std::vector<double>& s,
+                                const std::vector<double>& y, double sy, size_t n) {
+  double rho = 1.0 / sy;
+  std::vector<double> left = identity_flat(n), right = identity_flat(n);
+  std::vector<double> syt = outer_(s, y, n), yst = outer_(y, s, n), sst = outer_(s, s, n);
+  for (size_t i = 0; i < n * n; ++i) left[i] -= rho * syt[i];
+  for (size_t i = 0; i < n * n; ++i) right[i] -= rho * yst[i];
+  std::vector<double> h_new = mat_mat(mat_mat(left, h, n), right, n);
+  for (size_t i = 0; i < n * n; ++i) h_new[i] += rho * sst[i];
+  return h_new;
+}
+
+// optim.rs:207-275 bfgs.
+template <class F, class G>
+std::pair<std::vector<double>, double> bfgs(F&& f, G&& grad, const std::vector<double>& x0,
+                                            size_t max_iter) {
+  size_t n = x0.size();
+  std::vector<double> x = x0;
+  std::vector<double> h = identity_flat(n);
+  std::vector<double> g = grad(x);
+  double fx = f(x);
+  std::vector<double> best_x = x;
+  double best_fx = fx;
+  for (size_t it = 0; it < max_iter; ++it) {
+    double gnorm = std::sqrt(dot_(g, g));
+    if (gnorm < 1e-10) break;
+    std::vector<double> p = neg_mat_vec(h, g, n);
+    double slope = dot_(g, p);
+    if (slope >= 0.0) {
+      h = identity_flat(n);
+      for (size_t i = 0; i < n; ++i) p[i] = -g[i];
+      slope = dot_(g, p);
+    }
+    const double c1 = 1e-4;
+    double alpha = 1.0;
+    std::vector<double> x_new(n);
+    double f_new;
+    while (true) {
+      for (size_t i = 0; i < n; ++i) x_new[i] = x[i] + alpha * p[i];
+      double f_cand = f(x_new);
+      if (f_cand <= fx + c1 * alpha * slope || alpha < 1e-12) {
+        f_new = f_cand;
+        break;
+      }
+      alpha *= 0.5;
+    }
+    std::vector<double> g_new = grad(x_new);
+    std::vector<double> sv(n), yv(n);
+    for (size_t i = 0; i < n; ++i) sv[i] = x_new[i] - x[i];
+    for (size_t i = 0; i < n; ++i) yv[i] = g_new[i] - g[i];
+    double sy = dot_(sv, yv);
+    if (sy > 1e-10) h = bfgs_update(h, sv, yv, sy, n);
+    bool stalled = std::fabs(fx - f_new) <= 1e-13 * (1.0 + std::fabs(fx)) &&
+                   std::sqrt(dot_(sv, sv)) <= 1e-10 * (1.0 + std::sqrt(dot_(x, x)));
+    x = x_new;
+    g = g_new;
+    fx = f_new;
+    if (fx < best_fx) {
+      best_fx = fx;
+      best_x = x;
+    }
+    if (stalled) break;
+  }
+  return {best_x, best_fx};
+}
+
+// optim.rs:281-289 bfgs_multistart.
+template <class F, class G>
+std::pair<std::vector<double>, double> bfgs_multistart(F&& f, G&& grad,
+                                                       const std::vector<std::vector<double>>& starts,
+                                                       size_t max_iter) {
+  bool have = false;
+  std::pair<std::vector<double>, double> best;
+  for (const auto& x0 : starts) {
+    auto r = bfgs(f, grad, x0, max_iter);
+    if (!have || r.second < best.second) {
+      best = r;
+      have = true;
+    }
+  }
+  return best;
+}
+
+// vecchia.rs:1039-1061 objective_grad of mle_fit_with_plan.
+std::vector<double> mle_objective_grad(const double* coords, const double* values, size_t n,
+                                       int dim, int kind, const Plan& plan, double range_max,
+                                       const std::vector<double>& x) {
+  double nugget = x[0] * x[0];
+  double psill = std::exp(x[1]);
+  double range = std::exp(x[2]);
+  double ll, g[3];
+  if (loglik_grad(coords, values, n, dim, kind, nugget, psill, range, plan, &ll, g) != OR_OK)
+    return {0.0, 0.0, 0.0};
+  std::vector<double> gx = {-g[0] * 2.0 * x[0], -g[1] * psill, -g[2] * range};
+  if (range > range_max) {
+    double dreg_drange = 2.0 * (range - range_max) / (range_max * range_max);
+    gx[2] += 1e6 * dreg_drange * range;
+  }
+  return gx;
+}
+
 void test_field_2d(size_t n, uint64_t seed, double* coords, double* values) {
   Rng rng(seed);
   for (size_t i = 0; i < n; ++i) {
@@ -1801,6 +2100,62 @@ int or_vecchia_mle_nm(int dim, int64_t n, const double* coords, const double* va
   for (int i = 0; i < 3; ++i) x_out[i] = r.first[i];
   *f_out = r.second;
   if (n_evals) *n_evals = evals;
+  return OR_OK;
+}
+
+int or_g_and_dg(int32_t kind, double d, double* g, double* dg) {
+  return g_and_dg(kind, d, g, dg) ? OR_OK : OR_INVALID_PARAMETER;
+}
+
+int or_vecchia_loglik_grad(int dim, int64_t n, const double* coords, const double* values,
+                           int32_t kind, double nugget, double psill, double range, int64_t m,
+                           const int64_t* order, const int64_t* nb, const int32_t* nb_count,
+                           double* ll, double* grad3) {
+  Plan plan;
+  plan_from_arrays((size_t)n, (size_t)m, order, nb, nb_count, plan);
+  return loglik_grad(coords, values, (size_t)n, dim, kind, nugget, psill, range, plan, ll, grad3);
+}
+
+int or_vecchia_mle_bfgs(int dim, int64_t n, const double* coords, const double* values,
+                        int32_t kind, int64_t m, const int64_t* order_in, int64_t max_iter,
+                        double* x_out, double* f_out, int64_t* n_evals) {
+  Plan plan;
+  int rc = vecchia_plan(coords, (size_t)n, dim, (size_t)m, order_in, plan);
+  if (rc) return rc;
+  double s9[9], range_max;
+  mle_setup(coords, values, (size_t)n, dim, s9, &range_max);
+  int64_t evals = 0;
+  auto f = [&](const std::vector<double>& x) {
+    ++evals;
+    return mle_objective(coords, values, (size_t)n, dim, kind, 0.0, plan, range_max, x.data());
+  };
+  auto g = [&](const std::vector<double>& x) {
+    ++evals;
+    return mle_objective_grad(coords, values, (size_t)n, dim, kind, plan, range_max, x);
+  };
+  std::vector<std::vector<double>> st;
+  for (int i = 0; i < 3; ++i) st.push_back({s9[i * 3], s9[i * 3 + 1], s9[i * 3 + 2]});
+  auto r = bfgs_multistart(f, g, st, (size_t)max_iter);
+  for (int i = 0; i < 3; ++i) x_out[i] = r.first[i];
+  *f_out = r.second;
+  if (n_evals) *n_evals = evals;
+  if (r.second >= 1e12) return fail(OR_SINGULAR_SYSTEM, "Vecchia MLE did not converge");
+  return OR_OK;
+}
+
+int or_bfgs_multistart(or_objective_fn f, or_gradient_fn g, void* ctx, int64_t n, int64_t nstarts,
+                       const double* starts, int64_t max_iter, double* x_out, double* f_out) {
+  std::vector<std::vector<double>> st;
+  for (int64_t i = 0; i < nstarts; ++i) st.push_back(std::vector<double>(starts + i * n, starts + (i + 1) * n));
+  auto obj = [&](const std::vector<double>& x) { return f(x.data(), n, ctx); };
+  auto grad = [&](const std::vector<double>& x) {
+    std::vector<double> out(n);
+    g(x.data(), n, out.data(), ctx);
+    return out;
+  };
+  auto r = bfgs_multistart(obj, grad, st, (size_t)max_iter);
+  for (int64_t i = 0; i < n; ++i) x_out[i] = r.first[i];
+  *f_out = r.second;
   return OR_OK;
 }
 

@@ -154,6 +154,21 @@ int or_vecchia_mle_nm(int dim, int64_t n, const double* coords, const double* va
 
 /* optim.rs nelder_mead_multistart over a C callback (for driver parity). */
 typedef double (*or_objective_fn)(const double* x, int64_t n, void* ctx);
+/* vecchia.rs:353-389 g_and_dg; vecchia.rs:428-530 loglik_grad_inner on a plan
+ * given as arrays; vecchia.rs:1018-1061 + optim.rs:207-289: the BFGS path of
+ * mle_fit_with_plan (three reference starts, max_iter iterations). */
+int or_g_and_dg(int32_t kind, double d, double* g, double* dg);
+int or_vecchia_loglik_grad(int dim, int64_t n, const double* coords, const double* values,
+                           int32_t kind, double nugget, double psill, double range, int64_t m,
+                           const int64_t* order, const int64_t* nb, const int32_t* nb_count,
+                           double* ll, double* grad3);
+int or_vecchia_mle_bfgs(int dim, int64_t n, const double* coords, const double* values,
+                        int32_t kind, int64_t m, const int64_t* order_in, int64_t max_iter,
+                        double* x_out, double* f_out, int64_t* n_evals);
+/* optim.rs:281-289 bfgs_multistart over host callbacks. */
+typedef void (*or_gradient_fn)(const double* x, int64_t n, double* g, void* ctx);
+int or_bfgs_multistart(or_objective_fn f, or_gradient_fn g, void* ctx, int64_t n, int64_t nstarts,
+                       const double* starts, int64_t max_iter, double* x_out, double* f_out);
 int or_nelder_mead_multistart(or_objective_fn f, void* ctx, int64_t n, int64_t nstarts,
                               const double* starts, double step, int64_t max_iter, double* x_out,
                               double* f_out);

@@ -68,6 +68,7 @@ def build(quiet: bool = True) -> str:
 
 _lib = None
 _OBJ = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int64, C.c_void_p)
+_GRAD = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double), C.c_void_p)
 
 
 def lib():
@@ -115,6 +116,12 @@ def _declare(L):
         "or_vecchia_mle_nm": (C.c_int, [C.c_int, i64, pd, pd, i32, d, i64, pi64, i64, pd, d, i64,
                                         pd, pd, pi64]),
         "or_nelder_mead_multistart": (C.c_int, [_OBJ, vp, i64, i64, pd, d, i64, pd, pd]),
+        "or_g_and_dg": (C.c_int, [i32, d, pd, pd]),
+        "or_vecchia_loglik_grad": (C.c_int, [C.c_int, i64, pd, pd, i32, d, d, d, i64, pi64, pi64,
+                                             pi32, pd, pd]),
+        "or_vecchia_mle_bfgs": (C.c_int, [C.c_int, i64, pd, pd, i32, i64, pi64, i64, pd, pd,
+                                          pi64]),
+        "or_bfgs_multistart": (C.c_int, [_OBJ, _GRAD, vp, i64, i64, pd, i64, pd, pd]),
         "or_rng_u64": (None, [u64, i64, C.POINTER(C.c_uint64)]),
         "or_rng_uniform": (None, [u64, i64, pd]),
         "or_rng_normal": (None, [u64, i64, pd]),
@@ -421,6 +428,61 @@ def vecchia_mle_nm(coords, values, kind, m, starts, step=0.3, max_iter=2000, ord
         _p(o, C.c_int64) if o is not None else None, len(starts), _p(starts), C.c_double(step),
         int(max_iter), _p(x), C.byref(f), C.byref(ne)))
     return x, f.value, ne.value
+
+
+def g_and_dg(kind, d):
+    g, dg = C.c_double(), C.c_double()
+    rc = lib().or_g_and_dg(KINDS[kind] if isinstance(kind, str) else int(kind), C.c_double(d),
+                           C.byref(g), C.byref(dg))
+    return (g.value, dg.value) if rc == 0 else None
+
+
+def vecchia_loglik_grad(coords, values, kind, nugget, psill, rng, order, nb, cnt):
+    """loglik_grad_inner (vecchia.rs:428-530): (loglik, [d/dnugget, d/dpsill, d/drange])."""
+    coords, values = _f64(coords), _f64(values)
+    nb = np.ascontiguousarray(nb, dtype=np.int64)
+    ll = C.c_double()
+    g = np.zeros(3)
+    _check(lib().or_vecchia_loglik_grad(
+        coords.shape[1], len(coords), _p(coords), _p(values),
+        KINDS[kind] if isinstance(kind, str) else int(kind), C.c_double(nugget), C.c_double(psill),
+        C.c_double(rng), nb.shape[1] if nb.ndim == 2 else 1,
+        _p(np.ascontiguousarray(order, np.int64), C.c_int64), _p(nb, C.c_int64),
+        _p(np.ascontiguousarray(cnt, np.int32), C.c_int32), C.byref(ll), _p(g)))
+    return ll.value, g
+
+
+def vecchia_mle_bfgs(coords, values, kind, m, max_iter=200, order=None):
+    """The BFGS path of mle_fit_with_plan (vecchia.rs:1018-1078)."""
+    coords, values = _f64(coords), _f64(values)
+    x = np.zeros(3)
+    f = C.c_double()
+    ne = C.c_int64()
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    _check(lib().or_vecchia_mle_bfgs(
+        coords.shape[1], len(coords), _p(coords), _p(values),
+        KINDS[kind] if isinstance(kind, str) else int(kind), int(m),
+        _p(o, C.c_int64) if o is not None else None, int(max_iter), _p(x), C.byref(f),
+        C.byref(ne)))
+    return x, f.value, ne.value
+
+
+def bfgs_multistart(fn, grad, starts, max_iter):
+    starts = _f64(starts)
+    nstarts, n = starts.shape
+
+    def gcb(xp, nn, gp, ctx):
+        g = np.asarray(grad(np.ctypeslib.as_array(xp, shape=(nn,)).copy()), dtype=np.float64)
+        for i in range(nn):
+            gp[i] = float(g[i])
+
+    cf = _OBJ(lambda xp, nn, ctx: float(fn(np.ctypeslib.as_array(xp, shape=(nn,)).copy())))
+    cg = _GRAD(gcb)
+    x = np.zeros(n)
+    f = C.c_double()
+    _check(lib().or_bfgs_multistart(cf, cg, None, n, nstarts, _p(starts), int(max_iter), _p(x),
+                                    C.byref(f)))
+    return x, f.value
 
 
 def nelder_mead_multistart(fn, starts, step, max_iter):

@@ -420,3 +420,77 @@ def test_nelder_mead_rosenbrock_and_multistart():
     assert single > -2.5
     x, fx = O.nelder_mead_multistart(wells, [[-3.0], [3.0], [0.0]], 0.1, 500)
     assert abs(x[0] - 3.0) < 1e-2 and fx < -2.9
+
+
+# ------------------------------------------------ gradient / BFGS (a19, a21) --
+def test_g_and_dg_matches_finite_differences():
+    # vecchia.rs:2846-2875
+    h = 1e-6
+    unit = lambda kind: VariogramModel(0.0, [Structure(kind, 1.0, 1.0)])
+    for kind in ("spherical", "exponential", "gaussian", "matern15", "matern25"):
+        for d in (0.1, 0.3, 0.7, 1.5, 2.5):
+            g, dg = O.g_and_dg(kind, d)
+            gam = lambda x: O.gamma_dh(unit(kind), [x, 0.0])
+            assert abs(g - gam(d)) < 1e-12, (kind, d)
+            fd = (gam(d + h) - gam(d - h)) / (2 * h)
+            assert abs(dg - fd) < 1e-5, (kind, d, dg, fd)
+    for kind in ("circular", "hole", "wave"):
+        assert O.g_and_dg(kind, 0.5) is None
+
+
+def test_loglik_gradient_matches_finite_differences():
+    # vecchia.rs:2878-2935
+    c, v = O.test_field_2d(60, 11)
+    order, nb, cnt = O.vecchia_plan(c, 8)
+    for kind in ("spherical", "exponential", "gaussian", "matern15", "matern25"):
+        nug, ps, rg = 0.05, 0.9, 22.0
+        ll, g = O.vecchia_loglik_grad(c, v, kind, nug, ps, rg, order, nb, cnt)
+        at = lambda a, b, r: O.vecchia_loglik_plan(
+            c, v, VariogramModel(a, [Structure(kind, b, r)]), order, nb, cnt)
+        assert abs(ll - at(nug, ps, rg)) < 1e-9, kind
+        fd = [(at(nug * (1 + 1e-4), ps, rg) - at(nug * (1 - 1e-4), ps, rg)) / (2e-4 * nug),
+              (at(nug, ps * (1 + 1e-4), rg) - at(nug, ps * (1 - 1e-4), rg)) / (2e-4 * ps),
+              (at(nug, ps, rg * (1 + 1e-4)) - at(nug, ps, rg * (1 - 1e-4))) / (2e-4 * rg)]
+        for q in range(3):
+            assert abs(g[q] - fd[q]) < 1e-2 * max(abs(fd[q]), 1.0), (kind, q, g[q], fd[q])
+
+
+def test_gradient_is_zero_for_a_clamped_variance():
+    # vecchia.rs:2937-2990
+    c = np.array([[0.0, 0.0], [1e-13, 0.0]])
+    v = np.array([0.3, -0.7])
+    ll, g = O.vecchia_loglik_grad(c, v, "spherical", 0.0, 1.0, 10.0, [0, 1],
+                                  np.array([[-1], [0]]), np.array([0, 1]))
+    z0 = 0.5
+    assert abs(g[1] - (-0.5 / 1.0 + 0.5 * z0 * z0 / 1.0)) < 1e-9
+
+
+def test_bfgs_reference_known_answers():
+    # optim.rs tests: Rosenbrock, two-well multistart, quadratic
+    f = lambda x: (1 - x[0]) ** 2 + 100 * (x[1] - x[0] ** 2) ** 2
+    gr = lambda x: [-2 * (1 - x[0]) - 400 * x[0] * (x[1] - x[0] ** 2), 200 * (x[1] - x[0] ** 2)]
+    x, fx = O.bfgs_multistart(f, gr, [[-1.2, 1.0]], 200)
+    assert abs(x[0] - 1) < 1e-4 and abs(x[1] - 1) < 1e-4 and fx < 1e-8
+    w = lambda x: -2 * np.exp(-0.5 * (x[0] + 3) ** 2) - 3 * np.exp(-0.5 * (x[0] - 3) ** 2)
+    wg = lambda x: [2 * (x[0] + 3) * np.exp(-0.5 * (x[0] + 3) ** 2)
+                    + 3 * (x[0] - 3) * np.exp(-0.5 * (x[0] - 3) ** 2)]
+    _, single = O.bfgs_multistart(w, wg, [[-3.0]], 100)
+    assert single > -2.5
+    x, fx = O.bfgs_multistart(w, wg, [[-3.0], [3.0], [0.0]], 100)
+    assert abs(x[0] - 3) < 1e-3 and fx < -2.9
+    ctr = np.array([2.0, -1.0, 0.5])
+    x, fx = O.bfgs_multistart(lambda x: float(np.sum((x - ctr) ** 2)),
+                              lambda x: list(2 * (x - ctr)), [[0.0, 0.0, 0.0]], 100)
+    assert np.max(np.abs(x - ctr)) < 1e-6 and fx < 1e-10
+    # never worse than the best point visited (wrong-signed gradient)
+    x, fx = O.bfgs_multistart(lambda x: x[0] ** 2, lambda x: [-2 * x[0]], [[1.0]], 50)
+    assert fx <= 1.0 + 1e-13
+
+
+def test_vecchia_mle_bfgs_path_improves_on_the_starts():
+    c, v = O.test_field_2d(300, 21)
+    x, f, ne = O.vecchia_mle_bfgs(c, v, "exponential", 10)
+    starts, rmax = O.vecchia_mle_setup(c, v)
+    o, nb, cnt = O.vecchia_plan(c, 10)
+    f0 = O.vecchia_mle_objective(c, v, "exponential", 10, o, nb, cnt, rmax, starts)
+    assert f < np.min(f0) and np.isfinite(f) and ne > 3
