@@ -580,4 +580,132 @@ std::pair<std::vector<double>, double> multistart_best(const std::vector<NelderM
   return best;
 }
 
+
+// ------------------------------------------------------------------ BFGS --
+namespace {
+double dotv(const std::vector<double>& a, const std::vector<double>& b) {
+  double s = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+std::vector<double> eye(size_t n) {
+  std::vector<double> m(n * n, 0.0);
+  for (size_t i = 0; i < n * n; ++i) m[i] = (i % (n + 1) == 0) ? 1.0 : 0.0;
+  return m;
+}
+std::vector<double> matmul(const std::vector<double>& a, const std::vector<double>& b, size_t n) {
+  std::vector<double> c(n * n, 0.0);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (size_t k = 0; k < n; ++k) s += a[i * n + k] * b[k * n + j];
+      c[i * n + j] = s;
+    }
+  return c;
+}
+// Nocedal & Wright eq. 6.17 in the operation order of optim.rs:166-182.
+std::vector<double> inv_hessian_update(const std::vector<double>& h, const std::vector<double>& s,
+                                       const std::vector<double>& y, double sy, size_t n) {
+  const double rho = 1.0 / sy;
+  std::vector<double> left = eye(n), right = eye(n);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j < n; ++j) {
+      left[i * n + j] -= rho * (s[i] * y[j]);
+      right[i * n + j] -= rho * (y[i] * s[j]);
+    }
+  std::vector<double> out = matmul(matmul(left, h, n), right, n);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t j = 0; j < n; ++j) out[i * n + j] += rho * (s[i] * s[j]);
+  return out;
+}
+}  // namespace
+
+Bfgs::Bfgs(const std::vector<double>& x0, int64_t max_iter)
+    : n_(x0.size()), max_iter_(max_iter), x_(x0), h_(eye(x0.size())), req_(x0), best_x_(x0) {}
+
+void Bfgs::begin_iteration() {
+  if (it_ >= max_iter_ || std::sqrt(dotv(g_, g_)) < 1e-10) {
+    stage_ = kDone;
+    return;
+  }
+  p_.assign(n_, 0.0);
+  for (size_t i = 0; i < n_; ++i) {
+    double s = 0.0;
+    for (size_t j = 0; j < n_; ++j) s += h_[i * n_ + j] * g_[j];
+    p_[i] = -s;
+  }
+  slope_ = dotv(g_, p_);
+  if (slope_ >= 0.0) {
+    h_ = eye(n_);
+    for (size_t i = 0; i < n_; ++i) p_[i] = -g_[i];
+    slope_ = dotv(g_, p_);
+  }
+  alpha_ = 1.0;
+  req_.assign(n_, 0.0);
+  for (size_t i = 0; i < n_; ++i) req_[i] = x_[i] + alpha_ * p_[i];
+  stage_ = kSearch;
+}
+
+void Bfgs::supply_g(const std::vector<double>& g) {
+  if (stage_ == kInitG) {
+    g_ = g;
+    stage_ = kInitF;  // the objective at the same point comes next
+    return;
+  }
+  if (stage_ != kGnew) return;
+  std::vector<double> sv(n_), yv(n_);
+  for (size_t i = 0; i < n_; ++i) sv[i] = xnew_[i] - x_[i];
+  for (size_t i = 0; i < n_; ++i) yv[i] = g[i] - g_[i];
+  const double sy = dotv(sv, yv);
+  if (sy > 1e-10) h_ = inv_hessian_update(h_, sv, yv, sy, n_);
+  const bool stalled = std::fabs(fx_ - fnew_) <= 1e-13 * (1.0 + std::fabs(fx_)) &&
+                       std::sqrt(dotv(sv, sv)) <= 1e-10 * (1.0 + std::sqrt(dotv(x_, x_)));
+  x_ = xnew_;
+  g_ = g;
+  fx_ = fnew_;
+  if (fx_ < best_f_) {
+    best_f_ = fx_;
+    best_x_ = x_;
+  }
+  ++it_;
+  if (stalled) {
+    stage_ = kDone;
+    return;
+  }
+  begin_iteration();
+}
+
+void Bfgs::supply_f(double f) {
+  if (stage_ == kInitF) {
+    fx_ = f;
+    best_f_ = f;
+    best_x_ = x_;
+    begin_iteration();
+    return;
+  }
+  if (stage_ != kSearch) return;
+  const double c1 = 1e-4;
+  if (f <= fx_ + c1 * alpha_ * slope_ || alpha_ < 1e-12) {
+    xnew_ = req_;
+    fnew_ = f;
+    stage_ = kGnew;  // gradient at the accepted point
+    return;
+  }
+  alpha_ *= 0.5;
+  for (size_t i = 0; i < n_; ++i) req_[i] = x_[i] + alpha_ * p_[i];
+}
+
+std::pair<std::vector<double>, double> bfgs_multistart_best(const std::vector<Bfgs>& runs) {
+  bool have = false;
+  std::pair<std::vector<double>, double> best;
+  for (const auto& r : runs) {
+    auto b = r.best();
+    if (!have || b.second < best.second) {
+      best = b;
+      have = true;
+    }
+  }
+  return best;
+}
+
 }  // namespace gs

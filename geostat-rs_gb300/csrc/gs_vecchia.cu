@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
 // whose element e lives at S[e * T] (one slab per thread, interleaved): the
 // unpivoted factor with the reference's failure test !(d > 1e-12 max diag),
 // then the forward and back substitutions of W in place.
-__device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
+__device__ bool chol_factor_strided(double* S, int s, int64_t T) {
   double scale = 0.0;
   for (int q = 0; q < s; ++q) scale = fmax(scale, S[(int64_t)(q * s + q) * T]);
   scale = fmax(scale, 2.2250738585072014e-308);
@@ -433,6 +433,10 @@ __device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
       S[(int64_t)(r * s + kk) * T] = acc / d;
     }
   }
+  return true;
+}
+// cholesky_forward_solve + cholesky_back_solve (linalg.rs:160-180) of W in place.
+__device__ void chol_subst_strided(const double* S, double* W, int s, int64_t T) {
   for (int r = 0; r < s; ++r) {
     double acc = W[(int64_t)r * T];
     for (int j = 0; j < r; ++j) acc -= S[(int64_t)(r * s + j) * T] * W[(int64_t)j * T];
@@ -443,6 +447,10 @@ __device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
     for (int j = r + 1; j < s; ++j) acc -= S[(int64_t)(j * s + r) * T] * W[(int64_t)j * T];
     W[(int64_t)r * T] = acc / S[(int64_t)(r * s + r) * T];
   }
+}
+__device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
+  if (!chol_factor_strided(S, s, T)) return false;
+  chol_subst_strided(S, W, s, T);
   return true;
 }
 
@@ -688,6 +696,562 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     } else {
       ll[c] = hll[c];
     }
+  }
+  return GS_OK;
+}
+
+// ---------------------------------------------- log-likelihood gradient --
+// loglik_grad_inner (vecchia.rs:428-530) for single-structure isotropic
+// models of the closed-form kinds (g_and_dg, vecchia.rs:353-389): the
+// log-likelihood and its derivatives in (nugget, psill, range), per point
+// and candidate, reduced per candidate in the same fixed order as the
+// log-likelihood.  With w = K^{-1} k the derivative of each conditional
+// follows from dw = K^{-1} (dk - dK w) on the same factorisation.
+namespace {
+
+// rho = 1 - g and dg/dd at d (df), branch free.
+__device__ __forceinline__ void rho_dg_df(int kind, df d, const ExpTable& tab, const DfConsts& k,
+                                          df& rho, df& dg) {
+  switch (kind) {
+    case GS_KIND_SPHERICAL: {
+      const bool inside = !(d.hi > 1.0f || (d.hi == 1.0f && d.lo >= 0.0f));
+      rho = rho_sph_df(d);
+      // 1.5 (1 - d^2); scaling by 1.5 is not exact in FP32, so it goes through df_mul_f
+      const df v = df_mul_f(df_add_f(df_neg(df_sqr(d)), 1.0f), 1.5f);
+      dg = inside ? v : df_make(0.0f, 0.0f);
+      break;
+    }
+    case GS_KIND_EXPONENTIAL:
+      rho = df_expneg(d, tab, k);
+      dg = rho;
+      break;
+    case GS_KIND_GAUSSIAN: {
+      rho = df_expneg(df_sqr(d), tab, k);
+      const df twod = df_make(2.0f * d.hi, 2.0f * d.lo);
+      dg = df_mul(twod, rho);
+      break;
+    }
+    case GS_KIND_MATERN15: {
+      const df sq = df_mul(d, df_make(k.s3h, k.s3l));
+      const df e = df_expneg(sq, tab, k);
+      rho = df_mul(df_add_f(sq, 1.0f), e);
+      dg = df_mul(df_mul_f(d, 3.0f), e);
+      break;
+    }
+    default: {  // GS_KIND_MATERN25: dg = 5 d (1 + s) / 3 e
+      const df sq = df_mul(d, df_make(k.s5h, k.s5l));
+      const df e = df_expneg(sq, tab, k);
+      rho = rho_mat25_df(d, tab, k);
+      const df num = df_mul(df_mul_f(d, 5.0f), df_add_f(sq, 1.0f));
+      const float q = num.hi * (1.0f / 3.0f);
+      const df q3 = two_prod(q, 3.0f);
+      const float rq = (num.hi - q3.hi - q3.lo + num.lo) * (1.0f / 3.0f);
+      dg = df_mul(fast_two_sum(q, rq), e);
+      break;
+    }
+  }
+}
+
+// Per-warp shared-memory layout of vecchia_grad_kernel.
+struct VGLayout {
+  size_t off_a, off_dp, off_dr, off_h, off_v, off_h0, off_z, off_b, off_bp, off_br, off_wv, off_rhs,
+      off_row, off_vec, off_xd, total;
+};
+
+__host__ __device__ inline VGLayout vecchia_grad_layout(int m, int dim) {
+  VGLayout L;
+  const int np = m * (m + 1) / 2;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = o;
+    o += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  L.off_a = take((size_t)np * sizeof(df));
+  L.off_dp = take((size_t)np * sizeof(df));
+  L.off_dr = take((size_t)np * sizeof(df));
+  L.off_h = take((size_t)np * sizeof(df));
+  L.off_v = take((size_t)dim * m * sizeof(df));
+  L.off_h0 = take((size_t)m * sizeof(df));
+  L.off_z = take((size_t)m * sizeof(df));
+  L.off_b = take((size_t)m * sizeof(df));
+  L.off_bp = take((size_t)m * sizeof(df));
+  L.off_br = take((size_t)m * sizeof(df));
+  L.off_wv = take((size_t)m * sizeof(df));
+  L.off_rhs = take((size_t)m * sizeof(df));
+  L.off_row = take(kWarpN * sizeof(float));
+  L.off_vec = take(kWarpN * sizeof(float));
+  L.off_xd = take(kWarpN * sizeof(df));
+  L.total = o;
+  return L;
+}
+
+// terms: (4 x ncand) x n -- log term, then d/dnugget, d/dpsill, d/drange.
+template <int D>
+__global__ void __launch_bounds__(32 * kVWarps) vecchia_grad_kernel(VArgs a, ExpTable tab_g,
+                                                                   DfConsts kc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ ExpTable tab;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tab.v[i] = tab_g.v[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int M = a.m;
+  const int64_t NC = (int64_t)a.ncand * a.n;
+  const VGLayout lay = vecchia_grad_layout(M, D);
+  unsigned char* base = smem_raw + (size_t)wib * lay.total;
+  df* A = reinterpret_cast<df*>(base + lay.off_a);
+  df* DP = reinterpret_cast<df*>(base + lay.off_dp);
+  df* DR = reinterpret_cast<df*>(base + lay.off_dr);
+  df* H = reinterpret_cast<df*>(base + lay.off_h);
+  df* V = reinterpret_cast<df*>(base + lay.off_v);
+  df* H0 = reinterpret_cast<df*>(base + lay.off_h0);
+  df* ZV = reinterpret_cast<df*>(base + lay.off_z);
+  df* B = reinterpret_cast<df*>(base + lay.off_b);
+  df* BP = reinterpret_cast<df*>(base + lay.off_bp);
+  df* BR = reinterpret_cast<df*>(base + lay.off_br);
+  df* WV = reinterpret_cast<df*>(base + lay.off_wv);
+  df* RHS = reinterpret_cast<df*>(base + lay.off_rhs);
+  WarpScratch W;
+  W.row = reinterpret_cast<float*>(base + lay.off_row);
+  W.vec = reinterpret_cast<float*>(base + lay.off_vec);
+  W.xd = reinterpret_cast<df*>(base + lay.off_xd);
+  const int64_t nwarps = (int64_t)gridDim.x * kVWarps;
+  for (int64_t k = (int64_t)blockIdx.x * kVWarps + wib; k < a.n; k += nwarps) {
+    const int64_t i = a.order[k];
+    const int s = a.cnt[k];
+    const df zi = df_sub(a.vdf[i], a.mean_df);
+    if (s == 0) {
+      // first point: N(0, sill); only nugget and psill move the sill
+      const double z = df_to_double(zi);
+      for (int c = lane; c < a.ncand; c += 32) {
+        const double var = a.models[c].c0;
+        const int64_t at = (int64_t)c * a.n + k;
+        a.terms[at] = -0.5 * (kLn2Pi + log(var) + z * z / var);
+        const double common = -0.5 / var + 0.5 * z * z / (var * var);
+        a.terms[NC + at] = common;
+        a.terms[2 * NC + at] = common;
+        a.terms[3 * NC + at] = 0.0;
+        a.flag[at] = 0;
+      }
+      continue;
+    }
+    __syncwarp();
+    if (lane < s) {
+      const int j = a.nb[k * (int64_t)M + lane];
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        V[d * M + lane] = df_sub(a.cdf[(int64_t)d * a.n + j], a.cdf[(int64_t)d * a.n + i]);
+      ZV[lane] = df_sub(a.vdf[j], a.mean_df);
+    }
+    __syncwarp();
+    if (lane < s) H0[lane] = norm_origin<D>(V, M, 0, lane);
+    for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+      const df h0 = norm_pair<D>(V, M, 0, i0, j0);
+      const df h1 = norm_pair<D>(V, M, 0, i1, j1);
+      H[pk(i0, j0)] = h0;
+      if (two) H[pk(i1, j1)] = h1;
+    });
+    __syncwarp();
+    for (int c = 0; c < a.ncand; ++c) {
+      const DevModel& mdl = a.models[c];
+      const DevStruct& st = mdl.s[0];
+      const int64_t at = (int64_t)c * a.n + k;
+      // covariances and their psill / range derivatives
+      auto entry = [&](df h, df& cv, df& dp, df& dr) {
+        const df d = df_mul(h, st.inv_range_df);
+        df rho, dg;
+        rho_dg_df(st.kind, d, tab, kc, rho, dg);
+        cv = df_mul(st.sill_df, rho);
+        dp = rho;
+        dr = df_mul(df_mul(st.sill_df, dg), df_mul(d, st.inv_range_df));
+      };
+      if (lane < s) {
+        entry(H0[lane], B[lane], BP[lane], BR[lane]);
+        A[pk(lane, lane)] = mdl.c0_df;
+        DP[pk(lane, lane)] = df_make(1.0f, 0.0f);
+        DR[pk(lane, lane)] = df_make(0.0f, 0.0f);
+      }
+      for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+        df c0, p0, r0;
+        entry(H[pk(i0, j0)], c0, p0, r0);
+        A[pk(i0, j0)] = c0;
+        DP[pk(i0, j0)] = p0;
+        DR[pk(i0, j0)] = r0;
+        if (two) {
+          df c1, p1, r1;
+          entry(H[pk(i1, j1)], c1, p1, r1);
+          A[pk(i1, j1)] = c1;
+          DP[pk(i1, j1)] = p1;
+          DR[pk(i1, j1)] = r1;
+        }
+      });
+      __syncwarp();
+      WarpFactor f;
+      bool ok = warp_factor(A, s, lane, f, W) && warp_refine(f, B, s, lane, W);
+      if (!ok) {
+        if (lane == 0) a.flag[at] = 1;
+        __syncwarp();
+        continue;
+      }
+      const df w = lane < s ? W.xd[lane] : df_make(0.0f, 0.0f);
+      if (lane < s) WV[lane] = w;
+      df mu = warp_sum_df(lane < s ? df_mul(w, ZV[lane]) : df_make(0.0f, 0.0f));
+      df red = warp_sum_df(lane < s ? df_mul(w, B[lane]) : df_make(0.0f, 0.0f));
+      const df rawv = df_sub(mdl.c0_df, red);
+      const double raw_var = df_to_double(rawv);
+      const double var = fmax(raw_var, 1e-12);
+      const bool clamped = raw_var <= 1e-12;
+      const double r = df_to_double(df_sub(zi, mu));
+      double g3[3];
+      for (int prm = 0; prm < 3 && ok; ++prm) {
+        __syncwarp();
+        // right-hand side: -w (nugget), dk - dK w (psill, range)
+        if (lane < s) {
+          df rhs = df_neg(w);
+          if (prm > 0) {
+            const df* DK = prm == 1 ? DP : DR;
+            df acc = prm == 1 ? BP[lane] : BR[lane];
+            for (int b = 0; b < s; ++b)
+              acc = df_sub(acc, df_mul(DK[lane >= b ? pk(lane, b) : pk(b, lane)], WV[b]));
+            rhs = acc;
+          }
+          RHS[lane] = rhs;
+        }
+        __syncwarp();
+        ok = warp_refine(f, RHS, s, lane, W);
+        if (!ok) break;
+        const df dw = lane < s ? W.xd[lane] : df_make(0.0f, 0.0f);
+        const df dmu = warp_sum_df(lane < s ? df_mul(dw, ZV[lane]) : df_make(0.0f, 0.0f));
+        df dred = lane < s ? df_mul(dw, B[lane]) : df_make(0.0f, 0.0f);
+        if (prm > 0 && lane < s) dred = df_add(dred, df_mul(w, prm == 1 ? BP[lane] : BR[lane]));
+        dred = warp_sum_df(dred);
+        const double dsill = prm < 2 ? 1.0 : 0.0;
+        const double dvar = clamped ? 0.0 : dsill - df_to_double(dred);
+        const double dm = df_to_double(dmu);
+        g3[prm] = -0.5 * dvar / var + r * dm / var + 0.5 * r * r / (var * var) * dvar;
+      }
+      if (!ok) {
+        if (lane == 0) a.flag[at] = 1;
+        __syncwarp();
+        continue;
+      }
+      if (lane == 0) {
+        a.terms[at] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+        a.terms[NC + at] = g3[0];
+        a.terms[2 * NC + at] = g3[1];
+        a.terms[3 * NC + at] = g3[2];
+        a.flag[at] = 0;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__device__ __forceinline__ void g_and_dg_fp64(int kind, double d, double& g, double& dg) {
+  switch (kind) {
+    case GS_KIND_SPHERICAL:
+      if (d >= 1.0) {
+        g = 1.0;
+        dg = 0.0;
+      } else {
+        g = 1.5 * d - 0.5 * d * d * d;
+        dg = 1.5 - 1.5 * d * d;
+      }
+      break;
+    case GS_KIND_EXPONENTIAL: {
+      const double e = exp(-d);
+      g = 1.0 - e;
+      dg = e;
+      break;
+    }
+    case GS_KIND_GAUSSIAN: {
+      const double e = exp(-(d * d));
+      g = 1.0 - e;
+      dg = 2.0 * d * e;
+      break;
+    }
+    case GS_KIND_MATERN15: {
+      const double sq = 1.7320508075688772 * d;
+      const double e = exp(-sq);
+      g = 1.0 - (1.0 + sq) * e;
+      dg = 3.0 * d * e;
+      break;
+    }
+    default: {
+      const double sq = 2.23606797749979 * d;
+      const double e = exp(-sq);
+      g = 1.0 - (1.0 + sq + sq * sq / 3.0) * e;
+      dg = 5.0 * d * (1.0 + sq) / 3.0 * e;
+      break;
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ double vg_dist(const VArgs& a, int64_t p, int64_t q) {
+  double s2 = 0.0;
+  const double* c[3] = {a.x, a.y, a.z};
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double v = c[d][p] - c[d][q];
+    s2 += v * v;
+  }
+  return sqrt(s2);
+}
+
+// One thread per flagged (candidate, point): loglik_grad_inner's per-point
+// body in FP64 (vecchia.rs:463-527).  Scratch per thread: K (s x s), then
+// k, dk_psill, dk_range, w, dw.
+template <int D>
+__global__ void vecchia_grad_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
+                                         double* scratch, int64_t T, int32_t* cand_status) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (tid >= T) return;
+  const int M = a.m;
+  const int64_t NC = (int64_t)a.ncand * a.n;
+  double* S = scratch + tid;
+  double* KI = scratch + (int64_t)M * M * T + tid;
+  double* KP = KI + (int64_t)M * T;
+  double* KR = KP + (int64_t)M * T;
+  double* Wv = KR + (int64_t)M * T;
+  double* DW = Wv + (int64_t)M * T;
+  for (int64_t it = tid; it < nlist; it += T) {
+    const int64_t code = list ? list[it] : it;
+    const int c = (int)(code / a.n);
+    const int64_t k = code % a.n;
+    const DevModel& mdl = a.models[c];
+    const int kind = mdl.s[0].kind;
+    const double psill = mdl.s[0].sill, nugget = mdl.nugget, sill = mdl.c0;
+    const double range = 1.0 / mdl.s[0].inv_range;
+    const int64_t i = a.order[k];
+    const int s = a.cnt[k];
+    const double zi = a.v[i] - a.mean;
+    if (s == 0) {
+      a.terms[code] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
+      const double common = -0.5 / sill + 0.5 * zi * zi / (sill * sill);
+      a.terms[NC + code] = common;
+      a.terms[2 * NC + code] = common;
+      a.terms[3 * NC + code] = 0.0;
+      continue;
+    }
+    const int32_t* nbk = a.nb + k * (int64_t)M;
+    for (int p = 0; p < s; ++p) {
+      const double h = vg_dist<D>(a, i, nbk[p]);
+      double g, dg;
+      g_and_dg_fp64(kind, h / range, g, dg);
+      KI[(int64_t)p * T] = sill - (nugget + psill * g);
+      KP[(int64_t)p * T] = 1.0 - g;
+      KR[(int64_t)p * T] = psill * dg * h / (range * range);
+      S[(int64_t)(p * s + p) * T] = sill;
+      for (int q = p + 1; q < s; ++q) {
+        const double hq = vg_dist<D>(a, nbk[p], nbk[q]);
+        double gq, dgq;
+        g_and_dg_fp64(kind, hq / range, gq, dgq);
+        const double cv = sill - (nugget + psill * gq);
+        S[(int64_t)(p * s + q) * T] = cv;
+        S[(int64_t)(q * s + p) * T] = cv;
+      }
+    }
+    if (!chol_factor_strided(S, s, T)) {
+      atomicExch(&cand_status[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
+      for (int q = 0; q < 4; ++q) a.terms[q * NC + code] = __longlong_as_double(0x7ff8000000000000ll);
+      continue;
+    }
+    for (int p = 0; p < s; ++p) Wv[(int64_t)p * T] = KI[(int64_t)p * T];
+    chol_subst_strided(S, Wv, s, T);
+    double mu = 0.0, red = 0.0;
+    for (int p = 0; p < s; ++p) mu += Wv[(int64_t)p * T] * (a.v[nbk[p]] - a.mean);
+    for (int p = 0; p < s; ++p) red += Wv[(int64_t)p * T] * KI[(int64_t)p * T];
+    const double raw_var = sill - red;
+    const double var = fmax(raw_var, 1e-12);
+    const bool clamped = raw_var <= 1e-12;
+    const double r = zi - mu;
+    a.terms[code] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+    for (int prm = 0; prm < 3; ++prm) {
+      // rhs = dk - dK w (dK rebuilt from the distances), or -w for the nugget
+      for (int p = 0; p < s; ++p) {
+        double rhs;
+        if (prm == 0) {
+          rhs = -Wv[(int64_t)p * T];
+        } else {
+          double acc = 0.0;
+          for (int q = 0; q < s; ++q) {
+            double dk;
+            if (q == p) {
+              dk = prm == 1 ? 1.0 : 0.0;
+            } else {
+              const double hq = vg_dist<D>(a, nbk[p], nbk[q]);
+              double gq, dgq;
+              g_and_dg_fp64(kind, hq / range, gq, dgq);
+              dk = prm == 1 ? 1.0 - gq : psill * dgq * hq / (range * range);
+            }
+            acc += dk * Wv[(int64_t)q * T];
+          }
+          rhs = (prm == 1 ? KP[(int64_t)p * T] : KR[(int64_t)p * T]) - acc;
+        }
+        DW[(int64_t)p * T] = rhs;
+      }
+      chol_subst_strided(S, DW, s, T);
+      double dmu = 0.0, d1 = 0.0, d2 = 0.0;
+      for (int p = 0; p < s; ++p) dmu += DW[(int64_t)p * T] * (a.v[nbk[p]] - a.mean);
+      for (int p = 0; p < s; ++p) d1 += DW[(int64_t)p * T] * KI[(int64_t)p * T];
+      if (prm > 0)
+        for (int p = 0; p < s; ++p)
+          d2 += Wv[(int64_t)p * T] * (prm == 1 ? KP[(int64_t)p * T] : KR[(int64_t)p * T]);
+      const double dsill = prm < 2 ? 1.0 : 0.0;
+      const double dvar = clamped ? 0.0 : dsill - (d1 + d2);
+      a.terms[(1 + prm) * NC + code] =
+          -0.5 * dvar / var + r * dmu / var + 0.5 * r * r / (var * var) * dvar;
+    }
+  }
+}
+
+}  // namespace
+
+// Single-structure isotropic models of the closed-form kinds only.
+int reject_grad_model(const gs_model& m, int dim) {
+  GS_TRY(reject_vecchia_model(m, dim));
+  if (m.n_structures != 1 || m.s[0].has_anis)
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "the log-likelihood gradient needs a single isotropic structure");
+  const int k = m.s[0].kind;
+  if (k != GS_KIND_SPHERICAL && k != GS_KIND_EXPONENTIAL && k != GS_KIND_GAUSSIAN &&
+      k != GS_KIND_MATERN15 && k != GS_KIND_MATERN25)
+    return fail(GS_ERR_INVALID_PARAMETER, "no closed-form range derivative for this kind");
+  return GS_OK;
+}
+
+// Log-likelihood and gradient of ncand candidates on a plan.
+int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
+                      double* grad, int32_t* status, int precision, cudaStream_t s) {
+  const gs_pointset* ps = P->ps;
+  const int dim = ps->dim;
+  const int64_t n = P->n;
+  const int M = (int)P->m;
+  if (!g_vready) {
+    df_consts_host(&g_vtab, &g_vkc);
+    g_vready = true;
+  }
+  std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
+  for (int64_t c = 0; c < ncand; ++c) {
+    status[c] = GS_OK;
+    ll[c] = NAN;
+    for (int q = 0; q < 3; ++q) grad[c * 3 + q] = NAN;
+    int rc = reject_grad_model(models[c], dim);
+    if (!rc) rc = make_dev_model(models[c], dim, &dms[c], true);
+    if (rc) {
+      // a harmless stand-in the kernels can evaluate; its results are dropped
+      status[c] = rc;
+      gs_model stand{};
+      stand.nugget = 0.1;
+      stand.n_structures = 1;
+      stand.s[0].kind = GS_KIND_EXPONENTIAL;
+      stand.s[0].sill = 1.0;
+      stand.s[0].range = 1.0;
+      make_dev_model(stand, dim, &dms[c], true);
+    }
+  }
+  if (ncand == 0) return GS_OK;
+  const int64_t NC = ncand * n;
+  DevBuf dmod, terms, flag, partial, out, cstat, list;
+  GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
+  GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
+  GS_TRY(terms.alloc((size_t)4 * NC * 8, s));
+  GS_TRY(flag.alloc((size_t)NC, s));
+  GS_TRY(cstat.alloc((size_t)ncand * 4, s));
+  GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
+  VArgs a{};
+  a.dim = dim;
+  a.n = n;
+  a.m = M;
+  a.ncand = (int)ncand;
+  a.iso_shared = 1;
+  a.x = ps->d_x;
+  a.y = ps->d_y;
+  a.z = ps->d_z;
+  a.v = ps->d_v;
+  a.mean = P->mean;
+  a.cdf = (const df*)ps->d_cdf;
+  a.vdf = (const df*)ps->d_vdf;
+  a.mean_df = df_from_double(P->mean);
+  a.order = P->d_order;
+  a.nb = P->d_nb;
+  a.cnt = P->d_cnt;
+  a.models = (const DevModel*)dmod.ptr;
+  a.terms = (double*)terms.ptr;
+  a.flag = (uint8_t*)flag.ptr;
+  int64_t nfl = 0;
+  const bool mixed = precision != GS_PREC_FP64 && M <= kWarpN;
+  if (mixed) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t smem = vecchia_grad_layout(std::max(M, 1), dim).total * kVWarps;
+    auto kern = dim == 2 ? vecchia_grad_kernel<2> : vecchia_grad_kernel<3>;
+    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kVWarps, smem));
+    per_sm = std::max(per_sm, 1);
+    const int blocks = (int)std::min<int64_t>((n + kVWarps - 1) / kVWarps, (int64_t)sms * per_sm);
+    kern<<<blocks, 32 * kVWarps, smem, s>>>(a, g_vtab, g_vkc);
+    GS_CUDA(cudaGetLastError());
+    count_launch(1);
+    DevBuf nsel, tmp;
+    GS_TRY(nsel.alloc(8, s));
+    GS_TRY(list.alloc((size_t)NC * 8, s));
+    size_t tb = 0;
+    GS_CUDA(cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<int64_t>(0),
+                                       (uint8_t*)flag.ptr, (int64_t*)list.ptr, (int64_t*)nsel.ptr,
+                                       NC, s));
+    GS_TRY(tmp.alloc(tb, s));
+    GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, tb, thrust::counting_iterator<int64_t>(0),
+                                       (uint8_t*)flag.ptr, (int64_t*)list.ptr, (int64_t*)nsel.ptr,
+                                       NC, s));
+    GS_CUDA(cudaMemcpyAsync(&nfl, nsel.ptr, 8, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaStreamSynchronize(s));
+  }
+  if (!mixed || nfl > 0) {
+    const int64_t work = mixed ? nfl : NC;
+    const int64_t per = ((int64_t)M * M + 5 * (int64_t)M) * 8;
+    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 1024);
+    T = std::min<int64_t>(T, ((work + 127) / 128) * 128);
+    T = std::max<int64_t>(T, 128);
+    DevBuf scratch;
+    GS_TRY(scratch.alloc((size_t)T * per, s));
+    const int blocks = (int)((T + 127) / 128);
+    if (dim == 2)
+      vecchia_grad_fp64_kernel<2><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
+                                                         work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
+    else
+      vecchia_grad_fp64_kernel<3><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
+                                                         work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
+    GS_CUDA(cudaGetLastError());
+    count_launch(1);
+  }
+  const int64_t chunk = 8192;
+  const int nblk = (int)((n + chunk - 1) / chunk);
+  GS_TRY(partial.alloc((size_t)nblk * 4 * ncand * 8, s));
+  GS_TRY(out.alloc((size_t)4 * ncand * 8, s));
+  reduce_terms<<<dim3(nblk, (unsigned)(4 * ncand)), 256, 0, s>>>((double*)terms.ptr, n, chunk,
+                                                                  (double*)partial.ptr);
+  reduce_partials<<<(int)((4 * ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk,
+                                                                 (int)(4 * ncand), (double*)out.ptr);
+  GS_CUDA(cudaGetLastError());
+  count_launch(2);
+  std::vector<double> hout(4 * ncand);
+  std::vector<int32_t> hst(ncand);
+  GS_CUDA(cudaMemcpyAsync(hout.data(), out.ptr, 4 * ncand * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hst.data(), cstat.ptr, ncand * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  for (int64_t c = 0; c < ncand; ++c) {
+    if (status[c] != GS_OK) continue;
+    if (hst[c] != GS_OK) {
+      status[c] = hst[c];
+      continue;
+    }
+    ll[c] = hout[c];
+    for (int q = 0; q < 3; ++q) grad[c * 3 + q] = hout[(1 + q) * ncand + c];
   }
   return GS_OK;
 }
@@ -1376,9 +1940,12 @@ int gs_vecchia_loglik(const gs_pointset* ps, const gs_model* model, int64_t m,
 
 // mle_fit_with_plan (vecchia.rs:952-1081) with every start's simplex
 // advanced in lock step so each round's evaluations form one batch.
-int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
-                   int64_t nstarts, const double* starts, double step, int64_t max_iter,
-                   gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals) {
+}  // extern "C"
+
+namespace gs {
+namespace {
+
+int check_fit_kind(const gs_pointset* ps, int32_t kind) {
   if (!ps) return fail(GS_ERR_INVALID_PARAMETER, "null point set");
   if (kind == GS_KIND_POWER)
     return fail(GS_ERR_INVALID_PARAMETER,
@@ -1388,18 +1955,25 @@ int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t
   if (kind < 0 || kind > GS_KIND_MATERN25)
     return fail(GS_ERR_INVALID_PARAMETER,
                 "the CUDA path fits spherical, exponential, gaussian, matern15 and matern25");
-  gs_vecchia_plan* P = nullptr;
-  GS_TRY(plan_create(ps, m, order, &P));
+  return GS_OK;
+}
+
+// Initial scales of mle_fit_with_plan (vecchia.rs:958-980): sample variance,
+// domain extent, range0 = extent / 3 and the range regulariser's bound.
+struct FitSetup {
+  double var0, range0, range_max;
+};
+
+FitSetup fit_setup(const gs_pointset* ps, double mean) {
   const int64_t n = ps->n;
   const int dim = ps->dim;
-  // initial scales (vecchia.rs:958-980)
-  double mean = P->mean;
   double sq = 0.0;
   for (int64_t i = 0; i < n; ++i) {
     double t = ps->values[i] - mean;
     sq += t * t;
   }
-  double var0 = std::fmax(sq / (double)n, 1e-12);
+  FitSetup f;
+  f.var0 = std::fmax(sq / (double)n, 1e-12);
   double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int64_t i = 0; i < n; ++i)
     for (int d = 0; d < dim; ++d) {
@@ -1412,21 +1986,160 @@ int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t
     e2 += t * t;
   }
   const double extent = std::sqrt(e2);
-  const double range0 = std::fmax(extent / 3.0, 1e-9);
-  const double range_max = 10.0 * extent;
+  f.range0 = std::fmax(extent / 3.0, 1e-9);
+  f.range_max = 10.0 * extent;
+  return f;
+}
+
+// x = (sqrt nugget, ln psill, ln range) -> a single-structure model.
+gs_model model_from_x(int32_t kind, const std::vector<double>& x) {
+  gs_model mdl;
+  std::memset(&mdl, 0, sizeof(mdl));
+  mdl.nugget = x[0] * x[0];
+  mdl.n_structures = 1;
+  mdl.s[0].kind = kind;
+  mdl.s[0].sill = std::exp(x[1]);
+  mdl.s[0].range = std::exp(x[2]);
+  mdl.s[0].ratio = mdl.s[0].ratio_z = 1.0;
+  return mdl;
+}
+
+double range_reg(double range, double range_max) {
+  if (range > range_max) {
+    double t = (range - range_max) / range_max;
+    return t * t;
+  }
+  return 0.0;
+}
+
+// The objective of mle_fit_with_plan (vecchia.rs:1001-1016) for a batch of
+// points: -loglik + 1e6 reg(range), 1e12 for a rejected candidate.
+int batch_objective(const gs_vecchia_plan* P, int32_t kind, double range_max,
+                    const std::vector<std::vector<double>>& xs, std::vector<double>& f) {
+  std::vector<gs_model> batch;
+  for (const auto& x : xs) batch.push_back(model_from_x(kind, x));
+  std::vector<double> ll(batch.size());
+  std::vector<int32_t> sts(batch.size());
+  GS_TRY(vecchia_eval(P, (int64_t)batch.size(), batch.data(), ll.data(), sts.data(), GS_PREC_MIXED,
+                      P->stream));
+  f.resize(batch.size());
+  for (size_t b = 0; b < batch.size(); ++b)
+    f[b] = (sts[b] == 0 && std::isfinite(ll[b]))
+               ? -ll[b] + 1e6 * range_reg(batch[b].s[0].range, range_max)
+               : 1e12;
+  return GS_OK;
+}
+
+// objective_grad of mle_fit_with_plan (vecchia.rs:1039-1061) for a batch.
+int batch_gradient(const gs_vecchia_plan* P, int32_t kind, double range_max,
+                   const std::vector<std::vector<double>>& xs, std::vector<std::vector<double>>& g) {
+  std::vector<gs_model> batch;
+  for (const auto& x : xs) batch.push_back(model_from_x(kind, x));
+  std::vector<double> ll(batch.size()), gr(3 * batch.size());
+  std::vector<int32_t> sts(batch.size());
+  GS_TRY(vecchia_eval_grad(P, (int64_t)batch.size(), batch.data(), ll.data(), gr.data(), sts.data(),
+                           GS_PREC_MIXED, P->stream));
+  g.assign(batch.size(), std::vector<double>(3, 0.0));
+  for (size_t b = 0; b < batch.size(); ++b) {
+    if (sts[b] != 0) continue;  // singular: no meaningful direction
+    const auto& x = xs[b];
+    const double psill = batch[b].s[0].sill, range = batch[b].s[0].range;
+    g[b] = {-gr[3 * b] * 2.0 * x[0], -gr[3 * b + 1] * psill, -gr[3 * b + 2] * range};
+    if (range > range_max) {
+      const double dreg = 2.0 * (range - range_max) / (range_max * range_max);
+      g[b][2] += 1e6 * dreg * range;
+    }
+  }
+  return GS_OK;
+}
+
+int finish_fit(int32_t kind, const std::pair<std::vector<double>, double>& best,
+               gs_model* out_model, double* out_loglik, double* out_x) {
+  if (best.second >= 1e12)
+    return fail(GS_ERR_SINGULAR_SYSTEM,
+                "Vecchia MLE did not converge to a feasible fit: every starting point stayed on a "
+                "singular/degenerate covariance");
+  const auto& xb = best.first;
+  if (out_x)
+    for (int i = 0; i < 3; ++i) out_x[i] = xb[i];
+  if (out_model) {
+    *out_model = model_from_x(kind, xb);
+    GS_TRY(validate_model(*out_model));
+  }
+  if (out_loglik) *out_loglik = -best.second;
+  return GS_OK;
+}
+
+}  // namespace
+}  // namespace gs
+
+extern "C" {
+
+int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                   gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals) {
+  GS_TRY(check_fit_kind(ps, kind));
+  gs_vecchia_plan* P = nullptr;
+  GS_TRY(plan_create(ps, m, order, &P));
+  const FitSetup fs = fit_setup(ps, P->mean);
+  // the reference's three starts (vecchia.rs:1018-1023) and 200 iterations
+  const double lr0 = std::log(fs.range0);
+  std::vector<Bfgs> runs;
+  for (double f : {0.3, 1.0, 3.0})
+    runs.emplace_back(std::vector<double>{std::sqrt(0.1 * fs.var0), std::log(0.9 * fs.var0),
+                                          lr0 + std::log(f)},
+                      200);
+  int64_t evals = 0;
+  int rc = GS_OK;
+  for (int guard = 0; guard < 100000 && !rc; ++guard) {
+    std::vector<std::vector<double>> fx, gx;
+    std::vector<size_t> fo, go;
+    for (size_t r = 0; r < runs.size(); ++r) {
+      if (runs[r].done()) continue;
+      if (runs[r].wants_gradient()) {
+        gx.push_back(runs[r].pending_x());
+        go.push_back(r);
+      } else {
+        fx.push_back(runs[r].pending_x());
+        fo.push_back(r);
+      }
+    }
+    if (fx.empty() && gx.empty()) break;
+    std::vector<double> fv;
+    std::vector<std::vector<double>> gv;
+    if (!fx.empty()) rc = batch_objective(P, kind, fs.range_max, fx, fv);
+    if (!rc && !gx.empty()) rc = batch_gradient(P, kind, fs.range_max, gx, gv);
+    if (rc) break;
+    evals += (int64_t)(fx.size() + gx.size());
+    for (size_t b = 0; b < fo.size(); ++b) runs[fo[b]].supply_f(fv[b]);
+    for (size_t b = 0; b < go.size(); ++b) runs[go[b]].supply_g(gv[b]);
+  }
+  delete P;
+  if (rc) return rc;
+  if (n_evals) *n_evals = evals;
+  return finish_fit(kind, bfgs_multistart_best(runs), out_model, out_loglik, out_x);
+}
+
+int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                      int64_t nstarts, const double* starts, double step, int64_t max_iter,
+                      gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals) {
+  GS_TRY(check_fit_kind(ps, kind));
+  gs_vecchia_plan* P = nullptr;
+  GS_TRY(plan_create(ps, m, order, &P));
+  const FitSetup fs = fit_setup(ps, P->mean);
   std::vector<std::vector<double>> st;
   if (starts) {
     for (int64_t q = 0; q < nstarts; ++q) st.push_back({starts[q * 3], starts[q * 3 + 1], starts[q * 3 + 2]});
   } else {
-    const double lr0 = std::log(range0);
+    const double lr0 = std::log(fs.range0);
     if (nstarts <= 3) {
-      for (double f : {0.3, 1.0, 3.0}) st.push_back({std::sqrt(0.1 * var0), std::log(0.9 * var0), lr0 + std::log(f)});
+      for (double f : {0.3, 1.0, 3.0})
+        st.push_back({std::sqrt(0.1 * fs.var0), std::log(0.9 * fs.var0), lr0 + std::log(f)});
     } else {
       // a deterministic spread over range and nugget share
       for (int64_t q = 0; q < nstarts; ++q) {
         const double fr = std::pow(10.0, -1.0 + 2.0 * (double)(q % 4) / 3.0);
         const double nugf = 0.05 + 0.15 * (double)((q / 4) % 4);
-        st.push_back({std::sqrt(nugf * var0), std::log((1.0 - nugf) * var0), lr0 + std::log(fr)});
+        st.push_back({std::sqrt(nugf * fs.var0), std::log((1.0 - nugf) * fs.var0), lr0 + std::log(fr)});
       }
     }
   }
@@ -1439,70 +2152,40 @@ int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t
   int64_t evals = 0;
   int rc = GS_OK;
   for (int guard = 0; guard < 1000000 && !rc; ++guard) {
-    std::vector<gs_model> batch;
-    std::vector<std::pair<size_t, size_t>> owner;
-    std::vector<double> regs;
+    std::vector<std::vector<double>> xs;
+    std::vector<size_t> owner;
     for (size_t r = 0; r < runs.size(); ++r) {
       if (runs[r].done()) continue;
-      const auto& pend = runs[r].pending();
-      for (size_t q = 0; q < pend.size(); ++q) {
-        const auto& x = pend[q];
-        gs_model mdl;
-        std::memset(&mdl, 0, sizeof(mdl));
-        mdl.nugget = x[0] * x[0];
-        mdl.n_structures = 1;
-        mdl.s[0].kind = kind;
-        mdl.s[0].sill = std::exp(x[1]);
-        mdl.s[0].range = std::exp(x[2]);
-        mdl.s[0].ratio = mdl.s[0].ratio_z = 1.0;
-        const double range = mdl.s[0].range;
-        double reg = 0.0;
-        if (range > range_max) {
-          double t = (range - range_max) / range_max;
-          reg = t * t;
-        }
-        batch.push_back(mdl);
-        owner.push_back({r, q});
-        regs.push_back(reg);
+      for (const auto& x : runs[r].pending()) {
+        xs.push_back(x);
+        owner.push_back(r);
       }
     }
-    if (batch.empty()) break;
-    std::vector<double> ll(batch.size());
-    std::vector<int32_t> sts(batch.size());
-    rc = vecchia_eval(P, (int64_t)batch.size(), batch.data(), ll.data(), sts.data(), GS_PREC_MIXED, P->stream);
+    if (xs.empty()) break;
+    std::vector<double> fv;
+    rc = batch_objective(P, kind, fs.range_max, xs, fv);
     if (rc) break;
-    evals += (int64_t)batch.size();
+    evals += (int64_t)xs.size();
     std::vector<std::vector<double>> fvals(runs.size());
-    for (size_t b = 0; b < batch.size(); ++b) {
-      double f = (sts[b] == 0 && std::isfinite(ll[b])) ? -ll[b] + 1e6 * regs[b] : 1e12;
-      fvals[owner[b].first].push_back(f);
-    }
+    for (size_t b = 0; b < xs.size(); ++b) fvals[owner[b]].push_back(fv[b]);
     for (size_t r = 0; r < runs.size(); ++r)
       if (!fvals[r].empty()) runs[r].supply(fvals[r]);
   }
   delete P;
   if (rc) return rc;
-  auto best = multistart_best(runs);
   if (n_evals) *n_evals = evals;
-  if (best.second >= 1e12)
-    return fail(GS_ERR_SINGULAR_SYSTEM,
-                "Vecchia MLE did not converge to a feasible fit: every starting point stayed on a "
-                "singular/degenerate covariance");
-  const auto& xb = best.first;
-  if (out_x)
-    for (int i = 0; i < 3; ++i) out_x[i] = xb[i];
-  if (out_model) {
-    std::memset(out_model, 0, sizeof(*out_model));
-    out_model->nugget = xb[0] * xb[0];
-    out_model->n_structures = 1;
-    out_model->s[0].kind = kind;
-    out_model->s[0].sill = std::exp(xb[1]);
-    out_model->s[0].range = std::exp(xb[2]);
-    out_model->s[0].ratio = out_model->s[0].ratio_z = 1.0;
-    GS_TRY(validate_model(*out_model));
-  }
-  if (out_loglik) *out_loglik = -best.second;
-  return GS_OK;
+  return finish_fit(kind, multistart_best(runs), out_model, out_loglik, out_x);
+}
+
+int gs_vecchia_loglik_grad_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs_model* models,
+                                 double* loglik, double* grad, int32_t* status, int precision,
+                                 void* stream) {
+  if (!plan) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
+  if (ncand < 0) return fail(GS_ERR_INVALID_PARAMETER, "negative candidate count");
+  if (ncand > 0 && (!models || !loglik || !grad || !status))
+    return fail(GS_ERR_INVALID_PARAMETER, "null model or output buffer");
+  cudaStream_t s = stream ? (cudaStream_t)stream : plan->stream;
+  return vecchia_eval_grad(plan, ncand, models, loglik, grad, status, precision, s);
 }
 
 int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t nstarts,

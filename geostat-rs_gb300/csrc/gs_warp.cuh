@@ -15,7 +15,8 @@
 //
 // Refinement residuals b - A x use the double-float entries held in registers
 // (compensated FP32 dot products, Ogita, Rump & Oishi 2005); corrections are
-// register GEMVs with -A^{-1}.
+// register GEMVs with -A^{-1}.  One factorisation serves any number of
+// right-hand sides (warp_refine).
 #pragma once
 
 #include "gs_solve.cuh"
@@ -28,6 +29,13 @@ struct WarpScratch {
   float* row;  // 32 (+1 for d) floats: the published pivot row
   float* vec;  // 32 floats: broadcast vector
   df* xd;      // 32 df: solution
+};
+
+// The factorisation one lane holds: its row of the double-float matrix
+// (ah + al) and of -(sc A)^{-1} + 2I (t), with the power-of-two scale sc.
+struct WarpFactor {
+  float ah[kWarpN], al[kWarpN], t[kWarpN];
+  float sc;
 };
 
 // Loads row `lane` of the packed df matrix A (N x N) into registers; rows and
@@ -58,31 +66,32 @@ __device__ __forceinline__ void warp_gemv_neg_inv(const float (&t)[kWarpN], cons
   y = fmaf(-2.0f, vec[lane], s);
 }
 
-// Solves A x = B (N <= 32 unknowns) and refines to ~1e-13 relative; on
-// success W.xd[i] holds x_i.  Returns false (uniformly in the warp) when a
-// pivot is too small for FP32 or the refinement stalls.
-__device__ bool warp_solve(const df* A, const df* B, int N, int lane, const WarpScratch& W) {
-  float ah[kWarpN], al[kWarpN], t[kWarpN];
-  warp_load_rows(A, N, lane, ah, al);
+// FP32 inverse of the packed df matrix A (N <= 32 unknowns).  Returns false
+// (uniformly in the warp) when a pivot is too small for FP32.
+__device__ __forceinline__ bool warp_factor(const df* A, int N, int lane, WarpFactor& f,
+                                            const WarpScratch& W) {
+  warp_load_rows(A, N, lane, f.ah, f.al);
   float amax = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kWarpN; ++j) amax = fmaxf(amax, lane < N ? fabsf(ah[j]) : 0.0f);
+  for (int j = 0; j < kWarpN; ++j) amax = fmaxf(amax, lane < N ? fabsf(f.ah[j]) : 0.0f);
   amax = warp_max_f(amax);
+  f.sc = 1.0f;
   if (!(amax > 0.0f)) return false;
   // power-of-two scale: sc * max|A| in [0.5, 1), so every pivot is <= 1 and
   // the pivot lane's multiplier 1 - 1/d never cancels; the swept rows then
   // hold -(sc A)^{-1}, i.e. -A^{-1} / sc
   int ex = 0;
   frexpf(amax, &ex);
-  const float sc = ldexpf(1.0f, -ex);
+  f.sc = ldexpf(1.0f, -ex);
 #pragma unroll
-  for (int j = 0; j < kWarpN; ++j) t[j] = (lane < N && j < N) ? ah[j] * sc : ah[j];
-  const float tol = 1e-6f * amax * sc;
+  for (int j = 0; j < kWarpN; ++j) f.t[j] = (lane < N && j < N) ? f.ah[j] * f.sc : f.ah[j];
+  const float tol = 1e-6f * amax * f.sc;
   for (int k = 0; k < N; ++k) {
     if (lane == k) {
 #pragma unroll
       for (int j = 0; j < kWarpN; j += 4)
-        *reinterpret_cast<float4*>(W.row + j) = make_float4(t[j], t[j + 1], t[j + 2], t[j + 3]);
+        *reinterpret_cast<float4*>(W.row + j) =
+            make_float4(f.t[j], f.t[j + 1], f.t[j + 2], f.t[j + 3]);
     }
     __syncwarp();
     const float d = W.row[k];
@@ -95,19 +104,28 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
 #pragma unroll
     for (int j = 0; j < kWarpN; j += 4) {
       const float4 r = *reinterpret_cast<const float4*>(W.row + j);
-      t[j] = fmaf(-l, r.x, t[j]);
-      t[j + 1] = fmaf(-l, r.y, t[j + 1]);
-      t[j + 2] = fmaf(-l, r.z, t[j + 2]);
-      t[j + 3] = fmaf(-l, r.w, t[j + 3]);
+      f.t[j] = fmaf(-l, r.x, f.t[j]);
+      f.t[j + 1] = fmaf(-l, r.y, f.t[j + 1]);
+      f.t[j + 2] = fmaf(-l, r.z, f.t[j + 2]);
+      f.t[j + 3] = fmaf(-l, r.w, f.t[j + 3]);
     }
     __syncwarp();
   }
+  return true;
+}
+
+// Solves A x = B with the factorisation f and refines to ~1e-13 relative; on
+// success W.xd[i] holds x_i.  Returns false (uniformly) when the refinement
+// stalls.
+__device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, int N, int lane,
+                                            const WarpScratch& W) {
   // x0 = A^{-1} b_hi = -(-A^{-1}) b_hi
+  __syncwarp();
   W.vec[lane] = lane < N ? B[lane].hi : 0.0f;
   __syncwarp();
   float y;
-  warp_gemv_neg_inv(t, W.vec, lane, y);
-  y *= sc;
+  warp_gemv_neg_inv(f.t, W.vec, lane, y);
+  y *= f.sc;
   df x = df_make(lane < N ? -y : 0.0f, 0.0f);
   const float nx = warp_max_f(fabsf(x.hi));
   float nd_prev = nx;
@@ -120,10 +138,10 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
 #pragma unroll
     for (int j = 0; j < kWarpN; ++j) {
       const df xj = W.xd[j];
-      const float ph = __fmul_rn(-ah[j], xj.hi);
-      float pe = __fmaf_rn(-ah[j], xj.hi, -ph);
-      pe = __fmaf_rn(-ah[j], xj.lo, pe);
-      pe = __fmaf_rn(-al[j], xj.hi, pe);
+      const float ph = __fmul_rn(-f.ah[j], xj.hi);
+      float pe = __fmaf_rn(-f.ah[j], xj.hi, -ph);
+      pe = __fmaf_rn(-f.ah[j], xj.lo, pe);
+      pe = __fmaf_rn(-f.al[j], xj.hi, pe);
       const float tsum = __fadd_rn(s, ph);
       const float bb = __fsub_rn(tsum, s);
       const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
@@ -134,27 +152,32 @@ __device__ bool warp_solve(const df* A, const df* B, int N, int lane, const Warp
     __syncwarp();
     W.vec[lane] = r;
     __syncwarp();
-    warp_gemv_neg_inv(t, W.vec, lane, y);
-    y *= sc;
+    warp_gemv_neg_inv(f.t, W.vec, lane, y);
+    y *= f.sc;
     if (lane < N) x = df_add_f(x, -y);
     const float nd = warp_max_f(lane < N ? fabsf(y) : 0.0f);
-    if (nd <= 1e-15f * nx) {
+    bool done = nd <= 1e-15f * nx;
+    if (!done && sweep >= 2) {
+      const float rho = nd / nd_prev;
+      done = rho < 0.5f && rho * nd <= 1e-13f * nx;
+    }
+    if (done) {
+      __syncwarp();
       W.xd[lane] = x;
       __syncwarp();
       return true;
     }
-    if (sweep >= 2) {
-      const float rho = nd / nd_prev;
-      if (rho < 0.5f && rho * nd <= 1e-13f * nx) {
-        __syncwarp();
-        W.xd[lane] = x;
-        __syncwarp();
-        return true;
-      }
-    }
     nd_prev = nd;
   }
   return false;
+}
+
+// Factor and solve one right-hand side.
+__device__ __forceinline__ bool warp_solve(const df* A, const df* B, int N, int lane,
+                                           const WarpScratch& W) {
+  WarpFactor f;
+  if (!warp_factor(A, N, lane, f, W)) return false;
+  return warp_refine(f, B, N, lane, W);
 }
 
 }  // namespace gs

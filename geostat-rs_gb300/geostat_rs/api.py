@@ -406,6 +406,18 @@ class VecchiaPlan:
                                                    _p(nb, C.c_int64), _p(cnt, C.c_int32)))
         return order, nb.reshape(n, m), cnt
 
+    def loglik_grad(self, models, precision="mixed"):
+        """loglik_grad_with_plan for single-structure isotropic models:
+        returns (loglik[ncand], grad[ncand, 3], status[ncand])."""
+        arr = (_abi.Model * len(models))(*[model_struct(m) for m in models])
+        n = len(models)
+        ll, g = np.empty(n), np.empty((n, 3))
+        st = np.empty(n, dtype=np.int32)
+        _abi.check(_abi.load().gs_vecchia_loglik_grad_batch(self._h, n, arr, _p(ll), _p(g),
+                                                            _p(st, C.c_int32),
+                                                            PRECISIONS[precision], None))
+        return ll, g, st
+
     def loglik(self, models: Sequence[VariogramModel], precision="mixed"):
         """Log-likelihood of each candidate model in one batched launch.
         Returns ``(loglik, status)``."""
@@ -449,11 +461,31 @@ def vecchia_loglik(x, y, values, model, m=20):
     return ll.value
 
 
-def vecchia_mle_fit(data: PointSet, kind="exponential", m=20, starts=None, nstarts=3, step=0.3,
-                    max_iter=2000, order=None):
-    """Batched multi-start Nelder-Mead fit; returns ``(model, loglik, x, n_evals)``."""
+def _fit_kind(kind):
     from .model import parse_kind
     kname, _ = parse_kind(kind) if kind not in KIND_CODES else (kind, 0.0)
+    return kname
+
+
+def vecchia_mle_fit(data: PointSet, kind="exponential", m=20, order=None):
+    """``vecchia_mle`` (vecchia.rs:921-1081): the reference's BFGS fit with the
+    analytical gradient; returns ``(model, loglik, x, n_evals)``."""
+    kname = _fit_kind(kind)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    out = _abi.Model()
+    ll = C.c_double()
+    x = np.zeros(3)
+    ne = C.c_int64()
+    _abi.check(_abi.load().gs_vecchia_mle(data._h, KIND_CODES[kname], int(m), _p(o, C.c_int64),
+                                          C.byref(out), C.byref(ll), _p(x), C.byref(ne)))
+    model = VariogramModel(out.nugget, [Structure(kname, out.s[0].sill, out.s[0].range)])
+    return model, ll.value, x, ne.value
+
+
+def vecchia_mle_nm_fit(data: PointSet, kind="exponential", m=20, starts=None, nstarts=3, step=0.3,
+                       max_iter=2000, order=None):
+    """Batched multi-start Nelder-Mead fit; returns ``(model, loglik, x, n_evals)``."""
+    kname = _fit_kind(kind)
     st = None if starts is None else _f64(starts).reshape(-1, 3)
     ns = len(st) if st is not None else int(nstarts)
     o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
@@ -461,15 +493,15 @@ def vecchia_mle_fit(data: PointSet, kind="exponential", m=20, starts=None, nstar
     ll = C.c_double()
     x = np.zeros(3)
     ne = C.c_int64()
-    _abi.check(_abi.load().gs_vecchia_mle(data._h, KIND_CODES[kname], int(m), _p(o, C.c_int64),
-                                          ns, _p(st), float(step), int(max_iter), C.byref(out),
-                                          C.byref(ll), _p(x), C.byref(ne)))
+    _abi.check(_abi.load().gs_vecchia_mle_nm(data._h, KIND_CODES[kname], int(m), _p(o, C.c_int64),
+                                             ns, _p(st), float(step), int(max_iter), C.byref(out),
+                                             C.byref(ll), _p(x), C.byref(ne)))
     model = VariogramModel(out.nugget, [Structure(kname, out.s[0].sill, out.s[0].range)])
     return model, ll.value, x, ne.value
 
 
 def vecchia_mle(x, y, values, kind="exponential", m=20):
-    """lib.rs:351-367 ``vecchia_mle`` (Nelder-Mead multistart on the GPU)."""
+    """lib.rs:351-367 ``vecchia_mle``."""
     data = PointSet.from_xyz(x, y, values)
     return vecchia_mle_fit(data, kind, m)[0]
 

@@ -208,21 +208,39 @@ int gs_vecchia_loglik_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs
 /* vecchia_loglik (vecchia.rs:874-884). */
 int gs_vecchia_loglik(const gs_pointset* ps, const gs_model* model, int64_t m,
                       const int64_t* order, double* loglik);
-/* vecchia_mle (vecchia.rs:921-1081) with a batched multi-start
- * Nelder-Mead: every start's pending simplex evaluations go to the device
- * in one gs_vecchia_loglik_batch launch.  starts (nstarts x 3, in the
- * reference's x = (sqrt nugget, ln psill, ln range) parameters) may be NULL
- * for the reference's three starts.  out_x receives the optimum. */
+/* loglik_grad_with_plan (vecchia.rs:416-530): log-likelihood and its
+ * gradient with respect to (nugget, psill, range), grad[c * 3 + q], for
+ * ncand single-structure isotropic models of the closed-form kinds
+ * (g_and_dg, vecchia.rs:353-389) in one launch.  status[c] is 0, a singular
+ * conditioning system, or GS_ERR_INVALID_PARAMETER for a model without a
+ * closed-form gradient. */
+int gs_vecchia_loglik_grad_batch(const gs_vecchia_plan* plan, int64_t ncand,
+                                 const gs_model* models, double* loglik, double* grad,
+                                 int32_t* status, int precision, void* stream);
+/* vecchia_mle (vecchia.rs:921-1081 mle_fit_with_plan): the reference's fit
+ * -- its three starts, BFGS (optim.rs:207-289, 200 iterations) with the
+ * analytical gradient for the closed-form kinds, which are all the kinds the
+ * CUDA path evaluates.  The three starts advance in lock-step: each round's
+ * objective requests go to the device in one gs_vecchia_loglik_batch launch
+ * and its gradient requests in one gs_vecchia_loglik_grad_batch launch.
+ * out_x receives the optimum in x = (sqrt nugget, ln psill, ln range). */
 int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
-                   int64_t nstarts, const double* starts, double step, int64_t max_iter,
                    gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals);
+/* Multi-start Nelder-Mead fit (the reference's gradient-free path,
+ * optim.rs:6-123, step and max_iter as given) with every start's pending
+ * simplex evaluations batched into one launch per round -- the form for
+ * many starts.  starts (nstarts x 3, in x) may be NULL: nstarts <= 3 gives
+ * the reference's three starts, more a deterministic spread. */
+int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                      int64_t nstarts, const double* starts, double step, int64_t max_iter,
+                      gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals);
 /* vecchia_predict (vecchia.rs:748-866): level-scheduled on the device. */
 int gs_vecchia_predict(const gs_pointset* ps, const gs_model* model, int64_t nt,
                        const double* tx, const double* ty, const double* tz, int64_t m,
                        double* value, double* variance);
 
 /* optim::nelder_mead_multistart (crates/geostat-core/src/optim.rs:6-123)
- * over a host callback: the same state machine gs_vecchia_mle drives with
+ * over a host callback: the same state machine gs_vecchia_mle_nm drives with
  * batched device evaluations, exposed for driver parity checks. */
 typedef double (*gs_objective_fn)(const double* x, int64_t n, void* ctx);
 int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t nstarts,

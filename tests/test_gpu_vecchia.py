@@ -96,7 +96,7 @@ def test_mle_objective_parity_and_batched_nelder_mead():
     c, v = O.test_field_2d(400, 21)
     ps = G.PointSet(c, v)
     starts, rmax = O.vecchia_mle_setup(c, v)
-    model, ll, x, nev = G.vecchia_mle_fit(ps, "exponential", 12, starts=starts, max_iter=400)
+    model, ll, x, nev = G.vecchia_mle_nm_fit(ps, "exponential", 12, starts=starts, max_iter=400)
     xr, fr, nr = O.vecchia_mle_nm(c, v, "exponential", 12, starts, max_iter=400)
     # same algorithm, same objective to ~1e-12: the optimum agrees closely
     assert abs(-ll - fr) <= 1e-7 * abs(fr)
@@ -171,3 +171,48 @@ def test_vecchia_predict_deterministic_and_edge_cases():
     dup = np.vstack([c, c[:1]])
     with pytest.raises(G.DuplicatePoints):
         G.vecchia_predict(dup, np.append(v, 1.0), mdl, t, 8)
+
+
+# ---------------------------------------------- gradient and BFGS fit (a19, a21) --
+@pytest.mark.parametrize("kind", ["spherical", "exponential", "gaussian", "matern15", "matern25"])
+def test_loglik_gradient_matches_oracle(kind):
+    """loglik_grad_with_plan (vecchia.rs:416-530) for a batch of candidates."""
+    c = uniform_points(6000, 2, 31, [1.0, 1.0])
+    v = 0.5 + G.rff_field(c, matern25(), 1024, 7)
+    plan = G.VecchiaPlan(G.PointSet(c, v), 20)
+    order, nb, cnt = plan.arrays()
+    cands = [VariogramModel(0.02, [Structure(kind, 1.0, 0.08)]),
+             VariogramModel(0.2, [Structure(kind, 0.6, 0.03)]),
+             VariogramModel(0.0004, [Structure(kind, 1.3, 0.15)])]
+    for prec, tol in (("mixed", 1e-9), ("fp64", 1e-11)):
+        ll, g, st = plan.loglik_grad(cands, prec)
+        assert (st == 0).all()
+        for i, mdl in enumerate(cands):
+            s0 = mdl.structures[0]
+            rl, rg = O.vecchia_loglik_grad(c, v, kind, mdl.nugget, s0.sill, s0.range, order, nb, cnt)
+            assert_close([ll[i]], [rl], 1.0, tol, f"{prec} {kind} loglik {i}")
+            # gradient components: relative to max(|component|, n * 1e-4)
+            assert_close(g[i], rg, len(c) * 1e-4, tol, f"{prec} {kind} gradient {i}")
+
+
+def test_gradient_rejects_models_without_closed_form():
+    c = uniform_points(500, 2, 32, [1.0, 1.0])
+    plan = G.VecchiaPlan(G.PointSet(c, c[:, 0] + c[:, 1]), 10)
+    bad = [VariogramModel(0.1, [Structure("exponential", 0.5, 0.2), Structure("spherical", 0.4, 0.1)]),
+           VariogramModel(0.1, [Structure.with_anisotropy("exponential", 0.5, 0.2, 30.0, 0.5)]),
+           VariogramModel(0.1, [Structure("circular", 0.5, 0.2)])]
+    ll, g, st = plan.loglik_grad(bad + [matern25()])
+    assert (st[:3] == G.InvalidParameter.code).all() and st[3] == 0
+
+
+def test_mle_bfgs_matches_oracle():
+    """vecchia_mle (vecchia.rs:921-1081): the reference's three starts and
+    analytical-gradient BFGS, with the starts advanced in lock-step."""
+    for kind, n, m in (("exponential", 400, 12), ("matern25", 300, 10)):
+        c, v = O.test_field_2d(n, 40 + n)
+        model, ll, x, nev = G.vecchia_mle_fit(G.PointSet(c, v), kind, m)
+        xr, fr, nr = O.vecchia_mle_bfgs(c, v, kind, m)
+        assert abs(-ll - fr) <= 1e-7 * abs(fr), (kind, -ll, fr)
+        assert abs(x[0] ** 2 - xr[0] ** 2) < 1e-3 * max(xr[0] ** 2, 1e-3), (kind, x, xr)
+        assert np.max(np.abs(x[1:] - xr[1:])) < 1e-3, (kind, x, xr)
+        assert nev < 1000  # BFGS: tens to hundreds of evaluations, not thousands
