@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "geostat_rs", "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgeostat_gb300.so")
-SOURCES = ["gs_host.cu", "gs_search.cu", "gs_krige.cu", "gs_api.cu", "gs_noalloc.cu", "gs_vecchia.cu",
+SOURCES = ["gs_host.cu", "gs_search.cu", "gs_krige.cu", "gs_api.cu", "gs_noalloc.cu", "gs_serve.cu", "gs_vecchia.cu",
            "gs_synth.cu", "gs_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",

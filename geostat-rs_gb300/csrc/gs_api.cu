@@ -417,6 +417,10 @@ struct PhaseTimer {
   }
 };
 
+}  // namespace
+
+namespace gs {
+
 // Search + solves for targets already on the device.
 int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
                    const double* tz, const double* tdrift, double* value, double* variance,
@@ -598,7 +602,7 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   return GS_OK;
 }
 
-}  // namespace
+}  // namespace gs
 
 extern "C" {
 

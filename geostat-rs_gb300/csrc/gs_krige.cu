@@ -21,6 +21,7 @@
 // so neighbouring threads touch neighbouring addresses.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "gs_internal.h"
 #include "gs_krige.cuh"
@@ -682,13 +683,10 @@ __global__ void grid_centers_kernel(double x0, double y0, double z0, double dx, 
 
 static ExpTable g_tab;
 static DfConsts g_kc;
-static bool g_tab_ready = false;
+static std::once_flag g_tab_once;
 
 static void ensure_tables() {
-  if (!g_tab_ready) {
-    df_consts_host(&g_tab, &g_kc);
-    g_tab_ready = true;
-  }
+  std::call_once(g_tab_once, [] { df_consts_host(&g_tab, &g_kc); });
 }
 
 template <int D, int R, int PC>

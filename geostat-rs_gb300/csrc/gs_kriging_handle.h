@@ -34,3 +34,11 @@ struct gs_kriging {
     if (stream) cudaStreamDestroy(stream);
   }
 };
+
+namespace gs {
+// Search + solves for nt targets whose coordinates are already on the device
+// (outputs in device memory); synchronises `stream` before returning.
+int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                   const double* tz, const double* tdrift, double* value, double* variance,
+                   double* lagrange, uint8_t* status, int precision, cudaStream_t stream);
+}  // namespace gs

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "gs_common.cuh"
@@ -536,7 +537,11 @@ __global__ void reduce_partials(const double* partial, int nblk, int ncand, doub
 
 ExpTable g_vtab;
 DfConsts g_vkc;
-bool g_vready = false;
+std::once_flag g_vonce;
+
+void ensure_vtables() {
+  std::call_once(g_vonce, [] { df_consts_host(&g_vtab, &g_vkc); });
+}
 
 int reject_vecchia_model(const gs_model& m, int dim) {
   GS_TRY(validate_model(m));
@@ -558,10 +563,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   const int dim = ps->dim;
   const int64_t n = P->n;
   const int M = (int)P->m;
-  if (!g_vready) {
-    df_consts_host(&g_vtab, &g_vkc);
-    g_vready = true;
-  }
+  ensure_vtables();
   std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
   std::vector<int> valid(ncand, 0);
   bool all_iso = true;
@@ -699,6 +701,8 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   }
   return GS_OK;
 }
+
+int64_t vecchia_plan_points(const gs_vecchia_plan* P) { return P->n; }
 
 // ---------------------------------------------- log-likelihood gradient --
 // loglik_grad_inner (vecchia.rs:428-530) for single-structure isotropic
@@ -1129,10 +1133,7 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
   const int dim = ps->dim;
   const int64_t n = P->n;
   const int M = (int)P->m;
-  if (!g_vready) {
-    df_consts_host(&g_vtab, &g_vkc);
-    g_vready = true;
-  }
+  ensure_vtables();
   std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
   for (int64_t c = 0; c < ncand; ++c) {
     status[c] = GS_OK;
@@ -1651,10 +1652,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
   if (kout > GS_MAX_SYSTEM)
     return fail(GS_ERR_INVALID_PARAMETER, "the CUDA path conditions on at most " +
                                               std::to_string(GS_MAX_SYSTEM) + " points");
-  if (!g_vready) {
-    df_consts_host(&g_vtab, &g_vkc);
-    g_vready = true;
-  }
+  ensure_vtables();
   double sum = 0.0;
   for (int64_t i = 0; i < n; ++i) sum += ps->values[i];
   const double mean = sum / (double)n;

@@ -1,0 +1,16 @@
+// gs_vecchia.h -- Vecchia entry points shared with other translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/geostat_gb300.h"
+
+namespace gs {
+// Log-likelihood of ncand candidate models on a plan (one batched launch);
+// ll[c] and status[c] per candidate; synchronises `s` before returning.
+int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
+                 int32_t* status, int precision, cudaStream_t s);
+// Points of the plan's data set.
+int64_t vecchia_plan_points(const gs_vecchia_plan* P);
+}  // namespace gs

@@ -71,6 +71,14 @@ SIGNATURES = {
                                               _int, _vp]),
     "gs_kriging_predict_fp64_noalloc": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                                _vp, _vp]),
+    "gs_server_create": (_int, [_i64, _i32, C.POINTER(_vp)]),
+    "gs_server_add_kriging": (_int, [_vp, _vp, _pi32]),
+    "gs_server_add_vecchia": (_int, [_vp, _vp, _pi32]),
+    "gs_server_submit_predict": (_int, [_vp, _i32, _i64, _pd, _pd, _pd, _pd, _pd, _pu8, _pi64]),
+    "gs_server_submit_loglik": (_int, [_vp, _i32, _pm, _pd, _pi32, _pi64]),
+    "gs_server_wait": (_int, [_vp, _i64, _pd]),
+    "gs_server_stats": (_int, [_vp, _pd, _pd, _pi64, _pi64]),
+    "gs_server_destroy": (None, [_vp]),
     "gs_kriging_predict_grid": (_int, [_vp, _pd, _pd, _pi64, _pd, _pd, _pu8, _int, _vp]),
     "gs_kriging_neighbors": (_int, [_vp, _i64, _pd, _pd, _pd, _i64, _pi32, _pi32, _vp]),
     "gs_maxmin_order": (_int, [_int, _i64, _pd, _pd, _pd, _pi64]),

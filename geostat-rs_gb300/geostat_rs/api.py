@@ -519,6 +519,82 @@ def vecchia_krige(x, y, values, model, target_x, target_y, m=30):
     return v, var
 
 
+class Server:
+    """Continuous-batching request loop over resident data sets (the C ABI's
+    gs_server_*): ``add_kriging`` / ``add_vecchia`` register built
+    predictors and plans, ``submit_predict`` / ``submit_loglik`` queue
+    requests from any thread and return a request object, ``wait`` blocks
+    for one, ``stats`` gives (p50 ms, p99 ms, completed, launches)."""
+
+    class _Req:
+        def __init__(self, rid, keep, out):
+            self.id, self._keep, self.out = rid, keep, out
+
+    def __init__(self, mem_budget_bytes=64 << 30, executors=2):
+        h = C.c_void_p()
+        _abi.check(_abi.load().gs_server_create(int(mem_budget_bytes), int(executors),
+                                                C.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def add_kriging(self, k: "Kriging") -> int:
+        d = C.c_int32()
+        _abi.check(_abi.load().gs_server_add_kriging(self._h, k._h, C.byref(d)))
+        self._keep.append(k)
+        return d.value
+
+    def add_vecchia(self, plan: "VecchiaPlan") -> int:
+        d = C.c_int32()
+        _abi.check(_abi.load().gs_server_add_vecchia(self._h, plan._h, C.byref(d)))
+        self._keep.append(plan)
+        return d.value
+
+    def submit_predict(self, dataset: int, targets):
+        t = np.asarray(targets, dtype=np.float64)
+        cols = [np.ascontiguousarray(t[:, d]) for d in range(t.shape[1])]
+        nt = len(t)
+        v, var = np.empty(nt), np.empty(nt)
+        st = np.empty(nt, dtype=np.uint8)
+        rid = C.c_int64()
+        _abi.check(_abi.load().gs_server_submit_predict(
+            self._h, int(dataset), nt, _p(cols[0]), _p(cols[1]),
+            _p(cols[2]) if len(cols) == 3 else None, _p(v), _p(var), _p(st, C.c_uint8),
+            C.byref(rid)))
+        return Server._Req(rid.value, cols, (v, var, st))
+
+    def submit_loglik(self, dataset: int, model: VariogramModel):
+        ms = model_struct(model)
+        ll = np.empty(1)
+        st = np.empty(1, dtype=np.int32)
+        rid = C.c_int64()
+        _abi.check(_abi.load().gs_server_submit_loglik(self._h, int(dataset), C.byref(ms), _p(ll),
+                                                       _p(st, C.c_int32), C.byref(rid)))
+        return Server._Req(rid.value, ms, (ll, st))
+
+    def wait(self, req) -> float:
+        lat = C.c_double()
+        _abi.check(_abi.load().gs_server_wait(self._h, req.id, C.byref(lat)))
+        return lat.value
+
+    def stats(self):
+        p50, p99 = C.c_double(), C.c_double()
+        done, launches = C.c_int64(), C.c_int64()
+        _abi.check(_abi.load().gs_server_stats(self._h, C.byref(p50), C.byref(p99),
+                                               C.byref(done), C.byref(launches)))
+        return p50.value, p99.value, done.value, launches.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().gs_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def vecchia_predict(coords, values, model, targets, m=30):
     """``vecchia_predict`` (vecchia.rs:748-866) in 2-D or 3-D: joint Vecchia
     prediction at ``targets``; returns ``(values, variances)``."""

@@ -247,6 +247,30 @@ int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t n
                               const double* starts, double step, int64_t max_iter, double* x_out,
                               double* f_out);
 
+/* Serving loop (no counterpart in the reference, which serves one call at a
+ * time): data sets stay resident as built predictors and Vecchia plans;
+ * callers on any thread submit prediction and log-likelihood requests;
+ * `executors` threads, each with its own stream, admit the oldest pending
+ * request once the device-memory budget allows it, coalesce every pending
+ * request of the same data set and kind into the same launch, and scatter the
+ * results.  Host buffers of a request must stay valid until gs_server_wait
+ * returns for it; every request is waited for exactly once.
+ * gs_server_stats reports the median and 99th-percentile submit-to-finish
+ * latency of the completed requests and the number of launches formed. */
+typedef struct gs_server gs_server;
+int gs_server_create(int64_t mem_budget_bytes, int32_t executors, gs_server** out);
+int gs_server_add_kriging(gs_server* s, const gs_kriging* k, int32_t* dataset);
+int gs_server_add_vecchia(gs_server* s, const gs_vecchia_plan* plan, int32_t* dataset);
+int gs_server_submit_predict(gs_server* s, int32_t dataset, int64_t nt, const double* tx,
+                             const double* ty, const double* tz, double* value, double* variance,
+                             uint8_t* status, int64_t* request_id);
+int gs_server_submit_loglik(gs_server* s, int32_t dataset, const gs_model* model, double* loglik,
+                            int32_t* status, int64_t* request_id);
+int gs_server_wait(gs_server* s, int64_t request_id, double* latency_ms);
+int gs_server_stats(gs_server* s, double* p50_ms, double* p99_ms, int64_t* completed,
+                    int64_t* batches);
+void gs_server_destroy(gs_server* s);
+
 /* Seeded synthetic inputs (no reference counterpart beyond
  * crates/geostat-core/src/rng.rs): xoshiro256++ uniforms on the host and a
  * random-Fourier-feature Gaussian field evaluated on the device.  kind is
