@@ -286,6 +286,7 @@ def run_ours(args, rank, world):
         acc, cpu = cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var,
                                            fp64_v, kr, log)
         vec = vecchia_bench(args, log) if not args.no_vecchia else None
+        serve = serving_bench(args, log) if args.serve_requests > 0 else None
         peaks = measured_peaks()
         result = {
             "metric": METRIC,
@@ -329,6 +330,9 @@ def run_ours(args, rank, world):
         }
         if vec is not None:
             result["vecchia"] = vec
+        if serve is not None:
+            result["serving"] = serve
+            result["p99_latency_ms"] = serve["p99_ms"]
     return result
 
 
@@ -395,18 +399,118 @@ def vecchia_bench(args, log):
         ll, st = plan.loglik(cands)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
-    ll64, _ = plan.loglik(cands[:1], precision="fp64")
     t1 = time.perf_counter()
-    plan.loglik(cands[:1], precision="fp64")
+    ll64, _ = plan.loglik(cands, precision="fp64")
     dt64 = time.perf_counter() - t1
     t1 = time.perf_counter()
     ll1, _ = plan.loglik(cands[:1])
     dt1 = time.perf_counter() - t1
-    return {"points_per_s": n * len(cands) / dt, "unit": "Vecchia points/s",
-            "n": n, "m": 30, "candidates_per_batch": len(cands), "batch_ms": dt * 1e3,
-            "fp64_gpu_points_per_s": n / dt64, "single_candidate_points_per_s": n / dt1,
-            "mixed_vs_fp64_rel_diff": abs(ll1[0] - ll64[0]) / abs(ll64[0]),
-            "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
+    # gradient batch: one BFGS round of the three reference starts
+    gc = [VariogramModel(0.02 * f, [Structure("matern25", 1.0, 0.05 * f)]) for f in (0.5, 1.0, 2.0)]
+    plan.loglik_grad(gc)
+    t1 = time.perf_counter()
+    _, _, gst = plan.loglik_grad(gc)
+    dtg = time.perf_counter() - t1
+    out = {"points_per_s": n * len(cands) / dt, "unit": "Vecchia points/s",
+           "n": n, "m": 30, "candidates_per_batch": len(cands), "batch_ms": dt * 1e3,
+           "fp64_gpu_points_per_s": n * len(cands) / dt64,
+           "mixed_over_fp64": dt64 / dt,
+           "single_candidate_points_per_s": n / dt1,
+           "mixed_vs_fp64_max_rel_diff": float(np.max(np.abs(ll - ll64) / np.abs(ll64))),
+           "gradient_points_per_s": n * len(gc) / dtg, "gradient_status_ok": bool((gst == 0).all()),
+           "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
+    # joint prediction at args.vpred_n targets conditioning on the same data (m = 30)
+    if args.vpred_n > 0:
+        nt = args.vpred_n
+        t = G.rng_uniform(SEED + 7, 2 * nt).reshape(nt, 2)
+        t1 = time.perf_counter()
+        pv, pvar = G.vecchia_predict(None, None, base, t, 30, pointset=ps)
+        dtp = time.perf_counter() - t1
+        out["predict"] = {"targets": nt, "targets_per_s": nt / dtp, "seconds": dtp,
+                          "includes": "host max-min order of the targets, device search, "
+                                      "level-scheduled solves and row merges, copies",
+                          "finite": bool(np.isfinite(pv).all() and np.isfinite(pvar).all())}
+        # accuracy against the oracle on a small instance of the same kind
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as O
+        cs, ts_ = c[:20000], t[:4000]
+        vs = v[:20000]
+        gv, gvar = G.vecchia_predict(cs, vs, base, ts_, 30)
+        rv, rvar = O.vecchia_predict(cs, vs, base, ts_, 30)
+        out["predict"]["oracle_check"] = {
+            "data": 20000, "targets": 4000,
+            "max_rel_value": float(np.max(np.abs(gv - rv) / np.maximum(np.abs(rv), np.mean(np.abs(vs))))),
+            "max_rel_variance": float(np.max(np.abs(gvar - rvar) / np.maximum(np.abs(rvar), 1e-3)))}
+    return out
+
+
+def serving_bench(args, log):
+    """Serving loop on resident data sets: Poisson arrivals of prediction
+    requests (log-uniform target counts in [1, 1e6], n_max 16..64) and Vecchia
+    log-likelihood requests (m = 30).  Data sets: 2-D 10k (n_max 16), 3-D 50k
+    (n_max 32), 2-D 200k (n_max 48), 3-D 500k (n_max 64) for kriging; 2-D 10k
+    and 50k for Vecchia."""
+    import geostat_rs as G
+    from geostat_rs.model import Structure, VariogramModel
+    rng = np.random.default_rng(SEED + 11)
+    t0 = time.time()
+    m2 = VariogramModel(0.1, [Structure("spherical", 1.0, 200.0)])
+    m3 = make_model()
+    specs = [(2, 10_000, 16, m2), (3, 50_000, 32, m3), (2, 200_000, 48, m2), (3, 500_000, 64, m3)]
+    srv = G.Server(mem_budget_bytes=32 << 30, executors=3)
+    kds, pools = [], []
+    for dim, n, kmax, mdl in specs:
+        box = np.array([1000.0, 1000.0]) if dim == 2 else np.asarray(BOX)
+        cc = G.rng_uniform(SEED + n, dim * n).reshape(n, dim) * box
+        vv = G.rff_field(cc, mdl, 1024, SEED + n + 1)
+        k = G.Kriging.new(G.PointSet(cc, vv), mdl, G.KrigingConfig(max_neighbors=kmax))
+        kds.append(srv.add_kriging(k))
+        pools.append(rng.uniform(0, 1, size=(1_000_000, dim)) * box)
+    vds = []
+    base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
+    for n in (10_000, 50_000):
+        cc = G.rng_uniform(SEED + 3 * n, 2 * n).reshape(n, 2)
+        vv = 0.5 + G.rff_field(cc, base, 1024, SEED + 3 * n + 1)
+        vds.append(srv.add_vecchia(G.VecchiaPlan(G.PointSet(cc, vv), 30)))
+    log(f"[bench] serving set-up {time.time() - t0:.1f}s")
+    nreq, rate = args.serve_requests, 200.0
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    jobs = []
+    for q in range(nreq):
+        if rng.uniform() < 0.15:
+            f = rng.uniform(0.5, 2.0)
+            jobs.append(("ll", vds[q % 2], VariogramModel(0.02 * f, [Structure("matern25", 1.0, 0.05 * f)])))
+        else:
+            d = int(rng.integers(0, len(kds)))
+            nt = int(np.exp(rng.uniform(0.0, np.log(1e6))))
+            st = int(rng.integers(0, len(pools[d]) - nt + 1))
+            jobs.append(("p", kds[d], pools[d][st:st + nt]))
+    # warm-up: one request of each kind
+    srv.wait(srv.submit_predict(kds[0], pools[0][:100]))
+    srv.wait(srv.submit_loglik(vds[0], base))
+    _, _, done0, launches0 = srv.stats()
+    reqs, targets = [], 0
+    start = time.perf_counter()
+    for (kind, ds, arg), at in zip(jobs, arrivals):
+        delay = start + at - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        reqs.append(srv.submit_predict(ds, arg) if kind == "p" else srv.submit_loglik(ds, arg))
+        if kind == "p":
+            targets += len(arg)
+    lat = [srv.wait(r) for r in reqs]
+    wall = time.perf_counter() - start
+    lat = np.asarray(lat)
+    _, _, done, launches = srv.stats()
+    srv.close()
+    return {"requests": nreq, "arrival_rate_per_s": rate, "executors": 3,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "wall_s": wall, "targets": targets,
+            "targets_per_s": targets / wall, "requests_per_s": nreq / wall,
+            "launches": launches - launches0,
+            "datasets": "kriging 2-D 10k/n_max 16, 3-D 50k/32, 2-D 200k/48, 3-D 500k/64; "
+                        "Vecchia 2-D 10k and 50k, m = 30",
+            "mix": "85% predictions (target count log-uniform in [1, 1e6]), 15% log-likelihoods"}
 
 
 # ------------------------------------------------------------- reference --
@@ -499,6 +603,10 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--vecchia-n", type=int, default=2_000_000)
     ap.add_argument("--no-vecchia", action="store_true")
+    ap.add_argument("--vpred-n", type=int, default=500_000,
+                    help="targets of the Vecchia joint-prediction timing (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=1000,
+                    help="requests of the serving-loop run (0: skip)")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run one mixed-precision pass over the first N grid targets and exit "
                          "(the small case for ncu captures)")

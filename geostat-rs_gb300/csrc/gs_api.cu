@@ -39,6 +39,21 @@ int ensure_device() {
   return GS_OK;
 }
 
+int allow_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<uint64_t, size_t> limit;  // (device, function) -> bytes
+  int dev = 0;
+  GS_CUDA(cudaGetDevice(&dev));
+  const uint64_t key = ((uint64_t)(uintptr_t)func) ^ ((uint64_t)dev << 56);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limit[key];
+  if (bytes > cur) {
+    GS_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+  }
+  return GS_OK;
+}
+
 int DevBuf::alloc(size_t b, cudaStream_t s) {
   release();
   stream = s;

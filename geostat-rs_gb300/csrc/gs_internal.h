@@ -16,6 +16,12 @@ void count_launch(int n);
 // returning memory to the driver between calls).
 int ensure_device();
 
+// Allows launches of `func` with `bytes` of dynamic shared memory on the
+// current device.  The per-function limit is process-wide state, so it is
+// only ever raised (under a lock): a thread launching with a smaller size
+// can never invalidate another thread's larger launch.
+int allow_dynamic_smem(const void* func, size_t bytes);
+
 // Stream-ordered device allocation released at scope exit.
 struct DevBuf {
   void* ptr = nullptr;

@@ -695,7 +695,7 @@ static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   const RowsLayout lay = rows_layout(R, PC, nf, D);
   const size_t smem = lay.total;
   auto kern = krige_rows_kernel<D, R, PC>;
-  GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  GS_TRY(allow_dynamic_smem((const void*)kern, smem));
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

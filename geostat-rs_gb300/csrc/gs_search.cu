@@ -706,7 +706,7 @@ int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p
   int64_t blocks64 = (nt + wpb - 1) / wpb;
   int blocks = (int)std::min<int64_t>(blocks64, 152 * 64);
   auto launch = [&](auto kern) -> int {
-    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GS_TRY(allow_dynamic_smem((const void*)kern, smem));
     kern<<<blocks, wpb * 32, smem, stream>>>(g.dev, frame, p, nt, tx, ty, tz, nb, nbc);
     GS_CUDA(cudaGetLastError());
     count_launch(1);

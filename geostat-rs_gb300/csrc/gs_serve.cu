@@ -22,11 +22,13 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
 
 #include "gs_common.cuh"
+#include "gs_host.h"
 #include "gs_internal.h"
 #include "gs_kriging_handle.h"
 #include "gs_vecchia.h"
@@ -53,6 +55,7 @@ struct Request {
   int64_t bytes = 0;
   Clock::time_point submitted, finished;
   int rc = GS_OK;
+  std::string err;  // the failing call's message (worker thread)
   bool done = false;
 };
 
@@ -190,12 +193,14 @@ void worker_loop(gs_server* S) {
     }
     int rc = s ? (batch[0]->kind == 0 ? run_predictions(S, batch, s) : run_logliks(S, batch, s))
                : fail(GS_ERR_CUDA, "stream creation failed");
+    const std::string err = rc ? std::string(last_error()) : std::string();
     {
       std::lock_guard<std::mutex> lock(S->mu);
       S->in_use -= bytes;
       const auto now = Clock::now();
       for (Request* r : batch) {
         r->rc = rc;
+        r->err = err;
         r->done = true;
         r->finished = now;
         S->latencies_ms.push_back(
@@ -322,8 +327,9 @@ int gs_server_wait(gs_server* S, int64_t request_id, double* latency_ms) {
   if (latency_ms)
     *latency_ms = std::chrono::duration<double, std::milli>(r->finished - r->submitted).count();
   const int rc = r->rc;
+  const std::string err = r->err;
   S->requests.erase(it);
-  if (rc) return fail(rc, "request failed");
+  if (rc) return fail(rc, "request failed: " + err);
   return GS_OK;
 }
 

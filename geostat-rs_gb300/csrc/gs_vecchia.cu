@@ -622,7 +622,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     if (M <= kWarpN) {
       const size_t smem = vecchia_warp_layout(std::max(M, 1), dim).total * kVWarps;
       auto kern = dim == 2 ? vecchia_warp_kernel<2> : vecchia_warp_kernel<3>;
-      GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      GS_TRY(allow_dynamic_smem((const void*)kern, smem));
       int per_sm = 0;
       GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kVWarps, smem));
       per_sm = std::max(per_sm, 1);
@@ -635,7 +635,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
       const int tiles = lay.nbr * (lay.nbr + 1) / 2;
       const int block = std::min(256, std::max(64, ((tiles + 31) / 32) * 32));
       auto kern = dim == 2 ? vecchia_loglik_kernel<2, 256> : vecchia_loglik_kernel<3, 256>;
-      GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      GS_TRY(allow_dynamic_smem((const void*)kern, smem));
       int per_sm = 0;
       GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
       per_sm = std::max(per_sm, 1);
@@ -1190,7 +1190,7 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t smem = vecchia_grad_layout(std::max(M, 1), dim).total * kVWarps;
     auto kern = dim == 2 ? vecchia_grad_kernel<2> : vecchia_grad_kernel<3>;
-    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GS_TRY(allow_dynamic_smem((const void*)kern, smem));
     int per_sm = 0;
     GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kVWarps, smem));
     per_sm = std::max(per_sm, 1);
@@ -1790,7 +1790,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
   if (mixed) {
     vsmem = vecchia_warp_layout(kout, dim).total * kVPWarps;
     auto kern = dim == 2 ? vp_solve_kernel<2> : vp_solve_kernel<3>;
-    GS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vsmem));
+    GS_TRY(allow_dynamic_smem((const void*)kern, vsmem));
   }
   // FP64 slabs: up to 2 GiB, at least one block of threads
   const int64_t per = ((int64_t)kout * kout + 2 * (int64_t)kout) * 8;

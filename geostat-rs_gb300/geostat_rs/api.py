@@ -595,10 +595,11 @@ class Server:
             pass
 
 
-def vecchia_predict(coords, values, model, targets, m=30):
+def vecchia_predict(coords, values, model, targets, m=30, pointset=None):
     """``vecchia_predict`` (vecchia.rs:748-866) in 2-D or 3-D: joint Vecchia
-    prediction at ``targets``; returns ``(values, variances)``."""
-    data = PointSet(coords, values)
+    prediction at ``targets``; returns ``(values, variances)``.  An existing
+    ``pointset`` of the same data may be passed instead of coords/values."""
+    data = pointset if pointset is not None else PointSet(coords, values)
     targets = np.ascontiguousarray(np.asarray(targets, dtype=np.float64))
     if targets.ndim != 2 or targets.shape[1] != data.dim:
         raise DimensionMismatch("targets must be an (nt, dim) array matching the data")

@@ -32,11 +32,18 @@ def test_mixed_requests_match_their_results_alone():
     c3 = uniform_points(10000, 3, 502, [1000.0, 1000.0, 200.0])
     v3 = G.rff_field(c3, m3, 512, 6)
     k3 = G.Kriging.new(G.PointSet(c3, v3), m3, G.KrigingConfig(max_neighbors=24))
+    # a second 2-D set with another neighbour count and frame count: its
+    # launches use other shared-memory sizes of the same kernels
+    mi = VariogramModel(0.1, [Structure("exponential", 1.0, 150.0)])
+    ci = uniform_points(15000, 2, 505, [1000.0, 1000.0])
+    vi = 5.0 + G.rff_field(ci, mi, 512, 8)
+    ki = G.Kriging.new(G.PointSet(ci, vi), mi, G.KrigingConfig(max_neighbors=48))
     cv, vv = O.test_field_2d(5000, 503)
     plan = G.VecchiaPlan(G.PointSet(cv, vv), 20)
 
     srv = G.Server(mem_budget_bytes=1 << 30, executors=3)
     d2, d3, dv = srv.add_kriging(k2), srv.add_kriging(k3), srv.add_vecchia(plan)
+    di = srv.add_kriging(ki)
 
     rng = np.random.default_rng(7)
     jobs = []
@@ -46,7 +53,9 @@ def test_mixed_requests_match_their_results_alone():
             jobs.append(("ll", dv, mdl))
         else:
             nt = int(np.exp(rng.uniform(0.0, np.log(30000))))
-            if q % 2 == 0:
+            if q % 6 == 0:
+                jobs.append(("p", di, rng.uniform(0, 1000, size=(nt, 2))))
+            elif q % 2 == 0:
                 jobs.append(("p", d2, rng.uniform(0, 1000, size=(nt, 2))))
             else:
                 jobs.append(("p", d3, rng.uniform(0, 1, size=(nt, 3)) * [1000.0, 1000.0, 200.0]))
@@ -68,7 +77,7 @@ def test_mixed_requests_match_their_results_alone():
             assert r.out[1][0] == st[0] == 0
             assert r.out[0][0] == alone[0]
         else:
-            k, vals, sill = (k2, v2, 1.0) if ds == d2 else (k3, v3, 0.95)
+            k, vals, sill = {d2: (k2, v2, 1.0), d3: (k3, v3, 0.95), di: (ki, vi, 1.1)}[ds]
             alone = k.predict_many(arg, "mixed", full=True)
             v, var, st = r.out
             assert (st == alone.status).all()
