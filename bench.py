@@ -399,6 +399,9 @@ def vecchia_bench(args, log):
         ll, st = plan.loglik(cands)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
+    from geostat_rs import _abi
+    phase = G.last_timings()
+    resolved = int(_abi.load().gs_last_fallbacks())
     t1 = time.perf_counter()
     ll64, _ = plan.loglik(cands, precision="fp64")
     dt64 = time.perf_counter() - t1
@@ -418,6 +421,9 @@ def vecchia_bench(args, log):
            "single_candidate_points_per_s": n / dt1,
            "mixed_vs_fp64_max_rel_diff": float(np.max(np.abs(ll - ll64) / np.abs(ll64))),
            "gradient_points_per_s": n * len(gc) / dtg, "gradient_status_ok": bool((gst == 0).all()),
+           "mixed_kernel_ms": phase[1], "fp64_resolve_ms": phase[2],
+           "fp64_resolved_systems": resolved,
+           "fp64_resolved_fraction": resolved / (n * len(cands)),
            "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
     # joint prediction at args.vpred_n targets conditioning on the same data (m = 30)
     if args.vpred_n > 0:

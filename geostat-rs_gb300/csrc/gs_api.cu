@@ -69,6 +69,12 @@ void DevBuf::release() {
 DevBuf::~DevBuf() { release(); }
 
 static thread_local double g_timings[4] = {0, 0, 0, 0};
+static thread_local int64_t g_fallbacks = 0;
+
+void set_last_timings(const double* ms4, int64_t fallbacks) {
+  for (int i = 0; i < 4; ++i) g_timings[i] = ms4[i];
+  g_fallbacks = fallbacks;
+}
 
 }  // namespace gs
 
@@ -110,6 +116,8 @@ int gs_last_timings(double* ms4) {
   for (int i = 0; i < 4; ++i) ms4[i] = g_timings[i];
   return GS_OK;
 }
+
+int64_t gs_last_fallbacks(void) { return g_fallbacks; }
 
 // data.rs:15-83 (+ duplicate_coord_pair, data.rs:384-397).
 int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, const double* z,
@@ -528,6 +536,7 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) GS_CUDA(cudaEventCreate(&ev[i]));
   float t_search = 0, t_mixed = 0, t_fp64 = 0;
+  int64_t n_resolved = 0;
   GS_CUDA(cudaEventRecord(ev[0], stream));
   int rc = GS_OK;
   for (int64_t c0 = 0; c0 < nt && !rc; c0 += chunk) {
@@ -580,6 +589,7 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
                                          (int64_t*)nsel.ptr, cn, stream));
       GS_CUDA(cudaMemcpyAsync(&nflag, nsel.ptr, 8, cudaMemcpyDeviceToHost, stream));
       GS_CUDA(cudaStreamSynchronize(stream));
+      n_resolved += nflag;
       if (nflag > 0) {
         ca.nmax = nmax_all;
         ca.tlist = (const int64_t*)tlist.ptr;
@@ -612,6 +622,7 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   g_timings[1] = t_mixed;
   g_timings[2] = t_fp64;
   g_timings[3] = tot;
+  g_fallbacks = n_resolved;
   if (rc) return rc;
   GS_CUDA(cudaStreamSynchronize(stream));
   return GS_OK;

@@ -129,8 +129,7 @@ __device__ __forceinline__ df df_sqrt(df s) {
 // implementation of the exponential function in IEEE floating-point
 // arithmetic", ACM TOMS 15(2), 1989: d = n*ln2/256 + r with |r| <= ln2/512,
 // exp(-d) = 2^(-n/256) * exp(-r).  2^(-j/256) comes from a 256-entry df table;
-// exp(-r) = 1 - r + r^2 (1/2 - r/6 + r^2/24) with the polynomial part in FP32
-// (its terms are below 1e-6).  ln2/256 is split as l1 (9 significant bits, so
+// exp(-r) = 1 - r + r^2/2 - r^3/6 + r^4/24 with r^2/2 in double-float.  ln2/256 is split as l1 (9 significant bits, so
 // n*l1 is exact for n < 2^15, i.e. d < 88) + l2 + l3; n*l2 is formed exactly.
 struct ExpTable {
   df v[256];  // 2^(-j/256) as (hi, lo) pairs: one 8-byte load per lookup
@@ -153,9 +152,15 @@ __device__ __forceinline__ df df_expneg(df din, const ExpTable& tab, const ExpCo
   const df nl2 = two_prod(nf, k.l2);
   df r = two_sum(t1, -nl2.hi);
   r = fast_two_sum(r.hi, __fadd_rn(r.lo, __fsub_rn(__fsub_rn(d.lo, nl2.lo), __fmul_rn(nf, k.l3))));
+  // exp(-r) = 1 - r + r^2/2 - r^3/6 + r^4/24 for |r| <= ln2/512 (the next
+  // term is below 4e-17).  r^2/2 (up to ~9e-7) is formed as a double-float --
+  // its FP32 rounding alone would cost ~5e-14 -- and the cubic and quartic
+  // terms (below 4e-10) go in FP32.
   const float t = r.hi;
-  const float poly = t * t * (0.5f + t * (-(1.0f / 6.0f) + t * (1.0f / 24.0f)));
-  const df q = df_add_f(df_neg(r), poly);
+  const df r2 = two_prod(t, t);  // exact
+  const float small = __fmaf_rn(t * t * t, -(1.0f / 6.0f) + t * (1.0f / 24.0f), t * r.lo);
+  const df half = fast_two_sum(0.5f * r2.hi, __fmaf_rn(0.5f, r2.lo, small));
+  const df q = df_add(df_neg(r), half);
   const df e = df_add_f(q, 1.0f);
   const int j = n & 255;
   const int kk = n >> 8;

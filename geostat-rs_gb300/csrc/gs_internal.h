@@ -16,6 +16,10 @@ void count_launch(int n);
 // returning memory to the driver between calls).
 int ensure_device();
 
+// Records the phase timings (ms: search, mixed solve, FP64 re-solve, whole
+// call) and the number of FP64 re-solved systems of this thread's last call.
+void set_last_timings(const double* ms4, int64_t fallbacks);
+
 // Allows launches of `func` with `bytes` of dynamic shared memory on the
 // current device.  The per-function limit is process-wide state, so it is
 // only ever raised (under a lock): a thread launching with a smaller size

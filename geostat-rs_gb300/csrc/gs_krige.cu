@@ -26,6 +26,7 @@
 #include "gs_internal.h"
 #include "gs_krige.cuh"
 #include "gs_rows.cuh"
+#include "gs_warp.cuh"
 #include "gs_solve.cuh"
 
 namespace gs {
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     const float nx = rows_max<R>(mx, red, slot);
     float nd_prev = nx;
     bool conv = false;
-    for (int sweep = 1; sweep <= 4 && !conv; ++sweep) {
+    for (int sweep = 1; sweep <= kMaxRefineSweeps && !conv; ++sweep) {
       X[i] = x1;
       rows_bar<R>();
       // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q over occupied slots,
@@ -479,6 +480,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       else if (sweep >= 2) {
         const float rho = nd / nd_prev;
         if (rho < 0.5f && rho * nd <= 1e-13f * nx) conv = true;
+        else if (!(rho < 0.5f)) break;  // no longer contracting: FP64 re-solve
       }
       nd_prev = nd;
     }

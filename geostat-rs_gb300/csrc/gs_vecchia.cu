@@ -615,6 +615,15 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   int64_t nfl = 0;
   DevBuf list;
   const bool mixed = precision != GS_PREC_FP64 && M <= GS_MIXED_MAX_NEIGHBORS;
+  cudaEvent_t ev[4];
+  for (int e = 0; e < 4; ++e) GS_CUDA(cudaEventCreate(&ev[e]));
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      for (int q = 0; q < 4; ++q) cudaEventDestroy(e[q]);
+    }
+  } ev_guard{ev};
+  GS_CUDA(cudaEventRecord(ev[0], s));
   if (mixed) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -644,6 +653,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     }
     GS_CUDA(cudaGetLastError());
     count_launch(1);
+    GS_CUDA(cudaEventRecord(ev[1], s));
     // compact flagged (candidate, point) pairs
     DevBuf nsel, tmp;
     GS_TRY(nsel.alloc(8, s));
@@ -659,6 +669,8 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     GS_CUDA(cudaMemcpyAsync(&nfl, nsel.ptr, 8, cudaMemcpyDeviceToHost, s));
     GS_CUDA(cudaStreamSynchronize(s));
   }
+  if (!mixed) GS_CUDA(cudaEventRecord(ev[1], s));
+  GS_CUDA(cudaEventRecord(ev[2], s));
   if (!mixed || nfl > 0) {
     const int64_t work = mixed ? nfl : ncand * n;
     const int64_t per = ((int64_t)M * M + 2 * (int64_t)M) * 8;
@@ -677,6 +689,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     GS_CUDA(cudaGetLastError());
     count_launch(1);
   }
+  GS_CUDA(cudaEventRecord(ev[3], s));
   const int64_t chunk = 8192;
   const int nblk = (int)((n + chunk - 1) / chunk);
   GS_TRY(partial.alloc((size_t)nblk * ncand * 8, s));
@@ -690,6 +703,14 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   GS_CUDA(cudaMemcpyAsync(hll.data(), out.ptr, ncand * 8, cudaMemcpyDeviceToHost, s));
   GS_CUDA(cudaMemcpyAsync(hst.data(), cstat.ptr, ncand * 4, cudaMemcpyDeviceToHost, s));
   GS_CUDA(cudaStreamSynchronize(s));
+  {
+    float a01 = 0, a23 = 0, a03 = 0;
+    cudaEventElapsedTime(&a01, ev[0], ev[1]);
+    cudaEventElapsedTime(&a23, ev[2], ev[3]);
+    cudaEventElapsedTime(&a03, ev[0], ev[3]);
+    const double ms4[4] = {0.0, mixed ? (double)a01 : 0.0, (double)a23, (double)a03};
+    set_last_timings(ms4, mixed ? nfl : ncand * n);
+  }
   for (int64_t c = 0; c < ncand; ++c) {
     if (!valid[c]) continue;
     if (hst[c] != 0) {

@@ -114,6 +114,11 @@ __device__ __forceinline__ bool warp_factor(const df* A, int N, int lane, WarpFa
   return true;
 }
 
+// Refinement sweeps before a system is handed to the FP64 solver; a sweep
+// that no longer halves the correction ends the refinement earlier (the
+// double-float residual of an ill-conditioned system has reached its limit).
+constexpr int kMaxRefineSweeps = 8;
+
 // Solves A x = B with the factorisation f and refines to ~1e-13 relative; on
 // success W.xd[i] holds x_i.  Returns false (uniformly) when the refinement
 // stalls.
@@ -129,7 +134,7 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
   df x = df_make(lane < N ? -y : 0.0f, 0.0f);
   const float nx = warp_max_f(fabsf(x.hi));
   float nd_prev = nx;
-  for (int sweep = 1; sweep <= 4; ++sweep) {
+  for (int sweep = 1; sweep <= kMaxRefineSweeps; ++sweep) {
     // residual of row `lane`: b - A x, compensated, x broadcast as df
     __syncwarp();
     W.xd[lane] = x;
@@ -167,6 +172,7 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
       __syncwarp();
       return true;
     }
+    if (sweep >= 2 && !(nd < 0.5f * nd_prev)) return false;  // no longer contracting
     nd_prev = nd;
   }
   return false;

@@ -281,10 +281,15 @@ void gs_rng_normal(uint64_t seed, int64_t count, double* out);
 int gs_synth_rff_field(int dim, int64_t n, const double* x, const double* y, const double* z,
                        const gs_model* model, int64_t n_features, uint64_t seed, double* out);
 
-/* Timing of the last gs_kriging_predict_* call on this host thread (ms of
- * device time per phase, measured with CUDA events on the call's stream):
- * [0] search, [1] mixed solve, [2] FP64 re-solve, [3] whole call. */
+/* Timing of the last gs_kriging_predict_* or Vecchia log-likelihood call on
+ * this host thread (ms of device time per phase, measured with CUDA events on
+ * the call's stream): [0] search, [1] mixed solve, [2] FP64 re-solve,
+ * [3] whole call. */
 int gs_last_timings(double* ms4);
+/* Systems the last gs_kriging_predict_* or Vecchia log-likelihood call on
+ * this host thread solved with the FP64 kernels (mixed-precision systems
+ * the refinement could not certify, or all of them at GS_PREC_FP64). */
+int64_t gs_last_fallbacks(void);
 
 /* Measurement helpers (no reference counterpart): sustained CUDA-core FMA
  * throughput in TFLOP/s for FP32 (precision 0), FP64 (1) or packed FP32x2
