@@ -171,12 +171,18 @@ __device__ __forceinline__ int shell_size(int r) {
 // is <= T has an FP32 squared distance (from origin-relative FP32
 // coordinates) <= the returned value.  delta bounds the per-axis FP32
 // coordinate error (both roundings); the FP32 sum adds a relative 4 ulp.
-__device__ __forceinline__ float prefilter_bound(double T, double delta, int D) {
-  if (!(T < 1e300)) return __int_as_float(0x7f800000);  // +inf
-  const double sT = sqrt(T);
-  const double b = T * (1.0 + 1.0 / 1048576.0) + 2.0 * D * sT * delta + D * delta * delta +
-                   4.0 * D * 5.96e-8 * sT * delta;
-  return __double2float_ru(b * (1.0 + 1e-6));
+// Every term is positive and every operation rounds up, so the FP32 result
+// is an upper bound of the exact expression (no FP64 arithmetic).
+__device__ __forceinline__ float prefilter_bound(double T, float delta, int D) {
+  const float inf = __int_as_float(0x7f800000);
+  if (!(T < 1e300)) return inf;
+  const float t = __double2float_ru(T);
+  const float st = __fsqrt_ru(t);
+  const float sd = __fmul_ru(st, delta);
+  float b = __fmul_ru(t, 1.0f + 1.0f / 1048576.0f);
+  b = __fadd_ru(b, __fmul_ru(2.0f * (float)D * (1.0f + 2.4e-7f), sd));
+  b = __fadd_ru(b, __fmul_ru((float)D, __fmul_ru(delta, delta)));
+  return __fmul_ru(b, 1.0f + 1e-6f);
 }
 
 // Shared memory of one warp of knn_kernel: NB buffers of capb (d2, idx)
@@ -205,7 +211,7 @@ __device__ __forceinline__ bool diff_nonneg(double diff) {
 
 // Lane 0: refreshes the cached prefilter bound after a threshold changed.
 template <int NB>
-__device__ __forceinline__ void refresh_bound(const dkey* thr, float* tfs, double delta, int D,
+__device__ __forceinline__ void refresh_bound(const dkey* thr, float* tfs, float delta, int D,
                                               float r2f) {
   dkey tmax = thr[0];
 #pragma unroll
@@ -274,12 +280,14 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
     for (int d = 0; d < D; ++d) tc[d] = clamp_cell((q[d] - g.origin[d]) * g.inv_cell, g.n[d]);
     // prefilter: FP32 target coordinates and the per-axis error bound
     float qf[3] = {0.0f, 0.0f, 0.0f};
-    double delta = 0.0;
+    float delta = 0.0f;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       const double rel = q[d] - g.origin[d];
       qf[d] = (float)rel;
-      delta = fmax(delta, (g.ext[d] + fabs(rel)) * (1.0 / 8388608.0) + 1e-30);
+      // (extent + |rel|) * 2^-23, rounded up
+      const float mag = __fadd_ru(g.extf[d], __double2float_ru(fabs(rel)));
+      delta = fmaxf(delta, __fadd_ru(mag * (1.0f / 8388608.0f), 1e-30f));
     }
     const float r2f = prefilter_bound(r2, delta, D);
     int maxring = 0;
@@ -354,8 +362,11 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
     }
 
     for (int ring = 0; ring <= maxring; ++ring) {
-      double rmin = fmax((double)ring - 1.0 - 1e-9, 0.0) * g.cell;
-      const dkey rmin2k = d2key(rmin * rmin);
+      // lower bound of the distance to any point of this ring, in FP32
+      // rounded down (with a 2^-20 relative margin for the cell placement)
+      const float rmin = __fmul_rd(__fmul_rd((float)max(ring - 1, 0), g.cellf_lo),
+                                   1.0f - 1.0f / 1048576.0f);
+      const dkey rmin2k = d2key((double)__fmul_rd(rmin, rmin));
       unsigned active = 0;
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
@@ -651,7 +662,17 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
   GS_TRY(dalloc(&g->d_sidx, n));
   GS_TRY(dalloc(&g->d_cstart, total + 1));
   GS_TRY(dalloc(&g->d_f, 3 * n));
-  for (int d = 0; d < 3; ++d) G.ext[d] = d < dim ? ext[d] : 0.0;
+  for (int d = 0; d < 3; ++d) {
+    G.ext[d] = d < dim ? ext[d] : 0.0;
+    float f = (float)G.ext[d];
+    if ((double)f < G.ext[d]) f = std::nextafter(f, INFINITY);
+    G.extf[d] = f;
+  }
+  {
+    float f = (float)G.cell;
+    if ((double)f > G.cell) f = std::nextafter(f, -INFINITY);
+    G.cellf_lo = f;
+  }
   if (dim == 2)
     gather_kernel<2><<<blocks, threads, 0, stream>>>(n, vals2, tx, ty, tz, g->d_sx, g->d_sy,
                                                      g->d_sz, g->d_sidx, G, g->d_f);

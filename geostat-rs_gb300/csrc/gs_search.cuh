@@ -34,6 +34,8 @@ struct GridDev {
   const float* fy;
   const float* fz;
   double ext[3];
+  float extf[3];   // ext rounded up to FP32
+  float cellf_lo;  // cell rounded down to FP32
 };
 
 struct SearchParams {
