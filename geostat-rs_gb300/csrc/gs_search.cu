@@ -186,10 +186,11 @@ __device__ __forceinline__ float prefilter_bound(double T, float delta, int D) {
 }
 
 // Shared memory of one warp of knn_kernel: NB buffers of capb (d2, idx)
-// entries, then NB thresholds, counts and dirty flags, then the cached
-// prefilter bound.  Used by both the kernel and its launch.
+// entries, then NB thresholds, counts and dirty flags, the cached prefilter
+// bound, and a queue of 64 prefilter survivors.  Used by both the kernel and
+// its launch.
 __host__ __device__ inline size_t knn_per_warp(int NB, int capb) {
-  return (size_t)NB * capb * 12 + (size_t)NB * 16 + 16;
+  return (size_t)NB * capb * 12 + (size_t)NB * 16 + 16 + 64 * sizeof(uint32_t);
 }
 
 // Squared distances are never negative (and never -0: they are sums of
@@ -266,6 +267,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
   int* cnt = reinterpret_cast<int*>(thr + NB);
   int* dirty = cnt + NB;
   float* tfs = reinterpret_cast<float*>(dirty + NB);  // cached prefilter bound
+  uint32_t* sq = reinterpret_cast<uint32_t*>(tfs + 4);  // prefilter survivors (64)
   const double kInf = __longlong_as_double(0x7ff0000000000000ll);
   const double r2 = p.has_radius ? p.r2 : kInf;
   const dkey r2k = d2key(r2);
@@ -361,6 +363,62 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
       maxring = -1;  // skip the ring walk
     }
 
+    // Exact squared distance in the reference's operation order and insertion
+    // into the candidate buffers, for one batch of prefilter survivors
+    // (called by the whole warp).
+    auto process = [&](uint32_t pi, bool valid) {
+      double d2 = kInf;
+      uint32_t oid = 0;
+      int ob = 0;
+      if (valid) {
+        const double px = g.sx[pi], py = g.sy[pi];
+        const double dx = __dsub_rn(px, q[0]);
+        const double dy = __dsub_rn(py, q[1]);
+        d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        if (OCT) ob = (diff_nonneg(dx) ? 1 : 0) | (diff_nonneg(dy) ? 2 : 0);
+        if (D == 3) {
+          const double pz = g.sz[pi];
+          const double dz = __dsub_rn(pz, q[2]);
+          d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
+          if (OCT) ob |= (diff_nonneg(dz) ? 4 : 0);
+        }
+        oid = g.sidx[pi];
+      }
+      const dkey k2 = d2key(d2);
+      const bool inr = valid && k2 <= r2k && (!RANKED || (int64_t)oid < qrank);
+      if (p.unbounded) inrad += __popc(__ballot_sync(kFull, inr));
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        bool want = inr && (ob == b) && k2 <= thr[b];
+        unsigned m = __ballot_sync(kFull, want);
+        if (!m) continue;
+        if (cnt[b] + __popc(m) > capb) {
+          warp_sort(bd2 + b * capb, bid + b * capb, cnt[b], capb, lane);
+          if (lane == 0) {
+            cnt[b] = min(cnt[b], kb);
+            if (cnt[b] >= kb) thr[b] = bd2[b * capb + kb - 1];
+            dirty[b] = 0;
+            refresh_bound<NB>(thr, tfs, delta, D, r2f);
+          }
+          __syncwarp();
+          want = want && k2 <= thr[b];
+          m = __ballot_sync(kFull, want);
+        }
+        if (want) {
+          int slot = cnt[b] + __popc(m & ((1u << lane) - 1u));
+          bd2[b * capb + slot] = k2;
+          bid[b * capb + slot] = oid;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          cnt[b] += __popc(m);
+          dirty[b] = 1;
+        }
+        __syncwarp();
+      }
+    };
+    int qn = 0;  // queued survivors (warp-uniform)
+
     for (int ring = 0; ring <= maxring; ++ring) {
       // lower bound of the distance to any point of this ring, in FP32
       // rounded down (with a 2^-20 relative margin for the cell placement)
@@ -428,9 +486,6 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
           const uint32_t sst = __shfl_sync(kFull, cst, src);
           const int sex = __shfl_sync(kFull, excl, src);
           bool valid = my < tot;
-          double d2 = kInf;
-          uint32_t oid = 0;
-          int ob = 0;
           const uint32_t pi = sst + (uint32_t)(my - sex);
           if (valid) {
             // FP32 prefilter against the loosest live threshold
@@ -445,53 +500,27 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
             }
             valid = d2f <= tf;
           }
-          if (valid) {
-            const double px = g.sx[pi], py = g.sy[pi];
-            const double dx = __dsub_rn(px, q[0]);
-            const double dy = __dsub_rn(py, q[1]);
-            d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-            if (OCT) ob = (diff_nonneg(dx) ? 1 : 0) | (diff_nonneg(dy) ? 2 : 0);
-            if (D == 3) {
-              const double pz = g.sz[pi];
-              const double dz = __dsub_rn(pz, q[2]);
-              d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
-              if (OCT) ob |= (diff_nonneg(dz) ? 4 : 0);
-            }
-            oid = g.sidx[pi];
-          }
-          const dkey k2 = d2key(d2);
-          const bool inr = valid && k2 <= r2k && (!RANKED || (int64_t)oid < qrank);
-          if (p.unbounded) inrad += __popc(__ballot_sync(kFull, inr));
-#pragma unroll
-          for (int b = 0; b < NB; ++b) {
-            bool want = inr && (ob == b) && k2 <= thr[b];
-            unsigned m = __ballot_sync(kFull, want);
-            if (!m) continue;
-            if (cnt[b] + __popc(m) > capb) {
-              warp_sort(bd2 + b * capb, bid + b * capb, cnt[b], capb, lane);
-              if (lane == 0) {
-                cnt[b] = min(cnt[b], kb);
-                if (cnt[b] >= kb) thr[b] = bd2[b * capb + kb - 1];
-                dirty[b] = 0;
-                refresh_bound<NB>(thr, tfs, delta, D, r2f);
-              }
-              __syncwarp();
-              want = want && k2 <= thr[b];
-              m = __ballot_sync(kFull, want);
-            }
-            if (want) {
-              int slot = cnt[b] + __popc(m & ((1u << lane) - 1u));
-              bd2[b * capb + slot] = k2;
-              bid[b * capb + slot] = oid;
-            }
+          // queue the survivors; exact distances run on full batches of 32
+          const unsigned m = __ballot_sync(kFull, valid);
+          if (valid) sq[qn + __popc(m & ((1u << lane) - 1u))] = pi;
+          qn += __popc(m);
+          __syncwarp();
+          if (qn >= 32) {
+            const uint32_t bpi = sq[lane];
             __syncwarp();
-            if (lane == 0) {
-              cnt[b] += __popc(m);
-              dirty[b] = 1;
-            }
+            if (lane < qn - 32) sq[lane] = sq[32 + lane];
+            qn -= 32;
             __syncwarp();
+            process(bpi, true);
           }
         }
+      }
+      if (qn > 0) {  // the ring's last survivors
+        const bool v = lane < qn;
+        const uint32_t bpi = v ? sq[lane] : 0u;
+        qn = 0;
+        __syncwarp();
+        process(bpi, v);
       }
       // ring end: settle thresholds of buffers that reached k
 #pragma unroll
