@@ -444,10 +444,25 @@ struct PhaseTimer {
 
 namespace gs {
 
-// Search + solves for targets already on the device.
-int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
-                   const double* tz, const double* tdrift, double* value, double* variance,
-                   double* lagrange, uint8_t* status, int precision, cudaStream_t stream) {
+// Targets whose neighbour count is at most / above a threshold (binning).
+struct NbLe {
+  const int32_t* nbc;
+  int thr;
+  __host__ __device__ bool operator()(int64_t t) const { return nbc[t] <= thr; }
+};
+struct NbGt {
+  const int32_t* nbc;
+  int thr;
+  __host__ __device__ bool operator()(int64_t t) const { return nbc[t] > thr; }
+};
+
+// Search + solves for targets already on the device.  timed: phase timings,
+// FP64 re-solve count and a final synchronisation; otherwise the whole pass
+// is only enqueued on `stream` (no host synchronisation: it can be captured
+// into a CUDA graph).
+int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                 const double* tz, const double* tdrift, double* value, double* variance,
+                 double* lagrange, uint8_t* status, int precision, cudaStream_t stream, bool timed) {
   if (nt == 0) return GS_OK;
   const gs_pointset* ps = k->ps;
   const gs_kcfg& c = k->cfg;
@@ -516,37 +531,55 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   // chunking keeps the neighbour lists within a fixed budget (4 GiB: a
   // 4.19 M-target grid with 64 neighbours is one chunk)
   const int64_t chunk = std::max<int64_t>(1024, std::min<int64_t>(nt, (int64_t)(4ll << 30) / (4ll * kout + 16)));
-  DevBuf nb, nbc, flag, tlist, nsel, tmp;
+  const int64_t nchunks = (nt + chunk - 1) / chunk;
+  // uneven neighbourhoods (octant, radius) are binned by system size: the
+  // small systems run on the 32-thread kernel, the rest on the 64-thread one
+  const bool mixed = precision != GS_PREC_FP64;
+  const bool binned = mixed && kout > 32 && kout + p <= GS_MIXED_MAX_NEIGHBORS + p &&
+                      (sp.octant || sp.has_radius || sp.unbounded);
+  DevBuf nb, nbc, flag, tlist, nsel, tmp, bins, counts;
   GS_TRY(nb.alloc((size_t)chunk * kout * 4, stream));
   GS_TRY(nbc.alloc((size_t)chunk * 4, stream));
   GS_TRY(flag.alloc((size_t)chunk, stream));
   GS_TRY(tlist.alloc((size_t)chunk * 8, stream));
   GS_TRY(nsel.alloc(8, stream));
-  size_t sel_bytes = 0;
+  GS_TRY(counts.alloc((size_t)nchunks * 8, stream));
+  size_t sel_bytes = 0, bin_bytes = 0;
   GS_CUDA(cub::DeviceSelect::Flagged(nullptr, sel_bytes, thrust::counting_iterator<int64_t>(0),
                                      (uint8_t*)nullptr, (int64_t*)nullptr, (int64_t*)nullptr,
                                      (int64_t)chunk, stream));
-  GS_TRY(tmp.alloc(sel_bytes, stream));
+  if (binned) {
+    GS_CUDA(cub::DeviceSelect::If(nullptr, bin_bytes, thrust::counting_iterator<int64_t>(0),
+                                  (int64_t*)nullptr, (int64_t*)nullptr, (int64_t)chunk,
+                                  NbLe{nullptr, 32}, stream));
+    GS_TRY(bins.alloc((size_t)chunk * 2 * 8 + 16, stream));
+  }
+  GS_TRY(tmp.alloc(std::max(sel_bytes, bin_bytes), stream));
   // FP64 scratch (plain build or re-solve)
   const int64_t budget = (int64_t)2 << 30;
   const int64_t fthreads = fp64_threads_for(nmax_all, budget);
   DevBuf scratch;
   GS_TRY(scratch.alloc((size_t)fp64_scratch_doubles(nmax_all, fthreads) * 8, stream));
 
-  cudaEvent_t ev[6];
-  for (int i = 0; i < 6; ++i) GS_CUDA(cudaEventCreate(&ev[i]));
+  cudaEvent_t ev[6] = {};
+  if (timed)
+    for (int i = 0; i < 6; ++i) GS_CUDA(cudaEventCreate(&ev[i]));
+  auto mark = [&](int i) -> int {
+    if (timed) GS_CUDA(cudaEventRecord(ev[i], stream));
+    return GS_OK;
+  };
   float t_search = 0, t_mixed = 0, t_fp64 = 0;
-  int64_t n_resolved = 0;
-  GS_CUDA(cudaEventRecord(ev[0], stream));
+  GS_TRY(mark(0));
   int rc = GS_OK;
-  for (int64_t c0 = 0; c0 < nt && !rc; c0 += chunk) {
+  for (int64_t ci = 0; ci < nchunks && !rc; ++ci) {
+    const int64_t c0 = ci * chunk;
     const int64_t cn = std::min(chunk, nt - c0);
     const double* ctx = tx + c0;
     const double* cty = ty + c0;
     const double* ctz = dim == 3 ? tz + c0 : nullptr;
     int32_t* dnb = (int32_t*)nb.ptr;
     int32_t* dnbc = (int32_t*)nbc.ptr;
-    GS_CUDA(cudaEventRecord(ev[1], stream));
+    GS_TRY(mark(1));
     if (k->use_tree) {
       rc = search_launch(k->grid, k->frame, sp, cn, ctx, cty, ctz, dnb, dnbc, stream);
     } else {
@@ -555,7 +588,7 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
       rc = cudaGetLastError() == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "launch failed");
     }
     if (rc) break;
-    GS_CUDA(cudaEventRecord(ev[2], stream));
+    GS_TRY(mark(2));
     KrigeArgs ca = a;
     ca.tx = ctx;
     ca.ty = cty;
@@ -567,57 +600,86 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
     ca.out_var = variance + c0;
     ca.out_lag = lagrange ? lagrange + c0 : nullptr;
     ca.out_st = status + c0;
-    int64_t nflag = 0;
-    if (precision == GS_PREC_FP64) {
+    if (!mixed) {
       ca.nmax = nmax_all;
       ca.tlist = nullptr;
       ca.ntl = cn;
-      GS_CUDA(cudaEventRecord(ev[3], stream));
+      GS_TRY(mark(3));
       rc = krige_fp64_launch(ca, k->dm, (double*)scratch.ptr, fthreads, stream);
       if (rc) break;
-      GS_CUDA(cudaEventRecord(ev[4], stream));
+      GS_TRY(mark(4));
     } else {
       ca.nmax = std::min(nmax_all, GS_MIXED_MAX_NEIGHBORS + p);
       ca.tlist = nullptr;
       ca.ntl = cn;
-      rc = krige_mixed_launch(ca, k->dm, (uint8_t*)flag.ptr, 4, stream);
+      if (binned) {
+        int64_t* lists = (int64_t*)bins.ptr;
+        int64_t* cnts = lists + 2 * chunk;
+        size_t b = bin_bytes;
+        GS_CUDA(cub::DeviceSelect::If(tmp.ptr, b, thrust::counting_iterator<int64_t>(0), lists,
+                                      cnts, cn, NbLe{dnbc, 32}, stream));
+        b = bin_bytes;
+        GS_CUDA(cub::DeviceSelect::If(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
+                                      lists + chunk, cnts + 1, cn, NbGt{dnbc, 32}, stream));
+        KrigeArgs sa = ca;
+        sa.tlist = lists;
+        sa.ntl_dev = cnts;
+        rc = krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 32, stream);
+        if (rc) break;
+        sa.tlist = lists + chunk;
+        sa.ntl_dev = cnts + 1;
+        rc = krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 64, stream);
+      } else {
+        rc = krige_mixed_launch(ca, k->dm, (uint8_t*)flag.ptr, 0, stream);
+      }
       if (rc) break;
-      GS_CUDA(cudaEventRecord(ev[3], stream));
+      GS_TRY(mark(3));
+      // systems the refinement could not certify: FP64 re-solve over the
+      // flagged list, its length read on the device (no host round trip)
       size_t b = sel_bytes;
       GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
                                          (uint8_t*)flag.ptr, (int64_t*)tlist.ptr,
                                          (int64_t*)nsel.ptr, cn, stream));
-      GS_CUDA(cudaMemcpyAsync(&nflag, nsel.ptr, 8, cudaMemcpyDeviceToHost, stream));
-      GS_CUDA(cudaStreamSynchronize(stream));
-      n_resolved += nflag;
-      if (nflag > 0) {
-        ca.nmax = nmax_all;
-        ca.tlist = (const int64_t*)tlist.ptr;
-        ca.ntl = nflag;
-        rc = krige_fp64_launch(ca, k->dm, (double*)scratch.ptr, fthreads, stream);
-        if (rc) break;
-      }
-      GS_CUDA(cudaEventRecord(ev[4], stream));
+      GS_CUDA(cudaMemcpyAsync((int64_t*)counts.ptr + ci, nsel.ptr, 8, cudaMemcpyDeviceToDevice,
+                              stream));
+      ca.nmax = nmax_all;
+      ca.tlist = (const int64_t*)tlist.ptr;
+      ca.ntl = cn;
+      ca.ntl_dev = (const int64_t*)nsel.ptr;
+      rc = krige_fp64_launch(ca, k->dm, (double*)scratch.ptr, fthreads, stream);
+      if (rc) break;
+      GS_TRY(mark(4));
     }
-    GS_CUDA(cudaEventSynchronize(ev[4]));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ev[1], ev[2]);
-    t_search += ms;
-    if (precision == GS_PREC_FP64) {
-      cudaEventElapsedTime(&ms, ev[3], ev[4]);
-      t_fp64 += ms;
-    } else {
-      cudaEventElapsedTime(&ms, ev[2], ev[3]);
-      t_mixed += ms;
-      cudaEventElapsedTime(&ms, ev[3], ev[4]);
-      t_fp64 += ms;
+    if (timed) {
+      GS_CUDA(cudaEventSynchronize(ev[4]));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[1], ev[2]);
+      t_search += ms;
+      if (!mixed) {
+        cudaEventElapsedTime(&ms, ev[3], ev[4]);
+        t_fp64 += ms;
+      } else {
+        cudaEventElapsedTime(&ms, ev[2], ev[3]);
+        t_mixed += ms;
+        cudaEventElapsedTime(&ms, ev[3], ev[4]);
+        t_fp64 += ms;
+      }
     }
   }
-  GS_CUDA(cudaEventRecord(ev[5], stream));
+  if (!timed) return rc;  // enqueued only: the caller synchronises
+  GS_TRY(mark(5));
   GS_CUDA(cudaEventSynchronize(ev[5]));
   float tot = 0;
   cudaEventElapsedTime(&tot, ev[0], ev[5]);
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  int64_t n_resolved = nt;
+  if (mixed) {
+    std::vector<int64_t> hc(nchunks, 0);
+    GS_CUDA(cudaMemcpyAsync(hc.data(), counts.ptr, nchunks * 8, cudaMemcpyDeviceToHost, stream));
+    GS_CUDA(cudaStreamSynchronize(stream));
+    n_resolved = 0;
+    for (int64_t c : hc) n_resolved += c;
+  }
   g_timings[0] = t_search;
   g_timings[1] = t_mixed;
   g_timings[2] = t_fp64;
@@ -626,6 +688,13 @@ int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const doub
   if (rc) return rc;
   GS_CUDA(cudaStreamSynchronize(stream));
   return GS_OK;
+}
+
+int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
+                   const double* tz, const double* tdrift, double* value, double* variance,
+                   double* lagrange, uint8_t* status, int precision, cudaStream_t stream) {
+  return predict_pass(k, nt, tx, ty, tz, tdrift, value, variance, lagrange, status, precision,
+                      stream, true);
 }
 
 }  // namespace gs
@@ -658,6 +727,21 @@ int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double
     return fail(GS_ERR_INVALID_PARAMETER, "predict_with_drift requires KrigingMethod::ExternalDrift");
   cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
   return predict_device(k, nt, tx, ty, tz, tdrift, value, variance, lagrange, status, precision, s);
+}
+
+int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double* tx,
+                                  const double* ty, const double* tz, const double* tdrift,
+                                  double* value, double* variance, double* lagrange,
+                                  uint8_t* status, int precision, void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (k->cfg.method == GS_EXTERNAL_DRIFT && !tdrift)
+    return fail(GS_ERR_INVALID_PARAMETER, "external drift kriging requires predict_with_drift");
+  if (k->cfg.method != GS_EXTERNAL_DRIFT && tdrift)
+    return fail(GS_ERR_INVALID_PARAMETER, "predict_with_drift requires KrigingMethod::ExternalDrift");
+  if (nt == 0) return GS_OK;
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  return predict_pass(k, nt, tx, ty, tz, tdrift, value, variance, lagrange, status, precision, s,
+                      false);
 }
 
 int gs_kriging_predict_many(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,

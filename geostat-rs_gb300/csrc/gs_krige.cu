@@ -173,8 +173,9 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
   int my_idx = -1;  // data point in this thread's slot
   __syncthreads();
 
-  for (int64_t r0 = (int64_t)blockIdx.x * kRowsRun; r0 < a.ntl; r0 += (int64_t)gridDim.x * kRowsRun) {
-  const int64_t r1 = r0 + kRowsRun < a.ntl ? r0 + kRowsRun : a.ntl;
+  const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
+  for (int64_t r0 = (int64_t)blockIdx.x * kRowsRun; r0 < ntl; r0 += (int64_t)gridDim.x * kRowsRun) {
+  const int64_t r1 = r0 + kRowsRun < ntl ? r0 + kRowsRun : ntl;
   for (int64_t it = r0; it < r1; ++it) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
     const int n = a.nbc[t];
@@ -530,7 +531,8 @@ __global__ void __launch_bounds__(128) krige_fp64_kernel(KrigeArgs a, DevModel m
   double* Bv = scratch + (int64_t)NMAX * NMAX * T + tid;  // rhs / solution
   double* B0 = Bv + (int64_t)NMAX * T;                     // original rhs
   const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
-  for (int64_t it = tid; it < a.ntl; it += T) {
+  const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
+  for (int64_t it = tid; it < ntl; it += T) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
     const int n = a.nbc[t];
     const int p = a.p;
@@ -711,14 +713,14 @@ static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   return GS_OK;
 }
 
-int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int /*unused*/,
+int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int force_rows,
                        cudaStream_t stream) {
   if (a.ntl == 0) return GS_OK;
   ensure_tables();
   int nf = 1;
   for (int s = 0; s < m.ns; ++s) nf += m.s[s].aniso ? 1 : 0;
   const int nb = a.nmax - a.p;  // neighbour slots
-  const bool small = nb <= 32;
+  const bool small = force_rows ? force_rows == 32 : nb <= 32;
   const bool wide = a.p > 4;
   if (a.dim == 2) {
     if (small) return wide ? launch_rows<2, 32, 12>(a, m, flag, nf, stream)

@@ -46,13 +46,16 @@ struct KrigeArgs {
   double* out_lag;           // may be null
   uint8_t* out_st;
   const int64_t* tlist;      // targets to process (null: 0..nt-1)
-  int64_t ntl;
+  int64_t ntl;               // number of them (an upper bound when ntl_dev is set)
+  const int64_t* ntl_dev;    // the number on the device, read by the kernel, or null
 };
 
 // Mixed-precision kernel for systems with n <= 64 neighbours and at most
 // GS_MIXED_MAX_DRIFT drift terms.  Systems it cannot certify are marked in
 // `flag` (1 = re-solve in FP64).
-int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int warps_per_block,
+// force_rows: 0 picks the block size from the neighbour slots (32 or 64
+// threads), 32 / 64 forces it (binned launches).
+int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int force_rows,
                        cudaStream_t stream);
 // Plain FP64 kernel, one system per thread (also the re-solve path).
 // scratch must hold fp64_scratch_doubles(nmax, threads) doubles.

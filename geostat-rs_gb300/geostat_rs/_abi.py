@@ -69,6 +69,8 @@ SIGNATURES = {
                                        _vp]),
     "gs_kriging_predict_many_device": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                               _int, _vp]),
+    "gs_kriging_predict_many_async": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                             _int, _vp]),
     "gs_kriging_predict_fp64_noalloc": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                                _vp, _vp]),
     "gs_last_fallbacks": (_i64, []),

@@ -275,11 +275,15 @@ class Kriging:
         return idx.reshape(nt, kcap), cnt
 
     def predict_device(self, nt, x_ptr, y_ptr, z_ptr, v_ptr, var_ptr, st_ptr,
-                       precision="mixed", stream=None, tdrift_ptr=None, lag_ptr=None):
-        """Device-pointer variant (inputs/outputs already in HBM)."""
-        rc = _abi.load().gs_kriging_predict_many_device(
-            self._h, nt, x_ptr, y_ptr, z_ptr, tdrift_ptr, v_ptr, var_ptr, lag_ptr, st_ptr,
-            PRECISIONS[precision], stream)
+                       precision="mixed", stream=None, tdrift_ptr=None, lag_ptr=None,
+                       asynchronous=False):
+        """Device-pointer variant (inputs/outputs already in HBM).  With
+        ``asynchronous`` the call only enqueues its work on ``stream`` (it can
+        be captured into a CUDA graph)."""
+        fn = (_abi.load().gs_kriging_predict_many_async if asynchronous
+              else _abi.load().gs_kriging_predict_many_device)
+        rc = fn(self._h, nt, x_ptr, y_ptr, z_ptr, tdrift_ptr, v_ptr, var_ptr, lag_ptr, st_ptr,
+                PRECISIONS[precision], stream)
         _abi.check(rc)
 
     def close(self):

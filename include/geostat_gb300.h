@@ -159,6 +159,19 @@ int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double
                                    const double* ty, const double* tz, const double* tdrift,
                                    double* value, double* variance, double* lagrange,
                                    uint8_t* status, int precision, void* stream);
+/* Same as gs_kriging_predict_many_device, but the call only enqueues its
+ * work on `stream` (NULL: the predictor's stream) and never waits for the
+ * device: no phase timings and no re-solve count are recorded.  Targets whose
+ * double-float refinement fails are re-solved in FP64 with the length of
+ * their list read on the device, so the whole pass can be captured into a
+ * CUDA graph (stream capture) and replayed; its temporary buffers are
+ * stream-ordered allocations.  Make one ordinary call before capturing
+ * (it sets up constant tables and kernel attributes).  No counterpart in the
+ * reference: the batching entry of predict_many for serving loops. */
+int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double* tx,
+                                  const double* ty, const double* tz, const double* tdrift,
+                                  double* value, double* variance, double* lagrange,
+                                  uint8_t* status, int precision, void* stream);
 /* Allocation-free FP64 prediction (no counterpart in the reference).  The
  * same results as gs_kriging_predict_many_device with GS_PREC_FP64, for
  * callers that may not allocate device memory while they predict: the
