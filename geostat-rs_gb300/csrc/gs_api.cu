@@ -456,6 +456,27 @@ struct NbGt {
   __host__ __device__ bool operator()(int64_t t) const { return nbc[t] > thr; }
 };
 
+// Calls with at least this many targets are autotuned (per size class).
+constexpr int64_t kTuneMinTargets = 65536;
+// Targets of the first chunk the candidates are timed on.
+constexpr int64_t kTuneSample = 262144;
+
+int size_class(int64_t nt) {
+  int c = 0;
+  while ((nt >> (c + 1)) > 0) ++c;
+  return c;
+}
+
+// Launch shape without measurement: the longest run that still gives every
+// SM a few blocks.
+Tiles default_tiles(int64_t nt, bool binnable) {
+  Tiles t;
+  t.bins = binnable ? 1 : 0;
+  t.run = 64;
+  while (t.run > 8 && (nt + t.run - 1) / t.run < 152 * 4) t.run >>= 1;
+  return t;
+}
+
 // Search + solves for targets already on the device.  timed: phase timings,
 // FP64 re-solve count and a final synchronisation; otherwise the whole pass
 // is only enqueued on `stream` (no host synchronisation: it can be captured
@@ -535,8 +556,20 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   // uneven neighbourhoods (octant, radius) are binned by system size: the
   // small systems run on the 32-thread kernel, the rest on the 64-thread one
   const bool mixed = precision != GS_PREC_FP64;
-  const bool binned = mixed && kout > 32 && kout + p <= GS_MIXED_MAX_NEIGHBORS + p &&
-                      (sp.octant || sp.has_radius || sp.unbounded);
+  const bool binnable = mixed && kout > 32 && kout <= GS_MIXED_MAX_NEIGHBORS &&
+                        (sp.octant || sp.has_radius || sp.unbounded);
+  // launch shape: pinned, tuned earlier for this size class, tuned now on
+  // the first chunk (timed calls only), or the default
+  Tiles tiles = default_tiles(nt, binnable);
+  bool tune_now = false;
+  if (mixed) {
+    std::lock_guard<std::mutex> lk(k->tiles_mu);
+    auto it = k->tiles.find(size_class(nt));
+    if (k->pinned.run > 0) tiles = k->pinned;
+    else if (it != k->tiles.end()) tiles = it->second;
+    else tune_now = timed && nt >= kTuneMinTargets;
+  }
+  const bool binned = binnable;
   DevBuf nb, nbc, flag, tlist, nsel, tmp, bins, counts;
   GS_TRY(nb.alloc((size_t)chunk * kout * 4, stream));
   GS_TRY(nbc.alloc((size_t)chunk * 4, stream));
@@ -611,27 +644,62 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     } else {
       ca.nmax = std::min(nmax_all, GS_MIXED_MAX_NEIGHBORS + p);
       ca.tlist = nullptr;
-      ca.ntl = cn;
-      if (binned) {
+      // mixed solves of the chunk's first `count` targets with shape t
+      auto solve_mixed = [&](int64_t count, const Tiles& t) -> int {
+        KrigeArgs sa = ca;
+        sa.ntl = count;
+        sa.run = t.run;
+        if (!(binned && t.bins)) return krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 0, stream);
         int64_t* lists = (int64_t*)bins.ptr;
         int64_t* cnts = lists + 2 * chunk;
         size_t b = bin_bytes;
         GS_CUDA(cub::DeviceSelect::If(tmp.ptr, b, thrust::counting_iterator<int64_t>(0), lists,
-                                      cnts, cn, NbLe{dnbc, 32}, stream));
+                                      cnts, count, NbLe{dnbc, 32}, stream));
         b = bin_bytes;
         GS_CUDA(cub::DeviceSelect::If(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
-                                      lists + chunk, cnts + 1, cn, NbGt{dnbc, 32}, stream));
-        KrigeArgs sa = ca;
+                                      lists + chunk, cnts + 1, count, NbGt{dnbc, 32}, stream));
         sa.tlist = lists;
         sa.ntl_dev = cnts;
-        rc = krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 32, stream);
-        if (rc) break;
+        GS_TRY(krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 32, stream));
         sa.tlist = lists + chunk;
         sa.ntl_dev = cnts + 1;
-        rc = krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 64, stream);
-      } else {
-        rc = krige_mixed_launch(ca, k->dm, (uint8_t*)flag.ptr, 0, stream);
+        return krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 64, stream);
+      };
+      if (tune_now && ci == 0) {
+        // autotuner: every candidate once untimed (module loading), then
+        // timed on the same sample; the fastest shape serves this size class
+        const int64_t ns = std::min(cn, kTuneSample);
+        std::vector<Tiles> cand;
+        for (int run : {16, 32, 64, 128})
+          for (int bn = 0; bn <= (binned ? 1 : 0); ++bn) cand.push_back(Tiles{run, bn});
+        std::vector<cudaEvent_t> te(cand.size() + 1);
+        for (auto& e : te) GS_CUDA(cudaEventCreate(&e));
+        for (int pass = 0; pass < 2 && !rc; ++pass) {
+          for (size_t c = 0; c < cand.size() && !rc; ++c) {
+            if (pass == 1 && c == 0) GS_CUDA(cudaEventRecord(te[0], stream));
+            rc = solve_mixed(ns, cand[c]);
+            if (pass == 1) GS_CUDA(cudaEventRecord(te[c + 1], stream));
+          }
+        }
+        if (!rc) {
+          GS_CUDA(cudaEventSynchronize(te.back()));
+          float best = 0;
+          for (size_t c = 0; c < cand.size(); ++c) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, te[c], te[c + 1]);
+            if (c == 0 || ms < best) {
+              best = ms;
+              tiles = cand[c];
+            }
+          }
+          std::lock_guard<std::mutex> lk(k->tiles_mu);
+          k->tiles[size_class(nt)] = tiles;
+        }
+        for (auto& e : te) cudaEventDestroy(e);
+        if (rc) break;
       }
+      rc = solve_mixed(cn, tiles);
+      ca.ntl = cn;
       if (rc) break;
       GS_TRY(mark(3));
       // systems the refinement could not certify: FP64 re-solve over the
@@ -727,6 +795,34 @@ int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double
     return fail(GS_ERR_INVALID_PARAMETER, "predict_with_drift requires KrigingMethod::ExternalDrift");
   cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
   return predict_device(k, nt, tx, ty, tz, tdrift, value, variance, lagrange, status, precision, s);
+}
+
+int gs_kriging_set_tiles(gs_kriging* k, int run, int bins) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (run != 0 && (run < 1 || run > 1024 || (run & (run - 1))))
+    return fail(GS_ERR_INVALID_PARAMETER, "run must be 0 or a power of two in [1, 1024]");
+  if (bins != 0 && bins != 1) return fail(GS_ERR_INVALID_PARAMETER, "bins must be 0 or 1");
+  std::lock_guard<std::mutex> lk(k->tiles_mu);
+  k->pinned = gs::Tiles{run, bins};
+  return GS_OK;
+}
+
+int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins, int* tuned) {
+  if (!k || !run || !bins || !tuned) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
+  std::lock_guard<std::mutex> lk(k->tiles_mu);
+  auto it = k->tiles.find(gs::size_class(nt));
+  gs::Tiles t = gs::default_tiles(nt, true);
+  *tuned = 0;
+  if (k->pinned.run > 0) {
+    t = k->pinned;
+    *tuned = 2;
+  } else if (it != k->tiles.end()) {
+    t = it->second;
+    *tuned = 1;
+  }
+  *run = t.run;
+  *bins = t.bins;
+  return GS_OK;
 }
 
 int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double* tx,

@@ -174,8 +174,9 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
   __syncthreads();
 
   const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
-  for (int64_t r0 = (int64_t)blockIdx.x * kRowsRun; r0 < ntl; r0 += (int64_t)gridDim.x * kRowsRun) {
-  const int64_t r1 = r0 + kRowsRun < ntl ? r0 + kRowsRun : ntl;
+  const int run = a.run > 0 ? a.run : kRowsRun;
+  for (int64_t r0 = (int64_t)blockIdx.x * run; r0 < ntl; r0 += (int64_t)gridDim.x * run) {
+  const int64_t r1 = r0 + run < ntl ? r0 + run : ntl;
   for (int64_t it = r0; it < r1; ++it) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
     const int n = a.nbc[t];
@@ -706,7 +707,8 @@ static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   int per_sm = 0;
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R, smem));
   per_sm = std::max(per_sm, 1);
-  const int blocks = (int)std::min<int64_t>((a.ntl + kRowsRun - 1) / kRowsRun, (int64_t)sms * per_sm);
+  const int run = a.run > 0 ? a.run : kRowsRun;
+  const int blocks = (int)std::min<int64_t>((a.ntl + run - 1) / run, (int64_t)sms * per_sm);
   kern<<<blocks, R, smem, stream>>>(a, m, g_tab, g_kc, flag);
   GS_CUDA(cudaGetLastError());
   count_launch(1);

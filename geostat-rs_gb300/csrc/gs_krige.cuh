@@ -48,6 +48,7 @@ struct KrigeArgs {
   const int64_t* tlist;      // targets to process (null: 0..nt-1)
   int64_t ntl;               // number of them (an upper bound when ntl_dev is set)
   const int64_t* ntl_dev;    // the number on the device, read by the kernel, or null
+  int run;                   // consecutive targets per block sequence (0: 64)
 };
 
 // Mixed-precision kernel for systems with n <= 64 neighbours and at most

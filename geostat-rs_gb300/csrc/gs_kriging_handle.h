@@ -2,10 +2,24 @@
 // shared by the C-ABI translation units.
 #pragma once
 
+#include <map>
+#include <mutex>
+
 #include "gs_common.cuh"
 #include "gs_internal.h"
 #include "gs_krige.cuh"
 #include "gs_search.cuh"
+
+namespace gs {
+// Launch shape of the mixed solver: consecutive targets per block sequence
+// (longer runs share more matrix entries between neighbouring targets,
+// shorter ones spread small calls over more SMs) and whether uneven
+// neighbourhoods are split into the 32- and 64-thread solvers.
+struct Tiles {
+  int run = 64;
+  int bins = 0;
+};
+}  // namespace gs
 
 struct gs_kriging {
   const gs_pointset* ps = nullptr;
@@ -26,6 +40,11 @@ struct gs_kriging {
   gs::SearchFrame frame{};
   gs::Grid grid;
   cudaStream_t stream = nullptr;
+  // autotuned launch shapes per size class of a call (floor(log2(nt))),
+  // and a shape pinned by the caller (run 0: none)
+  mutable std::mutex tiles_mu;
+  mutable std::map<int, gs::Tiles> tiles;
+  gs::Tiles pinned{0, 0};
   ~gs_kriging() {
     cudaFree(d_drift);
     cudaFree(d_err);

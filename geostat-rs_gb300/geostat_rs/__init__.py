@@ -10,10 +10,11 @@ from .errors import (CudaError, DimensionMismatch, DuplicatePoints, GeostatError
                      InsufficientData, InvalidParameter, NoNeighbors, OutOfDeviceMemory,
                      SingularSystem)
 from .model import Anisotropy, Structure, VariogramModel, parse_kind
-from .api import (Kriging, KrigingConfig, KrigingResult, PointSet, Server, VecchiaPlan, krige,
-                  krige_3d, krige_grid, last_timings, maxmin_order, nelder_mead_multistart,
-                  rff_field, rng_normal, rng_uniform, seq_mean, vecchia_krige, vecchia_loglik,
-                  vecchia_mle, vecchia_mle_fit, vecchia_mle_nm_fit, vecchia_predict)
+from .api import (Kriging, KrigingConfig, KrigingResult, PointSet, Server, VecchiaPlan,
+                  clustered_points, krige, krige_3d, krige_grid, last_timings, maxmin_order,
+                  nelder_mead_multistart, rff_field, rng_normal, rng_uniform, seq_mean,
+                  vecchia_krige, vecchia_loglik, vecchia_mle, vecchia_mle_fit,
+                  vecchia_mle_nm_fit, vecchia_predict)
 from ._abi import LIB_PATH, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -286,6 +286,18 @@ class Kriging:
                 PRECISIONS[precision], stream)
         _abi.check(rc)
 
+    def set_tiles(self, run: int = 0, bins: int = 0):
+        """Pin the mixed solver's launch shape (run 0 returns to autotuning)."""
+        _abi.check(_abi.load().gs_kriging_set_tiles(self._h, int(run), int(bins)))
+
+    def tiles(self, nt: int):
+        """(run, bins, source) a call with ``nt`` targets would use; source is
+        "default", "tuned" or "pinned"."""
+        r, b, t = C.c_int32(), C.c_int32(), C.c_int32()
+        _abi.check(_abi.load().gs_kriging_tiles(self._h, int(nt), C.byref(r), C.byref(b),
+                                                C.byref(t)))
+        return r.value, b.value, ("default", "tuned", "pinned")[t.value]
+
     def close(self):
         if getattr(self, "_h", None):
             _abi.load().gs_kriging_destroy(self._h)
@@ -639,6 +651,20 @@ def rng_normal(seed: int, count: int) -> np.ndarray:
     out = np.empty(count)
     _abi.load().gs_rng_normal(seed, count, _p(out))
     return out
+
+
+def clustered_points(n: int, extent: float, n_blobs: int, sigma: float, frac_blobs: float,
+                     seed: int) -> np.ndarray:
+    """Seeded clustered 2-D layout: ``round(frac_blobs * n)`` points in
+    ``n_blobs`` isotropic Gaussian blobs (standard deviation ``sigma``, centres
+    uniform in [0, extent]^2, point i in blob i mod n_blobs) followed by the
+    rest uniform in [0, extent]^2."""
+    nb = int(round(frac_blobs * n))
+    cen = rng_uniform(seed, 2 * n_blobs).reshape(n_blobs, 2) * extent
+    g = rng_normal(seed + 1, 2 * nb).reshape(nb, 2) * sigma
+    pb = cen[np.arange(nb) % n_blobs] + g
+    pu = rng_uniform(seed + 2, 2 * (n - nb)).reshape(n - nb, 2) * extent
+    return np.vstack([pb, pu])
 
 
 def rff_field(coords, model: VariogramModel, n_features: int, seed: int) -> np.ndarray:

@@ -172,6 +172,20 @@ int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double*
                                   const double* ty, const double* tz, const double* tdrift,
                                   double* value, double* variance, double* lagrange,
                                   uint8_t* status, int precision, void* stream);
+/* Launch shapes of the mixed solver (no counterpart in the reference).  A
+ * call of at least 65,536 targets whose size class (floor(log2(nt))) has no
+ * shape yet times the candidate shapes -- runs of 16/32/64/128 consecutive
+ * targets per block, uneven neighbourhoods split onto the 32- and 64-thread
+ * solvers or not -- on its first 262,144 targets and keeps the fastest for
+ * that size class of this predictor; smaller and asynchronous calls use a
+ * default.  Results of different shapes agree within the parity tolerance
+ * (the order of roundings differs), and a predictor's results are
+ * reproducible once its shapes are fixed.
+ * gs_kriging_set_tiles pins one shape for every call (run a power of two in
+ * [1, 1024], bins 0/1; run 0 unpins).  gs_kriging_tiles reports the shape a
+ * call with nt targets would use; tuned = 0 default, 1 tuned, 2 pinned. */
+int gs_kriging_set_tiles(gs_kriging* k, int run, int bins);
+int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins, int* tuned);
 /* Allocation-free FP64 prediction (no counterpart in the reference).  The
  * same results as gs_kriging_predict_many_device with GS_PREC_FP64, for
  * callers that may not allocate device memory while they predict: the
