@@ -70,10 +70,12 @@ DevBuf::~DevBuf() { release(); }
 
 static thread_local double g_timings[4] = {0, 0, 0, 0};
 static thread_local int64_t g_fallbacks = 0;
+static thread_local int64_t g_lu_resolves = 0;
 
 void set_last_timings(const double* ms4, int64_t fallbacks) {
   for (int i = 0; i < 4; ++i) g_timings[i] = ms4[i];
   g_fallbacks = fallbacks;
+  g_lu_resolves = 0;
 }
 
 }  // namespace gs
@@ -118,6 +120,7 @@ int gs_last_timings(double* ms4) {
 }
 
 int64_t gs_last_fallbacks(void) { return g_fallbacks; }
+int64_t gs_last_lu_resolves(void) { return g_lu_resolves; }
 
 // data.rs:15-83 (+ duplicate_coord_pair, data.rs:384-397).
 int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, const double* z,
@@ -575,8 +578,8 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   GS_TRY(nbc.alloc((size_t)chunk * 4, stream));
   GS_TRY(flag.alloc((size_t)chunk, stream));
   GS_TRY(tlist.alloc((size_t)chunk * 8, stream));
-  GS_TRY(nsel.alloc(8, stream));
-  GS_TRY(counts.alloc((size_t)nchunks * 8, stream));
+  GS_TRY(nsel.alloc(16, stream));
+  GS_TRY(counts.alloc((size_t)nchunks * 16, stream));
   size_t sel_bytes = 0, bin_bytes = 0;
   GS_CUDA(cub::DeviceSelect::Flagged(nullptr, sel_bytes, thrust::counting_iterator<int64_t>(0),
                                      (uint8_t*)nullptr, (int64_t*)nullptr, (int64_t*)nullptr,
@@ -703,7 +706,10 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       if (rc) break;
       GS_TRY(mark(3));
       // systems the refinement could not certify: FP64 re-solve over the
-      // flagged list, its length read on the device (no host round trip)
+      // flagged list, its length read on the device (no host round trip);
+      // first the bordered LDL^T kernel, then the partial-pivoting LU for
+      // what it leaves flagged
+      int64_t* nsel2 = (int64_t*)nsel.ptr + 1;
       size_t b = sel_bytes;
       GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
                                          (uint8_t*)flag.ptr, (int64_t*)tlist.ptr,
@@ -714,6 +720,15 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       ca.tlist = (const int64_t*)tlist.ptr;
       ca.ntl = cn;
       ca.ntl_dev = (const int64_t*)nsel.ptr;
+      rc = krige_chol_launch(ca, k->dm, (uint8_t*)flag.ptr, stream);
+      if (rc) break;
+      b = sel_bytes;
+      GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
+                                         (uint8_t*)flag.ptr, (int64_t*)tlist.ptr, nsel2, cn,
+                                         stream));
+      GS_CUDA(cudaMemcpyAsync((int64_t*)counts.ptr + nchunks + ci, nsel2, 8,
+                              cudaMemcpyDeviceToDevice, stream));
+      ca.ntl_dev = nsel2;
       rc = krige_fp64_launch(ca, k->dm, (double*)scratch.ptr, fthreads, stream);
       if (rc) break;
       GS_TRY(mark(4));
@@ -740,14 +755,18 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   float tot = 0;
   cudaEventElapsedTime(&tot, ev[0], ev[5]);
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
-  int64_t n_resolved = nt;
+  int64_t n_resolved = nt, n_lu = nt;
   if (mixed) {
-    std::vector<int64_t> hc(nchunks, 0);
-    GS_CUDA(cudaMemcpyAsync(hc.data(), counts.ptr, nchunks * 8, cudaMemcpyDeviceToHost, stream));
+    std::vector<int64_t> hc(2 * nchunks, 0);
+    GS_CUDA(cudaMemcpyAsync(hc.data(), counts.ptr, nchunks * 16, cudaMemcpyDeviceToHost, stream));
     GS_CUDA(cudaStreamSynchronize(stream));
-    n_resolved = 0;
-    for (int64_t c : hc) n_resolved += c;
+    n_resolved = n_lu = 0;
+    for (int64_t c = 0; c < nchunks; ++c) {
+      n_resolved += hc[c];
+      n_lu += hc[nchunks + c];
+    }
   }
+  g_lu_resolves = n_lu;
   g_timings[0] = t_search;
   g_timings[1] = t_mixed;
   g_timings[2] = t_fp64;

@@ -519,6 +519,241 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
   }
 }
 
+// ----------------------------------------------- FP64 re-solve (LDL^T) --
+// Systems the mixed kernel could not certify are solved here in FP64, one
+// system per warp, with the matrix in shared memory.  The covariance block C
+// (n x n) is bordered by q = p + 2 rows -- the covariances with the target
+// c, the drift columns F and the data values z -- into the symmetric
+//     [ C    c    F    z ]
+//     [ c'   C(0)           ]
+//     [ F'   f    0         ]
+//     [ z'   0    0    0    ]
+// and n steps of LDL^T elimination leave in the trailing q x q block the
+// Schur complements  C(0) - c'C^-1 c,  f - F'C^-1 c,  -F'C^-1 F,  -z'C^-1 c,
+// -z'C^-1 F.  With S = F'C^-1 F and g = F'C^-1 c - f the drift weights are
+// mu = S^-1 g (the kriging system's Lagrange multipliers), and
+//     estimate = z'C^-1 c - z'C^-1 F mu,   variance = C(0) - c'C^-1 c + g'mu,
+// the same quantities as solving [C F; F' 0][w; mu] = [c; f] and forming
+// w'z and C(0) - w'c - mu'f (kriging.rs:569-644), without the weights.
+// Entries come from the double-float covariances of the mixed kernel (about
+// 1e-14 relative) and FP64 drift bases and values; the elimination is FP64.
+//
+// Work split: an n-system is embedded at the bottom right of an Mmax x Mmax
+// frame, so the trailing update of pivot k always covers the pairs (i, j),
+// k < j <= i < Mmax -- a prefix of one pair table sorted by j descending,
+// shared by every system size.  Lanes take consecutive pairs of the prefix.
+// A pivot below 1e-11 of the largest diagonal entry (or a Schur complement
+// of the drift below 1e-11 of its largest diagonal entry) leaves the system
+// flagged for the partial-pivoting LU solver below, which also decides
+// singularity exactly as the reference does.
+constexpr int kCholWarps = 4;
+constexpr double kCholPivotTol = 1e-11;
+
+struct CholLayout {
+  size_t off_ptab, off_warp, warp_bytes, off_a, off_lsc, off_lun, off_v, off_idx, total;
+};
+
+__host__ __device__ inline CholLayout chol_layout(int Mmax, int nf, int dim) {
+  CholLayout L;
+  size_t o = 0, w = 0;
+  auto take = [&](size_t& at, size_t bytes) {
+    size_t r = at;
+    at += (bytes + 15) & ~(size_t)15;
+    return r;
+  };
+  L.off_ptab = take(o, (size_t)(Mmax * (Mmax - 1) / 2) * 4);
+  L.off_a = take(w, (size_t)(Mmax * (Mmax + 1) / 2) * 8);
+  L.off_lsc = take(w, (size_t)Mmax * 8);
+  L.off_lun = take(w, (size_t)Mmax * 8);
+  L.off_v = take(w, (size_t)nf * dim * GS_MIXED_MAX_NEIGHBORS * sizeof(df));
+  L.off_idx = take(w, (size_t)GS_MIXED_MAX_NEIGHBORS * 4);
+  L.warp_bytes = w;
+  L.off_warp = take(o, w * kCholWarps);
+  L.total = o;
+  return L;
+}
+
+// 1/d to FP64 accuracy: FP32 estimate of the power-of-two scaled value, two
+// Newton steps (e = 1 - d r, r += r e).  sc scales d into [2^-40, 2].
+__device__ __forceinline__ double rcp_fp64(double d, double sc) {
+  double r = (double)__frcp_rn((float)(d * sc)) * sc;
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kCholWarps * 32)
+    krige_chol_kernel(KrigeArgs a, DevModel m, ExpTable tab_g, DfConsts kc, uint8_t* flag,
+                      int Mmax) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ ExpTable tab;
+  for (int q = threadIdx.x; q < 256; q += blockDim.x) tab.v[q] = tab_g.v[q];
+  const Frames fr = frames_of(m);
+  const CholLayout L = chol_layout(Mmax, fr.nf, D);
+  // pairs (i, j), 1 <= j <= i < Mmax, j descending: packed index << 16 | i << 8 | j
+  uint32_t* ptab = reinterpret_cast<uint32_t*>(smem_raw + L.off_ptab);
+  for (int j = 1; j < Mmax; ++j) {
+    const int off = ((Mmax - 1 - j) * (Mmax - j)) >> 1;
+    for (int i = j + threadIdx.x; i < Mmax; i += blockDim.x)
+      ptab[off + i - j] = ((uint32_t)pk(i, j) << 16) | ((uint32_t)i << 8) | (uint32_t)j;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* wb = smem_raw + L.off_warp + (size_t)warp * L.warp_bytes;
+  double* A = reinterpret_cast<double*>(wb + L.off_a);
+  double* lsc = reinterpret_cast<double*>(wb + L.off_lsc);
+  double* lun = reinterpret_cast<double*>(wb + L.off_lun);
+  df* V = reinterpret_cast<df*>(wb + L.off_v);
+  int* ids = reinterpret_cast<int*>(wb + L.off_idx);
+  const double* coord[3] = {a.x, a.y, a.z};
+  const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
+  const int p = a.p;
+  const int q = p + 2;
+  const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
+  for (int64_t it = (int64_t)blockIdx.x * kCholWarps + warp; it < ntl;
+       it += (int64_t)gridDim.x * kCholWarps) {
+    const int64_t t = a.tlist ? a.tlist[it] : it;
+    const int n = a.nbc[t];
+    // only systems the mixed kernel flagged arrive; those outside this
+    // kernel's bounds stay flagged for the LU solver
+    if (n < 1 || n < p || n > GS_MIXED_MAX_NEIGHBORS || p > GS_MIXED_MAX_DRIFT || n + q > Mmax)
+      continue;
+    const int o = Mmax - (n + q);  // frame offset of the system
+    const int ic = o + n;           // row of c; F at ic + 1 .. ic + p; z at ic + p + 1
+    const int iz = ic + p + 1;
+    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+    const int32_t* nbt = a.nb + t * (int64_t)a.kout;
+    for (int s = lane; s < n; s += 32) {
+      const int idx = nbt[s];
+      ids[s] = idx;
+      df ud[3];
+#pragma unroll
+      for (int d = 0; d < D; ++d) ud[d] = df_sub(a.cdf[(int64_t)d * a.n + idx], df_from_double(tp[d]));
+      frame_coords<D>(m, fr, ud, V, GS_MIXED_MAX_NEIGHBORS, s);
+    }
+    __syncwarp();
+    for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+      df c0, c1;
+      cov_pair2<D>(m, fr, V, GS_MIXED_MAX_NEIGHBORS, i0, j0, i1, j1, tab, kc, c0, c1);
+      A[pk(o + i0, o + j0)] = df_to_double(c0);
+      if (two) A[pk(o + i1, o + j1)] = df_to_double(c1);
+    });
+    const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
+    double scale = 0.0;
+    for (int s = lane; s < n; s += 32) {
+      const int idx = ids[s];
+      const double dg = m.c0 + (a.meas_err ? a.meas_err[idx] : 0.0);
+      A[pk(o + s, o + s)] = dg;
+      scale = fmax(scale, dg);
+      const double pt[3] = {a.x[idx], a.y[idx], D == 3 ? a.z[idx] : 0.0};
+      bool zero = true;
+#pragma unroll
+      for (int d = 0; d < D; ++d) zero = zero && same_double(coord[d][idx], tp[d]);
+      A[pk(ic, o + s)] =
+          zero ? m.c0 : df_to_double(cov_origin<D>(m, fr, V, GS_MIXED_MAX_NEIGHBORS, s, tab, kc));
+      for (int k = 0; k < p; ++k)
+        A[pk(ic + 1 + k, o + s)] =
+            basis_at<D>(a, pt, a.drift ? a.drift + (int64_t)idx * a.nv : nullptr, k);
+      A[pk(iz, o + s)] = a.method == GS_SIMPLE ? a.val[idx] - a.sk_mean : a.val[idx];
+    }
+    // the border block: C(0), the target's drift bases, zeros
+    for (int r = lane; r < q; r += 32) {
+      for (int c = 0; c <= r; ++c) {
+        double v = 0.0;
+        if (r == 0) v = m.c0;
+        else if (c == 0 && r <= p) v = basis_at<D>(a, tp, trow, r - 1);
+        A[pk(ic + r, ic + c)] = v;
+      }
+    }
+    scale = warp_max_d(scale);
+    int ex = 0;
+    frexp(scale, &ex);
+    const double sc = ldexp(1.0, -ex);
+    __syncwarp();
+    bool ok = true;
+    for (int k = o; k < ic; ++k) {
+      const double d = A[pk(k, k)];
+      if (!(d > kCholPivotTol * scale)) {  // the same value in every lane
+        ok = false;
+        break;
+      }
+      const double r = rcp_fp64(d, sc);
+      for (int i = k + 1 + lane; i < Mmax; i += 32) {
+        const double v = A[pk(i, k)];
+        lun[i] = v;
+        lsc[i] = v * r;
+      }
+      __syncwarp();
+      const int T = ((Mmax - 1 - k) * (Mmax - k)) >> 1;
+#pragma unroll 4
+      for (int e = lane; e < T; e += 32) {
+        const uint32_t en = ptab[e];
+        const int pe = (int)(en >> 16), i = (int)((en >> 8) & 255u), j = (int)(en & 255u);
+        A[pe] = fma(-lsc[i], lun[j], A[pe]);
+      }
+      __syncwarp();
+    }
+    if (ok && lane == 0) {
+      const double Tcc = A[pk(ic, ic)], Tzc = A[pk(iz, ic)];
+      double v, var, lag = kNaN;
+      if (p == 0) {
+        v = a.sk_mean - Tzc;
+        var = Tcc;
+      } else {
+        // S mu = g, S = -T_FF, g = -T_Fc, by LDL^T (p <= GS_MIXED_MAX_DRIFT)
+        double S[GS_MIXED_MAX_DRIFT * (GS_MIXED_MAX_DRIFT + 1) / 2], g[GS_MIXED_MAX_DRIFT];
+        double smax = 0.0;
+        for (int k = 0; k < p; ++k) {
+          g[k] = -A[pk(ic + 1 + k, ic)];
+          for (int l = 0; l <= k; ++l) S[pk(k, l)] = -A[pk(ic + 1 + k, ic + 1 + l)];
+          smax = fmax(smax, fabs(S[pk(k, k)]));
+        }
+        for (int k = 0; k < p && ok; ++k) {
+          const double d = S[pk(k, k)];
+          if (!(d > kCholPivotTol * smax)) {
+            ok = false;
+            break;
+          }
+          // rows from the bottom up, so column k still holds S's values
+          // (not multipliers) when the rows above use them
+          for (int i = p - 1; i > k; --i) {
+            const double l = S[pk(i, k)] / d;
+            for (int j = k + 1; j <= i; ++j) S[pk(i, j)] -= l * S[pk(j, k)];
+            g[i] -= l * g[k];
+            S[pk(i, k)] = l;
+          }
+        }
+        if (ok) {
+          // back substitution with L^T D: mu_k = g_k / d_k - sum_{i>k} l_ik mu_i
+          double mu[GS_MIXED_MAX_DRIFT];
+          for (int k = p - 1; k >= 0; --k) {
+            double s = g[k] / S[pk(k, k)];
+            for (int i = k + 1; i < p; ++i) s -= S[pk(i, k)] * mu[i];
+            mu[k] = s;
+          }
+          v = -Tzc;
+          var = Tcc;
+          for (int k = 0; k < p; ++k) {
+            v = fma(A[pk(iz, ic + 1 + k)], mu[k], v);
+            var = fma(-A[pk(ic + 1 + k, ic)], mu[k], var);
+          }
+          lag = mu[0];
+        }
+      }
+      if (ok) {
+        a.out_v[t] = v;
+        a.out_var[t] = fmax(var, 0.0);
+        if (a.out_lag) a.out_lag[t] = lag;
+        a.out_st[t] = GS_ST_OK | GS_ST_FP64_RESOLVED;
+        flag[t] = 0;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // ------------------------------------------------------------- FP64 path --
 template <int D>
 __global__ void __launch_bounds__(128) krige_fp64_kernel(KrigeArgs a, DevModel m, double* scratch,
@@ -734,6 +969,35 @@ int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
                          : launch_rows<3, 32, 4>(a, m, flag, nf, stream);
   return wide ? launch_rows<3, 64, 12>(a, m, flag, nf, stream)
               : launch_rows<3, 64, 4>(a, m, flag, nf, stream);
+}
+
+template <int D>
+static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int nf, int Mmax,
+                       cudaStream_t stream) {
+  const CholLayout lay = chol_layout(Mmax, nf, D);
+  auto kern = krige_chol_kernel<D>;
+  GS_TRY(allow_dynamic_smem((const void*)kern, lay.total));
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int per_sm = 0;
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCholWarps * 32, lay.total));
+  per_sm = std::max(per_sm, 1);
+  const int blocks = (int)std::min<int64_t>((a.ntl + kCholWarps - 1) / kCholWarps, (int64_t)sms * per_sm);
+  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, g_tab, g_kc, flag, Mmax);
+  GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  return GS_OK;
+}
+
+int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, cudaStream_t stream) {
+  if (a.ntl == 0) return GS_OK;
+  ensure_tables();
+  int nf = 1;
+  for (int s = 0; s < m.ns; ++s) nf += m.s[s].aniso ? 1 : 0;
+  const int Mmax = std::min(a.kout, GS_MIXED_MAX_NEIGHBORS) + a.p + 2;
+  if (a.dim == 2) return launch_chol<2>(a, m, flag, nf, Mmax, stream);
+  return launch_chol<3>(a, m, flag, nf, Mmax, stream);
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {

@@ -58,7 +58,12 @@ struct KrigeArgs {
 // threads), 32 / 64 forces it (binned launches).
 int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int force_rows,
                        cudaStream_t stream);
-// Plain FP64 kernel, one system per thread (also the re-solve path).
+// FP64 re-solve of the flagged systems (bordered LDL^T, one system per
+// warp); clears the flag of every system it solves.  Systems left flagged
+// (near-singular, or beyond 64 neighbours) go to krige_fp64_launch.
+int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, cudaStream_t stream);
+// Plain FP64 kernel, one system per thread (the reference's partial-pivoting
+// LU; the FP64 build and the last re-solve tier).
 // scratch must hold fp64_scratch_doubles(nmax, threads) doubles.
 int krige_fp64_launch(const KrigeArgs& a, const DevModel& m, double* scratch, int64_t threads,
                       cudaStream_t stream);

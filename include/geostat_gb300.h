@@ -317,6 +317,11 @@ int gs_last_timings(double* ms4);
  * this host thread solved with the FP64 kernels (mixed-precision systems
  * the refinement could not certify, or all of them at GS_PREC_FP64). */
 int64_t gs_last_fallbacks(void);
+/* Of those, the systems of the last gs_kriging_predict_* call on this host
+ * thread that went on from the FP64 LDL^T re-solve to the partial-pivoting
+ * LU (near-singular systems, more than 64 neighbours; all of them at
+ * GS_PREC_FP64; 0 after a Vecchia call). */
+int64_t gs_last_lu_resolves(void);
 
 /* Measurement helpers (no reference counterpart): sustained CUDA-core FMA
  * throughput in TFLOP/s for FP32 (precision 0), FP64 (1) or packed FP32x2
