@@ -286,6 +286,7 @@ def run_ours(args, rank, world):
         acc, cpu = cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var,
                                            fp64_v, kr, log)
         vec = vecchia_bench(args, log) if not args.no_vecchia else None
+        clu = clustered_bench(args, log) if not args.no_clustered else None
         serve = serving_bench(args, log) if args.serve_requests > 0 else None
         peaks = measured_peaks()
         result = {
@@ -330,6 +331,8 @@ def run_ours(args, rank, world):
         }
         if vec is not None:
             result["vecchia"] = vec
+        if clu is not None:
+            result["clustered"] = clu
         if serve is not None:
             result["serving"] = serve
             result["p99_latency_ms"] = serve["p99_ms"]
@@ -448,6 +451,170 @@ def vecchia_bench(args, log):
             "max_rel_value": float(np.max(np.abs(gv - rv) / np.maximum(np.abs(rv), np.mean(np.abs(vs))))),
             "max_rel_variance": float(np.max(np.abs(gvar - rvar) / np.maximum(np.abs(rvar), 1e-3)))}
     return out
+
+
+CL_N = 1_000_000
+CL_EXTENT = 10000.0
+CL_GRID = 2048
+CL_SEARCH = dict(max_per_octant=16, max_neighbors=64, min_neighbors=4)
+CL_KINDS = ("ordinary", "universal", "external_drift")
+
+
+def clustered_setup(n=CL_N, grid=CL_GRID, extent=CL_EXTENT, nblobs=500):
+    """Clustered uneven workload: n 2-D points (70 % in Gaussian blobs of
+    sigma 15 m, 30 % uniform) over [0, extent]^2; Matern 3/2 field (sill 1,
+    range 500 m, ratio 0.5 at azimuth 45, no nugget); one U[0,1] covariate;
+    the grid x grid cell centres split into three bands of rows: ordinary,
+    universal (linear drift) and external-drift kriging, all with octant
+    search (4 x 16, at most 64, at least 4)."""
+    import geostat_rs as G
+    from geostat_rs.model import Structure, VariogramModel
+    c = G.clustered_points(n, extent, nblobs, 15.0, 0.7, SEED + 21)
+    m = VariogramModel(0.0, [Structure.with_anisotropy("matern15", 1.0, 500.0, 45.0, 0.5)])
+    v = G.rff_field(c, m, 4096, SEED + 22)
+    cov = G.rng_uniform(SEED + 23, n)
+    g = (np.arange(grid) + 0.5) * (extent / grid)
+    yy, xx = np.meshgrid(g, g, indexing="ij")
+    tg = np.stack([xx.ravel(), yy.ravel()], 1)
+    tcov = G.rng_uniform(SEED + 24, len(tg))
+    cuts = [0, (grid // 3) * grid, (2 * grid // 3) * grid, grid * grid]
+    ps = G.PointSet(c, v)
+    preds = [G.Kriging.new(ps, m, G.KrigingConfig(**CL_SEARCH)),
+             G.Kriging.new(ps, m, G.KrigingConfig("universal", degree=1, **CL_SEARCH)),
+             G.Kriging.with_external_drift(ps, m, G.KrigingConfig("external_drift", n_vars=1,
+                                                                  **CL_SEARCH),
+                                           cov.reshape(-1, 1))]
+    return c, v, m, cov, tg, tcov, cuts, preds
+
+
+def clustered_bench(args, log):
+    """The clustered uneven workload as one CUDA-graph replay per step."""
+    import torch
+    import geostat_rs as G
+    from geostat_rs import _abi
+    lib = _abi.load()
+    t0 = time.time()
+    c, v, m, cov, tg, tcov, cuts, preds = clustered_setup()
+    nt = len(tg)
+    log(f"[bench] clustered set-up {time.time() - t0:.1f}s")
+    dev = torch.device("cuda")
+    cols = [torch.from_numpy(np.ascontiguousarray(tg[:, d])).to(dev) for d in range(2)]
+    tdr = torch.from_numpy(np.ascontiguousarray(tcov)).to(dev)
+    out_v = torch.empty(nt, dtype=torch.float64, device=dev)
+    out_var = torch.empty(nt, dtype=torch.float64, device=dev)
+    out_st = torch.empty(nt, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    s = torch.cuda.Stream()
+    sp = s.cuda_stream
+
+    def enqueue(prec, asynchronous):
+        for b, k in enumerate(preds):
+            lo, hi = cuts[b], cuts[b + 1]
+            k.predict_device(hi - lo, cols[0][lo:].data_ptr(), cols[1][lo:].data_ptr(), None,
+                             out_v[lo:].data_ptr(), out_var[lo:].data_ptr(),
+                             out_st[lo:].data_ptr(), prec, stream=sp,
+                             tdrift_ptr=tdr[lo:].data_ptr() if b == 2 else None,
+                             asynchronous=asynchronous)
+
+    # ordinary calls first: autotuning (per kind and size class), tables;
+    # phases and re-solve counts per kind from the second call
+    kinds = {}
+    for rep in range(2):
+        for b, k in enumerate(preds):
+            lo, hi = cuts[b], cuts[b + 1]
+            k.predict_device(hi - lo, cols[0][lo:].data_ptr(), cols[1][lo:].data_ptr(), None,
+                             out_v[lo:].data_ptr(), out_var[lo:].data_ptr(),
+                             out_st[lo:].data_ptr(), "mixed", stream=sp,
+                             tdrift_ptr=tdr[lo:].data_ptr() if b == 2 else None)
+            if rep == 1:
+                ph = G.last_timings()
+                run, bins, src = k.tiles(hi - lo)
+                kinds[CL_KINDS[b]] = {
+                    "targets": hi - lo, "search_ms": ph[0], "mixed_ms": ph[1],
+                    "fp64_resolve_ms": ph[2], "total_ms": ph[3],
+                    "fp64_resolved": int(lib.gs_last_fallbacks()),
+                    "lu_resolved": int(lib.gs_last_lu_resolves()),
+                    "tiles": {"run": run, "bins": bins, "source": src}}
+    torch.cuda.synchronize()
+    l0 = lib.gs_launch_count()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        enqueue("mixed", True)
+    nodes = lib.gs_launch_count() - l0
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    cur = torch.cuda.current_stream()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(cur)
+        g.replay()
+        e1.record(cur)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.mean(times)
+    mixed_v = out_v.cpu().numpy()
+    mixed_var = out_var.cpu().numpy()
+    st = out_st.cpu().numpy()
+    # the plain FP64 build on the same job
+    t64 = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        enqueue("fp64", False)
+        e1.record(s)
+        torch.cuda.synchronize()
+        t64.append(e0.elapsed_time(e1))
+    ms64 = min(t64)
+    fp64_v = out_v.cpu().numpy()
+    log(f"[bench] clustered: {ms:.1f} ms/step (graph replay), fp64 build {ms64:.1f} ms")
+    # oracle on a sample of each band
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    rng = np.random.RandomState(11)
+    vs = float(np.mean(np.abs(v)))
+    acc, cpu_t, cpu_n = {}, 0.0, 0
+    for b, kind in enumerate(CL_KINDS):
+        lo, hi = cuts[b], cuts[b + 1]
+        idx = np.sort(rng.choice(np.arange(lo, hi), args.cl_sample, replace=False))
+        t1 = time.perf_counter()
+        ref = O.krige(c, v, m, tg[idx], method=kind, degree=1,
+                      drift=cov.reshape(-1, 1) if b == 2 else None,
+                      target_drift=tcov[idx].reshape(-1, 1) if b == 2 else None,
+                      nthreads=cores, **CL_SEARCH)
+        cpu_t += time.perf_counter() - t1
+        cpu_n += len(idx)
+        rel = lambda a, r, f: float(np.max(np.abs(a - r) / np.maximum(np.abs(r), f)))
+        acc[kind] = {"mixed_max_rel_value": rel(mixed_v[idx], ref["value"], vs),
+                     "mixed_max_rel_variance": rel(mixed_var[idx], ref["variance"], 1e-3),
+                     "fp64_max_rel_value": rel(fp64_v[idx], ref["value"], vs),
+                     "status_match": bool(((st[idx] & 0x3f) == ref["status"]).all())}
+    log(f"[bench] clustered oracle: {cpu_n} targets in {cpu_t:.1f}s on {cores} threads")
+    return {"workload": "clustered uneven kriging: n=1,000,000 2-D points (70% in 500 Gaussian "
+                        "blobs, sigma 15 m; 30% uniform) over [0,10000]^2 m; Matern 3/2 (sill 1, "
+                        "range 500 m, ratio 0.5, azimuth 45, no nugget); 2048x2048 grid targets "
+                        "(4,194,304) in three bands: ordinary, universal (linear drift), external "
+                        "drift (one U[0,1] covariate); octant search 4 x 16, max 64, min 4",
+            "value": nt / (ms * 1e-3), "unit": "kriged targets/s", "ms_per_step": ms,
+            "steps": args.steps, "warmup": args.warmup,
+            "step": "one CUDA-graph replay of the three passes (search, binned mixed solve, "
+                    "device-side routing, FP64 LDL^T and LU re-solves)",
+            "graph_kernel_nodes": nodes,
+            "fp64_gpu_build": {"value": nt / (ms64 * 1e-3), "ms_per_step": ms64,
+                               "mixed_over_fp64": ms64 / ms},
+            "kinds": kinds, "accuracy": acc,
+            "fp64_resolved_fraction": sum(k["fp64_resolved"] for k in kinds.values()) / nt,
+            "cpu_baseline": {"value": cpu_n / cpu_t, "unit": "kriged targets/s", "cores": cores,
+                             "kind": "port",
+                             "sample": f"{args.cl_sample} random targets per band"},
+            "l2": "flushed between steps (256 MiB write)"}
 
 
 def serving_bench(args, log):
@@ -609,6 +776,10 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--vecchia-n", type=int, default=2_000_000)
     ap.add_argument("--no-vecchia", action="store_true")
+    ap.add_argument("--no-clustered", action="store_true",
+                    help="skip the clustered uneven workload")
+    ap.add_argument("--cl-sample", type=int, default=200,
+                    help="oracle targets per band of the clustered workload")
     ap.add_argument("--vpred-n", type=int, default=500_000,
                     help="targets of the Vecchia joint-prediction timing (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=1000,

@@ -463,6 +463,8 @@ struct NbGt {
 constexpr int64_t kTuneMinTargets = 65536;
 // Targets of the first chunk the candidates are timed on.
 constexpr int64_t kTuneSample = 262144;
+// Leading targets of each chunk whose FP32 failure rate routes the rest.
+constexpr int64_t kRouteSample = 16384;
 
 int size_class(int64_t nt) {
   int c = 0;
@@ -578,7 +580,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   GS_TRY(nbc.alloc((size_t)chunk * 4, stream));
   GS_TRY(flag.alloc((size_t)chunk, stream));
   GS_TRY(tlist.alloc((size_t)chunk * 8, stream));
-  GS_TRY(nsel.alloc(16, stream));
+  GS_TRY(nsel.alloc(32, stream));
   GS_TRY(counts.alloc((size_t)nchunks * 16, stream));
   size_t sel_bytes = 0, bin_bytes = 0;
   GS_CUDA(cub::DeviceSelect::Flagged(nullptr, sel_bytes, thrust::counting_iterator<int64_t>(0),
@@ -648,25 +650,39 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       ca.nmax = std::min(nmax_all, GS_MIXED_MAX_NEIGHBORS + p);
       ca.tlist = nullptr;
       // mixed solves of the chunk's first `count` targets with shape t
-      auto solve_mixed = [&](int64_t count, const Tiles& t) -> int {
+      // mixed solves of the chunk's targets [b0, b0 + count) with shape t
+      // (per-target arrays offset to b0); route: the FP64 routing switch
+      auto solve_mixed = [&](int64_t b0, int64_t count, const Tiles& t, const int* route) -> int {
         KrigeArgs sa = ca;
+        sa.tx += b0;
+        sa.ty += b0;
+        if (sa.tz) sa.tz += b0;
+        if (sa.tdrift) sa.tdrift += b0 * k->nv;
+        sa.nb += b0 * kout;
+        sa.nbc += b0;
+        sa.out_v += b0;
+        sa.out_var += b0;
+        if (sa.out_lag) sa.out_lag += b0;
+        sa.out_st += b0;
         sa.ntl = count;
         sa.run = t.run;
-        if (!(binned && t.bins)) return krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 0, stream);
+        sa.route_fp64 = route;
+        uint8_t* fl = (uint8_t*)flag.ptr + b0;
+        if (!(binned && t.bins)) return krige_mixed_launch(sa, k->dm, fl, 0, stream);
         int64_t* lists = (int64_t*)bins.ptr;
         int64_t* cnts = lists + 2 * chunk;
         size_t b = bin_bytes;
         GS_CUDA(cub::DeviceSelect::If(tmp.ptr, b, thrust::counting_iterator<int64_t>(0), lists,
-                                      cnts, count, NbLe{dnbc, 32}, stream));
+                                      cnts, count, NbLe{sa.nbc, 32}, stream));
         b = bin_bytes;
         GS_CUDA(cub::DeviceSelect::If(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),
-                                      lists + chunk, cnts + 1, count, NbGt{dnbc, 32}, stream));
+                                      lists + chunk, cnts + 1, count, NbGt{sa.nbc, 32}, stream));
         sa.tlist = lists;
         sa.ntl_dev = cnts;
-        GS_TRY(krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 32, stream));
+        GS_TRY(krige_mixed_launch(sa, k->dm, fl, 32, stream));
         sa.tlist = lists + chunk;
         sa.ntl_dev = cnts + 1;
-        return krige_mixed_launch(sa, k->dm, (uint8_t*)flag.ptr, 64, stream);
+        return krige_mixed_launch(sa, k->dm, fl, 64, stream);
       };
       if (tune_now && ci == 0) {
         // autotuner: every candidate once untimed (module loading), then
@@ -680,7 +696,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
         for (int pass = 0; pass < 2 && !rc; ++pass) {
           for (size_t c = 0; c < cand.size() && !rc; ++c) {
             if (pass == 1 && c == 0) GS_CUDA(cudaEventRecord(te[0], stream));
-            rc = solve_mixed(ns, cand[c]);
+            rc = solve_mixed(0, ns, cand[c], nullptr);
             if (pass == 1) GS_CUDA(cudaEventRecord(te[c + 1], stream));
           }
         }
@@ -701,7 +717,15 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
         for (auto& e : te) cudaEventDestroy(e);
         if (rc) break;
       }
-      rc = solve_mixed(cn, tiles);
+      // the first kRouteSample targets decide (on the device) whether the
+      // rest of the chunk goes straight to the FP64 re-solve
+      const int64_t nprobe = std::min(cn, kRouteSample);
+      int* route = (int*)((int64_t*)nsel.ptr + 2);
+      rc = solve_mixed(0, nprobe, tiles, nullptr);
+      if (!rc && cn > nprobe) {
+        rc = route_launch((const uint8_t*)flag.ptr, nprobe, route, stream);
+        if (!rc) rc = solve_mixed(nprobe, cn - nprobe, tiles, route);
+      }
       ca.ntl = cn;
       if (rc) break;
       GS_TRY(mark(3));

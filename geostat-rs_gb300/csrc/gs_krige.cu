@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
 
   const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
   const int run = a.run > 0 ? a.run : kRowsRun;
+  const bool route = a.route_fp64 && *a.route_fp64;
   for (int64_t r0 = (int64_t)blockIdx.x * run; r0 < ntl; r0 += (int64_t)gridDim.x * run) {
   const int64_t r1 = r0 + run < ntl ? r0 + run : ntl;
   for (int64_t it = r0; it < r1; ++it) {
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       }
       continue;
     }
-    if (n > R || p > PC) {
+    if (n > R || p > PC || route) {
       if (i == 0) flag[t] = 1;
       continue;
     }
@@ -535,8 +536,10 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
 //     estimate = z'C^-1 c - z'C^-1 F mu,   variance = C(0) - c'C^-1 c + g'mu,
 // the same quantities as solving [C F; F' 0][w; mu] = [c; f] and forming
 // w'z and C(0) - w'c - mu'f (kriging.rs:569-644), without the weights.
-// Entries come from the double-float covariances of the mixed kernel (about
-// 1e-14 relative) and FP64 drift bases and values; the elimination is FP64.
+// Every entry is FP64 as in the reference (cov_fp64, basis_at): with
+// condition numbers up to ~1e11 the double-float covariances of the mixed
+// kernel (~1e-14 relative) would move estimates and variances by more than
+// 1e-9.  The elimination is FP64.
 //
 // Work split: an n-system is embedded at the bottom right of an Mmax x Mmax
 // frame, so the trailing update of pivot k always covers the pairs (i, j),
@@ -553,7 +556,7 @@ struct CholLayout {
   size_t off_ptab, off_warp, warp_bytes, off_a, off_lsc, off_lun, off_v, off_idx, total;
 };
 
-__host__ __device__ inline CholLayout chol_layout(int Mmax, int nf, int dim) {
+__host__ __device__ inline CholLayout chol_layout(int Mmax, int dim) {
   CholLayout L;
   size_t o = 0, w = 0;
   auto take = [&](size_t& at, size_t bytes) {
@@ -565,7 +568,7 @@ __host__ __device__ inline CholLayout chol_layout(int Mmax, int nf, int dim) {
   L.off_a = take(w, (size_t)(Mmax * (Mmax + 1) / 2) * 8);
   L.off_lsc = take(w, (size_t)Mmax * 8);
   L.off_lun = take(w, (size_t)Mmax * 8);
-  L.off_v = take(w, (size_t)nf * dim * GS_MIXED_MAX_NEIGHBORS * sizeof(df));
+  L.off_v = take(w, (size_t)dim * GS_MIXED_MAX_NEIGHBORS * sizeof(double));
   L.off_idx = take(w, (size_t)GS_MIXED_MAX_NEIGHBORS * 4);
   L.warp_bytes = w;
   L.off_warp = take(o, w * kCholWarps);
@@ -585,13 +588,9 @@ __device__ __forceinline__ double rcp_fp64(double d, double sc) {
 
 template <int D>
 __global__ void __launch_bounds__(kCholWarps * 32)
-    krige_chol_kernel(KrigeArgs a, DevModel m, ExpTable tab_g, DfConsts kc, uint8_t* flag,
-                      int Mmax) {
+    krige_chol_kernel(KrigeArgs a, DevModel m, uint8_t* flag, int Mmax) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ ExpTable tab;
-  for (int q = threadIdx.x; q < 256; q += blockDim.x) tab.v[q] = tab_g.v[q];
-  const Frames fr = frames_of(m);
-  const CholLayout L = chol_layout(Mmax, fr.nf, D);
+  const CholLayout L = chol_layout(Mmax, D);
   // pairs (i, j), 1 <= j <= i < Mmax, j descending: packed index << 16 | i << 8 | j
   uint32_t* ptab = reinterpret_cast<uint32_t*>(smem_raw + L.off_ptab);
   for (int j = 1; j < Mmax; ++j) {
@@ -605,9 +604,10 @@ __global__ void __launch_bounds__(kCholWarps * 32)
   double* A = reinterpret_cast<double*>(wb + L.off_a);
   double* lsc = reinterpret_cast<double*>(wb + L.off_lsc);
   double* lun = reinterpret_cast<double*>(wb + L.off_lun);
-  df* V = reinterpret_cast<df*>(wb + L.off_v);
+  double* P = reinterpret_cast<double*>(wb + L.off_v);  // P[d * 64 + s]: slot s's coordinates
   int* ids = reinterpret_cast<int*>(wb + L.off_idx);
   const double* coord[3] = {a.x, a.y, a.z};
+  constexpr int NS = GS_MIXED_MAX_NEIGHBORS;
   const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
   const int p = a.p;
   const int q = p + 2;
@@ -628,17 +628,22 @@ __global__ void __launch_bounds__(kCholWarps * 32)
     for (int s = lane; s < n; s += 32) {
       const int idx = nbt[s];
       ids[s] = idx;
-      df ud[3];
 #pragma unroll
-      for (int d = 0; d < D; ++d) ud[d] = df_sub(a.cdf[(int64_t)d * a.n + idx], df_from_double(tp[d]));
-      frame_coords<D>(m, fr, ud, V, GS_MIXED_MAX_NEIGHBORS, s);
+      for (int d = 0; d < D; ++d) P[d * NS + s] = coord[d][idx];
     }
     __syncwarp();
+    // build_lhs (kriging.rs:527-567): separations p_i - p_j, FP64 covariances
     for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
-      df c0, c1;
-      cov_pair2<D>(m, fr, V, GS_MIXED_MAX_NEIGHBORS, i0, j0, i1, j1, tab, kc, c0, c1);
-      A[pk(o + i0, o + j0)] = df_to_double(c0);
-      if (two) A[pk(o + i1, o + j1)] = df_to_double(c1);
+      double h0[3], h1[3];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        h0[d] = P[d * NS + i0] - P[d * NS + j0];
+        h1[d] = P[d * NS + i1] - P[d * NS + j1];
+      }
+      const double c0 = cov_fp64<D>(m, h0);
+      const double c1 = cov_fp64<D>(m, h1);
+      A[pk(o + i0, o + j0)] = c0;
+      if (two) A[pk(o + i1, o + j1)] = c1;
     });
     const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
     double scale = 0.0;
@@ -647,12 +652,9 @@ __global__ void __launch_bounds__(kCholWarps * 32)
       const double dg = m.c0 + (a.meas_err ? a.meas_err[idx] : 0.0);
       A[pk(o + s, o + s)] = dg;
       scale = fmax(scale, dg);
-      const double pt[3] = {a.x[idx], a.y[idx], D == 3 ? a.z[idx] : 0.0};
-      bool zero = true;
-#pragma unroll
-      for (int d = 0; d < D; ++d) zero = zero && same_double(coord[d][idx], tp[d]);
-      A[pk(ic, o + s)] =
-          zero ? m.c0 : df_to_double(cov_origin<D>(m, fr, V, GS_MIXED_MAX_NEIGHBORS, s, tab, kc));
+      const double pt[3] = {P[s], P[NS + s], D == 3 ? P[2 * NS + s] : 0.0};
+      const double h[3] = {pt[0] - tp[0], pt[1] - tp[1], pt[2] - tp[2]};
+      A[pk(ic, o + s)] = cov_fp64<D>(m, h);
       for (int k = 0; k < p; ++k)
         A[pk(ic + 1 + k, o + s)] =
             basis_at<D>(a, pt, a.drift ? a.drift + (int64_t)idx * a.nv : nullptr, k);
@@ -904,6 +906,21 @@ __global__ void __launch_bounds__(128) krige_fp64_kernel(KrigeArgs a, DevModel m
   }
 }
 
+__global__ void route_kernel(const uint8_t* flag, int64_t n, int* route) {
+  __shared__ int part[32];
+  int c = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) c += flag[i] ? 1 : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w];
+    *route = 4 * tot > 3 * n ? 1 : 0;
+  }
+}
+
 template <int D>
 __global__ void grid_centers_kernel(double x0, double y0, double z0, double dx, double dy,
                                     double dz, int64_t nx, int64_t ny, int64_t total, double* x,
@@ -972,9 +989,9 @@ int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
 }
 
 template <int D>
-static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int nf, int Mmax,
+static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int Mmax,
                        cudaStream_t stream) {
-  const CholLayout lay = chol_layout(Mmax, nf, D);
+  const CholLayout lay = chol_layout(Mmax, D);
   auto kern = krige_chol_kernel<D>;
   GS_TRY(allow_dynamic_smem((const void*)kern, lay.total));
   int dev = 0, sms = 152;
@@ -984,7 +1001,14 @@ static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCholWarps * 32, lay.total));
   per_sm = std::max(per_sm, 1);
   const int blocks = (int)std::min<int64_t>((a.ntl + kCholWarps - 1) / kCholWarps, (int64_t)sms * per_sm);
-  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, g_tab, g_kc, flag, Mmax);
+  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, flag, Mmax);
+  GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  return GS_OK;
+}
+
+int route_launch(const uint8_t* flag, int64_t n, int* route, cudaStream_t stream) {
+  route_kernel<<<1, 256, 0, stream>>>(flag, n, route);
   GS_CUDA(cudaGetLastError());
   count_launch(1);
   return GS_OK;
@@ -992,12 +1016,9 @@ static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
 
 int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, cudaStream_t stream) {
   if (a.ntl == 0) return GS_OK;
-  ensure_tables();
-  int nf = 1;
-  for (int s = 0; s < m.ns; ++s) nf += m.s[s].aniso ? 1 : 0;
   const int Mmax = std::min(a.kout, GS_MIXED_MAX_NEIGHBORS) + a.p + 2;
-  if (a.dim == 2) return launch_chol<2>(a, m, flag, nf, Mmax, stream);
-  return launch_chol<3>(a, m, flag, nf, Mmax, stream);
+  if (a.dim == 2) return launch_chol<2>(a, m, flag, Mmax, stream);
+  return launch_chol<3>(a, m, flag, Mmax, stream);
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {

@@ -49,6 +49,8 @@ struct KrigeArgs {
   int64_t ntl;               // number of them (an upper bound when ntl_dev is set)
   const int64_t* ntl_dev;    // the number on the device, read by the kernel, or null
   int run;                   // consecutive targets per block sequence (0: 64)
+  const int* route_fp64;     // when set and nonzero: flag every valid system
+                             // for the FP64 re-solve without attempting it
 };
 
 // Mixed-precision kernel for systems with n <= 64 neighbours and at most
@@ -58,6 +60,10 @@ struct KrigeArgs {
 // threads), 32 / 64 forces it (binned launches).
 int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int force_rows,
                        cudaStream_t stream);
+// Routing for the rest of a call: *route = 1 when more than three quarters
+// of the first n systems were flagged (the FP32 attempt then costs more
+// than it saves), else 0.
+int route_launch(const uint8_t* flag, int64_t n, int* route, cudaStream_t stream);
 // FP64 re-solve of the flagged systems (bordered LDL^T, one system per
 // warp); clears the flag of every system it solves.  Systems left flagged
 // (near-singular, or beyond 64 neighbours) go to krige_fp64_launch.

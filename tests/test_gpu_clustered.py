@@ -110,3 +110,24 @@ def test_tuner_and_pinned_shapes(data):
     # an oracle check on a slice of the tuned call
     ref = O.krige(c, v, m, t[:600], **SEARCH)
     assert_close(base.value[:600], ref["value"], vs, 1e-9, "tuned value")
+
+
+@pytest.mark.parametrize("kind", ["ordinary", "universal", "external_drift"])
+def test_clustered_mixed_matches_fp64_build_at_scale(data, kind):
+    """300,000 targets, half in the blobs' cores: the mixed path (FP32 attempt,
+    routing, FP64 LDL^T and LU re-solves) against the plain FP64 build, whose
+    agreement with the oracle the test above pins."""
+    c, v, m, cov, _, _ = data
+    k = _predictor(kind, c, v, m, cov)
+    u = O.rng_uniform(46, 2 * 50 + 4 * 150_000)
+    centres = u[:100].reshape(50, 2) * EXTENT
+    near = centres[np.arange(150_000) % 50] + (u[100:300_100].reshape(-1, 2) - 0.5) * 60.0
+    far = u[300_100:600_100].reshape(-1, 2) * EXTENT
+    t = np.concatenate([near, far])
+    tcov = O.rng_uniform(47, len(t))
+    mixed = _predict(k, kind, t, tcov, "mixed")
+    plain = _predict(k, kind, t, tcov, "fp64")
+    assert ((mixed.status & 0x3f) == (plain.status & 0x3f)).all()
+    vs = float(np.mean(np.abs(v)))
+    assert_close(mixed.value, plain.value, vs, 1e-9, f"{kind} value")
+    assert_close(mixed.variance, plain.variance, 1e-3, 1e-9, f"{kind} variance")
