@@ -752,6 +752,14 @@ def profile_case(args):
             v, var = kr.predict_many(tg)
         torch.cuda.synchronize()
         print(f"profile case: {len(tg)} targets, mean estimate {np.nanmean(v):.6f}")
+    if args.profile_clustered:
+        # the clustered workload's data with a band of grid rows as targets
+        c, v, m, cov, tg, tcov, cuts, preds = clustered_setup()
+        t = tg[CL_GRID * 1000:CL_GRID * 1000 + args.profile_clustered]
+        for _ in range(2):
+            r = preds[0].predict_many(t, "mixed", full=True)
+        torch.cuda.synchronize()
+        print(f"profile clustered: {len(t)} targets, mean estimate {np.nanmean(r.value):.6f}")
     if args.profile_vecchia:
         from geostat_rs.model import Structure, VariogramModel
         n = args.profile_vecchia
@@ -787,6 +795,9 @@ def main():
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run one mixed-precision pass over the first N grid targets and exit "
                          "(the small case for ncu captures)")
+    ap.add_argument("--profile-clustered", type=int, default=0,
+                    help="run two ordinary-kriging passes of the clustered workload over N "
+                         "grid targets and exit")
     ap.add_argument("--profile-vecchia", type=int, default=0,
                     help="run one 16-candidate Vecchia batch on N points and exit")
     args = ap.parse_args()
@@ -796,7 +807,7 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
-    if args.profile_case or args.profile_vecchia:
+    if args.profile_case or args.profile_vecchia or args.profile_clustered:
         profile_case(args)
         return
     if args.impl == "reference":

@@ -463,6 +463,8 @@ struct NbGt {
 constexpr int64_t kTuneMinTargets = 65536;
 // Targets of the first chunk the candidates are timed on.
 constexpr int64_t kTuneSample = 262144;
+// Warps of the FP64 LDL^T re-solve (slot-covariance scratch, 16.6 KB each).
+constexpr int64_t kCholScratchWarps = 152 * 16;
 // Leading targets of each chunk whose FP32 failure rate routes the rest.
 constexpr int64_t kRouteSample = 16384;
 
@@ -596,8 +598,9 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   // FP64 scratch (plain build or re-solve)
   const int64_t budget = (int64_t)2 << 30;
   const int64_t fthreads = fp64_threads_for(nmax_all, budget);
-  DevBuf scratch;
+  DevBuf scratch, cscratch;
   GS_TRY(scratch.alloc((size_t)fp64_scratch_doubles(nmax_all, fthreads) * 8, stream));
+  if (mixed) GS_TRY(cscratch.alloc((size_t)chol_scratch_doubles(kCholScratchWarps) * 8, stream));
 
   cudaEvent_t ev[6] = {};
   if (timed)
@@ -744,7 +747,8 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       ca.tlist = (const int64_t*)tlist.ptr;
       ca.ntl = cn;
       ca.ntl_dev = (const int64_t*)nsel.ptr;
-      rc = krige_chol_launch(ca, k->dm, (uint8_t*)flag.ptr, stream);
+      rc = krige_chol_launch(ca, k->dm, (uint8_t*)flag.ptr, (double*)cscratch.ptr, kCholScratchWarps,
+                             stream);
       if (rc) break;
       b = sel_bytes;
       GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),

@@ -550,10 +550,13 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
 // flagged for the partial-pivoting LU solver below, which also decides
 // singularity exactly as the reference does.
 constexpr int kCholWarps = 4;
+// Packed slot covariances per warp (global scratch, L2-resident): keeping
+// them out of shared memory leaves room for two blocks per SM.
+constexpr int kCholSlotDoubles = GS_MIXED_MAX_NEIGHBORS * (GS_MIXED_MAX_NEIGHBORS + 1) / 2;
 constexpr double kCholPivotTol = 1e-11;
 
 struct CholLayout {
-  size_t off_ptab, off_warp, warp_bytes, off_a, off_lsc, off_lun, off_v, off_idx, total;
+  size_t off_ptab, off_warp, warp_bytes, off_a, off_cs, off_lsc, off_lun, off_v, off_idx, total;
 };
 
 __host__ __device__ inline CholLayout chol_layout(int Mmax, int dim) {
@@ -565,11 +568,13 @@ __host__ __device__ inline CholLayout chol_layout(int Mmax, int dim) {
     return r;
   };
   L.off_ptab = take(o, (size_t)(Mmax * (Mmax - 1) / 2) * 4);
+  constexpr int NS = GS_MIXED_MAX_NEIGHBORS;
   L.off_a = take(w, (size_t)(Mmax * (Mmax + 1) / 2) * 8);
+  L.off_cs = 0;  // the slot covariances live in global scratch (kCholSlotDoubles per warp)
   L.off_lsc = take(w, (size_t)Mmax * 8);
   L.off_lun = take(w, (size_t)Mmax * 8);
-  L.off_v = take(w, (size_t)dim * GS_MIXED_MAX_NEIGHBORS * sizeof(double));
-  L.off_idx = take(w, (size_t)GS_MIXED_MAX_NEIGHBORS * 4);
+  L.off_v = take(w, (size_t)dim * NS * sizeof(double));
+  L.off_idx = take(w, (size_t)6 * NS * 4);
   L.warp_bytes = w;
   L.off_warp = take(o, w * kCholWarps);
   L.total = o;
@@ -588,7 +593,7 @@ __device__ __forceinline__ double rcp_fp64(double d, double sc) {
 
 template <int D>
 __global__ void __launch_bounds__(kCholWarps * 32)
-    krige_chol_kernel(KrigeArgs a, DevModel m, uint8_t* flag, int Mmax) {
+    krige_chol_kernel(KrigeArgs a, DevModel m, uint8_t* flag, int Mmax, double* cs_scratch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const CholLayout L = chol_layout(Mmax, D);
   // pairs (i, j), 1 <= j <= i < Mmax, j descending: packed index << 16 | i << 8 | j
@@ -601,64 +606,151 @@ __global__ void __launch_bounds__(kCholWarps * 32)
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* wb = smem_raw + L.off_warp + (size_t)warp * L.warp_bytes;
+  constexpr int NS = GS_MIXED_MAX_NEIGHBORS;
   double* A = reinterpret_cast<double*>(wb + L.off_a);
+  // slot covariances, packed (this warp's part of the global scratch)
+  double* Cs = cs_scratch + ((int64_t)blockIdx.x * kCholWarps + warp) * kCholSlotDoubles;
   double* lsc = reinterpret_cast<double*>(wb + L.off_lsc);
   double* lun = reinterpret_cast<double*>(wb + L.off_lun);
-  double* P = reinterpret_cast<double*>(wb + L.off_v);  // P[d * 64 + s]: slot s's coordinates
-  int* ids = reinterpret_cast<int*>(wb + L.off_idx);
+  double* P = reinterpret_cast<double*>(wb + L.off_v);  // P[d * NS + s]: slot s's coordinates
+  int* sidx = reinterpret_cast<int*>(wb + L.off_idx);   // data point in slot s, or -1
+  int* newi = sidx + NS;                                 // this target's neighbours
+  int* mt = newi + NS;                                   // neighbour q already in a slot
+  int* um = mt + NS;                                     // k-th unplaced neighbour
+  int* act = um + NS;                                    // system row r -> slot (ascending)
+  int* frl = act + NS;                                   // newly filled slots (ascending)
   const double* coord[3] = {a.x, a.y, a.z};
-  constexpr int NS = GS_MIXED_MAX_NEIGHBORS;
   const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
   const int p = a.p;
   const int q = p + 2;
+  sidx[lane] = -1;
+  sidx[lane + 32] = -1;
+  __syncwarp();
   const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
-  for (int64_t it = (int64_t)blockIdx.x * kCholWarps + warp; it < ntl;
-       it += (int64_t)gridDim.x * kCholWarps) {
+  // each warp walks runs of consecutive list entries: neighbouring targets
+  // share most neighbours, whose slots keep their covariances (only pairs
+  // with a newly placed point are evaluated)
+  const int64_t nwarps = (int64_t)gridDim.x * kCholWarps;
+  const int64_t run = ntl >= 64 * nwarps ? 64 : (ntl + nwarps - 1) / nwarps;
+  for (int64_t r0 = ((int64_t)blockIdx.x * kCholWarps + warp) * run; r0 < ntl; r0 += nwarps * run) {
+  const int64_t r1 = r0 + run < ntl ? r0 + run : ntl;
+  for (int64_t it = r0; it < r1; ++it) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
     const int n = a.nbc[t];
     // only systems the mixed kernel flagged arrive; those outside this
     // kernel's bounds stay flagged for the LU solver
-    if (n < 1 || n < p || n > GS_MIXED_MAX_NEIGHBORS || p > GS_MIXED_MAX_DRIFT || n + q > Mmax)
-      continue;
+    if (n < 1 || n < p || n > NS || p > GS_MIXED_MAX_DRIFT || n + q > Mmax) continue;
     const int o = Mmax - (n + q);  // frame offset of the system
     const int ic = o + n;           // row of c; F at ic + 1 .. ic + p; z at ic + p + 1
     const int iz = ic + p + 1;
     const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
     const int32_t* nbt = a.nb + t * (int64_t)a.kout;
-    for (int s = lane; s < n; s += 32) {
-      const int idx = nbt[s];
-      ids[s] = idx;
-#pragma unroll
-      for (int d = 0; d < D; ++d) P[d * NS + s] = coord[d][idx];
+    // --- slots: kept neighbours stay, new ones fill the vacated slots
+    for (int s = lane; s < NS; s += 32) {
+      newi[s] = s < n ? nbt[s] : -2;
+      mt[s] = 0;
     }
     __syncwarp();
-    // build_lhs (kriging.rs:527-567): separations p_i - p_j, FP64 covariances
-    for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
-      double h0[3], h1[3];
+    bool keep[2];
 #pragma unroll
-      for (int d = 0; d < D; ++d) {
-        h0[d] = P[d * NS + i0] - P[d * NS + j0];
-        h1[d] = P[d * NS + i1] - P[d * NS + j1];
+    for (int h = 0; h < 2; ++h) {
+      const int id = sidx[lane + 32 * h];
+      int pos = -1;
+      if (id >= 0)
+        for (int u = 0; u < n; ++u) pos = newi[u] == id ? u : pos;
+      keep[h] = pos >= 0;
+      if (keep[h]) mt[pos] = 1;
+    }
+    __syncwarp();
+    const unsigned un0 = __ballot_sync(0xffffffffu, lane < n && !mt[lane]);
+    const unsigned un1 = __ballot_sync(0xffffffffu, lane + 32 < n && !mt[lane + 32]);
+    const unsigned fr0 = __ballot_sync(0xffffffffu, !keep[0]);
+    const unsigned fr1 = __ballot_sync(0xffffffffu, !keep[1]);
+    const unsigned below = (1u << lane) - 1u;
+    if ((un0 >> lane) & 1u) um[__popc(un0 & below)] = lane;
+    if ((un1 >> lane) & 1u) um[__popc(un0) + __popc(un1 & below)] = lane + 32;
+    const int n_un = __popc(un0) + __popc(un1);
+    __syncwarp();
+    bool fresh[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int s = lane + 32 * h;
+      const int rk = h == 0 ? __popc(fr0 & below) : __popc(fr0) + __popc(fr1 & below);
+      fresh[h] = !keep[h] && rk < n_un;
+      if (fresh[h]) {
+        const int id = newi[um[rk]];
+        sidx[s] = id;
+#pragma unroll
+        for (int d = 0; d < D; ++d) P[d * NS + s] = coord[d][id];
+        Cs[pk(s, s)] = m.c0 + (a.meas_err ? a.meas_err[id] : 0.0);
+      } else if (!keep[h]) {
+        sidx[s] = -1;
       }
-      const double c0 = cov_fp64<D>(m, h0);
-      const double c1 = cov_fp64<D>(m, h1);
-      A[pk(o + i0, o + j0)] = c0;
-      if (two) A[pk(o + i1, o + j1)] = c1;
-    });
+    }
+    const unsigned ac0 = __ballot_sync(0xffffffffu, keep[0] || fresh[0]);
+    const unsigned ac1 = __ballot_sync(0xffffffffu, keep[1] || fresh[1]);
+    const unsigned fs0 = __ballot_sync(0xffffffffu, fresh[0]);
+    const unsigned fs1 = __ballot_sync(0xffffffffu, fresh[1]);
+    const unsigned long long mfresh = (unsigned long long)fs0 | ((unsigned long long)fs1 << 32);
+    if (keep[0] || fresh[0]) act[__popc(ac0 & below)] = lane;
+    if (keep[1] || fresh[1]) act[__popc(ac0) + __popc(ac1 & below)] = lane + 32;
+    if (fresh[0]) frl[__popc(fs0 & below)] = lane;
+    if (fresh[1]) frl[__popc(fs0) + __popc(fs1 & below)] = lane + 32;
+    const int nfresh = __popc(fs0) + __popc(fs1);
+    __syncwarp();
+    // --- build_lhs (kriging.rs:527-567): FP64 covariances of the pairs with
+    // a newly placed point (separations p_i - p_j as in the reference)
+    auto cov_slots = [&](int s0, int u0) {
+      double h[3];
+#pragma unroll
+      for (int d = 0; d < D; ++d) h[d] = P[d * NS + s0] - P[d * NS + u0];
+      return cov_fp64<D>(m, h);
+    };
+    if (2 * nfresh >= n) {
+      for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+        const int s0 = act[i0], u0 = act[j0], s1 = act[i1], u1 = act[j1];
+        const double c0 = cov_slots(s0, u0);
+        const double c1 = cov_slots(s1, u1);
+        Cs[pk(s0, u0)] = c0;  // act ascending: s > u
+        if (two) Cs[pk(s1, u1)] = c1;
+      });
+    } else {
+      const int np = nfresh * n;
+      for (int e = lane; e < np; e += 32) {
+        const int f = e / n, c = e - f * n;
+        const int s0 = frl[f], u0 = act[c];
+        if (u0 != s0 && (!((mfresh >> u0) & 1ull) || u0 < s0)) {
+          const double cv = cov_slots(s0, u0);
+          Cs[s0 > u0 ? pk(s0, u0) : pk(u0, s0)] = cv;
+        }
+      }
+    }
+    __syncwarp();
+    // --- the system in slot order, embedded at the frame's bottom right
+    for (int e = lane; e < (n * (n + 1)) >> 1; e += 32) {
+      int r = 0;
+      {
+        // row of packed entry e: the largest r with r (r + 1) / 2 <= e
+        r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+        while ((r * (r + 1)) >> 1 > e) --r;
+        while (((r + 1) * (r + 2)) >> 1 <= e) ++r;
+      }
+      const int c = e - ((r * (r + 1)) >> 1);
+      A[pk(o + r, o + c)] = Cs[pk(act[r], act[c])];
+    }
     const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
     double scale = 0.0;
-    for (int s = lane; s < n; s += 32) {
-      const int idx = ids[s];
-      const double dg = m.c0 + (a.meas_err ? a.meas_err[idx] : 0.0);
-      A[pk(o + s, o + s)] = dg;
-      scale = fmax(scale, dg);
+    for (int r = lane; r < n; r += 32) {
+      const int s = act[r];
+      const int idx = sidx[s];
+      scale = fmax(scale, Cs[pk(s, s)]);
       const double pt[3] = {P[s], P[NS + s], D == 3 ? P[2 * NS + s] : 0.0};
       const double h[3] = {pt[0] - tp[0], pt[1] - tp[1], pt[2] - tp[2]};
-      A[pk(ic, o + s)] = cov_fp64<D>(m, h);
+      A[pk(ic, o + r)] = cov_fp64<D>(m, h);
       for (int k = 0; k < p; ++k)
-        A[pk(ic + 1 + k, o + s)] =
+        A[pk(ic + 1 + k, o + r)] =
             basis_at<D>(a, pt, a.drift ? a.drift + (int64_t)idx * a.nv : nullptr, k);
-      A[pk(iz, o + s)] = a.method == GS_SIMPLE ? a.val[idx] - a.sk_mean : a.val[idx];
+      A[pk(iz, o + r)] = a.method == GS_SIMPLE ? a.val[idx] - a.sk_mean : a.val[idx];
     }
     // the border block: C(0), the target's drift bases, zeros
     for (int r = lane; r < q; r += 32) {
@@ -753,6 +845,7 @@ __global__ void __launch_bounds__(kCholWarps * 32)
       }
     }
     __syncwarp();
+  }
   }
 }
 
@@ -990,7 +1083,7 @@ int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
 
 template <int D>
 static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int Mmax,
-                       cudaStream_t stream) {
+                       double* cs_scratch, int64_t scratch_warps, cudaStream_t stream) {
   const CholLayout lay = chol_layout(Mmax, D);
   auto kern = krige_chol_kernel<D>;
   GS_TRY(allow_dynamic_smem((const void*)kern, lay.total));
@@ -1000,8 +1093,11 @@ static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   int per_sm = 0;
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCholWarps * 32, lay.total));
   per_sm = std::max(per_sm, 1);
-  const int blocks = (int)std::min<int64_t>((a.ntl + kCholWarps - 1) / kCholWarps, (int64_t)sms * per_sm);
-  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, flag, Mmax);
+  const int blocks = (int)std::min<int64_t>(
+      std::min<int64_t>((a.ntl + kCholWarps - 1) / kCholWarps, (int64_t)sms * per_sm),
+      scratch_warps / kCholWarps);
+  if (blocks < 1) return fail(GS_ERR_INVALID_PARAMETER, "re-solve scratch too small");
+  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, flag, Mmax, cs_scratch);
   GS_CUDA(cudaGetLastError());
   count_launch(1);
   return GS_OK;
@@ -1014,11 +1110,14 @@ int route_launch(const uint8_t* flag, int64_t n, int* route, cudaStream_t stream
   return GS_OK;
 }
 
-int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, cudaStream_t stream) {
+int64_t chol_scratch_doubles(int64_t warps) { return warps * kCholSlotDoubles; }
+
+int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, double* scratch,
+                      int64_t scratch_warps, cudaStream_t stream) {
   if (a.ntl == 0) return GS_OK;
   const int Mmax = std::min(a.kout, GS_MIXED_MAX_NEIGHBORS) + a.p + 2;
-  if (a.dim == 2) return launch_chol<2>(a, m, flag, Mmax, stream);
-  return launch_chol<3>(a, m, flag, Mmax, stream);
+  if (a.dim == 2) return launch_chol<2>(a, m, flag, Mmax, scratch, scratch_warps, stream);
+  return launch_chol<3>(a, m, flag, Mmax, scratch, scratch_warps, stream);
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {

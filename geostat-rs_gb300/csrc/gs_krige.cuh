@@ -67,7 +67,11 @@ int route_launch(const uint8_t* flag, int64_t n, int* route, cudaStream_t stream
 // FP64 re-solve of the flagged systems (bordered LDL^T, one system per
 // warp); clears the flag of every system it solves.  Systems left flagged
 // (near-singular, or beyond 64 neighbours) go to krige_fp64_launch.
-int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, cudaStream_t stream);
+// scratch: chol_scratch_doubles(scratch_warps) doubles (the grid is capped
+// at scratch_warps warps; 152 * 16 warps fill a GB300).
+int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, double* scratch,
+                      int64_t scratch_warps, cudaStream_t stream);
+int64_t chol_scratch_doubles(int64_t warps);
 // Plain FP64 kernel, one system per thread (the reference's partial-pivoting
 // LU; the FP64 build and the last re-solve tier).
 // scratch must hold fp64_scratch_doubles(nmax, threads) doubles.
