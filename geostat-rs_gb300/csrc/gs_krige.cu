@@ -591,6 +591,114 @@ __device__ __forceinline__ double rcp_fp64(double d, double sc) {
   return fma(r, e, r);
 }
 
+// Warp-private neighbour slots of the FP64 re-solve kernels: slot s holds
+// data point sidx[s] (or -1), its coordinates P[d * NS + s] and, in global
+// scratch, the packed FP64 covariances cs between slot points.
+struct WarpSlots {
+  int* sidx;
+  int* newi;  // the target's neighbours
+  int* mt;    // neighbour q already in a slot
+  int* um;    // k-th unplaced neighbour
+  int* act;   // occupied slots, ascending (system row -> slot)
+  int* frl;   // newly filled slots, ascending
+  double* P;
+  double* cs;
+};
+
+// Places a target's n neighbours (nbt) in the slots -- neighbours already in
+// a slot keep it, new ones fill vacated slots -- and evaluates the FP64
+// covariances (kriging.rs:527-567, separations p_i - p_j as in the
+// reference) of every pair with a newly placed point.  Afterwards act[0..n)
+// lists the occupied slots.  Ends with a warp barrier.
+template <int D>
+__device__ __forceinline__ void slots_update(const WarpSlots& ws, const KrigeArgs& a,
+                                             const DevModel& m, const int32_t* nbt, int n,
+                                             int lane) {
+  constexpr int NS = GS_MIXED_MAX_NEIGHBORS;
+  const double* coord[3] = {a.x, a.y, a.z};
+  // --- slots: kept neighbours stay, new ones fill the vacated slots
+  for (int s = lane; s < NS; s += 32) {
+    ws.newi[s] = s < n ? nbt[s] : -2;
+    ws.mt[s] = 0;
+  }
+  __syncwarp();
+  bool keep[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int id = ws.sidx[lane + 32 * h];
+    int pos = -1;
+    if (id >= 0)
+      for (int u = 0; u < n; ++u) pos = ws.newi[u] == id ? u : pos;
+    keep[h] = pos >= 0;
+    if (keep[h]) ws.mt[pos] = 1;
+  }
+  __syncwarp();
+  const unsigned un0 = __ballot_sync(0xffffffffu, lane < n && !ws.mt[lane]);
+  const unsigned un1 = __ballot_sync(0xffffffffu, lane + 32 < n && !ws.mt[lane + 32]);
+  const unsigned fr0 = __ballot_sync(0xffffffffu, !keep[0]);
+  const unsigned fr1 = __ballot_sync(0xffffffffu, !keep[1]);
+  const unsigned below = (1u << lane) - 1u;
+  if ((un0 >> lane) & 1u) ws.um[__popc(un0 & below)] = lane;
+  if ((un1 >> lane) & 1u) ws.um[__popc(un0) + __popc(un1 & below)] = lane + 32;
+  const int n_un = __popc(un0) + __popc(un1);
+  __syncwarp();
+  bool fresh[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int s = lane + 32 * h;
+    const int rk = h == 0 ? __popc(fr0 & below) : __popc(fr0) + __popc(fr1 & below);
+    fresh[h] = !keep[h] && rk < n_un;
+    if (fresh[h]) {
+      const int id = ws.newi[ws.um[rk]];
+      ws.sidx[s] = id;
+#pragma unroll
+      for (int d = 0; d < D; ++d) ws.P[d * NS + s] = coord[d][id];
+      const double dg = m.c0 + (a.meas_err ? a.meas_err[id] : 0.0);
+      ws.cs[pk(s, s)] = dg;
+    } else if (!keep[h]) {
+      ws.sidx[s] = -1;
+    }
+  }
+  const unsigned ac0 = __ballot_sync(0xffffffffu, keep[0] || fresh[0]);
+  const unsigned ac1 = __ballot_sync(0xffffffffu, keep[1] || fresh[1]);
+  const unsigned fs0 = __ballot_sync(0xffffffffu, fresh[0]);
+  const unsigned fs1 = __ballot_sync(0xffffffffu, fresh[1]);
+  const unsigned long long mfresh = (unsigned long long)fs0 | ((unsigned long long)fs1 << 32);
+  if (keep[0] || fresh[0]) ws.act[__popc(ac0 & below)] = lane;
+  if (keep[1] || fresh[1]) ws.act[__popc(ac0) + __popc(ac1 & below)] = lane + 32;
+  if (fresh[0]) ws.frl[__popc(fs0 & below)] = lane;
+  if (fresh[1]) ws.frl[__popc(fs0) + __popc(fs1 & below)] = lane + 32;
+  const int nfresh = __popc(fs0) + __popc(fs1);
+  __syncwarp();
+  auto put = [&](int e, double v) { ws.cs[e] = v; };
+  auto cov_slots = [&](int s0, int u0) {
+    double h[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d) h[d] = ws.P[d * NS + s0] - ws.P[d * NS + u0];
+    return cov_fp64<D>(m, h);
+  };
+  if (2 * nfresh >= n) {
+    for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+      const int s0 = ws.act[i0], u0 = ws.act[j0], s1 = ws.act[i1], u1 = ws.act[j1];
+      const double c0 = cov_slots(s0, u0);
+      const double c1 = cov_slots(s1, u1);
+      put(pk(s0, u0), c0);  // act ascending: s > u
+      if (two) put(pk(s1, u1), c1);
+    });
+  } else {
+    const int np = nfresh * n;
+    for (int e = lane; e < np; e += 32) {
+      const int f = e / n, c = e - f * n;
+      const int s0 = ws.frl[f], u0 = ws.act[c];
+      if (u0 != s0 && (!((mfresh >> u0) & 1ull) || u0 < s0)) {
+        const double cv = cov_slots(s0, u0);
+        put(s0 > u0 ? pk(s0, u0) : pk(u0, s0), cv);
+      }
+    }
+  }
+  __syncwarp();
+}
+
 template <int D>
 __global__ void __launch_bounds__(kCholWarps * 32)
     krige_chol_kernel(KrigeArgs a, DevModel m, uint8_t* flag, int Mmax, double* cs_scratch) {
@@ -619,6 +727,7 @@ __global__ void __launch_bounds__(kCholWarps * 32)
   int* um = mt + NS;                                     // k-th unplaced neighbour
   int* act = um + NS;                                    // system row r -> slot (ascending)
   int* frl = act + NS;                                   // newly filled slots (ascending)
+  const WarpSlots ws{sidx, newi, mt, um, act, frl, P, Cs};
   const double* coord[3] = {a.x, a.y, a.z};
   const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
   const int p = a.p;
@@ -645,87 +754,7 @@ __global__ void __launch_bounds__(kCholWarps * 32)
     const int iz = ic + p + 1;
     const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
     const int32_t* nbt = a.nb + t * (int64_t)a.kout;
-    // --- slots: kept neighbours stay, new ones fill the vacated slots
-    for (int s = lane; s < NS; s += 32) {
-      newi[s] = s < n ? nbt[s] : -2;
-      mt[s] = 0;
-    }
-    __syncwarp();
-    bool keep[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int id = sidx[lane + 32 * h];
-      int pos = -1;
-      if (id >= 0)
-        for (int u = 0; u < n; ++u) pos = newi[u] == id ? u : pos;
-      keep[h] = pos >= 0;
-      if (keep[h]) mt[pos] = 1;
-    }
-    __syncwarp();
-    const unsigned un0 = __ballot_sync(0xffffffffu, lane < n && !mt[lane]);
-    const unsigned un1 = __ballot_sync(0xffffffffu, lane + 32 < n && !mt[lane + 32]);
-    const unsigned fr0 = __ballot_sync(0xffffffffu, !keep[0]);
-    const unsigned fr1 = __ballot_sync(0xffffffffu, !keep[1]);
-    const unsigned below = (1u << lane) - 1u;
-    if ((un0 >> lane) & 1u) um[__popc(un0 & below)] = lane;
-    if ((un1 >> lane) & 1u) um[__popc(un0) + __popc(un1 & below)] = lane + 32;
-    const int n_un = __popc(un0) + __popc(un1);
-    __syncwarp();
-    bool fresh[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int s = lane + 32 * h;
-      const int rk = h == 0 ? __popc(fr0 & below) : __popc(fr0) + __popc(fr1 & below);
-      fresh[h] = !keep[h] && rk < n_un;
-      if (fresh[h]) {
-        const int id = newi[um[rk]];
-        sidx[s] = id;
-#pragma unroll
-        for (int d = 0; d < D; ++d) P[d * NS + s] = coord[d][id];
-        Cs[pk(s, s)] = m.c0 + (a.meas_err ? a.meas_err[id] : 0.0);
-      } else if (!keep[h]) {
-        sidx[s] = -1;
-      }
-    }
-    const unsigned ac0 = __ballot_sync(0xffffffffu, keep[0] || fresh[0]);
-    const unsigned ac1 = __ballot_sync(0xffffffffu, keep[1] || fresh[1]);
-    const unsigned fs0 = __ballot_sync(0xffffffffu, fresh[0]);
-    const unsigned fs1 = __ballot_sync(0xffffffffu, fresh[1]);
-    const unsigned long long mfresh = (unsigned long long)fs0 | ((unsigned long long)fs1 << 32);
-    if (keep[0] || fresh[0]) act[__popc(ac0 & below)] = lane;
-    if (keep[1] || fresh[1]) act[__popc(ac0) + __popc(ac1 & below)] = lane + 32;
-    if (fresh[0]) frl[__popc(fs0 & below)] = lane;
-    if (fresh[1]) frl[__popc(fs0) + __popc(fs1 & below)] = lane + 32;
-    const int nfresh = __popc(fs0) + __popc(fs1);
-    __syncwarp();
-    // --- build_lhs (kriging.rs:527-567): FP64 covariances of the pairs with
-    // a newly placed point (separations p_i - p_j as in the reference)
-    auto cov_slots = [&](int s0, int u0) {
-      double h[3];
-#pragma unroll
-      for (int d = 0; d < D; ++d) h[d] = P[d * NS + s0] - P[d * NS + u0];
-      return cov_fp64<D>(m, h);
-    };
-    if (2 * nfresh >= n) {
-      for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
-        const int s0 = act[i0], u0 = act[j0], s1 = act[i1], u1 = act[j1];
-        const double c0 = cov_slots(s0, u0);
-        const double c1 = cov_slots(s1, u1);
-        Cs[pk(s0, u0)] = c0;  // act ascending: s > u
-        if (two) Cs[pk(s1, u1)] = c1;
-      });
-    } else {
-      const int np = nfresh * n;
-      for (int e = lane; e < np; e += 32) {
-        const int f = e / n, c = e - f * n;
-        const int s0 = frl[f], u0 = act[c];
-        if (u0 != s0 && (!((mfresh >> u0) & 1ull) || u0 < s0)) {
-          const double cv = cov_slots(s0, u0);
-          Cs[s0 > u0 ? pk(s0, u0) : pk(u0, s0)] = cv;
-        }
-      }
-    }
-    __syncwarp();
+    slots_update<D>(ws, a, m, nbt, n, lane);
     // --- the system in slot order, embedded at the frame's bottom right
     for (int e = lane; e < (n * (n + 1)) >> 1; e += 32) {
       int r = 0;
