@@ -618,71 +618,121 @@ def clustered_bench(args, log):
 
 
 def serving_bench(args, log):
-    """Serving loop on resident data sets: Poisson arrivals of prediction
-    requests (log-uniform target counts in [1, 1e6], n_max 16..64) and Vecchia
-    log-likelihood requests (m = 30).  Data sets: 2-D 10k (n_max 16), 3-D 50k
-    (n_max 32), 2-D 200k (n_max 48), 3-D 500k (n_max 64) for kriging; 2-D 10k
-    and 50k for Vecchia."""
+    """Serving loop on eight resident data sets -- 10k, 50k, 200k, 500k, 1M,
+    1M, 2M and 4M points; 2-D (uniform in 1000 x 1000 m, nugget 0.1 +
+    Sph(1, 200 m)): 10k, 200k, 1M, 2M; 3-D (the 3-D workload's box and model):
+    50k, 500k, 1M, 4M -- each with ordinary-kriging predictors at n_max 16,
+    32, 48 and 64, and Vecchia plans (m = 30) on the 2-D sets of 10k, 200k and
+    1M points.  Poisson arrivals at 200 requests/s: 85 % predictions
+    (log-uniform target counts in [1, 1e6], random data set and n_max), 15 %
+    Vecchia log-likelihoods at a new parameter vector.  The first requests of
+    the same stream are then served by the plain FP64 build and compared."""
     import geostat_rs as G
     from geostat_rs.model import Structure, VariogramModel
     rng = np.random.default_rng(SEED + 11)
     t0 = time.time()
     m2 = VariogramModel(0.1, [Structure("spherical", 1.0, 200.0)])
     m3 = make_model()
-    specs = [(2, 10_000, 16, m2), (3, 50_000, 32, m3), (2, 200_000, 48, m2), (3, 500_000, 64, m3)]
-    srv = G.Server(mem_budget_bytes=32 << 30, executors=3)
-    kds, pools = [], []
-    for dim, n, kmax, mdl in specs:
+    specs = [(2, 10_000), (3, 50_000), (2, 200_000), (3, 500_000), (2, 1_000_000),
+             (3, 1_000_000), (2, 2_000_000), (3, 4_000_000)]
+    nmaxes = (16, 32, 48, 64)
+    srv = G.Server(mem_budget_bytes=48 << 30, executors=3)
+    kds, boxes, vds, keep = [], [], [], []
+    for q, (dim, n) in enumerate(specs):
         box = np.array([1000.0, 1000.0]) if dim == 2 else np.asarray(BOX)
-        cc = G.rng_uniform(SEED + n, dim * n).reshape(n, dim) * box
-        vv = G.rff_field(cc, mdl, 1024, SEED + n + 1)
-        k = G.Kriging.new(G.PointSet(cc, vv), mdl, G.KrigingConfig(max_neighbors=kmax))
-        kds.append(srv.add_kriging(k))
-        pools.append(rng.uniform(0, 1, size=(1_000_000, dim)) * box)
-    vds = []
-    base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
-    for n in (10_000, 50_000):
-        cc = G.rng_uniform(SEED + 3 * n, 2 * n).reshape(n, 2)
-        vv = 0.5 + G.rff_field(cc, base, 1024, SEED + 3 * n + 1)
-        vds.append(srv.add_vecchia(G.VecchiaPlan(G.PointSet(cc, vv), 30)))
-    log(f"[bench] serving set-up {time.time() - t0:.1f}s")
+        mdl = m2 if dim == 2 else m3
+        cc = G.rng_uniform(SEED + 100 + q, dim * n).reshape(n, dim) * box
+        vv = G.rff_field(cc, mdl, 1024, SEED + 200 + q)
+        ps = G.PointSet(cc, vv)
+        row = []
+        for km in nmaxes:
+            k = G.Kriging.new(ps, mdl, G.KrigingConfig(max_neighbors=km))
+            keep.append(k)
+            row.append(srv.add_kriging(k))
+        kds.append(row)
+        boxes.append(box)
+        if dim == 2 and n <= 1_000_000:
+            plan = G.VecchiaPlan(ps, 30)
+            keep.append(plan)
+            vds.append(srv.add_vecchia(plan))
+    log(f"[bench] serving set-up {time.time() - t0:.1f}s (8 data sets, 32 predictors, "
+        f"{len(vds)} Vecchia plans)")
     nreq, rate = args.serve_requests, 200.0
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
     jobs = []
     for q in range(nreq):
         if rng.uniform() < 0.15:
             f = rng.uniform(0.5, 2.0)
-            jobs.append(("ll", vds[q % 2], VariogramModel(0.02 * f, [Structure("matern25", 1.0, 0.05 * f)])))
+            mdl = VariogramModel(0.05 * f, [Structure("matern25", 1.0, 60.0 * f)])
+            jobs.append(("ll", vds[int(rng.integers(0, len(vds)))], mdl))
         else:
-            d = int(rng.integers(0, len(kds)))
+            d = int(rng.integers(0, len(specs)))
+            km = int(rng.integers(0, len(nmaxes)))
             nt = int(np.exp(rng.uniform(0.0, np.log(1e6))))
-            st = int(rng.integers(0, len(pools[d]) - nt + 1))
-            jobs.append(("p", kds[d], pools[d][st:st + nt]))
+            t = rng.uniform(0, 1, size=(nt, specs[d][0])) * boxes[d]
+            jobs.append(("p", kds[d][km], t))
     # warm-up: one request of each kind
-    srv.wait(srv.submit_predict(kds[0], pools[0][:100]))
-    srv.wait(srv.submit_loglik(vds[0], base))
+    srv.wait(srv.submit_predict(kds[0][0], np.full((10, 2), 500.0)))
+    srv.wait(srv.submit_loglik(vds[0], m2))
     _, _, done0, launches0 = srv.stats()
-    reqs, targets = [], 0
-    start = time.perf_counter()
-    for (kind, ds, arg), at in zip(jobs, arrivals):
-        delay = start + at - time.perf_counter()
-        if delay > 0:
-            time.sleep(delay)
-        reqs.append(srv.submit_predict(ds, arg) if kind == "p" else srv.submit_loglik(ds, arg))
-        if kind == "p":
-            targets += len(arg)
-    lat = [srv.wait(r) for r in reqs]
-    wall = time.perf_counter() - start
-    lat = np.asarray(lat)
+
+    def serve(subset, paced):
+        reqs, targets = [], 0
+        start = time.perf_counter()
+        for q in subset:
+            kind, ds, arg = jobs[q]
+            if paced:
+                delay = start + arrivals[q] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            reqs.append(srv.submit_predict(ds, arg) if kind == "p" else srv.submit_loglik(ds, arg))
+            if kind == "p":
+                targets += len(arg)
+        lat = np.asarray([srv.wait(r) for r in reqs])
+        return reqs, lat, time.perf_counter() - start, targets
+
+    reqs, lat, wall, targets = serve(range(nreq), True)
     _, _, done, launches = srv.stats()
+    # the plain FP64 build on the first requests of the stream, compared
+    nsub = min(nreq, args.serve_fp64_requests)
+    srv.set_precision("fp64")
+    reqs64, lat64, wall64, targets64 = serve(range(nsub), False)
+    srv.set_precision("mixed")
+    worst_v = worst_var = worst_ll = 0.0
+    status_ok = True
+    for q in range(nsub):
+        (kind, ds, arg), a_, b_ = jobs[q], reqs[q].out, reqs64[q].out
+        if kind == "p":
+            vs = max(float(np.mean(np.abs(b_[0][np.isfinite(b_[0])]))) if len(b_[0]) else 1.0, 1e-300)
+            ok = np.isfinite(b_[0])
+            worst_v = max(worst_v, float(np.max(np.abs(a_[0][ok] - b_[0][ok]) /
+                                                np.maximum(np.abs(b_[0][ok]), vs), initial=0.0)))
+            worst_var = max(worst_var, float(np.max(np.abs(a_[1][ok] - b_[1][ok]) /
+                                                    np.maximum(np.abs(b_[1][ok]), 1e-3),
+                                                    initial=0.0)))
+            status_ok = status_ok and bool(((a_[2] & 0x3f) == (b_[2] & 0x3f)).all())
+        else:
+            worst_ll = max(worst_ll, abs(a_[0][0] - b_[0][0]) / abs(b_[0][0]))
     srv.close()
+    log(f"[bench] serving: p50 {np.percentile(lat, 50):.1f} ms, p99 {np.percentile(lat, 99):.1f} ms, "
+        f"{targets / wall / 1e6:.1f} M targets/s; fp64 build on {nsub} requests "
+        f"{targets64 / wall64 / 1e6:.2f} M targets/s")
     return {"requests": nreq, "arrival_rate_per_s": rate, "executors": 3,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "wall_s": wall, "targets": targets,
             "targets_per_s": targets / wall, "requests_per_s": nreq / wall,
             "launches": launches - launches0,
-            "datasets": "kriging 2-D 10k/n_max 16, 3-D 50k/32, 2-D 200k/48, 3-D 500k/64; "
-                        "Vecchia 2-D 10k and 50k, m = 30",
+            "fp64_gpu_build": {"requests": nsub, "unpaced": True, "targets": targets64,
+                               "targets_per_s": targets64 / wall64,
+                               "p50_ms": float(np.percentile(lat64, 50)),
+                               "p99_ms": float(np.percentile(lat64, 99)),
+                               "max_rel_value": worst_v, "max_rel_variance": worst_var,
+                               "max_rel_loglik": worst_ll, "status_match": status_ok,
+                               "tolerance": "1e-9 (floors: mean |estimate|, 1e-3 sill)"},
+            "datasets": "2-D 10k/200k/1M/2M (1000 x 1000 m, 0.1 + Sph(1, 200 m)); 3-D "
+                        "50k/500k/1M/4M (2000 x 2000 x 200 m, the 3-D workload's model); "
+                        "ordinary kriging at n_max 16/32/48/64 each; Vecchia plans m = 30 on "
+                        "the 2-D 10k/200k/1M sets",
             "mix": "85% predictions (target count log-uniform in [1, 1e6]), 15% log-likelihoods"}
 
 
@@ -790,6 +840,8 @@ def main():
                     help="oracle targets per band of the clustered workload")
     ap.add_argument("--vpred-n", type=int, default=500_000,
                     help="targets of the Vecchia joint-prediction timing (0: skip)")
+    ap.add_argument("--serve-fp64-requests", type=int, default=60,
+                    help="leading requests of the serving stream re-served by the FP64 build")
     ap.add_argument("--serve-requests", type=int, default=1000,
                     help="requests of the serving-loop run (0: skip)")
     ap.add_argument("--profile-case", type=int, default=0,

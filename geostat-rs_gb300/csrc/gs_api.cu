@@ -600,7 +600,9 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   const int64_t fthreads = fp64_threads_for(nmax_all, budget);
   DevBuf scratch, cscratch;
   GS_TRY(scratch.alloc((size_t)fp64_scratch_doubles(nmax_all, fthreads) * 8, stream));
-  if (mixed) GS_TRY(cscratch.alloc((size_t)chol_scratch_doubles(kCholScratchWarps) * 8, stream));
+  // slot scratch for at most one warp per target of a chunk
+  const int64_t cwarps = std::min<int64_t>(kCholScratchWarps, (chunk + 3) / 4 * 4);
+  if (mixed) GS_TRY(cscratch.alloc((size_t)chol_scratch_doubles(cwarps) * 8, stream));
 
   cudaEvent_t ev[6] = {};
   if (timed)
@@ -747,8 +749,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       ca.tlist = (const int64_t*)tlist.ptr;
       ca.ntl = cn;
       ca.ntl_dev = (const int64_t*)nsel.ptr;
-      rc = krige_chol_launch(ca, k->dm, (uint8_t*)flag.ptr, (double*)cscratch.ptr, kCholScratchWarps,
-                             stream);
+      rc = krige_chol_launch(ca, k->dm, (uint8_t*)flag.ptr, (double*)cscratch.ptr, cwarps, stream);
       if (rc) break;
       b = sel_bytes;
       GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, b, thrust::counting_iterator<int64_t>(0),

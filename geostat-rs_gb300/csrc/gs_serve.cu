@@ -17,6 +17,7 @@
 // bit-identical alone or in a batch.
 #include <algorithm>
 #include <chrono>
+#include <atomic>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -82,6 +83,7 @@ struct gs_server {
   int64_t in_use = 0;
   int64_t next_id = 1;
   int64_t batches = 0;
+  std::atomic<int> precision{GS_PREC_MIXED};
   bool stop = false;
   std::vector<std::thread> workers;
   std::vector<double> latencies_ms;
@@ -96,7 +98,9 @@ int64_t request_bytes(const gs_server* S, const Request& r) {
   if (r.kind == 0) {
     const gs_kriging* k = S->datasets[r.dataset].k;
     const int64_t kout = k->cfg.max_neighbors > 0 ? k->cfg.max_neighbors : GS_MAX_SYSTEM;
-    return r.nt * (3 * 8 + 8 + 8 + 8 + 1 + 4 * kout + 4 + 1 + 8) + (1 << 20);
+    // + the FP64 re-solve's slot scratch (up to 40.5 MB)
+    return r.nt * (3 * 8 + 8 + 8 + 8 + 1 + 4 * kout + 4 + 1 + 8) + (1 << 20) +
+           std::min<int64_t>(r.nt * 16640, (int64_t)152 * 16 * 16640);
   }
   return vecchia_plan_points(S->datasets[r.dataset].plan) * 9 + (1 << 20);
 }
@@ -123,7 +127,7 @@ int run_predictions(gs_server* S, const std::vector<Request*>& batch, cudaStream
   }
   GS_TRY(predict_device(k, nt, (double*)x.ptr, (double*)y.ptr, (double*)z.ptr, nullptr,
                         (double*)v.ptr, (double*)var.ptr, nullptr, (uint8_t*)st.ptr,
-                        GS_PREC_MIXED, s));
+                        S->precision.load(), s));
   off = 0;
   for (Request* r : batch) {
     GS_CUDA(cudaMemcpyAsync(r->value, (double*)v.ptr + off, r->nt * 8, cudaMemcpyDeviceToHost, s));
@@ -144,7 +148,7 @@ int run_logliks(gs_server* S, const std::vector<Request*>& batch, cudaStream_t s
   std::vector<double> ll(models.size());
   std::vector<int32_t> st(models.size());
   GS_TRY(vecchia_eval(plan, (int64_t)models.size(), models.data(), ll.data(), st.data(),
-                      GS_PREC_MIXED, s));
+                      S->precision.load(), s));
   for (size_t i = 0; i < batch.size(); ++i) {
     *batch[i]->loglik = ll[i];
     if (batch[i]->lstatus) *batch[i]->lstatus = st[i];
@@ -315,6 +319,14 @@ int gs_server_submit_loglik(gs_server* S, int32_t dataset, const gs_model* model
   r->loglik = loglik;
   r->lstatus = status;
   return submit(S, std::move(r), request_id);
+}
+
+int gs_server_set_precision(gs_server* s, int precision) {
+  if (!s) return gs::fail(GS_ERR_INVALID_PARAMETER, "null server");
+  if (precision != GS_PREC_MIXED && precision != GS_PREC_FP64)
+    return gs::fail(GS_ERR_INVALID_PARAMETER, "unknown precision");
+  s->precision.store(precision);
+  return GS_OK;
 }
 
 int gs_server_wait(gs_server* S, int64_t request_id, double* latency_ms) {

@@ -83,6 +83,7 @@ SIGNATURES = {
     "gs_server_submit_predict": (_int, [_vp, _i32, _i64, _pd, _pd, _pd, _pd, _pd, _pu8, _pi64]),
     "gs_server_submit_loglik": (_int, [_vp, _i32, _pm, _pd, _pi32, _pi64]),
     "gs_server_wait": (_int, [_vp, _i64, _pd]),
+    "gs_server_set_precision": (_int, [_vp, _int]),
     "gs_server_stats": (_int, [_vp, _pd, _pd, _pi64, _pi64]),
     "gs_server_destroy": (None, [_vp]),
     "gs_kriging_predict_grid": (_int, [_vp, _pd, _pd, _pi64, _pd, _pd, _pu8, _int, _vp]),

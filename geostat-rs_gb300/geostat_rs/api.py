@@ -587,6 +587,10 @@ class Server:
                                                        _p(st, C.c_int32), C.byref(rid)))
         return Server._Req(rid.value, ms, (ll, st))
 
+    def set_precision(self, precision: str):
+        """Precision of the launches formed from now on ("mixed" or "fp64")."""
+        _abi.check(_abi.load().gs_server_set_precision(self._h, PRECISIONS[precision]))
+
     def wait(self, req) -> float:
         lat = C.c_double()
         _abi.check(_abi.load().gs_server_wait(self._h, req.id, C.byref(lat)))

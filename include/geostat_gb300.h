@@ -293,6 +293,9 @@ int gs_server_submit_predict(gs_server* s, int32_t dataset, int64_t nt, const do
                              uint8_t* status, int64_t* request_id);
 int gs_server_submit_loglik(gs_server* s, int32_t dataset, const gs_model* model, double* loglik,
                             int32_t* status, int64_t* request_id);
+/* Precision of the launches formed from now on (GS_PREC_MIXED by default;
+ * GS_PREC_FP64 serves the same requests through the plain FP64 build). */
+int gs_server_set_precision(gs_server* s, int precision);
 int gs_server_wait(gs_server* s, int64_t request_id, double* latency_ms);
 int gs_server_stats(gs_server* s, double* p50_ms, double* p99_ms, int64_t* completed,
                     int64_t* batches);
