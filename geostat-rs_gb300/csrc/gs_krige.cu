@@ -581,10 +581,11 @@ __host__ __device__ inline CholLayout chol_layout(int Mmax, int dim) {
   return L;
 }
 
-// 1/d to FP64 accuracy: FP32 estimate of the power-of-two scaled value, two
-// Newton steps (e = 1 - d r, r += r e).  sc scales d into [2^-40, 2].
-__device__ __forceinline__ double rcp_fp64(double d, double sc) {
-  double r = (double)__frcp_rn((float)(d * sc)) * sc;
+// 1/d to FP64 accuracy: FP32 estimate, two Newton steps (e = 1 - d r,
+// r += r e).  sc (a power of two) scales d into FP32's range first when the
+// system's scale is outside [1e-20, 1e20] (scaled = true).
+__device__ __forceinline__ double rcp_fp64(double d, double sc, bool scaled) {
+  double r = scaled ? (double)__frcp_rn((float)(d * sc)) * sc : (double)__frcp_rn((float)d);
   double e = fma(-d, r, 1.0);
   r = fma(r, e, r);
   e = fma(-d, r, 1.0);
@@ -794,15 +795,17 @@ __global__ void __launch_bounds__(kCholWarps * 32)
     int ex = 0;
     frexp(scale, &ex);
     const double sc = ldexp(1.0, -ex);
+    const bool scaled = !(scale > 1e-20 && scale < 1e20);  // pivots then fit FP32
+    const double tol = kCholPivotTol * scale;
     __syncwarp();
     bool ok = true;
     for (int k = o; k < ic; ++k) {
       const double d = A[pk(k, k)];
-      if (!(d > kCholPivotTol * scale)) {  // the same value in every lane
+      if (!(d > tol)) {  // the same value in every lane
         ok = false;
         break;
       }
-      const double r = rcp_fp64(d, sc);
+      const double r = rcp_fp64(d, sc, scaled);
       for (int i = k + 1 + lane; i < Mmax; i += 32) {
         const double v = A[pk(i, k)];
         lun[i] = v;
@@ -810,8 +813,23 @@ __global__ void __launch_bounds__(kCholWarps * 32)
       }
       __syncwarp();
       const int T = ((Mmax - 1 - k) * (Mmax - k)) >> 1;
-#pragma unroll 4
-      for (int e = lane; e < T; e += 32) {
+      // pairs are distinct, so four of them are loaded before any store
+      int e = lane;
+      for (; e + 96 < T; e += 128) {
+        uint32_t en[4];
+        double av[4], lv[4], uv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) en[u] = ptab[e + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          av[u] = A[en[u] >> 16];
+          lv[u] = lsc[(en[u] >> 8) & 255u];
+          uv[u] = lun[en[u] & 255u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) A[en[u] >> 16] = fma(-lv[u], uv[u], av[u]);
+      }
+      for (; e < T; e += 32) {
         const uint32_t en = ptab[e];
         const int pe = (int)(en >> 16), i = (int)((en >> 8) & 255u), j = (int)(en & 255u);
         A[pe] = fma(-lsc[i], lun[j], A[pe]);
