@@ -220,6 +220,60 @@ __device__ __forceinline__ double rho_fp64(int kind, double d) {
   }
 }
 
+// FP64 exp(-x) by Tang's table-driven method (P. T. P. Tang, "Table-driven
+// implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2), 1989), for the re-solve kernels' covariances:
+// x = (64 m + j) ln2/64 + r with |r| <= ln2/128, so
+//     exp(-x) = 2^-m * 2^(-j/64) * exp(-r),
+// exp(-r) - 1 from its Taylor polynomial through r^5 (remainder < 4e-17),
+// 2^(-j/64) as a two-double table entry, ln2/64 in two parts (the first with
+// 36 significant bits, so k * part1 is exact).  About 1 ulp; x >= 708 gives 0.
+struct Exp64Table {
+  double hi[64], lo[64];  // 2^(-j/64) = hi + lo
+  double l1, l2, inv;     // ln2/64 = l1 + l2, 64/ln2
+};
+void exp64_table_host(Exp64Table* t);
+
+__device__ __forceinline__ double expneg_fp64(double x, const Exp64Table& T) {
+  const double magic = 6755399441055744.0;  // 1.5 * 2^52: integer part in the low word
+  const bool in = x < 708.0;
+  const double xc = in ? x : 0.0;
+  const double km = fma(xc, T.inv, magic);
+  const int k = __double2loint(km);
+  const double kd = km - magic;
+  const double r = fma(-kd, T.l2, fma(-kd, T.l1, xc));
+  double p = fma(r, -1.0 / 120.0, 1.0 / 24.0);
+  p = fma(r, p, -1.0 / 6.0);
+  p = fma(r, p, 0.5);
+  p = fma(r, p, -1.0);
+  p *= r;
+  const int j = k & 63, mexp = k >> 6;
+  const double th = T.hi[j];
+  const double res = th + fma(th, p, T.lo[j]);  // in (0.49, 1.01): exponent 1022 or 1023
+  const double scaled = __hiloint2double(__double2hiint(res) - (mexp << 20), __double2loint(res));
+  return in ? scaled : 0.0;
+}
+
+// rho_fp64 with expneg_fp64 in place of exp.
+__device__ __forceinline__ double rho_fp64x(int kind, double d, const Exp64Table& T) {
+  switch (kind) {
+    case GS_KIND_SPHERICAL:
+      return d >= 1.0 ? 0.0 : 1.0 - (1.5 * d - 0.5 * d * d * d);
+    case GS_KIND_EXPONENTIAL:
+      return expneg_fp64(d, T);
+    case GS_KIND_GAUSSIAN:
+      return expneg_fp64(d * d, T);
+    case GS_KIND_MATERN15: {
+      double s = 1.7320508075688772 * d;
+      return (1.0 + s) * expneg_fp64(s, T);
+    }
+    default: {  // GS_KIND_MATERN25
+      double s = 2.23606797749979 * d;
+      return (1.0 + s + s * s / 3.0) * expneg_fp64(s, T);
+    }
+  }
+}
+
 // Covariance C(h) = c0 - gamma(h) in FP64 for a separation vector.
 template <int D>
 __device__ __forceinline__ double cov_fp64(const DevModel& m, const double* h) {
@@ -244,6 +298,35 @@ __device__ __forceinline__ double cov_fp64(const DevModel& m, const double* h) {
       for (int d = 0; d < D; ++d) q += h[d] * h[d];
     }
     acc += s.sill * rho_fp64(s.kind, sqrt(q) * s.inv_range);
+  }
+  return acc;
+}
+
+// cov_fp64 with the table-driven exp (the same operation order otherwise).
+template <int D>
+__device__ __forceinline__ double cov_fp64x(const DevModel& m, const double* h,
+                                            const Exp64Table& T) {
+  bool zero = true;
+#pragma unroll
+  for (int d = 0; d < D; ++d) zero = zero && (h[d] == 0.0);
+  if (zero) return m.c0;
+  double acc = 0.0;
+  for (int k = 0; k < m.ns; ++k) {
+    const DevStruct& s = m.s[k];
+    double q = 0.0;
+    if (s.aniso) {
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        double e = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) e += s.rot[r * 3 + c] * h[c];
+        q += e * e;
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) q += h[d] * h[d];
+    }
+    acc += s.sill * rho_fp64x(s.kind, sqrt(q) * s.inv_range, T);
   }
   return acc;
 }

@@ -67,6 +67,22 @@ void df_consts_host(ExpTable* tab, DfConsts* k) {
   }
 }
 
+void exp64_table_host(Exp64Table* t) {
+  const long double ln2 = 0.693147180559945309417232121458176568L;
+  const long double L = ln2 / 64.0L;
+  int e;
+  const long double mant = frexpl(L, &e);
+  const double l1 = (double)ldexpl(roundl(ldexpl(mant, 36)), e - 36);  // 36 bits
+  t->l1 = l1;
+  t->l2 = (double)(L - (long double)l1);
+  t->inv = (double)(64.0L / ln2);
+  for (int j = 0; j < 64; ++j) {
+    const long double v = exp2l(-(long double)j / 64.0L);
+    t->hi[j] = (double)v;
+    t->lo[j] = (double)(v - (long double)t->hi[j]);
+  }
+}
+
 // ---------------------------------------------------------------- model --
 static const double kRadsPerDeg = 3.14159265358979323846 / 180.0;
 

@@ -613,8 +613,8 @@ struct WarpSlots {
 // lists the occupied slots.  Ends with a warp barrier.
 template <int D>
 __device__ __forceinline__ void slots_update(const WarpSlots& ws, const KrigeArgs& a,
-                                             const DevModel& m, const int32_t* nbt, int n,
-                                             int lane) {
+                                             const DevModel& m, const Exp64Table& et,
+                                             const int32_t* nbt, int n, int lane) {
   constexpr int NS = GS_MIXED_MAX_NEIGHBORS;
   const double* coord[3] = {a.x, a.y, a.z};
   // --- slots: kept neighbours stay, new ones fill the vacated slots
@@ -676,7 +676,7 @@ __device__ __forceinline__ void slots_update(const WarpSlots& ws, const KrigeArg
     double h[3];
 #pragma unroll
     for (int d = 0; d < D; ++d) h[d] = ws.P[d * NS + s0] - ws.P[d * NS + u0];
-    return cov_fp64<D>(m, h);
+    return cov_fp64x<D>(m, h, et);
   };
   if (2 * nfresh >= n) {
     for_pairs2(n, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
@@ -702,8 +702,19 @@ __device__ __forceinline__ void slots_update(const WarpSlots& ws, const KrigeArg
 
 template <int D>
 __global__ void __launch_bounds__(kCholWarps * 32)
-    krige_chol_kernel(KrigeArgs a, DevModel m, uint8_t* flag, int Mmax, double* cs_scratch) {
+    krige_chol_kernel(KrigeArgs a, DevModel m, Exp64Table et_g, uint8_t* flag, int Mmax,
+                      double* cs_scratch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Exp64Table et;
+  for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+    et.hi[q] = et_g.hi[q];
+    et.lo[q] = et_g.lo[q];
+  }
+  if (threadIdx.x == 0) {
+    et.l1 = et_g.l1;
+    et.l2 = et_g.l2;
+    et.inv = et_g.inv;
+  }
   const CholLayout L = chol_layout(Mmax, D);
   // pairs (i, j), 1 <= j <= i < Mmax, j descending: packed index << 16 | i << 8 | j
   uint32_t* ptab = reinterpret_cast<uint32_t*>(smem_raw + L.off_ptab);
@@ -755,7 +766,7 @@ __global__ void __launch_bounds__(kCholWarps * 32)
     const int iz = ic + p + 1;
     const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
     const int32_t* nbt = a.nb + t * (int64_t)a.kout;
-    slots_update<D>(ws, a, m, nbt, n, lane);
+    slots_update<D>(ws, a, m, et, nbt, n, lane);
     // --- the system in slot order, embedded at the frame's bottom right
     for (int e = lane; e < (n * (n + 1)) >> 1; e += 32) {
       int r = 0;
@@ -776,7 +787,7 @@ __global__ void __launch_bounds__(kCholWarps * 32)
       scale = fmax(scale, Cs[pk(s, s)]);
       const double pt[3] = {P[s], P[NS + s], D == 3 ? P[2 * NS + s] : 0.0};
       const double h[3] = {pt[0] - tp[0], pt[1] - tp[1], pt[2] - tp[2]};
-      A[pk(ic, o + r)] = cov_fp64<D>(m, h);
+      A[pk(ic, o + r)] = cov_fp64x<D>(m, h, et);
       for (int k = 0; k < p; ++k)
         A[pk(ic + 1 + k, o + r)] =
             basis_at<D>(a, pt, a.drift ? a.drift + (int64_t)idx * a.nv : nullptr, k);
@@ -1082,8 +1093,13 @@ static ExpTable g_tab;
 static DfConsts g_kc;
 static std::once_flag g_tab_once;
 
+static Exp64Table g_et;
+
 static void ensure_tables() {
-  std::call_once(g_tab_once, [] { df_consts_host(&g_tab, &g_kc); });
+  std::call_once(g_tab_once, [] {
+    df_consts_host(&g_tab, &g_kc);
+    exp64_table_host(&g_et);
+  });
 }
 
 template <int D, int R, int PC>
@@ -1144,7 +1160,7 @@ static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
       std::min<int64_t>((a.ntl + kCholWarps - 1) / kCholWarps, (int64_t)sms * per_sm),
       scratch_warps / kCholWarps);
   if (blocks < 1) return fail(GS_ERR_INVALID_PARAMETER, "re-solve scratch too small");
-  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, flag, Mmax, cs_scratch);
+  kern<<<blocks, kCholWarps * 32, lay.total, stream>>>(a, m, g_et, flag, Mmax, cs_scratch);
   GS_CUDA(cudaGetLastError());
   count_launch(1);
   return GS_OK;
@@ -1162,6 +1178,7 @@ int64_t chol_scratch_doubles(int64_t warps) { return warps * kCholSlotDoubles; }
 int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, double* scratch,
                       int64_t scratch_warps, cudaStream_t stream) {
   if (a.ntl == 0) return GS_OK;
+  ensure_tables();
   const int Mmax = std::min(a.kout, GS_MIXED_MAX_NEIGHBORS) + a.p + 2;
   if (a.dim == 2) return launch_chol<2>(a, m, flag, Mmax, scratch, scratch_warps, stream);
   return launch_chol<3>(a, m, flag, Mmax, scratch, scratch_warps, stream);

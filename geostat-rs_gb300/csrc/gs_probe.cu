@@ -85,8 +85,31 @@ int probe(double* tflops, int iters, int lanes) {
   return GS_OK;
 }
 
+__global__ void expneg_probe(int64_t n, const double* x, double* out, Exp64Table et) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = expneg_fp64(x[i], et);
+}
+
 }  // namespace
 }  // namespace gs
+
+extern "C" int gs_probe_expneg(int64_t n, const double* x, double* out) {
+  if (n < 0 || (n > 0 && (!x || !out))) return gs::fail(GS_ERR_INVALID_PARAMETER, "bad arguments");
+  if (n == 0) return GS_OK;
+  GS_TRY(gs::ensure_device());
+  gs::Exp64Table et;
+  gs::exp64_table_host(&et);
+  gs::DevBuf dx, dout;
+  GS_TRY(dx.alloc((size_t)n * 8, nullptr));
+  GS_TRY(dout.alloc((size_t)n * 8, nullptr));
+  GS_CUDA(cudaMemcpy(dx.ptr, x, (size_t)n * 8, cudaMemcpyHostToDevice));
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+  gs::expneg_probe<<<blocks, 256>>>(n, (const double*)dx.ptr, (double*)dout.ptr, et);
+  GS_CUDA(cudaGetLastError());
+  GS_CUDA(cudaMemcpy(out, dout.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  return GS_OK;
+}
 
 extern "C" int gs_probe_fma_tflops(int precision, double* tflops) {
   GS_TRY(gs::ensure_device());

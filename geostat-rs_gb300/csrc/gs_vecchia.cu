@@ -457,9 +457,27 @@ __device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
 
 // FP64 per-(candidate, point) solve: cholesky_solve_in_place
 // (linalg.rs:123-203) on the assembled K_SS of vecchia.rs:302-320.
-template <int D>
+// OWN_EXP: covariances with the table-driven FP64 exp (the re-solve of
+// flagged systems); the FP64 build keeps the library exp.
+template <int D, bool OWN_EXP>
 __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist, double* scratch,
-                                    int64_t T, int32_t* cand_status) {
+                                    int64_t T, int32_t* cand_status, Exp64Table et_g) {
+  __shared__ Exp64Table et;
+  if (OWN_EXP) {
+    for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+      et.hi[q] = et_g.hi[q];
+      et.lo[q] = et_g.lo[q];
+    }
+    if (threadIdx.x == 0) {
+      et.l1 = et_g.l1;
+      et.l2 = et_g.l2;
+      et.inv = et_g.inv;
+    }
+    __syncthreads();
+  }
+  auto cov = [&](const DevModel& md, const double* h) {
+    return OWN_EXP ? cov_fp64x<D>(md, h, et) : cov_fp64<D>(md, h);
+  };
   const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (tid >= T) return;
   const int M = a.m;
@@ -484,13 +502,13 @@ __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
     for (int aa = 0; aa < s; ++aa) {
       const int ja = nbk[aa];
       double h[3] = {pi[0] - a.x[ja], pi[1] - a.y[ja], D == 3 ? pi[2] - a.z[ja] : 0.0};
-      const double kv = cov_fp64<D>(mdl, h);
+      const double kv = cov(mdl, h);
       W[(int64_t)aa * T] = kv;
       K0[(int64_t)aa * T] = kv;
       for (int bb = aa; bb < s; ++bb) {
         const int jb = nbk[bb];
         double g[3] = {a.x[ja] - a.x[jb], a.y[ja] - a.y[jb], D == 3 ? a.z[ja] - a.z[jb] : 0.0};
-        const double cv = cov_fp64<D>(mdl, g);
+        const double cv = cov(mdl, g);
         S[(int64_t)(aa * s + bb) * T] = cv;
         S[(int64_t)(bb * s + aa) * T] = cv;
       }
@@ -536,11 +554,15 @@ __global__ void reduce_partials(const double* partial, int nblk, int ncand, doub
 }
 
 ExpTable g_vtab;
+Exp64Table g_vet;
 DfConsts g_vkc;
 std::once_flag g_vonce;
 
 void ensure_vtables() {
-  std::call_once(g_vonce, [] { df_consts_host(&g_vtab, &g_vkc); });
+  std::call_once(g_vonce, [] {
+    df_consts_host(&g_vtab, &g_vkc);
+    exp64_table_host(&g_vet);
+  });
 }
 
 int reject_vecchia_model(const gs_model& m, int dim) {
@@ -680,12 +702,17 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     DevBuf scratch;
     GS_TRY(scratch.alloc((size_t)T * per, s));
     const int blocks = (int)((T + 127) / 128);
-    if (dim == 2)
-      vecchia_fp64_kernel<2><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
-                                                    work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
+    const int64_t* lp = mixed ? (const int64_t*)list.ptr : nullptr;
+    double* sp = (double*)scratch.ptr;
+    int32_t* cs = (int32_t*)cstat.ptr;
+    if (dim == 2 && mixed)
+      vecchia_fp64_kernel<2, true><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
+    else if (dim == 2)
+      vecchia_fp64_kernel<2, false><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
+    else if (mixed)
+      vecchia_fp64_kernel<3, true><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
     else
-      vecchia_fp64_kernel<3><<<blocks, 128, 0, s>>>(a, mixed ? (const int64_t*)list.ptr : nullptr,
-                                                    work, (double*)scratch.ptr, T, (int32_t*)cstat.ptr);
+      vecchia_fp64_kernel<3, false><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
     GS_CUDA(cudaGetLastError());
     count_launch(1);
   }

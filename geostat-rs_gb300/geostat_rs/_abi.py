@@ -77,6 +77,7 @@ SIGNATURES = {
                                                _vp, _vp]),
     "gs_last_fallbacks": (_i64, []),
     "gs_last_lu_resolves": (_i64, []),
+    "gs_probe_expneg": (_int, [_i64, _pd, _pd]),
     "gs_server_create": (_int, [_i64, _i32, C.POINTER(_vp)]),
     "gs_server_add_kriging": (_int, [_vp, _vp, _pi32]),
     "gs_server_add_vecchia": (_int, [_vp, _vp, _pi32]),

@@ -331,6 +331,9 @@ int64_t gs_last_lu_resolves(void);
  * FMAs (2) -- the roofline denominator of the per-system kernels -- and the
  * number of kernels this library has launched since it was loaded. */
 int gs_probe_fma_tflops(int precision, double* tflops);
+/* exp(-x) for x >= 0 as the FP64 re-solve kernels compute it (table-driven
+ * exp on the device; 0 for x >= 708), for accuracy checks. */
+int gs_probe_expneg(int64_t n, const double* x, double* out);
 int64_t gs_launch_count(void);
 
 #ifdef __cplusplus
