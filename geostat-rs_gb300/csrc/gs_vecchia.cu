@@ -696,7 +696,9 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   if (!mixed || nfl > 0) {
     const int64_t work = mixed ? nfl : ncand * n;
     const int64_t per = ((int64_t)M * M + 2 * (int64_t)M) * 8;
-    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 1024);
+    // 512 threads per SM: measured fastest (the strided scratch then stays
+    // mostly in L2; more threads spill it to HBM)
+    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 512);
     T = std::min<int64_t>(T, ((work + 127) / 128) * 128);
     T = std::max<int64_t>(T, 128);
     DevBuf scratch;
@@ -1263,7 +1265,9 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
   if (!mixed || nfl > 0) {
     const int64_t work = mixed ? nfl : NC;
     const int64_t per = ((int64_t)M * M + 5 * (int64_t)M) * 8;
-    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 1024);
+    // 512 threads per SM: measured fastest (the strided scratch then stays
+    // mostly in L2; more threads spill it to HBM)
+    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 512);
     T = std::min<int64_t>(T, ((work + 127) / 128) * 128);
     T = std::max<int64_t>(T, 128);
     DevBuf scratch;
