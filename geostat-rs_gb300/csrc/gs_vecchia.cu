@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
 // Per-warp shared-memory layout of vecchia_warp_kernel (conditioning sets of
 // at most 32 points).
 struct VWLayout {
-  size_t off_a, off_h, off_v, off_b, off_h0, off_z, off_row, off_vec, off_xd, total;
+  size_t off_a, off_h, off_v, off_b, off_h0, off_z, off_row, off_vec, off_xd, off_lt, total;
 };
 
 __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim) {
@@ -294,6 +294,7 @@ __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim) {
   L.off_row = take(kWarpN * sizeof(float));
   L.off_vec = take(kWarpN * sizeof(float));
   L.off_xd = take(kWarpN * sizeof(df));
+  L.off_lt = take(2 * kWarpN * sizeof(double));  // (variance, residual) of 32 candidates
   L.total = o;
   return L;
 }
@@ -325,6 +326,19 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
   W.row = reinterpret_cast<float*>(base + lay.off_row);
   W.vec = reinterpret_cast<float*>(base + lay.off_vec);
   W.xd = reinterpret_cast<df*>(base + lay.off_xd);
+  // per-candidate (variance, residual), -1 variance: flagged; the log terms
+  // of up to 32 candidates are then evaluated by one lane each
+  double* LT = reinterpret_cast<double*>(base + lay.off_lt);
+  auto flush_terms = [&](int64_t k, int c0, int cnt) {
+    __syncwarp();
+    if (lane < cnt) {
+      const int c = c0 + lane;
+      const double var = LT[2 * lane], r = LT[2 * lane + 1];
+      if (var >= 0.0) a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+      a.flag[(int64_t)c * a.n + k] = var >= 0.0 ? 0 : 1;
+    }
+    __syncwarp();
+  };
   const int64_t nwarps = (int64_t)gridDim.x * kVWarps;
   for (int64_t k = (int64_t)blockIdx.x * kVWarps + wib; k < a.n; k += nwarps) {
     const int64_t i = a.order[k];
@@ -392,23 +406,21 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
       __syncwarp();
       const bool ok = warp_solve(A, B, s, lane, W);
       if (!ok) {
-        if (lane == 0) a.flag[(int64_t)c * a.n + k] = 1;
-        __syncwarp();
-        continue;
+        if (lane == 0) LT[2 * (c & 31)] = -1.0;
+      } else {
+        df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
+        if (lane < s) {
+          mu = df_fma_acc(mu, W.xd[lane], ZV[lane]);
+          red = df_fma_acc(red, W.xd[lane], B[lane]);
+        }
+        mu = warp_sum_df(mu);
+        red = warp_sum_df(red);
+        if (lane == 0) {
+          LT[2 * (c & 31)] = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
+          LT[2 * (c & 31) + 1] = df_to_double(df_sub(zi, mu));
+        }
       }
-      df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
-      if (lane < s) {
-        mu = df_fma_acc(mu, W.xd[lane], ZV[lane]);
-        red = df_fma_acc(red, W.xd[lane], B[lane]);
-      }
-      mu = warp_sum_df(mu);
-      red = warp_sum_df(red);
-      if (lane == 0) {
-        const double var = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
-        const double r = df_to_double(df_sub(zi, mu));
-        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
-        a.flag[(int64_t)c * a.n + k] = 0;
-      }
+      if ((c & 31) == 31 || c == a.ncand - 1) flush_terms(k, c & ~31, (c & 31) + 1);
       __syncwarp();
     }
   }
