@@ -645,14 +645,17 @@ def serving_bench(args, log):
         vv = G.rff_field(cc, mdl, 1024, SEED + 200 + q)
         ps = G.PointSet(cc, vv)
         row = []
+        warm = G.rng_uniform(SEED + 300 + q, dim * 131072).reshape(-1, dim) * box
         for km in nmaxes:
             k = G.Kriging.new(ps, mdl, G.KrigingConfig(max_neighbors=km))
+            k.predict_many(warm)  # registration: autotunes the predictor's launch shape
             keep.append(k)
             row.append(srv.add_kriging(k))
         kds.append(row)
         boxes.append(box)
         if dim == 2 and n <= 1_000_000:
             plan = G.VecchiaPlan(ps, 30)
+            plan.loglik([VariogramModel(0.05, [Structure("matern25", 1.0, 60.0)])])
             keep.append(plan)
             vds.append(srv.add_vecchia(plan))
     log(f"[bench] serving set-up {time.time() - t0:.1f}s (8 data sets, 32 predictors, "

@@ -462,17 +462,16 @@ struct NbGt {
 // Calls with at least this many targets are autotuned (per size class).
 constexpr int64_t kTuneMinTargets = 65536;
 // Targets of the first chunk the candidates are timed on.
-constexpr int64_t kTuneSample = 262144;
+constexpr int64_t kTuneSample = 131072;
 // Warps of the FP64 LDL^T re-solve (slot-covariance scratch, 16.6 KB each).
 constexpr int64_t kCholScratchWarps = 152 * 16;
 // Leading targets of each chunk whose FP32 failure rate routes the rest.
 constexpr int64_t kRouteSample = 16384;
 
-int size_class(int64_t nt) {
-  int c = 0;
-  while ((nt >> (c + 1)) > 0) ++c;
-  return c;
-}
+// Calls large enough to fill the GPU share one tuned shape per predictor
+// (the best run length depends on the systems, not on how many there are);
+// smaller calls use the default.
+int size_class(int64_t nt) { return nt >= kTuneMinTargets ? 1 : 0; }
 
 // Launch shape without measurement: the longest run that still gives every
 // SM a few blocks.

@@ -356,9 +356,11 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
     __syncwarp();
     if (lane < s) {
       const int j = a.nb[k * (int64_t)M + lane];
+      // separations from the FP64 coordinates (exact for nearby points), so
+      // short lags keep their full relative precision
+      const double* xs[3] = {a.x, a.y, a.z};
 #pragma unroll
-      for (int d = 0; d < D; ++d)
-        V[d * M + lane] = df_sub(a.cdf[(int64_t)d * a.n + j], a.cdf[(int64_t)d * a.n + i]);
+      for (int d = 0; d < D; ++d) V[d * M + lane] = df_from_double(xs[d][j] - xs[d][i]);
       ZV[lane] = df_sub(a.vdf[j], a.mean_df);
     }
     __syncwarp();

@@ -172,12 +172,12 @@ int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double*
                                   const double* ty, const double* tz, const double* tdrift,
                                   double* value, double* variance, double* lagrange,
                                   uint8_t* status, int precision, void* stream);
-/* Launch shapes of the mixed solver (no counterpart in the reference).  A
- * call of at least 65,536 targets whose size class (floor(log2(nt))) has no
- * shape yet times the candidate shapes -- runs of 16/32/64/128 consecutive
- * targets per block, uneven neighbourhoods split onto the 32- and 64-thread
- * solvers or not -- on its first 262,144 targets and keeps the fastest for
- * that size class of this predictor; smaller and asynchronous calls use a
+/* Launch shapes of the mixed solver (no counterpart in the reference).  The
+ * first call of at least 65,536 targets on a predictor times the candidate
+ * shapes -- runs of 16/32/64/128 consecutive targets per block, uneven
+ * neighbourhoods split onto the 32- and 64-thread solvers or not -- on its
+ * first 131,072 targets and keeps the fastest for every later call of at
+ * least 65,536 targets; smaller and asynchronous calls before that use a
  * default.  Results of different shapes agree within the parity tolerance
  * (the order of roundings differs), and a predictor's results are
  * reproducible once its shapes are fixed.
