@@ -422,6 +422,21 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
   return GS_OK;
 }
 
+// Global neighbourhood in cross-validation: target c0 + t (a data point)
+// conditions on every point with another label, in index order.
+__global__ void excl_rows_kernel(int64_t nt, int64_t c0, int n, const int32_t* label, int kout,
+                                 int32_t* nb, int32_t* nbc) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t own = label[c0 + t];
+    int32_t* row = nb + t * (int64_t)kout;
+    int c = 0;
+    for (int j = 0; j < n && c < kout; ++j)
+      if (label[j] != own) row[c++] = j;
+    nbc[t] = c;
+  }
+}
+
 __global__ void iota_rows_kernel(int64_t nt, int n, int32_t* nb, int32_t* nbc) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nt * n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -489,7 +504,8 @@ Tiles default_tiles(int64_t nt, bool binnable) {
 // into a CUDA graph).
 int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
                  const double* tz, const double* tdrift, double* value, double* variance,
-                 double* lagrange, uint8_t* status, int precision, cudaStream_t stream, bool timed) {
+                 double* lagrange, uint8_t* status, int precision, cudaStream_t stream, bool timed,
+                 const int32_t* excl_labels = nullptr) {
   if (nt == 0) return GS_OK;
   const gs_pointset* ps = k->ps;
   const gs_kcfg& c = k->cfg;
@@ -499,12 +515,13 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   // neighbourhood geometry
   SearchParams sp{};
   int kout;
+  const int64_t navail = excl_labels ? n - 1 : n;  // cross-validation: at most n - 1 others
   if (!k->use_tree) {
-    if (n + p > GS_MAX_SYSTEM)
+    if (navail + p > GS_MAX_SYSTEM)
       return fail(GS_ERR_INVALID_PARAMETER,
-                  "global neighbourhood of " + std::to_string(n) +
+                  "global neighbourhood of " + std::to_string(navail) +
                       " points exceeds the CUDA path's system limit; set max_neighbors");
-    kout = (int)n;
+    kout = (int)navail;
   } else if (c.max_per_octant >= 0) {
     const int NB = 1 << dim;
     int per = (int)std::min<int64_t>(c.max_per_octant, n);
@@ -524,6 +541,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood plus drift terms exceed " +
                                               std::to_string(GS_MAX_SYSTEM) + " on the CUDA path");
   sp.kout = kout;
+  sp.excl_label = excl_labels;
   sp.has_radius = c.has_search_radius ? 1 : 0;
   sp.r2 = c.has_search_radius ? c.search_radius * c.search_radius : 0.0;
   const int nmax_all = kout + p;
@@ -623,7 +641,13 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     int32_t* dnbc = (int32_t*)nbc.ptr;
     GS_TRY(mark(1));
     if (k->use_tree) {
-      rc = search_launch(k->grid, k->frame, sp, cn, ctx, cty, ctz, dnb, dnbc, stream);
+      SearchParams spc = sp;
+      if (excl_labels) spc.target_label = excl_labels + c0;  // targets are the data points
+      rc = search_launch(k->grid, k->frame, spc, cn, ctx, cty, ctz, dnb, dnbc, stream);
+    } else if (excl_labels) {
+      excl_rows_kernel<<<(int)std::min<int64_t>((cn + 127) / 128, 152 * 64), 128, 0, stream>>>(
+          cn, c0, (int)n, excl_labels, kout, dnb, dnbc);
+      rc = cudaGetLastError() == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "launch failed");
     } else {
       iota_rows_kernel<<<(int)std::min<int64_t>((cn * kout + 255) / 256, 152 * 64), 256, 0, stream>>>(
           cn, kout, dnb, dnbc);
@@ -851,6 +875,69 @@ int gs_kriging_set_tiles(gs_kriging* k, int run, int bins) {
   if (bins != 0 && bins != 1) return fail(GS_ERR_INVALID_PARAMETER, "bins must be 0 or 1");
   std::lock_guard<std::mutex> lk(k->tiles_mu);
   k->pinned = gs::Tiles{run, bins};
+  return GS_OK;
+}
+
+// validation.rs:136-153 fold_assignment: a seeded shuffle of 0..n-1 (rng.rs
+// shuffle), position j of the shuffled order goes to fold j mod k.
+static void fold_assignment(int64_t n, int64_t k, uint64_t seed, std::vector<int32_t>& fold_of) {
+  std::vector<int64_t> order(n);
+  for (int64_t i = 0; i < n; ++i) order[i] = i;
+  gs::Xoshiro r(seed);
+  for (int64_t i = n - 1; i >= 1; --i) {
+    const int64_t j = (int64_t)(r.next() % (uint64_t)(i + 1));
+    std::swap(order[i], order[j]);
+  }
+  fold_of.assign(n, 0);
+  for (int64_t j = 0; j < n; ++j) fold_of[order[j]] = (int32_t)(j % k);
+}
+
+int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed, double* predicted,
+                              double* variance, uint8_t* status, int precision) {
+  if (!k || !predicted || !variance) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
+  const gs_pointset* ps = k->ps;
+  const int64_t n = ps->n;
+  if (n < 3)
+    return fail(GS_ERR_INSUFFICIENT_DATA, nfolds == 0
+                                              ? "leave-one-out cross-validation requires at least 3 points"
+                                              : "cross-validation requires at least 3 points");
+  if (nfolds != 0 && !(nfolds >= 2 && nfolds <= n))
+    return fail(GS_ERR_INVALID_PARAMETER, "k-fold requires 2 <= k <= n (k=" + std::to_string(nfolds) +
+                                              ", n=" + std::to_string(n) + ")");
+  std::vector<int32_t> label(n);
+  if (nfolds == 0) {
+    for (int64_t i = 0; i < n; ++i) label[i] = (int32_t)i;
+  } else {
+    fold_assignment(n, nfolds, seed, label);
+  }
+  cudaStream_t s = k->stream;
+  gs::DevBuf dl, dv, dvar, dst;
+  GS_TRY(dl.alloc((size_t)n * 4, s));
+  GS_TRY(dv.alloc((size_t)n * 8, s));
+  GS_TRY(dvar.alloc((size_t)n * 8, s));
+  GS_TRY(dst.alloc((size_t)n, s));
+  GS_CUDA(cudaMemcpyAsync(dl.ptr, label.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+  GS_TRY(gs::predict_pass(k, n, ps->d_x, ps->d_y, ps->dim == 3 ? ps->d_z : nullptr,
+                          k->cfg.method == GS_EXTERNAL_DRIFT ? k->d_drift : nullptr,
+                          (double*)dv.ptr, (double*)dvar.ptr, nullptr, (uint8_t*)dst.ptr, precision,
+                          s, true, (const int32_t*)dl.ptr));
+  std::vector<uint8_t> st(n);
+  GS_CUDA(cudaMemcpyAsync(predicted, dv.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(variance, dvar.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(st.data(), dst.ptr, (size_t)n, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  if (status) std::memcpy(status, st.data(), (size_t)n);
+  // the reference stops at a point whose prediction fails (Kriging::predict)
+  for (int64_t i = 0; i < n; ++i) {
+    const int code = st[i] & 0x3f;
+    if (code == GS_ST_OK) continue;
+    const std::string at = "cross-validation at point " + std::to_string(i) + ": ";
+    if (code == GS_ST_NO_NEIGHBORS) return fail(GS_ERR_NO_NEIGHBORS, at + "not enough neighbours");
+    if (code == GS_ST_INSUFFICIENT_DATA)
+      return fail(GS_ERR_INSUFFICIENT_DATA, at + "fewer neighbours than drift terms");
+    if (code == GS_ST_SINGULAR) return fail(GS_ERR_SINGULAR_SYSTEM, at + "singular kriging system");
+    return fail(GS_ERR_INVALID_PARAMETER, at + "neighbourhood beyond the CUDA path's system limit");
+  }
   return GS_OK;
 }
 

@@ -319,6 +319,7 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
     __syncwarp();
     long long inrad = 0;
     const int64_t qrank = RANKED ? p.rank0 + t : 0;
+    const int32_t tlabel = p.excl_label ? p.target_label[t] : 0;
     if (RANKED && qrank <= p.brute_below) {
       // early ranks: scan the whole (short) prefix of the store
       for (int64_t rb = 0; rb < qrank; rb += 32) {
@@ -385,7 +386,8 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
         oid = g.sidx[pi];
       }
       const dkey k2 = d2key(d2);
-      const bool inr = valid && k2 <= r2k && (!RANKED || (int64_t)oid < qrank);
+      const bool inr = valid && k2 <= r2k && (!RANKED || (int64_t)oid < qrank) &&
+                       !(p.excl_label && p.excl_label[oid] == tlabel);
       if (p.unbounded) inrad += __popc(__ballot_sync(kFull, inr));
 #pragma unroll
       for (int b = 0; b < NB; ++b) {

@@ -55,6 +55,11 @@ struct SearchParams {
   const double* px;
   const double* py;
   const double* pz;
+  // Cross-validation: when set, candidates j with excl_label[j] equal to the
+  // target's target_label[t] do not exist for it (its own point for
+  // leave-one-out, its fold for k-fold).
+  const int32_t* excl_label;
+  const int32_t* target_label;
 };
 
 // Owns the device buffers of one grid.

@@ -10,8 +10,10 @@ from .errors import (CudaError, DimensionMismatch, DuplicatePoints, GeostatError
                      InsufficientData, InvalidParameter, NoNeighbors, OutOfDeviceMemory,
                      SingularSystem)
 from .model import Anisotropy, Structure, VariogramModel, parse_kind
-from .api import (Kriging, KrigingConfig, KrigingResult, PointSet, Server, VecchiaPlan,
-                  clustered_points, krige, krige_3d, krige_grid, last_timings, maxmin_order,
+from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Server, TuneResult,
+                  VecchiaPlan, clustered_points, k_fold, krige, krige_3d, krige_grid,
+                  last_timings, leave_one_out, leave_one_out_with_drift, maxmin_order,
+                  tune_kriging_neighbors,
                   nelder_mead_multistart, rff_field, rng_normal, rng_uniform, seq_mean,
                   vecchia_krige, vecchia_loglik, vecchia_mle, vecchia_mle_fit,
                   vecchia_mle_nm_fit, vecchia_predict)

@@ -319,6 +319,144 @@ def last_timings():
 
 
 # -------------------------------------------------- reference Python API --
+# ------------------------------------------------------- cross-validation --
+@dataclass
+class CvResult:
+    """Cross-validation result (validation.rs:10-117): observed values in data
+    order, held-out predictions and kriging variances."""
+    observed: np.ndarray
+    predicted: np.ndarray
+    variance: np.ndarray
+
+    def _res(self):
+        return self.predicted - self.observed
+
+    def mean_error(self) -> float:
+        return float(np.sum(self._res()) / len(self.observed))
+
+    def mae(self) -> float:
+        return float(np.sum(np.abs(self._res())) / len(self.observed))
+
+    def mse(self) -> float:
+        r = self._res()
+        return float(np.sum(r * r) / len(self.observed))
+
+    def rmse(self) -> float:
+        return float(np.sqrt(self.mse()))
+
+    def _obs_mean(self) -> float:
+        return float(np.sum(self.observed) / len(self.observed))
+
+    def rme(self) -> float:
+        m = self._obs_mean()
+        return float("nan") if abs(m) < np.finfo(float).eps else -self.mean_error() / m * 100.0
+
+    def rmae(self) -> float:
+        m = self._obs_mean()
+        return float("nan") if abs(m) < np.finfo(float).eps else self.mae() / m * 100.0
+
+    def rrmse(self) -> float:
+        m = self._obs_mean()
+        return float("nan") if abs(m) < np.finfo(float).eps else self.rmse() / m * 100.0
+
+    def vecv(self) -> float:
+        m = self._obs_mean()
+        r = self._res()
+        sst = float(np.sum((self.observed - m) ** 2))
+        return float("nan") if sst <= 0.0 else (1.0 - float(np.sum(r * r)) / sst) * 100.0
+
+    def e1(self) -> float:
+        m = self._obs_mean()
+        sad = float(np.sum(np.abs(self.observed - m)))
+        return float("nan") if sad <= 0.0 else (1.0 - float(np.sum(np.abs(self._res()))) / sad) * 100.0
+
+    def msdr(self) -> float:
+        ok = self.variance > 1e-12
+        if not ok.any():
+            return float("nan")
+        e = (self.predicted - self.observed)[ok]
+        return float(np.sum(e * e / self.variance[ok]) / int(ok.sum()))
+
+
+def _cross_validate(k: "Kriging", data: "PointSet", nfolds: int, seed: int,
+                    precision: str) -> CvResult:
+    n = data.n
+    pred, var = np.empty(n), np.empty(n)
+    st = np.empty(n, dtype=np.uint8)
+    _abi.check(_abi.load().gs_kriging_cross_validate(k._h, int(nfolds), int(seed) & (2**64 - 1),
+                                                     _p(pred), _p(var), _p(st, C.c_uint8),
+                                                     PRECISIONS[precision]))
+    return CvResult(np.array(data.values, dtype=float), pred, var)
+
+
+def leave_one_out(data: "PointSet", model: VariogramModel, config: KrigingConfig = None,
+                  precision: str = "mixed") -> CvResult:
+    """``validation::leave_one_out`` (validation.rs:136-159): every point
+    predicted from all the others."""
+    if data.n < 3:
+        from .errors import InsufficientData
+        raise InsufficientData("leave-one-out cross-validation requires at least 3 points")
+    return _cross_validate(Kriging.new(data, model, config), data, 0, 0, precision)
+
+
+def leave_one_out_with_drift(data: "PointSet", drift_data, model: VariogramModel,
+                             config: KrigingConfig, precision: str = "mixed") -> CvResult:
+    """``validation::leave_one_out_with_drift`` (validation.rs:161-192)."""
+    if data.n < 3:
+        from .errors import InsufficientData
+        raise InsufficientData("leave-one-out cross-validation requires at least 3 points")
+    if len(drift_data) != data.n:
+        raise DimensionMismatch(f"{len(drift_data)} drift rows vs {data.n} data points")
+    k = Kriging.with_external_drift(data, model, config, drift_data)
+    return _cross_validate(k, data, 0, 0, precision)
+
+
+def k_fold(data: "PointSet", model: VariogramModel, config: KrigingConfig, k: int, seed: int,
+           precision: str = "mixed") -> CvResult:
+    """``validation::k_fold`` (validation.rs:236-253): seeded fold assignment,
+    each fold predicted from the others."""
+    if data.n < 3:
+        from .errors import InsufficientData
+        raise InsufficientData("cross-validation requires at least 3 points")
+    if not 2 <= k <= data.n:
+        raise InvalidParameter(f"k-fold requires 2 <= k <= n (k={k}, n={data.n})")
+    return _cross_validate(Kriging.new(data, model, config), data, k, seed, precision)
+
+
+@dataclass
+class TuneResult:
+    """``tuning::TuneResult``: the best candidate, its VEcv and the trace."""
+    best: object
+    best_vecv: float
+    trace: list
+
+
+def tune_kriging_neighbors(data: "PointSet", model: VariogramModel, method: str,
+                           candidates: Sequence[int], radius: Optional[float] = None,
+                           precision: str = "mixed") -> TuneResult:
+    """``tuning::tune_kriging_neighbors`` (tuning.rs:97-125): leave-one-out
+    VEcv per neighbourhood size (NaN where the cross-validation fails); the
+    largest finite VEcv wins."""
+    if len(candidates) == 0:
+        raise InvalidParameter("no neighborhood sizes to try")
+    trace = []
+    for nb in candidates:
+        cfg = KrigingConfig(method, max_neighbors=int(nb), search_radius=radius)
+        try:
+            v = leave_one_out(data, model, cfg, precision).vecv()
+        except Exception:
+            v = float("nan")
+        trace.append((int(nb), v))
+    finite = [t for t in trace if np.isfinite(t[1])]
+    if not finite:
+        raise InvalidParameter("no candidate produced a finite VEcv")
+    best = finite[0]
+    for t in finite[1:]:
+        if t[1] >= best[1]:  # max_by keeps the last of equal maxima
+            best = t
+    return TuneResult(best[0], best[1], trace)
+
+
 def _build_method(method: str, mean, degree, data_values) -> KrigingConfig:
     # crates/geostat-python/src/lib.rs:104-121 build_method
     if method == "ordinary":

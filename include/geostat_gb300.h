@@ -172,6 +172,18 @@ int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double*
                                   const double* ty, const double* tz, const double* tdrift,
                                   double* value, double* variance, double* lagrange,
                                   uint8_t* status, int precision, void* stream);
+/* Cross-validation of a built predictor over its own data points
+ * (validation.rs:136-253): nfolds = 0 is leave_one_out (each point predicted
+ * from all the others), nfolds = k >= 2 is k_fold with the reference's seeded
+ * fold assignment (each fold predicted from the other folds).  Every point's
+ * estimate and variance are written (status may be NULL); as in the reference
+ * the call fails -- with the error of the first failing point -- if any
+ * prediction fails.  Neighbour sets are those of a predictor built on the
+ * remaining points; drift bases keep the full data's normalisation, which
+ * changes estimates and variances only by rounding.  Errors: fewer than 3
+ * points (InsufficientData), k outside [2, n] (InvalidParameter). */
+int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed,
+                              double* predicted, double* variance, uint8_t* status, int precision);
 /* Launch shapes of the mixed solver (no counterpart in the reference).  The
  * first call of at least 65,536 targets on a predictor times the candidate
  * shapes -- runs of 16/32/64/128 consecutive targets per block, uneven
