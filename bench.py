@@ -285,6 +285,7 @@ def run_ours(args, rank, world):
         # accuracy and CPU baseline on a bounded sample
         acc, cpu = cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var,
                                            fp64_v, kr, log)
+        cvr = cv_bench(args, coords, values, model, log) if args.cv_sample > 0 else None
         vec = vecchia_bench(args, log) if not args.no_vecchia else None
         clu = clustered_bench(args, log) if not args.no_clustered else None
         serve = serving_bench(args, log) if args.serve_requests > 0 else None
@@ -333,6 +334,8 @@ def run_ours(args, rank, world):
             result["vecchia"] = vec
         if clu is not None:
             result["clustered"] = clu
+        if cvr is not None:
+            result["cross_validation"] = cvr
         if serve is not None:
             result["serving"] = serve
             result["p99_latency_ms"] = serve["p99_ms"]
@@ -376,6 +379,49 @@ def cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_
     cpu = {"value": ns / dt, "unit": "kriged targets/s", "cores": cores, "kind": "port",
            "sample": f"{ns} random targets of the 4,194,304-cell grid (same data, model, n_max=64)"}
     return acc, cpu
+
+
+def cv_bench(args, coords, values, model, log):
+    """Leave-one-out cross-validation of the 3-D workload's 200,000 points (64
+    nearest, each point predicted from all the others), on the GPU; the oracle
+    follows the reference (a predictor rebuilt without the held-out point, so
+    a kd-tree build per point) on a bounded sample of points."""
+    import geostat_rs as G
+    ps = G.PointSet(coords, values)
+    cfg = G.KrigingConfig(max_neighbors=K_NEIGH)
+    cv = G.leave_one_out(ps, model, cfg)  # warm-up (and launch-shape tuning)
+    ts = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        cv = G.leave_one_out(ps, model, cfg)
+        ts.append(time.perf_counter() - t1)
+    dt = statistics.median(ts)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    rng = np.random.RandomState(13)
+    sample = rng.choice(len(coords), args.cv_sample, replace=False)
+    t1 = time.perf_counter()
+    ref_p, ref_v = [], []
+    for i in sample:
+        keep = np.ones(len(coords), bool)
+        keep[i] = False
+        r = O.krige(coords[keep], values[keep], model, coords[i:i + 1], max_neighbors=K_NEIGH,
+                    nthreads=1)
+        ref_p.append(r["value"][0])
+        ref_v.append(r["variance"][0])
+    dcpu = time.perf_counter() - t1
+    vs = float(np.mean(np.abs(values)))
+    rel = lambda a, b, f: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), f)))
+    log(f"[bench] leave-one-out: {len(coords)} points in {dt * 1e3:.1f} ms; oracle "
+        f"{len(sample)} points in {dcpu:.1f}s")
+    return {"points": len(coords), "max_neighbors": K_NEIGH, "seconds": dt,
+            "points_per_s": len(coords) / dt, "vecv": cv.vecv(), "rmse": cv.rmse(),
+            "oracle_sample": len(sample),
+            "cpu_points_per_s": len(sample) / dcpu, "cpu_cores": 1,
+            "cpu_kind": "port (a predictor rebuilt per held-out point, as validation.rs:148)",
+            "max_rel_value": rel(cv.predicted[sample], np.array(ref_p), vs),
+            "max_rel_variance": rel(cv.variance[sample], np.array(ref_v), 1e-3)}
 
 
 def vecchia_bench(args, log):
@@ -839,6 +885,8 @@ def main():
     ap.add_argument("--no-vecchia", action="store_true")
     ap.add_argument("--no-clustered", action="store_true",
                     help="skip the clustered uneven workload")
+    ap.add_argument("--cv-sample", type=int, default=40,
+                    help="oracle points of the leave-one-out leg (0: skip the leg)")
     ap.add_argument("--cl-sample", type=int, default=200,
                     help="oracle targets per band of the clustered workload")
     ap.add_argument("--vpred-n", type=int, default=500_000,
