@@ -238,6 +238,16 @@ bool valid_in_dim(const gs_model& m, int dim) {
 }
 
 // Kriging::build and the three constructors (kriging.rs:166-408).
+}  // namespace
+namespace gs {
+KrigeArgs base_args(const gs_kriging* k);
+}  // namespace gs
+namespace {
+
+// Global neighbourhoods larger than the mixed solver's systems are factored
+// once at build (kriging.rs:396-406); up to this many unknowns (2 GiB).
+constexpr int kGlobalLuMax = 16384;
+
 int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* cfg, int ctor,
                    const double* drift, const double* errors, gs_kriging** out) {
   *out = nullptr;
@@ -414,6 +424,39 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
     double ppc = dim == 2 ? 3.0 : 4.0;
     rc = grid_build(&k->grid, dim, n, ps->d_x, ps->d_y, ps->d_z, f, ppc, k->stream);
   }
+  if (!rc && !k->use_tree && n > GS_MIXED_MAX_NEIGHBORS && n >= k->p) {
+    const int64_t N = n + k->p;
+    if (N > kGlobalLuMax) {
+      rc = fail(GS_ERR_INVALID_PARAMETER,
+                "global neighbourhood of " + std::to_string(N) + " unknowns exceeds " +
+                    std::to_string(kGlobalLuMax) + " on the CUDA path; set max_neighbors");
+    } else if (cudaMalloc(&k->d_lu, (size_t)N * N * 8) != cudaSuccess ||
+               cudaMalloc(&k->d_perm, (size_t)N * 4) != cudaSuccess) {
+      rc = fail(GS_ERR_OUT_OF_MEMORY, "global system allocation failed");
+    } else {
+      DevBuf piv;
+      int state = 0;
+      rc = piv.alloc((size_t)N * 4, k->stream);
+      if (!rc)
+        rc = global_factor(gs::base_args(k), k->dm, (int)N, k->d_lu, (int32_t*)piv.ptr, &state,
+                           k->stream);
+      if (!rc) {
+        // Lu::solve's row swaps applied in order, as one permutation
+        std::vector<int32_t> pv(N), perm(N);
+        if (cudaMemcpy(pv.data(), piv.ptr, N * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+          rc = fail(GS_ERR_CUDA, "pivot download failed");
+        } else {
+          for (int64_t i = 0; i < N; ++i) perm[i] = (int32_t)i;
+          if (state == 1)
+            for (int64_t kk = 0; kk < N; ++kk) std::swap(perm[kk], perm[pv[kk]]);
+          if (cudaMemcpy(k->d_perm, perm.data(), N * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = fail(GS_ERR_CUDA, "permutation upload failed");
+        }
+        k->lu_n = (int)N;
+        k->lu_state = state;
+      }
+    }
+  }
   if (rc) {
     delete k;
     return rc;
@@ -498,6 +541,39 @@ Tiles default_tiles(int64_t nt, bool binnable) {
   return t;
 }
 
+// The predictor's part of the kernel arguments (targets, lists and outputs
+// are filled in by the caller).
+KrigeArgs base_args(const gs_kriging* k) {
+  const gs_pointset* ps = k->ps;
+  const gs_kcfg& c = k->cfg;
+  KrigeArgs a{};
+  a.dim = ps->dim;
+  a.method = (int)c.method;
+  a.p = k->p;
+  a.nv = k->nv;
+  a.uk_degree = (int)c.uk_degree;
+  a.min_nb = c.min_neighbors >= 0 ? (int)c.min_neighbors : 1;
+  a.sk_mean = c.sk_mean;
+  for (int d = 0; d < 3; ++d) a.center[d] = k->center[d];
+  a.scale = k->scale;
+  for (int v = 0; v < GS_MAX_KED_VARS; ++v) {
+    a.dmean[v] = k->dmean[v];
+    a.dscale[v] = k->dscale[v];
+  }
+  a.x = ps->d_x;
+  a.y = ps->d_y;
+  a.z = ps->d_z;
+  a.val = ps->d_v;
+  a.meas_err = k->d_err;
+  a.drift = k->d_drift;
+  a.cdf = (const df*)ps->d_cdf;
+  a.vdf = (const df*)ps->d_vdf;
+  a.basis_df = k->d_basis_df;
+  a.err_df = k->d_err_df;
+  a.n = ps->n;
+  return a;
+}
+
 // Search + solves for targets already on the device.  timed: phase timings,
 // FP64 re-solve count and a final synchronisation; otherwise the whole pass
 // is only enqueued on `stream` (no host synchronisation: it can be captured
@@ -516,7 +592,9 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   SearchParams sp{};
   int kout;
   const int64_t navail = excl_labels ? n - 1 : n;  // cross-validation: at most n - 1 others
-  if (!k->use_tree) {
+  if (!k->use_tree && k->lu_state != 0 && !excl_labels) {
+    kout = (int)n;  // the factored global path below
+  } else if (!k->use_tree) {
     if (navail + p > GS_MAX_SYSTEM)
       return fail(GS_ERR_INVALID_PARAMETER,
                   "global neighbourhood of " + std::to_string(navail) +
@@ -537,7 +615,8 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     sp.k = (int)std::min<int64_t>(n, GS_MAX_SYSTEM - p);
     kout = sp.k;
   }
-  if (kout + p > GS_MAX_SYSTEM)
+  const bool global_lu = !k->use_tree && k->lu_state != 0 && !excl_labels;
+  if (!global_lu && kout + p > GS_MAX_SYSTEM)
     return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood plus drift terms exceed " +
                                               std::to_string(GS_MAX_SYSTEM) + " on the CUDA path");
   sp.kout = kout;
@@ -546,32 +625,49 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   sp.r2 = c.has_search_radius ? c.search_radius * c.search_radius : 0.0;
   const int nmax_all = kout + p;
 
-  KrigeArgs a{};
-  a.dim = dim;
-  a.method = (int)c.method;
-  a.p = p;
-  a.nv = k->nv;
-  a.uk_degree = (int)c.uk_degree;
-  a.min_nb = c.min_neighbors >= 0 ? (int)c.min_neighbors : 1;
+  KrigeArgs a = base_args(k);
   a.kout = kout;
-  a.sk_mean = c.sk_mean;
-  for (int d = 0; d < 3; ++d) a.center[d] = k->center[d];
-  a.scale = k->scale;
-  for (int v = 0; v < GS_MAX_KED_VARS; ++v) {
-    a.dmean[v] = k->dmean[v];
-    a.dscale[v] = k->dscale[v];
+
+  // global neighbourhood factored at build: per-target solves only
+  if (global_lu) {
+    const int N = k->lu_n;
+    const int64_t warps = std::max<int64_t>(
+        1, std::min<int64_t>(152 * 32, ((int64_t)512 << 20) / (16 * (int64_t)N)));
+    DevBuf scratch;
+    GS_TRY(scratch.alloc((size_t)warps * 2 * N * 8, stream));
+    KrigeArgs g = a;
+    g.tx = tx;
+    g.ty = ty;
+    g.tz = tz;
+    g.tdrift = tdrift;
+    g.out_v = value;
+    g.out_var = variance;
+    g.out_lag = lagrange;
+    g.out_st = status;
+    g.ntl = nt;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (timed) {
+      GS_CUDA(cudaEventCreate(&e0));
+      GS_CUDA(cudaEventCreate(&e1));
+      GS_CUDA(cudaEventRecord(e0, stream));
+    }
+    GS_TRY(global_solve_launch(g, k->dm, N, k->d_lu, k->d_perm, k->lu_state,
+                               (double*)scratch.ptr, warps, stream));
+    if (!timed) return GS_OK;
+    GS_CUDA(cudaEventRecord(e1, stream));
+    GS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_timings[0] = 0;
+    g_timings[1] = 0;
+    g_timings[2] = ms;
+    g_timings[3] = ms;
+    g_fallbacks = nt;
+    g_lu_resolves = 0;
+    return GS_OK;
   }
-  a.x = ps->d_x;
-  a.y = ps->d_y;
-  a.z = ps->d_z;
-  a.val = ps->d_v;
-  a.meas_err = k->d_err;
-  a.drift = k->d_drift;
-  a.cdf = (const df*)ps->d_cdf;
-  a.vdf = (const df*)ps->d_vdf;
-  a.basis_df = k->d_basis_df;
-  a.err_df = k->d_err_df;
-  a.n = n;
 
   // chunking keeps the neighbour lists within a fixed budget (4 GiB: a
   // 4.19 M-target grid with 64 neighbours is one chunk)

@@ -1072,6 +1072,207 @@ __global__ void route_kernel(const uint8_t* flag, int64_t n, int* route) {
   }
 }
 
+// ---------------------------------------------------- global neighbourhood --
+// Kriging::build's global system (kriging.rs:396-406): build_lhs over all n
+// points, factored once by lu_factor (linalg.rs:27-76) on the device; each
+// target then only solves with the factors (Lu::solve, linalg.rs:87-111).
+
+// A[i * N + j], i, j < N = n + p (row-major; both triangles).
+template <int D>
+__global__ void global_lhs_kernel(KrigeArgs a, DevModel m, int N, double* A) {
+  const int64_t total = (int64_t)N * N;
+  const int n = (int)a.n, p = a.p;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / N), j = (int)(e % N);
+    double v = 0.0;
+    if (i < n && j < n) {
+      if (i == j) {
+        v = m.c0 + (a.meas_err ? a.meas_err[i] : 0.0);
+      } else {
+        const double h[3] = {a.x[i] - a.x[j], a.y[i] - a.y[j], D == 3 ? a.z[i] - a.z[j] : 0.0};
+        v = cov_fp64<D>(m, h);
+      }
+    } else if (i < n || j < n) {
+      const int r = i < n ? i : j, q = (i < n ? j : i) - n;
+      const double pt[3] = {a.x[r], a.y[r], D == 3 ? a.z[r] : 0.0};
+      if (q < p) v = basis_at<D>(a, pt, a.drift ? a.drift + (int64_t)r * a.nv : nullptr, q);
+    }
+    A[e] = v;
+  }
+}
+
+// max |A| as the bits of a non-negative double (they order like the values).
+__global__ void absmax_kernel(const double* A, int64_t total, unsigned long long* out) {
+  double mx = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    mx = fmax(mx, fabs(A[e]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+}
+
+// Step k: pivot = first row i >= k with the largest |A[i, k]|; singular (state
+// 2) below tol; the rows are swapped in full.  One block.
+__global__ void lu_pivot_kernel(double* A, int N, int k, int32_t* piv, int* state,
+                                const unsigned long long* scale_bits) {
+  if (*state != 0) return;
+  __shared__ double sv[32];
+  __shared__ int si[32];
+  double best = -1.0;
+  int bi = N;
+  for (int i = k + threadIdx.x; i < N; i += blockDim.x) {
+    const double v = fabs(A[(int64_t)i * N + k]);
+    if (v > best) {  // ascending i per thread: the first of equal maxima
+      best = v;
+      bi = i;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ov > best || (ov == best && oi < bi)) {
+      best = ov;
+      bi = oi;
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sv[threadIdx.x >> 5] = best;
+    si[threadIdx.x >> 5] = bi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      if (sv[w] > best || (sv[w] == best && si[w] < bi)) {
+        best = sv[w];
+        bi = si[w];
+      }
+    const double scale = fmax(__longlong_as_double((long long)*scale_bits), 2.2250738585072014e-308);
+    piv[k] = bi;
+    if (best < 1e-12 * scale) *state = 2;
+    si[0] = bi;
+  }
+  __syncthreads();
+  if (*state != 0) return;
+  const int pr = si[0];
+  if (pr != k)
+    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+      const double t = A[(int64_t)k * N + c];
+      A[(int64_t)k * N + c] = A[(int64_t)pr * N + c];
+      A[(int64_t)pr * N + c] = t;
+    }
+}
+
+// Step k: multipliers f_i = A[i, k] / A[k, k] stored in place (rows > k).
+__global__ void lu_scale_kernel(double* A, int N, int k, const int* state) {
+  if (*state != 0) return;
+  const double pivot = A[(int64_t)k * N + k];
+  for (int i = k + 1 + blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    A[(int64_t)i * N + k] = A[(int64_t)i * N + k] / pivot;
+}
+
+// Step k: trailing update A[i, c] -= f_i A[k, c] for rows i > k with f_i != 0.
+__global__ void lu_update_kernel(double* A, int N, int k, const int* state) {
+  if (*state != 0) return;
+  const int i = k + 1 + blockIdx.y;
+  const double f = A[(int64_t)i * N + k];
+  if (f == 0.0) return;
+  const double* rk = A + (int64_t)k * N;
+  double* ri = A + (int64_t)i * N;
+  for (int c = k + 1 + blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x)
+    ri[c] -= f * rk[c];
+}
+
+// One warp per target: the right-hand side (kriging.rs:580-598), Lu::solve
+// with the factors (rows permuted by perm, unit-lower forward and upper back
+// substitution), outputs as krige_fp64_kernel.  scratch: 2 N doubles per warp.
+template <int D>
+__global__ void global_solve_kernel(KrigeArgs a, DevModel m, int N, const double* LU,
+                                    const int32_t* perm, int state, double* scratch,
+                                    int64_t nwarps_scratch) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  if (w0 >= nwarps_scratch) return;
+  double* R = scratch + w0 * 2 * (int64_t)N;  // b in system order
+  double* Y = R + N;                            // permuted b, then the solution
+  const int n = (int)a.n, p = a.p;
+  const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
+  for (int64_t t = w0; t < a.ntl; t += nw) {
+    uint8_t st = GS_ST_OK;
+    if (n < a.min_nb) st = GS_ST_NO_NEIGHBORS;
+    else if (n < p) st = GS_ST_INSUFFICIENT_DATA;
+    else if (state != 1) st = GS_ST_SINGULAR;
+    if (st != GS_ST_OK) {
+      if (lane == 0) {
+        a.out_v[t] = kNaN;
+        a.out_var[t] = kNaN;
+        if (a.out_lag) a.out_lag[t] = kNaN;
+        a.out_st[t] = st;
+      }
+      continue;
+    }
+    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+    const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
+    for (int i = lane; i < N; i += 32) {
+      double b;
+      if (i < n) {
+        const double h[3] = {a.x[i] - tp[0], a.y[i] - tp[1], D == 3 ? a.z[i] - tp[2] : 0.0};
+        b = cov_fp64<D>(m, h);
+      } else {
+        b = basis_at<D>(a, tp, trow, i - n);
+      }
+      R[i] = b;
+    }
+    __syncwarp();
+    for (int i = lane; i < N; i += 32) Y[i] = R[perm[i]];
+    __syncwarp();
+    // forward: y_i -= sum_{j < i} L_ij y_j (unit lower)
+    for (int i = 1; i < N; ++i) {
+      const double* Li = LU + (int64_t)i * N;
+      double s = 0.0;
+      for (int j = lane; j < i; j += 32) s = fma(Li[j], Y[j], s);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) Y[i] -= s;
+      __syncwarp();
+    }
+    // back: y_i = (y_i - sum_{j > i} U_ij y_j) / U_ii
+    for (int i = N - 1; i >= 0; --i) {
+      const double* Ui = LU + (int64_t)i * N;
+      double s = 0.0;
+      for (int j = i + 1 + lane; j < N; j += 32) s = fma(Ui[j], Y[j], s);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) Y[i] = (Y[i] - s) / Ui[i];
+      __syncwarp();
+    }
+    // outputs (kriging.rs:614-643)
+    double v = 0.0, red = 0.0;
+    if (a.method == GS_SIMPLE) {
+      for (int i = lane; i < n; i += 32) {
+        v = fma(Y[i], a.val[i] - a.sk_mean, v);
+        red = fma(Y[i], R[i], red);
+      }
+    } else {
+      for (int i = lane; i < n; i += 32) v = fma(Y[i], a.val[i], v);
+      for (int i = lane; i < N; i += 32) red = fma(Y[i], R[i], red);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+      red += __shfl_xor_sync(0xffffffffu, red, o);
+    }
+    if (lane == 0) {
+      a.out_v[t] = a.method == GS_SIMPLE ? a.sk_mean + v : v;
+      a.out_var[t] = fmax(m.c0 - red, 0.0);
+      if (a.out_lag) a.out_lag[t] = a.method == GS_SIMPLE ? kNaN : Y[n];
+      a.out_st[t] = GS_ST_OK;
+    }
+    __syncwarp();
+  }
+}
+
 template <int D>
 __global__ void grid_centers_kernel(double x0, double y0, double z0, double dx, double dy,
                                     double dz, int64_t nx, int64_t ny, int64_t total, double* x,
@@ -1182,6 +1383,54 @@ int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, doub
   const int Mmax = std::min(a.kout, GS_MIXED_MAX_NEIGHBORS) + a.p + 2;
   if (a.dim == 2) return launch_chol<2>(a, m, flag, Mmax, scratch, scratch_warps, stream);
   return launch_chol<3>(a, m, flag, Mmax, scratch, scratch_warps, stream);
+}
+
+int global_factor(const KrigeArgs& a, const DevModel& m, int N, double* A, int32_t* piv,
+                  int* state_out, cudaStream_t stream) {
+  DevBuf st, sc;
+  GS_TRY(st.alloc(sizeof(int), stream));
+  GS_TRY(sc.alloc(sizeof(unsigned long long), stream));
+  GS_CUDA(cudaMemsetAsync(st.ptr, 0, sizeof(int), stream));
+  GS_CUDA(cudaMemsetAsync(sc.ptr, 0, sizeof(unsigned long long), stream));
+  const int64_t total = (int64_t)N * N;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  if (a.dim == 2) global_lhs_kernel<2><<<blocks, 256, 0, stream>>>(a, m, N, A);
+  else global_lhs_kernel<3><<<blocks, 256, 0, stream>>>(a, m, N, A);
+  absmax_kernel<<<blocks, 256, 0, stream>>>(A, total, (unsigned long long*)sc.ptr);
+  GS_CUDA(cudaGetLastError());
+  int* dstate = (int*)st.ptr;
+  for (int k = 0; k < N; ++k) {
+    lu_pivot_kernel<<<1, 1024, 0, stream>>>(A, N, k, piv, dstate, (const unsigned long long*)sc.ptr);
+    const int rows = N - 1 - k;
+    if (rows > 0) {
+      lu_scale_kernel<<<(rows + 255) / 256, 256, 0, stream>>>(A, N, k, dstate);
+      const int cols = N - 1 - k;
+      dim3 grid((unsigned)std::min((cols + 127) / 128, 8), (unsigned)rows);
+      lu_update_kernel<<<grid, 128, 0, stream>>>(A, N, k, dstate);
+    }
+  }
+  GS_CUDA(cudaGetLastError());
+  count_launch(2 + 3 * N);
+  int state = 0;
+  GS_CUDA(cudaMemcpyAsync(&state, dstate, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  GS_CUDA(cudaStreamSynchronize(stream));
+  *state_out = state == 0 ? 1 : 2;
+  return GS_OK;
+}
+
+int global_solve_launch(const KrigeArgs& a, const DevModel& m, int N, const double* LU,
+                        const int32_t* perm, int state, double* scratch, int64_t scratch_warps,
+                        cudaStream_t stream) {
+  if (a.ntl == 0) return GS_OK;
+  const int64_t warps = std::min<int64_t>(scratch_warps, a.ntl);
+  const int blocks = (int)((warps * 32 + 127) / 128);
+  if (a.dim == 2)
+    global_solve_kernel<2><<<blocks, 128, 0, stream>>>(a, m, N, LU, perm, state, scratch, warps);
+  else
+    global_solve_kernel<3><<<blocks, 128, 0, stream>>>(a, m, N, LU, perm, state, scratch, warps);
+  GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  return GS_OK;
 }
 
 int64_t fp64_scratch_doubles(int nmax, int64_t threads) {

@@ -78,6 +78,16 @@ int64_t chol_scratch_doubles(int64_t warps);
 int krige_fp64_launch(const KrigeArgs& a, const DevModel& m, double* scratch, int64_t threads,
                       cudaStream_t stream);
 int64_t fp64_scratch_doubles(int nmax, int64_t threads);
+// Global neighbourhood (kriging.rs:396-406): build_lhs over all points and
+// lu_factor on the device into A (N x N, row-major), pivots piv[N];
+// *state = 1 factored, 2 singular (as lu_factor's error).  Synchronises.
+int global_factor(const KrigeArgs& a, const DevModel& m, int N, double* A, int32_t* piv,
+                  int* state, cudaStream_t stream);
+// Per-target Lu::solve with the factors (perm: the row order after the
+// pivots' swaps); scratch: 2 N doubles per warp, at most scratch_warps warps.
+int global_solve_launch(const KrigeArgs& a, const DevModel& m, int N, const double* LU,
+                        const int32_t* perm, int state, double* scratch, int64_t scratch_warps,
+                        cudaStream_t stream);
 int64_t fp64_threads_for(int nmax, int64_t budget_bytes);
 
 // Grid2D / Grid3D cell centres (grid.rs:80-96, 188-203) on the device.

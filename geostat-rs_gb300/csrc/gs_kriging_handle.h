@@ -45,7 +45,15 @@ struct gs_kriging {
   mutable std::mutex tiles_mu;
   mutable std::map<int, gs::Tiles> tiles;
   gs::Tiles pinned{0, 0};
+  // global neighbourhood: LU factors of the (n + p) system (row-major), the
+  // solve's row order; lu_state 0 none, 1 factored, 2 singular
+  double* d_lu = nullptr;
+  int32_t* d_perm = nullptr;
+  int lu_n = 0;
+  int lu_state = 0;
   ~gs_kriging() {
+    cudaFree(d_lu);
+    cudaFree(d_perm);
     cudaFree(d_drift);
     cudaFree(d_err);
     cudaFree(d_basis_df);
