@@ -286,6 +286,7 @@ def run_ours(args, rank, world):
         acc, cpu = cpu_sample_and_accuracy(args, coords, values, model, tg, mixed_value, mixed_var,
                                            fp64_v, kr, log)
         cvr = cv_bench(args, coords, values, model, log) if args.cv_sample > 0 else None
+        glb = global_bench(args, log) if not args.no_global else None
         vec = vecchia_bench(args, log) if not args.no_vecchia else None
         clu = clustered_bench(args, log) if not args.no_clustered else None
         serve = serving_bench(args, log) if args.serve_requests > 0 else None
@@ -336,6 +337,8 @@ def run_ours(args, rank, world):
             result["clustered"] = clu
         if cvr is not None:
             result["cross_validation"] = cvr
+        if glb is not None:
+            result["global_neighbourhood"] = glb
         if serve is not None:
             result["serving"] = serve
             result["p99_latency_ms"] = serve["p99_ms"]
@@ -422,6 +425,49 @@ def cv_bench(args, coords, values, model, log):
             "cpu_kind": "port (a predictor rebuilt per held-out point, as validation.rs:148)",
             "max_rel_value": rel(cv.predicted[sample], np.array(ref_p), vs),
             "max_rel_variance": rel(cv.variance[sample], np.array(ref_v), 1e-3)}
+
+
+def global_bench(args, log):
+    """Global-neighbourhood ordinary kriging (kriging.rs:396-406): the 2-D
+    workload's 2,000 points (uniform in 1000 x 1000 m, 10 + field, nugget 0.1 +
+    Sph(1, 200 m)) with no neighbour limit -- one 2,001-unknown system factored
+    at build -- predicted at the 100 x 100 grid; the oracle (the same global LU
+    path) on all host cores."""
+    import geostat_rs as G
+    from geostat_rs.model import Structure, VariogramModel
+    n = 2000
+    c = G.rng_uniform(SEED + 31, 2 * n).reshape(n, 2) * 1000.0
+    m = VariogramModel(0.1, [Structure("spherical", 1.0, 200.0)])
+    v = 10.0 + G.rff_field(c, m, 2048, SEED + 32)
+    g = (np.arange(100) + 0.5) * 10.0
+    yy, xx = np.meshgrid(g, g, indexing="ij")
+    t = np.stack([xx.ravel(), yy.ravel()], 1)
+    t0 = time.perf_counter()
+    k = G.Kriging.new(G.PointSet(c, v), m)
+    build = time.perf_counter() - t0
+    k.predict_many(t)
+    ts = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        out = k.predict_many(t, full=True)
+        ts.append(time.perf_counter() - t1)
+    dt = statistics.median(ts)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    t1 = time.perf_counter()
+    ref = O.krige(c, v, m, t, nthreads=cores)
+    dcpu = time.perf_counter() - t1
+    vs = float(np.mean(np.abs(v)))
+    rel = lambda a, b, f: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), f)))
+    log(f"[bench] global neighbourhood: build {build * 1e3:.0f} ms, {len(t)} targets in "
+        f"{dt * 1e3:.1f} ms; oracle {dcpu:.2f} s on {cores} threads")
+    return {"data": n, "unknowns": n + 1, "targets": len(t), "build_seconds": build,
+            "predict_seconds": dt, "targets_per_s": len(t) / dt,
+            "cpu_targets_per_s": len(t) / dcpu, "cpu_cores": cores, "cpu_seconds_incl_factor": dcpu,
+            "max_rel_value": rel(out.value, ref["value"], vs),
+            "max_rel_variance": rel(out.variance, ref["variance"], 1e-3)}
 
 
 def vecchia_bench(args, log):
@@ -885,6 +931,8 @@ def main():
     ap.add_argument("--no-vecchia", action="store_true")
     ap.add_argument("--no-clustered", action="store_true",
                     help="skip the clustered uneven workload")
+    ap.add_argument("--no-global", action="store_true",
+                    help="skip the global-neighbourhood leg")
     ap.add_argument("--cv-sample", type=int, default=40,
                     help="oracle points of the leave-one-out leg (0: skip the leg)")
     ap.add_argument("--cl-sample", type=int, default=200,
