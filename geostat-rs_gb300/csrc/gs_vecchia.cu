@@ -41,7 +41,24 @@ struct gs_vecchia_plan {
   int32_t* d_cnt = nullptr;
   double mean = 0.0;
   cudaStream_t stream = nullptr;
+  // grouped likelihood blocks per group size: block b's joint set (the
+  // members' predecessors, then the members) at vid[off[b] .. off[b + 1]),
+  // the first slen[b] of them predecessors; vmax = the largest set
+  struct Groups {
+    int64_t nblocks = 0;
+    int vmax = 0;
+    int64_t* d_off = nullptr;
+    int32_t* d_vid = nullptr;
+    int32_t* d_slen = nullptr;
+  };
+  mutable std::mutex groups_mu;
+  mutable std::map<int64_t, Groups> groups;
   ~gs_vecchia_plan() {
+    for (auto& g : groups) {
+      cudaFree(g.second.d_off);
+      cudaFree(g.second.d_vid);
+      cudaFree(g.second.d_slen);
+    }
     cudaFree(d_order);
     cudaFree(d_nb);
     cudaFree(d_cnt);
@@ -565,6 +582,116 @@ __global__ void reduce_partials(const double* partial, int nblk, int ncand, doub
   double s = 0.0;
   for (int b = 0; b < nblk; ++b) s += partial[(int64_t)c * nblk + b];
   out[c] = s;
+}
+
+// ---------------------------------------- grouped likelihood (Guinness) --
+// loglik_with_blocks (vecchia.rs:613-668) in FP64, one warp per (block,
+// candidate): the joint covariance of a block's set V (sill on the diagonal,
+// sill - gamma off it) bordered by the centred values z_V as a last row,
+// LDL^T over V (the reference's Cholesky test: pivot > 1e-12 sill).  For a
+// member t, Cholesky's L_tt^2 is the pivot d_t and its forward-solved value
+// is a_t / sqrt(d_t), a_t = the border row's entry after t's elimination, so
+//     term_t = -1/2 (ln 2 pi + ln d_t + a_t^2 / d_t).
+// Trailing updates use the flattened pair table of the kriging re-solve
+// (the system embedded at the bottom right of a Vmax frame).
+struct GroupArgs {
+  const int64_t* off;
+  const int32_t* vid;
+  const int32_t* slen;
+  int64_t nblocks;
+  int vmax;  // frame size: the largest set + the border row
+};
+
+__host__ __device__ inline size_t group_warp_doubles(int vmax) {
+  return (size_t)vmax * (vmax + 1) / 2 + 2 * (size_t)vmax;
+}
+
+template <int D>
+__global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cstat) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int Vmax = g.vmax;
+  uint32_t* ptab = reinterpret_cast<uint32_t*>(smem_raw);
+  const size_t ptab_bytes = (((size_t)Vmax * (Vmax - 1) / 2) * 4 + 15) & ~(size_t)15;
+  for (int j = 1; j < Vmax; ++j) {
+    const int off = ((Vmax - 1 - j) * (Vmax - j)) >> 1;
+    for (int i = j + threadIdx.x; i < Vmax; i += blockDim.x)
+      ptab[off + i - j] = ((uint32_t)pk(i, j) << 16) | ((uint32_t)i << 8) | (uint32_t)j;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* A = reinterpret_cast<double*>(smem_raw + ptab_bytes) + (size_t)warp * group_warp_doubles(Vmax);
+  double* lsc = A + (size_t)Vmax * (Vmax + 1) / 2;
+  double* lun = lsc + Vmax;
+  const int64_t items = (int64_t)a.ncand * g.nblocks;
+  const int64_t nw = (int64_t)gridDim.x * wpb;
+  const double* xs[3] = {a.x, a.y, a.z};
+  for (int64_t it = (int64_t)blockIdx.x * wpb + warp; it < items; it += nw) {
+    const int c = (int)(it / g.nblocks);
+    const int64_t b = it % g.nblocks;
+    const DevModel& mdl = a.models[c];
+    const int32_t* ids = g.vid + g.off[b];
+    const int vn = (int)(g.off[b + 1] - g.off[b]);
+    const int sl = g.slen[b];
+    const int M = vn + 1;
+    const int o = Vmax - M;
+    const int iz = o + vn;  // border row
+    for (int e = lane; e < (vn * (vn - 1)) / 2 + vn; e += 32) {
+      // (r, q), q <= r < vn, packed order
+      int r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+      while ((r * (r + 1)) / 2 > e) --r;
+      while (((r + 1) * (r + 2)) / 2 <= e) ++r;
+      const int q = e - (r * (r + 1)) / 2;
+      double v = mdl.c0;
+      if (q != r) {
+        double h[3];
+#pragma unroll
+        for (int d = 0; d < D; ++d) h[d] = xs[d][ids[q]] - xs[d][ids[r]];
+        v = cov_fp64<D>(mdl, h);
+      }
+      A[pk(o + r, o + q)] = v;
+    }
+    for (int q = lane; q < vn; q += 32) A[pk(iz, o + q)] = a.v[ids[q]] - a.mean;
+    if (lane == 0) A[pk(iz, iz)] = 0.0;
+    __syncwarp();
+    const double tol = 1e-12 * fmax(mdl.c0, 2.2250738585072014e-308);
+    bool ok = true;
+    for (int k = o; k < iz; ++k) {
+      const double dk = A[pk(k, k)];
+      if (!(dk > tol)) {
+        ok = false;
+        break;
+      }
+      const double r = 1.0 / dk;
+      for (int i = k + 1 + lane; i < Vmax; i += 32) {
+        const double v = A[pk(i, k)];
+        lun[i] = v;
+        lsc[i] = v * r;
+      }
+      __syncwarp();
+      const int T = ((Vmax - 1 - k) * (Vmax - k)) >> 1;
+      for (int e = lane; e < T; e += 32) {
+        const uint32_t en = ptab[e];
+        const int pe = (int)(en >> 16), i = (int)((en >> 8) & 255u), j = (int)(en & 255u);
+        A[pe] = fma(-lsc[i], lun[j], A[pe]);
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      double sum = __longlong_as_double(0x7ff8000000000000ll);
+      if (ok) {
+        sum = 0.0;
+        for (int t = sl; t < vn; ++t) {
+          const double dt = A[pk(o + t, o + t)];
+          const double at = A[pk(iz, o + t)];
+          sum += -0.5 * (kLn2Pi + log(dt) + at * at / dt);
+        }
+      } else {
+        atomicExch(&cstat[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
+      }
+      a.terms[(int64_t)c * g.nblocks + b] = sum;
+    }
+    __syncwarp();
+  }
 }
 
 ExpTable g_vtab;
@@ -1191,6 +1318,177 @@ int reject_grad_model(const gs_model& m, int dim) {
 }
 
 // Log-likelihood and gradient of ncand candidates on a plan.
+// guinness_blocks (vecchia.rs:570-602) and each block's joint set
+// (vecchia.rs:628-641) on the host, with per-point marks instead of the
+// reference's list searches (the same sets, in the same order).
+static int build_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan::Groups* out) {
+  const int64_t n = P->n, M = P->m;
+  std::vector<int32_t> nb((size_t)n * M), cnt(n);
+  GS_CUDA(cudaMemcpy(nb.data(), P->d_nb, nb.size() * 4, cudaMemcpyDeviceToHost));
+  GS_CUDA(cudaMemcpy(cnt.data(), P->d_cnt, cnt.size() * 4, cudaMemcpyDeviceToHost));
+  const std::vector<int64_t>& order = P->order;
+  std::vector<int64_t> mark_v(n, -1), mark_b(n, -1);
+  std::vector<std::pair<int64_t, int64_t>> blocks;
+  int64_t stamp = 0;
+  for (int64_t k0 = 0; k0 < n;) {
+    ++stamp;
+    for (int a = 0; a < cnt[k0]; ++a) mark_v[nb[k0 * M + a]] = stamp;
+    mark_b[order[k0]] = stamp;
+    int64_t k1 = k0 + 1;
+    while (k1 < n && (k1 - k0) < gsize) {
+      const int c = cnt[k1];
+      const int m = std::max(c, 1);
+      int fresh = 0;
+      for (int a = 0; a < c; ++a) {
+        const int32_t j = nb[k1 * M + a];
+        if (mark_v[j] != stamp && mark_b[j] != stamp) ++fresh;
+      }
+      if ((double)fresh > 0.34 * (double)m) break;
+      for (int a = 0; a < c; ++a) {
+        const int32_t j = nb[k1 * M + a];
+        if (mark_v[j] != stamp && mark_b[j] != stamp) mark_v[j] = stamp;
+      }
+      mark_b[order[k1]] = stamp;
+      ++k1;
+    }
+    blocks.emplace_back(k0, k1);
+    k0 = k1;
+  }
+  std::vector<int64_t> off(blocks.size() + 1, 0);
+  std::vector<int32_t> vid, slen(blocks.size());
+  std::vector<int64_t> mark_m(n, -1), mark_s(n, -1);
+  int vmax = 0;
+  for (size_t b = 0; b < blocks.size(); ++b) {
+    const int64_t k0 = blocks[b].first, k1 = blocks[b].second;
+    const int64_t st = (int64_t)b;
+    for (int64_t k = k0; k < k1; ++k) mark_m[order[k]] = st;
+    const size_t start = vid.size();
+    for (int64_t k = k0; k < k1; ++k)
+      for (int a = 0; a < cnt[k]; ++a) {
+        const int32_t j = nb[k * M + a];
+        if (mark_m[j] != st && mark_s[j] != st) {
+          mark_s[j] = st;
+          vid.push_back(j);
+        }
+      }
+    slen[b] = (int32_t)(vid.size() - start);
+    for (int64_t k = k0; k < k1; ++k) vid.push_back((int32_t)order[k]);
+    off[b + 1] = (int64_t)vid.size();
+    vmax = std::max(vmax, (int)(vid.size() - start));
+  }
+  if (vmax + 1 > 255)
+    return fail(GS_ERR_INVALID_PARAMETER, "a grouped conditioning set of " + std::to_string(vmax) +
+                                              " points exceeds 254 on the CUDA path");
+  out->nblocks = (int64_t)blocks.size();
+  out->vmax = vmax + 1;
+  if (cudaMalloc(&out->d_off, off.size() * 8) != cudaSuccess ||
+      cudaMalloc(&out->d_vid, std::max<size_t>(vid.size(), 1) * 4) != cudaSuccess ||
+      cudaMalloc(&out->d_slen, slen.size() * 4) != cudaSuccess)
+    return fail(GS_ERR_OUT_OF_MEMORY, "grouped plan allocation failed");
+  GS_CUDA(cudaMemcpy(out->d_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice));
+  GS_CUDA(cudaMemcpy(out->d_vid, vid.data(), vid.size() * 4, cudaMemcpyHostToDevice));
+  GS_CUDA(cudaMemcpy(out->d_slen, slen.data(), slen.size() * 4, cudaMemcpyHostToDevice));
+  return GS_OK;
+}
+
+int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
+                         int64_t gsize, double* ll, int32_t* status, cudaStream_t s) {
+  if (gsize <= 1) return vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s);
+  const gs_pointset* ps = P->ps;
+  const int dim = ps->dim;
+  gs_vecchia_plan::Groups G;
+  {
+    std::lock_guard<std::mutex> lk(P->groups_mu);
+    auto it = P->groups.find(gsize);
+    if (it == P->groups.end()) {
+      gs_vecchia_plan::Groups fresh;
+      const int rc = build_groups(P, gsize, &fresh);
+      if (rc) {
+        cudaFree(fresh.d_off);
+        cudaFree(fresh.d_vid);
+        cudaFree(fresh.d_slen);
+        return rc;
+      }
+      it = P->groups.emplace(gsize, fresh).first;
+    }
+    G = it->second;
+  }
+  std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
+  std::vector<int> valid(ncand, 0);
+  for (int64_t c = 0; c < ncand; ++c) {
+    status[c] = GS_OK;
+    ll[c] = NAN;
+    int rc = reject_vecchia_model(models[c], dim);
+    if (!rc) rc = make_dev_model(models[c], dim, &dms[c], true);
+    if (rc) {
+      status[c] = rc;
+      dms[c] = DevModel{};
+      dms[c].c0 = 1.0;
+      continue;
+    }
+    valid[c] = 1;
+  }
+  if (ncand == 0) return GS_OK;
+  DevBuf dmod, terms, partial, out, cstat;
+  GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
+  GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
+  GS_TRY(terms.alloc((size_t)ncand * G.nblocks * 8, s));
+  GS_TRY(cstat.alloc((size_t)ncand * 4, s));
+  GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
+  VArgs a{};
+  a.dim = dim;
+  a.n = P->n;
+  a.m = (int)P->m;
+  a.ncand = (int)ncand;
+  a.x = ps->d_x;
+  a.y = ps->d_y;
+  a.z = ps->d_z;
+  a.v = ps->d_v;
+  a.mean = P->mean;
+  a.models = (const DevModel*)dmod.ptr;
+  a.terms = (double*)terms.ptr;
+  GroupArgs g{G.d_off, G.d_vid, G.d_slen, G.nblocks, G.vmax};
+  const size_t ptab_bytes = (((size_t)G.vmax * (G.vmax - 1) / 2) * 4 + 15) & ~(size_t)15;
+  const size_t per_warp = group_warp_doubles(G.vmax) * 8;
+  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024 - ptab_bytes) / per_warp));
+  const size_t smem = ptab_bytes + wpb * per_warp;
+  auto kern = dim == 2 ? vecchia_group_kernel<2> : vecchia_group_kernel<3>;
+  GS_TRY(allow_dynamic_smem((const void*)kern, smem));
+  int dev = 0, sms = 152, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * wpb, smem));
+  const int64_t items = ncand * G.nblocks;
+  const int blocks = (int)std::max<int64_t>(
+      1, std::min<int64_t>((items + wpb - 1) / wpb, (int64_t)sms * std::max(per_sm, 1)));
+  kern<<<blocks, 32 * wpb, smem, s>>>(a, g, wpb, (int32_t*)cstat.ptr);
+  GS_CUDA(cudaGetLastError());
+  const int64_t chunk = 8192;
+  const int nblk = (int)((G.nblocks + chunk - 1) / chunk);
+  GS_TRY(partial.alloc((size_t)nblk * ncand * 8, s));
+  GS_TRY(out.alloc((size_t)ncand * 8, s));
+  reduce_terms<<<dim3(nblk, (unsigned)ncand), 256, 0, s>>>((double*)terms.ptr, G.nblocks, chunk,
+                                                          (double*)partial.ptr);
+  reduce_partials<<<(int)((ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)ncand,
+                                                             (double*)out.ptr);
+  GS_CUDA(cudaGetLastError());
+  count_launch(3);
+  std::vector<double> hll(ncand);
+  std::vector<int32_t> hst(ncand);
+  GS_CUDA(cudaMemcpyAsync(hll.data(), out.ptr, ncand * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hst.data(), cstat.ptr, ncand * 4, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  for (int64_t c = 0; c < ncand; ++c) {
+    if (!valid[c]) continue;
+    if (hst[c] != 0) {
+      status[c] = hst[c];
+      continue;
+    }
+    ll[c] = hll[c];
+  }
+  return GS_OK;
+}
+
 int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
                       double* grad, int32_t* status, int precision, cudaStream_t s) {
   const gs_pointset* ps = P->ps;
@@ -1985,6 +2283,14 @@ int gs_vecchia_loglik_batch(const gs_vecchia_plan* P, int64_t ncand, const gs_mo
   if (!P) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
   cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
   return vecchia_eval(P, ncand, models, loglik, status, precision, s);
+}
+
+int gs_vecchia_loglik_grouped_batch(const gs_vecchia_plan* P, int64_t ncand,
+                                    const gs_model* models, int64_t group_size, double* loglik,
+                                    int32_t* status, void* stream) {
+  if (!P) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
+  cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
+  return vecchia_eval_grouped(P, ncand, models, group_size, loglik, status, s);
 }
 
 // vecchia_loglik (vecchia.rs:874-884).

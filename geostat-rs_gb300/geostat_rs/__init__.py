@@ -15,7 +15,7 @@ from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Ser
                   last_timings, leave_one_out, leave_one_out_with_drift, maxmin_order,
                   tune_kriging_neighbors,
                   nelder_mead_multistart, rff_field, rng_normal, rng_uniform, seq_mean,
-                  vecchia_krige, vecchia_loglik, vecchia_mle, vecchia_mle_fit,
+                  vecchia_krige, vecchia_loglik, vecchia_loglik_grouped, vecchia_mle, vecchia_mle_fit,
                   vecchia_mle_nm_fit, vecchia_predict)
 from ._abi import LIB_PATH, load as load_library
 

@@ -95,6 +95,7 @@ SIGNATURES = {
     "gs_vecchia_plan_get": (_int, [_vp, _pi64, _pi64, _pi32]),
     "gs_vecchia_plan_destroy": (None, [_vp]),
     "gs_vecchia_loglik_batch": (_int, [_vp, _i64, _pm, _pd, _pi32, _int, _vp]),
+    "gs_vecchia_loglik_grouped_batch": (_int, [_vp, _i64, _pm, _i64, _pd, _pi32, _vp]),
     "gs_vecchia_loglik": (_int, [_vp, _pm, _i64, _pi64, _pd]),
     "gs_vecchia_mle": (_int, [_vp, _i32, _i64, _pi64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_mle_nm": (_int, [_vp, _i32, _i64, _pi64, _i64, _pd, _d, _i64, _pm, _pd, _pd, _pi64]),

@@ -583,6 +583,18 @@ class VecchiaPlan:
                                                        PRECISIONS[precision], None))
         return ll, st
 
+    def loglik_grouped(self, models: Sequence[VariogramModel], group_size: int):
+        """``loglik_with_plan_grouped`` (vecchia.rs:604-668, Guinness
+        grouping) of each candidate model; ``group_size <= 1`` is
+        :meth:`loglik`.  Returns ``(loglik, status)``."""
+        arr = (_abi.Model * len(models))(*[model_struct(m) for m in models])
+        ll = np.empty(len(models))
+        st = np.empty(len(models), dtype=np.int32)
+        _abi.check(_abi.load().gs_vecchia_loglik_grouped_batch(self._h, len(models), arr,
+                                                               int(group_size), _p(ll),
+                                                               _p(st, C.c_int32), None))
+        return ll, st
+
     def close(self):
         if getattr(self, "_h", None):
             _abi.load().gs_vecchia_plan_destroy(self._h)
@@ -613,6 +625,17 @@ def vecchia_loglik(x, y, values, model, m=20):
     _abi.check(_abi.load().gs_vecchia_loglik(data._h, C.byref(model_struct(model)), int(m), None,
                                              C.byref(ll)))
     return ll.value
+
+
+def vecchia_loglik_grouped(data: PointSet, model: VariogramModel, m: int, order=None,
+                           group_size: int = 1) -> float:
+    """``vecchia_loglik_grouped`` (vecchia.rs:891-901)."""
+    plan = VecchiaPlan(data, m, order)
+    ll, st = plan.loglik_grouped([model], group_size)
+    if st[0] != 0:
+        from .errors import raise_for
+        raise_for(int(st[0]), "singular conditioning system")
+    return float(ll[0])
 
 
 def _fit_kind(kind):

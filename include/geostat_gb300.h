@@ -244,6 +244,15 @@ void gs_vecchia_plan_destroy(gs_vecchia_plan* plan);
  * GeostatError code (a singular conditioning system). */
 int gs_vecchia_loglik_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs_model* models,
                             double* loglik, int32_t* status, int precision, void* stream);
+/* loglik_with_plan_grouped (vecchia.rs:604-668, Guinness 2018 grouping) for
+ * ncand candidates: blocks of up to group_size consecutive ordered points
+ * (guinness_blocks, vecchia.rs:570-602) conditioned jointly on the union of
+ * their predecessor sets, one FP64 factorisation per block and candidate.
+ * group_size <= 1 is gs_vecchia_loglik_batch.  The blocks of a group size
+ * are built once per plan.  Joint sets beyond 254 points: InvalidParameter. */
+int gs_vecchia_loglik_grouped_batch(const gs_vecchia_plan* plan, int64_t ncand,
+                                    const gs_model* models, int64_t group_size, double* loglik,
+                                    int32_t* status, void* stream);
 /* vecchia_loglik (vecchia.rs:874-884). */
 int gs_vecchia_loglik(const gs_pointset* ps, const gs_model* model, int64_t m,
                       const int64_t* order, double* loglik);

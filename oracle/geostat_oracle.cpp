@@ -1247,6 +1247,97 @@ int loglik_with_plan(const double* coords, const double* values, size_t n, int d
   return OR_OK;
 }
 
+// vecchia.rs:570-602 guinness_blocks: consecutive ordered points join a
+// block while at most 34 % of a new member's predecessors are new to it.
+std::vector<std::pair<size_t, size_t>> guinness_blocks(const Plan& plan, size_t group_size) {
+  const size_t n = plan.order.size();
+  std::vector<std::pair<size_t, size_t>> blocks;
+  std::vector<size_t> v_ids;
+  auto contains = [](const std::vector<size_t>& v, size_t x) {
+    return std::find(v.begin(), v.end(), x) != v.end();
+  };
+  size_t k0 = 0;
+  while (k0 < n) {
+    v_ids.assign(plan.nb[k0].begin(), plan.nb[k0].end());
+    size_t k1 = k0 + 1;
+    while (k1 < n && (k1 - k0) < group_size) {
+      const std::vector<size_t>& nb = plan.nb[k1];
+      const size_t m = std::max<size_t>(nb.size(), 1);
+      auto in_block = [&](size_t j) {
+        for (size_t q = k0; q < k1; ++q)
+          if (plan.order[q] == j) return true;
+        return false;
+      };
+      size_t new_count = 0;
+      for (size_t j : nb)
+        if (!contains(v_ids, j) && !in_block(j)) ++new_count;
+      if ((double)new_count > 0.34 * (double)m) break;
+      for (size_t j : nb)
+        if (!contains(v_ids, j) && !in_block(j)) v_ids.push_back(j);
+      ++k1;
+    }
+    blocks.emplace_back(k0, k1);
+    k0 = k1;
+  }
+  return blocks;
+}
+
+// vecchia.rs:613-668 loglik_with_blocks: per block, the union S of the
+// members' predecessors (members excluded) followed by the members; one
+// Cholesky of the joint covariance; each member's term from its pivot and
+// its forward-solved value.
+int loglik_with_blocks(const double* coords, const double* values, size_t n, int dim,
+                       const or_model& model, const Plan& plan,
+                       const std::vector<std::pair<size_t, size_t>>& blocks, double* out) {
+  const double mean = mean_of(values, n);
+  std::vector<double> z(n);
+  for (size_t i = 0; i < n; ++i) z[i] = values[i] - mean;
+  const double sill = total_sill(model);
+  const double ln2pi = std::log(2.0 * kPi);
+  std::vector<size_t> v_ids;
+  std::vector<double> kvv, w;
+  double loglik = 0.0;
+  for (const auto& blk : blocks) {
+    const size_t k0 = blk.first, k1 = blk.second;
+    auto in_block = [&](size_t j) {
+      for (size_t q = k0; q < k1; ++q)
+        if (plan.order[q] == j) return true;
+      return false;
+    };
+    v_ids.clear();
+    for (size_t k = k0; k < k1; ++k)
+      for (size_t j : plan.nb[k])
+        if (!in_block(j) && std::find(v_ids.begin(), v_ids.end(), j) == v_ids.end())
+          v_ids.push_back(j);
+    const size_t s_len = v_ids.size();
+    for (size_t k = k0; k < k1; ++k) v_ids.push_back(plan.order[k]);
+    const size_t vn = v_ids.size();
+    kvv.assign(vn * vn, 0.0);
+    for (size_t a = 0; a < vn; ++a) {
+      kvv[a * vn + a] = sill;
+      for (size_t b = a + 1; b < vn; ++b) {
+        double h[3];
+        for (int d = 0; d < dim; ++d) h[d] = coords[v_ids[a] * dim + d] - coords[v_ids[b] * dim + d];
+        const double c = sill - gamma_dh(model, dim, h);
+        kvv[a * vn + b] = c;
+        kvv[b * vn + a] = c;
+      }
+    }
+    int rc = cholesky_factor(kvv.data(), vn);
+    if (rc) return rc;
+    w.resize(vn);
+    for (size_t a = 0; a < vn; ++a) w[a] = z[v_ids[a]];
+    cholesky_forward(kvv.data(), vn, w.data());
+    for (size_t t = s_len; t < vn; ++t) {
+      const double l_tt = kvv[t * vn + t];
+      const double var = l_tt * l_tt;
+      loglik += -0.5 * (ln2pi + std::log(var) + w[t] * w[t]);
+    }
+  }
+  *out = loglik;
+  return OR_OK;
+}
+
 int reject_vecchia_model(const or_model& model, int dim) {
   int rc = validate_model(model);
   if (rc) return rc;
@@ -2018,6 +2109,21 @@ int or_vecchia_loglik_plan(int dim, int64_t n, const double* coords, const doubl
   Plan plan;
   plan_from_arrays((size_t)n, (size_t)m, order, nb, nb_count, plan);
   return loglik_with_plan(coords, values, (size_t)n, dim, *model, plan, ll, terms);
+}
+
+// vecchia.rs:604-611 loglik_with_plan_grouped (group_size <= 1: ungrouped).
+int or_vecchia_loglik_grouped(int dim, int64_t n, const double* coords, const double* values,
+                              const or_model* model, int64_t m, const int64_t* order,
+                              const int64_t* nb, const int32_t* nb_count, int64_t group_size,
+                              double* ll) {
+  int rc = reject_vecchia_model(*model, dim);
+  if (rc) return rc;
+  Plan plan;
+  plan_from_arrays((size_t)n, (size_t)m, order, nb, nb_count, plan);
+  if (group_size <= 1)
+    return loglik_with_plan(coords, values, (size_t)n, dim, *model, plan, ll, nullptr);
+  return loglik_with_blocks(coords, values, (size_t)n, dim, *model, plan,
+                            guinness_blocks(plan, (size_t)group_size), ll);
 }
 
 int or_vecchia_loglik(int dim, int64_t n, const double* coords, const double* values,

@@ -126,6 +126,10 @@ int or_maxmin_order(int dim, int64_t n, const double* coords, int64_t* order);
 int or_maxmin_order_brute(int dim, int64_t n, const double* coords, int64_t* order);
 int or_vecchia_plan(int dim, int64_t n, const double* coords, int64_t m, const int64_t* order_in,
                     int64_t* order_out, int64_t* nb, int32_t* nb_count);
+int or_vecchia_loglik_grouped(int dim, int64_t n, const double* coords, const double* values,
+                              const or_model* model, int64_t m, const int64_t* order,
+                              const int64_t* nb, const int32_t* nb_count, int64_t group_size,
+                              double* ll);
 int or_vecchia_loglik_plan(int dim, int64_t n, const double* coords, const double* values,
                            const or_model* model, int64_t m, const int64_t* order,
                            const int64_t* nb, const int32_t* nb_count, double* ll,

@@ -105,6 +105,8 @@ def _declare(L):
         "or_maxmin_order": (C.c_int, [C.c_int, i64, pd, pi64]),
         "or_maxmin_order_brute": (C.c_int, [C.c_int, i64, pd, pi64]),
         "or_vecchia_plan": (C.c_int, [C.c_int, i64, pd, i64, pi64, pi64, pi64, pi32]),
+        "or_vecchia_loglik_grouped": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pi64, pi64, pi32,
+                                                i64, pd]),
         "or_vecchia_loglik_plan": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pi64, pi64, pi32,
                                              pd, pd]),
         "or_vecchia_loglik": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pi64, pd]),
@@ -359,6 +361,21 @@ def vecchia_loglik_plan(coords, values, model, order, nb, cnt, terms=False):
                                         _p(np.ascontiguousarray(cnt, np.int32), C.c_int32),
                                         C.byref(ll), _p(t)))
     return (ll.value, t) if terms else ll.value
+
+
+def vecchia_loglik_grouped(coords, values, model, order, nb, cnt, group_size):
+    """vecchia.rs:604-668 (Guinness grouping over an existing plan)."""
+    coords, values = _f64(coords), _f64(values)
+    n, m = nb.shape
+    ll = C.c_double()
+    mm = model_struct(model)
+    _check(lib().or_vecchia_loglik_grouped(coords.shape[1], n, _p(coords), _p(values),
+                                           C.byref(mm), m,
+                                           _p(np.ascontiguousarray(order, np.int64), C.c_int64),
+                                           _p(np.ascontiguousarray(nb, np.int64), C.c_int64),
+                                           _p(np.ascontiguousarray(cnt, np.int32), C.c_int32),
+                                           int(group_size), C.byref(ll)))
+    return ll.value
 
 
 def vecchia_loglik(coords, values, model, m, order=None):

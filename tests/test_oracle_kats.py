@@ -494,3 +494,39 @@ def test_vecchia_mle_bfgs_path_improves_on_the_starts():
     o, nb, cnt = O.vecchia_plan(c, 10)
     f0 = O.vecchia_mle_objective(c, v, "exponential", 10, o, nb, cnt, rmax, starts)
     assert f < np.min(f0) and np.isfinite(f) and ne > 3
+
+
+# ----------------------------------------- grouped Vecchia (Guinness 2018) --
+def _exp_model(nug, rng_):
+    return VariogramModel(nug, [Structure("exponential", 1.0, rng_)])
+
+
+def test_grouped_matches_ungrouped_at_group_size_one():
+    # vecchia.rs:2050-2063
+    c, v = O.test_field_2d(90, 11)
+    m = _exp_model(0.05, 30.0)
+    order = O.maxmin_order(c)
+    o, nb, cnt = O.vecchia_plan(c, 12, order)
+    ungrouped = O.vecchia_loglik_plan(c, v, m, o, nb, cnt)
+    assert abs(O.vecchia_loglik_grouped(c, v, m, o, nb, cnt, 1) - ungrouped) < 1e-12
+
+
+def test_grouped_full_conditioning_equals_exact():
+    # vecchia.rs:2066-2085
+    c, v = O.test_field_2d(20, 4)
+    m = _exp_model(0.05, 40.0)
+    exact = O.exact_loglik(c, v, m)
+    o, nb, cnt = O.vecchia_plan(c, len(c) - 1, O.maxmin_order(c))
+    for g in (2, 3, 5, 8):
+        assert abs(O.vecchia_loglik_grouped(c, v, m, o, nb, cnt, g) - exact) < 1e-8
+
+
+def test_grouped_at_least_as_close_as_ungrouped():
+    # vecchia.rs:2088-2107
+    c, v = O.test_field_2d(90, 11)
+    m = _exp_model(0.05, 30.0)
+    exact = O.exact_loglik(c, v, m)
+    o, nb, cnt = O.vecchia_plan(c, 12, O.maxmin_order(c))
+    err0 = abs(O.vecchia_loglik_plan(c, v, m, o, nb, cnt) - exact)
+    for g in (2, 4, 6):
+        assert abs(O.vecchia_loglik_grouped(c, v, m, o, nb, cnt, g) - exact) <= err0 + 1e-9
