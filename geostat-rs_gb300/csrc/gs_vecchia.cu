@@ -17,9 +17,12 @@
 #include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -587,11 +590,16 @@ __global__ void reduce_partials(const double* partial, int nblk, int ncand, doub
 // ---------------------------------------- grouped likelihood (Guinness) --
 // loglik_with_blocks (vecchia.rs:613-668) in FP64, one warp per (block,
 // candidate): the joint covariance of a block's set V (sill on the diagonal,
-// sill - gamma off it) bordered by the centred values z_V as a last row,
-// LDL^T over V (the reference's Cholesky test: pivot > 1e-12 sill).  For a
-// member t, Cholesky's L_tt^2 is the pivot d_t and its forward-solved value
-// is a_t / sqrt(d_t), a_t = the border row's entry after t's elimination, so
-//     term_t = -1/2 (ln 2 pi + ln d_t + a_t^2 / d_t).
+// sill - gamma off it) bordered by nr data rows, LDL^T over V (the
+// reference's Cholesky test: pivot > 1e-12 sill).  For a member t,
+// Cholesky's L_tt^2 is the pivot d_t and a data row's forward-solved value
+// is a_t / sqrt(d_t), a_t = that row's entry after t's elimination, so the
+// likelihood's terms are
+//     term_t = -1/2 (ln 2 pi + ln d_t + a_t^2 / d_t)     (one row: z - mean)
+// and REML (vecchia.rs:1366-1457; rows: z, then the trend basis columns)
+// sums, per block, ln d_t, a_z^2 / d_t, a_f a_z / d_t and a_f a_g / d_t.
+// Singleton blocks stand for the ungrouped REML (vecchia.rs:1278-1345),
+// whose member variance is max(d, 1e-12) rather than a pivot test.
 // Trailing updates use the flattened pair table of the kriging re-solve
 // (the system embedded at the bottom right of a Vmax frame).
 struct GroupArgs {
@@ -599,14 +607,19 @@ struct GroupArgs {
   const int32_t* vid;
   const int32_t* slen;
   int64_t nblocks;
-  int vmax;  // frame size: the largest set + the border row
+  int vmax;             // frame size: the largest set + the data rows
+  int nr;               // data rows: 1, or 1 + p for REML
+  const double* basis;  // REML: p x n trend basis, column-major; else null
+  int clamp_member;     // singleton blocks of the ungrouped REML
 };
 
 __host__ __device__ inline size_t group_warp_doubles(int vmax) {
   return (size_t)vmax * (vmax + 1) / 2 + 2 * (size_t)vmax;
 }
 
-template <int D>
+__host__ __device__ inline int reml_sums(int p) { return 2 + p + p * (p + 1) / 2; }
+
+template <int D, bool REML>
 __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cstat) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Vmax = g.vmax;
@@ -622,6 +635,8 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
   double* A = reinterpret_cast<double*>(smem_raw + ptab_bytes) + (size_t)warp * group_warp_doubles(Vmax);
   double* lsc = A + (size_t)Vmax * (Vmax + 1) / 2;
   double* lun = lsc + Vmax;
+  const int nr = g.nr;
+  const int p = nr - 1;
   const int64_t items = (int64_t)a.ncand * g.nblocks;
   const int64_t nw = (int64_t)gridDim.x * wpb;
   const double* xs[3] = {a.x, a.y, a.z};
@@ -632,9 +647,9 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
     const int32_t* ids = g.vid + g.off[b];
     const int vn = (int)(g.off[b + 1] - g.off[b]);
     const int sl = g.slen[b];
-    const int M = vn + 1;
+    const int M = vn + nr;
     const int o = Vmax - M;
-    const int iz = o + vn;  // border row
+    const int iz = o + vn;  // first data row
     for (int e = lane; e < (vn * (vn - 1)) / 2 + vn; e += 32) {
       // (r, q), q <= r < vn, packed order
       int r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
@@ -650,14 +665,28 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
       }
       A[pk(o + r, o + q)] = v;
     }
-    for (int q = lane; q < vn; q += 32) A[pk(iz, o + q)] = a.v[ids[q]] - a.mean;
-    if (lane == 0) A[pk(iz, iz)] = 0.0;
+    for (int e = lane; e < nr * vn; e += 32) {
+      const int row = e / vn, q = e - row * vn;
+      double v;
+      if (REML)
+        v = row == 0 ? a.v[ids[q]] : g.basis[(int64_t)(row - 1) * a.n + ids[q]];
+      else
+        v = a.v[ids[q]] - a.mean;
+      A[pk(iz + row, o + q)] = v;
+    }
+    for (int e = lane; e < (nr * (nr + 1)) / 2; e += 32) {
+      int r = 0;
+      while (((r + 1) * (r + 2)) / 2 <= e) ++r;
+      A[pk(iz + r, iz + e - (r * (r + 1)) / 2)] = 0.0;
+    }
     __syncwarp();
     const double tol = 1e-12 * fmax(mdl.c0, 2.2250738585072014e-308);
     bool ok = true;
     for (int k = o; k < iz; ++k) {
-      const double dk = A[pk(k, k)];
-      if (!(dk > tol)) {
+      double dk = A[pk(k, k)];
+      if (g.clamp_member && k >= o + sl) {
+        dk = fmax(dk, 1e-12);
+      } else if (!(dk > tol)) {
         ok = false;
         break;
       }
@@ -676,19 +705,50 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
       }
       __syncwarp();
     }
-    if (lane == 0) {
-      double sum = __longlong_as_double(0x7ff8000000000000ll);
-      if (ok) {
-        sum = 0.0;
-        for (int t = sl; t < vn; ++t) {
-          const double dt = A[pk(o + t, o + t)];
-          const double at = A[pk(iz, o + t)];
-          sum += -0.5 * (kLn2Pi + log(dt) + at * at / dt);
+    if (!REML) {
+      if (lane == 0) {
+        double sum = __longlong_as_double(0x7ff8000000000000ll);
+        if (ok) {
+          sum = 0.0;
+          for (int t = sl; t < vn; ++t) {
+            const double dt = A[pk(o + t, o + t)];
+            const double at = A[pk(iz, o + t)];
+            sum += -0.5 * (kLn2Pi + log(dt) + at * at / dt);
+          }
+        } else {
+          atomicExch(&cstat[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
         }
-      } else {
-        atomicExch(&cstat[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
+        a.terms[(int64_t)c * g.nblocks + b] = sum;
       }
-      a.terms[(int64_t)c * g.nblocks + b] = sum;
+    } else {
+      // sums: [0] ln d, [1] a_z^2 / d, [2, 2 + p) a_f a_z / d, then a_f a_g / d
+      // over f <= g, row-packed
+      const int W = reml_sums(p);
+      if (!ok && lane == 0) atomicExch(&cstat[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
+      for (int w = lane; w < W; w += 32) {
+        int r1 = 0, r2 = 0;  // data rows multiplied (w >= 1)
+        if (w >= 2 && w < 2 + p) {
+          r1 = 1 + (w - 2);
+        } else if (w >= 2 + p) {
+          int e = w - 2 - p, f = 0;
+          while (e >= p - f) {
+            e -= p - f;
+            ++f;
+          }
+          r1 = 1 + f;
+          r2 = 1 + f + e;
+        }
+        double sum = __longlong_as_double(0x7ff8000000000000ll);
+        if (ok) {
+          sum = 0.0;
+          for (int t = sl; t < vn; ++t) {
+            double dt = A[pk(o + t, o + t)];
+            if (g.clamp_member) dt = fmax(dt, 1e-12);
+            sum += w == 0 ? log(dt) : A[pk(iz + r1, o + t)] * A[pk(iz + r2, o + t)] / dt;
+          }
+        }
+        a.terms[((int64_t)c * W + w) * g.nblocks + b] = sum;
+      }
     }
     __syncwarp();
   }
@@ -1376,11 +1436,8 @@ static int build_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan
     off[b + 1] = (int64_t)vid.size();
     vmax = std::max(vmax, (int)(vid.size() - start));
   }
-  if (vmax + 1 > 255)
-    return fail(GS_ERR_INVALID_PARAMETER, "a grouped conditioning set of " + std::to_string(vmax) +
-                                              " points exceeds 254 on the CUDA path");
   out->nblocks = (int64_t)blocks.size();
-  out->vmax = vmax + 1;
+  out->vmax = vmax;
   if (cudaMalloc(&out->d_off, off.size() * 8) != cudaSuccess ||
       cudaMalloc(&out->d_vid, std::max<size_t>(vid.size(), 1) * 4) != cudaSuccess ||
       cudaMalloc(&out->d_slen, slen.size() * 4) != cudaSuccess)
@@ -1391,33 +1448,42 @@ static int build_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan
   return GS_OK;
 }
 
-int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
-                         int64_t gsize, double* ll, int32_t* status, cudaStream_t s) {
-  if (gsize <= 1) return vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s);
+// The blocks of one group size, built on first use and kept on the plan.
+int plan_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan::Groups* G) {
+  std::lock_guard<std::mutex> lk(P->groups_mu);
+  auto it = P->groups.find(gsize);
+  if (it == P->groups.end()) {
+    gs_vecchia_plan::Groups fresh;
+    const int rc = build_groups(P, gsize, &fresh);
+    if (rc) {
+      cudaFree(fresh.d_off);
+      cudaFree(fresh.d_vid);
+      cudaFree(fresh.d_slen);
+      return rc;
+    }
+    it = P->groups.emplace(gsize, fresh).first;
+  }
+  *G = it->second;
+  return GS_OK;
+}
+
+// One launch of vecchia_group_kernel over every (candidate, block) and the
+// fixed-order reduction over blocks: per candidate the log-likelihood
+// (nr = 1) or the reml_sums(nr - 1) REML sums, into sums[c * per + w].
+// status[c] / valid[c] as in vecchia_eval.
+int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
+                const gs_vecchia_plan::Groups& G, int nr, const double* d_basis, bool clamp,
+                std::vector<double>& sums, int32_t* status, std::vector<int>& valid,
+                cudaStream_t s) {
   const gs_pointset* ps = P->ps;
   const int dim = ps->dim;
-  gs_vecchia_plan::Groups G;
-  {
-    std::lock_guard<std::mutex> lk(P->groups_mu);
-    auto it = P->groups.find(gsize);
-    if (it == P->groups.end()) {
-      gs_vecchia_plan::Groups fresh;
-      const int rc = build_groups(P, gsize, &fresh);
-      if (rc) {
-        cudaFree(fresh.d_off);
-        cudaFree(fresh.d_vid);
-        cudaFree(fresh.d_slen);
-        return rc;
-      }
-      it = P->groups.emplace(gsize, fresh).first;
-    }
-    G = it->second;
-  }
+  const bool reml = d_basis != nullptr;
+  const int per = reml ? reml_sums(nr - 1) : 1;
   std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
-  std::vector<int> valid(ncand, 0);
+  valid.assign(ncand, 0);
+  sums.assign((size_t)ncand * per, NAN);
   for (int64_t c = 0; c < ncand; ++c) {
     status[c] = GS_OK;
-    ll[c] = NAN;
     int rc = reject_vecchia_model(models[c], dim);
     if (!rc) rc = make_dev_model(models[c], dim, &dms[c], true);
     if (rc) {
@@ -1429,10 +1495,25 @@ int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model
     valid[c] = 1;
   }
   if (ncand == 0) return GS_OK;
+  const int frame = G.vmax + nr;
+  const size_t ptab_bytes = (((size_t)frame * (frame - 1) / 2) * 4 + 15) & ~(size_t)15;
+  const size_t per_warp = group_warp_doubles(frame) * 8;
+  int dev = 0, sms = 152, per_sm = 0, smem_max = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (frame > 255 || ptab_bytes + per_warp > (size_t)smem_max)
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "a grouped conditioning set of " + std::to_string(G.vmax) + " points with " +
+                    std::to_string(nr) + " data rows exceeds the CUDA path's shared-memory frame");
+  const int wpb = (int)std::max<size_t>(
+      1, std::min<size_t>(4, (std::min<size_t>(smem_max, 200 * 1024) - ptab_bytes) / per_warp));
+  const size_t smem = ptab_bytes + wpb * per_warp;
   DevBuf dmod, terms, partial, out, cstat;
   GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
   GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
-  GS_TRY(terms.alloc((size_t)ncand * G.nblocks * 8, s));
+  const int64_t rows = ncand * per;
+  GS_TRY(terms.alloc((size_t)rows * G.nblocks * 8, s));
   GS_TRY(cstat.alloc((size_t)ncand * 4, s));
   GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
   VArgs a{};
@@ -1447,16 +1528,10 @@ int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model
   a.mean = P->mean;
   a.models = (const DevModel*)dmod.ptr;
   a.terms = (double*)terms.ptr;
-  GroupArgs g{G.d_off, G.d_vid, G.d_slen, G.nblocks, G.vmax};
-  const size_t ptab_bytes = (((size_t)G.vmax * (G.vmax - 1) / 2) * 4 + 15) & ~(size_t)15;
-  const size_t per_warp = group_warp_doubles(G.vmax) * 8;
-  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024 - ptab_bytes) / per_warp));
-  const size_t smem = ptab_bytes + wpb * per_warp;
-  auto kern = dim == 2 ? vecchia_group_kernel<2> : vecchia_group_kernel<3>;
+  GroupArgs g{G.d_off, G.d_vid, G.d_slen, G.nblocks, frame, nr, d_basis, clamp ? 1 : 0};
+  auto kern = reml ? (dim == 2 ? vecchia_group_kernel<2, true> : vecchia_group_kernel<3, true>)
+                   : (dim == 2 ? vecchia_group_kernel<2, false> : vecchia_group_kernel<3, false>);
   GS_TRY(allow_dynamic_smem((const void*)kern, smem));
-  int dev = 0, sms = 152, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * wpb, smem));
   const int64_t items = ncand * G.nblocks;
   const int blocks = (int)std::max<int64_t>(
@@ -1465,17 +1540,22 @@ int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model
   GS_CUDA(cudaGetLastError());
   const int64_t chunk = 8192;
   const int nblk = (int)((G.nblocks + chunk - 1) / chunk);
-  GS_TRY(partial.alloc((size_t)nblk * ncand * 8, s));
-  GS_TRY(out.alloc((size_t)ncand * 8, s));
-  reduce_terms<<<dim3(nblk, (unsigned)ncand), 256, 0, s>>>((double*)terms.ptr, G.nblocks, chunk,
-                                                          (double*)partial.ptr);
-  reduce_partials<<<(int)((ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)ncand,
-                                                             (double*)out.ptr);
+  GS_TRY(partial.alloc((size_t)nblk * rows * 8, s));
+  GS_TRY(out.alloc((size_t)rows * 8, s));
+  int launches = 1;
+  for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
+    const int64_t nr_ = std::min<int64_t>(65535, rows - r0);
+    reduce_terms<<<dim3(nblk, (unsigned)nr_), 256, 0, s>>>(
+        (double*)terms.ptr + r0 * G.nblocks, G.nblocks, chunk, (double*)partial.ptr + r0 * nblk);
+    ++launches;
+  }
+  reduce_partials<<<(int)((rows + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)rows,
+                                                            (double*)out.ptr);
   GS_CUDA(cudaGetLastError());
-  count_launch(3);
-  std::vector<double> hll(ncand);
+  count_launch(launches + 1);
+  std::vector<double> hout(rows);
   std::vector<int32_t> hst(ncand);
-  GS_CUDA(cudaMemcpyAsync(hll.data(), out.ptr, ncand * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(hout.data(), out.ptr, rows * 8, cudaMemcpyDeviceToHost, s));
   GS_CUDA(cudaMemcpyAsync(hst.data(), cstat.ptr, ncand * 4, cudaMemcpyDeviceToHost, s));
   GS_CUDA(cudaStreamSynchronize(s));
   for (int64_t c = 0; c < ncand; ++c) {
@@ -1484,7 +1564,90 @@ int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model
       status[c] = hst[c];
       continue;
     }
-    ll[c] = hll[c];
+    for (int w = 0; w < per; ++w) sums[c * per + w] = hout[c * per + w];
+  }
+  return GS_OK;
+}
+
+int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
+                         int64_t gsize, double* ll, int32_t* status, cudaStream_t s) {
+  if (gsize <= 1) return vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s);
+  gs_vecchia_plan::Groups G;
+  GS_TRY(plan_groups(P, gsize, &G));
+  std::vector<double> sums;
+  std::vector<int> valid;
+  GS_TRY(eval_blocks(P, ncand, models, G, 1, nullptr, false, sums, status, valid, s));
+  for (int64_t c = 0; c < ncand; ++c) ll[c] = (valid[c] && status[c] == 0) ? sums[c] : NAN;
+  return GS_OK;
+}
+
+// The GLS step of reml_loglik_with_plan (vecchia.rs:1347-1356): A = F'S^-1F
+// and c = F'S^-1z from the sums, LU with partial pivoting (lu_factor's
+// pivot test: the largest candidate below 1e-12 max|A| is singular), then
+//     ll = -1/2 ((n - p) ln 2 pi + ln det S + ln |det A| + z'S^-1z - c'beta).
+int gls_finish(int64_t n, int p, const double* sums, double* ll) {
+  std::vector<double> A((size_t)p * p), c(p);
+  int w = 2 + p;
+  for (int f = 0; f < p; ++f) {
+    c[f] = sums[2 + f];
+    for (int g = f; g < p; ++g, ++w) A[(size_t)f * p + g] = A[(size_t)g * p + f] = sums[w];
+  }
+  double scale = 2.2250738585072014e-308;
+  for (double v : A) scale = std::fmax(scale, std::fabs(v));
+  std::vector<int> piv(p);
+  for (int k = 0; k < p; ++k) {
+    int best = k;
+    double mx = std::fabs(A[(size_t)k * p + k]);
+    for (int i = k + 1; i < p; ++i)
+      if (std::fabs(A[(size_t)i * p + k]) > mx) {
+        mx = std::fabs(A[(size_t)i * p + k]);
+        best = i;
+      }
+    if (!(mx >= 1e-12 * scale)) return GS_ERR_SINGULAR_SYSTEM;
+    piv[k] = best;
+    if (best != k)
+      for (int j = 0; j < p; ++j) std::swap(A[(size_t)k * p + j], A[(size_t)best * p + j]);
+    for (int i = k + 1; i < p; ++i) {
+      const double f = A[(size_t)i * p + k] / A[(size_t)k * p + k];
+      A[(size_t)i * p + k] = f;
+      if (f != 0.0)
+        for (int j = k + 1; j < p; ++j) A[(size_t)i * p + j] -= f * A[(size_t)k * p + j];
+    }
+  }
+  std::vector<double> beta = c;
+  for (int k = 0; k < p; ++k) std::swap(beta[k], beta[piv[k]]);
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < i; ++j) beta[i] -= A[(size_t)i * p + j] * beta[j];
+  for (int i = p - 1; i >= 0; --i) {
+    for (int j = i + 1; j < p; ++j) beta[i] -= A[(size_t)i * p + j] * beta[j];
+    beta[i] /= A[(size_t)i * p + i];
+  }
+  double ln_det_a = 0.0, cb = 0.0;
+  for (int i = 0; i < p; ++i) {
+    ln_det_a += std::log(std::fabs(A[(size_t)i * p + i]));
+    cb += c[i] * beta[i];
+  }
+  *ll = -0.5 * ((double)(n - p) * kLn2Pi + sums[0] + ln_det_a + (sums[1] - cb));
+  return GS_OK;
+}
+
+// Vecchia REML log-likelihoods of ncand candidates with the trend basis
+// d_basis (p x n on the device, column-major): reml_loglik_with_plan
+// (gsize <= 1, as singleton blocks) or reml_loglik_with_blocks.
+int vecchia_eval_reml(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
+                      int64_t gsize, const double* d_basis, int p, double* ll, int32_t* status,
+                      cudaStream_t s) {
+  gs_vecchia_plan::Groups G;
+  GS_TRY(plan_groups(P, std::max<int64_t>(gsize, 1), &G));
+  std::vector<double> sums;
+  std::vector<int> valid;
+  GS_TRY(eval_blocks(P, ncand, models, G, 1 + p, d_basis, gsize <= 1, sums, status, valid, s));
+  const int per = reml_sums(p);
+  for (int64_t c = 0; c < ncand; ++c) {
+    ll[c] = NAN;
+    if (!valid[c] || status[c] != 0) continue;
+    const int rc = gls_finish(P->n, p, &sums[(size_t)c * per], &ll[c]);
+    if (rc) status[c] = rc;
   }
   return GS_OK;
 }
@@ -2440,6 +2603,186 @@ int finish_fit(int32_t kind, const std::pair<std::vector<double>, double>& best,
   return GS_OK;
 }
 
+// Nelder-Mead multistart (optim.rs:106-123) with every start's simplex
+// advanced in lock step: each round's pending points of all starts are one
+// batch of `objective` (xs -> f).
+template <class Obj>
+int nm_lockstep(const std::vector<std::vector<double>>& starts, double step, int64_t max_iter,
+                Obj objective, std::pair<std::vector<double>, double>* best, int64_t* n_evals) {
+  std::vector<NelderMead> runs;
+  for (const auto& x0 : starts) runs.emplace_back(x0, step, max_iter);
+  int64_t evals = 0;
+  for (int guard = 0; guard < 1000000; ++guard) {
+    std::vector<std::vector<double>> xs;
+    std::vector<size_t> owner;
+    for (size_t r = 0; r < runs.size(); ++r) {
+      if (runs[r].done()) continue;
+      for (const auto& x : runs[r].pending()) {
+        xs.push_back(x);
+        owner.push_back(r);
+      }
+    }
+    if (xs.empty()) break;
+    std::vector<double> fv;
+    GS_TRY(objective(xs, fv));
+    evals += (int64_t)xs.size();
+    std::vector<std::vector<double>> fvals(runs.size());
+    for (size_t b = 0; b < xs.size(); ++b) fvals[owner[b]].push_back(fv[b]);
+    for (size_t r = 0; r < runs.size(); ++r)
+      if (!fvals[r].empty()) runs[r].supply(fvals[r]);
+  }
+  if (n_evals) *n_evals = evals;
+  *best = multistart_best(runs);
+  return GS_OK;
+}
+
+// The reference's three starts (vecchia.rs:1018-1023, 1636-1640).
+std::vector<std::vector<double>> reference_starts(const FitSetup& fs) {
+  const double lr0 = std::log(fs.range0);
+  std::vector<std::vector<double>> st;
+  for (double f : {0.3, 1.0, 3.0})
+    st.push_back({std::sqrt(0.1 * fs.var0), std::log(0.9 * fs.var0), lr0 + std::log(f)});
+  return st;
+}
+
+// -loglik + 1e6 reg(range), 1e12 for a rejected candidate, from a batch of
+// log-likelihoods and statuses.
+void to_objective(int32_t kind, double range_max, const std::vector<std::vector<double>>& xs,
+                  const std::vector<double>& ll, const std::vector<int32_t>& st,
+                  std::vector<double>& f) {
+  f.resize(xs.size());
+  for (size_t b = 0; b < xs.size(); ++b)
+    f[b] = (st[b] == 0 && std::isfinite(ll[b]))
+               ? -ll[b] + 1e6 * range_reg(std::exp(xs[b][2]), range_max)
+               : 1e12;
+}
+
+// poly_basis (vecchia.rs:1181-1233): monomials of total degree <= degree
+// (the first dimension's exponent varying slowest) of the coordinates
+// centred and divided by their standard deviation (floored at 1e-12);
+// column-major p x n.
+std::vector<double> poly_basis_host(const gs_pointset* ps, int degree, int* p_out) {
+  const int64_t n = ps->n;
+  const int dim = ps->dim;
+  double mean[3] = {0, 0, 0}, scale[3] = {1, 1, 1};
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < dim; ++d) mean[d] += ps->host[i * dim + d] / (double)n;
+  for (int d = 0; d < dim; ++d) {
+    double var = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      const double t = ps->host[i * dim + d] - mean[d];
+      var += t * t;
+    }
+    scale[d] = std::fmax(std::sqrt(var / (double)n), 1e-12);
+  }
+  std::vector<std::array<int, 3>> exps;
+  std::array<int, 3> cur{0, 0, 0};
+  std::function<void(int, int)> rec = [&](int d, int rem) {
+    if (d == dim) {
+      exps.push_back(cur);
+      return;
+    }
+    for (int e = 0; e <= rem; ++e) {
+      cur[d] = e;
+      rec(d + 1, rem - e);
+    }
+    cur[d] = 0;
+  };
+  rec(0, degree);
+  const int p = (int)exps.size();
+  std::vector<double> f((size_t)p * n);
+  for (int64_t i = 0; i < n; ++i) {
+    double cs[3];
+    for (int d = 0; d < dim; ++d) cs[d] = (ps->host[i * dim + d] - mean[d]) / scale[d];
+    for (int col = 0; col < p; ++col) {
+      double v = 1.0;
+      for (int d = 0; d < dim; ++d)
+        for (int e = 0; e < exps[col][d]; ++e) v *= cs[d];
+      f[(size_t)col * n + i] = v;
+    }
+  }
+  *p_out = p;
+  return f;
+}
+
+// standardized_drift_basis (vecchia.rs:1246-1272): an intercept, then each
+// covariate centred and divided by its standard deviation (floored at
+// 1e-12); column-major (1 + ncov) x n.
+std::vector<double> drift_basis_host(const double* drift, int64_t n, int64_t ncov) {
+  std::vector<double> f((size_t)(ncov + 1) * n);
+  for (int64_t i = 0; i < n; ++i) f[i] = 1.0;
+  for (int64_t k = 0; k < ncov; ++k) {
+    double mean = 0.0, var = 0.0;
+    for (int64_t i = 0; i < n; ++i) mean += drift[i * ncov + k] / (double)n;
+    for (int64_t i = 0; i < n; ++i) {
+      const double t = drift[i * ncov + k] - mean;
+      var += t * t;
+    }
+    const double sd = std::fmax(std::sqrt(var / (double)n), 1e-12);
+    for (int64_t i = 0; i < n; ++i) f[(size_t)(k + 1) * n + i] = (drift[i * ncov + k] - mean) / sd;
+  }
+  return f;
+}
+
+// The trend basis of vecchia_reml (drift == null: poly_basis of degree) or
+// vecchia_reml_drift, with the reference's checks (vecchia.rs:1508-1526).
+int make_basis(const gs_pointset* ps, int32_t degree, const double* drift, int64_t n_rows,
+               int64_t ncov, std::vector<double>* basis, int* p) {
+  if (drift) {
+    if (n_rows != ps->n)
+      return fail(GS_ERR_DIMENSION_MISMATCH, std::to_string(n_rows) + " drift rows vs " +
+                                                 std::to_string(ps->n) + " data points");
+    if (ncov <= 0)
+      return fail(GS_ERR_INVALID_PARAMETER, "external-drift REML needs at least one covariate column");
+    *basis = drift_basis_host(drift, ps->n, ncov);
+    *p = (int)(ncov + 1);
+  } else {
+    if (degree < 0 || degree > 255) return fail(GS_ERR_INVALID_PARAMETER, "drift degree out of range");
+    *basis = poly_basis_host(ps, degree, p);
+  }
+  return GS_OK;
+}
+
+// reml_fit_with_basis (vecchia.rs:1572-1644) and the grouped path of
+// mle_fit_with_plan (vecchia.rs:983, 1001-1016, 1063-1064): Nelder-Mead
+// from the reference's three starts, step 0.3, 2000 iterations.
+int fit_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order, int64_t gsize,
+           const std::vector<double>* basis, int p, gs_model* out_model, double* out_loglik,
+           double* out_x, int64_t* n_evals) {
+  gs_vecchia_plan* P = nullptr;
+  GS_TRY(plan_create(ps, m, order, &P));
+  std::unique_ptr<gs_vecchia_plan> own(P);
+  if (basis && ps->n <= p + 1)
+    return fail(GS_ERR_INSUFFICIENT_DATA, "REML with " + std::to_string(p) +
+                                              " trend terms needs more than " +
+                                              std::to_string(p + 1) + " points");
+  const FitSetup fs = fit_setup(ps, P->mean);
+  DevBuf dbasis;
+  if (basis) {
+    GS_TRY(dbasis.alloc(basis->size() * 8, P->stream));
+    GS_CUDA(cudaMemcpyAsync(dbasis.ptr, basis->data(), basis->size() * 8, cudaMemcpyHostToDevice,
+                            P->stream));
+  }
+  auto objective = [&](const std::vector<std::vector<double>>& xs,
+                       std::vector<double>& f) -> int {
+    std::vector<gs_model> batch;
+    for (const auto& x : xs) batch.push_back(model_from_x(kind, x));
+    std::vector<double> ll(batch.size());
+    std::vector<int32_t> st(batch.size());
+    if (basis)
+      GS_TRY(vecchia_eval_reml(P, (int64_t)batch.size(), batch.data(), gsize,
+                               (const double*)dbasis.ptr, p, ll.data(), st.data(), P->stream));
+    else
+      GS_TRY(vecchia_eval_grouped(P, (int64_t)batch.size(), batch.data(), gsize, ll.data(),
+                                  st.data(), P->stream));
+    to_objective(kind, fs.range_max, xs, ll, st, f);
+    return GS_OK;
+  };
+  std::pair<std::vector<double>, double> best;
+  GS_TRY(nm_lockstep(reference_starts(fs), 0.3, 2000, objective, &best, n_evals));
+  return finish_fit(kind, best, out_model, out_loglik, out_x);
+}
+
 }  // namespace
 }  // namespace gs
 
@@ -2545,6 +2888,65 @@ int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int6
   if (rc) return rc;
   if (n_evals) *n_evals = evals;
   return finish_fit(kind, multistart_best(runs), out_model, out_loglik, out_x);
+}
+
+// vecchia_mle_grouped (vecchia.rs:939-950): group_size <= 1 is vecchia_mle.
+int gs_vecchia_mle_grouped(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                           int64_t group_size, gs_model* out_model, double* out_loglik,
+                           double* out_x, int64_t* n_evals) {
+  if (group_size <= 1)
+    return gs_vecchia_mle(ps, kind, m, order, out_model, out_loglik, out_x, n_evals);
+  GS_TRY(check_fit_kind(ps, kind));
+  return fit_nm(ps, kind, m, order, group_size, nullptr, 0, out_model, out_loglik, out_x, n_evals);
+}
+
+// vecchia_reml / vecchia_reml_grouped (vecchia.rs:1460-1493).
+int gs_vecchia_reml(const gs_pointset* ps, int32_t kind, int64_t m, int32_t drift_degree,
+                    const int64_t* order, int64_t group_size, gs_model* out_model,
+                    double* out_loglik, double* out_x, int64_t* n_evals) {
+  GS_TRY(check_fit_kind(ps, kind));
+  std::vector<double> basis;
+  int p = 0;
+  GS_TRY(make_basis(ps, drift_degree, nullptr, 0, 0, &basis, &p));
+  return fit_nm(ps, kind, m, order, group_size, &basis, p, out_model, out_loglik, out_x, n_evals);
+}
+
+// vecchia_reml_drift / vecchia_reml_drift_grouped (vecchia.rs:1500-1568):
+// drift is n_rows x ncov, row-major.
+int gs_vecchia_reml_drift(const gs_pointset* ps, int32_t kind, int64_t m, const double* drift,
+                          int64_t n_rows, int64_t ncov, const int64_t* order, int64_t group_size,
+                          gs_model* out_model, double* out_loglik, double* out_x,
+                          int64_t* n_evals) {
+  GS_TRY(check_fit_kind(ps, kind));
+  if (!drift && n_rows > 0 && ncov > 0) return fail(GS_ERR_INVALID_PARAMETER, "null drift");
+  std::vector<double> basis;
+  int p = 0;
+  static const double kNone = 0.0;
+  GS_TRY(make_basis(ps, 0, drift ? drift : &kNone, n_rows, ncov, &basis, &p));
+  return fit_nm(ps, kind, m, order, group_size, &basis, p, out_model, out_loglik, out_x, n_evals);
+}
+
+// REML log-likelihoods of ncand candidates on a plan (reml_loglik_with_plan
+// for group_size <= 1, reml_loglik_with_blocks otherwise) with the trend
+// basis of vecchia_reml (drift null: polynomial of drift_degree) or of
+// vecchia_reml_drift (drift: n x ncov covariates, row-major).
+int gs_vecchia_reml_loglik_batch(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
+                                 int32_t drift_degree, const double* drift, int64_t ncov,
+                                 int64_t group_size, double* loglik, int32_t* status,
+                                 void* stream) {
+  if (!P) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
+  if (ncand < 0) return fail(GS_ERR_INVALID_PARAMETER, "negative candidate count");
+  if (ncand > 0 && (!models || !loglik || !status))
+    return fail(GS_ERR_INVALID_PARAMETER, "null model or output buffer");
+  cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
+  std::vector<double> basis;
+  int p = 0;
+  GS_TRY(make_basis(P->ps, drift_degree, drift, drift ? P->n : 0, ncov, &basis, &p));
+  DevBuf dbasis;
+  GS_TRY(dbasis.alloc(basis.size() * 8, s));
+  GS_CUDA(cudaMemcpyAsync(dbasis.ptr, basis.data(), basis.size() * 8, cudaMemcpyHostToDevice, s));
+  return vecchia_eval_reml(P, ncand, models, group_size, (const double*)dbasis.ptr, p, loglik,
+                           status, s);
 }
 
 int gs_vecchia_loglik_grad_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs_model* models,

@@ -16,7 +16,8 @@ from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Ser
                   tune_kriging_neighbors,
                   nelder_mead_multistart, rff_field, rng_normal, rng_uniform, seq_mean,
                   vecchia_krige, vecchia_loglik, vecchia_loglik_grouped, vecchia_mle, vecchia_mle_fit,
-                  vecchia_mle_nm_fit, vecchia_predict)
+                  vecchia_mle_grouped_fit, vecchia_mle_nm_fit, vecchia_predict, vecchia_reml,
+                  vecchia_reml_drift, vecchia_reml_drift_fit, vecchia_reml_fit)
 from ._abi import LIB_PATH, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -100,6 +100,12 @@ SIGNATURES = {
     "gs_vecchia_mle": (_int, [_vp, _i32, _i64, _pi64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_mle_nm": (_int, [_vp, _i32, _i64, _pi64, _i64, _pd, _d, _i64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_loglik_grad_batch": (_int, [_vp, _i64, _pm, _pd, _pd, _pi32, _int, _vp]),
+    "gs_vecchia_reml_loglik_batch": (_int, [_vp, _i64, _pm, _i32, _pd, _i64, _i64, _pd, _pi32,
+                                            _vp]),
+    "gs_vecchia_mle_grouped": (_int, [_vp, _i32, _i64, _pi64, _i64, _pm, _pd, _pd, _pi64]),
+    "gs_vecchia_reml": (_int, [_vp, _i32, _i64, _i32, _pi64, _i64, _pm, _pd, _pd, _pi64]),
+    "gs_vecchia_reml_drift": (_int, [_vp, _i32, _i64, _pd, _i64, _i64, _pi64, _i64, _pm, _pd, _pd,
+                                     _pi64]),
     "gs_vecchia_predict": (_int, [_vp, _pm, _i64, _pd, _pd, _pd, _i64, _pd, _pd]),
     "gs_nelder_mead_multistart": (_int, [OBJECTIVE, _vp, _i64, _i64, _pd, _d, _i64, _pd, _pd]),
     "gs_rng_uniform": (None, [_u64, _i64, _pd]),

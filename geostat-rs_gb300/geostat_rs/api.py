@@ -595,6 +595,21 @@ class VecchiaPlan:
                                                                _p(st, C.c_int32), None))
         return ll, st
 
+    def reml_loglik(self, models: Sequence[VariogramModel], drift_degree: int = 1, drift=None,
+                    group_size: int = 1):
+        """Vecchia REML log-likelihood (vecchia.rs:1278-1457) of each
+        candidate: the mean a GLS trend over a polynomial basis of
+        ``drift_degree`` or, with ``drift`` (n x ncov covariates), the
+        intercept plus standardised covariates.  Returns ``(loglik, status)``."""
+        arr = (_abi.Model * len(models))(*[model_struct(m) for m in models])
+        ll = np.empty(len(models))
+        st = np.empty(len(models), dtype=np.int32)
+        d = None if drift is None else _f64(drift).reshape(self.data.n, -1)
+        _abi.check(_abi.load().gs_vecchia_reml_loglik_batch(
+            self._h, len(models), arr, int(drift_degree), _p(d),
+            0 if d is None else d.shape[1], int(group_size), _p(ll), _p(st, C.c_int32), None))
+        return ll, st
+
     def close(self):
         if getattr(self, "_h", None):
             _abi.load().gs_vecchia_plan_destroy(self._h)
@@ -675,6 +690,73 @@ def vecchia_mle_nm_fit(data: PointSet, kind="exponential", m=20, starts=None, ns
                                              C.byref(ll), _p(x), C.byref(ne)))
     model = VariogramModel(out.nugget, [Structure(kname, out.s[0].sill, out.s[0].range)])
     return model, ll.value, x, ne.value
+
+
+def _fit_result(kname, out, ll, x, ne):
+    model = VariogramModel(out.nugget, [Structure(kname, out.s[0].sill, out.s[0].range)])
+    return model, ll.value, x, ne.value
+
+
+def vecchia_mle_grouped_fit(data: PointSet, kind="exponential", m=20, order=None,
+                            group_size: int = 1):
+    """``vecchia_mle_grouped`` (vecchia.rs:939-950); returns
+    ``(model, loglik, x, n_evals)``."""
+    kname = _fit_kind(kind)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    out, ll, x, ne = _abi.Model(), C.c_double(), np.zeros(3), C.c_int64()
+    _abi.check(_abi.load().gs_vecchia_mle_grouped(data._h, KIND_CODES[kname], int(m),
+                                                  _p(o, C.c_int64), int(group_size), C.byref(out),
+                                                  C.byref(ll), _p(x), C.byref(ne)))
+    return _fit_result(kname, out, ll, x, ne)
+
+
+def vecchia_reml_fit(data: PointSet, kind="exponential", m=20, drift_degree: int = 1, order=None,
+                     group_size: int = 1):
+    """``vecchia_reml`` / ``vecchia_reml_grouped`` (vecchia.rs:1460-1493);
+    returns ``(model, loglik, x, n_evals)``."""
+    kname = _fit_kind(kind)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    out, ll, x, ne = _abi.Model(), C.c_double(), np.zeros(3), C.c_int64()
+    _abi.check(_abi.load().gs_vecchia_reml(data._h, KIND_CODES[kname], int(m), int(drift_degree),
+                                           _p(o, C.c_int64), int(group_size), C.byref(out),
+                                           C.byref(ll), _p(x), C.byref(ne)))
+    return _fit_result(kname, out, ll, x, ne)
+
+
+def vecchia_reml_drift_fit(data: PointSet, drift, kind="exponential", m=20, order=None,
+                           group_size: int = 1):
+    """``vecchia_reml_drift`` / ``vecchia_reml_drift_grouped``
+    (vecchia.rs:1500-1568), ``drift`` one row of covariates per point;
+    returns ``(model, loglik, x, n_evals)``."""
+    kname = _fit_kind(kind)
+    rows = [list(r) for r in drift] if not isinstance(drift, np.ndarray) else None
+    if rows is not None:
+        ncov = len(rows[0]) if rows else 0
+        if any(len(r) != ncov for r in rows):
+            raise DimensionMismatch("all drift rows must have the same number of covariates")
+        d = np.array(rows, dtype=np.float64).reshape(len(rows), ncov)
+    else:
+        d = drift.reshape(len(drift), -1) if drift.ndim == 1 else drift
+    d = _f64(d)
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    out, ll, x, ne = _abi.Model(), C.c_double(), np.zeros(3), C.c_int64()
+    _abi.check(_abi.load().gs_vecchia_reml_drift(data._h, KIND_CODES[kname], int(m), _p(d),
+                                                 d.shape[0], d.shape[1] if d.ndim == 2 else 0,
+                                                 _p(o, C.c_int64), int(group_size), C.byref(out),
+                                                 C.byref(ll), _p(x), C.byref(ne)))
+    return _fit_result(kname, out, ll, x, ne)
+
+
+def vecchia_reml(x, y, values, kind="exponential", m=20, drift_degree=1):
+    """lib.rs:370-392 ``vecchia_reml``."""
+    data = PointSet.from_xyz(x, y, values)
+    return vecchia_reml_fit(data, kind, m, drift_degree)[0]
+
+
+def vecchia_reml_drift(x, y, values, covariates, kind="exponential", m=20):
+    """lib.rs:394-417 ``vecchia_reml_drift``."""
+    data = PointSet.from_xyz(x, y, values)
+    return vecchia_reml_drift_fit(data, covariates, kind, m)[0]
 
 
 def vecchia_mle(x, y, values, kind="exponential", m=20):

@@ -249,10 +249,22 @@ int gs_vecchia_loglik_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs
  * (guinness_blocks, vecchia.rs:570-602) conditioned jointly on the union of
  * their predecessor sets, one FP64 factorisation per block and candidate.
  * group_size <= 1 is gs_vecchia_loglik_batch.  The blocks of a group size
- * are built once per plan.  Joint sets beyond 254 points: InvalidParameter. */
+ * are built once per plan.  A joint set too large for one shared-memory
+ * frame (about 190 points with its data rows): InvalidParameter. */
 int gs_vecchia_loglik_grouped_batch(const gs_vecchia_plan* plan, int64_t ncand,
                                     const gs_model* models, int64_t group_size, double* loglik,
                                     int32_t* status, void* stream);
+/* Vecchia REML log-likelihood (reml_loglik_with_plan, vecchia.rs:1278-1357,
+ * for group_size <= 1; reml_loglik_with_blocks, vecchia.rs:1366-1457,
+ * otherwise) for ncand candidates: the mean is a GLS trend over the basis of
+ * vecchia_reml (drift NULL: poly_basis of drift_degree, vecchia.rs:1199-1233)
+ * or of vecchia_reml_drift (drift: plan's n x ncov covariates, row-major;
+ * standardized_drift_basis, vecchia.rs:1246-1272).  Per-block FP64 sums on
+ * the device; the p x p GLS solve on the host. */
+int gs_vecchia_reml_loglik_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs_model* models,
+                                 int32_t drift_degree, const double* drift, int64_t ncov,
+                                 int64_t group_size, double* loglik, int32_t* status,
+                                 void* stream);
 /* vecchia_loglik (vecchia.rs:874-884). */
 int gs_vecchia_loglik(const gs_pointset* ps, const gs_model* model, int64_t m,
                       const int64_t* order, double* loglik);
@@ -282,6 +294,26 @@ int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t
 int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
                       int64_t nstarts, const double* starts, double step, int64_t max_iter,
                       gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals);
+/* vecchia_mle_grouped (vecchia.rs:939-950): group_size <= 1 is
+ * gs_vecchia_mle; otherwise Nelder-Mead (step 0.3, 2000 iterations) from
+ * the reference's three starts over the grouped likelihood, each round's
+ * simplex points batched into one launch. */
+int gs_vecchia_mle_grouped(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
+                           int64_t group_size, gs_model* out_model, double* out_loglik,
+                           double* out_x, int64_t* n_evals);
+/* vecchia_reml / vecchia_reml_grouped (vecchia.rs:1460-1493,
+ * reml_fit_with_basis 1572-1644): polynomial trend of drift_degree.
+ * InsufficientData when n <= p + 1. */
+int gs_vecchia_reml(const gs_pointset* ps, int32_t kind, int64_t m, int32_t drift_degree,
+                    const int64_t* order, int64_t group_size, gs_model* out_model,
+                    double* out_loglik, double* out_x, int64_t* n_evals);
+/* vecchia_reml_drift / vecchia_reml_drift_grouped (vecchia.rs:1500-1568):
+ * drift is n_rows x ncov, row-major; n_rows != n: DimensionMismatch, ncov
+ * == 0: InvalidParameter. */
+int gs_vecchia_reml_drift(const gs_pointset* ps, int32_t kind, int64_t m, const double* drift,
+                          int64_t n_rows, int64_t ncov, const int64_t* order, int64_t group_size,
+                          gs_model* out_model, double* out_loglik, double* out_x,
+                          int64_t* n_evals);
 /* vecchia_predict (vecchia.rs:748-866): level-scheduled on the device. */
 int gs_vecchia_predict(const gs_pointset* ps, const gs_model* model, int64_t nt,
                        const double* tx, const double* ty, const double* tz, int64_t m,

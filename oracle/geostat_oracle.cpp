@@ -1338,6 +1338,217 @@ int loglik_with_blocks(const double* coords, const double* values, size_t n, int
   return OR_OK;
 }
 
+// vecchia.rs:1181-1196 monomials: exponent tuples of total degree <= degree,
+// the first dimension's exponent varying slowest.
+void monomials(int d, int dim, int rem, int* cur, std::vector<std::array<int, 3>>& out) {
+  if (d == dim) {
+    out.push_back({cur[0], cur[1], cur[2]});
+    return;
+  }
+  for (int e = 0; e <= rem; ++e) {
+    cur[d] = e;
+    monomials(d + 1, dim, rem - e, cur, out);
+  }
+  cur[d] = 0;
+}
+
+// vecchia.rs:1199-1233 poly_basis: monomials of the centred, scaled
+// coordinates (row-major n x p).
+std::vector<double> poly_basis(const double* coords, size_t n, int dim, int degree, size_t* p_out) {
+  double mean[3] = {0, 0, 0}, scale[3] = {1, 1, 1};
+  for (size_t i = 0; i < n; ++i)
+    for (int d = 0; d < dim; ++d) mean[d] += coords[i * dim + d] / (double)n;
+  for (int d = 0; d < dim; ++d) {
+    double var = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      double t = coords[i * dim + d] - mean[d];
+      var += t * t;
+    }
+    var /= (double)n;
+    scale[d] = fmax_(std::sqrt(var), 1e-12);
+  }
+  std::vector<std::array<int, 3>> exps;
+  int cur[3] = {0, 0, 0};
+  monomials(0, dim, degree, cur, exps);
+  const size_t p = exps.size();
+  std::vector<double> f(n * p);
+  for (size_t i = 0; i < n; ++i) {
+    double cs[3];
+    for (int d = 0; d < dim; ++d) cs[d] = (coords[i * dim + d] - mean[d]) / scale[d];
+    for (size_t c = 0; c < p; ++c) {
+      double v = 1.0;
+      for (int d = 0; d < dim; ++d)
+        for (int e = 0; e < exps[c][d]; ++e) v *= cs[d];
+      f[i * p + c] = v;
+    }
+  }
+  *p_out = p;
+  return f;
+}
+
+// vecchia.rs:1246-1272 standardized_drift_basis: intercept, then each
+// covariate centred and divided by its standard deviation (floored at 1e-12).
+std::vector<double> drift_basis(const double* drift, size_t n, size_t ncov) {
+  std::vector<double> mean(ncov, 0.0), scale(ncov, 1.0);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t k = 0; k < ncov; ++k) mean[k] += drift[i * ncov + k] / (double)n;
+  for (size_t k = 0; k < ncov; ++k) {
+    double var = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      double t = drift[i * ncov + k] - mean[k];
+      var += t * t;
+    }
+    scale[k] = fmax_(std::sqrt(var / (double)n), 1e-12);
+  }
+  const size_t p = ncov + 1;
+  std::vector<double> f(n * p);
+  for (size_t i = 0; i < n; ++i) {
+    f[i * p] = 1.0;
+    for (size_t k = 0; k < ncov; ++k) f[i * p + 1 + k] = (drift[i * ncov + k] - mean[k]) / scale[k];
+  }
+  return f;
+}
+
+// vecchia.rs:1347-1356 (and 1447-1456): the GLS step on the accumulated
+// whitened sums and the restricted log-likelihood.
+int reml_finish(size_t n, size_t p, double logdet, double uz_uz, const std::vector<double>& a,
+                const std::vector<double>& c, double* out) {
+  Lu lu;
+  int rc = lu_factor(a, p, lu);
+  if (rc) return rc;
+  std::vector<double> beta = lu_solve(lu, c);
+  const double ln_det_a = lu_ln_det_abs(lu);
+  double cb = 0.0;
+  for (size_t i = 0; i < p; ++i) cb += c[i] * beta[i];
+  const double resid = uz_uz - cb;
+  const double nm = (double)(n - p);
+  *out = -0.5 * (nm * std::log(2.0 * kPi) + logdet + ln_det_a + resid);
+  return OR_OK;
+}
+
+// vecchia.rs:1278-1357 reml_loglik_with_plan: per ordered point the
+// whitened value and trend row from w = K_SS^-1 k_i (Cholesky), accumulated
+// into log det, z'z, F'z and F'F.
+int reml_loglik_with_plan(const double* coords, const double* values, size_t n, int dim,
+                          const or_model& model, const Plan& plan, const double* basis, size_t p,
+                          double* out) {
+  const double sill = total_sill(model);
+  double logdet = 0.0, uz_uz = 0.0;
+  std::vector<double> a(p * p, 0.0), c(p, 0.0), uf(p);
+  std::vector<double> kss, ki, w;
+  for (size_t k = 0; k < plan.order.size(); ++k) {
+    const size_t i = plan.order[k];
+    const std::vector<size_t>& nb = plan.nb[k];
+    double uz, d;
+    if (nb.empty()) {
+      const double sd = std::sqrt(sill);
+      for (size_t col = 0; col < p; ++col) uf[col] = basis[i * p + col] / sd;
+      uz = values[i] / sd;
+      d = sill;
+    } else {
+      const size_t s = nb.size();
+      kss.assign(s * s, 0.0);
+      ki.assign(s, 0.0);
+      for (size_t aa = 0; aa < s; ++aa) {
+        double h[3];
+        for (int dd = 0; dd < dim; ++dd) h[dd] = coords[i * dim + dd] - coords[nb[aa] * dim + dd];
+        ki[aa] = sill - gamma_dh(model, dim, h);
+        for (size_t bb = aa; bb < s; ++bb) {
+          for (int dd = 0; dd < dim; ++dd)
+            h[dd] = coords[nb[aa] * dim + dd] - coords[nb[bb] * dim + dd];
+          const double cv = sill - gamma_dh(model, dim, h);
+          kss[aa * s + bb] = cv;
+          kss[bb * s + aa] = cv;
+        }
+      }
+      w = ki;
+      int rc = cholesky_solve(kss.data(), s, w.data());
+      if (rc) return rc;
+      double red = 0.0;
+      for (size_t aa = 0; aa < s; ++aa) red += w[aa] * ki[aa];
+      d = fmax_(sill - red, 1e-12);
+      const double sd = std::sqrt(d);
+      double wz = 0.0;
+      for (size_t aa = 0; aa < s; ++aa) wz += w[aa] * values[nb[aa]];
+      uz = (values[i] - wz) / sd;
+      for (size_t col = 0; col < p; ++col) {
+        double wf = 0.0;
+        for (size_t aa = 0; aa < s; ++aa) wf += w[aa] * basis[nb[aa] * p + col];
+        uf[col] = (basis[i * p + col] - wf) / sd;
+      }
+    }
+    logdet += std::log(d);
+    uz_uz += uz * uz;
+    for (size_t aa = 0; aa < p; ++aa) {
+      c[aa] += uf[aa] * uz;
+      for (size_t bb = 0; bb < p; ++bb) a[aa * p + bb] += uf[aa] * uf[bb];
+    }
+  }
+  return reml_finish(n, p, logdet, uz_uz, a, c, out);
+}
+
+// vecchia.rs:1366-1457 reml_loglik_with_blocks: each block's joint
+// Cholesky factor whitens z and every basis column by forward solves.
+int reml_loglik_with_blocks(const double* coords, const double* values, size_t n, int dim,
+                            const or_model& model, const Plan& plan, const double* basis, size_t p,
+                            const std::vector<std::pair<size_t, size_t>>& blocks, double* out) {
+  const double sill = total_sill(model);
+  double logdet = 0.0, uz_uz = 0.0;
+  std::vector<double> a(p * p, 0.0), c(p, 0.0);
+  std::vector<size_t> v_ids;
+  std::vector<double> kvv, wz;
+  std::vector<std::vector<double>> wf(p);
+  for (const auto& blk : blocks) {
+    const size_t k0 = blk.first, k1 = blk.second;
+    auto in_block = [&](size_t j) {
+      for (size_t q = k0; q < k1; ++q)
+        if (plan.order[q] == j) return true;
+      return false;
+    };
+    v_ids.clear();
+    for (size_t k = k0; k < k1; ++k)
+      for (size_t j : plan.nb[k])
+        if (!in_block(j) && std::find(v_ids.begin(), v_ids.end(), j) == v_ids.end())
+          v_ids.push_back(j);
+    const size_t s_len = v_ids.size();
+    for (size_t k = k0; k < k1; ++k) v_ids.push_back(plan.order[k]);
+    const size_t vn = v_ids.size();
+    kvv.assign(vn * vn, 0.0);
+    for (size_t aa = 0; aa < vn; ++aa) {
+      kvv[aa * vn + aa] = sill;
+      for (size_t bb = aa + 1; bb < vn; ++bb) {
+        double h[3];
+        for (int d = 0; d < dim; ++d)
+          h[d] = coords[v_ids[aa] * dim + d] - coords[v_ids[bb] * dim + d];
+        const double cv = sill - gamma_dh(model, dim, h);
+        kvv[aa * vn + bb] = cv;
+        kvv[bb * vn + aa] = cv;
+      }
+    }
+    int rc = cholesky_factor(kvv.data(), vn);
+    if (rc) return rc;
+    wz.resize(vn);
+    for (size_t q = 0; q < vn; ++q) wz[q] = values[v_ids[q]];
+    cholesky_forward(kvv.data(), vn, wz.data());
+    for (size_t col = 0; col < p; ++col) {
+      wf[col].resize(vn);
+      for (size_t q = 0; q < vn; ++q) wf[col][q] = basis[v_ids[q] * p + col];
+      cholesky_forward(kvv.data(), vn, wf[col].data());
+    }
+    for (size_t t = s_len; t < vn; ++t) {
+      const double l_tt = kvv[t * vn + t];
+      const double uz = wz[t];
+      logdet += std::log(l_tt * l_tt);
+      uz_uz += uz * uz;
+      for (size_t aa = 0; aa < p; ++aa) {
+        c[aa] += wf[aa][t] * uz;
+        for (size_t bb = 0; bb < p; ++bb) a[aa * p + bb] += wf[aa][t] * wf[bb][t];
+      }
+    }
+  }
+  return reml_finish(n, p, logdet, uz_uz, a, c, out);
+}
+
 int reject_vecchia_model(const or_model& model, int dim) {
   int rc = validate_model(model);
   if (rc) return rc;
@@ -1597,6 +1808,36 @@ void mle_setup(const double* coords, const double* values, size_t n, int dim, do
     starts9[i * 3 + 1] = std::log(0.9 * var0);
     starts9[i * 3 + 2] = lr0 + std::log(fs[i]);
   }
+}
+
+// Objective of mle_fit_with_plan with blocks (vecchia.rs:983, 1001-1016) and
+// of reml_fit_with_basis (vecchia.rs:1609-1633): -loglik + 1e6 reg(range),
+// 1e12 for a rejected candidate.
+double fit_objective(const double* coords, const double* values, size_t n, int dim, int kind,
+                     const Plan& plan, double range_max, const double* x, const double* basis,
+                     size_t p, const std::vector<std::pair<size_t, size_t>>* blocks) {
+  or_model m{};
+  m.nugget = x[0] * x[0];
+  m.n_structures = 1;
+  m.s[0].kind = kind;
+  m.s[0].sill = std::exp(x[1]);
+  m.s[0].range = std::exp(x[2]);
+  const double range = m.s[0].range;
+  double reg = 0.0;
+  if (range > range_max) {
+    double t = (range - range_max) / range_max;
+    reg = t * t;
+  }
+  double ll = 0.0;
+  int rc;
+  if (basis)
+    rc = blocks ? reml_loglik_with_blocks(coords, values, n, dim, m, plan, basis, p, *blocks, &ll)
+                : reml_loglik_with_plan(coords, values, n, dim, m, plan, basis, p, &ll);
+  else
+    rc = blocks ? loglik_with_blocks(coords, values, n, dim, m, plan, *blocks, &ll)
+                : loglik_with_plan(coords, values, n, dim, m, plan, &ll, nullptr);
+  if (rc == OR_OK && std::isfinite(ll)) return -ll + 1e6 * reg;
+  return 1e12;
 }
 
 // vecchia.rs:353-389 g_and_dg: unit-sill variogram g(d) and dg/dd for the
@@ -2209,6 +2450,72 @@ int or_vecchia_mle_nm(int dim, int64_t n, const double* coords, const double* va
   return OR_OK;
 }
 
+int64_t or_poly_basis_terms(int dim, int32_t degree) {
+  std::vector<std::array<int, 3>> exps;
+  int cur[3] = {0, 0, 0};
+  monomials(0, dim, degree, cur, exps);
+  return (int64_t)exps.size();
+}
+
+int or_poly_basis(int dim, int64_t n, const double* coords, int32_t degree, double* out) {
+  size_t p = 0;
+  std::vector<double> f = poly_basis(coords, (size_t)n, dim, degree, &p);
+  std::copy(f.begin(), f.end(), out);
+  return OR_OK;
+}
+
+int or_drift_basis(int64_t n, int64_t ncov, const double* drift, double* out) {
+  std::vector<double> f = drift_basis(drift, (size_t)n, (size_t)ncov);
+  std::copy(f.begin(), f.end(), out);
+  return OR_OK;
+}
+
+// reml_loglik_with_plan / reml_loglik_with_blocks on a plan given as arrays
+// (group_size <= 1: ungrouped).
+int or_vecchia_reml_loglik(int dim, int64_t n, const double* coords, const double* values,
+                           const or_model* model, int64_t m, const int64_t* order,
+                           const int64_t* nb, const int32_t* nb_count, const double* basis,
+                           int64_t p, int64_t group_size, double* ll) {
+  int rc = reject_vecchia_model(*model, dim);
+  if (rc) return rc;
+  Plan plan;
+  plan_from_arrays((size_t)n, (size_t)m, order, nb, nb_count, plan);
+  if (group_size <= 1)
+    return reml_loglik_with_plan(coords, values, (size_t)n, dim, *model, plan, basis, (size_t)p, ll);
+  return reml_loglik_with_blocks(coords, values, (size_t)n, dim, *model, plan, basis, (size_t)p,
+                                 guinness_blocks(plan, (size_t)group_size), ll);
+}
+
+// Nelder-Mead multistart fits: basis null = mle_fit_with_plan's grouped
+// path (group_size > 1), else reml_fit_with_basis (vecchia.rs:1572-1644).
+int or_vecchia_fit_nm(int dim, int64_t n, const double* coords, const double* values, int32_t kind,
+                      int64_t m, const int64_t* order_in, const double* basis, int64_t p,
+                      int64_t group_size, int64_t nstarts, const double* starts, double step,
+                      int64_t max_iter, double* x_out, double* f_out, int64_t* n_evals) {
+  Plan plan;
+  int rc = vecchia_plan(coords, (size_t)n, dim, (size_t)m, order_in, plan);
+  if (rc) return rc;
+  if (basis && n <= p + 1)
+    return fail(OR_INSUFFICIENT_DATA, "REML needs more points than trend terms plus one");
+  double s9[9], range_max;
+  mle_setup(coords, values, (size_t)n, dim, s9, &range_max);
+  std::vector<std::pair<size_t, size_t>> blocks;
+  if (group_size > 1) blocks = guinness_blocks(plan, (size_t)group_size);
+  int64_t evals = 0;
+  auto f = [&](const std::vector<double>& x) {
+    ++evals;
+    return fit_objective(coords, values, (size_t)n, dim, kind, plan, range_max, x.data(), basis,
+                         (size_t)p, group_size > 1 ? &blocks : nullptr);
+  };
+  std::vector<std::vector<double>> st;
+  for (int64_t i = 0; i < nstarts; ++i) st.push_back({starts[i * 3], starts[i * 3 + 1], starts[i * 3 + 2]});
+  auto r = nelder_mead_multistart(f, st, step, (size_t)max_iter);
+  for (int i = 0; i < 3; ++i) x_out[i] = r.first[i];
+  *f_out = r.second;
+  if (n_evals) *n_evals = evals;
+  return OR_OK;
+}
+
 int or_g_and_dg(int32_t kind, double d, double* g, double* dg) {
   return g_and_dg(kind, d, g, dg) ? OR_OK : OR_INVALID_PARAMETER;
 }
@@ -2288,6 +2595,11 @@ void or_rng_uniform(uint64_t seed, int64_t count, double* out) {
 void or_rng_normal(uint64_t seed, int64_t count, double* out) {
   Rng r(seed);
   for (int64_t i = 0; i < count; ++i) out[i] = r.normal();
+}
+void or_rng_draw(uint64_t seed, int64_t n_uniform, int64_t n_normal, double* out) {
+  Rng r(seed);
+  for (int64_t i = 0; i < n_uniform; ++i) out[i] = r.uniform();
+  for (int64_t i = 0; i < n_normal; ++i) out[n_uniform + i] = r.normal();
 }
 void or_test_field_2d(int64_t n, uint64_t seed, double* coords, double* values) {
   test_field_2d((size_t)n, seed, coords, values);

@@ -156,6 +156,24 @@ int or_vecchia_mle_nm(int dim, int64_t n, const double* coords, const double* va
                       int64_t nstarts, const double* starts, double step, int64_t max_iter,
                       double* x_out, double* f_out, int64_t* n_evals);
 
+/* vecchia.rs:1181-1233 poly_basis (row-major n x p, p = or_poly_basis_terms)
+ * and vecchia.rs:1246-1272 standardized_drift_basis (n x (1 + ncov)). */
+int64_t or_poly_basis_terms(int dim, int32_t degree);
+int or_poly_basis(int dim, int64_t n, const double* coords, int32_t degree, double* out);
+int or_drift_basis(int64_t n, int64_t ncov, const double* drift, double* out);
+/* vecchia.rs:1278-1457 REML log-likelihood on a plan given as arrays, with a
+ * trend basis (row-major n x p); group_size <= 1 ungrouped. */
+int or_vecchia_reml_loglik(int dim, int64_t n, const double* coords, const double* values,
+                           const or_model* model, int64_t m, const int64_t* order,
+                           const int64_t* nb, const int32_t* nb_count, const double* basis,
+                           int64_t p, int64_t group_size, double* ll);
+/* Nelder-Mead multistart fit: basis null = grouped ML (vecchia.rs:939-1081
+ * with blocks), else REML (vecchia.rs:1572-1644). */
+int or_vecchia_fit_nm(int dim, int64_t n, const double* coords, const double* values, int32_t kind,
+                      int64_t m, const int64_t* order_in, const double* basis, int64_t p,
+                      int64_t group_size, int64_t nstarts, const double* starts, double step,
+                      int64_t max_iter, double* x_out, double* f_out, int64_t* n_evals);
+
 /* optim.rs nelder_mead_multistart over a C callback (for driver parity). */
 typedef double (*or_objective_fn)(const double* x, int64_t n, void* ctx);
 /* vecchia.rs:353-389 g_and_dg; vecchia.rs:428-530 loglik_grad_inner on a plan
@@ -181,6 +199,7 @@ int or_nelder_mead_multistart(or_objective_fn f, void* ctx, int64_t n, int64_t n
 void or_rng_u64(uint64_t seed, int64_t count, uint64_t* out);
 void or_rng_uniform(uint64_t seed, int64_t count, double* out);
 void or_rng_normal(uint64_t seed, int64_t count, double* out);
+void or_rng_draw(uint64_t seed, int64_t n_uniform, int64_t n_normal, double* out);
 /* vecchia.rs:1941 `field(n, seed)` and tests/three_d.rs:12 `synthetic_3d`. */
 void or_test_field_2d(int64_t n, uint64_t seed, double* coords, double* values);
 void or_test_field_3d(int64_t n, uint64_t seed, double* coords, double* values);

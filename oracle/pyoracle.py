@@ -117,6 +117,14 @@ def _declare(L):
         "or_vecchia_mle_setup": (C.c_int, [C.c_int, i64, pd, pd, pd, pd]),
         "or_vecchia_mle_nm": (C.c_int, [C.c_int, i64, pd, pd, i32, d, i64, pi64, i64, pd, d, i64,
                                         pd, pd, pi64]),
+        "or_poly_basis_terms": (i64, [C.c_int, i32]),
+        "or_poly_basis": (C.c_int, [C.c_int, i64, pd, i32, pd]),
+        "or_drift_basis": (C.c_int, [i64, i64, pd, pd]),
+        "or_vecchia_reml_loglik": (C.c_int, [C.c_int, i64, pd, pd, pm, i64, pi64, pi64, pi32, pd,
+                                             i64, i64, pd]),
+        "or_vecchia_fit_nm": (C.c_int, [C.c_int, i64, pd, pd, i32, i64, pi64, pd, i64, i64, i64,
+                                        pd, d, i64, pd, pd, pi64]),
+        "or_rng_draw": (None, [C.c_uint64, i64, i64, pd]),
         "or_nelder_mead_multistart": (C.c_int, [_OBJ, vp, i64, i64, pd, d, i64, pd, pd]),
         "or_g_and_dg": (C.c_int, [i32, d, pd, pd]),
         "or_vecchia_loglik_grad": (C.c_int, [C.c_int, i64, pd, pd, i32, d, d, d, i64, pi64, pi64,
@@ -445,6 +453,64 @@ def vecchia_mle_nm(coords, values, kind, m, starts, step=0.3, max_iter=2000, ord
         _p(o, C.c_int64) if o is not None else None, len(starts), _p(starts), C.c_double(step),
         int(max_iter), _p(x), C.byref(f), C.byref(ne)))
     return x, f.value, ne.value
+
+
+def poly_basis(coords, degree):
+    """vecchia.rs:1181-1233: monomials of the centred, scaled coordinates."""
+    coords = _f64(coords)
+    p = lib().or_poly_basis_terms(coords.shape[1], int(degree))
+    out = np.zeros((len(coords), p))
+    _check(lib().or_poly_basis(coords.shape[1], len(coords), _p(coords), int(degree), _p(out)))
+    return out
+
+
+def drift_basis(drift):
+    """vecchia.rs:1246-1272: intercept plus standardised covariates."""
+    drift = _f64(drift)
+    drift = drift.reshape(len(drift), -1)
+    out = np.zeros((len(drift), drift.shape[1] + 1))
+    _check(lib().or_drift_basis(len(drift), drift.shape[1], _p(drift), _p(out)))
+    return out
+
+
+def vecchia_reml_loglik(coords, values, model, order, nb, cnt, basis, group_size=1):
+    """vecchia.rs:1278-1457 on an existing plan (group_size <= 1: ungrouped)."""
+    coords, values, basis = _f64(coords), _f64(values), _f64(basis)
+    n, m = nb.shape
+    ll = C.c_double()
+    mm = model_struct(model)
+    _check(lib().or_vecchia_reml_loglik(coords.shape[1], n, _p(coords), _p(values), C.byref(mm), m,
+                                        _p(np.ascontiguousarray(order, np.int64), C.c_int64),
+                                        _p(np.ascontiguousarray(nb, np.int64), C.c_int64),
+                                        _p(np.ascontiguousarray(cnt, np.int32), C.c_int32),
+                                        _p(basis), basis.shape[1], int(group_size), C.byref(ll)))
+    return ll.value
+
+
+def vecchia_fit_nm(coords, values, kind, m, starts, basis=None, group_size=1, step=0.3,
+                   max_iter=2000, order=None):
+    """Nelder-Mead multistart: grouped ML (basis None) or REML with `basis`."""
+    coords, values = _f64(coords), _f64(values)
+    starts = _f64(starts).reshape(-1, 3)
+    b = None if basis is None else _f64(basis)
+    x = np.zeros(3)
+    f = C.c_double()
+    ne = C.c_int64()
+    o = None if order is None else np.ascontiguousarray(order, dtype=np.int64)
+    _check(lib().or_vecchia_fit_nm(
+        coords.shape[1], len(coords), _p(coords), _p(values),
+        KINDS[kind] if isinstance(kind, str) else int(kind), int(m),
+        _p(o, C.c_int64) if o is not None else None, _p(b) if b is not None else None,
+        0 if b is None else b.shape[1], int(group_size), len(starts), _p(starts),
+        C.c_double(step), int(max_iter), _p(x), C.byref(f), C.byref(ne)))
+    return x, f.value, ne.value
+
+
+def rng_draw(seed, n_uniform, n_normal):
+    """One xoshiro256++ stream: n_uniform uniforms, then n_normal normals."""
+    out = np.zeros(n_uniform + n_normal)
+    lib().or_rng_draw(int(seed), int(n_uniform), int(n_normal), _p(out))
+    return out[:n_uniform], out[n_uniform:]
 
 
 def g_and_dg(kind, d):

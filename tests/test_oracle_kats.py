@@ -530,3 +530,107 @@ def test_grouped_at_least_as_close_as_ungrouped():
     err0 = abs(O.vecchia_loglik_plan(c, v, m, o, nb, cnt) - exact)
     for g in (2, 4, 6):
         assert abs(O.vecchia_loglik_grouped(c, v, m, o, nb, cnt, g) - exact) <= err0 + 1e-9
+
+
+# ------------------------------------------------------- Vecchia REML --------
+def _cov_matrix(c, m):
+    sill = m.nugget + sum(s.sill for s in m.structures)
+    n = len(c)
+    out = np.empty((n, n))
+    for a in range(n):
+        for b in range(n):
+            out[a, b] = sill if a == b else sill - O.gamma_dh(m, c[a] - c[b])
+    return out
+
+
+def _exact_reml(c, v, m, f):
+    # vecchia.rs:2431-2463 exact_reml: the full restricted likelihood
+    n, p = f.shape
+    s = _cov_matrix(c, m)
+    siz = np.linalg.solve(s, v)
+    sif = np.linalg.solve(s, f)
+    amat = f.T @ sif
+    cvec = f.T @ siz
+    beta = np.linalg.solve(amat, cvec)
+    resid = v @ siz - cvec @ beta
+    return -0.5 * ((n - p) * math.log(2 * math.pi) + np.linalg.slogdet(s)[1]
+                   + np.linalg.slogdet(amat)[1] + resid)
+
+
+def test_poly_and_drift_bases():
+    # vecchia.rs:1181-1272: p = C(degree + dim, dim); centred, unit-variance columns
+    c, _ = O.test_field_3d(40, 3)
+    for deg, p in ((0, 1), (1, 4), (2, 10)):
+        f = O.poly_basis(c, deg)
+        assert f.shape == (40, p)
+        np.testing.assert_array_equal(f[:, 0], 1.0)
+    f = O.poly_basis(c[:, :2], 1)
+    # exponent order (0,0), (0,1), (1,0): the last dimension varies fastest
+    np.testing.assert_allclose(f[:, 1], (c[:, 1] - c[:, 1].mean()) / c[:, 1].std(), atol=1e-12)
+    np.testing.assert_allclose(f[:, 2], (c[:, 0] - c[:, 0].mean()) / c[:, 0].std(), atol=1e-12)
+    d = O.drift_basis(np.stack([c[:, 0] * 1e4 + 6e5, c[:, 2]], 1))
+    np.testing.assert_array_equal(d[:, 0], 1.0)
+    np.testing.assert_allclose(d[:, 1:].mean(0), 0.0, atol=1e-12)
+    np.testing.assert_allclose(d[:, 1:].std(0), 1.0, atol=1e-12)
+
+
+def test_reml_full_conditioning_equals_exact():
+    # vecchia.rs:2466-2481 (ungrouped), and every group size on the same plan
+    c, v = O.test_field_2d(16, 4)
+    m = _exp_model(0.05, 35.0)
+    f = O.poly_basis(c, 1)
+    exact = _exact_reml(c, v, m, f)
+    o, nb, cnt = O.vecchia_plan(c, len(c) - 1)
+    for g in (1, 2, 3, 5, 16):
+        assert abs(O.vecchia_reml_loglik(c, v, m, o, nb, cnt, f, g) - exact) < 1e-7
+    fq = O.poly_basis(c, 2)
+    assert abs(O.vecchia_reml_loglik(c, v, m, o, nb, cnt, fq, 4) - _exact_reml(c, v, m, fq)) < 1e-7
+
+
+def _gp_field(seed, n, truth):
+    # the reference tests' draw: 2n uniforms (x, y in [0, 60)), then n normals
+    # from one stream; values = L eps with L the Cholesky factor of Sigma
+    u, eps = O.rng_draw(seed, 2 * n, n)
+    c = u.reshape(n, 2) * 60.0
+    l = np.linalg.cholesky(_cov_matrix(c, truth))
+    return c, l @ eps
+
+
+def _reml_fit(c, v, kind, m, f, g=1):
+    starts, _ = O.vecchia_mle_setup(c, v)
+    x, fx, _ = O.vecchia_fit_nm(c, v, kind, m, starts, basis=f, group_size=g)
+    return math.exp(x[2]), -fx
+
+
+def test_reml_tames_the_range_under_a_trend():
+    # vecchia.rs:2504-2545
+    c, gp = _gp_field(20, 90, _exp_model(0.05, 10.0))
+    v = 0.3 * c[:, 0] - 0.2 * c[:, 1] + gp
+    x, _, _ = O.vecchia_mle_bfgs(c, v, "exponential", 8)
+    ml_r = math.exp(x[2])
+    reml_r, _ = _reml_fit(c, v, "exponential", 8, O.poly_basis(c, 1))
+    assert reml_r < ml_r and reml_r < 40.0
+
+
+@pytest.mark.parametrize("utm", [False, True])
+def test_reml_drift_recovers_range_with_a_covariate(utm):
+    # vecchia.rs:2548-2588 and 2590-2638 (UTM-scale covariate)
+    c, gp = _gp_field(21, 90, _exp_model(0.05, 10.0))
+    cov = np.exp(-((c[:, 0] - 30.0) ** 2 + (c[:, 1] - 30.0) ** 2) / 200.0)
+    v = 8.0 * cov + gp
+    drift = 600_000.0 + 1e4 * cov if utm else cov
+    r, _ = _reml_fit(c, v, "exponential", 8, O.drift_basis(drift.reshape(-1, 1)))
+    assert r < 40.0
+
+
+def test_vecchia_mle_grouped_matches_ungrouped_under_full_conditioning():
+    # vecchia.rs:2110-2128
+    c, v = O.test_field_2d(16, 21)
+    m = len(c) - 1
+    xu, fu, _ = O.vecchia_mle_bfgs(c, v, "exponential", m)
+    starts, _ = O.vecchia_mle_setup(c, v)
+    xg, fg, _ = O.vecchia_fit_nm(c, v, "exponential", m, starts, group_size=4)
+    assert abs(fu - fg) < 1e-6
+    assert abs(xu[0] ** 2 - xg[0] ** 2) < 1e-4
+    assert abs(math.exp(xu[1]) - math.exp(xg[1])) < 1e-3
+    assert abs(math.exp(xu[2]) - math.exp(xg[2])) < 1e-2
