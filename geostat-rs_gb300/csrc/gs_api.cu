@@ -578,10 +578,18 @@ KrigeArgs base_args(const gs_kriging* k) {
 // FP64 re-solve count and a final synchronisation; otherwise the whole pass
 // is only enqueued on `stream` (no host synchronisation: it can be captured
 // into a CUDA graph).
+// Block kriging: the shared discretisation offsets (noff x dim, device) and
+// the within-block covariance (device); the pass then runs the FP64 kernel.
+struct BlockSpec {
+  const double* off;
+  int noff;
+  const double* cbb;
+};
+
 int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
                  const double* tz, const double* tdrift, double* value, double* variance,
                  double* lagrange, uint8_t* status, int precision, cudaStream_t stream, bool timed,
-                 const int32_t* excl_labels = nullptr) {
+                 const int32_t* excl_labels = nullptr, const BlockSpec* blk = nullptr) {
   if (nt == 0) return GS_OK;
   const gs_pointset* ps = k->ps;
   const gs_kcfg& c = k->cfg;
@@ -592,7 +600,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   SearchParams sp{};
   int kout;
   const int64_t navail = excl_labels ? n - 1 : n;  // cross-validation: at most n - 1 others
-  if (!k->use_tree && k->lu_state != 0 && !excl_labels) {
+  if (!k->use_tree && k->lu_state != 0 && !excl_labels && !blk) {
     kout = (int)n;  // the factored global path below
   } else if (!k->use_tree) {
     if (navail + p > GS_MAX_SYSTEM)
@@ -615,7 +623,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     sp.k = (int)std::min<int64_t>(n, GS_MAX_SYSTEM - p);
     kout = sp.k;
   }
-  const bool global_lu = !k->use_tree && k->lu_state != 0 && !excl_labels;
+  const bool global_lu = !k->use_tree && k->lu_state != 0 && !excl_labels && !blk;
   if (!global_lu && kout + p > GS_MAX_SYSTEM)
     return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood plus drift terms exceed " +
                                               std::to_string(GS_MAX_SYSTEM) + " on the CUDA path");
@@ -627,6 +635,11 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
 
   KrigeArgs a = base_args(k);
   a.kout = kout;
+  if (blk) {
+    a.boff = blk->off;
+    a.nboff = blk->noff;
+    a.cbb = blk->cbb;
+  }
 
   // global neighbourhood factored at build: per-target solves only
   if (global_lu) {
@@ -675,7 +688,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   const int64_t nchunks = (nt + chunk - 1) / chunk;
   // uneven neighbourhoods (octant, radius) are binned by system size: the
   // small systems run on the 32-thread kernel, the rest on the 64-thread one
-  const bool mixed = precision != GS_PREC_FP64;
+  const bool mixed = precision != GS_PREC_FP64 && !blk;
   const bool binnable = mixed && kout > 32 && kout <= GS_MIXED_MAX_NEIGHBORS &&
                         (sp.octant || sp.has_radius || sp.unbounded);
   // launch shape: pinned, tuned earlier for this size class, tuned now on
@@ -988,6 +1001,11 @@ static void fold_assignment(int64_t n, int64_t k, uint64_t seed, std::vector<int
   for (int64_t j = 0; j < n; ++j) fold_of[order[j]] = (int32_t)(j % k);
 }
 
+}  // extern "C"
+static int cv_with_labels(const gs_kriging* k, const std::vector<int32_t>& label,
+                          double* predicted, double* variance, uint8_t* status, int precision);
+extern "C" {
+
 int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed, double* predicted,
                               double* variance, uint8_t* status, int precision) {
   if (!k || !predicted || !variance) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
@@ -1006,6 +1024,65 @@ int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed
   } else {
     fold_assignment(n, nfolds, seed, label);
   }
+  return cv_with_labels(k, label, predicted, variance, status, precision);
+}
+
+// validation.rs:298-328 spatial_block_assignment: a regular grid of
+// blocks_per_dim[d] cells over the bounding box, dimension 0 fastest.
+static void spatial_block_assignment(const gs_pointset* ps, const int64_t* bpd,
+                                     std::vector<int32_t>& label) {
+  const int dim = ps->dim;
+  const int64_t n = ps->n;
+  double lo[3], hi[3];
+  for (int d = 0; d < dim; ++d) lo[d] = hi[d] = ps->host[d];
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < dim; ++d) {
+      lo[d] = std::fmin(lo[d], ps->host[i * dim + d]);
+      hi[d] = std::fmax(hi[d], ps->host[i * dim + d]);
+    }
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t idx = 0, stride = 1;
+    for (int d = 0; d < dim; ++d) {
+      const double span = std::fmax(hi[d] - lo[d], 2.2250738585072014e-308);
+      const double frac = std::fmin(std::fmax((ps->host[i * dim + d] - lo[d]) / span, 0.0),
+                                    1.0 - 1e-12);
+      const int64_t bd = std::min<int64_t>((int64_t)(frac * (double)bpd[d]), bpd[d] - 1);
+      idx += bd * stride;
+      stride *= bpd[d];
+    }
+    label[i] = (int32_t)idx;
+  }
+}
+
+// validation.rs:348-374 block_cv.
+int gs_kriging_block_cv(const gs_kriging* k, const int64_t* blocks_per_dim, double* predicted,
+                        double* variance, uint8_t* status, int precision) {
+  if (!k || !blocks_per_dim || !predicted || !variance)
+    return fail(GS_ERR_INVALID_PARAMETER, "null argument");
+  const gs_pointset* ps = k->ps;
+  const int64_t n = ps->n;
+  if (n < 3) return fail(GS_ERR_INSUFFICIENT_DATA, "cross-validation requires at least 3 points");
+  double nblocks = 1.0;
+  for (int d = 0; d < ps->dim; ++d) {
+    if (blocks_per_dim[d] <= 0)
+      return fail(GS_ERR_INVALID_PARAMETER, "blocks_per_dim entries must be at least 1");
+    nblocks *= (double)blocks_per_dim[d];
+  }
+  if (nblocks < 2.0) return fail(GS_ERR_INVALID_PARAMETER, "block CV requires at least 2 blocks total");
+  if (nblocks > 2147483647.0) return fail(GS_ERR_INVALID_PARAMETER, "too many blocks");
+  std::vector<int32_t> label(n);
+  spatial_block_assignment(ps, blocks_per_dim, label);
+  return cv_with_labels(k, label, predicted, variance, status, precision);
+}
+
+}  // extern "C"
+
+// cv_with_folds (validation.rs:219-265) as one prediction pass over the data
+// points, each excluding the data points of its own label.
+static int cv_with_labels(const gs_kriging* k, const std::vector<int32_t>& label,
+                          double* predicted, double* variance, uint8_t* status, int precision) {
+  const gs_pointset* ps = k->ps;
+  const int64_t n = ps->n;
   cudaStream_t s = k->stream;
   gs::DevBuf dl, dv, dvar, dst;
   GS_TRY(dl.alloc((size_t)n * 4, s));
@@ -1036,6 +1113,8 @@ int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed
   }
   return GS_OK;
 }
+
+extern "C" {
 
 int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins, int* tuned) {
   if (!k || !run || !bins || !tuned) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
@@ -1134,6 +1213,147 @@ int gs_kriging_predict_grid(const gs_kriging* k, const double* bbox_min, const d
                              (double*)dz.ptr, s));
   GS_TRY(predict_device(k, total, (double*)dx.ptr, (double*)dy.ptr, (double*)dz.ptr, nullptr,
                         (double*)dv.ptr, (double*)dvar.ptr, nullptr, (uint8_t*)dst.ptr, precision, s));
+  GS_CUDA(cudaMemcpyAsync(value, dv.ptr, total * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(variance, dvar.ptr, total * 8, cudaMemcpyDeviceToHost, s));
+  if (status) GS_CUDA(cudaMemcpyAsync(status, dst.ptr, total, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+// block_offsets (kriging.rs:815-838): an n[0] x n[1] grid of cell centres
+// covering a block of `size`, centred on the origin, x fastest.
+int gs_block_offsets(const double* size, const int64_t* ndisc, double* out) {
+  if (!size || !ndisc || !out) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
+  if (ndisc[0] <= 0 || ndisc[1] <= 0)
+    return fail(GS_ERR_INVALID_PARAMETER, "block discretization needs at least 1 point per axis");
+  if (!(size[0] > 0.0) || !(size[1] > 0.0))
+    return fail(GS_ERR_INVALID_PARAMETER, "block size must be positive");
+  int64_t q = 0;
+  for (int64_t iy = 0; iy < ndisc[1]; ++iy)
+    for (int64_t ix = 0; ix < ndisc[0]; ++ix, ++q) {
+      out[2 * q] = (((double)ix + 0.5) / (double)ndisc[0] - 0.5) * size[0];
+      out[2 * q + 1] = (((double)iy + 0.5) / (double)ndisc[1] - 0.5) * size[1];
+    }
+  return GS_OK;
+}
+
+}  // extern "C"
+
+namespace gs {
+
+// predict_block's checks (kriging.rs:678-700), in its order.
+static int check_block(const gs_kriging* k, int64_t noff) {
+  if (k->cfg.method != GS_SIMPLE && k->cfg.method != GS_ORDINARY)
+    return fail(GS_ERR_INVALID_PARAMETER, "block kriging supports simple and ordinary kriging only");
+  if (has_power(k->model))
+    return fail(GS_ERR_INVALID_PARAMETER,
+                "block kriging with a Power model is not supported (needs a block-averaged "
+                "semivariogram)");
+  if (noff <= 0) return fail(GS_ERR_INVALID_PARAMETER, "block discretization needs at least one point");
+  if (noff > (1 << 20)) return fail(GS_ERR_INVALID_PARAMETER, "block discretization too large");
+  return GS_OK;
+}
+
+// Blocks centred at (cx, cy, cz) (device), offsets on the host: C(B,B) once,
+// then one FP64 prediction pass with block right-hand sides.
+static int block_pass(const gs_kriging* k, int64_t nb, const double* cx, const double* cy,
+               const double* cz, const double* offsets, int64_t noff, double* value,
+               double* variance, double* lagrange, uint8_t* status, cudaStream_t s) {
+  const int dim = k->ps->dim;
+  DevBuf doff, dcbb;
+  GS_TRY(doff.alloc((size_t)noff * dim * 8, s));
+  GS_TRY(dcbb.alloc(8, s));
+  GS_CUDA(cudaMemcpyAsync(doff.ptr, offsets, (size_t)noff * dim * 8, cudaMemcpyHostToDevice, s));
+  GS_TRY(block_cbb_launch(dim, k->dm, (const double*)doff.ptr, (int)noff, k->model.nugget,
+                          (double*)dcbb.ptr, s));
+  BlockSpec blk{(const double*)doff.ptr, (int)noff, (const double*)dcbb.ptr};
+  return predict_pass(k, nb, cx, cy, cz, nullptr, value, variance, lagrange, status, GS_PREC_FP64,
+                      s, true, nullptr, &blk);
+}
+
+}  // namespace gs
+
+extern "C" {
+
+// Kriging::predict_block (kriging.rs:674-779) for nb blocks sharing one
+// discretisation (offsets: noff x dim, host); host buffers.  Per-block
+// failures (no neighbours, singular) are NaN with their status.
+int gs_kriging_predict_block(const gs_kriging* k, int64_t nb, const double* cx, const double* cy,
+                             const double* cz, const double* offsets, int64_t noff, double* value,
+                             double* variance, double* lagrange, uint8_t* status, void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  GS_TRY(check_block(k, noff));
+  if (!offsets) return fail(GS_ERR_INVALID_PARAMETER, "null offsets");
+  if (nb == 0) return GS_OK;
+  const int dim = k->ps->dim;
+  if (!cx || !cy || (dim == 3 && !cz) || !value || !variance)
+    return fail(GS_ERR_INVALID_PARAMETER, "null centre or output buffer");
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  DevBuf dx, dy, dz, dv, dvar, dlag, dst;
+  GS_TRY(dx.alloc(nb * 8, s));
+  GS_TRY(dy.alloc(nb * 8, s));
+  if (dim == 3) GS_TRY(dz.alloc(nb * 8, s));
+  GS_TRY(dv.alloc(nb * 8, s));
+  GS_TRY(dvar.alloc(nb * 8, s));
+  if (lagrange) GS_TRY(dlag.alloc(nb * 8, s));
+  GS_TRY(dst.alloc(nb, s));
+  GS_CUDA(cudaMemcpyAsync(dx.ptr, cx, nb * 8, cudaMemcpyHostToDevice, s));
+  GS_CUDA(cudaMemcpyAsync(dy.ptr, cy, nb * 8, cudaMemcpyHostToDevice, s));
+  if (dim == 3) GS_CUDA(cudaMemcpyAsync(dz.ptr, cz, nb * 8, cudaMemcpyHostToDevice, s));
+  GS_TRY(block_pass(k, nb, (double*)dx.ptr, (double*)dy.ptr, (double*)dz.ptr, offsets, noff,
+                    (double*)dv.ptr, (double*)dvar.ptr, lagrange ? (double*)dlag.ptr : nullptr,
+                    (uint8_t*)dst.ptr, s));
+  GS_CUDA(cudaMemcpyAsync(value, dv.ptr, nb * 8, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaMemcpyAsync(variance, dvar.ptr, nb * 8, cudaMemcpyDeviceToHost, s));
+  if (lagrange) GS_CUDA(cudaMemcpyAsync(lagrange, dlag.ptr, nb * 8, cudaMemcpyDeviceToHost, s));
+  if (status) GS_CUDA(cudaMemcpyAsync(status, dst.ptr, nb, cudaMemcpyDeviceToHost, s));
+  GS_CUDA(cudaStreamSynchronize(s));
+  return GS_OK;
+}
+
+// Kriging::predict_block_grid (kriging.rs:787-805), 2-D: blocks of
+// block_size at every cell centre, discretised by block_offsets(block_size,
+// discr).  A method or model predict_block rejects gives NaN at every cell
+// (the reference's unwrap_or(NAN_ESTIMATE)) with status
+// GS_ST_INVALID_PARAMETER.
+int gs_kriging_predict_block_grid(const gs_kriging* k, const double* bbox_min,
+                                  const double* bbox_max, const int64_t* ncell,
+                                  const double* block_size, const int64_t* discr, double* value,
+                                  double* variance, uint8_t* status, void* stream) {
+  if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
+  if (k->ps->dim != 2) return fail(GS_ERR_INVALID_PARAMETER, "block grids are 2-D");
+  std::vector<double> off;
+  if (discr && discr[0] > 0 && discr[1] > 0 && discr[0] * discr[1] <= (1 << 20))
+    off.resize((size_t)(discr[0] * discr[1]) * 2);
+  else if (discr && (discr[0] <= 0 || discr[1] <= 0))
+    return fail(GS_ERR_INVALID_PARAMETER, "block discretization needs at least 1 point per axis");
+  else
+    return fail(GS_ERR_INVALID_PARAMETER, "block discretization too large");
+  GS_TRY(gs_block_offsets(block_size, discr, off.data()));
+  double step[3] = {0, 0, 0};
+  int64_t total = 1;
+  for (int d = 0; d < 2; ++d) {
+    if (ncell[d] == 0) return fail(GS_ERR_INVALID_PARAMETER, "grid must have at least one cell per axis");
+    if (!(bbox_max[d] > bbox_min[d])) return fail(GS_ERR_INVALID_PARAMETER, "degenerate bbox");
+    step[d] = (bbox_max[d] - bbox_min[d]) / (double)ncell[d];
+    total *= ncell[d];
+  }
+  if (check_block(k, (int64_t)off.size() / 2) != GS_OK) {
+    for (int64_t i = 0; i < total; ++i) value[i] = variance[i] = NAN;
+    if (status) std::memset(status, GS_ST_INVALID_PARAMETER, (size_t)total);
+    return GS_OK;
+  }
+  cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  DevBuf dx, dy, dv, dvar, dst;
+  GS_TRY(dx.alloc(total * 8, s));
+  GS_TRY(dy.alloc(total * 8, s));
+  GS_TRY(dv.alloc(total * 8, s));
+  GS_TRY(dvar.alloc(total * 8, s));
+  GS_TRY(dst.alloc(total, s));
+  GS_TRY(grid_centers_launch(2, bbox_min, step, ncell, (double*)dx.ptr, (double*)dy.ptr, nullptr, s));
+  GS_TRY(block_pass(k, total, (double*)dx.ptr, (double*)dy.ptr, nullptr, off.data(),
+                    (int64_t)off.size() / 2, (double*)dv.ptr, (double*)dvar.ptr, nullptr,
+                    (uint8_t*)dst.ptr, s));
   GS_CUDA(cudaMemcpyAsync(value, dv.ptr, total * 8, cudaMemcpyDeviceToHost, s));
   GS_CUDA(cudaMemcpyAsync(variance, dvar.ptr, total * 8, cudaMemcpyDeviceToHost, s));
   if (status) GS_CUDA(cudaMemcpyAsync(status, dst.ptr, total, cudaMemcpyDeviceToHost, s));

@@ -963,8 +963,22 @@ __global__ void __launch_bounds__(128) krige_fp64_kernel(KrigeArgs a, DevModel m
           AT(n + k, ii, N) = f[k];
         }
       }
-      double h[3] = {pi[0] - tp[0], pi[1] - tp[1], D == 3 ? pi[2] - tp[2] : 0.0};
-      const double bi = cov_fp64<D>(m, h);
+      double bi;
+      if (a.nboff > 0) {
+        // point-to-block covariance: the mean over the discretisation
+        // points centre + offset (kriging.rs:726-735)
+        double s = 0.0;
+        for (int u = 0; u < a.nboff; ++u) {
+          double h[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+          for (int d = 0; d < D; ++d) h[d] = pi[d] - (tp[d] + a.boff[u * D + d]);
+          s += cov_fp64<D>(m, h);
+        }
+        bi = s / (double)a.nboff;
+      } else {
+        double h[3] = {pi[0] - tp[0], pi[1] - tp[1], D == 3 ? pi[2] - tp[2] : 0.0};
+        bi = cov_fp64<D>(m, h);
+      }
       Bv[(int64_t)ii * T] = bi;
       B0[(int64_t)ii * T] = bi;
     }
@@ -1031,7 +1045,8 @@ __global__ void __launch_bounds__(128) krige_fp64_kernel(KrigeArgs a, DevModel m
       for (int j = i + 1; j < N; ++j) s -= AT(i, j, N) * Bv[(int64_t)j * T];
       Bv[(int64_t)i * T] = s / AT(i, i, N);
     }
-    // outputs (kriging.rs:614-643)
+    // outputs (kriging.rs:614-643; blocks: C(B,B) in place of c0, 758-778)
+    const double c_self = a.nboff > 0 ? *a.cbb : m.c0;
     double v, var, lag = kNaN;
     if (a.method == GS_SIMPLE) {
       v = a.sk_mean;
@@ -1041,13 +1056,13 @@ __global__ void __launch_bounds__(128) krige_fp64_kernel(KrigeArgs a, DevModel m
         v += w * (a.val[nbt[ii]] - a.sk_mean);
         red += w * B0[(int64_t)ii * T];
       }
-      var = m.c0 - red;
+      var = c_self - red;
     } else {
       v = 0.0;
       for (int ii = 0; ii < n; ++ii) v += Bv[(int64_t)ii * T] * a.val[nbt[ii]];
       double red = 0.0;
       for (int i = 0; i < N; ++i) red += Bv[(int64_t)i * T] * B0[(int64_t)i * T];
-      var = m.c0 - red;
+      var = c_self - red;
       lag = Bv[(int64_t)n * T];
     }
     a.out_v[t] = v;
@@ -1455,6 +1470,35 @@ int krige_fp64_launch(const KrigeArgs& a, const DevModel& m, double* scratch, in
   if (a.dim == 2) krige_fp64_kernel<2><<<blocks, tpb, 0, stream>>>(a, m, scratch, Tl);
   else krige_fp64_kernel<3><<<blocks, tpb, 0, stream>>>(a, m, scratch, Tl);
   GS_CUDA(cudaGetLastError());
+  count_launch(1);
+  return GS_OK;
+}
+
+template <int D>
+__global__ void block_cbb_kernel(DevModel m, const double* off, int nu, double nugget, double* out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const double c0c = m.c0 - nugget;
+  double s = 0.0;
+  for (int u = 0; u < nu; ++u)
+    for (int v = 0; v < nu; ++v) {
+      if (u == v) {
+        s += c0c;
+      } else {
+        double h[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < D; ++d) h[d] = off[u * D + d] - off[v * D + d];
+        s += cov_fp64<D>(m, h);
+      }
+    }
+  const double fn = (double)nu;
+  *out = s / (fn * fn);
+}
+
+int block_cbb_launch(int dim, const DevModel& m, const double* off, int noff, double nugget,
+                     double* out, cudaStream_t stream) {
+  if (dim == 2) block_cbb_kernel<2><<<1, 32, 0, stream>>>(m, off, noff, nugget, out);
+  else block_cbb_kernel<3><<<1, 32, 0, stream>>>(m, off, noff, nugget, out);
+  if (cudaGetLastError() != cudaSuccess) return fail(GS_ERR_CUDA, "block covariance launch failed");
   count_launch(1);
   return GS_OK;
 }

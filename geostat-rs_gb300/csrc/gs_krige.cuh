@@ -51,6 +51,9 @@ struct KrigeArgs {
   int run;                   // consecutive targets per block sequence (0: 64)
   const int* route_fp64;     // when set and nonzero: flag every valid system
                              // for the FP64 re-solve without attempting it
+  const double* boff;        // block kriging: nboff x dim discretisation offsets
+  int nboff;                 // (FP64 kernel only; 0 = point kriging)
+  const double* cbb;         // block kriging: the within-block covariance (device)
 };
 
 // Mixed-precision kernel for systems with n <= 64 neighbours and at most
@@ -89,6 +92,12 @@ int global_solve_launch(const KrigeArgs& a, const DevModel& m, int N, const doub
                         const int32_t* perm, int state, double* scratch, int64_t scratch_warps,
                         cudaStream_t stream);
 int64_t fp64_threads_for(int nmax, int64_t budget_bytes);
+
+// Block kriging's within-block covariance (kriging.rs:742-756): the mean of
+// C(u - v) over all discretisation pairs, with c0 - nugget for u = v; one
+// thread, the reference's summation order.
+int block_cbb_launch(int dim, const DevModel& m, const double* off, int noff, double nugget,
+                     double* out, cudaStream_t stream);
 
 // Grid2D / Grid3D cell centres (grid.rs:80-96, 188-203) on the device.
 int grid_centers_launch(int dim, const double* bmin, const double* step, const int64_t* ncell,

@@ -11,7 +11,8 @@ from .errors import (CudaError, DimensionMismatch, DuplicatePoints, GeostatError
                      SingularSystem)
 from .model import Anisotropy, Structure, VariogramModel, parse_kind
 from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Server, TuneResult,
-                  VecchiaPlan, clustered_points, k_fold, krige, krige_3d, krige_grid,
+                  VecchiaPlan, block_cv, block_offsets, clustered_points, k_fold, krige,
+                  krige_3d, krige_grid,
                   last_timings, leave_one_out, leave_one_out_with_drift, maxmin_order,
                   tune_kriging_neighbors,
                   nelder_mead_multistart, rff_field, rng_normal, rng_uniform, seq_mean,

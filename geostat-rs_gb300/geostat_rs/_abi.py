@@ -100,6 +100,12 @@ SIGNATURES = {
     "gs_vecchia_mle": (_int, [_vp, _i32, _i64, _pi64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_mle_nm": (_int, [_vp, _i32, _i64, _pi64, _i64, _pd, _d, _i64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_loglik_grad_batch": (_int, [_vp, _i64, _pm, _pd, _pd, _pi32, _int, _vp]),
+    "gs_kriging_block_cv": (_int, [_vp, _pi64, _pd, _pd, _pu8, _int]),
+    "gs_block_offsets": (_int, [_pd, _pi64, _pd]),
+    "gs_kriging_predict_block": (_int, [_vp, _i64, _pd, _pd, _pd, _pd, _i64, _pd, _pd, _pd, _pu8,
+                                        _vp]),
+    "gs_kriging_predict_block_grid": (_int, [_vp, _pd, _pd, _pi64, _pd, _pi64, _pd, _pd, _pu8,
+                                             _vp]),
     "gs_vecchia_reml_loglik_batch": (_int, [_vp, _i64, _pm, _i32, _pd, _i64, _i64, _pd, _pi32,
                                             _vp]),
     "gs_vecchia_mle_grouped": (_int, [_vp, _i32, _i64, _pi64, _i64, _pm, _pd, _pd, _pi64]),

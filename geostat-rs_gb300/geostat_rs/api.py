@@ -264,6 +264,49 @@ class Kriging:
             return KrigingResult(v, var, np.full(total, np.nan), st)
         return v, var
 
+    def predict_block_many(self, centers, offsets, full: bool = False):
+        """``Kriging::predict_block`` (kriging.rs:674-779) for many blocks
+        sharing one discretisation (``offsets``: noff x D).  Returns
+        ``(value, variance)``, or a :class:`KrigingResult` with ``full=True``;
+        a failing block is NaN with its status."""
+        nb, (x, y, z) = self._targets(centers)
+        off = _f64(offsets).reshape(-1, self.data.dim)
+        v, var, lag = np.empty(nb), np.empty(nb), np.empty(nb)
+        st = np.empty(nb, dtype=np.uint8)
+        _abi.check(_abi.load().gs_kriging_predict_block(self._h, nb, _p(x), _p(y), _p(z), _p(off),
+                                                        len(off), _p(v), _p(var), _p(lag),
+                                                        _p(st, C.c_uint8), None))
+        if full:
+            return KrigingResult(v, var, lag, st)
+        return v, var
+
+    def predict_block(self, center, offsets):
+        """One block: ``(value, variance, lagrange)``; raises as the
+        reference does (NoNeighbors, SingularSystem, ...)."""
+        r = self.predict_block_many(_f64(center).reshape(1, -1), offsets, full=True)
+        code = int(r.status[0]) & 0x3f
+        if code:
+            from .errors import raise_for
+            raise_for(code, "block kriging failed")
+        lag = None if self.config.method == "simple" else float(r.lagrange[0])
+        return float(r.value[0]), float(r.variance[0]), lag
+
+    def predict_block_grid(self, bbox_min, bbox_max, ncell, block_size, discr=(4, 4),
+                           full: bool = False):
+        """``Kriging::predict_block_grid`` (kriging.rs:787-805): a block of
+        ``block_size`` at every 2-D cell centre (x fastest)."""
+        nc = np.ascontiguousarray(ncell, dtype=np.int64)
+        total = int(np.prod(nc))
+        v, var = np.empty(total), np.empty(total)
+        st = np.empty(total, dtype=np.uint8)
+        _abi.check(_abi.load().gs_kriging_predict_block_grid(
+            self._h, _p(_f64(bbox_min)), _p(_f64(bbox_max)), _p(nc, C.c_int64),
+            _p(_f64(block_size)), _p(np.ascontiguousarray(discr, dtype=np.int64), C.c_int64),
+            _p(v), _p(var), _p(st, C.c_uint8), None))
+        if full:
+            return KrigingResult(v, var, np.full(total, np.nan), st)
+        return v, var
+
     def neighbors(self, targets, kcap: int):
         """Conditioning indices per target (``Kriging::neighbors``), -1 padded."""
         nt, (x, y, z) = self._targets(targets)
@@ -423,6 +466,23 @@ def k_fold(data: "PointSet", model: VariogramModel, config: KrigingConfig, k: in
     return _cross_validate(Kriging.new(data, model, config), data, k, seed, precision)
 
 
+def block_cv(data: "PointSet", model: VariogramModel, config: KrigingConfig, blocks_per_dim,
+             precision: str = "mixed") -> CvResult:
+    """``validation::block_cv`` (validation.rs:348-374): the data's bounding
+    box cut into a regular grid of blocks, each block predicted from the
+    points outside it."""
+    bpd = np.ascontiguousarray(blocks_per_dim, dtype=np.int64)
+    if len(bpd) != data.dim:
+        raise DimensionMismatch(f"{len(bpd)} block counts for {data.dim} dimensions")
+    k = Kriging.new(data, model, config)
+    n = data.n
+    pred, var = np.empty(n), np.empty(n)
+    st = np.empty(n, dtype=np.uint8)
+    _abi.check(_abi.load().gs_kriging_block_cv(k._h, _p(bpd, C.c_int64), _p(pred), _p(var),
+                                               _p(st, C.c_uint8), PRECISIONS[precision]))
+    return CvResult(np.array(data.values, dtype=float), pred, var)
+
+
 @dataclass
 class TuneResult:
     """``tuning::TuneResult``: the best candidate, its VEcv and the trace."""
@@ -502,10 +562,8 @@ def krige_grid(x, y, values, model, bbox, nx, ny, method="ordinary", mean=None, 
                max_neighbors=None, radius=None, block=None, block_discr=(4, 4),
                min_neighbors=None, octant=None, search_azimuth=None, search_ratio=1.0,
                search_ratio_z=1.0, search_dip=0.0, search_rake=0.0, precision="mixed"):
-    """lib.rs:632-696 ``krige_grid`` (point kriging; block kriging is not on
-    the CUDA path)."""
-    if block is not None:
-        raise InvalidParameter("block kriging is not available on the CUDA path")
+    """lib.rs:632-696 ``krige_grid``: point kriging, or block kriging of
+    ``block`` = (width, height) blocks discretised ``block_discr``."""
     if nx == 0 or ny == 0:
         raise InvalidParameter("grid must have at least one cell per axis")
     if not (bbox[2] > bbox[0]) or not (bbox[3] > bbox[1]):
@@ -519,7 +577,21 @@ def krige_grid(x, y, values, model, bbox, nx, ny, method="ordinary", mean=None, 
     cfg.anisotropic_search = _anisotropic_search(search_azimuth, search_ratio, search_ratio_z,
                                                  search_dip, search_rake)
     k = Kriging.new(data, model, cfg)
+    if block is not None:
+        return k.predict_block_grid([bbox[0], bbox[1]], [bbox[2], bbox[3]], [nx, ny],
+                                    [block[0], block[1]], [block_discr[0], block_discr[1]])
     return k.predict_grid([bbox[0], bbox[1]], [bbox[2], bbox[3]], [nx, ny], precision)
+
+
+def block_offsets(size, n):
+    """``block_offsets`` (kriging.rs:815-838): an n[0] x n[1] grid of cell
+    centres covering a block of ``size``, centred on the origin."""
+    nn = np.ascontiguousarray(n, dtype=np.int64)
+    if nn[0] <= 0 or nn[1] <= 0:
+        raise InvalidParameter("block discretization needs at least 1 point per axis")
+    out = np.empty((int(nn[0] * nn[1]), 2))
+    _abi.check(_abi.load().gs_block_offsets(_p(_f64(size)), _p(nn, C.c_int64), _p(out)))
+    return out
 
 
 def krige_3d(x, y, z, values, model, target_x, target_y, target_z, method="ordinary",

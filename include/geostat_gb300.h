@@ -76,6 +76,7 @@ enum {
   GS_ST_INSUFFICIENT_DATA = 1,
   GS_ST_SINGULAR = 3,
   GS_ST_NO_NEIGHBORS = 5,
+  GS_ST_INVALID_PARAMETER = 4, /* block grids: a method or model blocks do not support */
   GS_ST_CAPACITY = 7, /* neighbourhood larger than GS_MAX_SYSTEM */
   GS_ST_FP64_RESOLVED = 0x40
 };
@@ -184,6 +185,14 @@ int gs_kriging_predict_many_async(const gs_kriging* k, int64_t nt, const double*
  * points (InsufficientData), k outside [2, n] (InvalidParameter). */
 int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed,
                               double* predicted, double* variance, uint8_t* status, int precision);
+/* block_cv (validation.rs:348-374): labels from spatial_block_assignment
+ * (validation.rs:298-328, a blocks_per_dim[0] x ... grid over the bounding
+ * box, dimension 0 fastest), each point predicted from the points outside
+ * its block, otherwise as gs_kriging_cross_validate.  Errors: fewer than 3
+ * points (InsufficientData), an entry of 0 or fewer than 2 blocks in all
+ * (InvalidParameter). */
+int gs_kriging_block_cv(const gs_kriging* k, const int64_t* blocks_per_dim, double* predicted,
+                        double* variance, uint8_t* status, int precision);
 /* Launch shapes of the mixed solver (no counterpart in the reference).  The
  * first call of at least 65,536 targets on a predictor times the candidate
  * shapes -- runs of 16/32/64/128 consecutive targets per block, uneven
@@ -220,6 +229,22 @@ int gs_kriging_predict_fp64_noalloc(const gs_kriging* k, int64_t nt, const doubl
 int gs_kriging_predict_grid(const gs_kriging* k, const double* bbox_min, const double* bbox_max,
                             const int64_t* ncell, double* value, double* variance,
                             uint8_t* status, int precision, void* stream);
+/* block_offsets (kriging.rs:815-838): out receives n[0] * n[1] offsets
+ * (x, y pairs, x fastest) of the cell centres of a block of `size`. */
+int gs_block_offsets(const double* size, const int64_t* n, double* out);
+/* Kriging::predict_block (kriging.rs:674-779) for nb blocks sharing one
+ * discretisation (offsets: noff x dim, row-major); simple and ordinary
+ * kriging, FP64; host buffers.  A per-block failure is NaN with its
+ * status; lagrange and status may be NULL. */
+int gs_kriging_predict_block(const gs_kriging* k, int64_t nb, const double* cx, const double* cy,
+                             const double* cz, const double* offsets, int64_t noff, double* value,
+                             double* variance, double* lagrange, uint8_t* status, void* stream);
+/* Kriging::predict_block_grid (kriging.rs:787-805), 2-D grids: one block of
+ * block_size (discretised by block_offsets(block_size, discr)) per cell. */
+int gs_kriging_predict_block_grid(const gs_kriging* k, const double* bbox_min,
+                                  const double* bbox_max, const int64_t* ncell,
+                                  const double* block_size, const int64_t* discr, double* value,
+                                  double* variance, uint8_t* status, void* stream);
 /* Kriging::neighbors (kriging.rs:441-490): the conditioning indices the
  * path uses, in the reference's (squared distance, index) order; host
  * buffers, kcap slots per target, -1 padded.  count may be NULL. */

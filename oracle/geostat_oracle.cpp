@@ -934,6 +934,79 @@ struct Predictor {
     *variance = fmax_(var, 0.0);
     return OR_OK;
   }
+  // kriging.rs:674-779 predict_block: the point-to-block covariances are
+  // means over the discretisation points centre + offset; C(B,B) (coincident
+  // points without the nugget) replaces c0 in the variance.
+  int predict_block(const double* ctr, const double* offsets, size_t noff, double* value,
+                    double* variance, double* lagrange) const {
+    bool tie = false;
+    std::vector<size_t> nb = neighbors(ctr, &tie);
+    size_t min_nb = cfg.min_neighbors >= 0 ? (size_t)cfg.min_neighbors : 1;
+    if (nb.size() < min_nb) return OR_NO_NEIGHBORS;
+    const size_t m = n_drift();
+    const size_t nn = nb.size();
+    const size_t dimm = nn + m;
+    const double nu = (double)noff;
+    std::vector<double> a(dimm * dimm, 0.0), b(dimm, 0.0);
+    for (size_t ii = 0; ii < nn; ++ii) {
+      const double* pi = &coords[nb[ii] * dim];
+      a[ii * dimm + ii] = c0 + (meas_err.empty() ? 0.0 : meas_err[nb[ii]]);
+      for (size_t jj = ii + 1; jj < nn; ++jj) {
+        const double* pj = &coords[nb[jj] * dim];
+        double h[3];
+        for (int d = 0; d < dim; ++d) h[d] = pi[d] - pj[d];
+        const double c = c0 - gamma_dh(model, dim, h);
+        a[ii * dimm + jj] = c;
+        a[jj * dimm + ii] = c;
+      }
+      if (m == 1) {
+        a[ii * dimm + nn] = 1.0;
+        a[nn * dimm + ii] = 1.0;
+      }
+      double s = 0.0;
+      for (size_t u = 0; u < noff; ++u) {
+        double h[3];
+        for (int d = 0; d < dim; ++d) h[d] = pi[d] - (ctr[d] + offsets[u * dim + d]);
+        s += c0 - gamma_dh(model, dim, h);
+      }
+      b[ii] = s / nu;
+    }
+    if (m == 1) b[nn] = 1.0;
+    const double c0c = c0 - model.nugget;
+    double cbb = 0.0;
+    for (size_t u = 0; u < noff; ++u)
+      for (size_t v = 0; v < noff; ++v) {
+        if (u == v) {
+          cbb += c0c;
+        } else {
+          double h[3];
+          for (int d = 0; d < dim; ++d) h[d] = offsets[u * dim + d] - offsets[v * dim + d];
+          cbb += c0 - gamma_dh(model, dim, h);
+        }
+      }
+    cbb /= nu * nu;
+    std::vector<double> b0 = b;
+    Lu lu;
+    int rc = lu_factor(a, dimm, lu);
+    if (rc) return rc;
+    std::vector<double> w = lu_solve(lu, b);
+    double v = 0.0, red = 0.0;
+    if (cfg.method == 0) {
+      v = cfg.sk_mean;
+      for (size_t ii = 0; ii < nn; ++ii) {
+        v += w[ii] * (values[nb[ii]] - cfg.sk_mean);
+        red += w[ii] * b0[ii];
+      }
+      *lagrange = kNaN;
+    } else {
+      for (size_t ii = 0; ii < nn; ++ii) v += w[ii] * values[nb[ii]];
+      for (size_t q = 0; q < dimm; ++q) red += w[q] * b0[q];
+      *lagrange = w[nn];
+    }
+    *value = v;
+    *variance = fmax_(cbb - red, 0.0);
+    return OR_OK;
+  }
 };
 
 // kriging.rs:262-408 Kriging::build (plus the three constructors).
@@ -2447,6 +2520,57 @@ int or_vecchia_mle_nm(int dim, int64_t n, const double* coords, const double* va
   for (int i = 0; i < 3; ++i) x_out[i] = r.first[i];
   *f_out = r.second;
   if (n_evals) *n_evals = evals;
+  return OR_OK;
+}
+
+// Kriging::predict_block for nc blocks sharing one discretisation, with
+// predict_block's own checks (kriging.rs:678-700) first.
+int or_krige_block(int dim, int64_t n, const double* coords, const double* values,
+                   const double* meas_err, int ctor, const or_model* model, const or_kcfg* cfg,
+                   int64_t nc, const double* centers, const double* offsets, int64_t noff,
+                   double* value, double* variance, double* lagrange, int8_t* status) {
+  Predictor P;
+  int rc = build_predictor(P, dim, (size_t)n, coords, values, nullptr, meas_err, ctor, *model, *cfg);
+  if (rc) return rc;
+  if (cfg->method != 0 && cfg->method != 1)
+    return fail(OR_INVALID_PARAMETER, "block kriging supports simple and ordinary kriging only");
+  if (has_power(*model)) return fail(OR_INVALID_PARAMETER, "block kriging with a Power model");
+  if (noff <= 0) return fail(OR_INVALID_PARAMETER, "block discretization needs at least one point");
+  for (int64_t t = 0; t < nc; ++t) {
+    double v = kNaN, var = kNaN, lag = kNaN;
+    int st = P.predict_block(&centers[t * dim], offsets, (size_t)noff, &v, &var, &lag);
+    if (st != OR_OK) v = var = lag = kNaN;
+    value[t] = v;
+    variance[t] = var;
+    lagrange[t] = lag;
+    status[t] = (int8_t)st;
+  }
+  return OR_OK;
+}
+
+// validation.rs:298-328 spatial_block_assignment.
+int or_spatial_block_assignment(int dim, int64_t n, const double* coords, const int64_t* bpd,
+                                int64_t* fold_of) {
+  double lo[3], hi[3];
+  for (int d = 0; d < dim; ++d) lo[d] = hi[d] = coords[d];
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < dim; ++d) {
+      lo[d] = fmin_(lo[d], coords[i * dim + d]);
+      hi[d] = fmax_(hi[d], coords[i * dim + d]);
+    }
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t idx = 0, stride = 1;
+    for (int d = 0; d < dim; ++d) {
+      const double span = fmax_(hi[d] - lo[d], kMinPositive);
+      double frac = (coords[i * dim + d] - lo[d]) / span;
+      frac = frac < 0.0 ? 0.0 : (frac > 1.0 - 1e-12 ? 1.0 - 1e-12 : frac);
+      int64_t bd = (int64_t)(frac * (double)bpd[d]);
+      if (bd > bpd[d] - 1) bd = bpd[d] - 1;
+      idx += bd * stride;
+      stride *= bpd[d];
+    }
+    fold_of[i] = idx;
+  }
   return OR_OK;
 }
 

@@ -156,6 +156,15 @@ int or_vecchia_mle_nm(int dim, int64_t n, const double* coords, const double* va
                       int64_t nstarts, const double* starts, double step, int64_t max_iter,
                       double* x_out, double* f_out, int64_t* n_evals);
 
+/* kriging.rs:674-779 Kriging::predict_block for nc blocks sharing offsets
+ * (noff x dim); per-block status as or_krige. */
+int or_krige_block(int dim, int64_t n, const double* coords, const double* values,
+                   const double* meas_err, int ctor, const or_model* model, const or_kcfg* cfg,
+                   int64_t nc, const double* centers, const double* offsets, int64_t noff,
+                   double* value, double* variance, double* lagrange, int8_t* status);
+/* validation.rs:298-328 spatial_block_assignment (fold index per point). */
+int or_spatial_block_assignment(int dim, int64_t n, const double* coords, const int64_t* bpd,
+                                int64_t* fold_of);
 /* vecchia.rs:1181-1233 poly_basis (row-major n x p, p = or_poly_basis_terms)
  * and vecchia.rs:1246-1272 standardized_drift_basis (n x (1 + ncov)). */
 int64_t or_poly_basis_terms(int dim, int32_t degree);

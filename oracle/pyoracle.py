@@ -117,6 +117,9 @@ def _declare(L):
         "or_vecchia_mle_setup": (C.c_int, [C.c_int, i64, pd, pd, pd, pd]),
         "or_vecchia_mle_nm": (C.c_int, [C.c_int, i64, pd, pd, i32, d, i64, pi64, i64, pd, d, i64,
                                         pd, pd, pi64]),
+        "or_krige_block": (C.c_int, [C.c_int, i64, pd, pd, pd, C.c_int, pm, pk, i64, pd, pd, i64,
+                                     pd, pd, pd, pi8]),
+        "or_spatial_block_assignment": (C.c_int, [C.c_int, i64, pd, pi64, pi64]),
         "or_poly_basis_terms": (i64, [C.c_int, i32]),
         "or_poly_basis": (C.c_int, [C.c_int, i64, pd, i32, pd]),
         "or_drift_basis": (C.c_int, [i64, i64, pd, pd]),
@@ -326,6 +329,37 @@ def krige(coords, values, model, targets, *, method="ordinary", mean=None, degre
                boundary_ties=ties.value)
     if kcap:
         out["neighbors"] = nbo[:nt * kcap].reshape(nt, kcap)
+    return out
+
+
+def krige_block(coords, values, model, centers, offsets, *, method="ordinary", mean=None,
+                max_neighbors=None, min_neighbors=None, max_per_octant=None, radius=None,
+                anisotropic_search=None, measurement_error=None):
+    """Kriging::predict_block (kriging.rs:674-779) at each centre."""
+    coords, values, centers = _f64(coords), _f64(values), _f64(centers)
+    dim = coords.shape[1]
+    offsets = _f64(offsets).reshape(-1, dim)
+    nc = len(centers)
+    cfg = kcfg_struct(method, mean, 1, 0, max_neighbors, min_neighbors, max_per_octant, radius,
+                      anisotropic_search)
+    m = model_struct(model)
+    value, var, lag = np.zeros(nc), np.zeros(nc), np.zeros(nc)
+    status = np.zeros(nc, dtype=np.int8)
+    me = _f64(measurement_error) if measurement_error is not None else None
+    _check(lib().or_krige_block(dim, len(coords), _p(coords), _p(values), _p(me),
+                                2 if me is not None else 0, C.byref(m), C.byref(cfg), nc,
+                                _p(centers), _p(offsets), len(offsets), _p(value), _p(var),
+                                _p(lag), _p(status, C.c_int8)))
+    return dict(value=value, variance=var, lagrange=lag, status=status)
+
+
+def spatial_block_assignment(coords, blocks_per_dim):
+    """validation.rs:298-328: the block (fold) index of every point."""
+    coords = _f64(coords)
+    bpd = np.ascontiguousarray(blocks_per_dim, dtype=np.int64)
+    out = np.zeros(len(coords), dtype=np.int64)
+    _check(lib().or_spatial_block_assignment(coords.shape[1], len(coords), _p(coords),
+                                             _p(bpd, C.c_int64), _p(out, C.c_int64)))
     return out
 
 

@@ -634,3 +634,89 @@ def test_vecchia_mle_grouped_matches_ungrouped_under_full_conditioning():
     assert abs(xu[0] ** 2 - xg[0] ** 2) < 1e-4
     assert abs(math.exp(xu[1]) - math.exp(xg[1])) < 1e-3
     assert abs(math.exp(xu[2]) - math.exp(xg[2])) < 1e-2
+
+
+# ------------------------------------------------------- block kriging -------
+def _block_offsets(size, n):
+    # kriging.rs:815-838 block_offsets
+    return np.array([[((ix + 0.5) / n[0] - 0.5) * size[0], ((iy + 0.5) / n[1] - 0.5) * size[1]]
+                     for iy in range(n[1]) for ix in range(n[0])])
+
+
+def test_block_kriging_averages_point_predictions():
+    # kriging.rs:1525-1567: with a global neighbourhood the block BLUP is the
+    # mean of the point BLUPs, and the block variance is below the point's
+    c, v = sample_data()
+    m = sph_model()
+    ctr = np.array([[0.6, 0.4]])
+    off = _block_offsets([0.4, 0.4], [4, 4])
+    blk = O.krige_block(c, v, m, ctr, off)
+    assert blk["status"][0] == 0
+    pts = O.krige(c, v, m, ctr + off)
+    assert abs(blk["value"][0] - pts["value"].mean()) < 1e-10
+    assert blk["variance"][0] < O.krige(c, v, m, ctr)["variance"][0]
+    with pytest.raises(O.OracleError):
+        O.krige_block(c, v, m, ctr, off, method="universal")
+
+
+def test_power_model_rejects_block_kriging():
+    # kriging.rs:1314-1322
+    c, v = sample_data()
+    m = VariogramModel(0.0, [Structure("power", 1.0, 1.0, param=1.0)])
+    with pytest.raises(O.OracleError):
+        O.krige_block(c, v, m, [[0.5, 0.5]], [[0.0, 0.0], [0.1, 0.0], [0.0, 0.1], [0.1, 0.1]])
+
+
+def _smooth_field(n, seed, period=20.0):
+    # validation.rs:991-1002 smooth_field
+    u, _ = O.rng_draw(seed, 2 * n, 0)
+    c = u.reshape(n, 2) * 100.0
+    return c, np.sin(c[:, 0] / period) + np.cos(c[:, 1] / period)
+
+
+def _oracle_fold_cv(c, v, m, fold_of):
+    # cv_with_folds (validation.rs:219-265): a predictor per fold on the rest
+    pred, var = np.empty(len(c)), np.empty(len(c))
+    for f in np.unique(fold_of):
+        tr, te = fold_of != f, fold_of == f
+        r = O.krige(c[tr], v[tr], m, c[te])
+        assert (r["status"] == 0).all()
+        pred[te], var[te] = r["value"], r["variance"]
+    return pred, var
+
+
+def test_spatial_block_assignment():
+    # validation.rs:298-328: dimension 0 fastest, the maxima in the last block
+    c = np.array([[0.0, 0.0], [10.0, 0.0], [0.0, 10.0], [10.0, 10.0], [4.9, 5.1], [2.6, 7.4]])
+    f = O.spatial_block_assignment(c, [2, 2])
+    assert list(f) == [0, 1, 2, 3, 2, 2]
+    f = O.spatial_block_assignment(c, [4, 1])
+    assert list(f) == [0, 3, 0, 3, 1, 1]
+
+
+def test_block_cv_covers_every_point_and_has_skill():
+    # validation.rs:1052-1067
+    from geostat_rs.api import CvResult
+    c, v = _smooth_field(120, 7)
+    m = VariogramModel(0.01, [Structure("spherical", 1.0, 50.0)])
+    pred, var = _oracle_fold_cv(c, v, m, O.spatial_block_assignment(c, [4, 4]))
+    assert np.isfinite(pred).all() and (np.isfinite(var) & (var >= 0)).all()
+    assert CvResult(v, pred, var).vecv() > 0.0
+
+
+def test_block_cv_is_harsher_than_random_k_fold():
+    # validation.rs:1070-1097
+    from geostat_rs.api import CvResult
+    c, v = _smooth_field(150, 3, period=200.0)
+    v = np.sin(c[:, 0] / 200.0) + np.cos(c[:, 1] / 200.0)
+    m = VariogramModel(0.0, [Structure("spherical", 1.0, 300.0)])
+    order = np.arange(150)
+    u = O.rng_u64(1, 150)
+    for idx, i in enumerate(range(149, 0, -1)):
+        j = int(u[idx] % np.uint64(i + 1))
+        order[i], order[j] = order[j], order[i]
+    kf = np.empty(150, dtype=int)
+    kf[order] = np.arange(150) % 10
+    rnd = CvResult(v, *_oracle_fold_cv(c, v, m, kf))
+    blk = CvResult(v, *_oracle_fold_cv(c, v, m, O.spatial_block_assignment(c, [5, 5])))
+    assert blk.rmse() >= rnd.rmse()
