@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "geostat_rs", "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgeostat_gb300.so")
 SOURCES = ["gs_host.cu", "gs_search.cu", "gs_krige.cu", "gs_api.cu", "gs_noalloc.cu", "gs_serve.cu", "gs_vecchia.cu",
-           "gs_synth.cu", "gs_probe.cu"]
+           "gs_synth.cu", "gs_probe.cu", "gs_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
          "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
@@ -48,13 +48,13 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
         if _needs(o, [s] + headers) or ptxas_info:
             cmd = [nvcc, *ARCH, *FLAGS, "-c", s, "-o", o]
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append((src, cmd))
-    objs = [os.path.join(OBJ_DIR, s.replace(".cu", ".o")) for s in SOURCES]
+    objs = [os.path.join(OBJ_DIR, os.path.splitext(s)[0] + ".o") for s in SOURCES]
 
     def run(job):
         name, cmd = job

@@ -5,9 +5,13 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <string>
 #include <vector>
 
 namespace gs {
+
+// Records `msg` as this thread's last error (gs_last_error) and returns code.
+int fail(int code, const std::string& msg);
 
 // Counts kernels this library launched (reported by gs_launch_count).
 void count_launch(int n);

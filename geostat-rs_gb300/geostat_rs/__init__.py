@@ -7,7 +7,7 @@ configuration and entry points (``krige``, ``krige_grid``, ``krige_3d``,
 libgeostat_gb300.so through its C ABI.
 """
 from .errors import (CudaError, DimensionMismatch, DuplicatePoints, GeostatError,
-                     InsufficientData, InvalidParameter, NoNeighbors, OutOfDeviceMemory,
+                     InsufficientData, InvalidParameter, IoError, NoNeighbors, OutOfDeviceMemory,
                      SingularSystem)
 from .model import Anisotropy, Structure, VariogramModel, parse_kind
 from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Server, TuneResult,
@@ -19,6 +19,7 @@ from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Ser
                   vecchia_krige, vecchia_loglik, vecchia_loglik_grouped, vecchia_mle, vecchia_mle_fit,
                   vecchia_mle_grouped_fit, vecchia_mle_nm_fit, vecchia_predict, vecchia_reml,
                   vecchia_reml_drift, vecchia_reml_drift_fit, vecchia_reml_fit)
+from . import io  # geostat_rs.gpkg (sqlite3) is imported on use
 from ._abi import LIB_PATH, load as load_library
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -100,6 +100,11 @@ SIGNATURES = {
     "gs_vecchia_mle": (_int, [_vp, _i32, _i64, _pi64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_mle_nm": (_int, [_vp, _i32, _i64, _pi64, _i64, _pd, _d, _i64, _pm, _pd, _pd, _pi64]),
     "gs_vecchia_loglik_grad_batch": (_int, [_vp, _i64, _pm, _pd, _pd, _pi32, _int, _vp]),
+    "gs_csv_read": (_int, [C.c_char_p, C.POINTER(C.c_char_p), _int, _int, C.POINTER(_vp)]),
+    "gs_csv_table_info": (_int, [_vp, _pi64, _pi64]),
+    "gs_csv_table_copy": (_int, [_vp, _pd]),
+    "gs_csv_table_destroy": (None, [_vp]),
+    "gs_csv_write": (_int, [C.c_char_p, C.c_char_p, _int, C.POINTER(_pd), _i64, _int]),
     "gs_kriging_block_cv": (_int, [_vp, _pi64, _pd, _pd, _pu8, _int]),
     "gs_block_offsets": (_int, [_pd, _pi64, _pd]),
     "gs_kriging_predict_block": (_int, [_vp, _i64, _pd, _pd, _pd, _pd, _i64, _pd, _pd, _pd, _pu8,

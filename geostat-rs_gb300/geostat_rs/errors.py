@@ -46,9 +46,14 @@ class OutOfDeviceMemory(RuntimeError):
     code = 101
 
 
+class IoError(OSError):
+    """File input/output (the geostat CLI's I/O errors)."""
+    code = 102
+
+
 _BY_CODE = {c.code: c for c in (InsufficientData, DimensionMismatch, SingularSystem,
                                 InvalidParameter, NoNeighbors, DuplicatePoints, CudaError,
-                                OutOfDeviceMemory)}
+                                OutOfDeviceMemory, IoError)}
 
 
 def raise_for(code: int, message: str):

@@ -38,7 +38,8 @@ enum {
   GS_ERR_NO_NEIGHBORS = 5,
   GS_ERR_DUPLICATE_POINTS = 6,
   GS_ERR_CUDA = 100,
-  GS_ERR_OUT_OF_MEMORY = 101
+  GS_ERR_OUT_OF_MEMORY = 101,
+  GS_ERR_IO = 102 /* file input/output (the CLI's anyhow errors) */
 };
 
 /* ModelKind (crates/geostat-core/src/variogram/model.rs:50-101).  The CUDA
@@ -413,6 +414,24 @@ int gs_probe_fma_tflops(int precision, double* tflops);
  * exp on the device; 0 for x >= 708), for accuracy checks. */
 int gs_probe_expneg(int64_t n, const double* x, double* out);
 int64_t gs_launch_count(void);
+
+/* CSV input and output (crates/geostat-cli/src/io_utils.rs), host only.
+ * gs_csv_read reads the named numeric columns of a CSV file (header row,
+ * csv crate 1.4.0 quoting) into a table, skipping rows where a requested
+ * field is empty, "na", "nan" or not a number (io_utils.rs:12-18, 37-75);
+ * a missing column is InvalidParameter naming the available ones, a record
+ * whose field count differs from the header's is GS_ERR_IO.  nthreads <= 0
+ * uses the host's threads.  gs_csv_write writes `header` then nrows rows of
+ * ncols columns, each number as Rust's Display for f64 prints it (shortest
+ * round-trip digits, no exponent, NaN / inf / -inf). */
+typedef struct gs_csv_table gs_csv_table;
+int gs_csv_read(const char* path, const char* const* cols, int ncols, int nthreads,
+                gs_csv_table** out);
+int gs_csv_table_info(const gs_csv_table* t, int64_t* rows, int64_t* skipped);
+int gs_csv_table_copy(const gs_csv_table* t, double* out); /* rows x ncols, row-major */
+void gs_csv_table_destroy(gs_csv_table* t);
+int gs_csv_write(const char* path, const char* header, int ncols, const double* const* columns,
+                 int64_t nrows, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -641,3 +641,60 @@ def test_field_3d(n, seed):
     c, v = np.zeros(n * 3), np.zeros(n)
     lib().or_test_field_3d(n, C.c_uint64(seed), _p(c), _p(v))
     return c.reshape(n, 3), v
+
+
+# ------------------------------------------------------------ CSV I/O ------
+# crates/geostat-cli/src/io_utils.rs, restated with Python's csv module (the
+# csv crate's RFC 4180 quoting) and the reference's field rules.  Pure Python:
+# the checker for the native reader and writer.
+def parse_field(s):
+    """io_utils.rs:12-18 parse_field: None for empty / na / nan (any case) or
+    text Rust's f64::from_str rejects."""
+    import re
+    s = s.strip()
+    if not s or s.lower() in ("na", "nan"):
+        return None
+    body = s[1:] if s[:1] in "+-" else s
+    if body.lower() in ("inf", "infinity"):
+        return float(s[0] + "inf") if s[:1] == "-" else float("inf")
+    if not re.fullmatch(r"(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?", body):
+        return None
+    return float(s)
+
+
+def csv_read(path, cols):
+    """io_utils.rs:37-75: (rows x len(cols) array, skipped count); raises
+    KeyError for a missing column."""
+    import csv
+    with open(path, newline="", encoding="utf-8-sig") as f:
+        recs = [r for r in csv.reader(f) if r]
+    header = recs[0]
+    idx = []
+    for c in cols:
+        if c not in header:
+            raise KeyError(f"column '{c}' not found; available columns: {', '.join(header)}")
+        idx.append(header.index(c))
+    rows, skipped = [], 0
+    for r in recs[1:]:
+        if len(r) != len(header):
+            raise ValueError("unequal record length")
+        vals = [parse_field(r[i]) for i in idx]
+        if any(v is None for v in vals):
+            skipped += 1
+            continue
+        rows.append(vals)
+    return np.array(rows, dtype=float).reshape(-1, len(cols)), skipped
+
+
+def rust_display(x):
+    """Rust's `{}` for f64: shortest round-trip digits, never an exponent."""
+    from decimal import Decimal
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return "inf" if x > 0 else "-inf"
+    s = format(Decimal(repr(x)), "f")
+    if "." in s:
+        s = s.rstrip("0").rstrip(".")
+    return s

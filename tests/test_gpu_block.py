@@ -149,3 +149,28 @@ def test_block_cv_rejects_bad_config():
     with pytest.raises(G.InvalidParameter):
         G.block_cv(ps, m, G.KrigingConfig(), [1, 1])
     G.block_cv(ps, m, G.KrigingConfig(), [3, 3])
+
+
+def test_csv_end_to_end(tmp_path):
+    """io_utils.rs read_points / read_targets / write_estimates_csv around a
+    kriging run: the file written is the oracle's estimates, formatted as
+    Rust prints them."""
+    from geostat_rs import io as gio
+    c = uniform_points(1500, 2, 305, [1000.0, 1000.0])
+    v = smooth_values(c)
+    t = uniform_points(400, 2, 306, [1000.0, 1000.0])
+    gio.write_csv(tmp_path / "pts.csv", "east,north,grade", [c[:, 0], c[:, 1], v])
+    with open(tmp_path / "tg.csv", "w") as f:
+        f.write("x,y\n" + "".join(f"{a!r},{b!r}\n" for a, b in t))
+    ps = gio.read_points(tmp_path / "pts.csv", "east", "north", "grade")
+    assert np.array_equal(ps.coords, c) and np.array_equal(ps.values, v)
+    tg, _ = gio.read_targets(tmp_path / "tg.csv", "x", "y")
+    m = cfg1_model()
+    k = G.Kriging.new(ps, m, G.KrigingConfig(max_neighbors=16))
+    val, var = k.predict_many(tg)
+    gio.write_estimates_csv(tmp_path / "out.csv", tg, val, var)
+    ref = O.krige(c, v, m, t, max_neighbors=16)
+    back = gio._read_columns(tmp_path / "out.csv", ["x", "y", "prediction", "variance"], "rows")
+    assert np.array_equal(back[:, 0], t[:, 0]) and np.array_equal(back[:, 1], t[:, 1])
+    assert_close(back[:, 2], ref["value"], float(np.mean(np.abs(v))), 1e-9, "csv value")
+    assert_close(back[:, 3], ref["variance"], 1e-3 * m.total_sill(), 1e-9, "csv variance")
