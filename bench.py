@@ -287,6 +287,7 @@ def run_ours(args, rank, world):
                                            fp64_v, kr, log)
         cvr = cv_bench(args, coords, values, model, log) if args.cv_sample > 0 else None
         glb = global_bench(args, log) if not args.no_global else None
+        blk = block_bench(args, log) if not args.no_block else None
         vec = vecchia_bench(args, log) if not args.no_vecchia else None
         clu = clustered_bench(args, log) if not args.no_clustered else None
         serve = serving_bench(args, log) if args.serve_requests > 0 else None
@@ -339,6 +340,8 @@ def run_ours(args, rank, world):
             result["cross_validation"] = cvr
         if glb is not None:
             result["global_neighbourhood"] = glb
+        if blk is not None:
+            result["block_kriging"] = blk
         if serve is not None:
             result["serving"] = serve
             result["p99_latency_ms"] = serve["p99_ms"]
@@ -470,6 +473,49 @@ def global_bench(args, log):
             "max_rel_variance": rel(out.variance, ref["variance"], 1e-3)}
 
 
+def block_bench(args, log):
+    """Block kriging (kriging.rs:674-838): 2-D ordinary kriging of 100,000
+    points (uniform in 10 x 10 km, 10 + field, nugget 0.1 + Sph(1, 1500 m)),
+    32 nearest neighbours, 20 x 20 m blocks discretised 4 x 4 at every cell of
+    a 512 x 512 grid (predict_block_grid); the oracle's predict_block on a
+    sample of 2,000 blocks on all host cores."""
+    import geostat_rs as G
+    from geostat_rs.model import Structure, VariogramModel
+    n = 100_000
+    c = G.rng_uniform(SEED + 41, 2 * n).reshape(n, 2) * 10000.0
+    m = VariogramModel(0.1, [Structure("spherical", 1.0, 1500.0)])
+    v = 10.0 + G.rff_field(c, m, 2048, SEED + 42)
+    k = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig(max_neighbors=32))
+    lo, hi, nc, bs, disc = [0.0, 0.0], [10000.0, 10000.0], [512, 512], [20.0, 20.0], [4, 4]
+    k.predict_block_grid(lo, hi, nc, bs, disc)
+    ts = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        val, var = k.predict_block_grid(lo, hi, nc, bs, disc)
+        ts.append(time.perf_counter() - t1)
+    dt = statistics.median(ts)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    from geostat_rs.io import grid_centers
+    cen = grid_centers(lo, hi, nc)
+    pick = np.sort(np.random.default_rng(SEED).choice(len(cen), 2000, replace=False))
+    off = G.block_offsets(bs, disc)
+    t1 = time.perf_counter()
+    ref = O.krige_block(c, v, m, cen[pick], off, max_neighbors=32)
+    dcpu = time.perf_counter() - t1
+    vs = float(np.mean(np.abs(v)))
+    rel = lambda a, b, f: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), f)))
+    nb = int(np.prod(nc))
+    log(f"[bench] block kriging: {nb} blocks (4 x 4 points) in {dt * 1e3:.1f} ms; oracle "
+        f"{len(pick)} blocks in {dcpu:.2f} s")
+    return {"blocks": nb, "discretisation": "4x4", "data": n, "max_neighbors": 32,
+            "seconds": dt, "blocks_per_s": nb / dt, "includes": "grid centres, search, FP64 "
+            "block systems, copies", "cpu_blocks_per_s": len(pick) / dcpu, "cpu_cores": 1,
+            "cpu_kind": "port (predict_block per block)",
+            "max_rel_value": rel(val[pick], ref["value"], vs),
+            "max_rel_variance": rel(var[pick], ref["variance"], 1e-3)}
+
+
 def vecchia_bench(args, log):
     """Vecchia log-likelihood: n = 2,000,000 points in [0,1]^2, m = 30, 16 candidates."""
     import geostat_rs as G
@@ -520,6 +566,44 @@ def vecchia_bench(args, log):
            "fp64_resolved_systems": resolved,
            "fp64_resolved_fraction": resolved / (n * len(cands)),
            "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
+    # Guinness-grouped likelihood (group size 8) and REML (linear trend), four
+    # candidates each, on the same plan; oracle check on a 20,000-point plan
+    g4 = cands[:4]
+    plan.loglik_grouped(g4, 8)
+    t1 = time.perf_counter()
+    llg, stg = plan.loglik_grouped(g4, 8)
+    dtg8 = time.perf_counter() - t1
+    plan.reml_loglik(g4, drift_degree=1)
+    t1 = time.perf_counter()
+    llr, str_ = plan.reml_loglik(g4, drift_degree=1)
+    dtr = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    llr8, _ = plan.reml_loglik(g4, drift_degree=1, group_size=8)
+    dtr8 = time.perf_counter() - t1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    small = G.VecchiaPlan(G.PointSet(c[:20000], v[:20000]), 30)
+    so, snb, scnt = small.arrays()
+    sg, _ = small.loglik_grouped(g4[:1], 8)
+    sr, _ = small.reml_loglik(g4[:1], drift_degree=1)
+    t1 = time.perf_counter()
+    og = O.vecchia_loglik_grouped(c[:20000], v[:20000], g4[0], so, snb, scnt, 8)
+    dto = time.perf_counter() - t1
+    orr = O.vecchia_reml_loglik(c[:20000], v[:20000], g4[0], so, snb, scnt,
+                                O.poly_basis(c[:20000], 1), 1)
+    out["grouped"] = {"group_size": 8, "candidates": len(g4),
+                      "points_per_s": n * len(g4) / dtg8, "batch_ms": dtg8 * 1e3,
+                      "status_ok": bool((stg == 0).all()),
+                      "over_ungrouped_ll": float(np.max(llg - ll[:4])),
+                      "cpu_points_per_s": 20000 / dto, "cpu_cores": 1,
+                      "oracle_check_rel": float(abs(sg[0] - og) / abs(og))}
+    out["reml"] = {"drift_degree": 1, "candidates": len(g4),
+                   "points_per_s": n * len(g4) / dtr, "batch_ms": dtr * 1e3,
+                   "grouped8_points_per_s": n * len(g4) / dtr8,
+                   "status_ok": bool((str_ == 0).all()),
+                   "oracle_check_rel": float(abs(sr[0] - orr) / abs(orr))}
+    log(f"[bench] vecchia grouped(8) {dtg8 * 1e3:.0f} ms, REML {dtr * 1e3:.0f} ms, "
+        f"REML grouped(8) {dtr8 * 1e3:.0f} ms for {len(g4)} candidates")
     # joint prediction at args.vpred_n targets conditioning on the same data (m = 30)
     if args.vpred_n > 0:
         nt = args.vpred_n
@@ -931,6 +1015,7 @@ def main():
     ap.add_argument("--no-vecchia", action="store_true")
     ap.add_argument("--no-clustered", action="store_true",
                     help="skip the clustered uneven workload")
+    ap.add_argument("--no-block", action="store_true", help="skip the block-kriging leg")
     ap.add_argument("--no-global", action="store_true",
                     help="skip the global-neighbourhood leg")
     ap.add_argument("--cv-sample", type=int, default=40,
