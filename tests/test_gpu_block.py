@@ -161,7 +161,7 @@ def test_csv_end_to_end(tmp_path):
     t = uniform_points(400, 2, 306, [1000.0, 1000.0])
     gio.write_csv(tmp_path / "pts.csv", "east,north,grade", [c[:, 0], c[:, 1], v])
     with open(tmp_path / "tg.csv", "w") as f:
-        f.write("x,y\n" + "".join(f"{a!r},{b!r}\n" for a, b in t))
+        f.write("x,y\n" + "".join(f"{float(a)!r},{float(b)!r}\n" for a, b in t))
     ps = gio.read_points(tmp_path / "pts.csv", "east", "north", "grade")
     assert np.array_equal(ps.coords, c) and np.array_equal(ps.values, v)
     tg, _ = gio.read_targets(tmp_path / "tg.csv", "x", "y")
