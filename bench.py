@@ -1001,6 +1001,18 @@ def profile_case(args):
         for _ in range(2):
             ll, st = plan.loglik(cands)
         print(f"profile vecchia: {n} points, loglik[0] {ll[0]:.6f}")
+    if args.profile_reml:
+        from geostat_rs.model import Structure, VariogramModel
+        n = args.profile_reml
+        c = G.rng_uniform(SEED + 5, 2 * n).reshape(n, 2)
+        base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
+        v = 0.5 + G.rff_field(c, base, 1024, SEED + 6)
+        plan = G.VecchiaPlan(G.PointSet(c, v), 30)
+        cands = [VariogramModel(0.02 * (1 + 0.05 * i), [Structure("matern25", 1.0, 0.05)])
+                 for i in range(4)]
+        for _ in range(2):
+            ll, st = plan.reml_loglik(cands, drift_degree=1)
+        print(f"profile reml: {n} points, loglik[0] {ll[0]:.6f}")
 
 
 def main():
@@ -1036,6 +1048,9 @@ def main():
                          "grid targets and exit")
     ap.add_argument("--profile-vecchia", type=int, default=0,
                     help="run one 16-candidate Vecchia batch on N points and exit")
+    ap.add_argument("--profile-reml", type=int, default=0,
+                    help="run a 4-candidate Vecchia REML batch (linear trend) on N points "
+                         "and exit")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -1043,7 +1058,7 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
-    if args.profile_case or args.profile_vecchia or args.profile_clustered:
+    if args.profile_case or args.profile_vecchia or args.profile_clustered or args.profile_reml:
         profile_case(args)
         return
     if args.impl == "reference":

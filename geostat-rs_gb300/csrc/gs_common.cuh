@@ -403,4 +403,15 @@ __device__ __forceinline__ void rho_df2(int kind, df d0, df d1, const ExpTable& 
   }
 }
 
+// 1/d to FP64 accuracy: FP32 estimate, two Newton steps (e = 1 - d r,
+// r += r e).  sc (a power of two) scales d into FP32's range first when the
+// system's scale is outside [1e-20, 1e20] (scaled = true).
+__device__ __forceinline__ double rcp_fp64(double d, double sc, bool scaled) {
+  double r = scaled ? (double)__frcp_rn((float)(d * sc)) * sc : (double)__frcp_rn((float)d);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 }  // namespace gs

@@ -581,16 +581,6 @@ __host__ __device__ inline CholLayout chol_layout(int Mmax, int dim) {
   return L;
 }
 
-// 1/d to FP64 accuracy: FP32 estimate, two Newton steps (e = 1 - d r,
-// r += r e).  sc (a power of two) scales d into FP32's range first when the
-// system's scale is outside [1e-20, 1e20] (scaled = true).
-__device__ __forceinline__ double rcp_fp64(double d, double sc, bool scaled) {
-  double r = scaled ? (double)__frcp_rn((float)(d * sc)) * sc : (double)__frcp_rn((float)d);
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
-  return fma(r, e, r);
-}
 
 // Warp-private neighbour slots of the FP64 re-solve kernels: slot s holds
 // data point sidx[s] (or -1), its coordinates P[d * NS + s] and, in global

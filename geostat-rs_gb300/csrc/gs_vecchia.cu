@@ -53,6 +53,12 @@ struct gs_vecchia_plan {
     int64_t* d_off = nullptr;
     int32_t* d_vid = nullptr;
     int32_t* d_slen = nullptr;
+    // blocks of more than one member: their indices, the largest of their
+    // sets, and per ordered position whether it belongs to one of them
+    int64_t nmulti = 0;
+    int vmax_multi = 0;
+    int64_t* d_multi = nullptr;
+    uint8_t* d_in_multi = nullptr;
   };
   mutable std::mutex groups_mu;
   mutable std::map<int64_t, Groups> groups;
@@ -61,6 +67,8 @@ struct gs_vecchia_plan {
       cudaFree(g.second.d_off);
       cudaFree(g.second.d_vid);
       cudaFree(g.second.d_slen);
+      cudaFree(g.second.d_multi);
+      cudaFree(g.second.d_in_multi);
     }
     cudaFree(d_order);
     cudaFree(d_nb);
@@ -606,7 +614,8 @@ struct GroupArgs {
   const int64_t* off;
   const int32_t* vid;
   const int32_t* slen;
-  int64_t nblocks;
+  int64_t nblocks;      // blocks evaluated (the list's length when blist is set)
+  const int64_t* blist; // the blocks to evaluate, or null for all
   int vmax;             // frame size: the largest set + the data rows
   int nr;               // data rows: 1, or 1 + p for REML
   const double* basis;  // REML: p x n trend basis, column-major; else null
@@ -620,8 +629,19 @@ __host__ __device__ inline size_t group_warp_doubles(int vmax) {
 __host__ __device__ inline int reml_sums(int p) { return 2 + p + p * (p + 1) / 2; }
 
 template <int D, bool REML>
-__global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cstat) {
+__global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cstat,
+                                     Exp64Table et_g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Exp64Table et;  // the table-driven FP64 exp of the covariances
+  for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+    et.hi[q] = et_g.hi[q];
+    et.lo[q] = et_g.lo[q];
+  }
+  if (threadIdx.x == 0) {
+    et.l1 = et_g.l1;
+    et.l2 = et_g.l2;
+    et.inv = et_g.inv;
+  }
   const int Vmax = g.vmax;
   uint32_t* ptab = reinterpret_cast<uint32_t*>(smem_raw);
   const size_t ptab_bytes = (((size_t)Vmax * (Vmax - 1) / 2) * 4 + 15) & ~(size_t)15;
@@ -642,7 +662,8 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
   const double* xs[3] = {a.x, a.y, a.z};
   for (int64_t it = (int64_t)blockIdx.x * wpb + warp; it < items; it += nw) {
     const int c = (int)(it / g.nblocks);
-    const int64_t b = it % g.nblocks;
+    const int64_t bi = it % g.nblocks;  // output slot
+    const int64_t b = g.blist ? g.blist[bi] : bi;
     const DevModel& mdl = a.models[c];
     const int32_t* ids = g.vid + g.off[b];
     const int vn = (int)(g.off[b + 1] - g.off[b]);
@@ -661,7 +682,7 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
         double h[3];
 #pragma unroll
         for (int d = 0; d < D; ++d) h[d] = xs[d][ids[q]] - xs[d][ids[r]];
-        v = cov_fp64<D>(mdl, h);
+        v = cov_fp64x<D>(mdl, h, et);
       }
       A[pk(o + r, o + q)] = v;
     }
@@ -681,6 +702,9 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
     }
     __syncwarp();
     const double tol = 1e-12 * fmax(mdl.c0, 2.2250738585072014e-308);
+    // pivots lie in [1e-12 c0, c0] (or at the 1e-12 clamp): scaled by a power
+    // of two near 1 / c0 they are in FP32's range for the reciprocal's seed
+    const double sc = ldexp(1.0, -ilogb(fmax(mdl.c0, 1e-300)));
     bool ok = true;
     for (int k = o; k < iz; ++k) {
       double dk = A[pk(k, k)];
@@ -690,7 +714,7 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
         ok = false;
         break;
       }
-      const double r = 1.0 / dk;
+      const double r = (g.clamp_member && k >= o + sl) ? 1.0 / dk : rcp_fp64(dk, sc, true);
       for (int i = k + 1 + lane; i < Vmax; i += 32) {
         const double v = A[pk(i, k)];
         lun[i] = v;
@@ -718,7 +742,7 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
         } else {
           atomicExch(&cstat[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
         }
-        a.terms[(int64_t)c * g.nblocks + b] = sum;
+        a.terms[(int64_t)c * g.nblocks + bi] = sum;
       }
     } else {
       // sums: [0] ln d, [1] a_z^2 / d, [2, 2 + p) a_f a_z / d, then a_f a_g / d
@@ -747,7 +771,7 @@ __global__ void vecchia_group_kernel(VArgs a, GroupArgs g, int wpb, int32_t* cst
             sum += w == 0 ? log(dt) : A[pk(iz + r1, o + t)] * A[pk(iz + r2, o + t)] / dt;
           }
         }
-        a.terms[((int64_t)c * W + w) * g.nblocks + b] = sum;
+        a.terms[((int64_t)c * W + w) * g.nblocks + bi] = sum;
       }
     }
     __syncwarp();
@@ -780,8 +804,16 @@ int reject_vecchia_model(const gs_model& m, int dim) {
 }  // namespace
 
 // Evaluates ncand candidates on a plan; ll[c] and status[c] per candidate.
+__global__ void exclude_terms_kernel(double* terms, int64_t n, int64_t ncand,
+                                     const uint8_t* exclude) {
+  const int64_t total = n * ncand;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (exclude[i % n]) terms[i] = 0.0;
+}
+
 int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
-                 int32_t* status, int precision, cudaStream_t s) {
+                 int32_t* status, int precision, cudaStream_t s, const uint8_t* exclude = nullptr) {
   const gs_pointset* ps = P->ps;
   const int dim = ps->dim;
   const int64_t n = P->n;
@@ -920,6 +952,11 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     count_launch(1);
   }
   GS_CUDA(cudaEventRecord(ev[3], s));
+  if (exclude) {
+    exclude_terms_kernel<<<152 * 8, 256, 0, s>>>((double*)terms.ptr, n, ncand, exclude);
+    GS_CUDA(cudaGetLastError());
+    count_launch(1);
+  }
   const int64_t chunk = 8192;
   const int nblk = (int)((n + chunk - 1) / chunk);
   GS_TRY(partial.alloc((size_t)nblk * ncand * 8, s));
@@ -1438,6 +1475,15 @@ static int build_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan
   }
   out->nblocks = (int64_t)blocks.size();
   out->vmax = vmax;
+  std::vector<int64_t> multi;
+  std::vector<uint8_t> in_multi(n, 0);
+  for (size_t b = 0; b < blocks.size(); ++b) {
+    if (blocks[b].second - blocks[b].first < 2) continue;
+    multi.push_back((int64_t)b);
+    out->vmax_multi = std::max(out->vmax_multi, (int)(off[b + 1] - off[b]));
+    for (int64_t k = blocks[b].first; k < blocks[b].second; ++k) in_multi[k] = 1;
+  }
+  out->nmulti = (int64_t)multi.size();
   if (cudaMalloc(&out->d_off, off.size() * 8) != cudaSuccess ||
       cudaMalloc(&out->d_vid, std::max<size_t>(vid.size(), 1) * 4) != cudaSuccess ||
       cudaMalloc(&out->d_slen, slen.size() * 4) != cudaSuccess)
@@ -1445,6 +1491,12 @@ static int build_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan
   GS_CUDA(cudaMemcpy(out->d_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice));
   GS_CUDA(cudaMemcpy(out->d_vid, vid.data(), vid.size() * 4, cudaMemcpyHostToDevice));
   GS_CUDA(cudaMemcpy(out->d_slen, slen.data(), slen.size() * 4, cudaMemcpyHostToDevice));
+  if (cudaMalloc(&out->d_multi, std::max<size_t>(multi.size(), 1) * 8) != cudaSuccess ||
+      cudaMalloc(&out->d_in_multi, (size_t)n) != cudaSuccess)
+    return fail(GS_ERR_OUT_OF_MEMORY, "grouped plan allocation failed");
+  if (!multi.empty())
+    GS_CUDA(cudaMemcpy(out->d_multi, multi.data(), multi.size() * 8, cudaMemcpyHostToDevice));
+  GS_CUDA(cudaMemcpy(out->d_in_multi, in_multi.data(), (size_t)n, cudaMemcpyHostToDevice));
   return GS_OK;
 }
 
@@ -1459,6 +1511,8 @@ int plan_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan::Groups
       cudaFree(fresh.d_off);
       cudaFree(fresh.d_vid);
       cudaFree(fresh.d_slen);
+      cudaFree(fresh.d_multi);
+      cudaFree(fresh.d_in_multi);
       return rc;
     }
     it = P->groups.emplace(gsize, fresh).first;
@@ -1474,7 +1528,7 @@ int plan_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan::Groups
 int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
                 const gs_vecchia_plan::Groups& G, int nr, const double* d_basis, bool clamp,
                 std::vector<double>& sums, int32_t* status, std::vector<int>& valid,
-                cudaStream_t s) {
+                cudaStream_t s, bool multi_only = false) {
   const gs_pointset* ps = P->ps;
   const int dim = ps->dim;
   const bool reml = d_basis != nullptr;
@@ -1495,13 +1549,20 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
     valid[c] = 1;
   }
   if (ncand == 0) return GS_OK;
-  const int frame = G.vmax + nr;
+  const int64_t nbl = multi_only ? G.nmulti : G.nblocks;
+  if (nbl == 0) {
+    for (int64_t c = 0; c < ncand; ++c)
+      if (valid[c]) sums.assign(sums.size(), 0.0);
+    return GS_OK;
+  }
+  const int frame = (multi_only ? G.vmax_multi : G.vmax) + nr;
   const size_t ptab_bytes = (((size_t)frame * (frame - 1) / 2) * 4 + 15) & ~(size_t)15;
   const size_t per_warp = group_warp_doubles(frame) * 8;
   int dev = 0, sms = 152, per_sm = 0, smem_max = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  smem_max -= 2048;  // the kernel's static shared memory (the exp table)
   if (frame > 255 || ptab_bytes + per_warp > (size_t)smem_max)
     return fail(GS_ERR_INVALID_PARAMETER,
                 "a grouped conditioning set of " + std::to_string(G.vmax) + " points with " +
@@ -1513,7 +1574,7 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
   GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
   GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
   const int64_t rows = ncand * per;
-  GS_TRY(terms.alloc((size_t)rows * G.nblocks * 8, s));
+  GS_TRY(terms.alloc((size_t)rows * nbl * 8, s));
   GS_TRY(cstat.alloc((size_t)ncand * 4, s));
   GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
   VArgs a{};
@@ -1528,25 +1589,27 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
   a.mean = P->mean;
   a.models = (const DevModel*)dmod.ptr;
   a.terms = (double*)terms.ptr;
-  GroupArgs g{G.d_off, G.d_vid, G.d_slen, G.nblocks, frame, nr, d_basis, clamp ? 1 : 0};
+  GroupArgs g{G.d_off, G.d_vid, G.d_slen, nbl, multi_only ? G.d_multi : nullptr, frame, nr,
+              d_basis, clamp ? 1 : 0};
   auto kern = reml ? (dim == 2 ? vecchia_group_kernel<2, true> : vecchia_group_kernel<3, true>)
                    : (dim == 2 ? vecchia_group_kernel<2, false> : vecchia_group_kernel<3, false>);
   GS_TRY(allow_dynamic_smem((const void*)kern, smem));
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * wpb, smem));
-  const int64_t items = ncand * G.nblocks;
+  const int64_t items = ncand * nbl;
   const int blocks = (int)std::max<int64_t>(
       1, std::min<int64_t>((items + wpb - 1) / wpb, (int64_t)sms * std::max(per_sm, 1)));
-  kern<<<blocks, 32 * wpb, smem, s>>>(a, g, wpb, (int32_t*)cstat.ptr);
+  ensure_vtables();
+  kern<<<blocks, 32 * wpb, smem, s>>>(a, g, wpb, (int32_t*)cstat.ptr, g_vet);
   GS_CUDA(cudaGetLastError());
   const int64_t chunk = 8192;
-  const int nblk = (int)((G.nblocks + chunk - 1) / chunk);
+  const int nblk = (int)((nbl + chunk - 1) / chunk);
   GS_TRY(partial.alloc((size_t)nblk * rows * 8, s));
   GS_TRY(out.alloc((size_t)rows * 8, s));
   int launches = 1;
   for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
     const int64_t nr_ = std::min<int64_t>(65535, rows - r0);
     reduce_terms<<<dim3(nblk, (unsigned)nr_), 256, 0, s>>>(
-        (double*)terms.ptr + r0 * G.nblocks, G.nblocks, chunk, (double*)partial.ptr + r0 * nblk);
+        (double*)terms.ptr + r0 * nbl, nbl, chunk, (double*)partial.ptr + r0 * nblk);
     ++launches;
   }
   reduce_partials<<<(int)((rows + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)rows,
@@ -1574,10 +1637,21 @@ int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model
   if (gsize <= 1) return vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s);
   gs_vecchia_plan::Groups G;
   GS_TRY(plan_groups(P, gsize, &G));
+  // A one-member block's term is the ungrouped term of its point (its joint
+  // set is the point's conditioning set): those go through the mixed
+  // ungrouped path, which leaves out the positions of larger blocks; the
+  // larger blocks run on the FP64 block kernel.
+  GS_TRY(vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s,
+                      G.nmulti ? G.d_in_multi : nullptr));
+  if (G.nmulti == 0) return GS_OK;
   std::vector<double> sums;
   std::vector<int> valid;
-  GS_TRY(eval_blocks(P, ncand, models, G, 1, nullptr, false, sums, status, valid, s));
-  for (int64_t c = 0; c < ncand; ++c) ll[c] = (valid[c] && status[c] == 0) ? sums[c] : NAN;
+  std::vector<int32_t> st2(ncand);
+  GS_TRY(eval_blocks(P, ncand, models, G, 1, nullptr, false, sums, st2.data(), valid, s, true));
+  for (int64_t c = 0; c < ncand; ++c) {
+    if (status[c] == 0 && st2[c] != 0) status[c] = st2[c];
+    ll[c] = (status[c] == 0) ? ll[c] + sums[c] : NAN;
+  }
   return GS_OK;
 }
 

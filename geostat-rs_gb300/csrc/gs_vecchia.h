@@ -9,8 +9,11 @@
 namespace gs {
 // Log-likelihood of ncand candidate models on a plan (one batched launch);
 // ll[c] and status[c] per candidate; synchronises `s` before returning.
+// exclude (device, per ordered position, or null): positions whose terms
+// are left out of the sums.
 int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
-                 int32_t* status, int precision, cudaStream_t s);
+                 int32_t* status, int precision, cudaStream_t s,
+                 const uint8_t* exclude = nullptr);
 // Points of the plan's data set.
 int64_t vecchia_plan_points(const gs_vecchia_plan* P);
 }  // namespace gs
