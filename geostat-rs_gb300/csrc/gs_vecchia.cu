@@ -33,6 +33,7 @@
 #include "gs_cta.cuh"
 #include "gs_solve.cuh"
 #include "gs_warp.cuh"
+#include "gs_vecchia.h"
 
 struct gs_vecchia_plan {
   const gs_pointset* ps = nullptr;
@@ -119,6 +120,13 @@ struct VArgs {
   const DevModel* models;  // device array of ncand models
   double* terms;           // ncand x n (position order)
   uint8_t* flag;           // ncand x n
+  // REML (reml_loglik_with_plan, vecchia.rs:1278-1345): the trend basis
+  // (p x n, column-major), and per (candidate, position) the record
+  // (var, r, g_0 .. g_{p-1}) at rec[(c * n + k) * (2 + p)], with r and g the
+  // raw value's and the basis rows' residuals after the conditioning solve
+  const double* basis;
+  int p;
+  double* rec;
 };
 
 constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
@@ -304,7 +312,7 @@ struct VWLayout {
   size_t off_a, off_h, off_v, off_b, off_h0, off_z, off_row, off_vec, off_xd, off_lt, total;
 };
 
-__host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim) {
+__host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim, int lt_width = 2) {
   VWLayout L;
   const int np = m * (m + 1) / 2;
   size_t o = 0;
@@ -322,7 +330,8 @@ __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim) {
   L.off_row = take(kWarpN * sizeof(float));
   L.off_vec = take(kWarpN * sizeof(float));
   L.off_xd = take(kWarpN * sizeof(df));
-  L.off_lt = take(2 * kWarpN * sizeof(double));  // (variance, residual) of 32 candidates
+  // (variance, residual[, basis residuals]) of 32 candidates
+  L.off_lt = take((size_t)lt_width * kWarpN * sizeof(double));
   L.total = o;
   return L;
 }
@@ -332,7 +341,7 @@ constexpr int kVWarps = 4;  // warps (ordered points in flight) per block
 // One warp per ordered point for conditioning sets of at most 32 points: the
 // same assembly and certification as vecchia_loglik_kernel, with the
 // register-row solver of gs_warp.cuh (no block barriers).
-template <int D>
+template <int D, bool REML>
 __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, ExpTable tab_g,
                                                                    DfConsts kc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -342,7 +351,8 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int M = a.m;
-  const VWLayout lay = vecchia_warp_layout(M, D);
+  const int LW = REML ? 2 + a.p : 2;  // doubles per candidate in LT
+  const VWLayout lay = vecchia_warp_layout(M, D, LW);
   unsigned char* base = smem_raw + (size_t)wib * lay.total;
   df* A = reinterpret_cast<df*>(base + lay.off_a);
   df* H = reinterpret_cast<df*>(base + lay.off_h);
@@ -361,8 +371,15 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
     __syncwarp();
     if (lane < cnt) {
       const int c = c0 + lane;
-      const double var = LT[2 * lane], r = LT[2 * lane + 1];
-      if (var >= 0.0) a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+      const double var = LT[LW * lane], r = LT[LW * lane + 1];
+      if (REML) {
+        if (var >= 0.0) {
+          double* rc = a.rec + ((int64_t)c * a.n + k) * LW;
+          for (int q = 0; q < LW; ++q) rc[q] = LT[LW * lane + q];
+        }
+      } else if (var >= 0.0) {
+        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+      }
       a.flag[(int64_t)c * a.n + k] = var >= 0.0 ? 0 : 1;
     }
     __syncwarp();
@@ -371,12 +388,20 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
   for (int64_t k = (int64_t)blockIdx.x * kVWarps + wib; k < a.n; k += nwarps) {
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
-    const df zi = df_sub(a.vdf[i], a.mean_df);
+    // REML works on the raw values (vecchia.rs:1296-1337)
+    const df zi = REML ? a.vdf[i] : df_sub(a.vdf[i], a.mean_df);
     if (s == 0) {
       const double z = df_to_double(zi);
       for (int c = lane; c < a.ncand; c += 32) {
         const double sill = a.models[c].c0;
-        a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + z * z / sill);
+        if (REML) {
+          double* rc = a.rec + ((int64_t)c * a.n + k) * LW;
+          rc[0] = sill;
+          rc[1] = z;
+          for (int q = 0; q < a.p; ++q) rc[2 + q] = a.basis[(int64_t)q * a.n + i];
+        } else {
+          a.terms[(int64_t)c * a.n + k] = -0.5 * (kLn2Pi + log(sill) + z * z / sill);
+        }
         a.flag[(int64_t)c * a.n + k] = 0;
       }
       continue;
@@ -389,7 +414,7 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
       const double* xs[3] = {a.x, a.y, a.z};
 #pragma unroll
       for (int d = 0; d < D; ++d) V[d * M + lane] = df_from_double(xs[d][j] - xs[d][i]);
-      ZV[lane] = df_sub(a.vdf[j], a.mean_df);
+      ZV[lane] = REML ? a.vdf[j] : df_sub(a.vdf[j], a.mean_df);
     }
     __syncwarp();
     if (a.iso_shared) {
@@ -436,7 +461,7 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
       __syncwarp();
       const bool ok = warp_solve(A, B, s, lane, W);
       if (!ok) {
-        if (lane == 0) LT[2 * (c & 31)] = -1.0;
+        if (lane == 0) LT[LW * (c & 31)] = -1.0;
       } else {
         df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
         if (lane < s) {
@@ -446,8 +471,20 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
         mu = warp_sum_df(mu);
         red = warp_sum_df(red);
         if (lane == 0) {
-          LT[2 * (c & 31)] = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
-          LT[2 * (c & 31) + 1] = df_to_double(df_sub(zi, mu));
+          LT[LW * (c & 31)] = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
+          LT[LW * (c & 31) + 1] = df_to_double(df_sub(zi, mu));
+        }
+        if (REML) {
+          // the basis rows' residuals f_i - w . f_S
+          const int j = lane < s ? a.nb[k * (int64_t)M + lane] : 0;
+          for (int q = 0; q < a.p; ++q) {
+            df g = df_make(0.0f, 0.0f);
+            if (lane < s) g = df_fma_acc(g, W.xd[lane], df_from_double(a.basis[(int64_t)q * a.n + j]));
+            g = warp_sum_df(g);
+            if (lane == 0)
+              LT[LW * (c & 31) + 2 + q] =
+                  df_to_double(df_sub(df_from_double(a.basis[(int64_t)q * a.n + i]), g));
+          }
         }
       }
       if ((c & 31) == 31 || c == a.ncand - 1) flush_terms(k, c & ~31, (c & 31) + 1);
@@ -501,7 +538,7 @@ __device__ bool chol_solve_strided(double* S, double* W, int s, int64_t T) {
 // (linalg.rs:123-203) on the assembled K_SS of vecchia.rs:302-320.
 // OWN_EXP: covariances with the table-driven FP64 exp (the re-solve of
 // flagged systems); the FP64 build keeps the library exp.
-template <int D, bool OWN_EXP>
+template <int D, bool OWN_EXP, bool REML = false>
 __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist, double* scratch,
                                     int64_t T, int32_t* cand_status, Exp64Table et_g) {
   __shared__ Exp64Table et;
@@ -533,10 +570,17 @@ __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
     const DevModel& mdl = a.models[c];
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
-    const double zi = a.v[i] - a.mean;
+    const double zi = REML ? a.v[i] : a.v[i] - a.mean;
     const double sill = mdl.c0;
+    double* rc = REML ? a.rec + code * (2 + a.p) : nullptr;
     if (s == 0) {
-      a.terms[code] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
+      if (REML) {
+        rc[0] = sill;
+        rc[1] = zi;
+        for (int q = 0; q < a.p; ++q) rc[2 + q] = a.basis[(int64_t)q * a.n + i];
+      } else {
+        a.terms[code] = -0.5 * (kLn2Pi + log(sill) + zi * zi / sill);
+      }
       continue;
     }
     const int32_t* nbk = a.nb + k * (int64_t)M;
@@ -557,17 +601,70 @@ __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
     }
     if (!chol_solve_strided(S, W, s, T)) {
       atomicExch(&cand_status[c], (int32_t)GS_ERR_SINGULAR_SYSTEM);
-      a.terms[code] = __longlong_as_double(0x7ff8000000000000ll);
+      if (REML) rc[0] = __longlong_as_double(0x7ff8000000000000ll);
+      else a.terms[code] = __longlong_as_double(0x7ff8000000000000ll);
       continue;
     }
     double mu = 0.0, red = 0.0;
-    for (int q = 0; q < s; ++q) mu += W[(int64_t)q * T] * (a.v[nbk[q]] - a.mean);
+    for (int q = 0; q < s; ++q) mu += W[(int64_t)q * T] * (REML ? a.v[nbk[q]] : a.v[nbk[q]] - a.mean);
     for (int q = 0; q < s; ++q) red += W[(int64_t)q * T] * K0[(int64_t)q * T];
     const double var = fmax(sill - red, 1e-12);
     const double r = zi - mu;
-    a.terms[code] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+    if (REML) {
+      rc[0] = var;
+      rc[1] = r;
+      for (int col = 0; col < a.p; ++col) {
+        double g = 0.0;
+        for (int q = 0; q < s; ++q) g += W[(int64_t)q * T] * a.basis[(int64_t)col * a.n + nbk[q]];
+        rc[2 + col] = a.basis[(int64_t)col * a.n + i] - g;
+      }
+    } else {
+      a.terms[code] = -0.5 * (kLn2Pi + log(var) + r * r / var);
+    }
   }
 }
+
+// REML's sums over the points from the records (var, r, g): row y = c * W + w
+// of the output sums ln var (w = 0), r^2 / var (1), g_f r / var (2 .. 1 + p)
+// and g_f g_g / var (f <= g, row-packed); the same fixed-order tree as
+// reduce_terms.
+__global__ void reduce_reml(const double* rec, int64_t n, int p, int64_t chunk, int64_t y0,
+                            double* partial) {
+  __shared__ double sh[256];
+  const int W = 2 + p + p * (p + 1) / 2;
+  const int64_t y = y0 + blockIdx.y;
+  const int c = (int)(y / W), w = (int)(y % W);
+  int r1 = 0, r2 = 0;  // record fields multiplied: 1 = r, 2 + f = g_f
+  if (w == 1) {
+    r1 = r2 = 1;
+  } else if (w >= 2 && w < 2 + p) {
+    r1 = 2 + (w - 2);
+    r2 = 1;
+  } else if (w >= 2 + p) {
+    int e = w - 2 - p, f = 0;
+    while (e >= p - f) {
+      e -= p - f;
+      ++f;
+    }
+    r1 = 2 + f;
+    r2 = 2 + f + e;
+  }
+  const int64_t lo = blockIdx.x * chunk;
+  const int64_t hi = min(n, lo + chunk);
+  double acc = 0.0;
+  for (int64_t q = lo + threadIdx.x; q < hi; q += blockDim.x) {
+    const double* rc = rec + ((int64_t)c * n + q) * (2 + p);
+    acc += w == 0 ? log(rc[0]) : rc[r1] * rc[r2] / rc[0];
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if ((int)threadIdx.x < s2) sh[threadIdx.x] += sh[threadIdx.x + s2];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[y * gridDim.x + blockIdx.x] = sh[0];
+}
+
 
 // Fixed-order reduction: block b sums terms [b*chunk, (b+1)*chunk) of one
 // candidate in a fixed tree; the partials are added in block order.
@@ -812,8 +909,12 @@ __global__ void exclude_terms_kernel(double* terms, int64_t n, int64_t ncand,
     if (exclude[i % n]) terms[i] = 0.0;
 }
 
+// REML (basis set, p columns; conditioning sets of at most 32 points, mixed
+// precision): instead of log-likelihoods, reml_sums receives per candidate
+// the reml_sums(p) sums of the ungrouped REML (ll is left NaN).
 int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
-                 int32_t* status, int precision, cudaStream_t s, const uint8_t* exclude = nullptr) {
+                 int32_t* status, int precision, cudaStream_t s, const uint8_t* exclude,
+                 const double* basis, int p, double* reml_sums) {
   const gs_pointset* ps = P->ps;
   const int dim = ps->dim;
   const int64_t n = P->n;
@@ -843,7 +944,11 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   DevBuf dmod, terms, flag, partial, out, cstat;
   GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
   GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
-  GS_TRY(terms.alloc((size_t)ncand * n * 8, s));
+  const bool reml = basis != nullptr;
+  const int LW = 2 + p;
+  DevBuf rec;
+  if (reml) GS_TRY(rec.alloc((size_t)ncand * n * LW * 8, s));
+  else GS_TRY(terms.alloc((size_t)ncand * n * 8, s));
   GS_TRY(flag.alloc((size_t)ncand * n, s));
   GS_TRY(cstat.alloc((size_t)ncand * 4, s));
   GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
@@ -867,9 +972,14 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   a.models = (const DevModel*)dmod.ptr;
   a.terms = (double*)terms.ptr;
   a.flag = (uint8_t*)flag.ptr;
+  a.basis = basis;
+  a.p = p;
+  a.rec = (double*)rec.ptr;
   int64_t nfl = 0;
   DevBuf list;
   const bool mixed = precision != GS_PREC_FP64 && M <= GS_MIXED_MAX_NEIGHBORS;
+  if (reml && !(mixed && M <= kWarpN))
+    return fail(GS_ERR_INVALID_PARAMETER, "mixed REML needs conditioning sets of at most 32");
   cudaEvent_t ev[4];
   for (int e = 0; e < 4; ++e) GS_CUDA(cudaEventCreate(&ev[e]));
   struct EvGuard {
@@ -884,8 +994,9 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (M <= kWarpN) {
-      const size_t smem = vecchia_warp_layout(std::max(M, 1), dim).total * kVWarps;
-      auto kern = dim == 2 ? vecchia_warp_kernel<2> : vecchia_warp_kernel<3>;
+      const size_t smem = vecchia_warp_layout(std::max(M, 1), dim, reml ? LW : 2).total * kVWarps;
+      auto kern = reml ? (dim == 2 ? vecchia_warp_kernel<2, true> : vecchia_warp_kernel<3, true>)
+                       : (dim == 2 ? vecchia_warp_kernel<2, false> : vecchia_warp_kernel<3, false>);
       GS_TRY(allow_dynamic_smem((const void*)kern, smem));
       int per_sm = 0;
       GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kVWarps, smem));
@@ -940,7 +1051,11 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     const int64_t* lp = mixed ? (const int64_t*)list.ptr : nullptr;
     double* sp = (double*)scratch.ptr;
     int32_t* cs = (int32_t*)cstat.ptr;
-    if (dim == 2 && mixed)
+    if (reml && dim == 2)
+      vecchia_fp64_kernel<2, true, true><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
+    else if (reml)
+      vecchia_fp64_kernel<3, true, true><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
+    else if (dim == 2 && mixed)
       vecchia_fp64_kernel<2, true><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
     else if (dim == 2)
       vecchia_fp64_kernel<2, false><<<blocks, 128, 0, s>>>(a, lp, work, sp, T, cs, g_vet);
@@ -952,6 +1067,29 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     count_launch(1);
   }
   GS_CUDA(cudaEventRecord(ev[3], s));
+  if (reml) {
+    const int W = 2 + p + p * (p + 1) / 2;
+    const int64_t rows = ncand * W;
+    const int64_t chunk = 8192;
+    const int nblk = (int)((n + chunk - 1) / chunk);
+    GS_TRY(partial.alloc((size_t)nblk * rows * 8, s));
+    GS_TRY(out.alloc((size_t)rows * 8, s));
+    int launches = 1;
+    for (int64_t y0 = 0; y0 < rows; y0 += 65535, ++launches)
+      reduce_reml<<<dim3(nblk, (unsigned)std::min<int64_t>(65535, rows - y0)), 256, 0, s>>>(
+          (const double*)rec.ptr, n, p, chunk, y0, (double*)partial.ptr);
+    reduce_partials<<<(int)((rows + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)rows,
+                                                              (double*)out.ptr);
+    GS_CUDA(cudaGetLastError());
+    count_launch(launches);
+    std::vector<int32_t> hst(ncand);
+    GS_CUDA(cudaMemcpyAsync(reml_sums, out.ptr, rows * 8, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaMemcpyAsync(hst.data(), cstat.ptr, ncand * 4, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaStreamSynchronize(s));
+    for (int64_t c = 0; c < ncand; ++c)
+      if (valid[c] && hst[c] != 0) status[c] = hst[c];
+    return GS_OK;
+  }
   if (exclude) {
     exclude_terms_kernel<<<152 * 8, 256, 0, s>>>((double*)terms.ptr, n, ncand, exclude);
     GS_CUDA(cudaGetLastError());
@@ -1711,6 +1849,21 @@ int gls_finish(int64_t n, int p, const double* sums, double* ll) {
 int vecchia_eval_reml(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
                       int64_t gsize, const double* d_basis, int p, double* ll, int32_t* status,
                       cudaStream_t s) {
+  const int per_m = reml_sums(p);
+  if (gsize <= 1 && P->m <= kWarpN) {
+    // the ungrouped REML through the mixed warp kernel (the conditioning
+    // solve of the likelihood, plus the basis rows' residuals)
+    std::vector<double> sums((size_t)std::max<int64_t>(ncand, 1) * per_m, NAN);
+    GS_TRY(vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s, nullptr, d_basis, p,
+                        sums.data()));
+    for (int64_t c = 0; c < ncand; ++c) {
+      ll[c] = NAN;
+      if (status[c] != 0) continue;
+      const int rc = gls_finish(P->n, p, &sums[(size_t)c * per_m], &ll[c]);
+      if (rc) status[c] = rc;
+    }
+    return GS_OK;
+  }
   gs_vecchia_plan::Groups G;
   GS_TRY(plan_groups(P, std::max<int64_t>(gsize, 1), &G));
   std::vector<double> sums;

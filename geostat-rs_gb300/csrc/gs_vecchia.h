@@ -11,9 +11,13 @@ namespace gs {
 // ll[c] and status[c] per candidate; synchronises `s` before returning.
 // exclude (device, per ordered position, or null): positions whose terms
 // are left out of the sums.
+// REML (basis set: p x n trend basis on the device; conditioning sets of at
+// most 32 points): reml_sums receives per candidate the ungrouped REML's
+// sums instead of log-likelihoods.
 int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
                  int32_t* status, int precision, cudaStream_t s,
-                 const uint8_t* exclude = nullptr);
+                 const uint8_t* exclude = nullptr, const double* basis = nullptr, int p = 0,
+                 double* reml_sums = nullptr);
 // Points of the plan's data set.
 int64_t vecchia_plan_points(const gs_vecchia_plan* P);
 }  // namespace gs

@@ -47,6 +47,21 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_abi.SIGNATURES) == names
 
 
+def test_library_has_no_unresolved_internal_symbols():
+    """Every library-internal function the translation units call is defined
+    in the library itself (a declaration that drifted from its definition
+    would only fail when the library is loaded with immediate binding)."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--undefined-only", _abi.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    bad = [l for l in out.splitlines() if " gs_" in l or "_ZN2gs" in l or "_ZN12_GLOBAL" in l]
+    assert not bad, bad
+
+
 def test_abi_version_and_struct_layout(tmp_path):
     """The ctypes structs match the C header's layout (compiled with gcc)."""
     import ctypes as C
