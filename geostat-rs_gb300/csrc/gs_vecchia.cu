@@ -1688,9 +1688,10 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
   }
   if (ncand == 0) return GS_OK;
   const int64_t nbl = multi_only ? G.nmulti : G.nblocks;
-  if (nbl == 0) {
+  if (nbl == 0) {  // nothing to evaluate: every valid candidate's sums are zero
     for (int64_t c = 0; c < ncand; ++c)
-      if (valid[c]) sums.assign(sums.size(), 0.0);
+      if (valid[c])
+        for (int w = 0; w < per; ++w) sums[(size_t)c * per + w] = 0.0;
     return GS_OK;
   }
   const int frame = (multi_only ? G.vmax_multi : G.vmax) + nr;
