@@ -629,7 +629,7 @@ __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
 // and g_f g_g / var (f <= g, row-packed); the same fixed-order tree as
 // reduce_terms.
 __global__ void reduce_reml(const double* rec, int64_t n, int p, int64_t chunk, int64_t y0,
-                            double* partial) {
+                            const uint8_t* exclude, double* partial) {
   __shared__ double sh[256];
   const int W = 2 + p + p * (p + 1) / 2;
   const int64_t y = y0 + blockIdx.y;
@@ -653,6 +653,7 @@ __global__ void reduce_reml(const double* rec, int64_t n, int p, int64_t chunk, 
   const int64_t hi = min(n, lo + chunk);
   double acc = 0.0;
   for (int64_t q = lo + threadIdx.x; q < hi; q += blockDim.x) {
+    if (exclude && exclude[q]) continue;
     const double* rc = rec + ((int64_t)c * n + q) * (2 + p);
     acc += w == 0 ? log(rc[0]) : rc[r1] * rc[r2] / rc[0];
   }
@@ -1077,7 +1078,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     int launches = 1;
     for (int64_t y0 = 0; y0 < rows; y0 += 65535, ++launches)
       reduce_reml<<<dim3(nblk, (unsigned)std::min<int64_t>(65535, rows - y0)), 256, 0, s>>>(
-          (const double*)rec.ptr, n, p, chunk, y0, (double*)partial.ptr);
+          (const double*)rec.ptr, n, p, chunk, y0, exclude, (double*)partial.ptr);
     reduce_partials<<<(int)((rows + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)rows,
                                                               (double*)out.ptr);
     GS_CUDA(cudaGetLastError());
@@ -1851,12 +1852,27 @@ int vecchia_eval_reml(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
                       int64_t gsize, const double* d_basis, int p, double* ll, int32_t* status,
                       cudaStream_t s) {
   const int per_m = reml_sums(p);
-  if (gsize <= 1 && P->m <= kWarpN) {
+  if (P->m <= kWarpN) {
     // the ungrouped REML through the mixed warp kernel (the conditioning
-    // solve of the likelihood, plus the basis rows' residuals)
+    // solve of the likelihood, plus the basis rows' residuals); grouped:
+    // one-member blocks the same way (their sums are their points'), the
+    // larger blocks on the FP64 block kernel
+    gs_vecchia_plan::Groups G;
+    if (gsize > 1) GS_TRY(plan_groups(P, gsize, &G));
     std::vector<double> sums((size_t)std::max<int64_t>(ncand, 1) * per_m, NAN);
-    GS_TRY(vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s, nullptr, d_basis, p,
-                        sums.data()));
+    GS_TRY(vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s,
+                        G.nmulti ? G.d_in_multi : nullptr, d_basis, p, sums.data()));
+    if (G.nmulti) {
+      std::vector<double> sums2;
+      std::vector<int> valid;
+      std::vector<int32_t> st2(ncand);
+      GS_TRY(eval_blocks(P, ncand, models, G, 1 + p, d_basis, false, sums2, st2.data(), valid, s,
+                         true));
+      for (int64_t c = 0; c < ncand; ++c) {
+        if (status[c] == 0 && st2[c] != 0) status[c] = st2[c];
+        for (int w = 0; w < per_m; ++w) sums[(size_t)c * per_m + w] += sums2[(size_t)c * per_m + w];
+      }
+    }
     for (int64_t c = 0; c < ncand; ++c) {
       ll[c] = NAN;
       if (status[c] != 0) continue;

@@ -152,3 +152,31 @@ def test_grouped_mle_matches_ungrouped_under_full_conditioning():
     starts, _ = O.vecchia_mle_setup(c, v)
     xr, fr, _ = O.vecchia_fit_nm(c, v, "exponential", 15, starts, group_size=4)
     assert abs(-llg - fr) <= 1e-8 * abs(fr)
+
+
+def test_reml_large_sets_and_sorted_order_blocks():
+    """m = 40 (beyond the mixed warp kernel: the FP64 block kernel for every
+    point) and a coordinate-sorted order, whose consecutive points share
+    neighbours so that Guinness blocks have many members."""
+    c = uniform_points(2500, 2, 211, [1.0, 1.0])
+    v = 1.0 + 2.0 * c[:, 1] + G.rff_field(c, _models()[0], 512, 212)
+    plan = G.VecchiaPlan(G.PointSet(c, v), 40)
+    order, nb, cnt = plan.arrays()
+    ll, st = plan.reml_loglik(_models(), drift_degree=1)
+    assert (st == 0).all()
+    f = O.poly_basis(c, 1)
+    for i, mdl in enumerate(_models()):
+        ref = O.vecchia_reml_loglik(c, v, mdl, order, nb, cnt, f, 1)
+        assert abs(ll[i] - ref) <= 1e-9 * abs(ref), (i, ll[i], ref)
+    srt = np.lexsort((c[:, 1], np.floor(c[:, 0] * 20)))
+    plan = G.VecchiaPlan(G.PointSet(c, v), 12, srt)
+    order, nb, cnt = plan.arrays()
+    for g in (4, 8):
+        llg, stg = plan.loglik_grouped(_models(), g)
+        llr, str_ = plan.reml_loglik(_models(), drift_degree=1, group_size=g)
+        assert (stg == 0).all() and (str_ == 0).all()
+        for i, mdl in enumerate(_models()):
+            ref = O.vecchia_loglik_grouped(c, v, mdl, order, nb, cnt, g)
+            assert abs(llg[i] - ref) <= 1e-9 * abs(ref), (g, i, llg[i], ref)
+            ref = O.vecchia_reml_loglik(c, v, mdl, order, nb, cnt, f, g)
+            assert abs(llr[i] - ref) <= 1e-9 * abs(ref), (g, i, llr[i], ref)
