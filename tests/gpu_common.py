@@ -60,15 +60,18 @@ def clustered_points(n, seed, extent=10000.0, nblobs=50, sigma=15.0, frac=0.7):
     return np.clip(pts, 0.0, extent)
 
 
-def cfg1_model():
+def sph200_model():
+    """Nugget 0.1 + spherical (sill 1, range 200 m): the 2-D 2,000-point workload's model."""
     return VariogramModel(0.1, [Structure("spherical", 1.0, 200.0)])
 
 
-def cfg2_model():
+def rotated_3d_model():
+    """The 3-D workload's model: nugget 0.05 + rotated spherical + exponential."""
     return VariogramModel(0.05, [Structure.with_rotation("spherical", 0.6, 300.0, 30.0, 10.0, 0.0,
                                                          0.5, 40.0 / 300.0),
                                  Structure("exponential", 0.35, 800.0)])
 
 
-def cfg3_model():
+def clustered_matern_model():
+    """The clustered workload's model: Matern 3/2, range 500 m, ratio 0.5 at 45 degrees."""
     return VariogramModel(0.0, [Structure.with_anisotropy("matern15", 1.0, 500.0, 45.0, 0.5)])

@@ -13,7 +13,7 @@ import pytest
 import pyoracle as O
 import geostat_rs as G
 from geostat_rs.model import Structure, VariogramModel
-from gpu_common import assert_close, cfg1_model, smooth_values, uniform_points
+from gpu_common import assert_close, sph200_model, smooth_values, uniform_points
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +31,7 @@ def test_block_kriging_matches_oracle(case):
     n = 80 if case == "ok_global" else 3000
     c = uniform_points(n, dim, 301, [1000.0] * dim)
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     cfg = {"ok_knn": G.KrigingConfig(max_neighbors=24),
            "sk_knn": G.KrigingConfig("simple", mean=float(np.mean(v)), max_neighbors=24),
            "ok_octant": G.KrigingConfig(max_per_octant=4),
@@ -66,7 +66,7 @@ def test_block_kriging_matches_oracle(case):
 def test_block_grid_and_single_block_and_errors():
     c = uniform_points(2000, 2, 304, [1000.0, 1000.0])
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     k = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig(max_neighbors=16))
     vals, var = k.predict_block_grid([0.0, 0.0], [1000.0, 1000.0], [20, 15], [50.0, 66.0], [3, 5])
     gx = (np.arange(20) + 0.5) * 50.0
@@ -165,7 +165,7 @@ def test_csv_end_to_end(tmp_path):
     ps = gio.read_points(tmp_path / "pts.csv", "east", "north", "grade")
     assert np.array_equal(ps.coords, c) and np.array_equal(ps.values, v)
     tg, _ = gio.read_targets(tmp_path / "tg.csv", "x", "y")
-    m = cfg1_model()
+    m = sph200_model()
     k = G.Kriging.new(ps, m, G.KrigingConfig(max_neighbors=16))
     val, var = k.predict_many(tg)
     gio.write_estimates_csv(tmp_path / "out.csv", tg, val, var)

@@ -13,7 +13,7 @@ import pytest
 
 import pyoracle as O
 import geostat_rs as G
-from gpu_common import assert_close, cfg3_model, clustered_points
+from gpu_common import assert_close, clustered_matern_model, clustered_points
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +23,7 @@ SEARCH = dict(max_per_octant=16, max_neighbors=64, min_neighbors=4)
 
 def _data():
     c = clustered_points(100_000, 41, extent=EXTENT, nblobs=50)
-    m = cfg3_model()
+    m = clustered_matern_model()
     v = G.rff_field(c, m, 1024, 42)
     cov = O.rng_uniform(43, len(c))
     g = (np.arange(36) + 0.5) * (EXTENT / 36)

@@ -13,7 +13,7 @@ import pytest
 import pyoracle as O
 import geostat_rs as G
 from geostat_rs.model import Structure, VariogramModel
-from gpu_common import assert_close, cfg1_model, smooth_values, uniform_points
+from gpu_common import assert_close, sph200_model, smooth_values, uniform_points
 
 pytestmark = pytest.mark.gpu
 
@@ -53,7 +53,7 @@ def test_leave_one_out_matches_oracle(case):
     n = 60 if case == "global" else 400
     c = uniform_points(n, 2, 71, [1000.0, 1000.0])
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     cfg = {"knn": G.KrigingConfig(max_neighbors=16),
            "octant_uk": G.KrigingConfig("universal", degree=1, max_per_octant=5),
            "global": G.KrigingConfig(),
@@ -72,7 +72,7 @@ def test_leave_one_out_with_drift_matches_oracle():
     c = uniform_points(300, 2, 72, [1000.0, 1000.0])
     cov = O.rng_uniform(73, 300)
     v = smooth_values(c) + 2.0 * cov
-    m = cfg1_model()
+    m = sph200_model()
     cfg = G.KrigingConfig("external_drift", n_vars=1, max_neighbors=20)
     pred, var = oracle_loo(c, v, m, dict(method="external_drift", max_neighbors=20),
                            drift=cov.reshape(-1, 1))
@@ -85,7 +85,7 @@ def test_k_fold_matches_oracle(k, seed):
     n = 400
     c = uniform_points(n, 2, 74, [1000.0, 1000.0])
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     fold_of = folds(n, k, seed)
     pred, var = np.empty(n), np.empty(n)
     for f in range(k):
@@ -123,7 +123,7 @@ def test_cross_validation_3d_and_errors():
 def test_tune_kriging_neighbors_matches_oracle_trace():
     c = uniform_points(250, 2, 76, [1000.0, 1000.0])
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     cands = [4, 8, 16, 32]
     res = G.tune_kriging_neighbors(G.PointSet(c, v), m, "ordinary", cands)
     for (nb, vecv), k in zip(res.trace, cands):

@@ -11,7 +11,7 @@ import pytest
 import pyoracle as O
 import geostat_rs as G
 from geostat_rs.model import Structure, VariogramModel
-from gpu_common import assert_close, cfg1_model, smooth_values, uniform_points
+from gpu_common import assert_close, sph200_model, smooth_values, uniform_points
 
 pytestmark = pytest.mark.gpu
 
@@ -33,7 +33,7 @@ def _check(k, c, v, m, t, okw, tdrift=None, errors=None, drift=None):
 def test_global_2d_methods(method):
     c = uniform_points(300, 2, 81, [1000.0, 1000.0])
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     cfg = G.KrigingConfig(method, mean=float(np.mean(v)) if method == "simple" else None)
     k = G.Kriging.new(G.PointSet(c, v), m, cfg)
     t = uniform_points(500, 2, 82, [1100.0, 1100.0]) - 50.0
@@ -57,16 +57,16 @@ def test_global_large_3d_and_drift_and_errors():
     cov = O.rng_uniform(87, 300)
     ck = uniform_points(300, 2, 88, [1000.0, 1000.0])
     vk = smooth_values(ck) + cov
-    kk = G.Kriging.with_external_drift(G.PointSet(ck, vk), cfg1_model(),
+    kk = G.Kriging.with_external_drift(G.PointSet(ck, vk), sph200_model(),
                                        G.KrigingConfig("external_drift", n_vars=1),
                                        cov.reshape(-1, 1))
     tk = uniform_points(200, 2, 89, [1000.0, 1000.0])
     tc = O.rng_uniform(90, 200).reshape(-1, 1)
-    _check(kk, ck, vk, cfg1_model(), tk, dict(method="external_drift"), tdrift=tc,
+    _check(kk, ck, vk, sph200_model(), tk, dict(method="external_drift"), tdrift=tc,
            drift=cov.reshape(-1, 1))
     err = 0.05 * O.rng_uniform(91, 300)
-    ke = G.Kriging.with_measurement_error(G.PointSet(ck, vk), cfg1_model(), G.KrigingConfig(), err)
-    _check(ke, ck, vk, cfg1_model(), tk, {}, errors=err)
+    ke = G.Kriging.with_measurement_error(G.PointSet(ck, vk), sph200_model(), G.KrigingConfig(), err)
+    _check(ke, ck, vk, sph200_model(), tk, {}, errors=err)
 
 
 def test_global_singular_and_min_neighbors_validation():
@@ -74,7 +74,7 @@ def test_global_singular_and_min_neighbors_validation():
     x = np.linspace(0.0, 1000.0, 120)
     c = np.stack([x, 2.0 * x + 5.0], 1)
     v = np.sin(x / 100.0)
-    m = cfg1_model()
+    m = sph200_model()
     k = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig("universal", degree=1))
     t = uniform_points(50, 2, 92, [1000.0, 1000.0])
     ref = O.krige(c, v, m, t, method="universal", degree=1)
@@ -91,7 +91,7 @@ def test_global_equals_moving_at_k_equals_n():
     # kriging.rs:1570: the factored global system and the moving one at k = n
     c = uniform_points(120, 2, 94, [1000.0, 1000.0])
     v = smooth_values(c)
-    m = cfg1_model()
+    m = sph200_model()
     t = uniform_points(300, 2, 95, [1000.0, 1000.0])
     g = G.Kriging.new(G.PointSet(c, v), m).predict_many(t, "fp64", full=True)
     mv = G.Kriging.new(G.PointSet(c, v), m,

@@ -10,7 +10,7 @@ import pytest
 import pyoracle as O
 import geostat_rs as G
 from geostat_rs.model import Anisotropy, Structure, VariogramModel
-from gpu_common import (assert_close, cfg1_model, cfg2_model, cfg3_model, clustered_points,
+from gpu_common import (assert_close, sph200_model, rotated_3d_model, clustered_matern_model, clustered_points,
                         max_rel, smooth_values, uniform_points)
 
 pytestmark = pytest.mark.gpu
@@ -57,9 +57,9 @@ def test_knn_neighbour_sets_bit_exact(dim, n, k):
     c = uniform_points(n, dim, 7 + dim, ext)
     v = smooth_values(c)
     t = uniform_points(1500, dim, 99, np.asarray(ext) * 1.1) - 0.05 * np.asarray(ext)
-    ref = O.krige(c, v, cfg1_model(), t, max_neighbors=k, kcap=min(k, n))
+    ref = O.krige(c, v, sph200_model(), t, max_neighbors=k, kcap=min(k, n))
     assert ref["boundary_ties"] == 0
-    k_ = G.Kriging.new(G.PointSet(c, v), cfg1_model(), G.KrigingConfig(max_neighbors=k))
+    k_ = G.Kriging.new(G.PointSet(c, v), sph200_model(), G.KrigingConfig(max_neighbors=k))
     idx, cnt = k_.neighbors(t, min(k, n))
     assert (cnt == ref["nb_count"]).all()
     assert (idx == ref["neighbors"]).all()
@@ -76,10 +76,10 @@ def test_radius_and_octant_neighbour_sets_bit_exact():
     for case in cases:
         cfg = G.KrigingConfig(**case)
         kcap = 64
-        ref = O.krige(c, v, cfg1_model(), t, max_neighbors=cfg.max_neighbors,
+        ref = O.krige(c, v, sph200_model(), t, max_neighbors=cfg.max_neighbors,
                       max_per_octant=cfg.max_per_octant, radius=cfg.search_radius,
                       min_neighbors=cfg.min_neighbors, kcap=kcap)
-        kk = G.Kriging.new(G.PointSet(c, v), cfg1_model(), cfg)
+        kk = G.Kriging.new(G.PointSet(c, v), sph200_model(), cfg)
         idx, cnt = kk.neighbors(t, kcap)
         assert (cnt == ref["nb_count"]).all(), case
         assert (idx == ref["neighbors"]).all(), case
@@ -96,10 +96,10 @@ def test_anisotropic_search_and_octants_bit_exact(dim):
                  dict(max_neighbors=32, max_per_octant=6, anisotropic_search=an),
                  dict(max_neighbors=20, search_radius=120.0, anisotropic_search=an)):
         cfg = G.KrigingConfig(**case)
-        ref = O.krige(c, v, cfg1_model(), t, max_neighbors=cfg.max_neighbors,
+        ref = O.krige(c, v, sph200_model(), t, max_neighbors=cfg.max_neighbors,
                       max_per_octant=cfg.max_per_octant, radius=cfg.search_radius,
                       anisotropic_search=an, kcap=32)
-        kk = G.Kriging.new(G.PointSet(c, v), cfg1_model(), cfg)
+        kk = G.Kriging.new(G.PointSet(c, v), sph200_model(), cfg)
         idx, cnt = kk.neighbors(t, 32)
         assert (cnt == ref["nb_count"]).all(), case
         assert (idx == ref["neighbors"]).all(), case
@@ -109,7 +109,7 @@ def test_anisotropic_search_and_octants_bit_exact(dim):
 def test_config1_ordinary_kriging_full_size():
     """2-D OK: n=2000 in [0,1000]^2, nugget 0.1 + Sph(1, 200), 100x100 grid, n_max=32."""
     c = uniform_points(2000, 2, 2024, [1000.0, 1000.0])
-    m = cfg1_model()
+    m = sph200_model()
     v = 10.0 + G.rff_field(c, VariogramModel(0.1, [Structure("exponential", 1.0, 200.0 / 3)]),
                            2048, 11)
     t = O.grid_centers([0, 0], [1000, 1000], [100, 100])
@@ -135,7 +135,7 @@ def test_kinds_2d(kind):
 def test_config2_shape_3d_nested_rotated():
     """3-D OK with nugget + rotated Sph(300/150/40, az 30, dip 10) + Exp(800), n_max=64."""
     c = uniform_points(20000, 3, 5, [2000.0, 2000.0, 200.0])
-    m = cfg2_model()
+    m = rotated_3d_model()
     v = G.rff_field(c, m, 1024, 3)
     t = uniform_points(3000, 3, 6, [2000.0, 2000.0, 200.0])
     _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64))
@@ -182,7 +182,7 @@ def test_external_drift_and_measurement_error():
     c = uniform_points(2500, 2, 61, [1000.0, 1000.0])
     cov = O.rng_uniform(62, 2500)
     v = smooth_values(c) + 2.0 * cov
-    m = cfg3_model()
+    m = clustered_matern_model()
     t = uniform_points(400, 2, 63, [1000.0, 1000.0])
     tc = O.rng_uniform(64, 400).reshape(-1, 1)
     _, ref, outs = run_both(c, v, m, t, dict(method="external_drift", n_vars=1, max_neighbors=32),
@@ -190,7 +190,7 @@ def test_external_drift_and_measurement_error():
     for prec, out in outs.items():
         check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
     err = 0.05 * O.rng_uniform(65, 2500)
-    _, ref, outs = run_both(c, v, cfg1_model(), t, dict(max_neighbors=20), errors=err)
+    _, ref, outs = run_both(c, v, sph200_model(), t, dict(max_neighbors=20), errors=err)
     for prec, out in outs.items():
         check(ref, out, v, 1.1, 1e-9 if prec == "mixed" else 1e-10)
 
@@ -198,7 +198,7 @@ def test_external_drift_and_measurement_error():
 def test_octant_uneven_systems_clustered():
     """Octant search on clustered data: systems of 4..64 neighbours in one launch."""
     c = clustered_points(30000, 9, extent=10000.0, nblobs=60)
-    m = cfg3_model()
+    m = clustered_matern_model()
     v = G.rff_field(c, m, 512, 4)
     t = uniform_points(1500, 2, 10, [10000.0, 10000.0])
     _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64, max_per_octant=16,
@@ -318,13 +318,13 @@ def test_grid_targets_reuse_shared_neighbours(case):
 
 def test_grid_targets_reuse_3d_and_external_drift():
     c = uniform_points(8000, 3, 405, [600.0, 600.0, 60.0])
-    m = cfg2_model()
+    m = rotated_3d_model()
     v = G.rff_field(c, m, 1024, 13)
     t = O.grid_centers([50, 50, 5], [550, 550, 55], [64, 8, 4])
     k, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64), precisions=("mixed",))
     check(ref, outs["mixed"], v, m.total_sill())
     c2 = uniform_points(5000, 2, 406, [1000.0, 1000.0])
-    m2 = cfg1_model()
+    m2 = sph200_model()
     drift = 0.01 * c2[:, 0:1] + O.rng_uniform(407, 5000).reshape(-1, 1)
     v2 = 3.0 * drift[:, 0] + smooth_values(c2)
     t2 = O.grid_centers([100, 100], [900, 900], [100, 20])
