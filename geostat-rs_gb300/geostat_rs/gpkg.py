@@ -1,15 +1,15 @@
-"""GeoPackage point layers (crates/geostat-cli/src/gpkg.rs:1-310, 786-860).
+"""GeoPackage point layers and rasters (crates/geostat-cli/src/gpkg.rs).
 
 A GeoPackage is an SQLite database with the OGC schema; this module reads and
-writes 2-D point feature layers through Python's sqlite3 (the same SQLite
-engine the reference bundles through rusqlite).  Geometry blobs are
-StandardGeoPackageBinary: a ``GP`` header (optional envelope) and WKB, of
-which X and Y are taken (ISO Z/M and EWKB SRID forms accepted).  Blobs are
-packed and unpacked in bulk with numpy.  Raster (tiled PNG) coverages are not
-handled here.
+writes 2-D point feature layers and single-band 2D Gridded Coverage rasters
+through Python's sqlite3 (the same SQLite engine the reference bundles
+through rusqlite).  Geometry blobs are StandardGeoPackageBinary: a ``GP``
+header (optional envelope) and WKB, of which X and Y are taken (ISO Z/M and
+EWKB SRID forms accepted); they are packed and unpacked in bulk with numpy.
 """
 from __future__ import annotations
 
+import math
 import os
 import sqlite3
 import struct
@@ -229,3 +229,305 @@ def write_points(path, layer: str, srs_id: int, coords, columns: Sequence[Tuple[
         con.commit()
     finally:
         con.close()
+
+
+# --------------------------------------------------------------- rasters ---
+# gpkg.rs:314-785: a kriged grid as a single-band OGC 2D Gridded Coverage --
+# one 16-bit grayscale PNG tile with the linear map value = pixel * scale +
+# offset, pixel 0 = no data -- and its reader.  PNG (ISO/IEC 15948) is
+# written with filter type 0 and zlib; the reader undoes all five filter
+# types of non-interlaced 16-bit grayscale images.
+
+_PNG_SIG = b"\x89PNG\r\n\x1a\n"
+
+
+def _png_chunk(kind: bytes, data: bytes) -> bytes:
+    import zlib
+    return struct.pack(">I", len(data)) + kind + data + struct.pack(
+        ">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+
+def encode_png_u16(pixels) -> bytes:
+    """A 16-bit grayscale PNG of the (height, width) array ``pixels``."""
+    import zlib
+    px = np.asarray(pixels, dtype=">u2")
+    h, w = px.shape
+    raw = np.zeros((h, 1 + 2 * w), dtype=np.uint8)  # filter byte 0 per row
+    raw[:, 1:] = px.view(np.uint8).reshape(h, 2 * w)
+    ihdr = struct.pack(">IIBBBBB", w, h, 16, 0, 0, 0, 0)
+    return (_PNG_SIG + _png_chunk(b"IHDR", ihdr) +
+            _png_chunk(b"IDAT", zlib.compress(raw.tobytes(), 6)) + _png_chunk(b"IEND", b""))
+
+
+def decode_png_u16(blob: bytes, tw: int, th: int) -> np.ndarray:
+    """gpkg.rs:757-784: a 16-bit grayscale tile of tw x th pixels (row-major)."""
+    import zlib
+    b = bytes(blob)
+    if b[:8] != _PNG_SIG:
+        raise IoError("PNG header: not a PNG")
+    pos, ihdr, idat = 8, None, []
+    while pos + 8 <= len(b):
+        n, kind = struct.unpack(">I4s", b[pos:pos + 8])
+        data = b[pos + 8:pos + 8 + n]
+        if len(data) != n:
+            raise IoError("PNG data: truncated chunk")
+        if kind == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", data)
+        elif kind == b"IDAT":
+            idat.append(data)
+        elif kind == b"IEND":
+            break
+        pos += 12 + n
+    if ihdr is None:
+        raise IoError("PNG header: no IHDR")
+    w, h, depth, color, _, _, interlace = ihdr
+    if depth != 16 or color != 0:
+        raise IoError(f"tile is {depth}-bit colour type {color}; expected 16-bit grayscale")
+    if interlace != 0:
+        raise IoError("PNG data: interlaced tiles are not supported")
+    if w != tw or h != th:
+        raise IoError(f"tile is {w}x{h} but the tile matrix declares {tw}x{th}")
+    try:
+        raw = zlib.decompress(b"".join(idat))
+    except zlib.error as e:
+        raise IoError(f"PNG data: {e}") from e
+    stride, bpp = 2 * w, 2
+    if len(raw) < h * (1 + stride):
+        raise IoError("PNG data: short image data")
+    out = np.zeros((h, stride), dtype=np.int64)
+    prev = np.zeros(stride, dtype=np.int64)
+    for r in range(h):
+        ft = raw[r * (1 + stride)]
+        line = np.frombuffer(raw, dtype=np.uint8, count=stride, offset=r * (1 + stride) + 1)
+        line = line.astype(np.int64)
+        if ft == 0:
+            cur = line
+        elif ft == 2:
+            cur = (line + prev) & 0xFF
+        elif ft in (1, 3, 4):
+            cur = np.zeros(stride, dtype=np.int64)
+            for x in range(stride):
+                a = cur[x - bpp] if x >= bpp else 0
+                up = prev[x]
+                if ft == 1:
+                    pred = a
+                elif ft == 3:
+                    pred = (a + up) >> 1
+                else:
+                    c = prev[x - bpp] if x >= bpp else 0
+                    p = a + up - c
+                    pa, pb, pc = abs(p - a), abs(p - up), abs(p - c)
+                    pred = a if pa <= pb and pa <= pc else (up if pb <= pc else c)
+                cur[x] = (line[x] + pred) & 0xFF
+        else:
+            raise IoError(f"PNG data: unknown filter type {ft}")
+        out[r] = cur
+        prev = cur
+    by = out.astype(np.uint8)
+    return (by[:, 0::2].astype(np.uint16) << 8 | by[:, 1::2].astype(np.uint16)).reshape(h, w)
+
+
+def encode_raster(nx: int, ny: int, values):
+    """gpkg.rs:324-375: (png, scale, offset, min, max, mean, std_dev).  Finite
+    values map linearly onto pixels 1..65535 (min -> 1, max -> 65535,
+    rounded half away from zero), non-finite ones to 0; image rows run north
+    to south."""
+    v = np.asarray(values, dtype=np.float64).reshape(ny, nx)
+    fin = v[np.isfinite(v)]
+    if fin.size == 0:
+        raise IoError("raster has no finite values")
+    vmin, vmax = float(fin.min()), float(fin.max())
+    mean = float(np.cumsum(fin)[-1] / fin.size)
+    std = math.sqrt(float(np.cumsum((fin - mean) ** 2)[-1] / fin.size))
+    span = max(vmax - vmin, 2.2250738585072014e-308)
+    scale = span / 65534.0
+    offset = vmin - scale
+    with np.errstate(invalid="ignore"):
+        px = np.clip(np.floor(1.0 + (v - vmin) / span * 65534.0 + 0.5), 1.0, 65535.0)
+    px = np.where(np.isfinite(v), px, 0.0).astype(np.uint16)
+    return encode_png_u16(px[::-1]), scale, offset, vmin, vmax, mean, std
+
+
+def write_raster(path, layer: str, srs_id: int, nx: int, ny: int, bbox, values) -> None:
+    """gpkg.rs:384-518: a new GeoPackage holding the grid (values in grid
+    order, iy * nx + ix, y increasing; bbox = [min_x, min_y, max_x, max_y])
+    as one 2D Gridded Coverage tile."""
+    vals = np.asarray(values, dtype=np.float64).reshape(-1)
+    if len(vals) != nx * ny:
+        raise IoError(f"{len(vals)} values for an {nx}x{ny} grid")
+    png, scale, offset, vmin, vmax, mean, std = encode_raster(nx, ny, vals)
+    min_x, min_y, max_x, max_y = (float(b) for b in bbox)
+    if os.path.exists(path):
+        os.remove(path)
+    con = sqlite3.connect(os.fspath(path))
+    try:
+        con.execute(f"PRAGMA application_id = {0x47504B47}")
+        con.execute("PRAGMA user_version = 10300")
+        con.executescript(
+            "CREATE TABLE gpkg_spatial_ref_sys (srs_name TEXT NOT NULL, srs_id INTEGER PRIMARY "
+            "KEY, organization TEXT NOT NULL, organization_coordsys_id INTEGER NOT NULL, "
+            "definition TEXT NOT NULL, description TEXT);"
+            "CREATE TABLE gpkg_contents (table_name TEXT NOT NULL PRIMARY KEY, data_type TEXT "
+            "NOT NULL, identifier TEXT UNIQUE, description TEXT DEFAULT '', last_change TEXT NOT "
+            "NULL DEFAULT (strftime('%Y-%m-%dT%H:%M:%fZ','now')), min_x DOUBLE, min_y DOUBLE, "
+            "max_x DOUBLE, max_y DOUBLE, srs_id INTEGER);"
+            "CREATE TABLE gpkg_tile_matrix_set (table_name TEXT NOT NULL PRIMARY KEY, srs_id "
+            "INTEGER NOT NULL, min_x DOUBLE NOT NULL, min_y DOUBLE NOT NULL, max_x DOUBLE NOT "
+            "NULL, max_y DOUBLE NOT NULL);"
+            "CREATE TABLE gpkg_tile_matrix (table_name TEXT NOT NULL, zoom_level INTEGER NOT "
+            "NULL, matrix_width INTEGER NOT NULL, matrix_height INTEGER NOT NULL, tile_width "
+            "INTEGER NOT NULL, tile_height INTEGER NOT NULL, pixel_x_size DOUBLE NOT NULL, "
+            "pixel_y_size DOUBLE NOT NULL, CONSTRAINT pk_ttm PRIMARY KEY (table_name, "
+            "zoom_level));"
+            "CREATE TABLE gpkg_extensions (table_name TEXT, column_name TEXT, extension_name "
+            "TEXT NOT NULL, definition TEXT NOT NULL, scope TEXT NOT NULL, CONSTRAINT ge_tce "
+            "UNIQUE (table_name, column_name, extension_name));"
+            "CREATE TABLE gpkg_2d_gridded_coverage_ancillary (id INTEGER PRIMARY KEY "
+            "AUTOINCREMENT, tile_matrix_set_name TEXT NOT NULL UNIQUE, datatype TEXT NOT NULL "
+            "DEFAULT 'integer', scale REAL NOT NULL DEFAULT 1.0, offset REAL NOT NULL DEFAULT "
+            "0.0, precision REAL DEFAULT 1.0, data_null REAL, grid_cell_encoding TEXT DEFAULT "
+            "'grid-value-is-center', uom TEXT, field_name TEXT DEFAULT 'Height', "
+            "quantity_definition TEXT DEFAULT 'Height');"
+            "CREATE TABLE gpkg_2d_gridded_tile_ancillary (id INTEGER PRIMARY KEY AUTOINCREMENT, "
+            "tpudt_name TEXT NOT NULL, tpudt_id INTEGER NOT NULL, scale REAL NOT NULL DEFAULT "
+            "1.0, offset REAL NOT NULL DEFAULT 0.0, min REAL, max REAL, mean REAL, std_dev REAL, "
+            "UNIQUE (tpudt_name, tpudt_id));")
+        con.executemany("INSERT INTO gpkg_spatial_ref_sys VALUES (?, ?, ?, ?, 'undefined', NULL)",
+                        [("Undefined cartesian SRS", -1, "NONE", -1),
+                         ("Undefined geographic SRS", 0, "NONE", 0),
+                         ("WGS 84 geodetic", 4326, "EPSG", 4326)])
+        if srs_id not in (-1, 0, 4326):
+            con.execute("INSERT INTO gpkg_spatial_ref_sys VALUES (?, ?, 'EPSG', ?, 'undefined', "
+                        "NULL)", (f"SRS {srs_id}", srs_id, srs_id))
+        q = quote_ident(layer)
+        con.execute(f"CREATE TABLE {q} (id INTEGER PRIMARY KEY AUTOINCREMENT, zoom_level INTEGER "
+                    "NOT NULL, tile_column INTEGER NOT NULL, tile_row INTEGER NOT NULL, tile_data "
+                    "BLOB NOT NULL, UNIQUE (zoom_level, tile_column, tile_row))")
+        con.execute("INSERT INTO gpkg_contents (table_name, data_type, identifier, min_x, min_y, "
+                    "max_x, max_y, srs_id) VALUES (?, '2d-gridded-coverage', ?, ?, ?, ?, ?, ?)",
+                    (layer, layer, min_x, min_y, max_x, max_y, srs_id))
+        con.execute("INSERT INTO gpkg_tile_matrix_set VALUES (?, ?, ?, ?, ?, ?)",
+                    (layer, srs_id, min_x, min_y, max_x, max_y))
+        con.execute("INSERT INTO gpkg_tile_matrix VALUES (?, 0, 1, 1, ?, ?, ?, ?)",
+                    (layer, nx, ny, (max_x - min_x) / nx, (max_y - min_y) / ny))
+        d = "http://docs.opengeospatial.org/is/17-066r1/17-066r1.html"
+        con.executemany("INSERT INTO gpkg_extensions VALUES (?, ?, 'gpkg_2d_gridded_coverage', "
+                        "?, 'read-write')",
+                        [("gpkg_2d_gridded_coverage_ancillary", None, d),
+                         ("gpkg_2d_gridded_tile_ancillary", None, d), (layer, "tile_data", d)])
+        con.execute("INSERT INTO gpkg_2d_gridded_coverage_ancillary (tile_matrix_set_name, "
+                    "datatype, scale, offset, precision, data_null, field_name, "
+                    "quantity_definition) VALUES (?, 'integer', ?, ?, ?, 0.0, 'prediction', "
+                    "'prediction')", (layer, scale, offset, scale))
+        cur = con.execute(f"INSERT INTO {q} (zoom_level, tile_column, tile_row, tile_data) "
+                          "VALUES (0, 0, 0, ?)", (png,))
+        con.execute("INSERT INTO gpkg_2d_gridded_tile_ancillary (tpudt_name, tpudt_id, scale, "
+                    "offset, min, max, mean, std_dev) VALUES (?, ?, 1.0, 0.0, ?, ?, ?, ?)",
+                    (layer, cur.lastrowid, vmin, vmax, mean, std))
+        con.commit()
+    finally:
+        con.close()
+
+
+@dataclass
+class RasterGrid:
+    """gpkg.rs:523-583: a coverage read back, values in grid order (NaN =
+    no data)."""
+    name: str
+    srs_id: int
+    nx: int
+    ny: int
+    bbox: Tuple[float, float, float, float]
+    values: np.ndarray
+
+    def sample(self, x: float, y: float) -> Optional[float]:
+        """Nearest cell's value at (x, y); None outside the extent or on no
+        data."""
+        if self.nx == 0 or self.ny == 0:
+            return None
+        min_x, min_y, max_x, max_y = self.bbox
+        if x < min_x or x > max_x or y < min_y or y > max_y:
+            return None
+        ix = min(int((x - min_x) / ((max_x - min_x) / self.nx)), self.nx - 1)
+        iy = min(int((y - min_y) / ((max_y - min_y) / self.ny)), self.ny - 1)
+        v = float(self.values[iy * self.nx + ix])
+        return v if math.isfinite(v) else None
+
+
+def list_raster_layers(path) -> List[str]:
+    """gpkg.rs:586-599."""
+    con = _open(path)
+    try:
+        try:
+            rows = con.execute("SELECT table_name FROM gpkg_contents WHERE data_type = "
+                               "'2d-gridded-coverage' ORDER BY table_name").fetchall()
+        except sqlite3.Error as e:
+            raise IoError(f"querying gpkg_contents (is this a GeoPackage?): {e}") from e
+        return [r[0] for r in rows]
+    finally:
+        con.close()
+
+
+_MAX_TILE_DIM = 1 << 16
+_MAX_RASTER_CELLS = 1 << 28
+
+
+def read_raster(path, layer: Optional[str] = None) -> RasterGrid:
+    """gpkg.rs:609-755: an integer (PNG-tile) coverage at its finest zoom
+    level, tiles mosaicked, rows flipped into grid order; tile-matrix
+    dimensions outside [1, 65536] or more than 2^28 cells are rejected."""
+    names = list_raster_layers(path)
+    if not names:
+        raise IoError(f"no 2d-gridded-coverage layers found in {path}")
+    if layer is not None:
+        if layer not in names:
+            raise IoError(f"raster layer '{layer}' not found in {path}")
+        name = layer
+    else:
+        if len(names) > 1:
+            raise IoError(f"{path} has multiple raster layers; choose one with --layer "
+                          f"(available: {', '.join(names)})")
+        name = names[0]
+    con = _open(path)
+    try:
+        row = con.execute("SELECT datatype, scale, offset, data_null FROM "
+                          "gpkg_2d_gridded_coverage_ancillary WHERE tile_matrix_set_name = ?",
+                          (name,)).fetchone()
+        if row is None:
+            raise IoError(f"reading coverage ancillary for '{name}'")
+        datatype, scale, offset, data_null = row
+        if datatype != "integer":
+            raise IoError(f"coverage '{name}' has datatype '{datatype}'; only 'integer' (PNG) "
+                          "is supported")
+        null_px = 0.0 if data_null is None else float(data_null)
+        srs, min_x, min_y, max_x, max_y = con.execute(
+            "SELECT srs_id, min_x, min_y, max_x, max_y FROM gpkg_tile_matrix_set WHERE "
+            "table_name = ?", (name,)).fetchone()
+        zoom, mw, mh, tw, th = con.execute(
+            "SELECT zoom_level, matrix_width, matrix_height, tile_width, tile_height FROM "
+            "gpkg_tile_matrix WHERE table_name = ? ORDER BY zoom_level DESC LIMIT 1",
+            (name,)).fetchone()
+        for label, val in (("matrix_width", mw), ("matrix_height", mh), ("tile_width", tw),
+                           ("tile_height", th)):
+            if not 1 <= val <= _MAX_TILE_DIM:
+                raise IoError(f"coverage '{name}': {label} = {val} is out of the expected range "
+                              f"[1, {_MAX_TILE_DIM}]")
+        nx, ny = mw * tw, mh * th
+        if nx * ny > _MAX_RASTER_CELLS:
+            raise IoError(f"coverage '{name}': raster is {nx}x{ny} ({nx * ny} cells), exceeding "
+                          f"the {_MAX_RASTER_CELLS}-cell sanity limit")
+        img = np.full((ny, nx), np.nan)
+        for tcol, trow, blob in con.execute(
+                f"SELECT tile_column, tile_row, tile_data FROM {quote_ident(name)} WHERE "
+                "zoom_level = ?", (zoom,)):
+            px = decode_png_u16(blob, tw, th).astype(np.float64)
+            vals = np.where(px == null_px, np.nan, px * scale + offset)
+            r0, c0 = trow * th, tcol * tw
+            if r0 >= ny or c0 >= nx or r0 < 0 or c0 < 0:
+                continue
+            r1, c1 = min(r0 + th, ny), min(c0 + tw, nx)
+            img[r0:r1, c0:c1] = vals[:r1 - r0, :c1 - c0]
+    finally:
+        con.close()
+    return RasterGrid(name, int(srs), int(nx), int(ny), (min_x, min_y, max_x, max_y),
+                      img[::-1].reshape(-1).copy())
