@@ -12,12 +12,13 @@ from .errors import (CudaError, DimensionMismatch, DuplicatePoints, GeostatError
 from .model import Anisotropy, Structure, VariogramModel, parse_kind
 from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Server, TuneResult,
                   VecchiaPlan, block_cv, block_offsets, clustered_points, k_fold, krige,
-                  krige_3d, krige_grid,
+                  krige_3d, krige_grid, loo_cv,
                   last_timings, leave_one_out, leave_one_out_with_drift, maxmin_order,
                   tune_kriging_neighbors,
                   nelder_mead_multistart, rff_field, rng_normal, rng_uniform, seq_mean,
                   vecchia_krige, vecchia_loglik, vecchia_loglik_grouped, vecchia_mle, vecchia_mle_fit,
-                  vecchia_mle_grouped_fit, vecchia_mle_nm_fit, vecchia_predict, vecchia_reml,
+                  vecchia_mle_grouped_fit, vecchia_mle_nm_fit, vecchia_param_se,
+                  vecchia_param_se_fit, vecchia_predict, vecchia_reml,
                   vecchia_reml_drift, vecchia_reml_drift_fit, vecchia_reml_fit)
 from . import io  # geostat_rs.gpkg (sqlite3) is imported on use
 from ._abi import LIB_PATH, load as load_library

@@ -18,6 +18,7 @@ computes estimates.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 from typing import Optional, Sequence, Tuple
 
@@ -483,6 +484,32 @@ def block_cv(data: "PointSet", model: VariogramModel, config: KrigingConfig, blo
     return CvResult(np.array(data.values, dtype=float), pred, var)
 
 
+def loo_cv(x, y, values, model, method="ordinary", mean=None, degree=1, max_neighbors=None,
+           radius=None, folds=None, seed=0, min_neighbors=None, octant=None, blocks=None,
+           precision: str = "mixed") -> dict:
+    """lib.rs:695-745 ``loo_cv``: leave-one-out, ``folds``-fold or spatial
+    ``blocks`` = (nx, ny) cross-validation, as a dict of the accuracy
+    measures plus observed / predicted / variance."""
+    data = PointSet.from_xyz(x, y, values)
+    cfg = _build_method(method, mean, degree, values)
+    cfg.max_neighbors = max_neighbors
+    cfg.search_radius = radius
+    cfg.min_neighbors = min_neighbors
+    cfg.max_per_octant = octant
+    if blocks is not None and folds is not None:
+        raise InvalidParameter("blocks and folds are mutually exclusive")
+    if blocks is not None:
+        cv = block_cv(data, model, cfg, [blocks[0], blocks[1]], precision)
+    elif folds is not None:
+        cv = k_fold(data, model, cfg, int(folds), int(seed), precision)
+    else:
+        cv = leave_one_out(data, model, cfg, precision)
+    return {"me": cv.mean_error(), "mae": cv.mae(), "mse": cv.mse(), "rmse": cv.rmse(),
+            "msdr": cv.msdr(), "rme": cv.rme(), "rmae": cv.rmae(), "rrmse": cv.rrmse(),
+            "vecv": cv.vecv(), "e1": cv.e1(), "observed": cv.observed,
+            "predicted": cv.predicted, "variance": cv.variance}
+
+
 @dataclass
 class TuneResult:
     """``tuning::TuneResult``: the best candidate, its VEcv and the trace."""
@@ -817,6 +844,127 @@ def vecchia_reml_drift_fit(data: PointSet, drift, kind="exponential", m=20, orde
                                                  _p(o, C.c_int64), int(group_size), C.byref(out),
                                                  C.byref(ll), _p(x), C.byref(ne)))
     return _fit_result(kname, out, ll, x, ne)
+
+
+def _se_from_hessian(hess):
+    """vecchia.rs:1918-1935 se_from_hessian: sqrt of the diagonal of the
+    inverse (lu_factor's partial pivoting and singular test), NaN for a
+    singular matrix or a non-positive diagonal entry."""
+    n = len(hess)
+    a = [list(map(float, row)) for row in hess]
+    scale = max(max(abs(v) for v in row) for row in a)
+    scale = max(scale, 2.2250738585072014e-308)
+    piv = list(range(n))
+    for k in range(n):
+        p = max(range(k, n), key=lambda i: (abs(a[i][k]), -i))
+        if abs(a[p][k]) < 1e-12 * scale:
+            return [float("nan")] * n
+        piv[k] = p
+        a[k], a[p] = a[p], a[k]
+        for i in range(k + 1, n):
+            f = a[i][k] / a[k][k]
+            a[i][k] = f
+            if f != 0.0:
+                for j in range(k + 1, n):
+                    a[i][j] -= f * a[k][j]
+    out = []
+    for col in range(n):
+        b = [1.0 if q == col else 0.0 for q in range(n)]
+        for k in range(n):
+            b[k], b[piv[k]] = b[piv[k]], b[k]
+        for i in range(n):
+            b[i] -= sum(a[i][j] * b[j] for j in range(i))
+        for i in range(n - 1, -1, -1):
+            b[i] = (b[i] - sum(a[i][j] * b[j] for j in range(i + 1, n))) / a[i][i]
+        out.append(math.sqrt(b[col]) if b[col] > 0.0 else float("nan"))
+    return out
+
+
+def vecchia_param_se_fit(data: PointSet, model: VariogramModel, m: int = 20, order=None):
+    """``vecchia_param_se`` (vecchia.rs:1666-1918): asymptotic standard errors
+    of (nugget, partial sill, range) from the semi-analytical Hessian -- the
+    analytical gradient (one batched launch for all the +-h points)
+    differenced centrally with h = max(1e-3 |theta|, 1e-5) and symmetrised.
+    A nugget within one step of zero gives NaN for it and the SEs of the
+    restricted (sill, range) problem."""
+    from .model import GPU_KINDS
+    if len(model.structures) != 1:
+        raise InvalidParameter("standard errors are defined for a single-structure model")
+    st0 = model.structures[0]
+    kname = _fit_kind(st0.kind)
+    if kname == "power":
+        raise InvalidParameter("Vecchia needs a valid covariance function and cannot use the "
+                               "unbounded Power model")
+    if kname not in GPU_KINDS:
+        raise InvalidParameter("the CUDA path has closed-form gradients for spherical, "
+                               "exponential, gaussian, matern15 and matern25")
+    plan = VecchiaPlan(data, m, order)
+    theta = [model.nugget, st0.sill, st0.range]
+    h = [max(abs(t) * 1e-3, 1e-5) for t in theta]
+    free = [1, 2] if theta[0] - h[0] < 0.0 else [0, 1, 2]
+    pts = []
+    for i in free:
+        for sgn in (1.0, -1.0):
+            t = list(theta)
+            t[i] += sgn * h[i]
+            pts.append(t)
+    ok = all(t[1] > 0.0 and t[2] > 0.0 and t[0] >= 0.0 for t in pts)
+    hess = None
+    if ok:
+        mods = [VariogramModel(t[0], [Structure(kname, t[1], t[2])]) for t in pts]
+        _, g, st = plan.loglik_grad(mods)
+        if (st == 0).all() and np.isfinite(g).all():
+            k = len(free)
+            hess = [[0.0] * k for _ in range(k)]
+            for a, i in enumerate(free):
+                gp, gm = -g[2 * a], -g[2 * a + 1]  # gradients of the negative log-likelihood
+                for b, j in enumerate(free):
+                    hess[a][b] = (gp[j] - gm[j]) / (2.0 * h[i])
+            for a in range(k):
+                for b in range(a + 1, k):
+                    avg = 0.5 * (hess[a][b] + hess[b][a])
+                    hess[a][b] = hess[b][a] = avg
+    if hess is None:
+        # the fully numerical Hessian of the negative log-likelihood
+        def nll_batch(ts):
+            mods = [VariogramModel(t[0], [Structure(kname, t[1], t[2])]) for t in ts]
+            ll, st = plan.loglik(mods)
+            return [(-l if (s == 0 and np.isfinite(l) and t[1] > 0 and t[2] > 0 and t[0] >= 0)
+                     else float("inf")) for l, s, t in zip(ll, st, ts)]
+        k = len(free)
+        ts = [list(theta)]
+        for a, i in enumerate(free):
+            for sgn in (1.0, -1.0):
+                t = list(theta)
+                t[i] += sgn * h[i]
+                ts.append(t)
+        for a in range(k):
+            for b in range(a + 1, k):
+                i, j = free[a], free[b]
+                for si, sj in ((1, 1), (1, -1), (-1, 1), (-1, -1)):
+                    t = list(theta)
+                    t[i] += si * h[i]
+                    t[j] += sj * h[j]
+                    ts.append(t)
+        f = nll_batch(ts)
+        hess = [[0.0] * k for _ in range(k)]
+        q = 1 + 2 * k
+        for a, i in enumerate(free):
+            hess[a][a] = (f[1 + 2 * a] - 2.0 * f[0] + f[2 + 2 * a]) / (h[i] * h[i])
+        for a in range(k):
+            for b in range(a + 1, k):
+                i, j = free[a], free[b]
+                v = (f[q] - f[q + 1] - f[q + 2] + f[q + 3]) / (4.0 * h[i] * h[j])
+                q += 4
+                hess[a][b] = hess[b][a] = v
+    se = _se_from_hessian(hess)
+    return (float("nan"), se[0], se[1]) if len(free) == 2 else tuple(se)
+
+
+def vecchia_param_se(x, y, values, model, m=20):
+    """lib.rs:419-437 ``vecchia_param_se``."""
+    data = PointSet.from_xyz(x, y, values)
+    return vecchia_param_se_fit(data, model, m)
 
 
 def vecchia_reml(x, y, values, kind="exponential", m=20, drift_degree=1):

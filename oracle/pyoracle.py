@@ -698,3 +698,45 @@ def rust_display(x):
     if "." in s:
         s = s.rstrip("0").rstrip(".")
     return s
+
+
+# ------------------------------------------------- Vecchia parameter SEs ---
+def vecchia_param_se(coords, values, kind, nugget, psill, rng, m, order=None):
+    """vecchia.rs:1666-1935 vecchia_param_se for a closed-form kind: the
+    central difference of the analytical gradient (loglik_grad_with_plan),
+    symmetrised; a nugget within one step of zero gives NaN for it and the
+    restricted (sill, range) SEs; sqrt of the inverse's diagonal through
+    lu_factor / Lu::solve, NaN when singular or non-positive."""
+    coords, values = _f64(coords), _f64(values)
+    o, nb, cnt = vecchia_plan(coords, m, order)
+    theta = [float(nugget), float(psill), float(rng)]
+    h = [max(abs(t) * 1e-3, 1e-5) for t in theta]
+    free = [1, 2] if theta[0] - h[0] < 0.0 else [0, 1, 2]
+
+    def grad_nll(t):
+        _, g = vecchia_loglik_grad(coords, values, kind, t[0], t[1], t[2], o, nb, cnt)
+        return [-g[0], -g[1], -g[2]]
+
+    k = len(free)
+    hess = np.zeros((k, k))
+    for a, i in enumerate(free):
+        tp, tm = list(theta), list(theta)
+        tp[i] += h[i]
+        tm[i] -= h[i]
+        gp, gm = grad_nll(tp), grad_nll(tm)
+        for b, j in enumerate(free):
+            hess[a, b] = (gp[j] - gm[j]) / (2.0 * h[i])
+    for a in range(k):
+        for b in range(a + 1, k):
+            avg = 0.5 * (hess[a, b] + hess[b, a])
+            hess[a, b] = hess[b, a] = avg
+    se = []
+    for col in range(k):
+        e = np.zeros(k)
+        e[col] = 1.0
+        try:
+            x = lu_solve(hess, e)
+        except OracleError:
+            return [float("nan")] * 3
+        se.append(float(np.sqrt(x[col])) if x[col] > 0.0 else float("nan"))
+    return [float("nan"), se[0], se[1]] if k == 2 else se

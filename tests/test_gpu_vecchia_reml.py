@@ -180,3 +180,43 @@ def test_reml_large_sets_and_sorted_order_blocks():
             assert abs(llg[i] - ref) <= 1e-9 * abs(ref), (g, i, llg[i], ref)
             ref = O.vecchia_reml_loglik(c, v, mdl, order, nb, cnt, f, g)
             assert abs(llr[i] - ref) <= 1e-9 * abs(ref), (g, i, llr[i], ref)
+
+
+@pytest.mark.parametrize("seed,nug", [(31, 0.2), (51, 0.0)])
+def test_param_se_matches_oracle(seed, nug):
+    """vecchia_param_se (vecchia.rs:1666-1935): the batched GPU gradients
+    give the oracle's semi-analytical standard errors (finite differences of
+    the gradient: agreement at 1e-6 relative)."""
+    truth = VariogramModel(nug, [Structure("exponential", 1.0, 12.0)])
+    u, eps = O.rng_draw(seed, 280, 140)
+    c = u.reshape(140, 2) * 60.0
+    v = np.linalg.cholesky(_cov_matrix(c, truth)) @ eps
+    model = VariogramModel(nug, [Structure("exponential", 1.1, 13.0)])
+    got = G.vecchia_param_se_fit(G.PointSet(c, v), model, 12)
+    ref = O.vecchia_param_se(c, v, "exponential", nug, 1.1, 13.0, 12)
+    for a, b in zip(got, ref):
+        if np.isnan(b):
+            assert np.isnan(a)
+        else:
+            assert abs(a - b) <= 1e-6 * abs(b), (got, ref)
+    if nug == 0.0:
+        assert np.isnan(got[0]) and got[1] > 0 and got[2] > 0
+    got2 = G.vecchia_param_se(c[:, 0], c[:, 1], v, model, 12)
+    assert np.allclose(got2, got, equal_nan=True)
+
+
+def test_loo_cv_binding_forms():
+    """lib.rs:695-745 loo_cv: leave-one-out, k-fold and block forms."""
+    c = uniform_points(300, 2, 221, [100.0, 100.0])
+    v = np.sin(c[:, 0] / 20.0) + np.cos(c[:, 1] / 20.0)
+    m = VariogramModel(0.01, [Structure("spherical", 1.0, 50.0)])
+    loo = G.loo_cv(c[:, 0], c[:, 1], v, m, max_neighbors=16)
+    kf = G.loo_cv(c[:, 0], c[:, 1], v, m, max_neighbors=16, folds=5, seed=3)
+    bl = G.loo_cv(c[:, 0], c[:, 1], v, m, max_neighbors=16, blocks=(3, 3))
+    for d in (loo, kf, bl):
+        assert set(d) >= {"me", "mae", "rmse", "msdr", "vecv", "e1", "observed", "predicted",
+                          "variance"}
+        assert np.isfinite(d["predicted"]).all()
+    assert bl["rmse"] >= loo["rmse"]
+    with pytest.raises(G.InvalidParameter):
+        G.loo_cv(c[:, 0], c[:, 1], v, m, folds=5, blocks=(2, 2))

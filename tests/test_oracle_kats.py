@@ -720,3 +720,28 @@ def test_block_cv_is_harsher_than_random_k_fold():
     rnd = CvResult(v, *_oracle_fold_cv(c, v, m, kf))
     blk = CvResult(v, *_oracle_fold_cv(c, v, m, O.spatial_block_assignment(c, [5, 5])))
     assert blk.rmse() >= rnd.rmse()
+
+
+# ------------------------------------------------ Vecchia parameter SEs ------
+def _gp_draw(seed, n, truth):
+    u, eps = O.rng_draw(seed, 2 * n, n)
+    c = u.reshape(n, 2) * 60.0
+    return c, np.linalg.cholesky(_cov_matrix(c, truth)) @ eps
+
+
+def test_param_se_are_finite_and_informative():
+    # vecchia.rs:2651-2683
+    c, v = _gp_draw(31, 140, _exp_model(0.2, 12.0))
+    x, _, _ = O.vecchia_mle_bfgs(c, v, "exponential", 12)
+    rng_ = math.exp(x[2])
+    se = O.vecchia_param_se(c, v, "exponential", x[0] ** 2, math.exp(x[1]), rng_, 12)
+    assert np.isfinite(se[1]) and se[1] > 0
+    assert np.isfinite(se[2]) and 0 < se[2] < rng_
+
+
+def test_param_se_at_the_zero_nugget_boundary():
+    # vecchia.rs:2686-2725
+    c, v = _gp_draw(51, 140, _exp_model(0.0, 12.0))
+    se = O.vecchia_param_se(c, v, "exponential", 0.0, 1.0, 12.0, 12)
+    assert np.isnan(se[0])
+    assert np.isfinite(se[1]) and se[1] > 0 and np.isfinite(se[2]) and se[2] > 0
