@@ -153,3 +153,20 @@ def test_invalid_inputs_rejected_before_any_device_work():
         G.PointSet(np.array([[0.0, 0.0]]), np.array([np.inf]))
     with pytest.raises(G.DimensionMismatch):
         G.PointSet(np.zeros((2, 2)), np.zeros(3))
+
+
+def test_se_from_hessian_matches_the_oracle_lu():
+    """vecchia.rs:1918-1935: sqrt of the inverse's diagonal through
+    lu_factor / Lu::solve; NaN when singular or non-positive."""
+    from geostat_rs.api import _se_from_hessian
+    rng = np.random.default_rng(12)
+    for _ in range(20):
+        a = rng.normal(size=(3, 3))
+        h = a @ a.T + 0.1 * np.eye(3)
+        got = _se_from_hessian(h.tolist())
+        inv = np.stack([O.lu_solve(h, np.eye(3)[i]) for i in range(3)], 1)
+        want = [np.sqrt(inv[i, i]) if inv[i, i] > 0 else np.nan for i in range(3)]
+        np.testing.assert_allclose(got, want, rtol=1e-12)
+    assert all(np.isnan(_se_from_hessian([[1.0, 2.0], [2.0, 4.0]])))
+    se = _se_from_hessian([[-1.0, 0.0], [0.0, 2.0]])
+    assert np.isnan(se[0]) and abs(se[1] - np.sqrt(0.5)) < 1e-15
