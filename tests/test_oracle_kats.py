@@ -745,3 +745,51 @@ def test_param_se_at_the_zero_nugget_boundary():
     se = O.vecchia_param_se(c, v, "exponential", 0.0, 1.0, 12.0, 12)
     assert np.isnan(se[0])
     assert np.isfinite(se[1]) and se[1] > 0 and np.isfinite(se[2]) and se[2] > 0
+
+
+# ------------------------------------------- anisotropic search and limits ---
+def test_anisotropic_search_radius_is_the_major_axis_radius():
+    # kriging.rs:1068-1100: the radius is the ellipse's major-axis radius
+    c = np.array([[0.0, 5.0], [5.0, 0.0]])
+    v = np.array([100.0, 999.0])
+    r = O.krige(c, v, sph_model(), np.array([[0.0, 0.0]]), radius=5.0,
+                anisotropic_search=Anisotropy(0.0, 0.5))
+    assert r["status"][0] == 0 and abs(r["value"][0] - 100.0) < 1e-6
+
+
+def test_anisotropic_search_octants_follow_the_rotated_frame():
+    # kriging.rs:1102-1150
+    c = [[0.1, 1.0], [-0.1, 1.1], [0.2, 1.2], [-0.2, 1.3], [0.05, 1.4],
+         [0.5, -2.0], [-0.5, -2.0], [-2.0, 0.5], [2.0, 0.5]]
+    v = [10.0] * 5 + [0.0] * 4
+    t = np.array([[0.0, 0.0]])
+    nearest = O.krige(c, v, sph_model(), t, max_neighbors=4)["value"][0]
+    octant = O.krige(c, v, sph_model(), t, max_neighbors=4, max_per_octant=1,
+                     anisotropic_search=Anisotropy(90.0, 1.0))["value"][0]
+    assert nearest > 9.0 and octant < nearest - 2.0
+
+
+def test_anisotropic_search_works_in_3d_with_dip():
+    # kriging.rs:1152-1178: azimuth 0, dip 90 points the major axis along +z
+    c = np.array([[0.0, 0.0, 4.0], [4.0, 0.0, 0.0]])
+    v = np.array([100.0, 0.0])
+    r = O.krige(c, v, sph_model(), np.array([[0.0, 0.0, 0.0]]), max_neighbors=1,
+                anisotropic_search=Anisotropy(0.0, 0.2, 1.0, 90.0, 0.0))
+    assert abs(r["value"][0] - 100.0) < 1e-6
+
+
+def test_anisotropic_model_weights_by_direction():
+    # kriging.rs:1380-1402
+    c = np.array([[0.0, 30.0], [30.0, 0.0], [-25.0, -25.0]])
+    v = np.array([10.0, 0.0, 5.0])
+    m = VariogramModel(0.0, [Structure.with_anisotropy("spherical", 1.0, 100.0, 0.0, 0.25)])
+    assert O.krige(c, v, m, np.array([[0.0, 0.0]]))["value"][0] > 5.0
+
+
+def test_neighborhood_limits_apply():
+    # kriging.rs:1404-1420: nothing within the radius is NoNeighbors; a datum
+    # is reproduced
+    c, v = sample_data()
+    r = O.krige(c, v, sph_model(), np.array([[0.5, 0.2], c[0]]), max_neighbors=3, radius=0.001)
+    assert r["status"][0] == 5 and np.isnan(r["value"][0])
+    assert r["status"][1] == 0 and abs(r["value"][1] - v[0]) < 1e-8
