@@ -2574,6 +2574,19 @@ int or_spatial_block_assignment(int dim, int64_t n, const double* coords, const 
   return OR_OK;
 }
 
+// vecchia.rs:577-602 guinness_blocks on a plan given as arrays: k1 of each
+// block (block b covers [k1[b - 1], k1[b])), their number in *nblocks.
+int or_guinness_blocks(int64_t n, int64_t m, const int64_t* order, const int64_t* nb,
+                       const int32_t* nb_count, int64_t group_size, int64_t* k1,
+                       int64_t* nblocks) {
+  Plan plan;
+  plan_from_arrays((size_t)n, (size_t)m, order, nb, nb_count, plan);
+  auto blocks = guinness_blocks(plan, (size_t)group_size);
+  for (size_t b = 0; b < blocks.size(); ++b) k1[b] = (int64_t)blocks[b].second;
+  *nblocks = (int64_t)blocks.size();
+  return OR_OK;
+}
+
 int64_t or_poly_basis_terms(int dim, int32_t degree) {
   std::vector<std::array<int, 3>> exps;
   int cur[3] = {0, 0, 0};

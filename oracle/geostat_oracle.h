@@ -165,6 +165,10 @@ int or_krige_block(int dim, int64_t n, const double* coords, const double* value
 /* validation.rs:298-328 spatial_block_assignment (fold index per point). */
 int or_spatial_block_assignment(int dim, int64_t n, const double* coords, const int64_t* bpd,
                                 int64_t* fold_of);
+/* vecchia.rs:577-602 guinness_blocks: block ends k1[0 .. *nblocks). */
+int or_guinness_blocks(int64_t n, int64_t m, const int64_t* order, const int64_t* nb,
+                       const int32_t* nb_count, int64_t group_size, int64_t* k1,
+                       int64_t* nblocks);
 /* vecchia.rs:1181-1233 poly_basis (row-major n x p, p = or_poly_basis_terms)
  * and vecchia.rs:1246-1272 standardized_drift_basis (n x (1 + ncov)). */
 int64_t or_poly_basis_terms(int dim, int32_t degree);

@@ -120,6 +120,7 @@ def _declare(L):
         "or_krige_block": (C.c_int, [C.c_int, i64, pd, pd, pd, C.c_int, pm, pk, i64, pd, pd, i64,
                                      pd, pd, pd, pi8]),
         "or_spatial_block_assignment": (C.c_int, [C.c_int, i64, pd, pi64, pi64]),
+        "or_guinness_blocks": (C.c_int, [i64, i64, pi64, pi64, pi32, i64, pi64, pi64]),
         "or_poly_basis_terms": (i64, [C.c_int, i32]),
         "or_poly_basis": (C.c_int, [C.c_int, i64, pd, i32, pd]),
         "or_drift_basis": (C.c_int, [i64, i64, pd, pd]),
@@ -487,6 +488,19 @@ def vecchia_mle_nm(coords, values, kind, m, starts, step=0.3, max_iter=2000, ord
         _p(o, C.c_int64) if o is not None else None, len(starts), _p(starts), C.c_double(step),
         int(max_iter), _p(x), C.byref(f), C.byref(ne)))
     return x, f.value, ne.value
+
+
+def guinness_blocks(order, nb, cnt, group_size):
+    """vecchia.rs:577-602: the blocks [(k0, k1), ...] of a plan."""
+    n, m = nb.shape
+    k1 = np.zeros(n, dtype=np.int64)
+    nbk = C.c_int64()
+    _check(lib().or_guinness_blocks(n, m, _p(np.ascontiguousarray(order, np.int64), C.c_int64),
+                                    _p(np.ascontiguousarray(nb, np.int64), C.c_int64),
+                                    _p(np.ascontiguousarray(cnt, np.int32), C.c_int32),
+                                    int(group_size), _p(k1, C.c_int64), C.byref(nbk)))
+    ends = k1[:nbk.value].tolist()
+    return list(zip([0] + ends[:-1], ends))
 
 
 def poly_basis(coords, degree):

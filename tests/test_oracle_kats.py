@@ -793,3 +793,75 @@ def test_neighborhood_limits_apply():
     r = O.krige(c, v, sph_model(), np.array([[0.5, 0.2], c[0]]), max_neighbors=3, radius=0.001)
     assert r["status"][0] == 5 and np.isnan(r["value"][0])
     assert r["status"][1] == 0 and abs(r["value"][1] - v[0]) < 1e-8
+
+
+# ---------------------------------------------- more Vecchia known answers ---
+def test_guinness_blocks_partition_the_order_within_group_size():
+    # vecchia.rs:2031-2048
+    c, _ = O.test_field_2d(4000, 42)
+    o, nb, cnt = O.vecchia_plan(c, 30)
+    for g in (2, 4, 8, 16):
+        covered = 0
+        for k0, k1 in O.guinness_blocks(o, nb, cnt, g):
+            assert k0 == covered and 0 < k1 - k0 <= g
+            covered = k1
+        assert covered == len(c)
+
+
+def test_mle_full_conditioning_is_exact_optimum():
+    # vecchia.rs:2228-2259
+    c, v = O.test_field_2d(28, 5)
+    full = len(c) - 1
+    x, f, _ = O.vecchia_mle_bfgs(c, v, "exponential", full)
+    nug, sill, rng_ = x[0] ** 2, math.exp(x[1]), math.exp(x[2])
+    assert sill > 0 and rng_ > 0 and nug >= 0
+    for fn_, fp, fr in ((1.0, 0.7, 1.0), (1.0, 1.4, 1.0), (1.0, 1.0, 0.7), (1.0, 1.0, 1.4),
+                        (3.0, 1.0, 1.0)):
+        pert = VariogramModel(max(nug * fn_, 1e-9), [Structure("exponential", sill * fp, rng_ * fr)])
+        assert -f >= O.vecchia_loglik(c, v, pert, full) - 1e-6
+
+
+def test_mle_beats_a_wrong_model():
+    # vecchia.rs:2261-2270
+    c, v = O.test_field_2d(60, 9)
+    _, f, _ = O.vecchia_mle_bfgs(c, v, "exponential", 12)
+    wrong = VariogramModel(0.5, [Structure("exponential", 0.1, 5.0)])
+    assert -f > O.vecchia_loglik(c, v, wrong, 15)
+
+
+def test_semi_analytical_se_matches_the_full_finite_difference_reference():
+    # vecchia.rs:2727-2755 (with nll_hessian_se_reference, :2739-2799)
+    c, v = O.test_field_2d(80, 17)
+    o, nb, cnt = O.vecchia_plan(c, 10)
+    theta = [0.08, 0.9, 18.0]
+
+    def nll(p):
+        if p[1] <= 0 or p[2] <= 0 or p[0] < 0:
+            return math.inf
+        mdl = VariogramModel(p[0], [Structure("matern15", p[1], p[2])])
+        return -O.vecchia_loglik_plan(c, v, mdl, o, nb, cnt)
+
+    h = [max(abs(t) * 1e-3, 1e-5) for t in theta]
+    f0 = nll(theta)
+    hess = np.zeros((3, 3))
+    for i in range(3):
+        tp, tm = list(theta), list(theta)
+        tp[i] += h[i]
+        tm[i] -= h[i]
+        hess[i, i] = (nll(tp) - 2 * f0 + nll(tm)) / (h[i] * h[i])
+        for j in range(i + 1, 3):
+            q = []
+            for si, sj in ((1, 1), (1, -1), (-1, 1), (-1, -1)):
+                t = list(theta)
+                t[i] += si * h[i]
+                t[j] += sj * h[j]
+                q.append(nll(t))
+            hess[i, j] = hess[j, i] = (q[0] - q[1] - q[2] + q[3]) / (4 * h[i] * h[j])
+    diag = [O.lu_solve(hess, np.eye(3)[i])[i] for i in range(3)]
+    ref = [math.sqrt(d) if d > 0 else math.nan for d in diag]
+    new = O.vecchia_param_se(c, v, "matern15", *theta, 10)
+    for a, b in zip(new, ref):
+        if math.isnan(b):
+            assert math.isnan(a)
+        else:
+            assert abs(a - b) < 1e-3 * max(b, 1.0)
