@@ -865,3 +865,37 @@ def test_semi_analytical_se_matches_the_full_finite_difference_reference():
             assert math.isnan(a)
         else:
             assert abs(a - b) < 1e-3 * max(b, 1.0)
+
+
+# --------------------------------------------------- tests/three_d.rs ---------
+def test_universal_kriging_3d_reproduces_drift():
+    # tests/three_d.rs:77-110
+    c = np.array([[i * 10.0, j * 10.0, l * 5.0] for i in range(4) for j in range(4)
+                  for l in range(3)])
+    v = 1.0 + 0.2 * c[:, 0] - 0.1 * c[:, 1] + 0.5 * c[:, 2]
+    m = VariogramModel(0.05, [Structure("exponential", 1.0, 30.0)])
+    t = np.array([[15.0, 25.0, 7.5]])
+    r = O.krige(c, v, m, t, method="universal", degree=1)
+    assert abs(r["value"][0] - (1.0 + 0.2 * 15.0 - 0.1 * 25.0 + 0.5 * 7.5)) < 1e-7
+
+
+def test_vertical_anisotropy_shortens_z_range():
+    # tests/three_d.rs:112-134
+    m = VariogramModel(0.0, [Structure("spherical", 1.0, 100.0, Anisotropy(0.0, 1.0, 0.25))])
+    assert abs(O.gamma_dh(m, [0.0, 100.0, 0.0]) - 1.0) < 1e-12
+    assert abs(O.gamma_dh(m, [0.0, 0.0, 25.0]) - 1.0) < 1e-12
+    assert O.gamma_dh(m, [0.0, 0.0, 10.0]) > O.gamma_dh(m, [0.0, 10.0, 0.0])
+
+
+def test_block_kriging_3d_uses_z_separation():
+    # tests/three_d.rs:219-254
+    c, v = O.test_field_3d(100, 13)
+    m = VariogramModel(0.05, [Structure("spherical", 1.0, 30.0)])
+    ctr = np.array([[42.0, 37.0, 18.0]])
+    block = O.krige_block(c, v, m, ctr, [[0.0, 0.0, 0.0]])
+    point = O.krige(c, v, m, ctr)
+    assert abs(block["value"][0] - point["value"][0]) < 1e-10
+    assert abs(block["variance"][0] - (point["variance"][0] - m.nugget)) < 1e-10
+    deg = O.krige_block(c, v, m, ctr, [[0.0, 0.0, 0.0], [0.0, 0.0, 0.0]])
+    ver = O.krige_block(c, v, m, ctr, [[0.0, 0.0, -5.0], [0.0, 0.0, 5.0]])
+    assert abs(ver["value"][0] - deg["value"][0]) > 1e-6 and ver["variance"][0] >= 0.0
