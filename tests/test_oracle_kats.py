@@ -899,3 +899,56 @@ def test_block_kriging_3d_uses_z_separation():
     deg = O.krige_block(c, v, m, ctr, [[0.0, 0.0, 0.0], [0.0, 0.0, 0.0]])
     ver = O.krige_block(c, v, m, ctr, [[0.0, 0.0, -5.0], [0.0, 0.0, 5.0]])
     assert abs(ver["value"][0] - deg["value"][0]) > 1e-6 and ver["variance"][0] >= 0.0
+
+
+# ------------------------------------------- validation.rs / tuning.rs -------
+def _fold_assignment(n, k, seed):
+    # validation.rs:201-213 (rng.rs shuffle: Fisher-Yates from the end)
+    order = np.arange(n)
+    u = O.rng_u64(seed, n)
+    for idx, i in enumerate(range(n - 1, 0, -1)):
+        j = int(u[idx] % np.uint64(i + 1))
+        order[i], order[j] = order[j], order[i]
+    fold_of = np.empty(n, dtype=int)
+    fold_of[order] = np.arange(n) % k
+    return fold_of
+
+
+def test_k_equals_n_matches_leave_one_out_and_folds_are_balanced():
+    # validation.rs:1005-1037
+    from geostat_rs.api import CvResult
+    m = VariogramModel(0.01, [Structure("spherical", 1.0, 50.0)])
+    c, v = _smooth_field(40, 5)
+    fo = _fold_assignment(40, 40, 123)
+    assert sorted(fo) == list(range(40))
+    kf = _oracle_fold_cv(c, v, m, fo)
+    loo = _oracle_fold_cv(c, v, m, np.arange(40))
+    assert np.max(np.abs(kf[0] - loo[0])) < 1e-12 and np.max(np.abs(kf[1] - loo[1])) < 1e-12
+    c, v = _smooth_field(53, 8)
+    fo = _fold_assignment(53, 5, 42)
+    assert np.array_equal(fo, _fold_assignment(53, 5, 42))
+    sizes = np.bincount(fo)
+    assert sizes.sum() == 53 and sizes.max() - sizes.min() <= 1
+    assert CvResult(v, *_oracle_fold_cv(c, v, m, fo)).vecv() > 50.0
+
+
+def test_tunes_kriging_neighbors():
+    # tuning.rs:172-188 with tuning.rs:97-125 (the best leave-one-out VEcv)
+    from geostat_rs.api import CvResult
+    # tuning.rs:133-144 field(120, 9) draws the same stream as vecchia.rs's
+    # field (x, y uniform, then a normal, per point); only the signal differs
+    c, v = O.test_field_2d(120, 9)
+    noise = v - np.sin(c[:, 0] / 25.0) - np.cos(c[:, 1] / 30.0)
+    v = np.sin(c[:, 0] / 20.0) + np.cos(c[:, 1] / 25.0) + noise
+    m = VariogramModel(0.02, [Structure("spherical", 1.0, 40.0)])
+    trace = []
+    for k in (4, 8, 16, 32):
+        pred = np.empty(120)
+        var = np.empty(120)
+        for i in range(120):
+            keep = np.arange(120) != i
+            r = O.krige(c[keep], v[keep], m, c[i:i + 1], max_neighbors=k)
+            pred[i], var[i] = r["value"][0], r["variance"][0]
+        trace.append((k, CvResult(v, pred, var).vecv()))
+    best = max(trace, key=lambda kv: kv[1])
+    assert best[0] in (4, 8, 16, 32) and np.isfinite(best[1])
