@@ -952,3 +952,52 @@ def test_tunes_kriging_neighbors():
         trace.append((k, CvResult(v, pred, var).vecv()))
     best = max(trace, key=lambda kv: kv[1])
     assert best[0] in (4, 8, 16, 32) and np.isfinite(best[1])
+
+
+# ------------------------------------------------------ variogram/model.rs ---
+_GPU_KINDS = ("spherical", "exponential", "gaussian", "matern15", "matern25")
+
+
+def test_path_models_bounded_and_monotone_to_sill():
+    # variogram/model.rs all_models_bounded_and_monotone_to_sill (the kinds
+    # of the path)
+    for kind in _GPU_KINDS:
+        m = VariogramModel(0.0, [Structure(kind, 2.0, 50.0)])
+        prev = 0.0
+        for i in range(1, 101):
+            g = O.gamma_dh(m, [i * 5.0, 0.0])
+            assert prev - 1e-12 <= g <= 2.0 + 1e-12, kind
+            prev = g
+        assert O.gamma_dh(m, [5000.0, 0.0]) > 1.99, kind
+
+
+def test_anisotropy_stretches_minor_axis_and_zonal_ratio():
+    # variogram/model.rs anisotropy_stretches_minor_axis,
+    # zonal_anisotropy_ratio_above_one
+    m = VariogramModel(0.0, [Structure.with_anisotropy("spherical", 1.0, 100.0, 0.0, 0.5)])
+    assert abs(O.gamma_dh(m, [0.0, 100.0]) - 1.0) < 1e-12
+    assert O.gamma_dh(m, [0.0, 50.0]) < 1.0 - 1e-6
+    assert abs(O.gamma_dh(m, [50.0, 0.0]) - 1.0) < 1e-12
+    assert O.gamma_dh(m, [30.0, 0.0]) > O.gamma_dh(m, [0.0, 30.0])
+    iso = VariogramModel(0.1, [Structure("exponential", 0.9, 40.0)])
+    assert abs(O.gamma_dh(iso, [3.0, 4.0]) - O.gamma_dh(iso, [5.0, 0.0])) < 1e-12
+    z = VariogramModel(0.0, [Structure.with_anisotropy("spherical", 1.0, 50.0, 0.0, 2.0)])
+    assert abs(O.gamma_dh(z, [0.0, 50.0]) - 1.0) < 1e-12
+    assert abs(O.gamma_dh(z, [100.0, 0.0]) - 1.0) < 1e-12
+    assert O.gamma_dh(z, [50.0, 0.0]) < 1.0 - 1e-6
+    assert O.gamma_dh(z, [30.0, 0.0]) < O.gamma_dh(z, [0.0, 30.0])
+    mir = VariogramModel(0.0, [Structure.with_anisotropy("spherical", 1.0, 100.0, 90.0, 0.5)])
+    for dh in ([10.0, 20.0], [-35.0, 12.0], [60.0, -5.0]):
+        assert abs(O.gamma_dh(z, dh) - O.gamma_dh(mir, dh)) < 1e-12
+
+
+def test_rotation_3d_reduces_to_2d_style_when_dip_and_rake_are_zero():
+    # variogram/model.rs rotation_3d_reduces_to_2d_style_when_dip_and_rake_are_zero
+    full = VariogramModel(0.05, [Structure.with_rotation("exponential", 0.9, 80.0, 55.0, 0.0,
+                                                         0.0, 0.4, 0.6)])
+    az = math.radians(55.0)
+    s, c = math.sin(az), math.cos(az)
+    for x, y, zz in ((10.0, 20.0, 5.0), (-30.0, 15.0, -8.0), (40.0, -25.0, 0.0)):
+        hm, hn, hz = x * s + y * c, (x * c - y * s) / 0.4, zz / 0.6
+        old = 0.05 + 0.9 * (1.0 - math.exp(-math.sqrt(hm * hm + hn * hn + hz * hz) / 80.0))
+        assert abs(old - O.gamma_dh(full, [x, y, zz])) < 1e-12
