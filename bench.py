@@ -34,6 +34,8 @@ sys.path.insert(0, os.path.join(ROOT, "geostat-rs_gb300"))
 
 import numpy as np  # noqa: E402
 
+import gs_workload as W  # noqa: E402  (synthetic workloads and probes; no device work at import)
+
 METRIC = "kriged targets/s & Vecchia points/s, mixed-prec vs FP64 GPU @1e-9; p99 latency"
 WORKLOAD = ("3-D ordinary kriging: n=200,000 points in 2000x2000x200 m, RFF field (4,096 "
             "features) of nugget 0.05 + Sph(0.6; 300/150/40 m; az 30, dip 10) + Exp(0.35, 800 m); "
@@ -56,6 +58,14 @@ def make_model():
     return VariogramModel(0.05, [Structure.with_rotation("spherical", 0.6, 300.0, 30.0, 10.0, 0.0,
                                                          0.5, 40.0 / 300.0),
                                  Structure("exponential", 0.35, 800.0)])
+
+
+def workload_config(n_targets, world):
+    """The headline workload's config dict, identical in both arms."""
+    return {"workload": WORKLOAD, "n_data": N_DATA, "n_targets": n_targets,
+            "max_neighbors": K_NEIGH, "dim": 3,
+            "l2": "flushed between steps (256 MiB write); neighbour lists 1 GiB > L2",
+            "parallelism": f"replicas x{world} (targets independent)"}
 
 
 def make_coords():
@@ -158,7 +168,7 @@ def run_ours(args, rank, world):
     t0 = time.time()
     coords = make_coords()
     model = make_model()
-    values = G.rff_field(coords, model, 4096, SEED + 1)
+    values = W.rff_field(coords, model, 4096, SEED + 1)
     ps = G.PointSet(coords, values)
     kr = G.Kriging.new(ps, model, G.KrigingConfig(max_neighbors=K_NEIGH))
     tg = grid_targets()
@@ -276,9 +286,10 @@ def run_ours(args, rank, world):
         peak_fp32 = C.c_double()
         peak_fp64 = C.c_double()
         peak_x2 = C.c_double()
-        _abi.check(lib.gs_probe_fma_tflops(0, C.byref(peak_fp32)))
-        _abi.check(lib.gs_probe_fma_tflops(1, C.byref(peak_fp64)))
-        _abi.check(lib.gs_probe_fma_tflops(2, C.byref(peak_x2)))
+        wl = W.load()
+        _abi.check(wl.gs_probe_fma_tflops(0, C.byref(peak_fp32)))
+        _abi.check(wl.gs_probe_fma_tflops(1, C.byref(peak_fp64)))
+        _abi.check(wl.gs_probe_fma_tflops(2, C.byref(peak_x2)))
         bpt = read_profile_traffic()
         # one launch of the kriging kernel per step (the neighbour lists fit one chunk)
         traffic = bpt * nt if bpt is not None else None
@@ -305,10 +316,7 @@ def run_ours(args, rank, world):
             "vs_baseline": None,
             "dtype": "f32 factor + df64 refinement + f64 outputs",
             "data": "synthetic: seeded xoshiro256++ coordinates, random-Fourier-feature field",
-            "config": {"workload": WORKLOAD, "n_data": N_DATA, "n_targets": nt,
-                       "max_neighbors": K_NEIGH, "dim": 3,
-                       "l2": "flushed between steps (256 MiB write); neighbour lists 1 GiB > L2",
-                       "parallelism": f"replicas x{world} (targets independent)"},
+            "config": workload_config(nt, world),
             "phases_ms": {"search": search_ms, "mixed_solve": mixed_ms, "fp64_resolve": resolve_ms,
                           "fp64_resolved_targets": n_fallback, "failed_targets": n_fail},
             "fp64_gpu_build": {"value": fp64_value, "unit": "kriged targets/s",
@@ -441,7 +449,7 @@ def global_bench(args, log):
     n = 2000
     c = G.rng_uniform(SEED + 31, 2 * n).reshape(n, 2) * 1000.0
     m = VariogramModel(0.1, [Structure("spherical", 1.0, 200.0)])
-    v = 10.0 + G.rff_field(c, m, 2048, SEED + 32)
+    v = 10.0 + W.rff_field(c, m, 2048, SEED + 32)
     g = (np.arange(100) + 0.5) * 10.0
     yy, xx = np.meshgrid(g, g, indexing="ij")
     t = np.stack([xx.ravel(), yy.ravel()], 1)
@@ -484,7 +492,7 @@ def block_bench(args, log):
     n = 100_000
     c = G.rng_uniform(SEED + 41, 2 * n).reshape(n, 2) * 10000.0
     m = VariogramModel(0.1, [Structure("spherical", 1.0, 1500.0)])
-    v = 10.0 + G.rff_field(c, m, 2048, SEED + 42)
+    v = 10.0 + W.rff_field(c, m, 2048, SEED + 42)
     k = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig(max_neighbors=32))
     lo, hi, nc, bs, disc = [0.0, 0.0], [10000.0, 10000.0], [512, 512], [20.0, 20.0], [4, 4]
     k.predict_block_grid(lo, hi, nc, bs, disc)
@@ -524,7 +532,7 @@ def vecchia_bench(args, log):
     t0 = time.time()
     c = G.rng_uniform(SEED + 5, 2 * n).reshape(n, 2)
     base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
-    v = 0.5 + G.rff_field(c, base, 8192, SEED + 6)
+    v = 0.5 + W.rff_field(c, base, 8192, SEED + 6)
     ps = G.PointSet(c, v)
     t1 = time.time()
     plan = G.VecchiaPlan(ps, 30)
@@ -566,6 +574,51 @@ def vecchia_bench(args, log):
            "fp64_resolved_systems": resolved,
            "fp64_resolved_fraction": resolved / (n * len(cands)),
            "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
+    # the oracle at full size: candidate 0's log-likelihood on the same plan
+    # (sequential, as the reference sums), and the plan's predecessor sets at
+    # sampled positions against a brute-force search among the earlier points
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    po, pnb, pcnt = plan.arrays()
+    if args.vecchia_oracle:
+        t1 = time.perf_counter()
+        ref0 = O.vecchia_loglik_plan(c, v, cands[0], po, pnb, pcnt)
+        dto = time.perf_counter() - t1
+        out["oracle_full_size"] = {
+            "points": n, "candidate": 0, "oracle_loglik": float(ref0),
+            "mixed_rel_err": float(abs(ll[0] - ref0) / abs(ref0)),
+            "fp64_build_rel_err": float(abs(ll64[0] - ref0) / abs(ref0)),
+            "oracle_seconds": dto, "cpu_points_per_s": n / dto, "cpu_cores": 1}
+        log(f"[bench] vecchia oracle at {n} points: {dto:.1f}s, mixed rel err "
+            f"{out['oracle_full_size']['mixed_rel_err']:.2e}")
+    prng = np.random.default_rng(SEED + 8)
+    pos = np.sort(prng.choice(np.arange(1, n), 200, replace=False))
+    oc = c[po]
+    bad = 0
+    for k in pos:
+        d = oc[:k] - oc[k]
+        d2 = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]
+        keep = np.lexsort((np.arange(k), d2))[:min(30, k)]
+        bad += int(not np.array_equal(po[keep], pnb[k, :pcnt[k]]))
+    out["plan_spot_check"] = {"positions": len(pos), "mismatches": bad,
+                              "rule": "30 nearest earlier points by (squared distance, position)"}
+    # a Nelder-Mead fit with 16 starts, every round's simplex points of all
+    # starts in one batched launch (bounded iterations)
+    if args.mle_iters > 0:
+        from geostat_rs import _abi as _ab
+        t1 = time.perf_counter()
+        fm, fll, fx, fne = G.vecchia_mle_nm_fit(ps, "matern25", 30, nstarts=16,
+                                                max_iter=args.mle_iters, order=po)
+        dtf = time.perf_counter() - t1
+        out["mle_fit"] = {"starts": 16, "max_iter": args.mle_iters,
+                          "rounds": int(_ab.load().gs_last_fit_rounds()), "evaluations": int(fne),
+                          "seconds": dtf, "point_evaluations_per_s": fne * n / dtf,
+                          "loglik": float(fll),
+                          "model": {"nugget": fm.nugget, "psill": fm.structures[0].sill,
+                                    "range": fm.structures[0].range},
+                          "includes": "device plan from the given order, batched objective "
+                                      "launches, host simplex updates"}
+        log(f"[bench] vecchia 16-start NM fit: {fne} evaluations in {dtf:.1f}s")
     # Guinness-grouped likelihood (group size 8) and REML (linear trend), four
     # candidates each, on the same plan; oracle check on a 20,000-point plan
     g4 = cands[:4]
@@ -580,8 +633,6 @@ def vecchia_bench(args, log):
     t1 = time.perf_counter()
     llr8, _ = plan.reml_loglik(g4, drift_degree=1, group_size=8)
     dtr8 = time.perf_counter() - t1
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as O
     small = G.VecchiaPlan(G.PointSet(c[:20000], v[:20000]), 30)
     so, snb, scnt = small.arrays()
     sg, _ = small.loglik_grouped(g4[:1], 8)
@@ -645,9 +696,9 @@ def clustered_setup(n=CL_N, grid=CL_GRID, extent=CL_EXTENT, nblobs=500):
     search (4 x 16, at most 64, at least 4)."""
     import geostat_rs as G
     from geostat_rs.model import Structure, VariogramModel
-    c = G.clustered_points(n, extent, nblobs, 15.0, 0.7, SEED + 21)
+    c = W.clustered_points(n, extent, nblobs, 15.0, 0.7, SEED + 21)
     m = VariogramModel(0.0, [Structure.with_anisotropy("matern15", 1.0, 500.0, 45.0, 0.5)])
-    v = G.rff_field(c, m, 4096, SEED + 22)
+    v = W.rff_field(c, m, 4096, SEED + 22)
     cov = G.rng_uniform(SEED + 23, n)
     g = (np.arange(grid) + 0.5) * (extent / grid)
     yy, xx = np.meshgrid(g, g, indexing="ij")
@@ -802,7 +853,8 @@ def serving_bench(args, log):
     1M points.  Poisson arrivals at 200 requests/s: 85 % predictions
     (log-uniform target counts in [1, 1e6], random data set and n_max), 15 %
     Vecchia log-likelihoods at a new parameter vector.  The first requests of
-    the same stream are then served by the plain FP64 build and compared."""
+    the same stream are then served again at the same arrival times by the
+    mixed path and by the plain FP64 build, and compared."""
     import geostat_rs as G
     from geostat_rs.model import Structure, VariogramModel
     rng = np.random.default_rng(SEED + 11)
@@ -818,7 +870,7 @@ def serving_bench(args, log):
         box = np.array([1000.0, 1000.0]) if dim == 2 else np.asarray(BOX)
         mdl = m2 if dim == 2 else m3
         cc = G.rng_uniform(SEED + 100 + q, dim * n).reshape(n, dim) * box
-        vv = G.rff_field(cc, mdl, 1024, SEED + 200 + q)
+        vv = W.rff_field(cc, mdl, 1024, SEED + 200 + q)
         ps = G.PointSet(cc, vv)
         row = []
         warm = G.rng_uniform(SEED + 300 + q, dim * 131072).reshape(-1, dim) * box
@@ -872,10 +924,12 @@ def serving_bench(args, log):
 
     reqs, lat, wall, targets = serve(range(nreq), True)
     _, _, done, launches = srv.stats()
-    # the plain FP64 build on the first requests of the stream, compared
+    # the first requests of the stream again, paced at the same arrival
+    # times, through the mixed path and through the plain FP64 build
     nsub = min(nreq, args.serve_fp64_requests)
+    reqsm, latm, wallm, targetsm = serve(range(nsub), True)
     srv.set_precision("fp64")
-    reqs64, lat64, wall64, targets64 = serve(range(nsub), False)
+    reqs64, lat64, wall64, targets64 = serve(range(nsub), True)
     srv.set_precision("mixed")
     worst_v = worst_var = worst_ll = 0.0
     status_ok = True
@@ -901,7 +955,15 @@ def serving_bench(args, log):
             "mean_ms": float(lat.mean()), "wall_s": wall, "targets": targets,
             "targets_per_s": targets / wall, "requests_per_s": nreq / wall,
             "launches": launches - launches0,
-            "fp64_gpu_build": {"requests": nsub, "unpaced": True, "targets": targets64,
+            "same_stream_subset": {"requests": nsub, "paced": True, "targets": targetsm,
+                                   "mixed_targets_per_s": targetsm / wallm,
+                                   "mixed_p50_ms": float(np.percentile(latm, 50)),
+                                   "mixed_p99_ms": float(np.percentile(latm, 99)),
+                                   "fp64_targets_per_s": targets64 / wall64,
+                                   "fp64_p50_ms": float(np.percentile(lat64, 50)),
+                                   "fp64_p99_ms": float(np.percentile(lat64, 99)),
+                                   "mixed_over_fp64_wall": wall64 / wallm},
+            "fp64_gpu_build": {"requests": nsub, "paced": True, "targets": targets64,
                                "targets_per_s": targets64 / wall64,
                                "p50_ms": float(np.percentile(lat64, 50)),
                                "p99_ms": float(np.percentile(lat64, 99)),
@@ -928,12 +990,9 @@ def run_reference(args, rank, world):
     model = VariogramModel(0.05, [Structure.with_rotation("spherical", 0.6, 300.0, 30.0, 10.0, 0.0,
                                                           0.5, 40.0 / 300.0),
                                   Structure("exponential", 0.35, 800.0)])
-    # field values from a CPU random-Fourier-feature sum (the oracle's cost does
-    # not depend on the values)
-    rs = np.random.RandomState(SEED)
-    w = rs.standard_normal((3, 512)) / 300.0
-    ph = rs.uniform(0, 2 * np.pi, 512)
-    vals = np.cos(u @ w + ph).sum(axis=1) * np.sqrt(2.0 / 512)
+    # the same random-Fourier-feature field values as the GPU arm's workload,
+    # generated before any timing (input preparation, not the timed path)
+    vals = W.rff_field(u, model, 4096, SEED + 1)
     tg = grid_targets()
     rng = np.random.RandomState(11)
     probe = rng.choice(len(tg), 1000, replace=False)
@@ -956,8 +1015,7 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": mean * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_data": N_DATA, "n_targets": len(tg),
-                       "max_neighbors": K_NEIGH, "dim": 3},
+            "config": workload_config(len(tg), world),
             "cpu_baseline": {"value": value, "unit": "kriged targets/s", "cores": cores,
                              "kind": "port",
                              "sample": f"{ns} random grid targets per step (same data size, model, "
@@ -974,7 +1032,7 @@ def profile_case(args):
     if args.profile_case:
         coords = make_coords()
         model = make_model()
-        values = G.rff_field(coords, model, 4096, SEED + 1)
+        values = W.rff_field(coords, model, 4096, SEED + 1)
         kr = G.Kriging.new(G.PointSet(coords, values), model, G.KrigingConfig(max_neighbors=K_NEIGH))
         tg = grid_targets()[:args.profile_case]
         for _ in range(2):
@@ -994,7 +1052,7 @@ def profile_case(args):
         n = args.profile_vecchia
         c = G.rng_uniform(SEED + 5, 2 * n).reshape(n, 2)
         base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
-        v = 0.5 + G.rff_field(c, base, 1024, SEED + 6)
+        v = 0.5 + W.rff_field(c, base, 1024, SEED + 6)
         plan = G.VecchiaPlan(G.PointSet(c, v), 30)
         cands = [VariogramModel(0.02 * (1 + 0.05 * i), [Structure("matern25", 1.0, 0.05)])
                  for i in range(16)]
@@ -1006,7 +1064,7 @@ def profile_case(args):
         n = args.profile_reml
         c = G.rng_uniform(SEED + 5, 2 * n).reshape(n, 2)
         base = VariogramModel(0.02, [Structure("matern25", 1.0, 0.05)])
-        v = 0.5 + G.rff_field(c, base, 1024, SEED + 6)
+        v = 0.5 + W.rff_field(c, base, 1024, SEED + 6)
         # m = 40: beyond the mixed warp kernel, every point on the FP64 block kernel
         plan = G.VecchiaPlan(G.PointSet(c, v), 40)
         cands = [VariogramModel(0.02 * (1 + 0.05 * i), [Structure("matern25", 1.0, 0.05)])
@@ -1035,10 +1093,15 @@ def main():
                     help="oracle points of the leave-one-out leg (0: skip the leg)")
     ap.add_argument("--cl-sample", type=int, default=200,
                     help="oracle targets per band of the clustered workload")
+    ap.add_argument("--vecchia-oracle", type=int, default=1,
+                    help="time the oracle's full-size Vecchia log-likelihood (0: skip)")
+    ap.add_argument("--mle-iters", type=int, default=12,
+                    help="Nelder-Mead iterations per start of the 16-start fit (0: skip)")
     ap.add_argument("--vpred-n", type=int, default=500_000,
                     help="targets of the Vecchia joint-prediction timing (0: skip)")
-    ap.add_argument("--serve-fp64-requests", type=int, default=60,
-                    help="leading requests of the serving stream re-served by the FP64 build")
+    ap.add_argument("--serve-fp64-requests", type=int, default=150,
+                    help="leading requests of the serving stream re-served, paced, by the mixed "
+                         "path and by the FP64 build")
     ap.add_argument("--serve-requests", type=int, default=1000,
                     help="requests of the serving-loop run (0: skip)")
     ap.add_argument("--profile-case", type=int, default=0,

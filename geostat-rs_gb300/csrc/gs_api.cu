@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -54,10 +55,45 @@ int allow_dynamic_smem(const void* func, size_t bytes) {
   return GS_OK;
 }
 
+static std::atomic<int64_t> g_launches{0};
+static std::atomic<int64_t> g_device_allocs{0};
+// Stream-ordered allocations still to be refused (a host-side fake of an
+// exhausted device, for failure tests; 0 in normal use).
+static std::atomic<int64_t> g_refuse_allocs{0};
+
+void count_launch(int n) { g_launches += n; }
+
+int sm_count() {
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> cache[kMaxDev];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 1;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+    return 1;  // grid-stride loops stay correct on any grid
+  cache[dev].store(v, std::memory_order_relaxed);
+  return v;
+}
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  ++g_device_allocs;
+  return cudaMalloc(p, bytes);
+}
+
 int DevBuf::alloc(size_t b, cudaStream_t s) {
   release();
   stream = s;
   bytes = b;
+  ++g_device_allocs;
+  int64_t left = g_refuse_allocs.load();
+  while (left > 0 && !g_refuse_allocs.compare_exchange_weak(left, left - 1)) {
+  }
+  if (left > 0) {
+    bytes = 0;
+    return cuda_fail(cudaErrorMemoryAllocation, "cudaMallocAsync (refused on request)", __FILE__,
+                     __LINE__);
+  }
   GS_CUDA(cudaMallocAsync(&ptr, std::max<size_t>(b, 16), s));
   return GS_OK;
 }
@@ -113,6 +149,14 @@ extern "C" {
 
 const char* gs_last_error(void) { return gs::last_error(); }
 int gs_abi_version(void) { return GS_ABI_VERSION; }
+
+int64_t gs_launch_count(void) { return g_launches.load(); }
+int64_t gs_debug_device_allocations(void) { return g_device_allocs.load(); }
+int gs_debug_refuse_allocations(int64_t count) {
+  if (count < 0) return fail(GS_ERR_INVALID_PARAMETER, "negative count");
+  g_refuse_allocs.store(count);
+  return GS_OK;
+}
 
 int gs_last_timings(double* ms4) {
   for (int i = 0; i < 4; ++i) ms4[i] = g_timings[i];
@@ -174,7 +218,7 @@ int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, con
     }
   }
   auto up = [&](double** d, const double* h) -> int {
-    GS_CUDA(cudaMalloc(d, n * sizeof(double)));
+    GS_CUDA(dev_malloc((void**)d, n * sizeof(double)));
     GS_CUDA(cudaMemcpy(*d, h, n * sizeof(double), cudaMemcpyHostToDevice));
     return GS_OK;
   };
@@ -183,11 +227,11 @@ int gs_pointset_create(int dim, int64_t n, const double* x, const double* y, con
   if (!rc && dim == 3) rc = up(&ps->d_z, z);
   if (!rc) rc = up(&ps->d_v, values);
   if (!rc) {
-    if (cudaMalloc(&ps->d_cdf, (size_t)dim * n * sizeof(df)) != cudaSuccess ||
-        cudaMalloc(&ps->d_vdf, (size_t)n * sizeof(df)) != cudaSuccess) {
+    if (dev_malloc((void**)&ps->d_cdf, (size_t)dim * n * sizeof(df)) != cudaSuccess ||
+        dev_malloc((void**)&ps->d_vdf, (size_t)n * sizeof(df)) != cudaSuccess) {
       rc = fail(GS_ERR_OUT_OF_MEMORY, "point set allocation failed");
     } else {
-      split_df_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256>>>(
+      split_df_kernel<<<(int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 32), 256>>>(
           dim, n, ps->d_x, ps->d_y, ps->d_z, ps->d_v, (df*)ps->d_cdf, (df*)ps->d_vdf);
       if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
         rc = fail(GS_ERR_CUDA, "point set split failed");
@@ -239,9 +283,6 @@ bool valid_in_dim(const gs_model& m, int dim) {
 
 // Kriging::build and the three constructors (kriging.rs:166-408).
 }  // namespace
-namespace gs {
-KrigeArgs base_args(const gs_kriging* k);
-}  // namespace gs
 namespace {
 
 // Global neighbourhoods larger than the mixed solver's systems are factored
@@ -250,6 +291,7 @@ constexpr int kGlobalLuMax = 16384;
 
 int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* cfg, int ctor,
                    const double* drift, const double* errors, gs_kriging** out) {
+  NvtxRange nvtx_range("gs.kriging_build");
   *out = nullptr;
   if (!ps || !model || !cfg) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
   GS_TRY(validate_model(*model));
@@ -313,6 +355,7 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
   }
   // GPU-path limits (kinds, drift terms)
   auto* k = new gs_kriging();
+  if (cudaGetDevice(&k->device) != cudaSuccess) k->device = 0;
   int rc = make_dev_model(*model, dim, &k->dm, true);
   if (rc) {
     delete k;
@@ -358,12 +401,12 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
   }
   rc = cudaStreamCreateWithFlags(&k->stream, cudaStreamNonBlocking) == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "stream creation failed");
   if (!rc && ctor == 1) {
-    if (cudaMalloc(&k->d_drift, n * k->nv * sizeof(double)) != cudaSuccess ||
+    if (dev_malloc((void**)&k->d_drift, n * k->nv * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(k->d_drift, drift, n * k->nv * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
       rc = fail(GS_ERR_CUDA, "drift upload failed");
   }
   if (!rc && ctor == 2) {
-    if (cudaMalloc(&k->d_err, n * sizeof(double)) != cudaSuccess ||
+    if (dev_malloc((void**)&k->d_err, n * sizeof(double)) != cudaSuccess ||
         cudaMemcpy(k->d_err, errors, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
       rc = fail(GS_ERR_CUDA, "measurement-error upload failed");
   }
@@ -393,7 +436,7 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
         basis[(size_t)q * n + i] = df_from_double(f);
       }
     }
-    if (cudaMalloc(&k->d_basis_df, basis.size() * sizeof(df)) != cudaSuccess ||
+    if (dev_malloc((void**)&k->d_basis_df, basis.size() * sizeof(df)) != cudaSuccess ||
         cudaMemcpy(k->d_basis_df, basis.data(), basis.size() * sizeof(df),
                    cudaMemcpyHostToDevice) != cudaSuccess)
       rc = fail(GS_ERR_OUT_OF_MEMORY, "drift basis upload failed");
@@ -401,7 +444,7 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
   if (!rc && ctor == 2) {
     std::vector<df> e(n);
     for (int64_t i = 0; i < n; ++i) e[i] = df_from_double(errors[i]);
-    if (cudaMalloc(&k->d_err_df, n * sizeof(df)) != cudaSuccess ||
+    if (dev_malloc((void**)&k->d_err_df, n * sizeof(df)) != cudaSuccess ||
         cudaMemcpy(k->d_err_df, e.data(), n * sizeof(df), cudaMemcpyHostToDevice) != cudaSuccess)
       rc = fail(GS_ERR_OUT_OF_MEMORY, "measurement-error upload failed");
   }
@@ -430,8 +473,8 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
       rc = fail(GS_ERR_INVALID_PARAMETER,
                 "global neighbourhood of " + std::to_string(N) + " unknowns exceeds " +
                     std::to_string(kGlobalLuMax) + " on the CUDA path; set max_neighbors");
-    } else if (cudaMalloc(&k->d_lu, (size_t)N * N * 8) != cudaSuccess ||
-               cudaMalloc(&k->d_perm, (size_t)N * 4) != cudaSuccess) {
+    } else if (dev_malloc((void**)&k->d_lu, (size_t)N * N * 8) != cudaSuccess ||
+               dev_malloc((void**)&k->d_perm, (size_t)N * 4) != cudaSuccess) {
       rc = fail(GS_ERR_OUT_OF_MEMORY, "global system allocation failed");
     } else {
       DevBuf piv;
@@ -522,7 +565,7 @@ constexpr int64_t kTuneMinTargets = 65536;
 // Targets of the first chunk the candidates are timed on.
 constexpr int64_t kTuneSample = 131072;
 // Warps of the FP64 LDL^T re-solve (slot-covariance scratch, 16.6 KB each).
-constexpr int64_t kCholScratchWarps = 152 * 16;
+int64_t chol_scratch_warps() { return (int64_t)sm_count() * 16; }
 // Leading targets of each chunk whose FP32 failure rate routes the rest.
 constexpr int64_t kRouteSample = 16384;
 
@@ -537,12 +580,10 @@ Tiles default_tiles(int64_t nt, bool binnable) {
   Tiles t;
   t.bins = binnable ? 1 : 0;
   t.run = 64;
-  while (t.run > 8 && (nt + t.run - 1) / t.run < 152 * 4) t.run >>= 1;
+  while (t.run > 8 && (nt + t.run - 1) / t.run < (int64_t)sm_count() * 4) t.run >>= 1;
   return t;
 }
 
-// The predictor's part of the kernel arguments (targets, lists and outputs
-// are filled in by the caller).
 KrigeArgs base_args(const gs_kriging* k) {
   const gs_pointset* ps = k->ps;
   const gs_kcfg& c = k->cfg;
@@ -590,6 +631,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
                  const double* tz, const double* tdrift, double* value, double* variance,
                  double* lagrange, uint8_t* status, int precision, cudaStream_t stream, bool timed,
                  const int32_t* excl_labels = nullptr, const BlockSpec* blk = nullptr) {
+  NvtxRange nvtx_range("gs.predict_pass");
   if (nt == 0) return GS_OK;
   const gs_pointset* ps = k->ps;
   const gs_kcfg& c = k->cfg;
@@ -645,7 +687,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   if (global_lu) {
     const int N = k->lu_n;
     const int64_t warps = std::max<int64_t>(
-        1, std::min<int64_t>(152 * 32, ((int64_t)512 << 20) / (16 * (int64_t)N)));
+        1, std::min<int64_t>((int64_t)sm_count() * 32, ((int64_t)512 << 20) / (16 * (int64_t)N)));
     DevBuf scratch;
     GS_TRY(scratch.alloc((size_t)warps * 2 * N * 8, stream));
     KrigeArgs g = a;
@@ -727,7 +769,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   DevBuf scratch, cscratch;
   GS_TRY(scratch.alloc((size_t)fp64_scratch_doubles(nmax_all, fthreads) * 8, stream));
   // slot scratch for at most one warp per target of a chunk
-  const int64_t cwarps = std::min<int64_t>(kCholScratchWarps, (chunk + 3) / 4 * 4);
+  const int64_t cwarps = std::min<int64_t>(chol_scratch_warps(), (chunk + 3) / 4 * 4);
   if (mixed) GS_TRY(cscratch.alloc((size_t)chol_scratch_doubles(cwarps) * 8, stream));
 
   cudaEvent_t ev[6] = {};
@@ -754,11 +796,11 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       if (excl_labels) spc.target_label = excl_labels + c0;  // targets are the data points
       rc = search_launch(k->grid, k->frame, spc, cn, ctx, cty, ctz, dnb, dnbc, stream);
     } else if (excl_labels) {
-      excl_rows_kernel<<<(int)std::min<int64_t>((cn + 127) / 128, 152 * 64), 128, 0, stream>>>(
+      excl_rows_kernel<<<(int)std::min<int64_t>((cn + 127) / 128, (int64_t)sm_count() * 64), 128, 0, stream>>>(
           cn, c0, (int)n, excl_labels, kout, dnb, dnbc);
       rc = cudaGetLastError() == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "launch failed");
     } else {
-      iota_rows_kernel<<<(int)std::min<int64_t>((cn * kout + 255) / 256, 152 * 64), 256, 0, stream>>>(
+      iota_rows_kernel<<<(int)std::min<int64_t>((cn * kout + 255) / 256, (int64_t)sm_count() * 64), 256, 0, stream>>>(
           cn, kout, dnb, dnbc);
       rc = cudaGetLastError() == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "launch failed");
     }
@@ -1008,6 +1050,7 @@ extern "C" {
 
 int gs_kriging_cross_validate(const gs_kriging* k, int64_t nfolds, uint64_t seed, double* predicted,
                               double* variance, uint8_t* status, int precision) {
+  NvtxRange nvtx_range("gs.cross_validate");
   if (!k || !predicted || !variance) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
   const gs_pointset* ps = k->ps;
   const int64_t n = ps->n;

@@ -15,6 +15,7 @@
 
 #include "gs_common.cuh"
 #include "gs_host.h"
+#include "gs_internal.h"
 
 namespace gs {
 
@@ -418,6 +419,7 @@ inline double dist2(const double* a, const double* b, int dim) {
 }  // namespace
 
 void maxmin_order(const std::vector<double>& pts, int dim, int64_t n, int64_t* order) {
+  NvtxRange nvtx_range("gs.maxmin_order");
   if (n == 0) return;
   double c[3] = {0, 0, 0};
   for (int64_t i = 0; i < n; ++i)

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -16,6 +17,14 @@ int fail(int code, const std::string& msg);
 // Counts kernels this library launched (reported by gs_launch_count).
 void count_launch(int n);
 
+// Streaming multiprocessors of the current device, queried once per device
+// (grid caps and scratch sizes scale with it).
+int sm_count();
+
+// cudaMalloc that the library's device-allocation counter sees
+// (gs_debug_device_allocations); DevBuf::alloc counts its allocations too.
+cudaError_t dev_malloc(void** p, size_t bytes);
+
 // Initialises the device (and keeps the stream-ordered memory pool from
 // returning memory to the driver between calls).
 int ensure_device();
@@ -29,6 +38,15 @@ void set_last_timings(const double* ms4, int64_t fallbacks);
 // only ever raised (under a lock): a thread launching with a smaller size
 // can never invalidate another thread's larger launch.
 int allow_dynamic_smem(const void* func, size_t bytes);
+
+// NVTX range over a scope of host code (visible in Nsight timelines; costs a
+// few nanoseconds when no tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Stream-ordered device allocation released at scope exit.
 struct DevBuf {

@@ -1315,9 +1315,7 @@ static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   const size_t smem = lay.total;
   auto kern = krige_rows_kernel<D, R, PC>;
   GS_TRY(allow_dynamic_smem((const void*)kern, smem));
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = sm_count();
   int per_sm = 0;
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R, smem));
   per_sm = std::max(per_sm, 1);
@@ -1356,9 +1354,7 @@ static int launch_chol(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   const CholLayout lay = chol_layout(Mmax, D);
   auto kern = krige_chol_kernel<D>;
   GS_TRY(allow_dynamic_smem((const void*)kern, lay.total));
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = sm_count();
   int per_sm = 0;
   GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCholWarps * 32, lay.total));
   per_sm = std::max(per_sm, 1);
@@ -1392,13 +1388,14 @@ int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, doub
 
 int global_factor(const KrigeArgs& a, const DevModel& m, int N, double* A, int32_t* piv,
                   int* state_out, cudaStream_t stream) {
+  NvtxRange nvtx_range("gs.global_factor");
   DevBuf st, sc;
   GS_TRY(st.alloc(sizeof(int), stream));
   GS_TRY(sc.alloc(sizeof(unsigned long long), stream));
   GS_CUDA(cudaMemsetAsync(st.ptr, 0, sizeof(int), stream));
   GS_CUDA(cudaMemsetAsync(sc.ptr, 0, sizeof(unsigned long long), stream));
   const int64_t total = (int64_t)N * N;
-  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 16);
   if (a.dim == 2) global_lhs_kernel<2><<<blocks, 256, 0, stream>>>(a, m, N, A);
   else global_lhs_kernel<3><<<blocks, 256, 0, stream>>>(a, m, N, A);
   absmax_kernel<<<blocks, 256, 0, stream>>>(A, total, (unsigned long long*)sc.ptr);
@@ -1445,7 +1442,7 @@ int64_t fp64_scratch_doubles(int nmax, int64_t threads) {
 int64_t fp64_threads_for(int nmax, int64_t budget_bytes) {
   const int64_t per = ((int64_t)nmax * nmax + 2 * (int64_t)nmax) * 8;
   int64_t t = budget_bytes / std::max<int64_t>(per, 1);
-  t = std::min<int64_t>(t, 152 * 1024);
+  t = std::min<int64_t>(t, (int64_t)sm_count() * 1024);
   t = (t / 128) * 128;
   return std::max<int64_t>(t, 128);
 }
@@ -1498,7 +1495,7 @@ int grid_centers_launch(int dim, const double* bmin, const double* step, const i
   int64_t total = ncell[0] * ncell[1] * (dim == 3 ? ncell[2] : 1);
   if (total == 0) return GS_OK;
   const int tpb = 256;
-  const int blocks = (int)std::min<int64_t>((total + tpb - 1) / tpb, 152 * 64);
+  const int blocks = (int)std::min<int64_t>((total + tpb - 1) / tpb, (int64_t)sm_count() * 64);
   if (dim == 2)
     grid_centers_kernel<2><<<blocks, tpb, 0, stream>>>(bmin[0], bmin[1], 0.0, step[0], step[1], 0.0,
                                                        ncell[0], ncell[1], total, x, y, z);

@@ -71,7 +71,7 @@ int route_launch(const uint8_t* flag, int64_t n, int* route, cudaStream_t stream
 // warp); clears the flag of every system it solves.  Systems left flagged
 // (near-singular, or beyond 64 neighbours) go to krige_fp64_launch.
 // scratch: chol_scratch_doubles(scratch_warps) doubles (the grid is capped
-// at scratch_warps warps; 152 * 16 warps fill a GB300).
+// at scratch_warps warps; 16 warps per SM fill the device).
 int krige_chol_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, double* scratch,
                       int64_t scratch_warps, cudaStream_t stream);
 int64_t chol_scratch_doubles(int64_t warps);

@@ -40,6 +40,7 @@ struct gs_kriging {
   gs::SearchFrame frame{};
   gs::Grid grid;
   cudaStream_t stream = nullptr;
+  int device = 0;  // the device the predictor's data and stream live on
   // autotuned launch shapes per size class of a call (floor(log2(nt))),
   // and a shape pinned by the caller (run 0: none)
   mutable std::mutex tiles_mu;
@@ -63,6 +64,10 @@ struct gs_kriging {
 };
 
 namespace gs {
+// The predictor's part of the kernel arguments (targets, neighbour lists and
+// outputs are filled in by the caller).
+KrigeArgs base_args(const gs_kriging* k);
+
 // Search + solves for nt targets whose coordinates are already on the device
 // (outputs in device memory); synchronises `stream` before returning.
 int predict_device(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,

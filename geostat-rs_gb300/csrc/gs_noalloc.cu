@@ -16,7 +16,9 @@
 // to the kernels as an ordinary pointer.  A call therefore allocates nothing;
 // the first call on a device does that set-up (which also makes the driver
 // load this file's device code) and should come before any section in which
-// the caller cannot afford set-up work.
+// the caller cannot afford set-up work.  A call runs on the device the
+// predictor was built on: it makes that device current for its duration and
+// restores the caller's current device afterwards.
 //
 // Limits: at most GS_NOALLOC_MAX_TARGETS targets per call; the FP64 scratch
 // gets what the neighbour lists leave of GS_NOALLOC_SCRATCH_BYTES, so larger
@@ -49,10 +51,9 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kMaxDevices] = {};
 
-// Address of this device's copy of g_noalloc_scratch (set up on first use).
-int noalloc_scratch(void** out) {
-  int dev = 0;
-  GS_CUDA(cudaGetDevice(&dev));
+// Address of device dev's copy of g_noalloc_scratch (set up on first use;
+// dev must be the current device).
+int noalloc_scratch(int dev, void** out) {
   if (dev < 0 || dev >= kMaxDevices)
     return fail(GS_ERR_INVALID_PARAMETER, "device ordinal beyond the allocation-free path's table");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
@@ -67,6 +68,21 @@ int noalloc_scratch(void** out) {
   *out = g_noalloc_ptr[dev];
   return GS_OK;
 }
+
+// Makes `dev` the calling thread's current device for one call and puts the
+// previous one back afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  int enter(int dev) {
+    GS_CUDA(cudaGetDevice(&prev));
+    if (prev != dev) GS_CUDA(cudaSetDevice(dev));
+    return GS_OK;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
 
 // Global neighbourhood: every data point is a neighbour of every target.
 __global__ void noalloc_all_rows(int64_t nt, int n, int32_t* nb, int32_t* nbc) {
@@ -136,13 +152,16 @@ extern "C" int gs_kriging_predict_fp64_noalloc(const gs_kriging* k, int64_t nt, 
   if (k->cfg.method != GS_EXTERNAL_DRIFT && tdrift)
     return fail(GS_ERR_INVALID_PARAMETER, "predict_with_drift requires KrigingMethod::ExternalDrift");
   cudaStream_t s = stream ? (cudaStream_t)stream : k->stream;
+  // the predictor's device: its data, its stream and its copy of the array
+  DeviceGuard guard;
+  GS_TRY(guard.enter(k->device));
   const gs_pointset* ps = k->ps;
   const int dim = ps->dim;
   SearchParams sp;
   int kout = 0;
   GS_TRY(noalloc_geometry(k, &sp, &kout));
   void* base = nullptr;
-  GS_TRY(noalloc_scratch(&base));
+  GS_TRY(noalloc_scratch(k->device, &base));
   if (nt == 0) return GS_OK;
   // carve the array: neighbour lists, counts, then the FP64 slabs
   const int nmax = kout + k->p;
@@ -164,38 +183,16 @@ extern "C" int gs_kriging_predict_fp64_noalloc(const gs_kriging* k, int64_t nt, 
   if (k->use_tree) {
     GS_TRY(search_launch(k->grid, k->frame, sp, nt, tx, ty, dim == 3 ? tz : nullptr, dnb, dnbc, s));
   } else {
-    noalloc_all_rows<<<(int)std::min<int64_t>((nt * kout + 255) / 256, 152 * 64), 256, 0, s>>>(
+    const int64_t cap = (int64_t)sm_count() * 64;
+    noalloc_all_rows<<<(int)std::min<int64_t>((nt * kout + 255) / 256, cap), 256, 0, s>>>(
         nt, kout, dnb, dnbc);
     GS_CUDA(cudaGetLastError());
     count_launch(1);
   }
-  KrigeArgs a{};
-  a.dim = dim;
-  a.method = (int)k->cfg.method;
-  a.p = k->p;
-  a.nv = k->nv;
-  a.uk_degree = (int)k->cfg.uk_degree;
-  a.min_nb = k->cfg.min_neighbors >= 0 ? (int)k->cfg.min_neighbors : 1;
+  // the predictor's arguments as the generic path builds them, then this call's
+  KrigeArgs a = base_args(k);
   a.kout = kout;
   a.nmax = nmax;
-  a.sk_mean = k->cfg.sk_mean;
-  for (int d = 0; d < 3; ++d) a.center[d] = k->center[d];
-  a.scale = k->scale;
-  for (int v = 0; v < GS_MAX_KED_VARS; ++v) {
-    a.dmean[v] = k->dmean[v];
-    a.dscale[v] = k->dscale[v];
-  }
-  a.x = ps->d_x;
-  a.y = ps->d_y;
-  a.z = ps->d_z;
-  a.val = ps->d_v;
-  a.meas_err = k->d_err;
-  a.drift = k->d_drift;
-  a.cdf = (const df*)ps->d_cdf;
-  a.vdf = (const df*)ps->d_vdf;
-  a.basis_df = k->d_basis_df;
-  a.err_df = k->d_err_df;
-  a.n = ps->n;
   a.tx = tx;
   a.ty = ty;
   a.tz = dim == 3 ? tz : nullptr;

@@ -576,7 +576,7 @@ inline unsigned ceil_pow2(unsigned v) {
 
 template <class T>
 int dalloc(T** p, size_t count) {
-  GS_CUDA(cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
+  GS_CUDA(dev_malloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
   return GS_OK;
 }
 
@@ -593,6 +593,7 @@ Grid::~Grid() {
 
 int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, const double* z,
                const SearchFrame& frame, double points_per_cell, cudaStream_t stream) {
+  NvtxRange nvtx_range("gs.grid_build");
   if (n <= 0 || n > 0xfffffff0ll) return fail(GS_ERR_INVALID_PARAMETER, "point count out of range");
   g->dim = dim;
   g->n = n;
@@ -601,7 +602,7 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
   GS_TRY(dalloc(&ty, n));
   if (dim == 3) GS_TRY(dalloc(&tz, n));
   const int threads = 256;
-  const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, 152 * 32);
+  const int blocks = (int)std::min<int64_t>((n + threads - 1) / threads, (int64_t)sm_count() * 32);
   if (dim == 2) transform_kernel<2><<<blocks, threads, 0, stream>>>(frame, n, x, y, z, tx, ty, tz);
   else transform_kernel<3><<<blocks, threads, 0, stream>>>(frame, n, x, y, z, tx, ty, tz);
   GS_CUDA(cudaGetLastError());
@@ -615,7 +616,7 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
   size_t need = tmp_bytes;
   GS_CUDA(cub::DeviceReduce::Max(nullptr, tmp_bytes, tx, d_red, (int)n, stream));
   need = std::max(need, tmp_bytes);
-  GS_CUDA(cudaMalloc(&tmp, need));
+  GS_CUDA(dev_malloc((void**)&tmp, need));
   const double* axes[3] = {tx, ty, tz};
   for (int d = 0; d < dim; ++d) {
     tmp_bytes = need;
@@ -684,7 +685,7 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
   tmp_bytes = 0;
   GS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0,
                                           bits, stream));
-  GS_CUDA(cudaMalloc(&tmp, std::max<size_t>(tmp_bytes, 1)));
+  GS_CUDA(dev_malloc((void**)&tmp, std::max<size_t>(tmp_bytes, 1)));
   GS_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, vals, vals2, (int)n, 0,
                                           bits, stream));
   GS_TRY(dalloc(&g->d_sx, n));
@@ -712,7 +713,7 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
                                                      g->d_sz, g->d_sidx, G, g->d_f);
   GS_CUDA(cudaGetLastError());
   {
-    int cb = (int)std::min<int64_t>((total + 1 + threads - 1) / threads, 152 * 32);
+    int cb = (int)std::min<int64_t>((total + 1 + threads - 1) / threads, (int64_t)sm_count() * 32);
     cell_start_kernel<<<cb, threads, 0, stream>>>(total, n, keys2, g->d_cstart);
     GS_CUDA(cudaGetLastError());
   }
@@ -738,6 +739,7 @@ int grid_build(Grid* g, int dim, int64_t n, const double* x, const double* y, co
 
 int grid_build_ranked(Grid* g, int dim, int64_t n, const double* x, const double* y,
                       const double* z, double points_per_cell, cudaStream_t stream) {
+  NvtxRange nvtx_range("gs.grid_build_ranked");
   SearchFrame f;
   std::memset(&f, 0, sizeof(f));
   return grid_build(g, dim, n, x, y, z, f, points_per_cell, stream);
@@ -746,6 +748,7 @@ int grid_build_ranked(Grid* g, int dim, int64_t n, const double* x, const double
 int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p0, int64_t nt,
                   const double* tx, const double* ty, const double* tz, int32_t* nb,
                   int32_t* nbc, cudaStream_t stream) {
+  NvtxRange nvtx_range("gs.search");
   if (nt == 0) return GS_OK;
   SearchParams p = p0;
   p.capb = (int)ceil_pow2((unsigned)std::max(p.k + 32, 64));
@@ -756,7 +759,7 @@ int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p
   static const size_t kMaxSmem = 227 * 1024;
   if (smem > kMaxSmem) return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood too large for the device search");
   int64_t blocks64 = (nt + wpb - 1) / wpb;
-  int blocks = (int)std::min<int64_t>(blocks64, 152 * 64);
+  int blocks = (int)std::min<int64_t>(blocks64, (int64_t)sm_count() * 64);
   auto launch = [&](auto kern) -> int {
     GS_TRY(allow_dynamic_smem((const void*)kern, smem));
     kern<<<blocks, wpb * 32, smem, stream>>>(g.dev, frame, p, nt, tx, ty, tz, nb, nbc);

@@ -3,13 +3,26 @@
 // Data sets stay resident in device memory as built predictors (gs_kriging:
 // points, bucket grid, model) and Vecchia plans.  Callers submit prediction
 // and log-likelihood requests from any thread; executor threads, each with
-// its own CUDA stream, take the oldest pending request as soon as the
-// device-memory budget admits it, coalesce every other pending request of the
-// same data set and kind into the same launch (targets concatenated,
-// likelihood candidates batched), run it, and scatter the results back.
-// Requests that arrive while others are on the device join the next batch an
-// executor forms, so the device keeps working on mixed requests of very
-// different sizes; batches of different executors overlap on their streams.
+// its own CUDA stream, take a pending request as soon as device memory admits
+// it, coalesce every other pending request of the same data set and kind into
+// the same launch (targets concatenated, likelihood candidates batched), run
+// it, and scatter the results back.  Requests that arrive while others are on
+// the device join the next batch an executor forms, so the device keeps
+// working on mixed requests of very different sizes; batches of different
+// executors overlap on their streams.
+//
+// Size-aware admission: predictions of at least kLargeTargets targets are
+// large.  Executor 0 is the large lane: it serves large requests in arrival
+// order, one batch at a time, and small ones when no large request waits.
+// The other executors serve small requests only, in arrival order, so a small
+// request never waits behind a large one.  (With one executor, it serves the
+// oldest request of either size.)
+//
+// Admission by free device memory: a batch starts once its device bytes fit
+// both the caller's budget and the device's current headroom (free memory
+// plus what the stream-ordered pool holds unused), less a reserve.  A request
+// that could never fit the budget is refused at submission; pending requests
+// can be cancelled.
 //
 // A prediction's result does not depend on which requests it was batched
 // with beyond the order of roundings (each target's system is solved on its
@@ -58,6 +71,7 @@ struct Request {
   int rc = GS_OK;
   std::string err;  // the failing call's message (worker thread)
   bool done = false;
+  bool large = false;
 };
 
 struct Dataset {
@@ -69,6 +83,11 @@ struct Dataset {
 // likelihood launch.
 constexpr int64_t kMaxBatchTargets = (int64_t)1 << 22;
 constexpr int64_t kMaxBatchCandidates = 64;
+// Predictions of at least this many targets go to the large lane.
+constexpr int64_t kLargeTargets = (int64_t)1 << 17;
+// Device memory kept free of admitted batches (other allocations of the
+// process, the driver's own needs).
+constexpr int64_t kHeadroomReserve = (int64_t)512 << 20;
 
 }  // namespace
 }  // namespace gs
@@ -76,7 +95,7 @@ constexpr int64_t kMaxBatchCandidates = 64;
 struct gs_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<gs::Request*> pending;
+  std::deque<gs::Request*> pending_small, pending_large;
   std::unordered_map<int64_t, std::unique_ptr<gs::Request>> requests;
   std::vector<gs::Dataset> datasets;
   int64_t budget = 0;
@@ -85,8 +104,11 @@ struct gs_server {
   int64_t batches = 0;
   std::atomic<int> precision{GS_PREC_MIXED};
   bool stop = false;
+  int device = 0;
+  int executors = 1;
   std::vector<std::thread> workers;
   std::vector<double> latencies_ms;
+  int64_t cancelled = 0;
 };
 
 namespace gs {
@@ -100,7 +122,7 @@ int64_t request_bytes(const gs_server* S, const Request& r) {
     const int64_t kout = k->cfg.max_neighbors > 0 ? k->cfg.max_neighbors : GS_MAX_SYSTEM;
     // + the FP64 re-solve's slot scratch (up to 40.5 MB)
     return r.nt * (3 * 8 + 8 + 8 + 8 + 1 + 4 * kout + 4 + 1 + 8) + (1 << 20) +
-           std::min<int64_t>(r.nt * 16640, (int64_t)152 * 16 * 16640);
+           std::min<int64_t>(r.nt * 16640, (int64_t)sm_count() * 16 * 16640);
   }
   return vecchia_plan_points(S->datasets[r.dataset].plan) * 9 + (1 << 20);
 }
@@ -156,38 +178,73 @@ int run_logliks(gs_server* S, const std::vector<Request*>& batch, cudaStream_t s
   return GS_OK;
 }
 
-void worker_loop(gs_server* S) {
+// Device memory a new batch may still take: the device's free memory plus
+// what the stream-ordered pool holds unused, less the reserve (read outside
+// the server lock).
+int64_t device_headroom() {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return INT64_MAX;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaMemPool_t pool;
+  uint64_t reserved = 0, used = 0;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+  }
+  const int64_t pooled = reserved > used ? (int64_t)(reserved - used) : 0;
+  return (int64_t)free_b + pooled - kHeadroomReserve;
+}
+
+// The queue executor `lane` serves next (null: nothing it may take).
+std::deque<Request*>* pick_queue(gs_server* S, int lane) {
+  if (S->executors == 1) {
+    if (S->pending_small.empty()) return S->pending_large.empty() ? nullptr : &S->pending_large;
+    if (S->pending_large.empty()) return &S->pending_small;
+    return S->pending_large.front()->id < S->pending_small.front()->id ? &S->pending_large
+                                                                       : &S->pending_small;
+  }
+  if (lane == 0 && !S->pending_large.empty()) return &S->pending_large;
+  return S->pending_small.empty() ? nullptr : &S->pending_small;
+}
+
+void worker_loop(gs_server* S, int lane) {
   cudaStream_t s = nullptr;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) s = nullptr;
+  int64_t headroom = device_headroom();
   for (;;) {
     std::vector<Request*> batch;
     int64_t bytes = 0;
     {
       std::unique_lock<std::mutex> lock(S->mu);
+      std::deque<Request*>* q = nullptr;
       S->cv_work.wait(lock, [&] {
         if (S->stop) return true;
-        if (S->pending.empty()) return false;
-        // admission by memory: the oldest request runs once it fits (alone
-        // when nothing else is in flight, whatever its size)
-        return S->in_use == 0 || S->in_use + S->pending.front()->bytes <= S->budget;
+        q = pick_queue(S, lane);
+        if (!q) return false;
+        // admission by memory: the batch's bytes within the budget and
+        // within the device's headroom at the last reading (a request alone
+        // on an idle server always fits: submission refused larger ones)
+        const int64_t need = q->front()->bytes;
+        return S->in_use == 0 || (S->in_use + need <= S->budget && need <= headroom);
       });
-      if (S->stop && S->pending.empty()) break;
-      if (S->pending.empty()) continue;
-      Request* head = S->pending.front();
-      S->pending.pop_front();
+      if (S->stop && S->pending_small.empty() && S->pending_large.empty()) break;
+      if (!q) continue;
+      Request* head = q->front();
+      q->pop_front();
       batch.push_back(head);
       bytes = head->bytes;
       int64_t units = head->kind == 0 ? head->nt : 1;
       const int64_t cap = head->kind == 0 ? kMaxBatchTargets : kMaxBatchCandidates;
-      for (auto it = S->pending.begin(); it != S->pending.end();) {
+      for (auto it = q->begin(); it != q->end();) {
         Request* r = *it;
         const int64_t u = r->kind == 0 ? r->nt : 1;
         if (r->dataset == head->dataset && r->kind == head->kind && units + u <= cap &&
-            S->in_use + bytes + r->bytes <= S->budget) {
+            S->in_use + bytes + r->bytes <= S->budget && bytes + r->bytes <= headroom) {
           batch.push_back(r);
           bytes += r->bytes;
           units += u;
-          it = S->pending.erase(it);
+          it = q->erase(it);
         } else {
           ++it;
         }
@@ -198,6 +255,7 @@ void worker_loop(gs_server* S) {
     int rc = s ? (batch[0]->kind == 0 ? run_predictions(S, batch, s) : run_logliks(S, batch, s))
                : fail(GS_ERR_CUDA, "stream creation failed");
     const std::string err = rc ? std::string(last_error()) : std::string();
+    headroom = device_headroom();
     {
       std::lock_guard<std::mutex> lock(S->mu);
       S->in_use -= bytes;
@@ -224,15 +282,20 @@ int submit(gs_server* S, std::unique_ptr<Request> r, int64_t* request_id) {
   if ((r->kind == 0 && !d.k) || (r->kind == 1 && !d.plan))
     return fail(GS_ERR_INVALID_PARAMETER, "the data set does not serve this kind of request");
   r->bytes = request_bytes(S, *r);
+  if (r->bytes > S->budget)
+    return fail(GS_ERR_OUT_OF_MEMORY,
+                "request needs " + std::to_string(r->bytes) + " bytes of device memory, more than "
+                "the server's budget of " + std::to_string(S->budget) + "; split it");
+  r->large = r->kind == 0 && r->nt >= kLargeTargets;
   r->submitted = Clock::now();
   {
     std::lock_guard<std::mutex> lock(S->mu);
     r->id = S->next_id++;
     *request_id = r->id;
-    S->pending.push_back(r.get());
+    (r->large ? S->pending_large : S->pending_small).push_back(r.get());
     S->requests[r->id] = std::move(r);
   }
-  S->cv_work.notify_one();
+  S->cv_work.notify_all();
   return GS_OK;
 }
 
@@ -251,12 +314,14 @@ int gs_server_create(int64_t mem_budget_bytes, int32_t executors, gs_server** ou
   GS_TRY(ensure_device());
   auto* S = new gs_server();
   S->budget = mem_budget_bytes;
+  S->executors = executors;
   int dev = 0;
   cudaGetDevice(&dev);
+  S->device = dev;
   for (int i = 0; i < executors; ++i)
-    S->workers.emplace_back([S, dev] {
+    S->workers.emplace_back([S, dev, i] {
       cudaSetDevice(dev);
-      worker_loop(S);
+      worker_loop(S, i);
     });
   *out = S;
   return GS_OK;
@@ -287,6 +352,7 @@ int gs_server_add_vecchia(gs_server* S, const gs_vecchia_plan* plan, int32_t* da
 int gs_server_submit_predict(gs_server* S, int32_t dataset, int64_t nt, const double* tx,
                              const double* ty, const double* tz, double* value, double* variance,
                              uint8_t* status, int64_t* request_id) {
+  NvtxRange nvtx_range("gs.server_submit_predict");
   if (!S || !request_id) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
   if (nt <= 0 || !tx || !ty || !value || !variance)
     return fail(GS_ERR_INVALID_PARAMETER, "a prediction request needs targets and outputs");
@@ -311,6 +377,7 @@ int gs_server_submit_predict(gs_server* S, int32_t dataset, int64_t nt, const do
 
 int gs_server_submit_loglik(gs_server* S, int32_t dataset, const gs_model* model, double* loglik,
                             int32_t* status, int64_t* request_id) {
+  NvtxRange nvtx_range("gs.server_submit_loglik");
   if (!S || !model || !loglik || !request_id) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
   auto r = std::make_unique<Request>();
   r->kind = 1;
@@ -326,6 +393,36 @@ int gs_server_set_precision(gs_server* s, int precision) {
   if (precision != GS_PREC_MIXED && precision != GS_PREC_FP64)
     return gs::fail(GS_ERR_INVALID_PARAMETER, "unknown precision");
   s->precision.store(precision);
+  return GS_OK;
+}
+
+int gs_server_cancel(gs_server* S, int64_t request_id) {
+  if (!S) return fail(GS_ERR_INVALID_PARAMETER, "null server");
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    auto it = S->requests.find(request_id);
+    if (it == S->requests.end()) return fail(GS_ERR_INVALID_PARAMETER, "unknown request");
+    Request* r = it->second.get();
+    bool found = false;
+    for (auto* q : {&S->pending_small, &S->pending_large}) {
+      auto pos = std::find(q->begin(), q->end(), r);
+      if (pos != q->end()) {
+        q->erase(pos);
+        found = true;
+        break;
+      }
+    }
+    if (!found)
+      return fail(GS_ERR_INVALID_PARAMETER,
+                  r->done ? "request already finished" : "request already running");
+    r->rc = GS_ERR_CANCELLED;
+    r->err = "cancelled before it started";
+    r->done = true;
+    r->finished = Clock::now();
+    ++S->cancelled;
+  }
+  S->cv_done.notify_all();
+  S->cv_work.notify_all();
   return GS_OK;
 }
 

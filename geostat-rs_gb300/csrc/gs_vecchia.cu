@@ -120,6 +120,9 @@ struct VArgs {
   const DevModel* models;  // device array of ncand models
   double* terms;           // ncand x n (position order)
   uint8_t* flag;           // ncand x n
+  // ordered positions evaluated: [k0, k1) (the whole plan unless a
+  // point-range call asks for part of it)
+  int64_t k0, k1;
   // REML (reml_loglik_with_plan, vecchia.rs:1278-1345): the trend basis
   // (p x n, column-major), and per (candidate, position) the record
   // (var, r, g_0 .. g_{p-1}) at rec[(c * n + k) * (2 + p)], with r and g the
@@ -194,7 +197,7 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
   S.flag = reinterpret_cast<int*>(smem_raw + lay.off_flag);
   __syncthreads();
 
-  for (int64_t k = blockIdx.x; k < a.n; k += gridDim.x) {
+  for (int64_t k = a.k0 + blockIdx.x; k < a.k1; k += gridDim.x) {
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
     const df zi = df_sub(a.vdf[i], a.mean_df);
@@ -385,7 +388,7 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
     __syncwarp();
   };
   const int64_t nwarps = (int64_t)gridDim.x * kVWarps;
-  for (int64_t k = (int64_t)blockIdx.x * kVWarps + wib; k < a.n; k += nwarps) {
+  for (int64_t k = a.k0 + (int64_t)blockIdx.x * kVWarps + wib; k < a.k1; k += nwarps) {
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
     // REML works on the raw values (vecchia.rs:1296-1337)
@@ -564,7 +567,8 @@ __global__ void vecchia_fp64_kernel(VArgs a, const int64_t* list, int64_t nlist,
   double* W = scratch + (int64_t)M * M * T + tid;
   double* K0 = W + (int64_t)M * T;
   for (int64_t it = tid; it < nlist; it += T) {
-    const int64_t code = list ? list[it] : it;
+    const int64_t span = a.k1 - a.k0;
+    const int64_t code = list ? list[it] : (it / span) * a.n + a.k0 + it % span;
     const int c = (int)(code / a.n);
     const int64_t k = code % a.n;
     const DevModel& mdl = a.models[c];
@@ -667,13 +671,15 @@ __global__ void reduce_reml(const double* rec, int64_t n, int p, int64_t chunk, 
 }
 
 
-// Fixed-order reduction: block b sums terms [b*chunk, (b+1)*chunk) of one
-// candidate in a fixed tree; the partials are added in block order.
-__global__ void reduce_terms(const double* terms, int64_t n, int64_t chunk, double* partial) {
+// Fixed-order reduction: block b sums terms [k0 + b*chunk, k0 + (b+1)*chunk)
+// of one candidate (positions below k1) in a fixed tree; the partials are
+// added in block order.
+__global__ void reduce_terms(const double* terms, int64_t n, int64_t k0, int64_t k1, int64_t chunk,
+                             double* partial) {
   __shared__ double sh[256];
   const int c = blockIdx.y;
-  const int64_t lo = blockIdx.x * chunk;
-  const int64_t hi = min(n, lo + chunk);
+  const int64_t lo = k0 + blockIdx.x * chunk;
+  const int64_t hi = min(k1, lo + chunk);
   double acc = 0.0;
   for (int64_t q = lo + threadIdx.x; q < hi; q += blockDim.x) acc += terms[(int64_t)c * n + q];
   sh[threadIdx.x] = acc;
@@ -915,11 +921,21 @@ __global__ void exclude_terms_kernel(double* terms, int64_t n, int64_t ncand,
 // the reml_sums(p) sums of the ungrouped REML (ll is left NaN).
 int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
                  int32_t* status, int precision, cudaStream_t s, const uint8_t* exclude,
-                 const double* basis, int p, double* reml_sums) {
+                 const double* basis, int p, double* reml_sums, int64_t k0, int64_t k1) {
+  NvtxRange nvtx_range("gs.vecchia_loglik");
   const gs_pointset* ps = P->ps;
   const int dim = ps->dim;
   const int64_t n = P->n;
   const int M = (int)P->m;
+  if (k1 < 0) k1 = n;
+  if (k0 < 0 || k1 > n || k0 > k1)
+    return fail(GS_ERR_INVALID_PARAMETER, "point range [" + std::to_string(k0) + ", " +
+                                              std::to_string(k1) + ") outside the plan's " +
+                                              std::to_string(n) + " points");
+  const bool partial_range = k0 != 0 || k1 != n;
+  if (partial_range && basis)
+    return fail(GS_ERR_INVALID_PARAMETER, "REML sums cover the whole plan");
+  const int64_t span = k1 - k0;
   ensure_vtables();
   std::vector<DevModel> dms(std::max<int64_t>(ncand, 1));
   std::vector<int> valid(ncand, 0);
@@ -942,6 +958,11 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
       if (models[c].s[k].has_anis) all_iso = false;
   }
   if (ncand == 0) return GS_OK;
+  if (span == 0) {  // an empty point range sums to zero
+    for (int64_t c = 0; c < ncand; ++c)
+      if (valid[c]) ll[c] = 0.0;
+    return GS_OK;
+  }
   DevBuf dmod, terms, flag, partial, out, cstat;
   GS_TRY(dmod.alloc(sizeof(DevModel) * ncand, s));
   GS_CUDA(cudaMemcpyAsync(dmod.ptr, dms.data(), sizeof(DevModel) * ncand, cudaMemcpyHostToDevice, s));
@@ -951,11 +972,15 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   if (reml) GS_TRY(rec.alloc((size_t)ncand * n * LW * 8, s));
   else GS_TRY(terms.alloc((size_t)ncand * n * 8, s));
   GS_TRY(flag.alloc((size_t)ncand * n, s));
+  // positions outside a partial range are never written: no flagged systems there
+  if (partial_range) GS_CUDA(cudaMemsetAsync(flag.ptr, 0, (size_t)ncand * n, s));
   GS_TRY(cstat.alloc((size_t)ncand * 4, s));
   GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
   VArgs a{};
   a.dim = dim;
   a.n = n;
+  a.k0 = k0;
+  a.k1 = k1;
   a.m = M;
   a.ncand = (int)ncand;
   a.iso_shared = all_iso ? 1 : 0;
@@ -991,9 +1016,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   } ev_guard{ev};
   GS_CUDA(cudaEventRecord(ev[0], s));
   if (mixed) {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int sms = sm_count();
     if (M <= kWarpN) {
       const size_t smem = vecchia_warp_layout(std::max(M, 1), dim, reml ? LW : 2).total * kVWarps;
       auto kern = reml ? (dim == 2 ? vecchia_warp_kernel<2, true> : vecchia_warp_kernel<3, true>)
@@ -1003,7 +1026,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
       GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kVWarps, smem));
       per_sm = std::max(per_sm, 1);
       const int blocks =
-          (int)std::min<int64_t>((n + kVWarps - 1) / kVWarps, (int64_t)sms * per_sm);
+          (int)std::min<int64_t>((span + kVWarps - 1) / kVWarps, (int64_t)sms * per_sm);
       kern<<<blocks, 32 * kVWarps, smem, s>>>(a, g_vtab, g_vkc);
     } else {
       const VLayout lay = vecchia_layout(std::max(M, 1), dim);
@@ -1015,7 +1038,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
       int per_sm = 0;
       GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
       per_sm = std::max(per_sm, 1);
-      const int blocks = (int)std::min<int64_t>(n, (int64_t)sms * per_sm);
+      const int blocks = (int)std::min<int64_t>(span, (int64_t)sms * per_sm);
       kern<<<blocks, block, smem, s>>>(a, g_vtab, g_vkc);
     }
     GS_CUDA(cudaGetLastError());
@@ -1039,11 +1062,11 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   if (!mixed) GS_CUDA(cudaEventRecord(ev[1], s));
   GS_CUDA(cudaEventRecord(ev[2], s));
   if (!mixed || nfl > 0) {
-    const int64_t work = mixed ? nfl : ncand * n;
+    const int64_t work = mixed ? nfl : ncand * span;
     const int64_t per = ((int64_t)M * M + 2 * (int64_t)M) * 8;
     // 512 threads per SM: measured fastest (the strided scratch then stays
     // mostly in L2; more threads spill it to HBM)
-    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 512);
+    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), (int64_t)sm_count() * 512);
     T = std::min<int64_t>(T, ((work + 127) / 128) * 128);
     T = std::max<int64_t>(T, 128);
     DevBuf scratch;
@@ -1092,15 +1115,16 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     return GS_OK;
   }
   if (exclude) {
-    exclude_terms_kernel<<<152 * 8, 256, 0, s>>>((double*)terms.ptr, n, ncand, exclude);
+    exclude_terms_kernel<<<sm_count() * 8, 256, 0, s>>>((double*)terms.ptr, n, ncand, exclude);
     GS_CUDA(cudaGetLastError());
     count_launch(1);
   }
   const int64_t chunk = 8192;
-  const int nblk = (int)((n + chunk - 1) / chunk);
+  const int nblk = (int)((span + chunk - 1) / chunk);
   GS_TRY(partial.alloc((size_t)nblk * ncand * 8, s));
   GS_TRY(out.alloc((size_t)ncand * 8, s));
-  reduce_terms<<<dim3(nblk, (unsigned)ncand), 256, 0, s>>>((double*)terms.ptr, n, chunk, (double*)partial.ptr);
+  reduce_terms<<<dim3(nblk, (unsigned)ncand), 256, 0, s>>>((double*)terms.ptr, n, k0, k1, chunk,
+                                                           (double*)partial.ptr);
   reduce_partials<<<(int)((ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)ncand, (double*)out.ptr);
   GS_CUDA(cudaGetLastError());
   count_launch(2);
@@ -1115,7 +1139,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     cudaEventElapsedTime(&a23, ev[2], ev[3]);
     cudaEventElapsedTime(&a03, ev[0], ev[3]);
     const double ms4[4] = {0.0, mixed ? (double)a01 : 0.0, (double)a23, (double)a03};
-    set_last_timings(ms4, mixed ? nfl : ncand * n);
+    set_last_timings(ms4, mixed ? nfl : ncand * span);
   }
   for (int64_t c = 0; c < ncand; ++c) {
     if (!valid[c]) continue;
@@ -1623,15 +1647,15 @@ static int build_groups(const gs_vecchia_plan* P, int64_t gsize, gs_vecchia_plan
     for (int64_t k = blocks[b].first; k < blocks[b].second; ++k) in_multi[k] = 1;
   }
   out->nmulti = (int64_t)multi.size();
-  if (cudaMalloc(&out->d_off, off.size() * 8) != cudaSuccess ||
-      cudaMalloc(&out->d_vid, std::max<size_t>(vid.size(), 1) * 4) != cudaSuccess ||
-      cudaMalloc(&out->d_slen, slen.size() * 4) != cudaSuccess)
+  if (dev_malloc((void**)&out->d_off, off.size() * 8) != cudaSuccess ||
+      dev_malloc((void**)&out->d_vid, std::max<size_t>(vid.size(), 1) * 4) != cudaSuccess ||
+      dev_malloc((void**)&out->d_slen, slen.size() * 4) != cudaSuccess)
     return fail(GS_ERR_OUT_OF_MEMORY, "grouped plan allocation failed");
   GS_CUDA(cudaMemcpy(out->d_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice));
   GS_CUDA(cudaMemcpy(out->d_vid, vid.data(), vid.size() * 4, cudaMemcpyHostToDevice));
   GS_CUDA(cudaMemcpy(out->d_slen, slen.data(), slen.size() * 4, cudaMemcpyHostToDevice));
-  if (cudaMalloc(&out->d_multi, std::max<size_t>(multi.size(), 1) * 8) != cudaSuccess ||
-      cudaMalloc(&out->d_in_multi, (size_t)n) != cudaSuccess)
+  if (dev_malloc((void**)&out->d_multi, std::max<size_t>(multi.size(), 1) * 8) != cudaSuccess ||
+      dev_malloc((void**)&out->d_in_multi, (size_t)n) != cudaSuccess)
     return fail(GS_ERR_OUT_OF_MEMORY, "grouped plan allocation failed");
   if (!multi.empty())
     GS_CUDA(cudaMemcpy(out->d_multi, multi.data(), multi.size() * 8, cudaMemcpyHostToDevice));
@@ -1698,9 +1722,9 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
   const int frame = (multi_only ? G.vmax_multi : G.vmax) + nr;
   const size_t ptab_bytes = (((size_t)frame * (frame - 1) / 2) * 4 + 15) & ~(size_t)15;
   const size_t per_warp = group_warp_doubles(frame) * 8;
-  int dev = 0, sms = 152, per_sm = 0, smem_max = 0;
+  const int sms = sm_count();
+  int dev = 0, per_sm = 0, smem_max = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   smem_max -= 2048;  // the kernel's static shared memory (the exp table)
   if (frame > 255 || ptab_bytes + per_warp > (size_t)smem_max)
@@ -1720,6 +1744,8 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
   VArgs a{};
   a.dim = dim;
   a.n = P->n;
+  a.k0 = 0;
+  a.k1 = P->n;
   a.m = (int)P->m;
   a.ncand = (int)ncand;
   a.x = ps->d_x;
@@ -1749,7 +1775,7 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
   for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
     const int64_t nr_ = std::min<int64_t>(65535, rows - r0);
     reduce_terms<<<dim3(nblk, (unsigned)nr_), 256, 0, s>>>(
-        (double*)terms.ptr + r0 * nbl, nbl, chunk, (double*)partial.ptr + r0 * nblk);
+        (double*)terms.ptr + r0 * nbl, nbl, 0, nbl, chunk, (double*)partial.ptr + r0 * nblk);
     ++launches;
   }
   reduce_partials<<<(int)((rows + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk, (int)rows,
@@ -1774,6 +1800,7 @@ int eval_blocks(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
 
 int vecchia_eval_grouped(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
                          int64_t gsize, double* ll, int32_t* status, cudaStream_t s) {
+  NvtxRange nvtx_range("gs.vecchia_loglik_grouped");
   if (gsize <= 1) return vecchia_eval(P, ncand, models, ll, status, GS_PREC_MIXED, s);
   gs_vecchia_plan::Groups G;
   GS_TRY(plan_groups(P, gsize, &G));
@@ -1851,6 +1878,7 @@ int gls_finish(int64_t n, int p, const double* sums, double* ll) {
 int vecchia_eval_reml(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models,
                       int64_t gsize, const double* d_basis, int p, double* ll, int32_t* status,
                       cudaStream_t s) {
+  NvtxRange nvtx_range("gs.vecchia_reml");
   const int per_m = reml_sums(p);
   if (P->m <= kWarpN) {
     // the ungrouped REML through the mixed warp kernel (the conditioning
@@ -1898,6 +1926,7 @@ int vecchia_eval_reml(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
 
 int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
                       double* grad, int32_t* status, int precision, cudaStream_t s) {
+  NvtxRange nvtx_range("gs.vecchia_grad");
   const gs_pointset* ps = P->ps;
   const int dim = ps->dim;
   const int64_t n = P->n;
@@ -1934,6 +1963,8 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
   VArgs a{};
   a.dim = dim;
   a.n = n;
+  a.k0 = 0;
+  a.k1 = n;
   a.m = M;
   a.ncand = (int)ncand;
   a.iso_shared = 1;
@@ -1954,9 +1985,7 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
   int64_t nfl = 0;
   const bool mixed = precision != GS_PREC_FP64 && M <= kWarpN;
   if (mixed) {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int sms = sm_count();
     const size_t smem = vecchia_grad_layout(std::max(M, 1), dim).total * kVWarps;
     auto kern = dim == 2 ? vecchia_grad_kernel<2> : vecchia_grad_kernel<3>;
     GS_TRY(allow_dynamic_smem((const void*)kern, smem));
@@ -1986,7 +2015,7 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
     const int64_t per = ((int64_t)M * M + 5 * (int64_t)M) * 8;
     // 512 threads per SM: measured fastest (the strided scratch then stays
     // mostly in L2; more threads spill it to HBM)
-    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), 152 * 512);
+    int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / std::max<int64_t>(per, 1), 128), (int64_t)sm_count() * 512);
     T = std::min<int64_t>(T, ((work + 127) / 128) * 128);
     T = std::max<int64_t>(T, 128);
     DevBuf scratch;
@@ -2005,7 +2034,7 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
   const int nblk = (int)((n + chunk - 1) / chunk);
   GS_TRY(partial.alloc((size_t)nblk * 4 * ncand * 8, s));
   GS_TRY(out.alloc((size_t)4 * ncand * 8, s));
-  reduce_terms<<<dim3(nblk, (unsigned)(4 * ncand)), 256, 0, s>>>((double*)terms.ptr, n, chunk,
+  reduce_terms<<<dim3(nblk, (unsigned)(4 * ncand)), 256, 0, s>>>((double*)terms.ptr, n, 0, n, chunk,
                                                                   (double*)partial.ptr);
   reduce_partials<<<(int)((4 * ncand + 127) / 128), 128, 0, s>>>((double*)partial.ptr, nblk,
                                                                  (int)(4 * ncand), (double*)out.ptr);
@@ -2030,6 +2059,7 @@ int vecchia_eval_grad(const gs_vecchia_plan* P, int64_t ncand, const gs_model* m
 
 // vecchia_plan (vecchia.rs:232-282).
 int plan_create(const gs_pointset* ps, int64_t m, const int64_t* order, gs_vecchia_plan** out) {
+  NvtxRange nvtx_range("gs.vecchia_plan");
   *out = nullptr;
   const int64_t n = ps->n;
   const int dim = ps->dim;
@@ -2065,9 +2095,9 @@ int plan_create(const gs_pointset* ps, int64_t m, const int64_t* order, gs_vecch
                : fail(GS_ERR_CUDA, "stream creation failed");
   cudaStream_t s = P->stream;
   const int M = (int)P->m;
-  if (!rc && (cudaMalloc(&P->d_order, n * 8) != cudaSuccess ||
-              cudaMalloc(&P->d_nb, (size_t)n * M * 4) != cudaSuccess ||
-              cudaMalloc(&P->d_cnt, n * 4) != cudaSuccess))
+  if (!rc && (dev_malloc((void**)&P->d_order, n * 8) != cudaSuccess ||
+              dev_malloc((void**)&P->d_nb, (size_t)n * M * 4) != cudaSuccess ||
+              dev_malloc((void**)&P->d_cnt, n * 4) != cudaSuccess))
     rc = fail(GS_ERR_OUT_OF_MEMORY, "plan allocation failed");
   if (!rc) {
     DevBuf ox, oy, oz;
@@ -2076,7 +2106,7 @@ int plan_create(const gs_pointset* ps, int64_t m, const int64_t* order, gs_vecch
     if (!rc && dim == 3) rc = oz.alloc(n * 8, s);
     if (!rc) {
       cudaMemcpyAsync(P->d_order, P->order.data(), n * 8, cudaMemcpyHostToDevice, s);
-      const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
+      const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 32);
       gather_by_order<<<blocks, 256, 0, s>>>(n, P->d_order, ps->d_x, ps->d_y, ps->d_z,
                                             (double*)ox.ptr, (double*)oy.ptr,
                                             dim == 3 ? (double*)oz.ptr : nullptr);
@@ -2099,7 +2129,7 @@ int plan_create(const gs_pointset* ps, int64_t m, const int64_t* order, gs_vecch
                            P->d_cnt, s);
       }
       if (!rc) {
-        positions_to_ids<<<(int)std::min<int64_t>((n * M + 255) / 256, 152 * 64), 256, 0, s>>>(
+        positions_to_ids<<<(int)std::min<int64_t>((n * M + 255) / 256, (int64_t)sm_count() * 64), 256, 0, s>>>(
             n * M, P->d_order, P->d_nb);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
           rc = fail(GS_ERR_CUDA, "plan kernels failed");
@@ -2407,6 +2437,7 @@ __global__ void vp_merge_kernel(const int64_t* list, int64_t nlist, int64_t n, i
 int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t nt, const double* tx,
                          const double* ty, const double* tz, int64_t m, double* value,
                          double* variance) {
+  NvtxRange nvtx_range("gs.vecchia_predict");
   const int dim = ps->dim;
   GS_TRY(reject_vecchia_model(*model, dim));
   DevModel dm;
@@ -2466,7 +2497,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
   GS_TRY(cdf.alloc((size_t)dim * ns * sizeof(df), s));
   GS_TRY(sm64.alloc(ns * 8, s));
   GS_TRY(smdf.alloc(ns * sizeof(df), s));
-  vp_store_kernel<<<(int)std::min<int64_t>((ns + 255) / 256, 152 * 32), 256, 0, s>>>(
+  vp_store_kernel<<<(int)std::min<int64_t>((ns + 255) / 256, (int64_t)sm_count() * 32), 256, 0, s>>>(
       dim, n, ns, (double*)sx.ptr, (double*)sy.ptr, (double*)sz.ptr, ps->d_v, mean, (df*)cdf.ptr,
       (double*)sm64.ptr, (df*)smdf.ptr);
   GS_CUDA(cudaGetLastError());
@@ -2553,9 +2584,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
   a.d64 = (double*)d64.ptr;
   a.flag = (uint8_t*)flag.ptr;
   a.err = (int32_t*)err.ptr;
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = sm_count();
   const bool mixed = kout <= kWarpN;
   size_t vsmem = 0;
   if (mixed) {
@@ -2565,7 +2594,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
   }
   // FP64 slabs: up to 2 GiB, at least one block of threads
   const int64_t per = ((int64_t)kout * kout + 2 * (int64_t)kout) * 8;
-  int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / per, 128), 152 * 1024);
+  int64_t T = std::min<int64_t>(std::max<int64_t>(((int64_t)1 << 31) / per, 128), (int64_t)sm_count() * 1024);
   T = std::max<int64_t>((T / 128) * 128, 128);
   DevBuf slab;
   GS_TRY(slab.alloc((size_t)T * per, s));
@@ -2589,7 +2618,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
       GS_CUDA(cudaGetLastError());
       count_launch(1);
     }
-    const int gb = (int)std::min<int64_t>((ln + 255) / 256, 152 * 32);
+    const int gb = (int)std::min<int64_t>((ln + 255) / 256, (int64_t)sm_count() * 32);
     vp_bound_kernel<<<gb, 256, 0, s>>>(a.list, ln, n, kout, a.nb, a.cnt, (const int32_t*)rlen.ptr,
                                       (int64_t*)bound.ptr);
     GS_CUDA(cudaGetLastError());
@@ -2617,7 +2646,7 @@ int vecchia_predict_impl(const gs_pointset* ps, const gs_model* model, int64_t n
       std::swap(nc.bytes, pool_c.bytes);
       cap = ncap;
     }
-    const int mb = (int)std::min<int64_t>((ln * 32 + 255) / 256, 152 * 32);
+    const int mb = (int)std::min<int64_t>((ln * 32 + 255) / 256, (int64_t)sm_count() * 32);
     vp_merge_kernel<<<mb, 256, 0, s>>>(a.list, ln, n, kout, a.nb, a.cnt, a.w64, a.d64,
                                        (const int64_t*)offs.ptr, used, (int64_t*)roff.ptr,
                                        (int32_t*)rlen.ptr, (int32_t*)pool_i.ptr,
@@ -2690,6 +2719,19 @@ int gs_vecchia_loglik_batch(const gs_vecchia_plan* P, int64_t ncand, const gs_mo
   if (!P) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
   cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
   return vecchia_eval(P, ncand, models, loglik, status, precision, s);
+}
+
+int gs_vecchia_loglik_batch_range(const gs_vecchia_plan* P, int64_t lo, int64_t hi, int64_t ncand,
+                                  const gs_model* models, double* loglik, int32_t* status,
+                                  int precision, void* stream) {
+  if (!P) return fail(GS_ERR_INVALID_PARAMETER, "null plan");
+  if (lo < 0 || hi < lo || hi > P->n)
+    return fail(GS_ERR_INVALID_PARAMETER, "point range [" + std::to_string(lo) + ", " +
+                                              std::to_string(hi) + ") outside the plan's " +
+                                              std::to_string(P->n) + " points");
+  cudaStream_t s = stream ? (cudaStream_t)stream : P->stream;
+  return vecchia_eval(P, ncand, models, loglik, status, precision, s, nullptr, nullptr, 0, nullptr,
+                      lo, hi);
 }
 
 int gs_vecchia_loglik_grouped_batch(const gs_vecchia_plan* P, int64_t ncand,
@@ -2850,12 +2892,16 @@ int finish_fit(int32_t kind, const std::pair<std::vector<double>, double>& best,
 // Nelder-Mead multistart (optim.rs:106-123) with every start's simplex
 // advanced in lock step: each round's pending points of all starts are one
 // batch of `objective` (xs -> f).
+// Batched objective launches of this thread's last lock-step Nelder-Mead fit.
+thread_local int64_t g_fit_rounds = 0;
+
 template <class Obj>
 int nm_lockstep(const std::vector<std::vector<double>>& starts, double step, int64_t max_iter,
                 Obj objective, std::pair<std::vector<double>, double>* best, int64_t* n_evals) {
   std::vector<NelderMead> runs;
   for (const auto& x0 : starts) runs.emplace_back(x0, step, max_iter);
   int64_t evals = 0;
+  g_fit_rounds = 0;
   for (int guard = 0; guard < 1000000; ++guard) {
     std::vector<std::vector<double>> xs;
     std::vector<size_t> owner;
@@ -2870,6 +2916,7 @@ int nm_lockstep(const std::vector<std::vector<double>>& starts, double step, int
     std::vector<double> fv;
     GS_TRY(objective(xs, fv));
     evals += (int64_t)xs.size();
+    ++g_fit_rounds;
     std::vector<std::vector<double>> fvals(runs.size());
     for (size_t b = 0; b < xs.size(); ++b) fvals[owner[b]].push_back(fv[b]);
     for (size_t r = 0; r < runs.size(); ++r)
@@ -2993,6 +3040,7 @@ int make_basis(const gs_pointset* ps, int32_t degree, const double* drift, int64
 int fit_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order, int64_t gsize,
            const std::vector<double>* basis, int p, gs_model* out_model, double* out_loglik,
            double* out_x, int64_t* n_evals) {
+  NvtxRange nvtx_range("gs.fit_nelder_mead");
   gs_vecchia_plan* P = nullptr;
   GS_TRY(plan_create(ps, m, order, &P));
   std::unique_ptr<gs_vecchia_plan> own(P);
@@ -3031,6 +3079,8 @@ int fit_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
 }  // namespace gs
 
 extern "C" {
+
+int64_t gs_last_fit_rounds(void) { return g_fit_rounds; }
 
 int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
                    gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals) {

@@ -77,13 +77,16 @@ SIGNATURES = {
     "gs_kriging_predict_fp64_noalloc": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                                _vp, _vp]),
     "gs_last_fallbacks": (_i64, []),
+    "gs_last_fit_rounds": (_i64, []),
+    "gs_debug_device_allocations": (_i64, []),
+    "gs_debug_refuse_allocations": (_int, [_i64]),
     "gs_last_lu_resolves": (_i64, []),
-    "gs_probe_expneg": (_int, [_i64, _pd, _pd]),
     "gs_server_create": (_int, [_i64, _i32, C.POINTER(_vp)]),
     "gs_server_add_kriging": (_int, [_vp, _vp, _pi32]),
     "gs_server_add_vecchia": (_int, [_vp, _vp, _pi32]),
     "gs_server_submit_predict": (_int, [_vp, _i32, _i64, _pd, _pd, _pd, _pd, _pd, _pu8, _pi64]),
     "gs_server_submit_loglik": (_int, [_vp, _i32, _pm, _pd, _pi32, _pi64]),
+    "gs_server_cancel": (_int, [_vp, _i64]),
     "gs_server_wait": (_int, [_vp, _i64, _pd]),
     "gs_server_set_precision": (_int, [_vp, _int]),
     "gs_server_stats": (_int, [_vp, _pd, _pd, _pi64, _pi64]),
@@ -95,6 +98,7 @@ SIGNATURES = {
     "gs_vecchia_plan_get": (_int, [_vp, _pi64, _pi64, _pi32]),
     "gs_vecchia_plan_destroy": (None, [_vp]),
     "gs_vecchia_loglik_batch": (_int, [_vp, _i64, _pm, _pd, _pi32, _int, _vp]),
+    "gs_vecchia_loglik_batch_range": (_int, [_vp, _i64, _i64, _i64, _pm, _pd, _pi32, _int, _vp]),
     "gs_vecchia_loglik_grouped_batch": (_int, [_vp, _i64, _pm, _i64, _pd, _pi32, _vp]),
     "gs_vecchia_loglik": (_int, [_vp, _pm, _i64, _pi64, _pd]),
     "gs_vecchia_mle": (_int, [_vp, _i32, _i64, _pi64, _pm, _pd, _pd, _pi64]),
@@ -121,9 +125,7 @@ SIGNATURES = {
     "gs_nelder_mead_multistart": (_int, [OBJECTIVE, _vp, _i64, _i64, _pd, _d, _i64, _pd, _pd]),
     "gs_rng_uniform": (None, [_u64, _i64, _pd]),
     "gs_rng_normal": (None, [_u64, _i64, _pd]),
-    "gs_synth_rff_field": (_int, [_int, _i64, _pd, _pd, _pd, _pm, _i64, _u64, _pd]),
     "gs_last_timings": (_int, [_pd]),
-    "gs_probe_fma_tflops": (_int, [_int, _pd]),
     "gs_launch_count": (_i64, []),
 }
 

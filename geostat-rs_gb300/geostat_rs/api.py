@@ -682,6 +682,20 @@ class VecchiaPlan:
                                                        PRECISIONS[precision], None))
         return ll, st
 
+    def loglik_range(self, lo: int, hi: int, models: Sequence[VariogramModel],
+                     precision="mixed"):
+        """Sum of the log-likelihood terms of the ordered positions
+        ``[lo, hi)`` of each candidate model (one shard of the points).
+        Returns ``(partial_loglik, status)``."""
+        arr = (_abi.Model * len(models))(*[model_struct(m) for m in models])
+        ll = np.empty(len(models))
+        st = np.empty(len(models), dtype=np.int32)
+        _abi.check(_abi.load().gs_vecchia_loglik_batch_range(self._h, int(lo), int(hi),
+                                                             len(models), arr, _p(ll),
+                                                             _p(st, C.c_int32),
+                                                             PRECISIONS[precision], None))
+        return ll, st
+
     def loglik_grouped(self, models: Sequence[VariogramModel], group_size: int):
         """``loglik_with_plan_grouped`` (vecchia.rs:604-668, Guinness
         grouping) of each candidate model; ``group_size <= 1`` is
@@ -1054,6 +1068,11 @@ class Server:
         """Precision of the launches formed from now on ("mixed" or "fp64")."""
         _abi.check(_abi.load().gs_server_set_precision(self._h, PRECISIONS[precision]))
 
+    def cancel(self, req):
+        """Cancels a request that has not started (raises InvalidParameter
+        once it runs or has finished); its ``wait`` then raises Cancelled."""
+        _abi.check(_abi.load().gs_server_cancel(self._h, req.id))
+
     def wait(self, req) -> float:
         lat = C.c_double()
         _abi.check(_abi.load().gs_server_wait(self._h, req.id, C.byref(lat)))
@@ -1120,27 +1139,3 @@ def rng_normal(seed: int, count: int) -> np.ndarray:
     return out
 
 
-def clustered_points(n: int, extent: float, n_blobs: int, sigma: float, frac_blobs: float,
-                     seed: int) -> np.ndarray:
-    """Seeded clustered 2-D layout: ``round(frac_blobs * n)`` points in
-    ``n_blobs`` isotropic Gaussian blobs (standard deviation ``sigma``, centres
-    uniform in [0, extent]^2, point i in blob i mod n_blobs) followed by the
-    rest uniform in [0, extent]^2."""
-    nb = int(round(frac_blobs * n))
-    cen = rng_uniform(seed, 2 * n_blobs).reshape(n_blobs, 2) * extent
-    g = rng_normal(seed + 1, 2 * nb).reshape(nb, 2) * sigma
-    pb = cen[np.arange(nb) % n_blobs] + g
-    pu = rng_uniform(seed + 2, 2 * (n - nb)).reshape(n - nb, 2) * extent
-    return np.vstack([pb, pu])
-
-
-def rff_field(coords, model: VariogramModel, n_features: int, seed: int) -> np.ndarray:
-    """Seeded random-Fourier-feature Gaussian field at ``coords`` (device)."""
-    c = _f64(coords)
-    dim = c.shape[1]
-    cols = [_f64(c[:, d]) for d in range(dim)] + ([None] if dim == 2 else [])
-    out = np.empty(len(c))
-    _abi.check(_abi.load().gs_synth_rff_field(dim, len(c), _p(cols[0]), _p(cols[1]), _p(cols[2]),
-                                              C.byref(model_struct(model)), int(n_features),
-                                              int(seed), _p(out)))
-    return out

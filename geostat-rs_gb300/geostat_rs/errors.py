@@ -51,9 +51,14 @@ class IoError(OSError):
     code = 102
 
 
+class Cancelled(RuntimeError):
+    """A serving request cancelled before it started (no reference counterpart)."""
+    code = 103
+
+
 _BY_CODE = {c.code: c for c in (InsufficientData, DimensionMismatch, SingularSystem,
                                 InvalidParameter, NoNeighbors, DuplicatePoints, CudaError,
-                                OutOfDeviceMemory, IoError)}
+                                OutOfDeviceMemory, IoError, Cancelled)}
 
 
 def raise_for(code: int, message: str):

@@ -1,16 +1,15 @@
-// gs_probe.cu -- measurement helpers: CUDA-core FMA throughput (the roofline
-// denominator of the per-system kernels, which run on the FP32 pipe with a
-// little FP64) and the count of this library's kernel launches.
+// gs_probe.cu -- measurement helpers for the benchmark and the tests (not part
+// of the drop-in library): CUDA-core FMA throughput (the roofline denominator
+// of the per-system kernels, which run on the FP32 pipe with a little FP64)
+// and the FP64 re-solve kernels' table-driven exp(-x) for accuracy checks.
 #include <algorithm>
 #include <atomic>
 
 #include "gs_common.cuh"
 #include "gs_internal.h"
+#include "gs_workload.h"
 
 namespace gs {
-
-static std::atomic<long long> g_launches{0};
-void count_launch(int n) { g_launches += n; }
 
 namespace {
 
@@ -56,10 +55,7 @@ void launch_probe<float2>(float2* out, int blocks, int threads, int iters) {
 
 template <class T>
 int probe(double* tflops, int iters, int lanes) {
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int threads = 256, blocks = sms * 8;
+  const int threads = 256, blocks = sm_count() * 8;
   T* out = nullptr;
   GS_CUDA(cudaMalloc(&out, sizeof(T) * threads * blocks));
   cudaEvent_t e0, e1;
@@ -104,7 +100,7 @@ extern "C" int gs_probe_expneg(int64_t n, const double* x, double* out) {
   GS_TRY(dx.alloc((size_t)n * 8, nullptr));
   GS_TRY(dout.alloc((size_t)n * 8, nullptr));
   GS_CUDA(cudaMemcpy(dx.ptr, x, (size_t)n * 8, cudaMemcpyHostToDevice));
-  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)gs::sm_count() * 8);
   gs::expneg_probe<<<blocks, 256>>>(n, (const double*)dx.ptr, (double*)dout.ptr, et);
   GS_CUDA(cudaGetLastError());
   GS_CUDA(cudaMemcpy(out, dout.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost));
@@ -118,4 +114,3 @@ extern "C" int gs_probe_fma_tflops(int precision, double* tflops) {
   return gs::probe<float>(tflops, 1 << 16, 1);
 }
 
-extern "C" int64_t gs_launch_count(void) { return gs::g_launches.load(); }

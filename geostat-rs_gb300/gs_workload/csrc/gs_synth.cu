@@ -1,4 +1,5 @@
-// gs_synth.cu -- seeded synthetic Gaussian fields for benchmarks and tests.
+// gs_synth.cu -- seeded synthetic Gaussian fields for the benchmark and the
+// tests (not part of the drop-in library).
 //
 // A random-Fourier-feature field (Rahimi & Recht 2007): for each structure,
 // sqrt(2 sill / F) * sum_f cos(w_f . (R x) + phi_f) with w_f drawn from the
@@ -13,6 +14,7 @@
 #include "gs_common.cuh"
 #include "gs_host.h"
 #include "gs_internal.h"
+#include "gs_workload.h"
 
 namespace gs {
 namespace {
@@ -106,7 +108,7 @@ extern "C" int gs_synth_rff_field(int dim, int64_t n, const double* x, const dou
     cudaMemcpy(dw, w.data(), F * 3 * 8, cudaMemcpyHostToDevice);
     cudaMemcpy(dphi, phi.data(), F * 8, cudaMemcpyHostToDevice);
     double amp = std::sqrt(2.0 * st.sill / (double)F);
-    rff_kernel<<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256>>>(dim, n, dx, dy, dz, (int)F, dw, dphi, amp, dout);
+    rff_kernel<<<(int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 32), 256>>>(dim, n, dx, dy, dz, (int)F, dw, dphi, amp, dout);
   }
   cudaError_t e = cudaMemcpy(out, dout, n * 8, cudaMemcpyDeviceToHost);
   cleanup();

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define GS_ABI_VERSION 1
+#define GS_ABI_VERSION 2
 #define GS_MAX_STRUCTURES 4
 /* Largest conditioning set the mixed-precision kernel holds on chip, and the
  * largest neighbourhood (neighbours + drift terms) any GPU kernel accepts. */
@@ -39,7 +39,8 @@ enum {
   GS_ERR_DUPLICATE_POINTS = 6,
   GS_ERR_CUDA = 100,
   GS_ERR_OUT_OF_MEMORY = 101,
-  GS_ERR_IO = 102 /* file input/output (the CLI's anyhow errors) */
+  GS_ERR_IO = 102, /* file input/output (the CLI's anyhow errors) */
+  GS_ERR_CANCELLED = 103 /* a serving request cancelled before it started */
 };
 
 /* ModelKind (crates/geostat-core/src/variogram/model.rs:50-101).  The CUDA
@@ -270,6 +271,19 @@ void gs_vecchia_plan_destroy(gs_vecchia_plan* plan);
  * GeostatError code (a singular conditioning system). */
 int gs_vecchia_loglik_batch(const gs_vecchia_plan* plan, int64_t ncand, const gs_model* models,
                             double* loglik, int32_t* status, int precision, void* stream);
+/* The terms of loglik_with_plan's per-point loop (vecchia.rs:285-336) for
+ * the ordered positions [lo, hi) only, summed per candidate: one shard of
+ * the likelihood when the points are split across GPUs.  Position k is the
+ * k-th point of the plan's max-min order (position 0 contributes the
+ * unconditional N(0, sill) term).  Each range's sum is a fixed-order tree
+ * over 8192-position chunks starting at lo, so it does not depend on
+ * scheduling; sums over consecutive ranges covering [0, n), added in range
+ * order, equal gs_vecchia_loglik_batch's total up to re-association
+ * (relative differences near 1e-16).  lo = hi gives 0; a range outside
+ * [0, n) is InvalidParameter. */
+int gs_vecchia_loglik_batch_range(const gs_vecchia_plan* plan, int64_t lo, int64_t hi,
+                                  int64_t ncand, const gs_model* models, double* loglik,
+                                  int32_t* status, int precision, void* stream);
 /* loglik_with_plan_grouped (vecchia.rs:604-668, Guinness 2018 grouping) for
  * ncand candidates: blocks of up to group_size consecutive ordered points
  * (guinness_blocks, vecchia.rs:570-602) conditioned jointly on the union of
@@ -320,6 +334,9 @@ int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t
 int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
                       int64_t nstarts, const double* starts, double step, int64_t max_iter,
                       gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals);
+/* Batched objective launches (rounds) of the last lock-step Nelder-Mead fit
+ * on this host thread (gs_vecchia_mle_nm and the grouped / REML fits). */
+int64_t gs_last_fit_rounds(void);
 /* vecchia_mle_grouped (vecchia.rs:939-950): group_size <= 1 is
  * gs_vecchia_mle; otherwise Nelder-Mead (step 0.3, 2000 iterations) from
  * the reference's three starts over the grouped likelihood, each round's
@@ -356,11 +373,21 @@ int gs_nelder_mead_multistart(gs_objective_fn f, void* ctx, int64_t n, int64_t n
 /* Serving loop (no counterpart in the reference, which serves one call at a
  * time): data sets stay resident as built predictors and Vecchia plans;
  * callers on any thread submit prediction and log-likelihood requests;
- * `executors` threads, each with its own stream, admit the oldest pending
- * request once the device-memory budget allows it, coalesce every pending
- * request of the same data set and kind into the same launch, and scatter the
- * results.  Host buffers of a request must stay valid until gs_server_wait
- * returns for it; every request is waited for exactly once.
+ * `executors` threads, each with its own stream, take pending requests once
+ * device memory admits them -- their bytes within mem_budget_bytes and within
+ * the device's current headroom (free memory plus what the stream-ordered
+ * pool holds unused, less 512 MiB) -- coalesce every pending request of the
+ * same data set and kind into the same launch, and scatter the results.
+ * Size-aware admission: predictions of 131,072 targets or more are large;
+ * executor 0 serves large requests in arrival order (and small ones when no
+ * large request waits), the other executors serve small requests only, so a
+ * small request never waits behind a large one.  A request whose device
+ * bytes exceed mem_budget_bytes is refused at submission
+ * (GS_ERR_OUT_OF_MEMORY).  Host buffers of a request must stay valid until
+ * gs_server_wait returns for it; every request is waited for exactly once.
+ * gs_server_cancel removes a request that has not started (its wait then
+ * returns GS_ERR_CANCELLED); a running or finished request cannot be
+ * cancelled (GS_ERR_INVALID_PARAMETER).
  * gs_server_stats reports the median and 99th-percentile submit-to-finish
  * latency of the completed requests and the number of launches formed. */
 typedef struct gs_server gs_server;
@@ -375,20 +402,17 @@ int gs_server_submit_loglik(gs_server* s, int32_t dataset, const gs_model* model
 /* Precision of the launches formed from now on (GS_PREC_MIXED by default;
  * GS_PREC_FP64 serves the same requests through the plain FP64 build). */
 int gs_server_set_precision(gs_server* s, int precision);
+int gs_server_cancel(gs_server* s, int64_t request_id);
 int gs_server_wait(gs_server* s, int64_t request_id, double* latency_ms);
 int gs_server_stats(gs_server* s, double* p50_ms, double* p99_ms, int64_t* completed,
                     int64_t* batches);
 void gs_server_destroy(gs_server* s);
 
-/* Seeded synthetic inputs (no reference counterpart beyond
- * crates/geostat-core/src/rng.rs): xoshiro256++ uniforms on the host and a
- * random-Fourier-feature Gaussian field evaluated on the device.  kind is
- * the spectral family (exponential, gaussian, matern15, matern25; spherical
- * uses the exponential family at the same practical range). */
+/* Seeded xoshiro256++ streams (crates/geostat-core/src/rng.rs): uniforms in
+ * [0, 1) and standard normals, the generator behind seeded k-fold
+ * assignments. */
 void gs_rng_uniform(uint64_t seed, int64_t count, double* out);
 void gs_rng_normal(uint64_t seed, int64_t count, double* out);
-int gs_synth_rff_field(int dim, int64_t n, const double* x, const double* y, const double* z,
-                       const gs_model* model, int64_t n_features, uint64_t seed, double* out);
 
 /* Timing of the last gs_kriging_predict_* or Vecchia log-likelihood call on
  * this host thread (ms of device time per phase, measured with CUDA events on
@@ -405,15 +429,15 @@ int64_t gs_last_fallbacks(void);
  * GS_PREC_FP64; 0 after a Vecchia call). */
 int64_t gs_last_lu_resolves(void);
 
-/* Measurement helpers (no reference counterpart): sustained CUDA-core FMA
- * throughput in TFLOP/s for FP32 (precision 0), FP64 (1) or packed FP32x2
- * FMAs (2) -- the roofline denominator of the per-system kernels -- and the
- * number of kernels this library has launched since it was loaded. */
-int gs_probe_fma_tflops(int precision, double* tflops);
-/* exp(-x) for x >= 0 as the FP64 re-solve kernels compute it (table-driven
- * exp on the device; 0 for x >= 708), for accuracy checks. */
-int gs_probe_expneg(int64_t n, const double* x, double* out);
+/* Diagnostics (no reference counterpart): the number of kernels this library
+ * has launched since it was loaded, and the number of device allocations it
+ * has made (cudaMalloc and stream-ordered allocations alike). */
 int64_t gs_launch_count(void);
+int64_t gs_debug_device_allocations(void);
+/* Failure injection for tests (host side; no device fault): the next
+ * `count` stream-ordered allocations the library makes fail as if the device
+ * were out of memory (the calls return GS_ERR_OUT_OF_MEMORY); 0 ends it. */
+int gs_debug_refuse_allocations(int64_t count);
 
 /* CSV input and output (crates/geostat-cli/src/io_utils.rs), host only.
  * gs_csv_read reads the named numeric columns of a CSV file (header row,

@@ -13,6 +13,7 @@ import pytest
 
 import pyoracle as O
 import geostat_rs as G
+import gs_workload as W
 from gpu_common import assert_close, clustered_matern_model, clustered_points
 
 pytestmark = pytest.mark.gpu
@@ -24,7 +25,7 @@ SEARCH = dict(max_per_octant=16, max_neighbors=64, min_neighbors=4)
 def _data():
     c = clustered_points(100_000, 41, extent=EXTENT, nblobs=50)
     m = clustered_matern_model()
-    v = G.rff_field(c, m, 1024, 42)
+    v = W.rff_field(c, m, 1024, 42)
     cov = O.rng_uniform(43, len(c))
     g = (np.arange(36) + 0.5) * (EXTENT / 36)
     yy, xx = np.meshgrid(g, g, indexing="ij")
@@ -131,3 +132,52 @@ def test_clustered_mixed_matches_fp64_build_at_scale(data, kind):
     vs = float(np.mean(np.abs(v)))
     assert_close(mixed.value, plain.value, vs, 1e-9, f"{kind} value")
     assert_close(mixed.variance, plain.variance, 1e-3, 1e-9, f"{kind} variance")
+
+
+# ------------------------------------------------- the full-size workload --
+FULL_EXTENT = 10000.0
+FULL_GRID = 2048
+
+
+@pytest.fixture(scope="module")
+def full_data():
+    """1,000,000 points over 10 km x 10 km, 70 % in 500 blobs of sigma 15 m;
+    Matern 3/2 field; one U[0,1] covariate; the 2048 x 2048 grid."""
+    c = W.clustered_points(1_000_000, FULL_EXTENT, 500, 15.0, 0.7, 61)
+    m = clustered_matern_model()
+    v = W.rff_field(c, m, 1024, 62)
+    cov = O.rng_uniform(63, len(c))
+    centres = O.rng_uniform(61, 2 * 500).reshape(500, 2) * FULL_EXTENT
+    return c, v, m, cov, centres
+
+
+@pytest.mark.parametrize("kind,row0", [("ordinary", 300), ("universal", 1000),
+                                        ("external_drift", 1700)])
+def test_clustered_full_size_matches_oracle_on_a_sample(full_data, kind, row0):
+    """One band of 32 grid rows (65,536 targets) per kind through the whole
+    pass (search, FP32 attempt, routing, FP64 re-solves), checked against the
+    oracle on 150 random targets of the band and the 50 targets closest to a
+    blob centre, at both precisions."""
+    c, v, m, cov, centres = full_data
+    k = _predictor(kind, c, v, m, cov)
+    g = (np.arange(FULL_GRID) + 0.5) * (FULL_EXTENT / FULL_GRID)
+    yy, xx = np.meshgrid(g[row0:row0 + 32], g, indexing="ij")
+    t = np.stack([xx.ravel(), yy.ravel()], 1)
+    tcov = O.rng_uniform(64 + row0, len(t))
+    pick = np.random.default_rng(row0).choice(len(t), 150, replace=False)
+    from scipy.spatial import cKDTree
+    dmin = cKDTree(centres).query(t)[0]
+    core = np.argsort(dmin, kind="stable")[:50]
+    idx = np.unique(np.concatenate([pick, core]))
+    ref = O.krige(c, v, m, t[idx], method=kind, degree=1,
+                  drift=cov.reshape(-1, 1) if kind == "external_drift" else None,
+                  target_drift=tcov[idx].reshape(-1, 1) if kind == "external_drift" else None,
+                  **SEARCH)
+    vs = float(np.mean(np.abs(v)))
+    for prec in ("mixed", "fp64"):
+        out = _predict(k, kind, t, tcov, prec)
+        if prec == "mixed":
+            assert ((out.status & 0x40) != 0).mean() > 0.5  # mostly the FP64 re-solve tiers
+        assert ((out.status[idx] & 0x3f) == ref["status"].astype(np.uint8)).all()
+        assert_close(out.value[idx], ref["value"], vs, 1e-9, f"{kind} {prec} value")
+        assert_close(out.variance[idx], ref["variance"], 1e-3, 1e-9, f"{kind} {prec} variance")

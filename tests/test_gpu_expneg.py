@@ -4,22 +4,16 @@ Tolerance: at most 2 units in the last place of the host value for
 0 <= x < 708 (the method's error is about 1 ulp, the host's at most 1 ulp);
 exactly 0 for x >= 708, where exp(-x) < 3.3e-308.
 """
-import ctypes as C
-
 import numpy as np
 import pytest
 
-from geostat_rs import _abi
+import gs_workload as W
 
 pytestmark = pytest.mark.gpu
 
 
 def _dev_expneg(x):
-    x = np.ascontiguousarray(x, dtype=np.float64)
-    out = np.empty_like(x)
-    _abi.check(_abi.load().gs_probe_expneg(len(x), x.ctypes.data_as(C.POINTER(C.c_double)),
-                                           out.ctypes.data_as(C.POINTER(C.c_double))))
-    return out
+    return W.probe_expneg(x)
 
 
 def test_expneg_within_two_ulp():

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import geostat_rs as G
+import gs_workload as W
 from geostat_rs.model import Structure, VariogramModel
 from gpu_common import uniform_points
 
@@ -40,7 +41,7 @@ def test_captured_pass_replays_on_new_targets(case):
                               Structure("exponential", 0.25, 400.0)])
     ext = [1000.0, 1000.0, 200.0][:dim]
     c = uniform_points(20000, dim, 611 + dim, ext)
-    v = 10.0 + G.rff_field(c, m, 512, 9)
+    v = 10.0 + W.rff_field(c, m, 512, 9)
     k = G.Kriging.new(G.PointSet(c, v), m, cfg)
     nt = 6000
     rng = np.random.default_rng(17)
@@ -89,7 +90,7 @@ def test_captured_pass_replays_on_new_targets(case):
 def test_async_pass_without_capture_matches():
     m = VariogramModel(0.1, [Structure("exponential", 1.0, 150.0)])
     c = uniform_points(15000, 2, 621, [1000.0, 1000.0])
-    v = 5.0 + G.rff_field(c, m, 512, 3)
+    v = 5.0 + W.rff_field(c, m, 512, 3)
     k = G.Kriging.new(G.PointSet(c, v), m, G.KrigingConfig(max_per_octant=10))
     t = np.random.default_rng(3).uniform(0, 1000, size=(3000, 2))
     x, y = _cols(t)

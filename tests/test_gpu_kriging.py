@@ -9,6 +9,7 @@ import pytest
 
 import pyoracle as O
 import geostat_rs as G
+import gs_workload as W
 from geostat_rs.model import Anisotropy, Structure, VariogramModel
 from gpu_common import (assert_close, sph200_model, rotated_3d_model, clustered_matern_model, clustered_points,
                         max_rel, smooth_values, uniform_points)
@@ -65,6 +66,59 @@ def test_knn_neighbour_sets_bit_exact(dim, n, k):
     assert (idx == ref["neighbors"]).all()
 
 
+def _brute_d2(c, t):
+    """Squared distances in the reference's operation order
+    (((0 + dx0^2) + dx1^2) [+ dx2^2]), no fused multiply-adds."""
+    d2 = np.zeros((len(t), len(c)))
+    for d in range(c.shape[1]):
+        dx = t[:, d:d + 1] - c[None, :, d]
+        d2 = d2 + dx * dx
+    return d2
+
+
+def test_lattice_data_boundary_ties():
+    """Lattice data points and lattice-aligned targets, where the k-th and
+    (k+1)-th candidates often tie exactly.  The reference keeps, among
+    candidates tied at the k-th distance, the first its kd-tree traversal met
+    (search.rs:15-21 strict <; the traversal order comes from
+    select_nth_unstable_by in build_rec, search.rs:102-113); the device
+    search keeps the smaller indices.  Away from such ties the sets must be
+    identical; at a tie both sets must hold the same squared distances, and
+    the device's set must be the (squared distance, index) smallest.  The
+    number of tie targets and of targets where the two rules pick different
+    points is printed (and recorded in the design notes)."""
+    g = np.arange(60) * 10.0
+    yy, xx = np.meshgrid(g, g, indexing="ij")
+    c = np.stack([xx.ravel(), yy.ravel()], 1)
+    v = smooth_values(c)
+    k = 16
+    q = np.arange(40) * 14.5 + 5.0
+    ty, tx = np.meshgrid(q, q, indexing="ij")
+    t = np.concatenate([np.stack([tx.ravel(), ty.ravel()], 1),
+                        uniform_points(400, 2, 321, [590.0, 590.0])])
+    ref = O.krige(c, v, sph200_model(), t, max_neighbors=k, kcap=k)
+    kr = G.Kriging.new(G.PointSet(c, v), sph200_model(), G.KrigingConfig(max_neighbors=k))
+    idx, cnt = kr.neighbors(t, k)
+    assert (cnt == k).all() and (ref["nb_count"] == k).all()
+    d2 = _brute_d2(c, t)
+    order = np.lexsort((np.broadcast_to(np.arange(len(c)), d2.shape), d2), axis=1)
+    srt = np.take_along_axis(d2, order, axis=1)
+    tie = srt[:, k - 1] == srt[:, k]
+    assert tie.sum() > 100  # the lattice makes boundary ties routine
+    assert (idx[~tie] == ref["neighbors"][~tie]).all()
+    assert (idx == order[:, :k]).all()  # device: (squared distance, index) order
+    gd = np.take_along_axis(d2, idx.astype(np.int64), axis=1)
+    od = np.take_along_axis(d2, ref["neighbors"].astype(np.int64), axis=1)
+    assert (gd == od).all()  # the same distance classes at every target
+    differ = (idx != ref["neighbors"]).any(axis=1)
+    print(f"lattice k={k}: {len(t)} targets, {int(tie.sum())} with a boundary tie, "
+          f"{int(differ.sum())} where the traversal-order rule keeps other points")
+    ok = ~differ & (ref["status"] == 0)
+    out = kr.predict_many(t, "mixed", full=True)
+    assert_close(out.value[ok], ref["value"][ok], float(np.mean(np.abs(v))), 1e-9, "lattice value")
+    assert_close(out.variance[ok], ref["variance"][ok], 1e-3, 1e-9, "lattice variance")
+
+
 def test_radius_and_octant_neighbour_sets_bit_exact():
     c = clustered_points(20000, 3, extent=10000.0, nblobs=40)
     v = smooth_values(c)
@@ -110,7 +164,7 @@ def test_config1_ordinary_kriging_full_size():
     """2-D OK: n=2000 in [0,1000]^2, nugget 0.1 + Sph(1, 200), 100x100 grid, n_max=32."""
     c = uniform_points(2000, 2, 2024, [1000.0, 1000.0])
     m = sph200_model()
-    v = 10.0 + G.rff_field(c, VariogramModel(0.1, [Structure("exponential", 1.0, 200.0 / 3)]),
+    v = 10.0 + W.rff_field(c, VariogramModel(0.1, [Structure("exponential", 1.0, 200.0 / 3)]),
                            2048, 11)
     t = O.grid_centers([0, 0], [1000, 1000], [100, 100])
     k, ref, outs = run_both(c, v, m, t, dict(max_neighbors=32))
@@ -136,7 +190,7 @@ def test_config2_shape_3d_nested_rotated():
     """3-D OK with nugget + rotated Sph(300/150/40, az 30, dip 10) + Exp(800), n_max=64."""
     c = uniform_points(20000, 3, 5, [2000.0, 2000.0, 200.0])
     m = rotated_3d_model()
-    v = G.rff_field(c, m, 1024, 3)
+    v = W.rff_field(c, m, 1024, 3)
     t = uniform_points(3000, 3, 6, [2000.0, 2000.0, 200.0])
     _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64))
     for prec, out in outs.items():
@@ -199,7 +253,7 @@ def test_octant_uneven_systems_clustered():
     """Octant search on clustered data: systems of 4..64 neighbours in one launch."""
     c = clustered_points(30000, 9, extent=10000.0, nblobs=60)
     m = clustered_matern_model()
-    v = G.rff_field(c, m, 512, 4)
+    v = W.rff_field(c, m, 512, 4)
     t = uniform_points(1500, 2, 10, [10000.0, 10000.0])
     _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64, max_per_octant=16,
                                              min_neighbors=4))
@@ -310,7 +364,7 @@ def test_grid_targets_reuse_shared_neighbours(case):
     c = uniform_points(6000, 2, 404, [1000.0, 1000.0])
     m = VariogramModel(0.05, [Structure.with_anisotropy("spherical", 0.7, 150.0, 30.0, 0.5),
                               Structure("exponential", 0.25, 400.0)])
-    v = 10.0 + G.rff_field(c, m, 1024, 12)
+    v = 10.0 + W.rff_field(c, m, 1024, 12)
     t = O.grid_centers([100, 100], [900, 900], [120, 40])
     k, ref, outs = run_both(c, v, m, t, case, precisions=("mixed",))
     check(ref, outs["mixed"], v, m.total_sill())
@@ -319,7 +373,7 @@ def test_grid_targets_reuse_shared_neighbours(case):
 def test_grid_targets_reuse_3d_and_external_drift():
     c = uniform_points(8000, 3, 405, [600.0, 600.0, 60.0])
     m = rotated_3d_model()
-    v = G.rff_field(c, m, 1024, 13)
+    v = W.rff_field(c, m, 1024, 13)
     t = O.grid_centers([50, 50, 5], [550, 550, 55], [64, 8, 4])
     k, ref, outs = run_both(c, v, m, t, dict(max_neighbors=64), precisions=("mixed",))
     check(ref, outs["mixed"], v, m.total_sill())

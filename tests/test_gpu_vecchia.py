@@ -4,6 +4,7 @@ import pytest
 
 import pyoracle as O
 import geostat_rs as G
+import gs_workload as W
 from geostat_rs.model import Structure, VariogramModel
 from gpu_common import assert_close, uniform_points
 
@@ -40,7 +41,7 @@ def test_plan_with_given_order():
 
 def test_loglik_batch_matches_oracle_and_is_batch_invariant():
     c = uniform_points(20000, 2, 3, [1.0, 1.0])
-    v = 0.5 + G.rff_field(c, matern25(), 1024, 5)
+    v = 0.5 + W.rff_field(c, matern25(), 1024, 5)
     ps = G.PointSet(c, v)
     plan = G.VecchiaPlan(ps, 30)
     order, nb, cnt = plan.arrays()
@@ -178,7 +179,7 @@ def test_vecchia_predict_deterministic_and_edge_cases():
 def test_loglik_gradient_matches_oracle(kind):
     """loglik_grad_with_plan (vecchia.rs:416-530) for a batch of candidates."""
     c = uniform_points(6000, 2, 31, [1.0, 1.0])
-    v = 0.5 + G.rff_field(c, matern25(), 1024, 7)
+    v = 0.5 + W.rff_field(c, matern25(), 1024, 7)
     plan = G.VecchiaPlan(G.PointSet(c, v), 20)
     order, nb, cnt = plan.arrays()
     cands = [VariogramModel(0.02, [Structure(kind, 1.0, 0.08)]),

@@ -10,6 +10,7 @@ import pytest
 
 import pyoracle as O
 import geostat_rs as G
+import gs_workload as W
 from geostat_rs.model import Structure, VariogramModel
 from gpu_common import uniform_points
 
@@ -25,7 +26,7 @@ def _models():
 @pytest.mark.parametrize("dim,m,g", [(2, 15, 2), (2, 30, 4), (2, 10, 8), (3, 20, 4)])
 def test_grouped_loglik_matches_oracle(dim, m, g):
     c = uniform_points(3000, dim, 101 + dim, [1.0] * dim)
-    v = 0.5 + G.rff_field(c, _models()[1], 512, 102)
+    v = 0.5 + W.rff_field(c, _models()[1], 512, 102)
     plan = G.VecchiaPlan(G.PointSet(c, v), m)
     order, nb, cnt = plan.arrays()
     ll, st = plan.loglik_grouped(_models(), g)

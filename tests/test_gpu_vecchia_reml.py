@@ -13,6 +13,7 @@ import pytest
 
 import pyoracle as O
 import geostat_rs as G
+import gs_workload as W
 from geostat_rs.model import Structure, VariogramModel
 from gpu_common import uniform_points
 
@@ -29,7 +30,7 @@ def _models():
 def field(request):
     dim = request.param
     c = uniform_points(3000, dim, 201 + dim, [1.0] * dim)
-    v = 2.0 + 3.0 * c[:, 0] - c[:, 1] + G.rff_field(c, _models()[1], 512, 202)
+    v = 2.0 + 3.0 * c[:, 0] - c[:, 1] + W.rff_field(c, _models()[1], 512, 202)
     return c, v
 
 
@@ -159,7 +160,7 @@ def test_reml_large_sets_and_sorted_order_blocks():
     point) and a coordinate-sorted order, whose consecutive points share
     neighbours so that Guinness blocks have many members."""
     c = uniform_points(2500, 2, 211, [1.0, 1.0])
-    v = 1.0 + 2.0 * c[:, 1] + G.rff_field(c, _models()[0], 512, 212)
+    v = 1.0 + 2.0 * c[:, 1] + W.rff_field(c, _models()[0], 512, 212)
     plan = G.VecchiaPlan(G.PointSet(c, v), 40)
     order, nb, cnt = plan.arrays()
     ll, st = plan.reml_loglik(_models(), drift_degree=1)

@@ -66,7 +66,7 @@ def test_abi_version_and_struct_layout(tmp_path):
     """The ctypes structs match the C header's layout (compiled with gcc)."""
     import ctypes as C
     import subprocess
-    assert _abi.load().gs_abi_version() == 1
+    assert _abi.load().gs_abi_version() == 2
     src = tmp_path / "layout.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "geostat_gb300.h"\n'
