@@ -360,47 +360,51 @@ __device__ __forceinline__ df rho_mat25_df(df d, const ExpTable& tab, const ExpC
 }
 
 // rho(d) in df for d >= 0.
-__device__ __forceinline__ df rho_df(int kind, df d, const ExpTable& tab, const ExpConsts& k) {
-  switch (kind) {
-    case GS_KIND_SPHERICAL:
-      return rho_sph_df(d);
-    case GS_KIND_EXPONENTIAL:
-      return df_expneg(d, tab, k);
-    case GS_KIND_GAUSSIAN:
-      return df_expneg(df_sqr(d), tab, k);
-    case GS_KIND_MATERN15:
-      return rho_mat15_df(d, tab, k);
-    default:  // GS_KIND_MATERN25
-      return rho_mat25_df(d, tab, k);
+// Argument of the exponential of kind `kind` at d = h / range (Exponential:
+// d, Gaussian: d^2, Matern 3/2: sqrt(3) d, Matern 5/2: sqrt(5) d), and the
+// factor that multiplies it (1, 1, 1 + s, 1 + s + s^2/3); Spherical has no
+// exponential.  Splitting each kind this way gives one copy of df_expneg per
+// call site instead of one per kind, with the same operations per kind as
+// rho_mat15_df / rho_mat25_df.
+__device__ __forceinline__ df exp_arg_df(int kind, df d, const ExpConsts& k) {
+  if (kind == GS_KIND_GAUSSIAN) return df_sqr(d);
+  if (kind == GS_KIND_MATERN15) return df_mul(d, df_make(k.s3h, k.s3l));
+  if (kind == GS_KIND_MATERN25) return df_mul(d, df_make(k.s5h, k.s5l));
+  return d;
+}
+__device__ __forceinline__ df exp_factor_df(int kind, df s, df e) {
+  if (kind == GS_KIND_MATERN15) return df_mul(df_add_f(s, 1.0f), e);
+  if (kind == GS_KIND_MATERN25) {
+    const df s2 = df_sqr(s);
+    // 1 + s + s^2/3: s^2/3 as df via FP32 reciprocal correction
+    const float q = s2.hi * (1.0f / 3.0f);
+    const df q3 = two_prod(q, 3.0f);
+    const float rq = (s2.hi - q3.hi - q3.lo + s2.lo) * (1.0f / 3.0f);
+    const df third = fast_two_sum(q, rq);
+    const df p = df_add(df_add_f(s, 1.0f), third);
+    return df_mul(p, e);
   }
+  return e;
 }
 
-// rho at two arguments under one (uniform) branch on the kind: the two
-// evaluations are independent and interleave.
+__device__ __forceinline__ df rho_df(int kind, df d, const ExpTable& tab, const ExpConsts& k) {
+  if (kind == GS_KIND_SPHERICAL) return rho_sph_df(d);
+  const df s = exp_arg_df(kind, d, k);
+  return exp_factor_df(kind, s, df_expneg(s, tab, k));
+}
+
+// rho_df at two arguments side by side (one kind).
 __device__ __forceinline__ void rho_df2(int kind, df d0, df d1, const ExpTable& tab,
                                         const ExpConsts& k, df& r0, df& r1) {
-  switch (kind) {
-    case GS_KIND_SPHERICAL:
-      r0 = rho_sph_df(d0);
-      r1 = rho_sph_df(d1);
-      break;
-    case GS_KIND_EXPONENTIAL:
-      r0 = df_expneg(d0, tab, k);
-      r1 = df_expneg(d1, tab, k);
-      break;
-    case GS_KIND_GAUSSIAN:
-      r0 = df_expneg(df_sqr(d0), tab, k);
-      r1 = df_expneg(df_sqr(d1), tab, k);
-      break;
-    case GS_KIND_MATERN15:
-      r0 = rho_mat15_df(d0, tab, k);
-      r1 = rho_mat15_df(d1, tab, k);
-      break;
-    default:
-      r0 = rho_mat25_df(d0, tab, k);
-      r1 = rho_mat25_df(d1, tab, k);
-      break;
+  if (kind == GS_KIND_SPHERICAL) {
+    r0 = rho_sph_df(d0);
+    r1 = rho_sph_df(d1);
+    return;
   }
+  const df s0 = exp_arg_df(kind, d0, k), s1 = exp_arg_df(kind, d1, k);
+  const df e0 = df_expneg(s0, tab, k), e1 = df_expneg(s1, tab, k);
+  r0 = exp_factor_df(kind, s0, e0);
+  r1 = exp_factor_df(kind, s1, e1);
 }
 
 // 1/d to FP64 accuracy: FP32 estimate, two Newton steps (e = 1 - d r,

@@ -343,9 +343,12 @@ constexpr int kVWarps = 4;  // warps (ordered points in flight) per block
 
 // One warp per ordered point for conditioning sets of at most 32 points: the
 // same assembly and certification as vecchia_loglik_kernel, with the
-// register-row solver of gs_warp.cuh (no block barriers).
+// register-row solver of gs_warp.cuh (no block barriers).  The likelihood
+// form is compiled for four blocks (16 warps) per SM: it fits 128 registers
+// per thread without spills; the REML form would spill and keeps the default.
 template <int D, bool REML>
-__global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, ExpTable tab_g,
+__global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
+    vecchia_warp_kernel(VArgs a, ExpTable tab_g,
                                                                    DfConsts kc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
@@ -462,8 +465,19 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
         });
       }
       __syncwarp();
-      const bool ok = warp_solve(A, B, s, lane, W);
-      if (!ok) {
+      // the likelihood accepts a refinement stalled at the double-float
+      // noise floor when its first-order error on the log term is small
+      // (REML keeps the strict test: its records feed further sums)
+      int outcome = kRefineFailed;
+      float dl = 0.0f;
+      {
+        WarpFactor fct;
+        if (warp_factor(A, s, lane, fct, W)) {
+          if (REML) outcome = warp_refine(fct, B, s, lane, W) ? kRefineConverged : kRefineFailed;
+          else outcome = warp_refine_floor(fct, B, s, lane, W, &dl);
+        }
+      }
+      if (outcome == kRefineFailed) {
         if (lane == 0) LT[LW * (c & 31)] = -1.0;
       } else {
         df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
@@ -473,9 +487,33 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_warp_kernel(VArgs a, Exp
         }
         mu = warp_sum_df(mu);
         red = warp_sum_df(red);
+        // bounds on the errors of k.w and z_S.w left by the last correction
+        float ek = 0.0f, ez = 0.0f;
+        if (outcome == kRefineAtFloor) {
+          if (lane < s) {
+            ek = fabsf(B[lane].hi) * fabsf(dl);
+            ez = fabsf(ZV[lane].hi) * fabsf(dl);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            ek += __shfl_xor_sync(0xffffffffu, ek, o);
+            ez += __shfl_xor_sync(0xffffffffu, ez, o);
+          }
+        }
         if (lane == 0) {
-          LT[LW * (c & 31)] = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
-          LT[LW * (c & 31) + 1] = df_to_double(df_sub(zi, mu));
+          const double var = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
+          const double r = df_to_double(df_sub(zi, mu));
+          bool accept = true;
+          if (outcome == kRefineAtFloor) {
+            // first-order error of -0.5 (ln var + r^2 / var) from errors
+            // ek in var and ez in r, against 1e-10 of max(|term|, 1)
+            const double q = r * r / var;
+            const double term = -0.5 * (kLn2Pi + log(var) + q);
+            const double est = 0.5 * (double)ek / var * fabs(1.0 - q) + fabs(r) * (double)ez / var;
+            accept = est <= 1e-10 * fmax(fabs(term), 1.0);
+          }
+          LT[LW * (c & 31)] = accept ? var : -1.0;
+          LT[LW * (c & 31) + 1] = r;
         }
         if (REML) {
           // the basis rows' residuals f_i - w . f_S
@@ -3154,34 +3192,16 @@ int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int6
     delete P;
     return fail(GS_ERR_INVALID_PARAMETER, "at least one start is required");
   }
-  std::vector<NelderMead> runs;
-  for (auto& x0 : st) runs.emplace_back(x0, step, max_iter);
-  int64_t evals = 0;
-  int rc = GS_OK;
-  for (int guard = 0; guard < 1000000 && !rc; ++guard) {
-    std::vector<std::vector<double>> xs;
-    std::vector<size_t> owner;
-    for (size_t r = 0; r < runs.size(); ++r) {
-      if (runs[r].done()) continue;
-      for (const auto& x : runs[r].pending()) {
-        xs.push_back(x);
-        owner.push_back(r);
-      }
-    }
-    if (xs.empty()) break;
-    std::vector<double> fv;
-    rc = batch_objective(P, kind, fs.range_max, xs, fv);
-    if (rc) break;
-    evals += (int64_t)xs.size();
-    std::vector<std::vector<double>> fvals(runs.size());
-    for (size_t b = 0; b < xs.size(); ++b) fvals[owner[b]].push_back(fv[b]);
-    for (size_t r = 0; r < runs.size(); ++r)
-      if (!fvals[r].empty()) runs[r].supply(fvals[r]);
-  }
+  std::pair<std::vector<double>, double> best;
+  const int rc = nm_lockstep(
+      st, step, max_iter,
+      [&](const std::vector<std::vector<double>>& xs, std::vector<double>& fv) {
+        return batch_objective(P, kind, fs.range_max, xs, fv);
+      },
+      &best, n_evals);
   delete P;
   if (rc) return rc;
-  if (n_evals) *n_evals = evals;
-  return finish_fit(kind, multistart_best(runs), out_model, out_loglik, out_x);
+  return finish_fit(kind, best, out_model, out_loglik, out_x);
 }
 
 // vecchia_mle_grouped (vecchia.rs:939-950): group_size <= 1 is vecchia_mle.

@@ -26,7 +26,7 @@ def _check(k, c, v, m, t, okw, tdrift=None, errors=None, drift=None):
         assert_close(out.variance, ref["variance"], 1e-3 * m.total_sill(), 1e-9, "variance")
         ok = ref["status"] == 0
         if okw.get("method", "ordinary") != "simple":
-            assert_close(out.lagrange[ok], ref["lagrange"][ok], 1.0, 1e-7, "lagrange")
+            assert_close(out.lagrange[ok], ref["lagrange"][ok], 1.0, 1e-9, "lagrange")
 
 
 @pytest.mark.parametrize("method", ["ordinary", "simple", "universal"])

@@ -197,20 +197,62 @@ def test_config2_shape_3d_nested_rotated():
         check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
 
 
+def _ok_condition(c, model, nb, cnt):
+    """2-norm condition number of each target's ordinary-kriging matrix
+    [C 1; 1^T 0] (kriging.rs:527-567) over its neighbours, from the oracle's
+    gamma_dh."""
+    c0 = model.total_sill()
+    out = np.empty(len(cnt))
+    for t in range(len(cnt)):
+        ids = nb[t, :cnt[t]]
+        n = len(ids)
+        a = np.zeros((n + 1, n + 1))
+        for i in range(n):
+            for j in range(i, n):
+                g = O.gamma_dh(model, c[ids[i]] - c[ids[j]])
+                a[i, j] = a[j, i] = c0 - g
+        a[:n, n] = a[n, :n] = 1.0
+        out[t] = np.linalg.cond(a)
+    return out
+
+
 def test_ill_conditioned_gaussian_goes_to_fp64():
-    """Gaussian without nugget: cond(A) ~ 1e10+, beyond FP32 factorisation.  The
-    mixed kernel must hand such systems to the FP64 solver (status bit 0x40)
-    and then agree with the oracle as far as the conditioning allows."""
+    """Gaussian without nugget: cond(A) ~ 1e10 and beyond, out of reach of an
+    FP32 factorisation.  The mixed kernel must hand such systems to the FP64
+    tiers (status bit 0x40, statuses otherwise exact).  Two backward-stable
+    FP64 solvers of the same system (the bordered LDL^T tier and the plain
+    FP64 build's partial-pivoting LU) agree only to about cond(A) * 2^-53, and
+    so do the FP64 build and the oracle (their exp differs in the last bit);
+    the test therefore compares the mixed path with the FP64 build per target
+    within max(1e-9, 8 cond(A) 2^-53) relative, and the FP64 build with the
+    oracle within the same bound.  Measured on a GB300: mixed vs FP64 build
+    2.3e-7 (values), 8e-11 (variances); FP64 build vs oracle 3.9e-7."""
     c = uniform_points(600, 2, 33, [100.0, 100.0])
     v = smooth_values(c)
     m = VariogramModel(0.0, [Structure("gaussian", 1.0, 25.0)])
     t = uniform_points(200, 2, 34, [100.0, 100.0])
-    _, ref, outs = run_both(c, v, m, t, dict(max_neighbors=16))
-    out = outs["mixed"]
-    assert ((out.status & 0x40) != 0).sum() > 0
+    k, ref, outs = run_both(c, v, m, t, dict(max_neighbors=16))
+    out, f64 = outs["mixed"], outs["fp64"]
+    routed = (out.status & 0x40) != 0
+    assert routed.sum() > 0
+    assert ((out.status & 0x3f) == (f64.status & 0x3f)).all()
+    assert ((out.status & 0x3f) == ref["status"].astype(np.uint8)).all()
     ok = ref["status"] == 0
-    assert ((out.status & 0x3f)[ok] == 0).all()
-    assert max_rel(out.value[ok], ref["value"][ok], 10.0) < 1e-4
+    nb, cnt = k.neighbors(t, 16)
+    cond = _ok_condition(c, m, nb, cnt)
+    assert np.median(cond[routed]) > 1e8  # the routed systems are the ill-conditioned ones
+    bound = np.maximum(1e-9, 8.0 * cond * 2.0 ** -53)
+    vs = float(np.mean(np.abs(v)))
+    for name, a, b, floor in (("value", out.value, f64.value, vs),
+                              ("variance", out.variance, f64.variance, 1e-3),
+                              ("value vs oracle", f64.value, ref["value"], vs),
+                              ("variance vs oracle", f64.variance, ref["variance"], 1e-3)):
+        rel = np.abs(a - b)[ok] / np.maximum(np.abs(b), floor)[ok]
+        assert (rel <= bound[ok]).all(), f"{name}: worst {np.max(rel / bound[ok]):.2f} x bound"
+    # well-conditioned targets (none routed) meet the 1e-9 bar outright
+    well = ok & (cond < 1e6)
+    if well.any():
+        assert_close(out.value[well], f64.value[well], vs, 1e-9, "well-conditioned value")
 
 
 @pytest.mark.parametrize("method,deg", [("simple", 1), ("universal", 1), ("universal", 2)])
@@ -229,7 +271,7 @@ def test_methods_2d_and_3d(method, deg):
         for prec, out in outs.items():
             check(ref, out, v, m.total_sill(), 1e-9 if prec == "mixed" else 1e-10)
         if method != "simple":
-            assert_close(outs["mixed"].lagrange, ref["lagrange"], 1.0, 1e-8, "lagrange")
+            assert_close(outs["mixed"].lagrange, ref["lagrange"], 1.0, 1e-9, "lagrange")
 
 
 def test_external_drift_and_measurement_error():
