@@ -465,19 +465,8 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
         });
       }
       __syncwarp();
-      // the likelihood accepts a refinement stalled at the double-float
-      // noise floor when its first-order error on the log term is small
-      // (REML keeps the strict test: its records feed further sums)
-      int outcome = kRefineFailed;
-      float dl = 0.0f;
-      {
-        WarpFactor fct;
-        if (warp_factor(A, s, lane, fct, W)) {
-          if (REML) outcome = warp_refine(fct, B, s, lane, W) ? kRefineConverged : kRefineFailed;
-          else outcome = warp_refine_floor(fct, B, s, lane, W, &dl);
-        }
-      }
-      if (outcome == kRefineFailed) {
+      const bool ok = warp_solve(A, B, s, lane, W);
+      if (!ok) {
         if (lane == 0) LT[LW * (c & 31)] = -1.0;
       } else {
         df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
@@ -487,33 +476,9 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
         }
         mu = warp_sum_df(mu);
         red = warp_sum_df(red);
-        // bounds on the errors of k.w and z_S.w left by the last correction
-        float ek = 0.0f, ez = 0.0f;
-        if (outcome == kRefineAtFloor) {
-          if (lane < s) {
-            ek = fabsf(B[lane].hi) * fabsf(dl);
-            ez = fabsf(ZV[lane].hi) * fabsf(dl);
-          }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            ek += __shfl_xor_sync(0xffffffffu, ek, o);
-            ez += __shfl_xor_sync(0xffffffffu, ez, o);
-          }
-        }
         if (lane == 0) {
-          const double var = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
-          const double r = df_to_double(df_sub(zi, mu));
-          bool accept = true;
-          if (outcome == kRefineAtFloor) {
-            // first-order error of -0.5 (ln var + r^2 / var) from errors
-            // ek in var and ez in r, against 1e-10 of max(|term|, 1)
-            const double q = r * r / var;
-            const double term = -0.5 * (kLn2Pi + log(var) + q);
-            const double est = 0.5 * (double)ek / var * fabs(1.0 - q) + fabs(r) * (double)ez / var;
-            accept = est <= 1e-10 * fmax(fabs(term), 1.0);
-          }
-          LT[LW * (c & 31)] = accept ? var : -1.0;
-          LT[LW * (c & 31) + 1] = r;
+          LT[LW * (c & 31)] = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
+          LT[LW * (c & 31) + 1] = df_to_double(df_sub(zi, mu));
         }
         if (REML) {
           // the basis rows' residuals f_i - w . f_S

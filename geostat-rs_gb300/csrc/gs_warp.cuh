@@ -178,76 +178,6 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
   return false;
 }
 
-// Outcomes of warp_refine_floor.
-constexpr int kRefineConverged = 0;  // as warp_refine's success
-constexpr int kRefineAtFloor = 1;    // stalled at the double-float residual's noise floor
-constexpr int kRefineFailed = 2;     // the FP32 inverse does not contract the error
-
-// warp_refine, but a refinement that stops contracting after its corrections
-// have fallen below 1e-8 of |x| is reported as kRefineAtFloor instead of a
-// failure: the residual b - A x is then limited by the double-float entries
-// of A (about 2^-46 of each entry), not by the FP32 inverse, and more sweeps
-// cannot improve x.  In that case W.xd holds the last iterate (the last
-// correction added) and *dlast this lane's last correction, a first-order
-// estimate of x's remaining error that the caller turns into an error bound
-// on the quantities it needs.
-__device__ __forceinline__ int warp_refine_floor(const WarpFactor& f, const df* B, int N, int lane,
-                                                 const WarpScratch& W, float* dlast) {
-  __syncwarp();
-  W.vec[lane] = lane < N ? B[lane].hi : 0.0f;
-  __syncwarp();
-  float y;
-  warp_gemv_neg_inv(f.t, W.vec, lane, y);
-  y *= f.sc;
-  df x = df_make(lane < N ? -y : 0.0f, 0.0f);
-  const float nx = warp_max_f(fabsf(x.hi));
-  float nd_prev = nx;
-  *dlast = 0.0f;
-  for (int sweep = 1; sweep <= kMaxRefineSweeps; ++sweep) {
-    __syncwarp();
-    W.xd[lane] = x;
-    __syncwarp();
-    float s = lane < N ? B[lane].hi : 0.0f, c = lane < N ? B[lane].lo : 0.0f;
-#pragma unroll
-    for (int j = 0; j < kWarpN; ++j) {
-      const df xj = W.xd[j];
-      const float ph = __fmul_rn(-f.ah[j], xj.hi);
-      float pe = __fmaf_rn(-f.ah[j], xj.hi, -ph);
-      pe = __fmaf_rn(-f.ah[j], xj.lo, pe);
-      pe = __fmaf_rn(-f.al[j], xj.hi, pe);
-      const float tsum = __fadd_rn(s, ph);
-      const float bb = __fsub_rn(tsum, s);
-      const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
-      s = tsum;
-      c += e + pe;
-    }
-    const float r = lane < N ? s + c : 0.0f;
-    __syncwarp();
-    W.vec[lane] = r;
-    __syncwarp();
-    warp_gemv_neg_inv(f.t, W.vec, lane, y);
-    y *= f.sc;
-    if (lane < N) x = df_add_f(x, -y);
-    const float nd = warp_max_f(lane < N ? fabsf(y) : 0.0f);
-    bool done = nd <= 1e-15f * nx;
-    if (!done && sweep >= 2) {
-      const float rho = nd / nd_prev;
-      done = rho < 0.5f && rho * nd <= 1e-13f * nx;
-    }
-    const bool stalled = !done && sweep >= 2 && !(nd < 0.5f * nd_prev);
-    if (done || stalled || sweep == kMaxRefineSweeps) {
-      __syncwarp();
-      W.xd[lane] = x;
-      __syncwarp();
-      if (done) return kRefineConverged;
-      *dlast = lane < N ? y : 0.0f;
-      return nd <= 1e-8f * nx ? kRefineAtFloor : kRefineFailed;
-    }
-    nd_prev = nd;
-  }
-  return kRefineFailed;
-}
-
 // Factor and solve one right-hand side.
 __device__ __forceinline__ bool warp_solve(const df* A, const df* B, int N, int lane,
                                            const WarpScratch& W) {
