@@ -755,13 +755,14 @@ def clustered_bench(args, log):
                              tdrift_ptr=tdr[lo:].data_ptr() if b == 2 else None)
             if rep == 1:
                 ph = G.last_timings()
-                run, bins, src = k.tiles(hi - lo)
+                run, bins, spc, src = k.tiles(hi - lo)
                 kinds[CL_KINDS[b]] = {
                     "targets": hi - lo, "search_ms": ph[0], "mixed_ms": ph[1],
                     "fp64_resolve_ms": ph[2], "total_ms": ph[3],
                     "fp64_resolved": int(lib.gs_last_fallbacks()),
                     "lu_resolved": int(lib.gs_last_lu_resolves()),
-                    "tiles": {"run": run, "bins": bins, "source": src}}
+                    "tiles": {"run": run, "bins": bins, "systems_per_block": spc,
+                              "source": src}}
     torch.cuda.synchronize()
     l0 = lib.gs_launch_count()
     g = torch.cuda.CUDAGraph()

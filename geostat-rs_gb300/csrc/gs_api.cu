@@ -845,6 +845,7 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
         sa.out_st += b0;
         sa.ntl = count;
         sa.run = t.run;
+        sa.spc = t.spc;
         sa.route_fp64 = route;
         uint8_t* fl = (uint8_t*)flag.ptr + b0;
         if (!(binned && t.bins)) return krige_mixed_launch(sa, k->dm, fl, 0, stream);
@@ -864,36 +865,52 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
         return krige_mixed_launch(sa, k->dm, fl, 64, stream);
       };
       if (tune_now && ci == 0) {
-        // autotuner: every candidate once untimed (module loading), then
-        // timed on the same sample; the fastest shape serves this size class
+        // autotuner over run length, warps per system (binning) and systems
+        // per block: candidates are run once untimed (module loading), then
+        // timed on the same sample.  Stage 1 times every run length and
+        // binning at one system per block, stage 2 the winner at two systems
+        // per block; the fastest shape serves this size class.
         const int64_t ns = std::min(cn, kTuneSample);
-        std::vector<Tiles> cand;
-        for (int run : {16, 32, 64, 128})
-          for (int bn = 0; bn <= (binned ? 1 : 0); ++bn) cand.push_back(Tiles{run, bn});
-        std::vector<cudaEvent_t> te(cand.size() + 1);
-        for (auto& e : te) GS_CUDA(cudaEventCreate(&e));
-        for (int pass = 0; pass < 2 && !rc; ++pass) {
-          for (size_t c = 0; c < cand.size() && !rc; ++c) {
-            if (pass == 1 && c == 0) GS_CUDA(cudaEventRecord(te[0], stream));
-            rc = solve_mixed(0, ns, cand[c], nullptr);
-            if (pass == 1) GS_CUDA(cudaEventRecord(te[c + 1], stream));
-          }
-        }
-        if (!rc) {
-          GS_CUDA(cudaEventSynchronize(te.back()));
-          float best = 0;
-          for (size_t c = 0; c < cand.size(); ++c) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, te[c], te[c + 1]);
-            if (c == 0 || ms < best) {
-              best = ms;
-              tiles = cand[c];
+        auto time_shapes = [&](const std::vector<Tiles>& cand, std::vector<float>& ms) -> int {
+          std::vector<cudaEvent_t> te(cand.size() + 1);
+          for (auto& e : te) GS_CUDA(cudaEventCreate(&e));
+          int r = GS_OK;
+          for (int pass = 0; pass < 2 && !r; ++pass) {
+            for (size_t c = 0; c < cand.size() && !r; ++c) {
+              if (pass == 1 && c == 0 && cudaEventRecord(te[0], stream) != cudaSuccess)
+                r = fail(GS_ERR_CUDA, "event record failed");
+              if (!r) r = solve_mixed(0, ns, cand[c], nullptr);
+              if (!r && pass == 1 && cudaEventRecord(te[c + 1], stream) != cudaSuccess)
+                r = fail(GS_ERR_CUDA, "event record failed");
             }
           }
+          if (!r && cudaEventSynchronize(te.back()) != cudaSuccess)
+            r = fail(GS_ERR_CUDA, "event synchronisation failed");
+          ms.assign(cand.size(), 0.0f);
+          if (!r)
+            for (size_t c = 0; c < cand.size(); ++c) cudaEventElapsedTime(&ms[c], te[c], te[c + 1]);
+          for (auto& e : te) cudaEventDestroy(e);
+          return r;
+        };
+        std::vector<Tiles> cand;
+        for (int run : {16, 32, 64, 128})
+          for (int bn = 0; bn <= (binned ? 1 : 0); ++bn) cand.push_back(Tiles{run, bn, 1});
+        std::vector<float> ms;
+        rc = time_shapes(cand, ms);
+        if (!rc) {
+          size_t best = 0;
+          for (size_t c = 1; c < cand.size(); ++c)
+            if (ms[c] < ms[best]) best = c;
+          tiles = cand[best];
+          std::vector<float> ms2;
+          const std::vector<Tiles> cand2{Tiles{tiles.run, tiles.bins, 2}};
+          rc = time_shapes(cand2, ms2);
+          if (!rc && ms2[0] < ms[best]) tiles = cand2[0];
+        }
+        if (!rc) {
           std::lock_guard<std::mutex> lk(k->tiles_mu);
           k->tiles[size_class(nt)] = tiles;
         }
-        for (auto& e : te) cudaEventDestroy(e);
         if (rc) break;
       }
       // the first kRouteSample targets decide (on the device) whether the
@@ -1019,13 +1036,15 @@ int gs_kriging_predict_many_device(const gs_kriging* k, int64_t nt, const double
   return predict_device(k, nt, tx, ty, tz, tdrift, value, variance, lagrange, status, precision, s);
 }
 
-int gs_kriging_set_tiles(gs_kriging* k, int run, int bins) {
+int gs_kriging_set_tiles(gs_kriging* k, int run, int bins, int systems_per_block) {
   if (!k) return fail(GS_ERR_INVALID_PARAMETER, "null predictor");
   if (run != 0 && (run < 1 || run > 1024 || (run & (run - 1))))
     return fail(GS_ERR_INVALID_PARAMETER, "run must be 0 or a power of two in [1, 1024]");
   if (bins != 0 && bins != 1) return fail(GS_ERR_INVALID_PARAMETER, "bins must be 0 or 1");
+  if (systems_per_block != 1 && systems_per_block != 2)
+    return fail(GS_ERR_INVALID_PARAMETER, "systems per block must be 1 or 2");
   std::lock_guard<std::mutex> lk(k->tiles_mu);
-  k->pinned = gs::Tiles{run, bins};
+  k->pinned = gs::Tiles{run, bins, systems_per_block};
   return GS_OK;
 }
 
@@ -1159,8 +1178,10 @@ static int cv_with_labels(const gs_kriging* k, const std::vector<int32_t>& label
 
 extern "C" {
 
-int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins, int* tuned) {
-  if (!k || !run || !bins || !tuned) return fail(GS_ERR_INVALID_PARAMETER, "null argument");
+int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins,
+                     int* systems_per_block, int* tuned) {
+  if (!k || !run || !bins || !systems_per_block || !tuned)
+    return fail(GS_ERR_INVALID_PARAMETER, "null argument");
   std::lock_guard<std::mutex> lk(k->tiles_mu);
   auto it = k->tiles.find(gs::size_class(nt));
   gs::Tiles t = gs::default_tiles(nt, true);
@@ -1174,6 +1195,7 @@ int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins, int* 
   }
   *run = t.run;
   *bins = t.bins;
+  *systems_per_block = t.spc;
   return GS_OK;
 }
 

@@ -122,8 +122,9 @@ __host__ __device__ inline RowsLayout rows_layout(int R, int PC, int nf, int dim
   return L;
 }
 
-// K3: one system per block of R threads (n <= R neighbours, p <= PC drift
-// terms).  The system [C F; F^T 0] [w; mu] = [c; f] is solved through the
+// K3: one system per R threads (n <= R neighbours, p <= PC drift terms),
+// S systems per block side by side (each with its own part of the shared
+// memory, its own runs of targets and its own barriers).  The system [C F; F^T 0] [w; mu] = [c; f] is solved through the
 // covariance block: the sweep gives -C^{-1} and G = C^{-1} F in registers,
 // S = F^T G (p x p) is inverted in FP32, and a correction for a residual
 // (r1, r2) is
@@ -139,30 +140,32 @@ __host__ __device__ inline RowsLayout rows_layout(int R, int PC, int nf, int dim
 // packed matrix, and only pairs with a newly placed neighbour are evaluated.
 // Solving in slot order instead of neighbour order changes only the order of
 // roundings.
-template <int D, int R, int PC>
-__global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
+template <int D, int R, int PC, int S>
+__global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
     krige_rows_kernel(KrigeArgs a, DevModel m, ExpTable tab_g, DfConsts kc, uint8_t* flag) {
   constexpr int W = R + PC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
-  for (int q = threadIdx.x; q < 256; q += R) tab.v[q] = tab_g.v[q];
-  const int i = threadIdx.x;
+  for (int q = threadIdx.x; q < 256; q += R * S) tab.v[q] = tab_g.v[q];
+  const int i = rows_tid<R, S>();
   const Frames fr = frames_of(m);
   const RowsLayout L = rows_layout(R, PC, fr.nf, D);
-  df* A = reinterpret_cast<df*>(smem_raw + L.off_a);     // packed covariance block (slots)
-  df* F = reinterpret_cast<df*>(smem_raw + L.off_f);     // F[q * R + s]: drift q at slot s
-  df* V = reinterpret_cast<df*>(smem_raw + L.off_v);     // frame coordinates (slots)
-  df* B = reinterpret_cast<df*>(smem_raw + L.off_b);     // c (slots), f (R..R+p-1)
-  df* Z = reinterpret_cast<df*>(smem_raw + L.off_z);     // values (slots)
-  df* X = reinterpret_cast<df*>(smem_raw + L.off_x);     // current w, broadcast
-  float* rowbuf = reinterpret_cast<float*>(smem_raw + L.off_row);
-  float* vec = reinterpret_cast<float*>(smem_raw + L.off_vec);
-  float* red = reinterpret_cast<float*>(smem_raw + L.off_red);
-  df* redd = reinterpret_cast<df*>(smem_raw + L.off_redd);
-  float* Sinv = reinterpret_cast<float*>(smem_raw + L.off_s);
-  df* TD = reinterpret_cast<df*>(smem_raw + L.off_td);  // target coordinates, sk mean
-  int* sflag = reinterpret_cast<int*>(smem_raw + L.off_flag);
-  int* new_idx = reinterpret_cast<int*>(smem_raw + L.off_slots);  // this target's neighbours
+  // this system's part of the block's shared memory
+  unsigned char* const sbase = smem_raw + (size_t)rows_sys<R, S>() * L.total;
+  df* A = reinterpret_cast<df*>(sbase + L.off_a);     // packed covariance block (slots)
+  df* F = reinterpret_cast<df*>(sbase + L.off_f);     // F[q * R + s]: drift q at slot s
+  df* V = reinterpret_cast<df*>(sbase + L.off_v);     // frame coordinates (slots)
+  df* B = reinterpret_cast<df*>(sbase + L.off_b);     // c (slots), f (R..R+p-1)
+  df* Z = reinterpret_cast<df*>(sbase + L.off_z);     // values (slots)
+  df* X = reinterpret_cast<df*>(sbase + L.off_x);     // current w, broadcast
+  float* rowbuf = reinterpret_cast<float*>(sbase + L.off_row);
+  float* vec = reinterpret_cast<float*>(sbase + L.off_vec);
+  float* red = reinterpret_cast<float*>(sbase + L.off_red);
+  df* redd = reinterpret_cast<df*>(sbase + L.off_redd);
+  float* Sinv = reinterpret_cast<float*>(sbase + L.off_s);
+  df* TD = reinterpret_cast<df*>(sbase + L.off_td);  // target coordinates, sk mean
+  int* sflag = reinterpret_cast<int*>(sbase + L.off_flag);
+  int* new_idx = reinterpret_cast<int*>(sbase + L.off_slots);  // this target's neighbours
   int* matched = new_idx + R;     // neighbour already in a slot
   int* umap = matched + R;        // k-th unplaced neighbour
   int* act_list = umap + R;       // occupied slots, ascending (the pivot order)
@@ -176,7 +179,8 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
   const int64_t ntl = a.ntl_dev ? *a.ntl_dev : a.ntl;
   const int run = a.run > 0 ? a.run : kRowsRun;
   const bool route = a.route_fp64 && *a.route_fp64;
-  for (int64_t r0 = (int64_t)blockIdx.x * run; r0 < ntl; r0 += (int64_t)gridDim.x * run) {
+  for (int64_t r0 = ((int64_t)blockIdx.x * S + rows_sys<R, S>()) * run; r0 < ntl;
+       r0 += (int64_t)gridDim.x * S * run) {
   const int64_t r1 = r0 + run < ntl ? r0 + run : ntl;
   for (int64_t it = r0; it < r1; ++it) {
     const int64_t t = a.tlist ? a.tlist[it] : it;
@@ -207,25 +211,25 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     // --- slots: keep shared neighbours, place new ones in free slots
     if (i < n) new_idx[i] = a.nb[t * (int64_t)a.kout + i];
     matched[i] = 0;
-    rows_bar<R>();
+    rows_bar<R, S>();
     int pos = -1;
     if (my_idx >= 0) {
       for (int q = 0; q < n; ++q) pos = new_idx[q] == my_idx ? q : pos;
     }
     const bool keep = pos >= 0;
     if (keep) matched[pos] = 1;
-    rows_bar<R>();
+    rows_bar<R, S>();
     unsigned long long m_un, m_free;
-    rows_ballot2<R>(i < n && !matched[i], !keep, m_un, m_free, bal);
+    rows_ballot2<R, S>(i < n && !matched[i], !keep, m_un, m_free, bal);
     const int n_un = __popcll(m_un);
     if ((m_un >> i) & 1ull) umap[rank_below(m_un, i)] = i;
-    rows_bar<R>();
+    rows_bar<R, S>();
     const int rf = rank_below(m_free, i);
     const bool fresh = !keep && rf < n_un;
     my_idx = keep ? my_idx : (fresh ? new_idx[umap[rf]] : -1);
     const bool act = my_idx >= 0;
     unsigned long long m_act, m_fresh;
-    rows_ballot2<R>(act, fresh, m_act, m_fresh, bal + 4);
+    rows_ballot2<R, S>(act, fresh, m_act, m_fresh, bal + 4);
     const int nact = __popcll(m_act);  // == n
     const int nfresh = __popcll(m_fresh);
     if (act) act_list[rank_below(m_act, i)] = i;
@@ -248,53 +252,59 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       for (int q = 0; q < PC; ++q)
         if (q < p) F[q * R + i] = a.basis_df[(int64_t)q * a.n + idx];
     }
-    rows_bar<R>();
-    // --- covariances of pairs with a newly placed point, two at a time
-    auto put2 = [&](int s0, int u0, int s1, int u1, bool two) {
-      df c0, c1;
-      cov_pair2<D>(m, fr, V, R, s0, u0, s1, u1, tab, kc, c0, c1);
-      A[s0 >= u0 ? pk(s0, u0) : pk(u0, s0)] = c0;
-      if (two) A[s1 >= u1 ? pk(s1, u1) : pk(u1, s1)] = c1;
-    };
-    if (2 * nfresh >= nact) {
-      // most slots are new: the whole triangle over occupied slots
-      for_pairs2(nact, i, R, [&](int i0, int j0, int i1, int j1, bool two) {
-        put2(act_list[i0], act_list[j0], act_list[i1], act_list[j1], two);
-      });
-    } else {
-      // (new slot, occupied slot) pairs; a pair of two new slots once
-      const int P = nfresh * nact;
-      int fr0 = 0, c0 = i;
-      while (c0 >= nact) {
-        c0 -= nact;
-        ++fr0;
-      }
-      for (int q = i; q < P; q += 2 * R) {
-        int fr1 = fr0, c1 = c0 + R;
-        while (c1 >= nact) {
-          c1 -= nact;
-          ++fr1;
+    rows_bar<R, S>();
+    // --- covariances of pairs with a newly placed point, two at a time.
+    // When most slots are new, the whole strict lower triangle over the
+    // occupied slots (pair (a, b), b < a, of act_list); otherwise the
+    // (new slot, occupied slot) pairs (fresh_list[a], act_list[b]), a pair
+    // of two new slots once.  One loop and one call site of the covariance
+    // code for both, so the kernel carries a single copy of it.
+    {
+      const bool full = 2 * nfresh >= nact;
+      const int P = full ? ((nact * (nact - 1)) >> 1) : nfresh * nact;
+      // advance pair cursor (a, b) by `step` pair numbers
+      auto adv = [&](int& pa, int& pb, int step) {
+        pb += step;
+        if (full) {
+          while (pb >= pa && pa < nact) {
+            pb -= pa;
+            ++pa;
+          }
+        } else {
+          while (pb >= nact) {
+            pb -= nact;
+            ++pa;
+          }
         }
+      };
+      int a0 = full ? 1 : 0, b0 = 0;
+      adv(a0, b0, i);
+      for (int q = i; q < P; q += 2 * R) {
+        int a1 = a0, b1 = b0;
+        adv(a1, b1, R);
         const bool has1 = q + R < P;
-        const int s0 = fresh_list[fr0], u0 = act_list[c0];
-        const int s1 = has1 ? fresh_list[fr1] : s0, u1 = has1 ? act_list[c1] : u0;
-        const bool v0 = u0 != s0 && (!((m_fresh >> u0) & 1ull) || u0 < s0);
-        const bool v1 = has1 && u1 != s1 && (!((m_fresh >> u1) & 1ull) || u1 < s1);
+        if (!has1) {
+          a1 = a0;
+          b1 = b0;
+        }
+        const int s0 = full ? act_list[a0] : fresh_list[a0], u0 = act_list[b0];
+        const int s1 = full ? act_list[a1] : fresh_list[a1], u1 = act_list[b1];
+        const bool v0 = full || (u0 != s0 && (!((m_fresh >> u0) & 1ull) || u0 < s0));
+        const bool v1 = has1 && (full || (u1 != s1 && (!((m_fresh >> u1) & 1ull) || u1 < s1)));
         if (v0 || v1) {
           df e0, e1;
           cov_pair2<D>(m, fr, V, R, s0, u0, s1, u1, tab, kc, e0, e1);
           if (v0) A[s0 >= u0 ? pk(s0, u0) : pk(u0, s0)] = e0;
           if (v1) A[s1 >= u1 ? pk(s1, u1) : pk(u1, s1)] = e1;
         }
-        fr0 = fr1;
-        c0 = c1 + R;
-        while (c0 >= nact) {
-          c0 -= nact;
-          ++fr0;
+        if (has1) {
+          a0 = a1;
+          b0 = b1;
+          adv(a0, b0, R);
         }
       }
     }
-    rows_bar<R>();
+    rows_bar<R, S>();
     // --- FP32 rows: covariance block (identity off the occupied slots), drift block
     float2 tr[W / 2];
     auto cov_hi = [&](int j) {
@@ -308,7 +318,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
 #pragma unroll
     for (int j2 = 0; j2 < R / 2; ++j2)
       amax = fmaxf(amax, act ? fmaxf(fabsf(tr[j2].x), fabsf(tr[j2].y)) : 0.0f);
-    amax = rows_max<R>(amax, red, slot);
+    amax = rows_max<R, S>(amax, red, slot);
     // power-of-two scale sc with sc * max|C| in [0.5, 1): every pivot is then
     // <= 1, so the pivot thread's multiplier 1 - 1/d never cancels.  The
     // covariance rows and the drift columns are both scaled, so the drift
@@ -325,7 +335,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
 #pragma unroll
     for (int q2 = 0; q2 < PC / 2; ++q2) tr[R / 2 + q2] = make_float2(drift_hi(2 * q2), drift_hi(2 * q2 + 1));
     // (an empty simple-kriging system has nothing to invert: w = 0)
-    bool ok = nact == 0 || (amax > 0.0f && rows_sweep<R, W / 2>(tr, act_list, nact, 1e-6f * amax * sc, rowbuf));
+    bool ok = nact == 0 || (amax > 0.0f && rows_sweep<R, W / 2, S>(tr, act_list, nact, 1e-6f * amax * sc, rowbuf));
     // --- Schur complement S = F^T G and its FP32 inverse (thread 0)
     if (ok && p > 0) {
       for (int q = 0; q < p; ++q) {
@@ -333,7 +343,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         const float fq = act ? F[q * R + i].hi : 0.0f;
 #pragma unroll
         for (int r = 0; r < PC; ++r) v[r] = fq * row_elt(tr, R + r);
-        rows_sum<R, PC>(v, red, slot);
+        rows_sum<R, PC, S>(v, red, slot);
         if (i == 0) {
 #pragma unroll
           for (int r = 0; r < PC; ++r) Sinv[q * PC + r] = v[r];
@@ -364,17 +374,17 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         }
         sflag[0] = good;
       }
-      rows_bar<R>();
+      rows_bar<R, S>();
       ok = sflag[0] != 0;
     }
     if (!ok) {
       if (i == 0) flag[t] = 1;
-      rows_bar<R>();
+      rows_bar<R, S>();
       continue;
     }
     // --- correction operator: (r1 in vec[0..R), r2 in vec[R..R+p)) -> (d1, d2)
     auto apply = [&](float& d1, float (&d2)[PC]) {
-      const float y = sc * rows_cinv_apply<R, W / 2>(tr, vec, act);
+      const float y = sc * rows_cinv_apply<R, W / 2, S>(tr, vec, act);
       d1 = y;
 #pragma unroll
       for (int q = 0; q < PC; ++q) d2[q] = 0.0f;
@@ -382,7 +392,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         float u[PC];
 #pragma unroll
         for (int q = 0; q < PC; ++q) u[q] = (act && q < p) ? F[q * R + i].hi * y : 0.0f;
-        rows_sum<R, PC>(u, red, slot);
+        rows_sum<R, PC, S>(u, red, slot);
 #pragma unroll
         for (int q = 0; q < PC; ++q) u[q] = q < p ? u[q] - vec[R + q] : 0.0f;
 #pragma unroll
@@ -401,7 +411,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     // x0 from the hi parts of the right-hand side
     vec[i] = act ? B[i].hi : 0.0f;
     if (i < p) vec[R + i] = B[R + i].hi;
-    rows_bar<R>();
+    rows_bar<R, S>();
     float d1, d2[PC];
     apply(d1, d2);
     df x1 = df_make(d1, 0.0f);
@@ -411,12 +421,12 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     float mx = fabsf(d1);
 #pragma unroll
     for (int q = 0; q < PC; ++q) mx = fmaxf(mx, fabsf(d2[q]));
-    const float nx = rows_max<R>(mx, red, slot);
+    const float nx = rows_max<R, S>(mx, red, slot);
     float nd_prev = nx;
     bool conv = false;
     for (int sweep = 1; sweep <= kMaxRefineSweeps && !conv; ++sweep) {
       X[i] = x1;
-      rows_bar<R>();
+      rows_bar<R, S>();
       // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q over occupied slots,
       // two compensated accumulators for ILP
       float s = 0.0f, c = 0.0f, s1 = 0.0f, c1 = 0.0f;
@@ -457,7 +467,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       for (int q = 0; q < PC; ++q) r2[q] = 0.0f;
       for (int q = 0; q < p; ++q) {
         df v[1] = {act ? df_mul(F[q * R + i], x1) : df_make(0.0f, 0.0f)};
-        rows_sum_df<R, 1>(v, redd, slot);
+        rows_sum_df<R, 1, S>(v, redd, slot);
         const df rq = df_sub(B[R + q], v[0]);
 #pragma unroll
         for (int r = 0; r < PC; ++r)
@@ -469,7 +479,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         for (int q = 0; q < PC; ++q)
           if (q < p) vec[R + q] = r2[q];
       }
-      rows_bar<R>();
+      rows_bar<R, S>();
       apply(d1, d2);
       if (act) x1 = df_add_f(x1, d1);
       mx = fabsf(d1);
@@ -478,7 +488,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
         x2[q] = df_add_f(x2[q], d2[q]);
         mx = fmaxf(mx, fabsf(d2[q]));
       }
-      const float nd = rows_max<R>(mx, red, slot);
+      const float nd = rows_max<R, S>(mx, red, slot);
       if (nd <= 1e-15f * nx) conv = true;
       else if (sweep >= 2) {
         const float rho = nd / nd_prev;
@@ -489,7 +499,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
     }
     if (!conv) {
       if (i == 0) flag[t] = 1;
-      rows_bar<R>();
+      rows_bar<R, S>();
       continue;
     }
     // --- outputs: double-float sums, FP64 at the end
@@ -500,7 +510,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       o[0] = act ? df_mul(x1, Z[i]) : df_make(0.0f, 0.0f);
     }
     o[1] = act ? df_mul(x1, B[i]) : df_make(0.0f, 0.0f);
-    rows_sum_df<R, 2>(o, redd, slot);
+    rows_sum_df<R, 2, S>(o, redd, slot);
     if (i == 0) {
       df sr = o[1];
 #pragma unroll
@@ -515,7 +525,7 @@ __global__ void __launch_bounds__(R, R == 64 ? 8 : 16)
       a.out_st[t] = GS_ST_OK;
       flag[t] = 0;
     }
-    rows_bar<R>();
+    rows_bar<R, S>();
   }
   }
 }
@@ -1308,23 +1318,32 @@ static void ensure_tables() {
   });
 }
 
-template <int D, int R, int PC>
+template <int D, int R, int PC, int S>
 static int launch_rows(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int nf,
                        cudaStream_t stream) {
   const RowsLayout lay = rows_layout(R, PC, nf, D);
-  const size_t smem = lay.total;
-  auto kern = krige_rows_kernel<D, R, PC>;
+  const size_t smem = lay.total * S;
+  auto kern = krige_rows_kernel<D, R, PC, S>;
   GS_TRY(allow_dynamic_smem((const void*)kern, smem));
   const int sms = sm_count();
   int per_sm = 0;
-  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R, smem));
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, R * S, smem));
   per_sm = std::max(per_sm, 1);
   const int run = a.run > 0 ? a.run : kRowsRun;
-  const int blocks = (int)std::min<int64_t>((a.ntl + run - 1) / run, (int64_t)sms * per_sm);
-  kern<<<blocks, R, smem, stream>>>(a, m, g_tab, g_kc, flag);
+  const int64_t runs = (a.ntl + run - 1) / run;
+  const int blocks = (int)std::max<int64_t>(
+      1, std::min<int64_t>((runs + S - 1) / S, (int64_t)sms * per_sm));
+  kern<<<blocks, R * S, smem, stream>>>(a, m, g_tab, g_kc, flag);
   GS_CUDA(cudaGetLastError());
   count_launch(1);
   return GS_OK;
+}
+
+template <int D, int R, int PC>
+static int launch_rows_s(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int nf,
+                         cudaStream_t stream) {
+  return a.spc == 2 ? launch_rows<D, R, PC, 2>(a, m, flag, nf, stream)
+                    : launch_rows<D, R, PC, 1>(a, m, flag, nf, stream);
 }
 
 int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int force_rows,
@@ -1337,15 +1356,15 @@ int krige_mixed_launch(const KrigeArgs& a, const DevModel& m, uint8_t* flag, int
   const bool small = force_rows ? force_rows == 32 : nb <= 32;
   const bool wide = a.p > 4;
   if (a.dim == 2) {
-    if (small) return wide ? launch_rows<2, 32, 12>(a, m, flag, nf, stream)
-                           : launch_rows<2, 32, 4>(a, m, flag, nf, stream);
-    return wide ? launch_rows<2, 64, 12>(a, m, flag, nf, stream)
-                : launch_rows<2, 64, 4>(a, m, flag, nf, stream);
+    if (small) return wide ? launch_rows_s<2, 32, 12>(a, m, flag, nf, stream)
+                           : launch_rows_s<2, 32, 4>(a, m, flag, nf, stream);
+    return wide ? launch_rows_s<2, 64, 12>(a, m, flag, nf, stream)
+                : launch_rows_s<2, 64, 4>(a, m, flag, nf, stream);
   }
-  if (small) return wide ? launch_rows<3, 32, 12>(a, m, flag, nf, stream)
-                         : launch_rows<3, 32, 4>(a, m, flag, nf, stream);
-  return wide ? launch_rows<3, 64, 12>(a, m, flag, nf, stream)
-              : launch_rows<3, 64, 4>(a, m, flag, nf, stream);
+  if (small) return wide ? launch_rows_s<3, 32, 12>(a, m, flag, nf, stream)
+                         : launch_rows_s<3, 32, 4>(a, m, flag, nf, stream);
+  return wide ? launch_rows_s<3, 64, 12>(a, m, flag, nf, stream)
+              : launch_rows_s<3, 64, 4>(a, m, flag, nf, stream);
 }
 
 template <int D>

@@ -49,6 +49,7 @@ struct KrigeArgs {
   int64_t ntl;               // number of them (an upper bound when ntl_dev is set)
   const int64_t* ntl_dev;    // the number on the device, read by the kernel, or null
   int run;                   // consecutive targets per block sequence (0: 64)
+  int spc;                   // systems per block of the mixed solver (1 or 2; 0: 1)
   const int* route_fp64;     // when set and nonzero: flag every valid system
                              // for the FP64 re-solve without attempting it
   const double* boff;        // block kriging: nboff x dim discretisation offsets

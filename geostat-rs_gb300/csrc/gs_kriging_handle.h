@@ -11,13 +11,16 @@
 #include "gs_search.cuh"
 
 namespace gs {
-// Launch shape of the mixed solver: consecutive targets per block sequence
+// Launch shape of the mixed solver: consecutive targets per system's run
 // (longer runs share more matrix entries between neighbouring targets,
-// shorter ones spread small calls over more SMs) and whether uneven
-// neighbourhoods are split into the 32- and 64-thread solvers.
+// shorter ones spread small calls over more SMs), warps per system for
+// neighbourhoods of at most 32 points (bins 1: such systems go to the
+// one-warp solver, bins 0: every system uses the two-warp solver) and
+// systems per block (spc 1 or 2).
 struct Tiles {
   int run = 64;
   int bins = 0;
+  int spc = 1;
 };
 }  // namespace gs
 
@@ -45,7 +48,7 @@ struct gs_kriging {
   // and a shape pinned by the caller (run 0: none)
   mutable std::mutex tiles_mu;
   mutable std::map<int, gs::Tiles> tiles;
-  gs::Tiles pinned{0, 0};
+  gs::Tiles pinned{0, 0, 1};
   // global neighbourhood: LU factors of the (n + p) system (row-major), the
   // solve's row order; lu_state 0 none, 1 factored, 2 singular
   double* d_lu = nullptr;

@@ -14,15 +14,37 @@
 
 namespace gs {
 
-template <int R>
+// A block holds S systems side by side (R threads each); thread i of a
+// system is rows_tid<R, S>() and its system within the block rows_sys<R, S>().
+template <int R, int S>
+__device__ __forceinline__ int rows_tid() {
+  if constexpr (S == 1) return (int)threadIdx.x;
+  else return (int)(threadIdx.x & (unsigned)(R - 1));
+}
+template <int R, int S>
+__device__ __forceinline__ int rows_sys() {
+  if constexpr (S == 1) return 0;
+  else return (int)(threadIdx.x / (unsigned)R);
+}
+
+// Barrier over one system's threads: the warp for R = 32; for R = 64 the
+// block's barrier with one system per block, else the named barrier
+// 1 + (system in the block) over the system's two warps.
+template <int R, int S>
 __device__ __forceinline__ void rows_bar() {
-  if constexpr (R == 32) __syncwarp();
-  else __syncthreads();
+  if constexpr (R == 32) {
+    __syncwarp();
+  } else if constexpr (S == 1) {
+    __syncthreads();
+  } else {
+    static_assert(R == 64, "one or two warps per system");
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + rows_sys<R, S>()), "r"(R) : "memory");
+  }
 }
 
 // Sum of K floats over the block; every thread receives the sums.  The
 // per-warp partials are added in warp order (deterministic).
-template <int R, int K>
+template <int R, int K, int S = 1>
 __device__ __forceinline__ void rows_sum(float (&v)[K], float* red, int& slot) {
 #pragma unroll
   for (int k = 0; k < K; ++k)
@@ -33,9 +55,9 @@ __device__ __forceinline__ void rows_sum(float (&v)[K], float* red, int& slot) {
     float* r = red + slot * NW * K;
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-      for (int k = 0; k < K; ++k) r[(threadIdx.x >> 5) * K + k] = v[k];
+      for (int k = 0; k < K; ++k) r[(rows_tid<R, S>() >> 5) * K + k] = v[k];
     }
-    __syncthreads();
+    rows_bar<R, S>();
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       float s = r[k];
@@ -47,15 +69,15 @@ __device__ __forceinline__ void rows_sum(float (&v)[K], float* red, int& slot) {
   }
 }
 
-template <int R>
+template <int R, int S = 1>
 __device__ __forceinline__ float rows_max(float v, float* red, int& slot) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   if constexpr (R > 32) {
     constexpr int NW = R / 32;
     float* r = red + slot * NW;
-    if ((threadIdx.x & 31) == 0) r[threadIdx.x >> 5] = v;
-    __syncthreads();
+    if ((threadIdx.x & 31) == 0) r[rows_tid<R, S>() >> 5] = v;
+    rows_bar<R, S>();
     v = r[0];
 #pragma unroll
     for (int w = 1; w < NW; ++w) v = fmaxf(v, r[w]);
@@ -65,7 +87,7 @@ __device__ __forceinline__ float rows_max(float v, float* red, int& slot) {
 }
 
 // Double-float sum of K values over the block (compensated at every step).
-template <int R, int K>
+template <int R, int K, int S = 1>
 __device__ __forceinline__ void rows_sum_df(df (&v)[K], df* red, int& slot) {
 #pragma unroll
   for (int k = 0; k < K; ++k)
@@ -81,9 +103,9 @@ __device__ __forceinline__ void rows_sum_df(df (&v)[K], df* red, int& slot) {
     df* r = red + slot * NW * K;
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-      for (int k = 0; k < K; ++k) r[(threadIdx.x >> 5) * K + k] = v[k];
+      for (int k = 0; k < K; ++k) r[(rows_tid<R, S>() >> 5) * K + k] = v[k];
     }
-    __syncthreads();
+    rows_bar<R, S>();
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       df s = r[k];
@@ -119,12 +141,12 @@ __device__ __forceinline__ float row_elt(const float2 (&t)[W2], int j) {
 // columns are zero).  The update runs as packed FP32x2 FMAs (two columns per
 // instruction).  The row buffer is double-buffered, so one barrier per pivot
 // suffices.  Returns false (uniformly) when a pivot is not above tol.
-template <int R, int W2>
+template <int R, int W2, int S = 1>
 __device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int npiv, float tol,
                                            float* rowbuf) {
   constexpr int W = 2 * W2;
   static_assert(W2 % 2 == 0, "rows are published as float4");
-  const int i = threadIdx.x;
+  const int i = rows_tid<R, S>();
   for (int kk = 0; kk < npiv; ++kk) {
     const int k = piv[kk];
     float* rb = rowbuf + (kk & 1) * (W + 4);
@@ -137,7 +159,7 @@ __device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int 
       rb[k] = d - 1.0f;
       rb[W] = d;
     }
-    rows_bar<R>();
+    rows_bar<R, S>();
     const float d = rb[W];
     if (!(fabsf(d) > tol)) return false;
     const float invd = __fdividef(1.0f, d);  // an approximate inverse suffices
@@ -156,9 +178,9 @@ __device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int 
 // y_i = (M^{-1} v)_i for a pivot row i (act) from the rows swept on M (v
 // broadcast through shared memory, zero off the pivots); packed FP32x2
 // products.
-template <int R, int W2>
+template <int R, int W2, int S = 1>
 __device__ __forceinline__ float rows_cinv_apply(const float2 (&t)[W2], const float* v, bool act) {
-  const int i = threadIdx.x;
+  const int i = rows_tid<R, S>();
   float2 a0 = make_float2(0.0f, 0.0f), a1 = make_float2(0.0f, 0.0f);
 #pragma unroll
   for (int j2 = 0; j2 < R / 2; j2 += 2) {
@@ -173,7 +195,7 @@ __device__ __forceinline__ float rows_cinv_apply(const float2 (&t)[W2], const fl
 // 64-bit masks of two predicates over the block's threads (bit i = thread
 // i), identical in every thread.  sh: 4 words of shared scratch not read by
 // anyone else until the next barrier after this call.
-template <int R>
+template <int R, int S = 1>
 __device__ __forceinline__ void rows_ballot2(bool p0, bool p1, unsigned long long& m0,
                                              unsigned long long& m1, unsigned* sh) {
   const unsigned b0 = __ballot_sync(0xffffffffu, p0), b1 = __ballot_sync(0xffffffffu, p1);
@@ -182,12 +204,12 @@ __device__ __forceinline__ void rows_ballot2(bool p0, bool p1, unsigned long lon
     m1 = b1;
   } else {
     static_assert(R == 64, "one or two warps");
-    const int w = threadIdx.x >> 5;
+    const int w = rows_tid<R, S>() >> 5;
     if ((threadIdx.x & 31) == 0) {
       sh[2 * w] = b0;
       sh[2 * w + 1] = b1;
     }
-    __syncthreads();
+    rows_bar<R, S>();
     m0 = (unsigned long long)sh[0] | ((unsigned long long)sh[2] << 32);
     m1 = (unsigned long long)sh[1] | ((unsigned long long)sh[3] << 32);
   }

@@ -72,8 +72,8 @@ SIGNATURES = {
     "gs_kriging_predict_many_async": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                              _int, _vp]),
     "gs_kriging_cross_validate": (_int, [_vp, _i64, C.c_uint64, _pd, _pd, _pu8, _int]),
-    "gs_kriging_set_tiles": (_int, [_vp, _int, _int]),
-    "gs_kriging_tiles": (_int, [_vp, _i64, _pi32, _pi32, _pi32]),
+    "gs_kriging_set_tiles": (_int, [_vp, _int, _int, _int]),
+    "gs_kriging_tiles": (_int, [_vp, _i64, _pi32, _pi32, _pi32, _pi32]),
     "gs_kriging_predict_fp64_noalloc": (_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                                _vp, _vp]),
     "gs_last_fallbacks": (_i64, []),

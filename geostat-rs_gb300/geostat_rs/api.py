@@ -330,17 +330,18 @@ class Kriging:
                 PRECISIONS[precision], stream)
         _abi.check(rc)
 
-    def set_tiles(self, run: int = 0, bins: int = 0):
+    def set_tiles(self, run: int = 0, bins: int = 0, systems_per_block: int = 1):
         """Pin the mixed solver's launch shape (run 0 returns to autotuning)."""
-        _abi.check(_abi.load().gs_kriging_set_tiles(self._h, int(run), int(bins)))
+        _abi.check(_abi.load().gs_kriging_set_tiles(self._h, int(run), int(bins),
+                                                    int(systems_per_block)))
 
     def tiles(self, nt: int):
-        """(run, bins, source) a call with ``nt`` targets would use; source is
-        "default", "tuned" or "pinned"."""
-        r, b, t = C.c_int32(), C.c_int32(), C.c_int32()
+        """(run, bins, systems_per_block, source) a call with ``nt`` targets
+        would use; source is "default", "tuned" or "pinned"."""
+        r, b, sp, t = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         _abi.check(_abi.load().gs_kriging_tiles(self._h, int(nt), C.byref(r), C.byref(b),
-                                                C.byref(t)))
-        return r.value, b.value, ("default", "tuned", "pinned")[t.value]
+                                                C.byref(sp), C.byref(t)))
+        return r.value, b.value, sp.value, ("default", "tuned", "pinned")[t.value]
 
     def close(self):
         if getattr(self, "_h", None):

@@ -197,18 +197,22 @@ int gs_kriging_block_cv(const gs_kriging* k, const int64_t* blocks_per_dim, doub
                         double* variance, uint8_t* status, int precision);
 /* Launch shapes of the mixed solver (no counterpart in the reference).  The
  * first call of at least 65,536 targets on a predictor times the candidate
- * shapes -- runs of 16/32/64/128 consecutive targets per block, uneven
- * neighbourhoods split onto the 32- and 64-thread solvers or not -- on its
+ * shapes -- runs of 16/32/64/128 consecutive targets per system; warps per
+ * system for neighbourhoods of at most 32 points (bins 1: uneven
+ * neighbourhoods split onto the one-warp and two-warp solvers, bins 0: every
+ * system on the two-warp solver); one or two systems per block -- on its
  * first 131,072 targets and keeps the fastest for every later call of at
  * least 65,536 targets; smaller and asynchronous calls before that use a
  * default.  Results of different shapes agree within the parity tolerance
  * (the order of roundings differs), and a predictor's results are
  * reproducible once its shapes are fixed.
  * gs_kriging_set_tiles pins one shape for every call (run a power of two in
- * [1, 1024], bins 0/1; run 0 unpins).  gs_kriging_tiles reports the shape a
- * call with nt targets would use; tuned = 0 default, 1 tuned, 2 pinned. */
-int gs_kriging_set_tiles(gs_kriging* k, int run, int bins);
-int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins, int* tuned);
+ * [1, 1024], bins 0/1, systems_per_block 1/2; run 0 unpins).
+ * gs_kriging_tiles reports the shape a call with nt targets would use;
+ * tuned = 0 default, 1 tuned, 2 pinned. */
+int gs_kriging_set_tiles(gs_kriging* k, int run, int bins, int systems_per_block);
+int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins,
+                     int* systems_per_block, int* tuned);
 /* Allocation-free FP64 prediction (no counterpart in the reference).  The
  * same results as gs_kriging_predict_many_device with GS_PREC_FP64, for
  * callers that may not allocate device memory while they predict: the

@@ -88,26 +88,28 @@ def test_tuner_and_pinned_shapes(data):
     k = _predictor("ordinary", c, v, m, cov)
     nt = 70_000  # above the tuning threshold
     t = np.random.default_rng(5).uniform(0, EXTENT, size=(nt, 2))
-    assert k.tiles(nt)[2] == "default"
+    assert k.tiles(nt)[3] == "default"
     base = k.predict_many(t, "mixed", full=True)
-    run, bins, src = k.tiles(nt)
-    assert src == "tuned" and run in (16, 32, 64, 128) and bins in (0, 1)
+    run, bins, spc, src = k.tiles(nt)
+    assert src == "tuned" and run in (16, 32, 64, 128) and bins in (0, 1) and spc in (1, 2)
     again = k.predict_many(t, "mixed", full=True)
     # the tuned shape is kept: identical results
     np.testing.assert_array_equal(again.value, base.value)
     np.testing.assert_array_equal(again.variance, base.variance)
     vs = float(np.mean(np.abs(v)))
-    for run, bins in ((8, 0), (128, 1), (1, 1)):
-        k.set_tiles(run, bins)
-        assert k.tiles(nt) == (run, bins, "pinned")
+    for run, bins, spc in ((8, 0, 1), (128, 1, 2), (1, 1, 1), (32, 0, 2)):
+        k.set_tiles(run, bins, spc)
+        assert k.tiles(nt) == (run, bins, spc, "pinned")
         out = k.predict_many(t, "mixed", full=True)
         assert ((out.status & 0x3f) == (base.status & 0x3f)).all()
-        assert_close(out.value, base.value, vs, 1e-9, f"run {run} bins {bins}")
-        assert_close(out.variance, base.variance, 1e-3, 1e-9, f"run {run} bins {bins}")
+        assert_close(out.value, base.value, vs, 1e-9, f"run {run} bins {bins} spc {spc}")
+        assert_close(out.variance, base.variance, 1e-3, 1e-9, f"run {run} bins {bins} spc {spc}")
     k.set_tiles(0)
-    assert k.tiles(nt)[2] == "tuned"
+    assert k.tiles(nt)[3] == "tuned"
     with pytest.raises(G.InvalidParameter):
         k.set_tiles(48)
+    with pytest.raises(G.InvalidParameter):
+        k.set_tiles(32, 0, 3)
     # an oracle check on a slice of the tuned call
     ref = O.krige(c, v, m, t[:600], **SEARCH)
     assert_close(base.value[:600], ref["value"], vs, 1e-9, "tuned value")
