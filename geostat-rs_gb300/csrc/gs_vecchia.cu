@@ -341,6 +341,97 @@ __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim, int lt_w
 
 constexpr int kVWarps = 4;  // warps (ordered points in flight) per block
 
+// Refinement with residuals formed in FP64, for a likelihood system whose
+// double-float refinement stalled (its residual is limited by the 48-bit
+// entries): the warp evaluates the covariances of the conditioning set S and
+// of the point in FP64 (the table-driven exp of the FP64 re-solve kernel,
+// K64 packed lower over S, k64 per neighbour), starts from the stalled
+// solution in W.xd, and repeats w += C32^{-1} (k - K w) with the FP32 inverse
+// it already holds (the sweep rows of f) and the residual in FP64.  It
+// accepts when a correction falls below 1e-14 of |w|, or when the
+// corrections stop shrinking at or below 1e-12 of |w| -- the fixed point of
+// FP64-residual refinement, whose forward error is the size of that last
+// correction (cond(K) 2^-53, as for an FP64 factorisation; larger stalls go
+// to the FP64 re-solve kernel).  On success lane 0 receives the conditional
+// variance and residual of loglik_with_plan (vecchia.rs:302-330) from FP64
+// dot products; returns false (uniformly) otherwise.
+template <int D>
+__device__ bool vecchia_refine_fp64(const VArgs& a, const DevModel& mdl, const Exp64Table& et,
+                                    int64_t k, int64_t pt, int s, int lane, const WarpFactor& f,
+                                    const WarpScratch& W, double* K64, double* k64,
+                                    double& var, double& r) {
+  const int M = a.m;
+  const int32_t* nbk = a.nb + k * (int64_t)M;
+  const double* xs[3] = {a.x, a.y, a.z};
+  // the stalled double-float iterate, before the buffers are reused
+  __syncwarp();
+  double w = lane < s ? (double)W.xd[lane].hi + (double)W.xd[lane].lo : 0.0;
+  __syncwarp();
+  for (int e = lane; e < (s * (s + 1)) / 2; e += 32) {
+    // (q, p), p <= q < s, packed order
+    int q = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+    while ((q * (q + 1)) / 2 > e) --q;
+    while (((q + 1) * (q + 2)) / 2 <= e) ++q;
+    const int p = e - (q * (q + 1)) / 2;
+    double v = mdl.c0;
+    if (p != q) {
+      const int ip = nbk[p], iq = nbk[q];
+      double h[3];
+#pragma unroll
+      for (int d = 0; d < D; ++d) h[d] = xs[d][ip] - xs[d][iq];
+      v = cov_fp64x<D>(mdl, h, et);
+    }
+    K64[pk(q, p)] = v;
+  }
+  double zl = 0.0;
+  if (lane < s) {
+    const int j = nbk[lane];
+    double h[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d) h[d] = xs[d][pt] - xs[d][j];
+    k64[lane] = cov_fp64x<D>(mdl, h, et);
+    zl = a.v[j] - a.mean;
+  }
+  double* wb = reinterpret_cast<double*>(W.xd);  // broadcast of w
+  bool ok = false;
+  float nd_prev = 0.0f;
+  for (int sweep = 1; sweep <= 4; ++sweep) {
+    __syncwarp();
+    wb[lane] = w;
+    __syncwarp();
+    double rho = 0.0;
+    if (lane < s) {
+      rho = k64[lane];
+      for (int j = 0; j < s; ++j) rho = fma(-K64[lane >= j ? pk(lane, j) : pk(j, lane)], wb[j], rho);
+    }
+    W.vec[lane] = (float)rho;
+    __syncwarp();
+    float y;
+    warp_gemv_neg_inv(f.t, W.vec, lane, y);
+    y *= f.sc;
+    if (lane < s) w -= (double)y;
+    const float nd = warp_max_f(lane < s ? fabsf(y) : 0.0f);
+    const float nw = warp_max_f(lane < s ? (float)fabs(w) : 0.0f);
+    if (nd <= 1e-14f * nw) {
+      ok = true;
+      break;
+    }
+    if (sweep >= 2 && !(nd < 0.5f * nd_prev)) {
+      ok = nd <= 1e-12f * nw;
+      break;
+    }
+    nd_prev = nd;
+  }
+  if (!ok) return false;
+  double red = lane < s ? k64[lane] * w : 0.0, mu = lane < s ? zl * w : 0.0;
+  red = warp_sum_d(red);
+  mu = warp_sum_d(mu);
+  var = fmax(mdl.c0 - red, 1e-12);
+  r = (a.v[pt] - a.mean) - mu;
+  return true;
+}
+
+
 // One warp per ordered point for conditioning sets of at most 32 points: the
 // same assembly and certification as vecchia_loglik_kernel, with the
 // register-row solver of gs_warp.cuh (no block barriers).  The likelihood
@@ -348,11 +439,20 @@ constexpr int kVWarps = 4;  // warps (ordered points in flight) per block
 // per thread without spills; the REML form would spill and keeps the default.
 template <int D, bool REML>
 __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
-    vecchia_warp_kernel(VArgs a, ExpTable tab_g,
-                                                                   DfConsts kc) {
+    vecchia_warp_kernel(VArgs a, ExpTable tab_g, DfConsts kc, Exp64Table et_g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
+  __shared__ Exp64Table et;  // FP64 covariances of the FP64-residual refinement
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tab.v[i] = tab_g.v[i];
+  for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+    et.hi[q] = et_g.hi[q];
+    et.lo[q] = et_g.lo[q];
+  }
+  if (threadIdx.x == 0) {
+    et.l1 = et_g.l1;
+    et.l2 = et_g.l2;
+    et.inv = et_g.inv;
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -465,8 +565,27 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
         });
       }
       __syncwarp();
-      const bool ok = warp_solve(A, B, s, lane, W);
-      if (!ok) {
+      bool ok, ok64 = false;
+      {
+        WarpFactor fct;
+        const bool fok = warp_factor(A, s, lane, fct, W);
+        ok = fok && warp_refine(fct, B, s, lane, W);
+        if (!REML && fok && !ok) {
+          // stalled: refine with FP64 residuals (A's and B's storage take the
+          // FP64 entries; this candidate's double-float system is done with)
+          double v64 = 0.0, r64 = 0.0;
+          ok64 = vecchia_refine_fp64<D>(a, mdl, et, k, i, s, lane, fct, W,
+                                        reinterpret_cast<double*>(A),
+                                        reinterpret_cast<double*>(B), v64, r64);
+          if (ok64 && lane == 0) {
+            LT[LW * (c & 31)] = v64;
+            LT[LW * (c & 31) + 1] = r64;
+          }
+        }
+      }
+      if (ok64) {
+        // outputs written by the FP64-residual refinement
+      } else if (!ok) {
         if (lane == 0) LT[LW * (c & 31)] = -1.0;
       } else {
         df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
@@ -1030,7 +1149,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
       per_sm = std::max(per_sm, 1);
       const int blocks =
           (int)std::min<int64_t>((span + kVWarps - 1) / kVWarps, (int64_t)sms * per_sm);
-      kern<<<blocks, 32 * kVWarps, smem, s>>>(a, g_vtab, g_vkc);
+      kern<<<blocks, 32 * kVWarps, smem, s>>>(a, g_vtab, g_vkc, g_vet);
     } else {
       const VLayout lay = vecchia_layout(std::max(M, 1), dim);
       const size_t smem = lay.total;
