@@ -550,7 +550,7 @@ def vecchia_bench(args, log):
     dt = statistics.median(ts)
     from geostat_rs import _abi
     phase = G.last_timings()
-    resolved = int(_abi.load().gs_last_fallbacks())
+    floor_acc, fp64res, resolved = G.last_vecchia_tiers()
     t1 = time.perf_counter()
     ll64, _ = plan.loglik(cands, precision="fp64")
     dt64 = time.perf_counter() - t1
@@ -573,6 +573,8 @@ def vecchia_bench(args, log):
            "mixed_kernel_ms": phase[1], "fp64_resolve_ms": phase[2],
            "fp64_resolved_systems": resolved,
            "fp64_resolved_fraction": resolved / (n * len(cands)),
+           "floor_accepted_systems": floor_acc,
+           "fp64_residual_refined_systems": fp64res,
            "plan_seconds": t_plan, "status_ok": bool((st == 0).all())}
     # the oracle at full size: candidate 0's log-likelihood on the same plan
     # (sequential, as the reference sums), and the plan's predecessor sets at

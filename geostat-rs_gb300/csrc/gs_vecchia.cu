@@ -130,6 +130,9 @@ struct VArgs {
   const double* basis;
   int p;
   double* rec;
+  // likelihood systems accepted at the double-float floor [0] and refined
+  // with FP64 residuals [1] (one add per warp; may be null)
+  unsigned long long* tiers;
 };
 
 constexpr double kLn2Pi = 1.8378770664093453;  // ln(2*pi)
@@ -341,6 +344,14 @@ __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim, int lt_w
 
 constexpr int kVWarps = 4;  // warps (ordered points in flight) per block
 
+// Likelihood systems whose double-float refinement stops contracting with its
+// corrections at most this fraction of |w| are accepted (warp_refine's
+// accept_floor): the conditional mean and variance are linear functionals of
+// w, so their error at that floor is the double-float entries' rounding, as
+// for a converged refinement.  Larger stalls take the FP64-residual
+// refinement below.
+constexpr float kVecchiaFloor = 1e-10f;
+
 // Refinement with residuals formed in FP64, for a likelihood system whose
 // double-float refinement stalled (its residual is limited by the 48-bit
 // entries): the warp evaluates the covariances of the conditioning set S and
@@ -491,6 +502,7 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
     __syncwarp();
   };
   const int64_t nwarps = (int64_t)gridDim.x * kVWarps;
+  unsigned n_floor = 0, n_fp64res = 0;
   for (int64_t k = a.k0 + (int64_t)blockIdx.x * kVWarps + wib; k < a.k1; k += nwarps) {
     const int64_t i = a.order[k];
     const int s = a.cnt[k];
@@ -569,7 +581,10 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
       {
         WarpFactor fct;
         const bool fok = warp_factor(A, s, lane, fct, W);
-        ok = fok && warp_refine(fct, B, s, lane, W);
+        // REML keeps the strict test: its records feed further sums
+        bool at_floor = false;
+        ok = fok && warp_refine(fct, B, s, lane, W, REML ? 0.0f : kVecchiaFloor, &at_floor);
+        n_floor += ok && at_floor;
         if (!REML && fok && !ok) {
           // stalled: refine with FP64 residuals (A's and B's storage take the
           // FP64 entries; this candidate's double-float system is done with)
@@ -581,6 +596,7 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
             LT[LW * (c & 31)] = v64;
             LT[LW * (c & 31) + 1] = r64;
           }
+          n_fp64res += ok64;
         }
       }
       if (ok64) {
@@ -615,6 +631,10 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
       if ((c & 31) == 31 || c == a.ncand - 1) flush_terms(k, c & ~31, (c & 31) + 1);
       __syncwarp();
     }
+  }
+  if (lane == 0 && a.tiers) {
+    if (n_floor) atomicAdd(&a.tiers[0], (unsigned long long)n_floor);
+    if (n_fp64res) atomicAdd(&a.tiers[1], (unsigned long long)n_fp64res);
   }
 }
 
@@ -1041,6 +1061,10 @@ __global__ void exclude_terms_kernel(double* terms, int64_t n, int64_t ncand,
 // REML (basis set, p columns; conditioning sets of at most 32 points, mixed
 // precision): instead of log-likelihoods, reml_sums receives per candidate
 // the reml_sums(p) sums of the ungrouped REML (ll is left NaN).
+// Systems of the last mixed likelihood evaluation on this host thread that
+// were accepted at the double-float floor / refined with FP64 residuals.
+static thread_local int64_t g_vtiers[2] = {0, 0};
+
 int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models, double* ll,
                  int32_t* status, int precision, cudaStream_t s, const uint8_t* exclude,
                  const double* basis, int p, double* reml_sums, int64_t k0, int64_t k1) {
@@ -1098,6 +1122,10 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   if (partial_range) GS_CUDA(cudaMemsetAsync(flag.ptr, 0, (size_t)ncand * n, s));
   GS_TRY(cstat.alloc((size_t)ncand * 4, s));
   GS_CUDA(cudaMemsetAsync(cstat.ptr, 0, ncand * 4, s));
+  DevBuf tiers;
+  GS_TRY(tiers.alloc(2 * sizeof(unsigned long long), s));
+  GS_CUDA(cudaMemsetAsync(tiers.ptr, 0, 2 * sizeof(unsigned long long), s));
+  g_vtiers[0] = g_vtiers[1] = 0;
   VArgs a{};
   a.dim = dim;
   a.n = n;
@@ -1123,6 +1151,7 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
   a.basis = basis;
   a.p = p;
   a.rec = (double*)rec.ptr;
+  a.tiers = (unsigned long long*)tiers.ptr;
   int64_t nfl = 0;
   DevBuf list;
   const bool mixed = precision != GS_PREC_FP64 && M <= GS_MIXED_MAX_NEIGHBORS;
@@ -1178,8 +1207,12 @@ int vecchia_eval(const gs_vecchia_plan* P, int64_t ncand, const gs_model* models
     GS_CUDA(cub::DeviceSelect::Flagged(tmp.ptr, tb, thrust::counting_iterator<int64_t>(0),
                                        (uint8_t*)flag.ptr, (int64_t*)list.ptr, (int64_t*)nsel.ptr,
                                        (int64_t)(ncand * n), s));
+    unsigned long long ht[2] = {0, 0};
     GS_CUDA(cudaMemcpyAsync(&nfl, nsel.ptr, 8, cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaMemcpyAsync(ht, tiers.ptr, sizeof(ht), cudaMemcpyDeviceToHost, s));
     GS_CUDA(cudaStreamSynchronize(s));
+    g_vtiers[0] = (int64_t)ht[0];
+    g_vtiers[1] = (int64_t)ht[1];
   }
   if (!mixed) GS_CUDA(cudaEventRecord(ev[1], s));
   GS_CUDA(cudaEventRecord(ev[2], s));
@@ -3203,6 +3236,12 @@ int fit_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
 extern "C" {
 
 int64_t gs_last_fit_rounds(void) { return g_fit_rounds; }
+
+void gs_last_vecchia_tiers(int64_t* out2) {
+  if (!out2) return;
+  out2[0] = g_vtiers[0];
+  out2[1] = g_vtiers[1];
+}
 
 int gs_vecchia_mle(const gs_pointset* ps, int32_t kind, int64_t m, const int64_t* order,
                    gs_model* out_model, double* out_loglik, double* out_x, int64_t* n_evals) {

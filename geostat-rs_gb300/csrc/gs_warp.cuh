@@ -122,8 +122,22 @@ constexpr int kMaxRefineSweeps = 8;
 // Solves A x = B with the factorisation f and refines to ~1e-13 relative; on
 // success W.xd[i] holds x_i.  Returns false (uniformly) when the refinement
 // stalls.
+//
+// accept_floor > 0: a refinement that stops contracting (or runs out of
+// sweeps) once its corrections are at most accept_floor |x| is accepted as
+// well, with *at_floor set.  The residual b - A x is then limited by the
+// double-float entries (about 2^-48 of each entry and product), not by the
+// FP32 inverse.  A linear functional g.x of the last iterate then differs
+// from g.A^{-1}b by v.(r~ - r) + (v - v32).r, with v = A^{-1} g, v32 its FP32
+// approximation and r~ the computed residual of the previous iterate: the
+// first term is the effect of the entries' rounding, the same for a
+// refinement that converges (it converges to the double-float system's
+// solution), and the second is a product of two small factors.  Callers
+// whose outputs are such functionals (the Vecchia conditional mean and
+// variance) may use it.
 __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, int N, int lane,
-                                            const WarpScratch& W) {
+                                            const WarpScratch& W, float accept_floor = 0.0f,
+                                            bool* at_floor = nullptr) {
   // x0 = A^{-1} b_hi = -(-A^{-1}) b_hi
   __syncwarp();
   W.vec[lane] = lane < N ? B[lane].hi : 0.0f;
@@ -166,13 +180,16 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
       const float rho = nd / nd_prev;
       done = rho < 0.5f && rho * nd <= 1e-13f * nx;
     }
-    if (done) {
+    const bool stalled = sweep >= 2 && !(nd < 0.5f * nd_prev);  // no longer contracting
+    const bool floor_ok = (stalled || sweep == kMaxRefineSweeps) && nd <= accept_floor * nx;
+    if (done || floor_ok) {
       __syncwarp();
       W.xd[lane] = x;
       __syncwarp();
+      if (at_floor) *at_floor = !done;
       return true;
     }
-    if (sweep >= 2 && !(nd < 0.5f * nd_prev)) return false;  // no longer contracting
+    if (stalled) return false;
     nd_prev = nd;
   }
   return false;

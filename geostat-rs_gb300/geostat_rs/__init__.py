@@ -13,7 +13,7 @@ from .model import Anisotropy, Structure, VariogramModel, parse_kind
 from .api import (CvResult, Kriging, KrigingConfig, KrigingResult, PointSet, Server, TuneResult,
                   VecchiaPlan, block_cv, block_offsets, k_fold, krige,
                   krige_3d, krige_grid, loo_cv,
-                  last_timings, leave_one_out, leave_one_out_with_drift, maxmin_order,
+                  last_timings, last_vecchia_tiers, leave_one_out, leave_one_out_with_drift, maxmin_order,
                   tune_kriging_neighbors,
                   nelder_mead_multistart, rng_normal, rng_uniform, seq_mean,
                   vecchia_krige, vecchia_loglik, vecchia_loglik_grouped, vecchia_mle, vecchia_mle_fit,

@@ -78,6 +78,7 @@ SIGNATURES = {
                                                _vp, _vp]),
     "gs_last_fallbacks": (_i64, []),
     "gs_last_fit_rounds": (_i64, []),
+    "gs_last_vecchia_tiers": (None, [_pi64]),
     "gs_debug_device_allocations": (_i64, []),
     "gs_debug_refuse_allocations": (_int, [_i64]),
     "gs_last_lu_resolves": (_i64, []),

@@ -363,6 +363,16 @@ def last_timings():
     return tuple(out.tolist())
 
 
+def last_vecchia_tiers():
+    """Systems of the last mixed Vecchia likelihood call on this thread that
+    were (accepted at the double-float refinement floor, refined with FP64
+    residuals, re-solved by the FP64 kernel)."""
+    out = np.zeros(2, dtype=np.int64)
+    lib = _abi.load()
+    lib.gs_last_vecchia_tiers(out.ctypes.data_as(_abi._pi64))
+    return int(out[0]), int(out[1]), int(lib.gs_last_fallbacks())
+
+
 # -------------------------------------------------- reference Python API --
 # ------------------------------------------------------- cross-validation --
 @dataclass

@@ -341,6 +341,12 @@ int gs_vecchia_mle_nm(const gs_pointset* ps, int32_t kind, int64_t m, const int6
 /* Batched objective launches (rounds) of the last lock-step Nelder-Mead fit
  * on this host thread (gs_vecchia_mle_nm and the grouped / REML fits). */
 int64_t gs_last_fit_rounds(void);
+/* Diagnostics of the last mixed Vecchia likelihood evaluation on this host
+ * thread: out2[0] = (candidate, point) systems accepted when their
+ * double-float refinement reached its noise floor (corrections at most
+ * 1e-10 of |w|), out2[1] = systems refined with FP64 residuals.  Systems
+ * re-solved by the FP64 kernel are gs_last_fallbacks(). */
+void gs_last_vecchia_tiers(int64_t* out2);
 /* vecchia_mle_grouped (vecchia.rs:939-950): group_size <= 1 is
  * gs_vecchia_mle; otherwise Nelder-Mead (step 0.3, 2000 iterations) from
  * the reference's three starts over the grouped likelihood, each round's
