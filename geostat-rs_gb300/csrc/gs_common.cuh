@@ -393,20 +393,6 @@ __device__ __forceinline__ df rho_df(int kind, df d, const ExpTable& tab, const 
   return exp_factor_df(kind, s, df_expneg(s, tab, k));
 }
 
-// rho_df at two arguments side by side (one kind).
-__device__ __forceinline__ void rho_df2(int kind, df d0, df d1, const ExpTable& tab,
-                                        const ExpConsts& k, df& r0, df& r1) {
-  if (kind == GS_KIND_SPHERICAL) {
-    r0 = rho_sph_df(d0);
-    r1 = rho_sph_df(d1);
-    return;
-  }
-  const df s0 = exp_arg_df(kind, d0, k), s1 = exp_arg_df(kind, d1, k);
-  const df e0 = df_expneg(s0, tab, k), e1 = df_expneg(s1, tab, k);
-  r0 = exp_factor_df(kind, s0, e0);
-  r1 = exp_factor_df(kind, s1, e1);
-}
-
 // 1/d to FP64 accuracy: FP32 estimate, two Newton steps (e = 1 - d r,
 // r += r e).  sc (a power of two) scales d into FP32's range first when the
 // system's scale is outside [1e-20, 1e20] (scaled = true).

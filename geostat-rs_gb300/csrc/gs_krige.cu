@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
   df* V = reinterpret_cast<df*>(sbase + L.off_v);     // frame coordinates (slots)
   df* B = reinterpret_cast<df*>(sbase + L.off_b);     // c (slots), f (R..R+p-1)
   df* Z = reinterpret_cast<df*>(sbase + L.off_z);     // values (slots)
-  df* X = reinterpret_cast<df*>(sbase + L.off_x);     // current w, broadcast
+  float* Xh = reinterpret_cast<float*>(sbase + L.off_x);  // -w (hi parts), broadcast
+  float* Xl = Xh + R;                                      // -w (lo parts)
   float* rowbuf = reinterpret_cast<float*>(sbase + L.off_row);
   float* vec = reinterpret_cast<float*>(sbase + L.off_vec);
   float* red = reinterpret_cast<float*>(sbase + L.off_red);
@@ -306,18 +307,21 @@ __global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
     }
     rows_bar<R, S>();
     // --- FP32 rows: covariance block (identity off the occupied slots), drift block
-    float2 tr[W / 2];
+    float4 tr[W / 4];
     auto cov_hi = [&](int j) {
       float v = i == j ? 1.0f : 0.0f;
       if (act && ((m_act >> j) & 1ull)) v = i >= j ? A[pk(i, j)].hi : A[pk(j, i)].hi;
       return v;
     };
 #pragma unroll
-    for (int j2 = 0; j2 < R / 2; ++j2) tr[j2] = make_float2(cov_hi(2 * j2), cov_hi(2 * j2 + 1));
+    for (int q = 0; q < R / 4; ++q)
+      tr[q] = make_float4(cov_hi(4 * q), cov_hi(4 * q + 1), cov_hi(4 * q + 2), cov_hi(4 * q + 3));
     float amax = 0.0f;
 #pragma unroll
-    for (int j2 = 0; j2 < R / 2; ++j2)
-      amax = fmaxf(amax, act ? fmaxf(fabsf(tr[j2].x), fabsf(tr[j2].y)) : 0.0f);
+    for (int q = 0; q < R / 4; ++q)
+      amax = fmaxf(amax, act ? fmaxf(fmaxf(fabsf(tr[q].x), fabsf(tr[q].y)),
+                                     fmaxf(fabsf(tr[q].z), fabsf(tr[q].w)))
+                             : 0.0f);
     amax = rows_max<R, S>(amax, red, slot);
     // power-of-two scale sc with sc * max|C| in [0.5, 1): every pivot is then
     // <= 1, so the pivot thread's multiplier 1 - 1/d never cancels.  The
@@ -327,15 +331,19 @@ __global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
     frexpf(amax, &ex);
     const float sc = ldexpf(1.0f, -ex);
 #pragma unroll
-    for (int j2 = 0; j2 < R / 2; ++j2) {
-      if (act && ((m_act >> (2 * j2)) & 1ull)) tr[j2].x *= sc;
-      if (act && ((m_act >> (2 * j2 + 1)) & 1ull)) tr[j2].y *= sc;
+    for (int q = 0; q < R / 4; ++q) {
+      if (act && ((m_act >> (4 * q)) & 1ull)) tr[q].x *= sc;
+      if (act && ((m_act >> (4 * q + 1)) & 1ull)) tr[q].y *= sc;
+      if (act && ((m_act >> (4 * q + 2)) & 1ull)) tr[q].z *= sc;
+      if (act && ((m_act >> (4 * q + 3)) & 1ull)) tr[q].w *= sc;
     }
     auto drift_hi = [&](int q) { return (act && q < p) ? F[q * R + i].hi * sc : 0.0f; };
 #pragma unroll
-    for (int q2 = 0; q2 < PC / 2; ++q2) tr[R / 2 + q2] = make_float2(drift_hi(2 * q2), drift_hi(2 * q2 + 1));
+    for (int q4 = 0; q4 < PC / 4; ++q4)
+      tr[R / 4 + q4] = make_float4(drift_hi(4 * q4), drift_hi(4 * q4 + 1), drift_hi(4 * q4 + 2),
+                                   drift_hi(4 * q4 + 3));
     // (an empty simple-kriging system has nothing to invert: w = 0)
-    bool ok = nact == 0 || (amax > 0.0f && rows_sweep<R, W / 2, S>(tr, act_list, nact, 1e-6f * amax * sc, rowbuf));
+    bool ok = nact == 0 || (amax > 0.0f && rows_sweep<R, W / 4, S>(tr, act_list, nact, 1e-6f * amax * sc, rowbuf));
     // --- Schur complement S = F^T G and its FP32 inverse (thread 0)
     if (ok && p > 0) {
       for (int q = 0; q < p; ++q) {
@@ -384,7 +392,7 @@ __global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
     }
     // --- correction operator: (r1 in vec[0..R), r2 in vec[R..R+p)) -> (d1, d2)
     auto apply = [&](float& d1, float (&d2)[PC]) {
-      const float y = sc * rows_cinv_apply<R, W / 2, S>(tr, vec, act);
+      const float y = sc * rows_cinv_apply<R, W / 4, S>(tr, vec, act);
       d1 = y;
 #pragma unroll
       for (int q = 0; q < PC; ++q) d2[q] = 0.0f;
@@ -425,41 +433,51 @@ __global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
     float nd_prev = nx;
     bool conv = false;
     for (int sweep = 1; sweep <= kMaxRefineSweeps && !conv; ++sweep) {
-      X[i] = x1;
+      Xh[i] = -x1.hi;
+      Xl[i] = -x1.lo;
       rows_bar<R, S>();
-      // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q over occupied slots,
-      // two compensated accumulators for ILP
-      float s = 0.0f, c = 0.0f, s1 = 0.0f, c1 = 0.0f;
-      auto acc = [](float& sa, float& ca, df aij, df xj) {
-        const float ph = __fmul_rn(-aij.hi, xj.hi);
-        float pe = __fmaf_rn(-aij.hi, xj.hi, -ph);
-        pe = __fmaf_rn(-aij.hi, xj.lo, pe);
-        pe = __fmaf_rn(-aij.lo, xj.hi, pe);
-        const float tsum = __fadd_rn(sa, ph);
-        const float bb = __fsub_rn(tsum, sa);
-        const float e = __fadd_rn(__fsub_rn(sa, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
-        sa = tsum;
-        ca += e + pe;
+      // r1_i = c_i - sum_j A_ij w_j - sum_q F_iq mu_q over occupied slots:
+      // compensated products and sums (Dot2), two occupied slots at a time
+      // as packed FP32x2 operations (even and odd positions of act_list in
+      // the two lanes of the accumulator pair), joined by one error-free sum
+      float s = 0.0f, c = 0.0f;
+      // acc(sa, ca, a, -x): sa + ca += -a x
+      auto acc = [](float& sa, float& ca, df aij, df nxj) {
+        const float ph = __fmul_rn(aij.hi, nxj.hi);
+        float pe = __fmaf_rn(aij.hi, nxj.hi, -ph);
+        pe = __fmaf_rn(aij.hi, nxj.lo, pe);
+        pe = __fmaf_rn(aij.lo, nxj.hi, pe);
+        const df ts = two_sum(sa, ph);
+        sa = ts.hi;
+        ca += ts.lo + pe;
       };
       if (act) {
-        s = B[i].hi;
-        c = B[i].lo;
+        float2 s2 = make_float2(B[i].hi, 0.0f), c2 = make_float2(B[i].lo, 0.0f);
         int jj = 0;
         for (; jj + 1 < nact; jj += 2) {
           const int j0 = act_list[jj], j1 = act_list[jj + 1];
-          acc(s, c, A[j0 <= i ? pk(i, j0) : pk(j0, i)], X[j0]);
-          acc(s1, c1, A[j1 <= i ? pk(i, j1) : pk(j1, i)], X[j1]);
+          const df a0 = A[j0 <= i ? pk(i, j0) : pk(j0, i)];
+          const df a1 = A[j1 <= i ? pk(i, j1) : pk(j1, i)];
+          const float2 ah = make_float2(a0.hi, a1.hi), al = make_float2(a0.lo, a1.lo);
+          const float2 xh = make_float2(Xh[j0], Xh[j1]), xl = make_float2(Xl[j0], Xl[j1]);
+          const float2 ph = __fmul2_rn(ah, xh);
+          float2 pe = __ffma2_rn(ah, xh, p_neg(ph));
+          pe = __ffma2_rn(ah, xl, pe);
+          pe = __ffma2_rn(al, xh, pe);
+          const dfp ts = p_two_sum(s2, ph);
+          s2 = ts.hi;
+          c2 = p_add(c2, p_add(ts.lo, pe));
         }
+        const df st2 = two_sum(s2.x, s2.y);
+        s = st2.hi;
+        c = (c2.x + c2.y) + st2.lo;
         if (jj < nact) {
           const int j0 = act_list[jj];
-          acc(s, c, A[j0 <= i ? pk(i, j0) : pk(j0, i)], X[j0]);
+          acc(s, c, A[j0 <= i ? pk(i, j0) : pk(j0, i)], df_make(Xh[j0], Xl[j0]));
         }
 #pragma unroll
         for (int q = 0; q < PC; ++q)
-          if (q < p) acc(s1, c1, F[q * R + i], x2[q]);
-        const df st2 = two_sum(s, s1);
-        s = st2.hi;
-        c = c + c1 + st2.lo;
+          if (q < p) acc(s, c, F[q * R + i], df_neg(x2[q]));
       }
       // r2_q = f_q - sum_i F_iq w_i, as double-float block sums
       float r2[PC];
@@ -503,14 +521,13 @@ __global__ void __launch_bounds__(R * S, (R == 64 ? 8 : 16) / S)
       continue;
     }
     // --- outputs: double-float sums, FP64 at the end
-    df o[2];
-    if (a.method == GS_SIMPLE) {
-      o[0] = act ? df_mul(x1, df_sub(Z[i], TD[3])) : df_make(0.0f, 0.0f);
-    } else {
-      o[0] = act ? df_mul(x1, Z[i]) : df_make(0.0f, 0.0f);
-    }
-    o[1] = act ? df_mul(x1, B[i]) : df_make(0.0f, 0.0f);
-    rows_sum_df<R, 2, S>(o, redd, slot);
+    // (w . z, w . c) as one packed double-float product and block sum
+    dfp op = dp_zero();
+    if (act)
+      op = dp_mul(dp_splat(x1),
+                  dp_pack(a.method == GS_SIMPLE ? df_sub(Z[i], TD[3]) : Z[i], B[i]));
+    op = rows_sum_dfp<R, S>(op, redd, slot);
+    const df o[2] = {dp_first(op), dp_second(op)};
     if (i == 0) {
       df sr = o[1];
 #pragma unroll

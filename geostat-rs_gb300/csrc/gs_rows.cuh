@@ -117,15 +117,38 @@ __device__ __forceinline__ void rows_sum_df(df (&v)[K], df* red, int& slot) {
   }
 }
 
-// Element j of a register row stored as float2 pairs (j compile-time after
-// unrolling).
-template <int W2>
-__device__ __forceinline__ float row_elt(const float2 (&t)[W2], int j) {
-  return (j & 1) ? t[j >> 1].y : t[j >> 1].x;
+// rows_sum_df of two values, as one packed double-float pair.
+template <int R, int S = 1>
+__device__ __forceinline__ dfp rows_sum_dfp(dfp v, df* red, int& slot) {
+  v = warp_sum_dfp(v);
+  if constexpr (R > 32) {
+    constexpr int NW = R / 32;
+    df* r = red + slot * NW * 2;
+    if ((threadIdx.x & 31) == 0) {
+      const int w = rows_tid<R, S>() >> 5;
+      r[2 * w] = dp_first(v);
+      r[2 * w + 1] = dp_second(v);
+    }
+    rows_bar<R, S>();
+    v = dp_pack(r[0], r[1]);
+#pragma unroll
+    for (int w = 1; w < NW; ++w) v = dp_add(v, dp_pack(r[2 * w], r[2 * w + 1]));
+    slot ^= 1;
+  }
+  return v;
 }
 
-// In-place sweep inverse of the register rows (2 * W2 columns as packed
-// pairs) over the pivots piv[0..npiv): afterwards the covariance block holds
+// Element j of a register row stored as float4 quads (j compile-time after
+// unrolling).  Quads keep each published row's 16-byte stores on aligned
+// register quads, and their halves are the FP32x2 operand pairs.
+template <int W4>
+__device__ __forceinline__ float row_elt(const float4 (&t)[W4], int j) {
+  const float4 q = t[j >> 2];
+  return (j & 3) == 0 ? q.x : (j & 3) == 1 ? q.y : (j & 3) == 2 ? q.z : q.w;
+}
+
+// In-place sweep inverse of the register rows (4 * W4 columns as quads)
+// over the pivots piv[0..npiv): afterwards the covariance block holds
 // -C^{-1} with +2 on its diagonal (pivot rows) and the drift block holds
 // C^{-1} F.
 //
@@ -141,20 +164,17 @@ __device__ __forceinline__ float row_elt(const float2 (&t)[W2], int j) {
 // columns are zero).  The update runs as packed FP32x2 FMAs (two columns per
 // instruction).  The row buffer is double-buffered, so one barrier per pivot
 // suffices.  Returns false (uniformly) when a pivot is not above tol.
-template <int R, int W2, int S = 1>
-__device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int npiv, float tol,
+template <int R, int W4, int S = 1>
+__device__ __forceinline__ bool rows_sweep(float4 (&t)[W4], const int* piv, int npiv, float tol,
                                            float* rowbuf) {
-  constexpr int W = 2 * W2;
-  static_assert(W2 % 2 == 0, "rows are published as float4");
+  constexpr int W = 4 * W4;
   const int i = rows_tid<R, S>();
   for (int kk = 0; kk < npiv; ++kk) {
     const int k = piv[kk];
     float* rb = rowbuf + (kk & 1) * (W + 4);
     if (i == k) {
 #pragma unroll
-      for (int j2 = 0; j2 < W2; j2 += 2)
-        *reinterpret_cast<float4*>(rb + 2 * j2) =
-            make_float4(t[j2].x, t[j2].y, t[j2 + 1].x, t[j2 + 1].y);
+      for (int q = 0; q < W4; ++q) *reinterpret_cast<float4*>(rb + 4 * q) = t[q];
       const float d = rb[k];  // this thread's own store
       rb[k] = d - 1.0f;
       rb[W] = d;
@@ -166,10 +186,11 @@ __device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int 
     const float l = i == k ? 1.0f - invd : rb[i] * invd;
     const float2 nl = make_float2(-l, -l);
 #pragma unroll
-    for (int j2 = 0; j2 < W2; j2 += 2) {
-      const float4 r = *reinterpret_cast<const float4*>(rb + 2 * j2);
-      t[j2] = __ffma2_rn(nl, make_float2(r.x, r.y), t[j2]);
-      t[j2 + 1] = __ffma2_rn(nl, make_float2(r.z, r.w), t[j2 + 1]);
+    for (int q = 0; q < W4; ++q) {
+      const float4 r = *reinterpret_cast<const float4*>(rb + 4 * q);
+      const float2 u0 = __ffma2_rn(nl, make_float2(r.x, r.y), make_float2(t[q].x, t[q].y));
+      const float2 u1 = __ffma2_rn(nl, make_float2(r.z, r.w), make_float2(t[q].z, t[q].w));
+      t[q] = make_float4(u0.x, u0.y, u1.x, u1.y);
     }
   }
   return true;
@@ -178,15 +199,15 @@ __device__ __forceinline__ bool rows_sweep(float2 (&t)[W2], const int* piv, int 
 // y_i = (M^{-1} v)_i for a pivot row i (act) from the rows swept on M (v
 // broadcast through shared memory, zero off the pivots); packed FP32x2
 // products.
-template <int R, int W2, int S = 1>
-__device__ __forceinline__ float rows_cinv_apply(const float2 (&t)[W2], const float* v, bool act) {
+template <int R, int W4, int S = 1>
+__device__ __forceinline__ float rows_cinv_apply(const float4 (&t)[W4], const float* v, bool act) {
   const int i = rows_tid<R, S>();
   float2 a0 = make_float2(0.0f, 0.0f), a1 = make_float2(0.0f, 0.0f);
 #pragma unroll
-  for (int j2 = 0; j2 < R / 2; j2 += 2) {
-    const float4 q = *reinterpret_cast<const float4*>(v + 2 * j2);
-    a0 = __ffma2_rn(t[j2], make_float2(q.x, q.y), a0);
-    a1 = __ffma2_rn(t[j2 + 1], make_float2(q.z, q.w), a1);
+  for (int q4 = 0; q4 < R / 4; ++q4) {
+    const float4 q = *reinterpret_cast<const float4*>(v + 4 * q4);
+    a0 = __ffma2_rn(make_float2(t[q4].x, t[q4].y), make_float2(q.x, q.y), a0);
+    a1 = __ffma2_rn(make_float2(t[q4].z, t[q4].w), make_float2(q.z, q.w), a1);
   }
   const float s = (a0.x + a1.x) + (a0.y + a1.y);
   return act ? fmaf(2.0f, v[i], -s) : 0.0f;

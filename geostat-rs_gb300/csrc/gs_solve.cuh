@@ -6,6 +6,7 @@
 #pragma once
 
 #include "gs_common.cuh"
+#include "gs_pair.cuh"
 
 namespace gs {
 
@@ -136,20 +137,21 @@ __device__ __forceinline__ df cov_pair(const DevModel& m, const Frames& fr, cons
   return c;
 }
 
-// Covariances at two separation norms (isotropic models), side by side.
+// Covariances at two separation norms (isotropic models), side by side in
+// packed FP32x2 arithmetic.
 __device__ __forceinline__ void cov_from_norm2(const DevModel& m, df h0, df h1,
                                                const ExpTable& tab, const DfConsts& k, df& c0,
                                                df& c1) {
-  c0 = df_make(0.0f, 0.0f);
-  c1 = df_make(0.0f, 0.0f);
+  const dfp h = dp_pack(h0, h1);
+  dfp c = dp_zero();
 #pragma unroll 1
   for (int s = 0; s < m.ns; ++s) {
     const DevStruct& st = m.s[s];
-    df r0, r1;
-    rho_df2(st.kind, df_mul(h0, st.inv_range_df), df_mul(h1, st.inv_range_df), tab, k, r0, r1);
-    c0 = df_add_fast(c0, df_mul(r0, st.sill_df));
-    c1 = df_add_fast(c1, df_mul(r1, st.sill_df));
+    const dfp r = dp_rho(st.kind, dp_mul(h, dp_splat(st.inv_range_df)), tab, k);
+    c = dp_add_fast(c, dp_mul(r, dp_splat(st.sill_df)));  // >= 0 terms
   }
+  c0 = dp_first(c);
+  c1 = dp_second(c);
 }
 
 // Visits this thread's pairs (i, j), i > j, of the strict lower triangle of
@@ -185,36 +187,45 @@ __device__ __forceinline__ void for_pairs2(int n, int first, int stride, Fn&& fn
   }
 }
 
+// |a - b| of the pairs (i0, j0) and (i1, j1) of frame f, side by side
+// (norm_pair lane by lane).
+template <int D>
+__device__ __forceinline__ dfp norm_pair2(const df* V, int stride, int f, int i0, int j0, int i1,
+                                          int j1) {
+  auto diff = [&](int d) {
+    return dp_sub_fast(dp_pack(vget<D>(V, stride, f, d, i0), vget<D>(V, stride, f, d, i1)),
+                       dp_pack(vget<D>(V, stride, f, d, j0), vget<D>(V, stride, f, d, j1)));
+  };
+  dfp q = dp_sqr(diff(0));
+#pragma unroll
+  for (int d = 1; d < D; ++d) q = dp_add_fast(q, dp_sqr(diff(d)));
+  return dp_sqrt(q);
+}
+
 // Covariances of two pairs (i0, j0) and (i1, j1) of stored points, evaluated
-// side by side so the two independent double-float chains interleave.
+// side by side in packed FP32x2 arithmetic (cov_pair lane by lane).
 template <int D>
 __device__ __forceinline__ void cov_pair2(const DevModel& m, const Frames& fr, const df* V,
                                           int stride, int i0, int j0, int i1, int j1,
                                           const ExpTable& tab, const DfConsts& k, df& c0,
                                           df& c1) {
-  c0 = df_make(0.0f, 0.0f);
-  c1 = df_make(0.0f, 0.0f);
-  df h0iso = df_make(-1.0f, 0.0f), h1iso = df_make(-1.0f, 0.0f);
+  dfp c = dp_zero();
+  dfp hiso = dp_make(p_splat(-1.0f), p_splat(0.0f));
 #pragma unroll 1
   for (int s = 0; s < m.ns; ++s) {
     const DevStruct& st = m.s[s];
-    df h0, h1;
+    dfp h;
     if (st.aniso) {
-      h0 = norm_pair<D>(V, stride, fr.fid[s], i0, j0);
-      h1 = norm_pair<D>(V, stride, fr.fid[s], i1, j1);
+      h = norm_pair2<D>(V, stride, fr.fid[s], i0, j0, i1, j1);
     } else {
-      if (h0iso.hi < 0.0f) {
-        h0iso = norm_pair<D>(V, stride, 0, i0, j0);
-        h1iso = norm_pair<D>(V, stride, 0, i1, j1);
-      }
-      h0 = h0iso;
-      h1 = h1iso;
+      if (hiso.hi.x < 0.0f) hiso = norm_pair2<D>(V, stride, 0, i0, j0, i1, j1);
+      h = hiso;
     }
-    df r0, r1;
-    rho_df2(st.kind, df_mul(h0, st.inv_range_df), df_mul(h1, st.inv_range_df), tab, k, r0, r1);
-    c0 = df_add_fast(c0, df_mul(r0, st.sill_df));
-    c1 = df_add_fast(c1, df_mul(r1, st.sill_df));
+    const dfp r = dp_rho(st.kind, dp_mul(h, dp_splat(st.inv_range_df)), tab, k);
+    c = dp_add_fast(c, dp_mul(r, dp_splat(st.sill_df)));
   }
+  c0 = dp_first(c);
+  c1 = dp_second(c);
 }
 
 // Covariance between stored point i and the frame origin (the target).
@@ -248,6 +259,20 @@ __device__ __forceinline__ df warp_sum_df(df v) {
     w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
     w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
     v = df_add(v, w);
+  }
+  return v;
+}
+
+// Two warp_sum_df side by side (packed FP32x2 additions).
+__device__ __forceinline__ dfp warp_sum_dfp(dfp v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dfp w;
+    w.hi.x = __shfl_xor_sync(0xffffffffu, v.hi.x, o);
+    w.hi.y = __shfl_xor_sync(0xffffffffu, v.hi.y, o);
+    w.lo.x = __shfl_xor_sync(0xffffffffu, v.lo.x, o);
+    w.lo.y = __shfl_xor_sync(0xffffffffu, v.lo.y, o);
+    v = dp_add(v, w);
   }
   return v;
 }

@@ -315,8 +315,13 @@ __global__ void __launch_bounds__(BLOCK, 4) vecchia_loglik_kernel(VArgs a, ExpTa
 // Per-warp shared-memory layout of vecchia_warp_kernel (conditioning sets of
 // at most 32 points).
 struct VWLayout {
-  size_t off_a, off_h, off_v, off_b, off_h0, off_z, off_row, off_vec, off_xd, off_lt, total;
+  size_t off_a, off_h, off_v, off_b, off_z, off_row, off_vec, off_xd, off_lt, total;
 };
+
+// Entries of the split (hi parts, then lo parts) arrays of the likelihood
+// kernel's assembly: the packed triangle of m points, then the m covariances
+// with the point, rounded up to an even count (entries go in pairs).
+__host__ __device__ inline int vw_split_entries(int m) { return (m * (m + 1) / 2 + m + 1) & ~1; }
 
 __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim, int lt_width = 2) {
   VWLayout L;
@@ -327,13 +332,13 @@ __host__ __device__ inline VWLayout vecchia_warp_layout(int m, int dim, int lt_w
     o += (bytes + 15) & ~(size_t)15;
     return r;
   };
-  L.off_a = take((size_t)np * sizeof(df));
-  L.off_h = take((size_t)np * sizeof(df));
+  const int ne = vw_split_entries(m);
+  L.off_a = take((size_t)(np > ne ? np : ne) * sizeof(df));
+  L.off_h = take((size_t)ne * sizeof(df));
   L.off_v = take((size_t)(GS_MAX_STRUCTURES + 1) * dim * m * sizeof(df));
   L.off_b = take((size_t)m * sizeof(df));
-  L.off_h0 = take((size_t)m * sizeof(df));
   L.off_z = take((size_t)m * sizeof(df));
-  L.off_row = take(kWarpN * sizeof(float));
+  L.off_row = take(kWarpRowFloats * sizeof(float));
   L.off_vec = take(kWarpN * sizeof(float));
   L.off_xd = take(kWarpN * sizeof(df));
   // (variance, residual[, basis residuals]) of 32 candidates
@@ -446,10 +451,14 @@ __device__ bool vecchia_refine_fp64(const VArgs& a, const DevModel& mdl, const E
 // One warp per ordered point for conditioning sets of at most 32 points: the
 // same assembly and certification as vecchia_loglik_kernel, with the
 // register-row solver of gs_warp.cuh (no block barriers).  The likelihood
-// form is compiled for four blocks (16 warps) per SM: it fits 128 registers
-// per thread without spills; the REML form would spill and keeps the default.
+// form is compiled for three blocks (12 warps) per SM, at which it needs no
+// spills (measured faster than four blocks at 128 registers with spills);
+// the REML form keeps the default.
+#ifndef GS_VECCHIA_MIN_BLOCKS
+#define GS_VECCHIA_MIN_BLOCKS 3
+#endif
 template <int D, bool REML>
-__global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
+__global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : GS_VECCHIA_MIN_BLOCKS)
     vecchia_warp_kernel(VArgs a, ExpTable tab_g, DfConsts kc, Exp64Table et_g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
@@ -471,11 +480,16 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
   const int LW = REML ? 2 + a.p : 2;  // doubles per candidate in LT
   const VWLayout lay = vecchia_warp_layout(M, D, LW);
   unsigned char* base = smem_raw + (size_t)wib * lay.total;
-  df* A = reinterpret_cast<df*>(base + lay.off_a);
-  df* H = reinterpret_cast<df*>(base + lay.off_h);
+  // the matrix's packed entries and the point's covariances, split: hi parts
+  // at Ah[e], lo parts at Al[e] (e < np: packed triangle, np + q: point q);
+  // the separations of the isotropic form in the same split layout
+  const int NE = vw_split_entries(M);
+  float* Ah = reinterpret_cast<float*>(base + lay.off_a);
+  float* Al = Ah + NE;
+  float* Hh = reinterpret_cast<float*>(base + lay.off_h);
+  float* Hl = Hh + NE;
   df* V = reinterpret_cast<df*>(base + lay.off_v);
   df* B = reinterpret_cast<df*>(base + lay.off_b);
-  df* H0 = reinterpret_cast<df*>(base + lay.off_h0);
   df* ZV = reinterpret_cast<df*>(base + lay.off_z);
   WarpScratch W;
   W.row = reinterpret_cast<float*>(base + lay.off_row);
@@ -535,30 +549,56 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
       ZV[lane] = REML ? a.vdf[j] : df_sub(a.vdf[j], a.mean_df);
     }
     __syncwarp();
+    // entries of this set: packed triangle, then the point's covariances
+    const int np = (s * (s + 1)) >> 1;
+    const int ne = (np + s + 1) & ~1;
     if (a.iso_shared) {
-      if (lane < s) H0[lane] = norm_origin<D>(V, M, 0, lane);
+      // separation norms once per point (diagonal positions 0; the padding
+      // entry, if any, a harmless 0 too)
       for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
         const df h0 = norm_pair<D>(V, M, 0, i0, j0);
         const df h1 = norm_pair<D>(V, M, 0, i1, j1);
-        H[pk(i0, j0)] = h0;
-        if (two) H[pk(i1, j1)] = h1;
+        Hh[pk(i0, j0)] = h0.hi;
+        Hl[pk(i0, j0)] = h0.lo;
+        if (two) {
+          Hh[pk(i1, j1)] = h1.hi;
+          Hl[pk(i1, j1)] = h1.lo;
+        }
       });
+      if (lane < s) {
+        const df h = norm_origin<D>(V, M, 0, lane);
+        Hh[np + lane] = h.hi;
+        Hl[np + lane] = h.lo;
+        Hh[pk(lane, lane)] = 0.0f;
+        Hl[pk(lane, lane)] = 0.0f;
+      }
+      if (lane == 0 && ne > np + s) {
+        Hh[np + s] = 0.0f;
+        Hl[np + s] = 0.0f;
+      }
       __syncwarp();
     }
     for (int c = 0; c < a.ncand; ++c) {
       const DevModel& mdl = a.models[c];
       const Frames fr = frames_of(mdl);
       if (a.iso_shared) {
-        if (lane < s) {
-          B[lane] = cov_from_norm(mdl, H0[lane], tab, kc);
-          A[pk(lane, lane)] = mdl.c0_df;
-        }
-        for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
+        // every entry of the set, two adjacent ones per lane and step, by
+        // packed position: no pair indices, 8-byte loads and stores of
+        // aligned hi / lo pairs
+        for (int e = 2 * lane; e < ne; e += 64) {
           df c0, c1;
-          cov_from_norm2(mdl, H[pk(i0, j0)], H[pk(i1, j1)], tab, kc, c0, c1);
-          A[pk(i0, j0)] = c0;
-          if (two) A[pk(i1, j1)] = c1;
-        });
+          const float2 hh = *reinterpret_cast<const float2*>(Hh + e);
+          const float2 hl = *reinterpret_cast<const float2*>(Hl + e);
+          cov_from_norm2(mdl, df_make(hh.x, hl.x), df_make(hh.y, hl.y), tab, kc, c0, c1);
+          *reinterpret_cast<float2*>(Ah + e) = make_float2(c0.hi, c1.hi);
+          *reinterpret_cast<float2*>(Al + e) = make_float2(c0.lo, c1.lo);
+        }
+        __syncwarp();
+        if (lane < s) {
+          B[lane] = df_make(Ah[np + lane], Al[np + lane]);
+          Ah[pk(lane, lane)] = mdl.c0_df.hi;  // C(0), nugget included
+          Al[pk(lane, lane)] = mdl.c0_df.lo;
+        }
       } else {
         if (lane < s) {
           df ud[3];
@@ -566,21 +606,26 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
           for (int d = 0; d < D; ++d) ud[d] = V[d * M + lane];
           frame_coords<D>(mdl, fr, ud, V, M, lane);
           B[lane] = cov_origin<D>(mdl, fr, V, M, lane, tab, kc);
-          A[pk(lane, lane)] = mdl.c0_df;
+          Ah[pk(lane, lane)] = mdl.c0_df.hi;
+          Al[pk(lane, lane)] = mdl.c0_df.lo;
         }
         __syncwarp();
         for_pairs2(s, lane, 32, [&](int i0, int j0, int i1, int j1, bool two) {
           df c0, c1;
           cov_pair2<D>(mdl, fr, V, M, i0, j0, i1, j1, tab, kc, c0, c1);
-          A[pk(i0, j0)] = c0;
-          if (two) A[pk(i1, j1)] = c1;
+          Ah[pk(i0, j0)] = c0.hi;
+          Al[pk(i0, j0)] = c0.lo;
+          if (two) {
+            Ah[pk(i1, j1)] = c1.hi;
+            Al[pk(i1, j1)] = c1.lo;
+          }
         });
       }
       __syncwarp();
       bool ok, ok64 = false;
       {
         WarpFactor fct;
-        const bool fok = warp_factor(A, s, lane, fct, W);
+        const bool fok = warp_factor(Ah, Al, s, lane, fct, W);
         // REML keeps the strict test: its records feed further sums
         bool at_floor = false;
         ok = fok && warp_refine(fct, B, s, lane, W, REML ? 0.0f : kVecchiaFloor, &at_floor);
@@ -590,7 +635,7 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
           // FP64 entries; this candidate's double-float system is done with)
           double v64 = 0.0, r64 = 0.0;
           ok64 = vecchia_refine_fp64<D>(a, mdl, et, k, i, s, lane, fct, W,
-                                        reinterpret_cast<double*>(A),
+                                        reinterpret_cast<double*>(Ah),
                                         reinterpret_cast<double*>(B), v64, r64);
           if (ok64 && lane == 0) {
             LT[LW * (c & 31)] = v64;
@@ -604,13 +649,11 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : 4)
       } else if (!ok) {
         if (lane == 0) LT[LW * (c & 31)] = -1.0;
       } else {
-        df mu = df_make(0.0f, 0.0f), red = df_make(0.0f, 0.0f);
-        if (lane < s) {
-          mu = df_fma_acc(mu, W.xd[lane], ZV[lane]);
-          red = df_fma_acc(red, W.xd[lane], B[lane]);
-        }
-        mu = warp_sum_df(mu);
-        red = warp_sum_df(red);
+        // (w . z, w . k) as one packed double-float product and sum
+        dfp pr = dp_zero();
+        if (lane < s) pr = dp_mul(dp_splat(W.xd[lane]), dp_pack(ZV[lane], B[lane]));
+        pr = warp_sum_dfp(pr);
+        const df mu = dp_first(pr), red = dp_second(pr);
         if (lane == 0) {
           LT[LW * (c & 31)] = fmax(df_to_double(df_sub(mdl.c0_df, red)), 1e-12);
           LT[LW * (c & 31) + 1] = df_to_double(df_sub(zi, mu));
@@ -1389,7 +1432,7 @@ __host__ __device__ inline VGLayout vecchia_grad_layout(int m, int dim) {
   L.off_br = take((size_t)m * sizeof(df));
   L.off_wv = take((size_t)m * sizeof(df));
   L.off_rhs = take((size_t)m * sizeof(df));
-  L.off_row = take(kWarpN * sizeof(float));
+  L.off_row = take(kWarpRowFloats * sizeof(float));
   L.off_vec = take(kWarpN * sizeof(float));
   L.off_xd = take(kWarpN * sizeof(df));
   L.total = o;

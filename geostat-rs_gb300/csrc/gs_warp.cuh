@@ -20,60 +20,83 @@
 #pragma once
 
 #include "gs_solve.cuh"
+#include "gs_pair.cuh"
 
 namespace gs {
 
 constexpr int kWarpN = 32;
+constexpr int kWarpN2 = kWarpN / 2;  // column pairs of a register row
+// Floats of the published-row buffer: two alternating rows of kWarpN
+// entries plus the pivot (padded to 16 bytes).
+constexpr int kWarpRowFloats = 2 * (kWarpN + 4);
 
 struct WarpScratch {
-  float* row;  // 32 (+1 for d) floats: the published pivot row
+  float* row;  // kWarpRowFloats floats: the published pivot rows
   float* vec;  // 32 floats: broadcast vector
-  df* xd;      // 32 df: solution
+  df* xd;      // 32 df: solution (during a refinement: its hi parts, then its lo parts)
 };
 
+constexpr int kWarpN4 = kWarpN / 4;  // column quads of a register row
+
 // The factorisation one lane holds: its row of the double-float matrix
-// (ah + al) and of -(sc A)^{-1} + 2I (t), with the power-of-two scale sc.
+// (ah + al) as column pairs and of -(sc A)^{-1} + 2I (t) as column quads
+// (so a published row is stored straight from aligned registers), with the
+// power-of-two scale sc.
 struct WarpFactor {
-  float ah[kWarpN], al[kWarpN], t[kWarpN];
+  float2 ah[kWarpN2], al[kWarpN2];
+  float4 t[kWarpN4];
   float sc;
 };
 
-// Loads row `lane` of the packed df matrix A (N x N) into registers; rows and
-// columns beyond N hold the identity.
-__device__ __forceinline__ void warp_load_rows(const df* A, int N, int lane, float (&ah)[kWarpN],
-                                               float (&al)[kWarpN]) {
-#pragma unroll
-  for (int j = 0; j < kWarpN; ++j) {
+// Loads row `lane` of a packed symmetric df matrix (N x N; at(e) returns
+// packed entry e) into registers; rows and columns beyond N hold the
+// identity.
+template <class At>
+__device__ __forceinline__ void warp_load_rows(At&& at, int N, int lane, float2 (&ah)[kWarpN2],
+                                               float2 (&al)[kWarpN2]) {
+  auto elt = [&](int j) {
     df v = df_make(j == lane ? 1.0f : 0.0f, 0.0f);
-    if (lane < N && j < N) v = lane >= j ? A[pk(lane, j)] : A[pk(j, lane)];
-    ah[j] = v.hi;
-    al[j] = v.lo;
+    if (lane < N && j < N) v = at(lane >= j ? pk(lane, j) : pk(j, lane));
+    return v;
+  };
+#pragma unroll
+  for (int j2 = 0; j2 < kWarpN2; ++j2) {
+    const df v0 = elt(2 * j2), v1 = elt(2 * j2 + 1);
+    ah[j2] = make_float2(v0.hi, v1.hi);
+    al[j2] = make_float2(v0.lo, v1.lo);
   }
 }
 
-__device__ __forceinline__ void warp_gemv_neg_inv(const float (&t)[kWarpN], const float* vec,
+__device__ __forceinline__ void warp_gemv_neg_inv(const float4 (&t)[kWarpN4], const float* vec,
                                                   int lane, float& y) {
-  // y = (-A^{-1}) v with the +2 diagonal offset removed
-  float s = 0.0f;
+  // y = (-A^{-1}) v with the +2 diagonal offset removed; packed FP32x2
+  // products into two accumulator pairs
+  float2 a0 = make_float2(0.0f, 0.0f), a1 = make_float2(0.0f, 0.0f);
 #pragma unroll
-  for (int j = 0; j < kWarpN; j += 4) {
-    const float4 v = *reinterpret_cast<const float4*>(vec + j);
-    s = fmaf(t[j], v.x, s);
-    s = fmaf(t[j + 1], v.y, s);
-    s = fmaf(t[j + 2], v.z, s);
-    s = fmaf(t[j + 3], v.w, s);
+  for (int q = 0; q < kWarpN4; ++q) {
+    const float4 v = *reinterpret_cast<const float4*>(vec + 4 * q);
+    a0 = __ffma2_rn(make_float2(t[q].x, t[q].y), make_float2(v.x, v.y), a0);
+    a1 = __ffma2_rn(make_float2(t[q].z, t[q].w), make_float2(v.z, v.w), a1);
   }
-  y = fmaf(-2.0f, vec[lane], s);
+  y = fmaf(-2.0f, vec[lane], (a0.x + a1.x) + (a0.y + a1.y));
 }
 
 // FP32 inverse of the packed df matrix A (N <= 32 unknowns).  Returns false
 // (uniformly in the warp) when a pivot is too small for FP32.
-__device__ __forceinline__ bool warp_factor(const df* A, int N, int lane, WarpFactor& f,
-                                            const WarpScratch& W) {
-  warp_load_rows(A, N, lane, f.ah, f.al);
+//
+// Pivot k: lane k publishes its row in one of two alternating buffers, with
+// the pivot entry replaced by d - 1 and d stored after the row; one
+// __syncwarp, then every lane applies its packed FP32x2 update.  Lane k's
+// next write to the same buffer (pivot k + 2) comes after the next pivot's
+// __syncwarp, which every lane reaches only after reading this row.
+template <class At>
+__device__ __forceinline__ bool warp_factor_at(At&& at, int N, int lane, WarpFactor& f,
+                                               const WarpScratch& W) {
+  warp_load_rows(at, N, lane, f.ah, f.al);
   float amax = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kWarpN; ++j) amax = fmaxf(amax, lane < N ? fabsf(f.ah[j]) : 0.0f);
+  for (int j2 = 0; j2 < kWarpN2; ++j2)
+    amax = fmaxf(amax, lane < N ? fmaxf(fabsf(f.ah[j2].x), fabsf(f.ah[j2].y)) : 0.0f);
   amax = warp_max_f(amax);
   f.sc = 1.0f;
   if (!(amax > 0.0f)) return false;
@@ -83,35 +106,51 @@ __device__ __forceinline__ bool warp_factor(const df* A, int N, int lane, WarpFa
   int ex = 0;
   frexpf(amax, &ex);
   f.sc = ldexpf(1.0f, -ex);
+  auto scaled = [&](int j) {
+    const float v = (j & 1) ? f.ah[j >> 1].y : f.ah[j >> 1].x;
+    return (lane < N && j < N) ? v * f.sc : v;
+  };
 #pragma unroll
-  for (int j = 0; j < kWarpN; ++j) f.t[j] = (lane < N && j < N) ? f.ah[j] * f.sc : f.ah[j];
+  for (int q = 0; q < kWarpN4; ++q)
+    f.t[q] = make_float4(scaled(4 * q), scaled(4 * q + 1), scaled(4 * q + 2), scaled(4 * q + 3));
   const float tol = 1e-6f * amax * f.sc;
+  __syncwarp();  // the previous user of W.row is done with it
   for (int k = 0; k < N; ++k) {
+    float* rb = W.row + (k & 1) * (kWarpN + 4);
     if (lane == k) {
 #pragma unroll
-      for (int j = 0; j < kWarpN; j += 4)
-        *reinterpret_cast<float4*>(W.row + j) =
-            make_float4(f.t[j], f.t[j + 1], f.t[j + 2], f.t[j + 3]);
+      for (int q = 0; q < kWarpN4; ++q) *reinterpret_cast<float4*>(rb + 4 * q) = f.t[q];
+      const float d = rb[k];  // this lane's own store
+      rb[k] = d - 1.0f;
+      rb[kWarpN] = d;
     }
     __syncwarp();
-    const float d = W.row[k];
-    __syncwarp();
-    if (lane == k) W.row[k] = d - 1.0f;
-    __syncwarp();
+    const float d = rb[kWarpN];
     if (!(fabsf(d) > tol)) return false;  // the same value in every lane
     const float invd = __fdividef(1.0f, d);  // an approximate inverse suffices
-    const float l = lane == k ? 1.0f - invd : W.row[lane] * invd;
+    const float l = lane == k ? 1.0f - invd : rb[lane] * invd;
+    const float2 nl = make_float2(-l, -l);
 #pragma unroll
-    for (int j = 0; j < kWarpN; j += 4) {
-      const float4 r = *reinterpret_cast<const float4*>(W.row + j);
-      f.t[j] = fmaf(-l, r.x, f.t[j]);
-      f.t[j + 1] = fmaf(-l, r.y, f.t[j + 1]);
-      f.t[j + 2] = fmaf(-l, r.z, f.t[j + 2]);
-      f.t[j + 3] = fmaf(-l, r.w, f.t[j + 3]);
+    for (int q = 0; q < kWarpN4; ++q) {
+      const float4 r = *reinterpret_cast<const float4*>(rb + 4 * q);
+      const float2 u0 = __ffma2_rn(nl, make_float2(r.x, r.y), make_float2(f.t[q].x, f.t[q].y));
+      const float2 u1 = __ffma2_rn(nl, make_float2(r.z, r.w), make_float2(f.t[q].z, f.t[q].w));
+      f.t[q] = make_float4(u0.x, u0.y, u1.x, u1.y);
     }
-    __syncwarp();
   }
+  __syncwarp();
   return true;
+}
+
+// The matrix as packed df entries.
+__device__ __forceinline__ bool warp_factor(const df* A, int N, int lane, WarpFactor& f,
+                                            const WarpScratch& W) {
+  return warp_factor_at([&](int e) { return A[e]; }, N, lane, f, W);
+}
+// The matrix as packed entries split into hi parts Ah[e] and lo parts Al[e].
+__device__ __forceinline__ bool warp_factor(const float* Ah, const float* Al, int N, int lane,
+                                            WarpFactor& f, const WarpScratch& W) {
+  return warp_factor_at([&](int e) { return df_make(Ah[e], Al[e]); }, N, lane, f, W);
 }
 
 // Refinement sweeps before a system is handed to the FP64 solver; a sweep
@@ -149,24 +188,36 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
   const float nx = warp_max_f(fabsf(x.hi));
   float nd_prev = nx;
   for (int sweep = 1; sweep <= kMaxRefineSweeps; ++sweep) {
-    // residual of row `lane`: b - A x, compensated, x broadcast as df
+    // residual of row `lane`: b - A x, compensated (Dot2) in packed FP32x2
+    // over column pairs: two accumulator lanes (even and odd columns) with
+    // their compensations, joined by one more error-free sum.  x is
+    // broadcast negated and split (hi parts, then lo parts) so a 16-byte load
+    // gives the operands of two column pairs.
+    float* xs = reinterpret_cast<float*>(W.xd);
     __syncwarp();
-    W.xd[lane] = x;
+    xs[lane] = -x.hi;
+    xs[kWarpN + lane] = -x.lo;
     __syncwarp();
-    float s = lane < N ? B[lane].hi : 0.0f, c = lane < N ? B[lane].lo : 0.0f;
+    float2 s2 = make_float2(lane < N ? B[lane].hi : 0.0f, 0.0f);
+    float2 c2 = make_float2(lane < N ? B[lane].lo : 0.0f, 0.0f);
+    auto acc = [&](float2 ah, float2 al, float2 xh, float2 xl) {
+      const float2 ph = __fmul2_rn(ah, xh);
+      float2 pe = __ffma2_rn(ah, xh, p_neg(ph));
+      pe = __ffma2_rn(ah, xl, pe);
+      pe = __ffma2_rn(al, xh, pe);
+      const dfp ts = p_two_sum(s2, ph);
+      s2 = ts.hi;
+      c2 = p_add(c2, p_add(ts.lo, pe));
+    };
 #pragma unroll
-    for (int j = 0; j < kWarpN; ++j) {
-      const df xj = W.xd[j];
-      const float ph = __fmul_rn(-f.ah[j], xj.hi);
-      float pe = __fmaf_rn(-f.ah[j], xj.hi, -ph);
-      pe = __fmaf_rn(-f.ah[j], xj.lo, pe);
-      pe = __fmaf_rn(-f.al[j], xj.hi, pe);
-      const float tsum = __fadd_rn(s, ph);
-      const float bb = __fsub_rn(tsum, s);
-      const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(tsum, bb)), __fsub_rn(ph, bb));
-      s = tsum;
-      c += e + pe;
+    for (int j = 0; j < kWarpN; j += 4) {
+      const float4 xh = *reinterpret_cast<const float4*>(xs + j);
+      const float4 xl = *reinterpret_cast<const float4*>(xs + kWarpN + j);
+      acc(f.ah[j >> 1], f.al[j >> 1], make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
+      acc(f.ah[(j >> 1) + 1], f.al[(j >> 1) + 1], make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
     }
+    const df st = two_sum(s2.x, s2.y);
+    const float s = st.hi, c = (c2.x + c2.y) + st.lo;
     const float r = lane < N ? s + c : 0.0f;
     __syncwarp();
     W.vec[lane] = r;
@@ -189,9 +240,17 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
       if (at_floor) *at_floor = !done;
       return true;
     }
-    if (stalled) return false;
+    if (stalled) {
+      __syncwarp();
+      W.xd[lane] = x;  // the last iterate, for a caller that refines further
+      __syncwarp();
+      return false;
+    }
     nd_prev = nd;
   }
+  __syncwarp();
+  W.xd[lane] = x;
+  __syncwarp();
   return false;
 }
 
