@@ -161,6 +161,22 @@ __device__ __forceinline__ void shell_offset(int r, int s, int* o) {
   }
 }
 
+// Rings whose cell offsets the search reads from a table (built once per
+// block) instead of deriving them with integer divisions: rings 0..4 in 3-D
+// (9^3 cells), 0..8 in 2-D (17^2 cells).  Offset (o0, o1, o2) is packed as
+// (o0 + 128) | (o1 + 128) << 8 | (o2 + 128) << 16; ring r starts at entry
+// (2r - 1)^D.
+template <int D>
+struct ShellTab {
+  static constexpr int kRings = D == 3 ? 4 : 8;
+  static constexpr int kEntries = D == 3 ? 729 : 289;
+};
+template <int D>
+__device__ __forceinline__ int shell_start(int r) {
+  const int w = 2 * r - 1;
+  return r == 0 ? 0 : (D == 3 ? w * w * w : w * w);
+}
+
 template <int D>
 __device__ __forceinline__ int shell_size(int r) {
   if (r == 0) return 1;
@@ -185,12 +201,28 @@ __device__ __forceinline__ float prefilter_bound(double T, float delta, int D) {
   return __fmul_ru(b, 1.0f + 1e-6f);
 }
 
+// Per-target set-up of the search (FP64 frame coordinates, cell, FP32
+// prefilter coordinates and bounds), computed for a warp's group of targets
+// one lane per target and read by the whole warp when it reaches the target.
+struct TargetSetup {
+  double q[3];
+  int tc[3];
+  float qf[3];
+  float delta, r2f;
+  int pad[2];
+};
+// Targets per warp group (the lanes that compute set-ups side by side).
+constexpr int kSearchGroup = 32;
+
 // Shared memory of one warp of knn_kernel: NB buffers of capb (d2, idx)
 // entries, then NB thresholds, counts and dirty flags, the cached prefilter
-// bound, and a queue of 64 prefilter survivors.  Used by both the kernel and
-// its launch.
+// bound, a queue of 64 prefilter survivors and the group's target set-ups.
+// Used by both the kernel and its launch.
+__host__ __device__ inline size_t knn_setup_offset(int NB, int capb) {
+  return ((size_t)NB * capb * 12 + (size_t)NB * 16 + 16 + 64 * sizeof(uint32_t) + 15) & ~(size_t)15;
+}
 __host__ __device__ inline size_t knn_per_warp(int NB, int capb) {
-  return (size_t)NB * capb * 12 + (size_t)NB * 16 + 16 + 64 * sizeof(uint32_t);
+  return knn_setup_offset(NB, capb) + kSearchGroup * sizeof(TargetSetup);
 }
 
 // Squared distances are never negative (and never -0: they are sums of
@@ -250,9 +282,21 @@ __device__ __noinline__ void warp_sort(dkey* key, uint32_t* id, int n_valid, int
 }
 
 template <int D, bool OCT, bool RANKED>
-__global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, SearchParams p,
-                                                  int64_t nt, const double* tx, const double* ty,
-                                                  const double* tz, int32_t* nb, int32_t* nbc) {
+// Blocks per SM the compiler plans registers for, measured on GB300: eight
+// for the single-buffer search (64 registers, a few values spilled: 9 %
+// faster than the 80-96 registers the compiler takes unbounded; ten and
+// twelve were slower again), four for the octant search (18 % faster than
+// unbounded, six slower).
+#ifndef GS_KNN_MINB
+#define GS_KNN_MINB 8
+#endif
+#ifndef GS_KNN_MINB_OCT
+#define GS_KNN_MINB_OCT 4
+#endif
+__global__ void __launch_bounds__(128, OCT ? GS_KNN_MINB_OCT : GS_KNN_MINB) knn_kernel(GridDev g, SearchFrame fr, SearchParams p,
+                                                  int64_t nt, int gs, const double* tx,
+                                                  const double* ty, const double* tz, int32_t* nb,
+                                                  int32_t* nbc) {
   constexpr int NB = OCT ? (1 << D) : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -268,30 +312,63 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
   int* dirty = cnt + NB;
   float* tfs = reinterpret_cast<float*>(dirty + NB);  // cached prefilter bound
   uint32_t* sq = reinterpret_cast<uint32_t*>(tfs + 4);  // prefilter survivors (64)
+  TargetSetup* tset = reinterpret_cast<TargetSetup*>(base + knn_setup_offset(NB, capb));
+  __shared__ uint32_t shell_tab[ShellTab<D>::kEntries];
+  for (int r = 0; r <= ShellTab<D>::kRings; ++r) {
+    const int S = shell_size<D>(r), s0 = shell_start<D>(r);
+    for (int q = threadIdx.x; q < S; q += blockDim.x) {
+      int o[3];
+      shell_offset<D>(r, q, o);
+      shell_tab[s0 + q] = (uint32_t)(o[0] + 128) | ((uint32_t)(o[1] + 128) << 8) |
+                          ((uint32_t)(o[2] + 128) << 16);
+    }
+  }
+  __syncthreads();
   const double kInf = __longlong_as_double(0x7ff0000000000000ll);
   const double r2 = p.has_radius ? p.r2 : kInf;
   const dkey r2k = d2key(r2);
   const int kb = p.k;
 
-  for (int64_t t = (int64_t)blockIdx.x * wpb + wib; t < nt; t += (int64_t)gridDim.x * wpb) {
-    double pt[3] = {tx[t], ty[t], D == 3 ? tz[t] : 0.0};
-    double q[3];
-    to_search_frame<D>(fr, pt, q);
-    int tc[3] = {0, 0, 0};
-#pragma unroll
-    for (int d = 0; d < D; ++d) tc[d] = clamp_cell((q[d] - g.origin[d]) * g.inv_cell, g.n[d]);
-    // prefilter: FP32 target coordinates and the per-axis error bound
-    float qf[3] = {0.0f, 0.0f, 0.0f};
+  // A warp takes gs consecutive targets at a time; their FP64 set-up runs one
+  // lane per target (the same operations a lane-redundant set-up would do,
+  // at 1/gs of the FP64 issue).
+  for (int64_t g0 = ((int64_t)blockIdx.x * wpb + wib) * gs; g0 < nt;
+       g0 += (int64_t)gridDim.x * wpb * gs) {
+  const int gn = (int)min((int64_t)gs, nt - g0);
+  __syncwarp();
+  if (lane < gn) {
+    const int64_t t = g0 + lane;
+    const double pt[3] = {tx[t], ty[t], D == 3 ? tz[t] : 0.0};
+    TargetSetup& su = tset[lane];
+    to_search_frame<D>(fr, pt, su.q);
     float delta = 0.0f;
 #pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      su.tc[d] = 0;
+      su.qf[d] = 0.0f;
+    }
+#pragma unroll
     for (int d = 0; d < D; ++d) {
-      const double rel = q[d] - g.origin[d];
-      qf[d] = (float)rel;
+      su.tc[d] = clamp_cell((su.q[d] - g.origin[d]) * g.inv_cell, g.n[d]);
+      // prefilter: FP32 target coordinates and the per-axis error bound
+      const double rel = su.q[d] - g.origin[d];
+      su.qf[d] = (float)rel;
       // (extent + |rel|) * 2^-23, rounded up
       const float mag = __fadd_ru(g.extf[d], __double2float_ru(fabs(rel)));
       delta = fmaxf(delta, __fadd_ru(mag * (1.0f / 8388608.0f), 1e-30f));
     }
-    const float r2f = prefilter_bound(r2, delta, D);
+    su.delta = delta;
+    su.r2f = prefilter_bound(r2, delta, D);
+  }
+  __syncwarp();
+  for (int j = 0; j < gn; ++j) {
+    const int64_t t = g0 + j;
+    const TargetSetup& su = tset[j];
+    const double q[3] = {su.q[0], su.q[1], D == 3 ? su.q[2] : 0.0};
+    const int tc[3] = {su.tc[0], su.tc[1], su.tc[2]};
+    const float qf[3] = {su.qf[0], su.qf[1], su.qf[2]};
+    const float delta = su.delta;
+    const float r2f = su.r2f;
     int maxring = 0;
 #pragma unroll
     for (int d = 0; d < D; ++d) maxring = max(maxring, max(tc[d], g.n[d] - 1 - tc[d]));
@@ -441,7 +518,14 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
         uint32_t cst = 0;
         if (s < S) {
           int o[3];
-          shell_offset<D>(ring, s, o);
+          if (ring <= ShellTab<D>::kRings) {
+            const uint32_t v = shell_tab[shell_start<D>(ring) + s];
+            o[0] = (int)(v & 0xffu) - 128;
+            o[1] = (int)((v >> 8) & 0xffu) - 128;
+            o[2] = (int)((v >> 16) & 0xffu) - 128;
+          } else {
+            shell_offset<D>(ring, s, o);
+          }
           int c[3] = {tc[0] + o[0], tc[1] + o[1], tc[2] + o[2]};
           bool ok = true;
 #pragma unroll
@@ -559,12 +643,13 @@ __global__ void __launch_bounds__(128) knn_kernel(GridDev g, SearchFrame fr, Sea
     }
     const int kout = p.kout;
     const int outn = min(total, kout);
-    for (int j = lane; j < kout; j += 32) nb[t * kout + j] = j < outn ? (int32_t)bid[j] : -1;
+    for (int jj = lane; jj < kout; jj += 32) nb[t * kout + jj] = jj < outn ? (int32_t)bid[jj] : -1;
     if (lane == 0) {
       bool overflow = p.unbounded && inrad > (long long)kout;
       nbc[t] = overflow ? -1 : outn;
     }
     __syncwarp();
+  }
   }
 }
 
@@ -758,11 +843,16 @@ int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p
   size_t smem = per_warp * wpb;
   static const size_t kMaxSmem = 227 * 1024;
   if (smem > kMaxSmem) return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood too large for the device search");
-  int64_t blocks64 = (nt + wpb - 1) / wpb;
+  // targets per warp group: up to 32 once there are 16 warps' worth of
+  // groups per SM, fewer for small batches (latency)
+  const int64_t warps_full = (int64_t)sm_count() * 16;
+  const int gs = (int)std::min<int64_t>(kSearchGroup, std::max<int64_t>(1, (nt + warps_full - 1) / warps_full));
+  const int64_t groups = (nt + gs - 1) / gs;
+  int64_t blocks64 = (groups + wpb - 1) / wpb;
   int blocks = (int)std::min<int64_t>(blocks64, (int64_t)sm_count() * 64);
   auto launch = [&](auto kern) -> int {
     GS_TRY(allow_dynamic_smem((const void*)kern, smem));
-    kern<<<blocks, wpb * 32, smem, stream>>>(g.dev, frame, p, nt, tx, ty, tz, nb, nbc);
+    kern<<<blocks, wpb * 32, smem, stream>>>(g.dev, frame, p, nt, gs, tx, ty, tz, nb, nbc);
     GS_CUDA(cudaGetLastError());
     count_launch(1);
     return GS_OK;

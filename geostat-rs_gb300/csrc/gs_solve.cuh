@@ -143,12 +143,18 @@ __device__ __forceinline__ void cov_from_norm2(const DevModel& m, df h0, df h1,
                                                const ExpTable& tab, const DfConsts& k, df& c0,
                                                df& c1) {
   const dfp h = dp_pack(h0, h1);
+  auto term = [&](const DevStruct& st) {
+    return dp_mul(dp_rho(st.kind, dp_mul(h, dp_splat(st.inv_range_df)), tab, k),
+                  dp_splat(st.sill_df));
+  };
+  // the first structure's term as is (adding it to zero would return it
+  // unchanged), the others summed onto it (>= 0 terms); a pure nugget model
+  // has no structure and covariance 0 off the origin
   dfp c = dp_zero();
+  if (m.ns > 0) {
+    c = term(m.s[0]);
 #pragma unroll 1
-  for (int s = 0; s < m.ns; ++s) {
-    const DevStruct& st = m.s[s];
-    const dfp r = dp_rho(st.kind, dp_mul(h, dp_splat(st.inv_range_df)), tab, k);
-    c = dp_add_fast(c, dp_mul(r, dp_splat(st.sill_df)));  // >= 0 terms
+    for (int s = 1; s < m.ns; ++s) c = dp_add_fast(c, term(m.s[s]));
   }
   c0 = dp_first(c);
   c1 = dp_second(c);
