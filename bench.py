@@ -410,6 +410,13 @@ def cv_bench(args, coords, values, model, log):
         cv = G.leave_one_out(ps, model, cfg)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
+    out64 = k.predict_many(t, "fp64", full=True)
+    ts64 = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        out64 = k.predict_many(t, "fp64", full=True)
+        ts64.append(time.perf_counter() - t1)
+    dt64 = statistics.median(ts64)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     O.build()
@@ -442,8 +449,10 @@ def global_bench(args, log):
     """Global-neighbourhood ordinary kriging (kriging.rs:396-406): the 2-D
     workload's 2,000 points (uniform in 1000 x 1000 m, 10 + field, nugget 0.1 +
     Sph(1, 200 m)) with no neighbour limit -- one 2,001-unknown system factored
-    at build -- predicted at the 100 x 100 grid; the oracle (the same global LU
-    path) on all host cores."""
+    at build -- predicted at the 100 x 100 grid: the mixed path (the system's
+    matrix-product form: FP64 dot products for estimates, a double-float GEMM
+    for variances) and the FP64 build (per-target solves with the LU
+    factors); the oracle (the same global LU path) on all host cores."""
     import geostat_rs as G
     from geostat_rs.model import Structure, VariogramModel
     n = 2000
@@ -463,6 +472,13 @@ def global_bench(args, log):
         out = k.predict_many(t, full=True)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
+    out64 = k.predict_many(t, "fp64", full=True)
+    ts64 = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        out64 = k.predict_many(t, "fp64", full=True)
+        ts64.append(time.perf_counter() - t1)
+    dt64 = statistics.median(ts64)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     O.build()
@@ -473,12 +489,18 @@ def global_bench(args, log):
     vs = float(np.mean(np.abs(v)))
     rel = lambda a, b, f: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), f)))
     log(f"[bench] global neighbourhood: build {build * 1e3:.0f} ms, {len(t)} targets in "
-        f"{dt * 1e3:.1f} ms; oracle {dcpu:.2f} s on {cores} threads")
+        f"{dt * 1e3:.1f} ms (fp64 build {dt64 * 1e3:.1f} ms); oracle {dcpu:.2f} s on {cores} threads")
     return {"data": n, "unknowns": n + 1, "targets": len(t), "build_seconds": build,
             "predict_seconds": dt, "targets_per_s": len(t) / dt,
+            "includes": "host buffers in and out, copies included",
+            "fp64_gpu_build": {"predict_seconds": dt64, "targets_per_s": len(t) / dt64,
+                               "mixed_over_fp64": dt64 / dt,
+                               "max_rel_value": rel(out64.value, ref["value"], vs),
+                               "max_rel_variance": rel(out64.variance, ref["variance"], 1e-3)},
             "cpu_targets_per_s": len(t) / dcpu, "cpu_cores": cores, "cpu_seconds_incl_factor": dcpu,
             "max_rel_value": rel(out.value, ref["value"], vs),
-            "max_rel_variance": rel(out.variance, ref["variance"], 1e-3)}
+            "max_rel_variance": rel(out.variance, ref["variance"], 1e-3),
+            "max_rel_lagrange": rel(out.lagrange, ref["lagrange"], 1.0)}
 
 
 def block_bench(args, log):
@@ -502,6 +524,13 @@ def block_bench(args, log):
         val, var = k.predict_block_grid(lo, hi, nc, bs, disc)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
+    out64 = k.predict_many(t, "fp64", full=True)
+    ts64 = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        out64 = k.predict_many(t, "fp64", full=True)
+        ts64.append(time.perf_counter() - t1)
+    dt64 = statistics.median(ts64)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     from geostat_rs.io import grid_centers

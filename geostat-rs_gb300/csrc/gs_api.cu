@@ -498,6 +498,27 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
         k->lu_n = (int)N;
         k->lu_state = state;
       }
+      // the matrix-product form for mixed-precision calls (a factored,
+      // non-singular system); without room for it those calls take the
+      // per-target solves too
+      if (!rc && state == 1) {
+        const size_t nn = (size_t)N * N;
+        if (dev_malloc((void**)&k->d_rh, nn * 4) == cudaSuccess &&
+            dev_malloc((void**)&k->d_rl, nn * 4) == cudaSuccess &&
+            dev_malloc((void**)&k->d_lambda, (size_t)N * 8) == cudaSuccess &&
+            dev_malloc((void**)&k->d_arow, (size_t)N * 8) == cudaSuccess) {
+          rc = global_gemm_prepare(gs::base_args(k), (int)N, k->d_lu, k->d_perm, k->d_rh,
+                                   k->d_rl, k->d_lambda, k->d_arow, k->stream);
+        } else {
+          cudaGetLastError();  // clear the failed allocation
+          cudaFree(k->d_rh);
+          cudaFree(k->d_rl);
+          cudaFree(k->d_lambda);
+          cudaFree(k->d_arow);
+          k->d_rh = k->d_rl = nullptr;
+          k->d_lambda = k->d_arow = nullptr;
+        }
+      }
     }
   }
   if (rc) {
@@ -689,7 +710,8 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     const int64_t warps = std::max<int64_t>(
         1, std::min<int64_t>((int64_t)sm_count() * 32, ((int64_t)512 << 20) / (16 * (int64_t)N)));
     DevBuf scratch;
-    GS_TRY(scratch.alloc((size_t)warps * 2 * N * 8, stream));
+    const bool gemm = precision != GS_PREC_FP64 && k->lu_state == 1 && k->d_rh;
+    if (!gemm) GS_TRY(scratch.alloc((size_t)warps * 2 * N * 8, stream));
     KrigeArgs g = a;
     g.tx = tx;
     g.ty = ty;
@@ -706,8 +728,12 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
       GS_CUDA(cudaEventCreate(&e1));
       GS_CUDA(cudaEventRecord(e0, stream));
     }
-    GS_TRY(global_solve_launch(g, k->dm, N, k->d_lu, k->d_perm, k->lu_state,
-                               (double*)scratch.ptr, warps, stream));
+    if (gemm) {
+      GS_TRY(global_gemm_launch(g, k->dm, N, k->d_rh, k->d_rl, k->d_lambda, k->d_arow, stream));
+    } else {
+      GS_TRY(global_solve_launch(g, k->dm, N, k->d_lu, k->d_perm, k->lu_state,
+                                 (double*)scratch.ptr, warps, stream));
+    }
     if (!timed) return GS_OK;
     GS_CUDA(cudaEventRecord(e1, stream));
     GS_CUDA(cudaEventSynchronize(e1));

@@ -1305,6 +1305,268 @@ __global__ void global_solve_kernel(KrigeArgs a, DevModel m, int N, const double
   }
 }
 
+// ----------------------------------------- global neighbourhood, GEMM form --
+// For a factored global system a predict call's work is one matrix product.
+// At build the solves of A x = e_j with the LU factors (one warp per column,
+// the substitutions of global_solve_kernel) give R, row j = A^{-1} e_j, so
+// x = R^T b for any right-hand side b; R is kept split into FP32 hi / lo
+// parts, with lambda = R z (z the data values, or z - mean for simple
+// kriging, and 0 on the drift rows) and a = R e_n (the first drift row's
+// column).  Per target with right-hand side b (kriging.rs:580-598):
+//     estimate  = lambda . b   (+ mean, simple kriging),
+//     Lagrange  = a . b,
+//     variance  = C(0) - b^T R b,
+// the first two as FP64 dot products, the quadratic form through X = R B
+// for a tile of targets: a double-float GEMM on the CUDA cores (compensated
+// Dot2 accumulation in packed FP32x2 arithmetic) whose epilogue forms
+// sum_i B_it X_it per row tile; the row tiles' partial sums are added in a
+// fixed order.  b^T R b equals b^T x of the reference's solve
+// (kriging.rs:614-643: C(0) - w . c - mu . f).
+
+// Column j of A^{-1} for j = w, w + nw, ...: row j of R.
+__global__ void global_inverse_kernel(int N, const double* LU, const int32_t* perm, double* R,
+                                      double* scratch, int64_t nwarps_scratch) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  if (w0 >= nwarps_scratch) return;
+  double* Y = scratch + w0 * (int64_t)N;
+  for (int64_t j = w0; j < N; j += nw) {
+    for (int i = lane; i < N; i += 32) Y[i] = perm[i] == (int)j ? 1.0 : 0.0;
+    __syncwarp();
+    for (int i = 1; i < N; ++i) {
+      const double* Li = LU + (int64_t)i * N;
+      double sum = 0.0;
+      for (int q = lane; q < i; q += 32) sum = fma(Li[q], Y[q], sum);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) Y[i] -= sum;
+      __syncwarp();
+    }
+    for (int i = N - 1; i >= 0; --i) {
+      const double* Ui = LU + (int64_t)i * N;
+      double sum = 0.0;
+      for (int q = i + 1 + lane; q < N; q += 32) sum = fma(Ui[q], Y[q], sum);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) Y[i] = (Y[i] - sum) / Ui[i];
+      __syncwarp();
+    }
+    for (int i = lane; i < N; i += 32) R[j * N + i] = Y[i];
+    __syncwarp();
+  }
+}
+
+// lambda = R z (one warp per row), a = R e_n, and R split into hi / lo.
+__global__ void global_vectors_kernel(int N, int n, int p, int simple, double mean,
+                                      const double* val, const double* R, double* lambda,
+                                      double* arow, float* Rh, float* Rl) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = w0; i < N; i += nw) {
+    const double* Ri = R + i * N;
+    double sum = 0.0;
+    for (int j = lane; j < n; j += 32) sum = fma(Ri[j], simple ? val[j] - mean : val[j], sum);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) {
+      lambda[i] = sum;
+      arow[i] = p > 0 ? Ri[n] : 0.0;
+    }
+    for (int j = lane; j < N; j += 32) {
+      const double r = Ri[j];
+      const float h = (float)r;
+      Rh[i * N + j] = h;
+      Rl[i * N + j] = (float)(r - (double)h);
+    }
+  }
+}
+
+// Right-hand sides of a tile of targets, split: Bh/Bl[i * T + t] (i < N
+// system rows, t < T targets of this chunk).
+template <int D>
+__global__ void global_rhs_kernel(KrigeArgs a, DevModel m, int N, int64_t T, float* Bh, float* Bl) {
+  const int n = (int)a.n;
+  const int64_t total = (int64_t)N * T;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / T, t = e - i * T;
+    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+    double b;
+    if (i < n) {
+      const double h[3] = {a.x[i] - tp[0], a.y[i] - tp[1], D == 3 ? a.z[i] - tp[2] : 0.0};
+      b = cov_fp64<D>(m, h);
+    } else {
+      b = basis_at<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, (int)(i - n));
+    }
+    const float h = (float)b;
+    Bh[e] = h;
+    Bl[e] = (float)(b - (double)h);
+  }
+}
+
+// Tiles of the quadratic form: block (bx, by) multiplies rows
+// [64 by, 64 by + 64) of R with the targets [64 bx, 64 bx + 64) of B over
+// all N columns, 16 columns per stage, each thread a 4 x 4 block of X in
+// double-float (two FP32x2 accumulator pairs per row, compensated), and
+// writes sum_i B_it X_it over its row tile to Q[by * T + t] (hi, lo).
+constexpr int kGT = 64;   // rows / targets per tile
+constexpr int kGK = 16;   // columns per stage
+__global__ void __launch_bounds__(256) global_quad_kernel(int N, int64_t T, const float* Rh,
+                                                         const float* Rl, const float* Bh,
+                                                         const float* Bl, df* Q) {
+  __shared__ __align__(16) float Ms[2][kGK][kGT + 4];
+  __shared__ __align__(16) float Bs[2][kGK][kGT + 4];
+  __shared__ df red[16][kGT];
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int64_t i0 = (int64_t)blockIdx.y * kGT, t0 = (int64_t)blockIdx.x * kGT;
+  float2 s[4][2], c[4][2];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      s[r][q] = make_float2(0.0f, 0.0f);
+      c[r][q] = make_float2(0.0f, 0.0f);
+    }
+  for (int k0 = 0; k0 < N; k0 += kGK) {
+    for (int e = tid; e < kGT * kGK; e += 256) {
+      const int r = e / kGK, kk = e % kGK;
+      const int64_t gi = i0 + r;
+      const int gk = k0 + kk;
+      float h = 0.0f, l = 0.0f;
+      if (gi < N && gk < N) {
+        h = Rh[gi * N + gk];
+        l = Rl[gi * N + gk];
+      }
+      Ms[0][kk][r] = h;
+      Ms[1][kk][r] = l;
+    }
+    for (int e = tid; e < kGK * kGT; e += 256) {
+      const int kk = e / kGT, tt = e % kGT;
+      const int gk = k0 + kk;
+      const int64_t gt = t0 + tt;
+      float h = 0.0f, l = 0.0f;
+      if (gk < N && gt < T) {
+        h = Bh[(int64_t)gk * T + gt];
+        l = Bl[(int64_t)gk * T + gt];
+      }
+      Bs[0][kk][tt] = h;
+      Bs[1][kk][tt] = l;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kGK; ++kk) {
+      const float4 mh = *reinterpret_cast<const float4*>(&Ms[0][kk][ty * 4]);
+      const float4 ml = *reinterpret_cast<const float4*>(&Ms[1][kk][ty * 4]);
+      const float4 bh = *reinterpret_cast<const float4*>(&Bs[0][kk][tx * 4]);
+      const float4 bl = *reinterpret_cast<const float4*>(&Bs[1][kk][tx * 4]);
+      const float ah[4] = {mh.x, mh.y, mh.z, mh.w}, al[4] = {ml.x, ml.y, ml.z, ml.w};
+      const float2 bh2[2] = {make_float2(bh.x, bh.y), make_float2(bh.z, bh.w)};
+      const float2 bl2[2] = {make_float2(bl.x, bl.y), make_float2(bl.z, bl.w)};
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const float2 a2 = make_float2(ah[r], ah[r]), l2 = make_float2(al[r], al[r]);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float2 ph = __fmul2_rn(a2, bh2[q]);
+          float2 pe = __ffma2_rn(a2, bh2[q], p_neg(ph));
+          pe = __ffma2_rn(a2, bl2[q], pe);
+          pe = __ffma2_rn(l2, bh2[q], pe);
+          const dfp ts = p_two_sum(s[r][q], ph);
+          s[r][q] = ts.hi;
+          c[r][q] = p_add(c[r][q], p_add(ts.lo, pe));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // epilogue: this thread's rows' contribution sum_r B_(i0+4ty+r),t X_r,t
+  df part[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) part[u] = df_make(0.0f, 0.0f);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int64_t gi = i0 + ty * 4 + r;
+    if (gi >= N) continue;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const df x0 = fast_two_sum(s[r][q].x, c[r][q].x), x1 = fast_two_sum(s[r][q].y, c[r][q].y);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int u = 2 * q + h;
+        const int64_t gt = t0 + tx * 4 + u;
+        if (gt >= T) continue;
+        const df b = df_make(Bh[gi * T + gt], Bl[gi * T + gt]);
+        part[u] = df_add(part[u], df_mul(b, h ? x1 : x0));
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) red[ty][tx * 4 + u] = part[u];
+  __syncthreads();
+  if (tid < kGT) {
+    df sum = red[0][tid];
+    for (int w = 1; w < 16; ++w) sum = df_add(sum, red[w][tid]);
+    const int64_t gt = t0 + tid;
+    if (gt < T) Q[blockIdx.y * T + gt] = sum;
+  }
+}
+
+// Outputs of a tile of targets: one warp per target; FP64 right-hand side,
+// lambda . b and a . b in FP64, the quadratic form from the row tiles'
+// partial sums in tile order.
+template <int D>
+__global__ void global_finish_kernel(KrigeArgs a, DevModel m, int N, int64_t T, int ntiles,
+                                     const double* lambda, const double* arow, const df* Q) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int n = (int)a.n, p = a.p;
+  const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
+  for (int64_t t = w0; t < T; t += nw) {
+    uint8_t st = GS_ST_OK;
+    if (n < a.min_nb) st = GS_ST_NO_NEIGHBORS;
+    else if (n < p) st = GS_ST_INSUFFICIENT_DATA;
+    if (st != GS_ST_OK) {
+      if (lane == 0) {
+        a.out_v[t] = kNaN;
+        a.out_var[t] = kNaN;
+        if (a.out_lag) a.out_lag[t] = kNaN;
+        a.out_st[t] = st;
+      }
+      continue;
+    }
+    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+    const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
+    double v = 0.0, lg = 0.0;
+    for (int i = lane; i < N; i += 32) {
+      double b;
+      if (i < n) {
+        const double h[3] = {a.x[i] - tp[0], a.y[i] - tp[1], D == 3 ? a.z[i] - tp[2] : 0.0};
+        b = cov_fp64<D>(m, h);
+      } else {
+        b = basis_at<D>(a, tp, trow, i - n);
+      }
+      v = fma(lambda[i], b, v);
+      lg = fma(arow[i], b, lg);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+      lg += __shfl_xor_sync(0xffffffffu, lg, o);
+    }
+    if (lane == 0) {
+      df q = Q[t];
+      for (int r = 1; r < ntiles; ++r) q = df_add(q, Q[(int64_t)r * T + t]);
+      a.out_v[t] = a.method == GS_SIMPLE ? a.sk_mean + v : v;
+      a.out_var[t] = fmax(m.c0 - df_to_double(q), 0.0);
+      if (a.out_lag) a.out_lag[t] = a.method == GS_SIMPLE ? kNaN : lg;
+      a.out_st[t] = GS_ST_OK;
+    }
+  }
+}
+
 template <int D>
 __global__ void grid_centers_kernel(double x0, double y0, double z0, double dx, double dy,
                                     double dz, int64_t nx, int64_t ny, int64_t total, double* x,
@@ -1468,6 +1730,71 @@ int global_solve_launch(const KrigeArgs& a, const DevModel& m, int N, const doub
     global_solve_kernel<3><<<blocks, 128, 0, stream>>>(a, m, N, LU, perm, state, scratch, warps);
   GS_CUDA(cudaGetLastError());
   count_launch(1);
+  return GS_OK;
+}
+
+int global_gemm_prepare(const KrigeArgs& a, int N, const double* LU, const int32_t* perm,
+                        float* Rh, float* Rl, double* lambda, double* arow, cudaStream_t stream) {
+  NvtxRange nvtx_range("gs.global_gemm_prepare");
+  DevBuf R, scratch;
+  GS_TRY(R.alloc((size_t)N * N * 8, stream));
+  const int64_t warps = std::max<int64_t>(
+      1, std::min<int64_t>({(int64_t)sm_count() * 32, (int64_t)N, ((int64_t)512 << 20) / (8 * (int64_t)N)}));
+  GS_TRY(scratch.alloc((size_t)warps * N * 8, stream));
+  global_inverse_kernel<<<(int)((warps * 32 + 127) / 128), 128, 0, stream>>>(
+      N, LU, perm, (double*)R.ptr, (double*)scratch.ptr, warps);
+  GS_CUDA(cudaGetLastError());
+  const int64_t vw = std::min<int64_t>((int64_t)N, (int64_t)sm_count() * 32);
+  global_vectors_kernel<<<(int)((vw * 32 + 127) / 128), 128, 0, stream>>>(
+      N, (int)a.n, a.p, a.method == GS_SIMPLE ? 1 : 0, a.sk_mean, a.val, (const double*)R.ptr,
+      lambda, arow, Rh, Rl);
+  GS_CUDA(cudaGetLastError());
+  count_launch(2);
+  GS_CUDA(cudaStreamSynchronize(stream));
+  return GS_OK;
+}
+
+int global_gemm_launch(const KrigeArgs& a, const DevModel& m, int N, const float* Rh,
+                       const float* Rl, const double* lambda, const double* arow,
+                       cudaStream_t stream) {
+  if (a.ntl == 0) return GS_OK;
+  // targets per chunk: the split right-hand sides within 1 GiB
+  int64_t T = std::min<int64_t>(a.ntl, std::max<int64_t>(kGT, ((int64_t)1 << 30) / (8 * (int64_t)N)));
+  const int ntiles = (N + kGT - 1) / kGT;
+  DevBuf B, Q;
+  GS_TRY(B.alloc((size_t)N * T * 8, stream));
+  GS_TRY(Q.alloc((size_t)ntiles * T * sizeof(df), stream));
+  float* Bh = (float*)B.ptr;
+  float* Bl = Bh + (size_t)N * T;
+  for (int64_t c0 = 0; c0 < a.ntl; c0 += T) {
+    const int64_t tc = std::min<int64_t>(T, a.ntl - c0);
+    KrigeArgs ca = a;
+    ca.tx += c0;
+    ca.ty += c0;
+    if (ca.tz) ca.tz += c0;
+    if (ca.tdrift) ca.tdrift += c0 * a.nv;
+    ca.out_v += c0;
+    ca.out_var += c0;
+    if (ca.out_lag) ca.out_lag += c0;
+    ca.out_st += c0;
+    // Bh / Bl laid out with this chunk's count as the row stride
+    float* bh = Bh;
+    float* bl = Bh + (size_t)N * tc;
+    const int rb = (int)std::min<int64_t>(((int64_t)N * tc + 255) / 256, (int64_t)sm_count() * 64);
+    if (a.dim == 2) global_rhs_kernel<2><<<rb, 256, 0, stream>>>(ca, m, N, tc, bh, bl);
+    else global_rhs_kernel<3><<<rb, 256, 0, stream>>>(ca, m, N, tc, bh, bl);
+    dim3 grid((unsigned)((tc + kGT - 1) / kGT), (unsigned)ntiles);
+    global_quad_kernel<<<grid, 256, 0, stream>>>(N, tc, Rh, Rl, bh, bl, (df*)Q.ptr);
+    const int64_t fw = std::min<int64_t>(tc, (int64_t)sm_count() * 32);
+    if (a.dim == 2)
+      global_finish_kernel<2><<<(int)((fw * 32 + 127) / 128), 128, 0, stream>>>(
+          ca, m, N, tc, ntiles, lambda, arow, (const df*)Q.ptr);
+    else
+      global_finish_kernel<3><<<(int)((fw * 32 + 127) / 128), 128, 0, stream>>>(
+          ca, m, N, tc, ntiles, lambda, arow, (const df*)Q.ptr);
+    GS_CUDA(cudaGetLastError());
+    count_launch(3);
+  }
   return GS_OK;
 }
 

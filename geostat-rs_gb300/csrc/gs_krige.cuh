@@ -93,6 +93,18 @@ int global_solve_launch(const KrigeArgs& a, const DevModel& m, int N, const doub
                         const int32_t* perm, int state, double* scratch, int64_t scratch_warps,
                         cudaStream_t stream);
 int64_t fp64_threads_for(int nmax, int64_t budget_bytes);
+// Matrix-product form of the factored global system (the mixed-precision
+// predict path): at build, R (row j = A^{-1} e_j, from the LU factors) split
+// into hi / lo floats Rh, Rl (N x N), lambda = R z and arow = R e_n (N
+// doubles each); synchronises.  Per call, estimates and Lagrange
+// multipliers as FP64 dot products with lambda and arow, variances
+// C(0) - b^T R b through a double-float GEMM over tiles of targets.
+int global_gemm_prepare(const KrigeArgs& a, int N, const double* LU, const int32_t* perm,
+                        float* Rh, float* Rl, double* lambda, double* arow, cudaStream_t stream);
+int global_gemm_launch(const KrigeArgs& a, const DevModel& m, int N, const float* Rh,
+                       const float* Rl, const double* lambda, const double* arow,
+                       cudaStream_t stream);
+
 
 // Block kriging's within-block covariance (kriging.rs:742-756): the mean of
 // C(u - v) over all discretisation pairs, with c0 - nugget for u = v; one

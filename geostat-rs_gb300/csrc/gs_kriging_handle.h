@@ -55,9 +55,19 @@ struct gs_kriging {
   int32_t* d_perm = nullptr;
   int lu_n = 0;
   int lu_state = 0;
+  // its matrix-product form (mixed precision): R = A^{-T} split into hi / lo
+  // floats, lambda = R z, arow = R e_n; null when not prepared
+  float* d_rh = nullptr;
+  float* d_rl = nullptr;
+  double* d_lambda = nullptr;
+  double* d_arow = nullptr;
   ~gs_kriging() {
     cudaFree(d_lu);
     cudaFree(d_perm);
+    cudaFree(d_rh);
+    cudaFree(d_rl);
+    cudaFree(d_lambda);
+    cudaFree(d_arow);
     cudaFree(d_drift);
     cudaFree(d_err);
     cudaFree(d_basis_df);
