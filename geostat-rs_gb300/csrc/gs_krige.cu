@@ -1316,9 +1316,10 @@ __global__ void global_solve_kernel(KrigeArgs a, DevModel m, int N, const double
 //     estimate  = lambda . b   (+ mean, simple kriging),
 //     Lagrange  = a . b,
 //     variance  = C(0) - b^T R b,
-// the first two as FP64 dot products, the quadratic form through X = R B
-// for a tile of targets: a double-float GEMM on the CUDA cores (compensated
-// Dot2 accumulation in packed FP32x2 arithmetic) whose epilogue forms
+// the first two as FP64 dot products, the quadratic form through X = R' B
+// for a tile of targets, R' the upper triangle of R with its off-diagonal
+// entries doubled: a double-float GEMM on the CUDA cores (compensated Dot2
+// accumulation in packed FP32x2 arithmetic) whose epilogue forms
 // sum_i B_it X_it per row tile; the row tiles' partial sums are added in a
 // fixed order.  b^T R b equals b^T x of the reference's solve
 // (kriging.rs:614-643: C(0) - w . c - mu . f).
@@ -1408,7 +1409,7 @@ __global__ void global_rhs_kernel(KrigeArgs a, DevModel m, int N, int64_t T, flo
 
 // Tiles of the quadratic form: block (bx, by) multiplies rows
 // [64 by, 64 by + 64) of R with the targets [64 bx, 64 bx + 64) of B over
-// all N columns, 16 columns per stage, each thread a 4 x 4 block of X in
+// the columns from 64 by on, 16 columns per stage, each thread a 4 x 4 block of X in
 // double-float (two FP32x2 accumulator pairs per row, compensated), and
 // writes sum_i B_it X_it over its row tile to Q[by * T + t] (hi, lo).
 constexpr int kGT = 64;   // rows / targets per tile
@@ -1429,15 +1430,20 @@ __global__ void __launch_bounds__(256) global_quad_kernel(int N, int64_t T, cons
       s[r][q] = make_float2(0.0f, 0.0f);
       c[r][q] = make_float2(0.0f, 0.0f);
     }
-  for (int k0 = 0; k0 < N; k0 += kGK) {
+  // R is symmetric up to rounding, so b^T R b = sum_i R_ii b_i^2 +
+  // 2 sum_(i<k) R_ik b_i b_k: columns from the diagonal tile on, with the
+  // entries left of the diagonal weighted 0 and those right of it 2 (exact
+  // scalings) -- half the products of the full form
+  for (int k0 = (int)i0; k0 < N; k0 += kGK) {
     for (int e = tid; e < kGT * kGK; e += 256) {
       const int r = e / kGK, kk = e % kGK;
       const int64_t gi = i0 + r;
       const int gk = k0 + kk;
       float h = 0.0f, l = 0.0f;
-      if (gi < N && gk < N) {
-        h = Rh[gi * N + gk];
-        l = Rl[gi * N + gk];
+      if (gi < N && gk < N && gk >= gi) {
+        const float w = gk == gi ? 1.0f : 2.0f;
+        h = w * Rh[gi * N + gk];
+        l = w * Rl[gi * N + gk];
       }
       Ms[0][kk][r] = h;
       Ms[1][kk][r] = l;
