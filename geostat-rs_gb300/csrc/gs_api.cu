@@ -498,27 +498,6 @@ int kriging_create(const gs_pointset* ps, const gs_model* model, const gs_kcfg* 
         k->lu_n = (int)N;
         k->lu_state = state;
       }
-      // the matrix-product form for mixed-precision calls (a factored,
-      // non-singular system); without room for it those calls take the
-      // per-target solves too
-      if (!rc && state == 1) {
-        const size_t nn = (size_t)N * N;
-        if (dev_malloc((void**)&k->d_rh, nn * 4) == cudaSuccess &&
-            dev_malloc((void**)&k->d_rl, nn * 4) == cudaSuccess &&
-            dev_malloc((void**)&k->d_lambda, (size_t)N * 8) == cudaSuccess &&
-            dev_malloc((void**)&k->d_arow, (size_t)N * 8) == cudaSuccess) {
-          rc = global_gemm_prepare(gs::base_args(k), (int)N, k->d_lu, k->d_perm, k->d_rh,
-                                   k->d_rl, k->d_lambda, k->d_arow, k->stream);
-        } else {
-          cudaGetLastError();  // clear the failed allocation
-          cudaFree(k->d_rh);
-          cudaFree(k->d_rl);
-          cudaFree(k->d_lambda);
-          cudaFree(k->d_arow);
-          k->d_rh = k->d_rl = nullptr;
-          k->d_lambda = k->d_arow = nullptr;
-        }
-      }
     }
   }
   if (rc) {
@@ -648,6 +627,35 @@ struct BlockSpec {
   const double* cbb;
 };
 
+// The factored global system's matrix-product form, prepared on first use by
+// a mixed-precision call (N solves with the factors: about 2 N^3 FP64 FMAs,
+// so a predictor used only at FP64 never pays for it).  Without device
+// memory for it, mixed-precision calls take the per-target solves.
+static int ensure_global_gemm(const gs_kriging* k) {
+  std::lock_guard<std::mutex> lk(k->gemm_mu);
+  if (k->gemm_state != 0) return GS_OK;
+  const int N = k->lu_n;
+  const size_t nn = (size_t)N * N;
+  if (dev_malloc((void**)&k->d_rh, nn * 4) != cudaSuccess ||
+      dev_malloc((void**)&k->d_rl, nn * 4) != cudaSuccess ||
+      dev_malloc((void**)&k->d_lambda, (size_t)N * 8) != cudaSuccess ||
+      dev_malloc((void**)&k->d_arow, (size_t)N * 8) != cudaSuccess) {
+    cudaGetLastError();  // clear the failed allocation
+    cudaFree(k->d_rh);
+    cudaFree(k->d_rl);
+    cudaFree(k->d_lambda);
+    cudaFree(k->d_arow);
+    k->d_rh = k->d_rl = nullptr;
+    k->d_lambda = k->d_arow = nullptr;
+    k->gemm_state = 2;
+    return GS_OK;
+  }
+  GS_TRY(global_gemm_prepare(base_args(k), N, k->d_lu, k->d_perm, k->d_rh, k->d_rl, k->d_lambda,
+                             k->d_arow, k->stream));
+  k->gemm_state = 1;
+  return GS_OK;
+}
+
 int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double* ty,
                  const double* tz, const double* tdrift, double* value, double* variance,
                  double* lagrange, uint8_t* status, int precision, cudaStream_t stream, bool timed,
@@ -710,7 +718,8 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     const int64_t warps = std::max<int64_t>(
         1, std::min<int64_t>((int64_t)sm_count() * 32, ((int64_t)512 << 20) / (16 * (int64_t)N)));
     DevBuf scratch;
-    const bool gemm = precision != GS_PREC_FP64 && k->lu_state == 1 && k->d_rh;
+    if (precision != GS_PREC_FP64 && k->lu_state == 1) GS_TRY(ensure_global_gemm(k));
+    const bool gemm = precision != GS_PREC_FP64 && k->lu_state == 1 && k->gemm_state == 1;
     if (!gemm) GS_TRY(scratch.alloc((size_t)warps * 2 * N * 8, stream));
     KrigeArgs g = a;
     g.tx = tx;

@@ -56,11 +56,14 @@ struct gs_kriging {
   int lu_n = 0;
   int lu_state = 0;
   // its matrix-product form (mixed precision): R = A^{-T} split into hi / lo
-  // floats, lambda = R z, arow = R e_n; null when not prepared
-  float* d_rh = nullptr;
-  float* d_rl = nullptr;
-  double* d_lambda = nullptr;
-  double* d_arow = nullptr;
+  // floats, lambda = R z, arow = R e_n, prepared by the first mixed-precision
+  // call that needs it (gemm_state 0: not yet, 1: ready, 2: no room for it)
+  mutable std::mutex gemm_mu;
+  mutable int gemm_state = 0;
+  mutable float* d_rh = nullptr;
+  mutable float* d_rl = nullptr;
+  mutable double* d_lambda = nullptr;
+  mutable double* d_arow = nullptr;
   ~gs_kriging() {
     cudaFree(d_lu);
     cudaFree(d_perm);

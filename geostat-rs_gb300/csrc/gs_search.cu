@@ -841,7 +841,8 @@ int search_launch(const Grid& g, const SearchFrame& frame, const SearchParams& p
   const int wpb = 4;
   const size_t per_warp = knn_per_warp(NB, p.capb);
   size_t smem = per_warp * wpb;
-  static const size_t kMaxSmem = 227 * 1024;
+  // 227 KB per block, less the static ring-offset table
+  static const size_t kMaxSmem = 227 * 1024 - ShellTab<3>::kEntries * sizeof(uint32_t);
   if (smem > kMaxSmem) return fail(GS_ERR_INVALID_PARAMETER, "neighbourhood too large for the device search");
   // targets per warp group: up to 32 once there are 16 warps' worth of
   // groups per SM, fewer for small batches (latency)
