@@ -98,3 +98,28 @@ def test_global_equals_moving_at_k_equals_n():
                        G.KrigingConfig(max_neighbors=120)).predict_many(t, "fp64", full=True)
     assert np.max(np.abs(g.value - mv.value)) < 1e-10
     assert np.max(np.abs(g.variance - mv.variance)) < 1e-10
+
+
+def test_global_matrix_form_over_several_target_chunks():
+    """The mixed path's matrix-product form takes the targets in chunks (the
+    split right-hand sides within 1 GiB: 67 108 targets at 2 001 unknowns);
+    70 000 targets span two chunks.  Against the FP64 build (per-target
+    solves with the same factors) on every target, and the oracle on a
+    sample, statuses exact."""
+    c = uniform_points(2000, 2, 96, [1000.0, 1000.0])
+    v = smooth_values(c)
+    m = sph200_model()
+    k = G.Kriging.new(G.PointSet(c, v), m)
+    t = uniform_points(70000, 2, 97, [1000.0, 1000.0])
+    mixed = k.predict_many(t, "mixed", full=True)
+    f64 = k.predict_many(t, "fp64", full=True)
+    assert (mixed.status == f64.status).all() and (f64.status == 0).all()
+    vs = float(np.mean(np.abs(v)))
+    assert_close(mixed.value, f64.value, vs, 1e-9, "value")
+    assert_close(mixed.variance, f64.variance, 1e-3 * m.total_sill(), 1e-9, "variance")
+    assert_close(mixed.lagrange, f64.lagrange, 1.0, 1e-9, "lagrange")
+    sample = np.r_[0:300, 67000:67300, 69700:70000]
+    ref = O.krige(c, v, m, t[sample])
+    assert_close(mixed.value[sample], ref["value"], vs, 1e-9, "value vs oracle")
+    assert_close(mixed.variance[sample], ref["variance"], 1e-3 * m.total_sill(), 1e-9,
+                 "variance vs oracle")
