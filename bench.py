@@ -410,13 +410,6 @@ def cv_bench(args, coords, values, model, log):
         cv = G.leave_one_out(ps, model, cfg)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
-    out64 = k.predict_many(t, "fp64", full=True)
-    ts64 = []
-    for _ in range(3):
-        t1 = time.perf_counter()
-        out64 = k.predict_many(t, "fp64", full=True)
-        ts64.append(time.perf_counter() - t1)
-    dt64 = statistics.median(ts64)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     O.build()
@@ -524,13 +517,6 @@ def block_bench(args, log):
         val, var = k.predict_block_grid(lo, hi, nc, bs, disc)
         ts.append(time.perf_counter() - t1)
     dt = statistics.median(ts)
-    out64 = k.predict_many(t, "fp64", full=True)
-    ts64 = []
-    for _ in range(3):
-        t1 = time.perf_counter()
-        out64 = k.predict_many(t, "fp64", full=True)
-        ts64.append(time.perf_counter() - t1)
-    dt64 = statistics.median(ts64)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     from geostat_rs.io import grid_centers
