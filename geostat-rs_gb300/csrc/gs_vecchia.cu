@@ -371,9 +371,9 @@ constexpr float kVecchiaFloor = 1e-10f;
 // to the FP64 re-solve kernel).  On success lane 0 receives the conditional
 // variance and residual of loglik_with_plan (vecchia.rs:302-330) from FP64
 // dot products; returns false (uniformly) otherwise.
-template <int D>
+template <int D, class Factor>
 __device__ bool vecchia_refine_fp64(const VArgs& a, const DevModel& mdl, const Exp64Table& et,
-                                    int64_t k, int64_t pt, int s, int lane, const WarpFactor& f,
+                                    int64_t k, int64_t pt, int s, int lane, const Factor& f,
                                     const WarpScratch& W, double* K64, double* k64,
                                     double& var, double& r) {
   const int M = a.m;
@@ -451,11 +451,10 @@ __device__ bool vecchia_refine_fp64(const VArgs& a, const DevModel& mdl, const E
 // One warp per ordered point for conditioning sets of at most 32 points: the
 // same assembly and certification as vecchia_loglik_kernel, with the
 // register-row solver of gs_warp.cuh (no block barriers).  The likelihood
-// form is compiled for three blocks (12 warps) per SM, at which it needs no
-// spills (measured faster than four blocks at 128 registers with spills);
-// the REML form keeps the default.
+// form is compiled for four blocks (16 warps) per SM (128 registers: the
+// matrix entries stay in shared memory); the REML form keeps the default.
 #ifndef GS_VECCHIA_MIN_BLOCKS
-#define GS_VECCHIA_MIN_BLOCKS 3
+#define GS_VECCHIA_MIN_BLOCKS 4
 #endif
 template <int D, bool REML>
 __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : GS_VECCHIA_MIN_BLOCKS)
@@ -624,11 +623,12 @@ __global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : GS_VECCHIA_MIN_BLOCKS
       __syncwarp();
       bool ok, ok64 = false;
       {
+        const auto row = shared_row([&](int e) { return df_make(Ah[e], Al[e]); }, s, lane);
         WarpFactor fct;
-        const bool fok = warp_factor(Ah, Al, s, lane, fct, W);
+        const bool fok = warp_factor(row, s, lane, fct, W);
         // REML keeps the strict test: its records feed further sums
         bool at_floor = false;
-        ok = fok && warp_refine(fct, B, s, lane, W, REML ? 0.0f : kVecchiaFloor, &at_floor);
+        ok = fok && warp_refine(fct, row, B, s, lane, W, REML ? 0.0f : kVecchiaFloor, &at_floor);
         n_floor += ok && at_floor;
         if (!REML && fok && !ok) {
           // stalled: refine with FP64 residuals (A's and B's storage take the
@@ -1540,8 +1540,11 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_grad_kernel(VArgs a, Exp
         }
       });
       __syncwarp();
+      // one factorisation, four right-hand sides: the row stays in registers
+      RegisterRow row;
+      row.load([&](int e) { return A[e]; }, s, lane);
       WarpFactor f;
-      bool ok = warp_factor(A, s, lane, f, W) && warp_refine(f, B, s, lane, W);
+      bool ok = warp_factor(row, s, lane, f, W) && warp_refine(f, row, B, s, lane, W);
       if (!ok) {
         if (lane == 0) a.flag[at] = 1;
         __syncwarp();
@@ -1572,7 +1575,7 @@ __global__ void __launch_bounds__(32 * kVWarps) vecchia_grad_kernel(VArgs a, Exp
           RHS[lane] = rhs;
         }
         __syncwarp();
-        ok = warp_refine(f, RHS, s, lane, W);
+        ok = warp_refine(f, row, RHS, s, lane, W);
         if (!ok) break;
         const df dw = lane < s ? W.xd[lane] : df_make(0.0f, 0.0f);
         const df dmu = warp_sum_df(lane < s ? df_mul(dw, ZV[lane]) : df_make(0.0f, 0.0f));

@@ -13,10 +13,10 @@
 // (diagonal corrected once).  No per-element selects and no register-array
 // indexing are needed.  Symmetry gives a_ik as row_k[i].
 //
-// Refinement residuals b - A x use the double-float entries held in registers
-// (compensated FP32 dot products, Ogita, Rump & Oishi 2005); corrections are
-// register GEMVs with -A^{-1}.  One factorisation serves any number of
-// right-hand sides (warp_refine).
+// Refinement residuals b - A x use the double-float entries read from shared
+// memory (compensated FP32 dot products, Ogita, Rump & Oishi 2005);
+// corrections are register GEMVs with -A^{-1}.  One factorisation serves any
+// number of right-hand sides (warp_refine).
 #pragma once
 
 #include "gs_solve.cuh"
@@ -25,7 +25,6 @@
 namespace gs {
 
 constexpr int kWarpN = 32;
-constexpr int kWarpN2 = kWarpN / 2;  // column pairs of a register row
 // Floats of the published-row buffer: two alternating rows of kWarpN
 // entries plus the pivot (padded to 16 bytes).
 constexpr int kWarpRowFloats = 2 * (kWarpN + 4);
@@ -37,35 +36,6 @@ struct WarpScratch {
 };
 
 constexpr int kWarpN4 = kWarpN / 4;  // column quads of a register row
-
-// The factorisation one lane holds: its row of the double-float matrix
-// (ah + al) as column pairs and of -(sc A)^{-1} + 2I (t) as column quads
-// (so a published row is stored straight from aligned registers), with the
-// power-of-two scale sc.
-struct WarpFactor {
-  float2 ah[kWarpN2], al[kWarpN2];
-  float4 t[kWarpN4];
-  float sc;
-};
-
-// Loads row `lane` of a packed symmetric df matrix (N x N; at(e) returns
-// packed entry e) into registers; rows and columns beyond N hold the
-// identity.
-template <class At>
-__device__ __forceinline__ void warp_load_rows(At&& at, int N, int lane, float2 (&ah)[kWarpN2],
-                                               float2 (&al)[kWarpN2]) {
-  auto elt = [&](int j) {
-    df v = df_make(j == lane ? 1.0f : 0.0f, 0.0f);
-    if (lane < N && j < N) v = at(lane >= j ? pk(lane, j) : pk(j, lane));
-    return v;
-  };
-#pragma unroll
-  for (int j2 = 0; j2 < kWarpN2; ++j2) {
-    const df v0 = elt(2 * j2), v1 = elt(2 * j2 + 1);
-    ah[j2] = make_float2(v0.hi, v1.hi);
-    al[j2] = make_float2(v0.lo, v1.lo);
-  }
-}
 
 __device__ __forceinline__ void warp_gemv_neg_inv(const float4 (&t)[kWarpN4], const float* vec,
                                                   int lane, float& y) {
@@ -81,22 +51,88 @@ __device__ __forceinline__ void warp_gemv_neg_inv(const float4 (&t)[kWarpN4], co
   y = fmaf(-2.0f, vec[lane], (a0.x + a1.x) + (a0.y + a1.y));
 }
 
-// FP32 inverse of the packed df matrix A (N <= 32 unknowns).  Returns false
-// (uniformly in the warp) when a pivot is too small for FP32.
+// Refinement sweeps before a system is handed to the FP64 solver; a sweep
+// that no longer halves the correction ends the refinement earlier (the
+// double-float residual of an ill-conditioned system has reached its limit).
+constexpr int kMaxRefineSweeps = 8;
+
+// The factorisation one lane holds: its row of -(sc A)^{-1} + 2I as column
+// quads (so a published row is stored straight from aligned registers) and
+// the power-of-two scale sc.  The matrix's own entries stay in shared memory
+// (read through an accessor at(e) -> df of packed entry e), which keeps the
+// lane's registers for the inverse.
+struct WarpFactor {
+  float4 t[kWarpN4];
+  float sc;
+};
+
+// Entry (lane, j) of the packed symmetric matrix; rows and columns beyond N
+// hold the identity.
+template <class At>
+__device__ __forceinline__ df warp_entry(At&& at, int N, int lane, int j) {
+  df v = df_make(j == lane ? 1.0f : 0.0f, 0.0f);
+  if (lane < N && j < N) v = at(lane >= j ? pk(lane, j) : pk(j, lane));
+  return v;
+}
+
+// The lane's matrix row as the refinement reads it: pair(j, ah, al) gives
+// the hi and lo parts of entries j and j + 1 (j even).  SharedRow reads them
+// from shared memory at every use (registers stay free for the inverse);
+// RegisterRow loads the row once, for a factorisation that serves several
+// right-hand sides.
+template <class At>
+struct SharedRow {
+  At at;
+  int N, lane;
+  __device__ __forceinline__ void pair(int j, float2& ah, float2& al) const {
+    const df a0 = warp_entry(at, N, lane, j), a1 = warp_entry(at, N, lane, j + 1);
+    ah = make_float2(a0.hi, a1.hi);
+    al = make_float2(a0.lo, a1.lo);
+  }
+  __device__ __forceinline__ float hi(int j) const { return warp_entry(at, N, lane, j).hi; }
+};
+template <class At>
+__device__ __forceinline__ SharedRow<At> shared_row(At at, int N, int lane) {
+  return SharedRow<At>{at, N, lane};
+}
+struct RegisterRow {
+  float2 h[kWarpN / 2], l[kWarpN / 2];
+  template <class At>
+  __device__ __forceinline__ void load(At&& at, int N, int lane) {
+#pragma unroll
+    for (int j = 0; j < kWarpN; j += 2) {
+      const df a0 = warp_entry(at, N, lane, j), a1 = warp_entry(at, N, lane, j + 1);
+      h[j >> 1] = make_float2(a0.hi, a1.hi);
+      l[j >> 1] = make_float2(a0.lo, a1.lo);
+    }
+  }
+  __device__ __forceinline__ void pair(int j, float2& ah, float2& al) const {
+    ah = h[j >> 1];
+    al = l[j >> 1];
+  }
+  __device__ __forceinline__ float hi(int j) const { return (j & 1) ? h[j >> 1].y : h[j >> 1].x; }
+};
+
+// FP32 inverse of the packed df matrix (N <= 32 unknowns; the lane's row
+// `row`) by the sweep operator.  Returns false (uniformly in the warp) when a
+// pivot is too small for FP32.
 //
 // Pivot k: lane k publishes its row in one of two alternating buffers, with
 // the pivot entry replaced by d - 1 and d stored after the row; one
 // __syncwarp, then every lane applies its packed FP32x2 update.  Lane k's
 // next write to the same buffer (pivot k + 2) comes after the next pivot's
 // __syncwarp, which every lane reaches only after reading this row.
-template <class At>
-__device__ __forceinline__ bool warp_factor_at(At&& at, int N, int lane, WarpFactor& f,
-                                               const WarpScratch& W) {
-  warp_load_rows(at, N, lane, f.ah, f.al);
+template <class Row>
+__device__ __forceinline__ bool warp_factor(const Row& row, int N, int lane, WarpFactor& f,
+                                            const WarpScratch& W) {
   float amax = 0.0f;
 #pragma unroll
-  for (int j2 = 0; j2 < kWarpN2; ++j2)
-    amax = fmaxf(amax, lane < N ? fmaxf(fabsf(f.ah[j2].x), fabsf(f.ah[j2].y)) : 0.0f);
+  for (int q = 0; q < kWarpN4; ++q) {
+    f.t[q] = make_float4(row.hi(4 * q), row.hi(4 * q + 1), row.hi(4 * q + 2), row.hi(4 * q + 3));
+    if (lane < N)
+      amax = fmaxf(amax, fmaxf(fmaxf(fabsf(f.t[q].x), fabsf(f.t[q].y)),
+                               fmaxf(fabsf(f.t[q].z), fabsf(f.t[q].w))));
+  }
   amax = warp_max_f(amax);
   f.sc = 1.0f;
   if (!(amax > 0.0f)) return false;
@@ -106,13 +142,13 @@ __device__ __forceinline__ bool warp_factor_at(At&& at, int N, int lane, WarpFac
   int ex = 0;
   frexpf(amax, &ex);
   f.sc = ldexpf(1.0f, -ex);
-  auto scaled = [&](int j) {
-    const float v = (j & 1) ? f.ah[j >> 1].y : f.ah[j >> 1].x;
-    return (lane < N && j < N) ? v * f.sc : v;
-  };
 #pragma unroll
-  for (int q = 0; q < kWarpN4; ++q)
-    f.t[q] = make_float4(scaled(4 * q), scaled(4 * q + 1), scaled(4 * q + 2), scaled(4 * q + 3));
+  for (int q = 0; q < kWarpN4; ++q) {
+    if (lane < N && 4 * q < N) f.t[q].x *= f.sc;
+    if (lane < N && 4 * q + 1 < N) f.t[q].y *= f.sc;
+    if (lane < N && 4 * q + 2 < N) f.t[q].z *= f.sc;
+    if (lane < N && 4 * q + 3 < N) f.t[q].w *= f.sc;
+  }
   const float tol = 1e-6f * amax * f.sc;
   __syncwarp();  // the previous user of W.row is done with it
   for (int k = 0; k < N; ++k) {
@@ -120,7 +156,7 @@ __device__ __forceinline__ bool warp_factor_at(At&& at, int N, int lane, WarpFac
     if (lane == k) {
 #pragma unroll
       for (int q = 0; q < kWarpN4; ++q) *reinterpret_cast<float4*>(rb + 4 * q) = f.t[q];
-      const float d = rb[k];  // this lane's own store
+      const float d = rb[k];
       rb[k] = d - 1.0f;
       rb[kWarpN] = d;
     }
@@ -142,25 +178,9 @@ __device__ __forceinline__ bool warp_factor_at(At&& at, int N, int lane, WarpFac
   return true;
 }
 
-// The matrix as packed df entries.
-__device__ __forceinline__ bool warp_factor(const df* A, int N, int lane, WarpFactor& f,
-                                            const WarpScratch& W) {
-  return warp_factor_at([&](int e) { return A[e]; }, N, lane, f, W);
-}
-// The matrix as packed entries split into hi parts Ah[e] and lo parts Al[e].
-__device__ __forceinline__ bool warp_factor(const float* Ah, const float* Al, int N, int lane,
-                                            WarpFactor& f, const WarpScratch& W) {
-  return warp_factor_at([&](int e) { return df_make(Ah[e], Al[e]); }, N, lane, f, W);
-}
-
-// Refinement sweeps before a system is handed to the FP64 solver; a sweep
-// that no longer halves the correction ends the refinement earlier (the
-// double-float residual of an ill-conditioned system has reached its limit).
-constexpr int kMaxRefineSweeps = 8;
-
-// Solves A x = B with the factorisation f and refines to ~1e-13 relative; on
-// success W.xd[i] holds x_i.  Returns false (uniformly) when the refinement
-// stalls.
+// Solves A x = B with the factorisation f and refines to ~1e-13 relative
+// (residuals from the lane's matrix row `row`); on success W.xd[i] holds x_i.
+// Returns false (uniformly) when the refinement stalls.
 //
 // accept_floor > 0: a refinement that stops contracting (or runs out of
 // sweeps) once its corrections are at most accept_floor |x| is accepted as
@@ -174,10 +194,10 @@ constexpr int kMaxRefineSweeps = 8;
 // solution), and the second is a product of two small factors.  Callers
 // whose outputs are such functionals (the Vecchia conditional mean and
 // variance) may use it.
-__device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, int N, int lane,
-                                            const WarpScratch& W, float accept_floor = 0.0f,
-                                            bool* at_floor = nullptr) {
-  // x0 = A^{-1} b_hi = -(-A^{-1}) b_hi
+template <class Row>
+__device__ __forceinline__ bool warp_refine(const WarpFactor& f, const Row& row, const df* B,
+                                            int N, int lane, const WarpScratch& W,
+                                            float accept_floor = 0.0f, bool* at_floor = nullptr) {
   __syncwarp();
   W.vec[lane] = lane < N ? B[lane].hi : 0.0f;
   __syncwarp();
@@ -200,21 +220,24 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
     __syncwarp();
     float2 s2 = make_float2(lane < N ? B[lane].hi : 0.0f, 0.0f);
     float2 c2 = make_float2(lane < N ? B[lane].lo : 0.0f, 0.0f);
-    auto acc = [&](float2 ah, float2 al, float2 xh, float2 xl) {
-      const float2 ph = __fmul2_rn(ah, xh);
-      float2 pe = __ffma2_rn(ah, xh, p_neg(ph));
-      pe = __ffma2_rn(ah, xl, pe);
-      pe = __ffma2_rn(al, xh, pe);
-      const dfp ts = p_two_sum(s2, ph);
-      s2 = ts.hi;
-      c2 = p_add(c2, p_add(ts.lo, pe));
-    };
 #pragma unroll
     for (int j = 0; j < kWarpN; j += 4) {
       const float4 xh = *reinterpret_cast<const float4*>(xs + j);
       const float4 xl = *reinterpret_cast<const float4*>(xs + kWarpN + j);
-      acc(f.ah[j >> 1], f.al[j >> 1], make_float2(xh.x, xh.y), make_float2(xl.x, xl.y));
-      acc(f.ah[(j >> 1) + 1], f.al[(j >> 1) + 1], make_float2(xh.z, xh.w), make_float2(xl.z, xl.w));
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float2 ah, al;
+        row.pair(j + 2 * h, ah, al);
+        const float2 xh2 = h ? make_float2(xh.z, xh.w) : make_float2(xh.x, xh.y);
+        const float2 xl2 = h ? make_float2(xl.z, xl.w) : make_float2(xl.x, xl.y);
+        const float2 ph = __fmul2_rn(ah, xh2);
+        float2 pe = __ffma2_rn(ah, xh2, p_neg(ph));
+        pe = __ffma2_rn(ah, xl2, pe);
+        pe = __ffma2_rn(al, xh2, pe);
+        const dfp ts = p_two_sum(s2, ph);
+        s2 = ts.hi;
+        c2 = p_add(c2, p_add(ts.lo, pe));
+      }
     }
     const df st = two_sum(s2.x, s2.y);
     const float s = st.hi, c = (c2.x + c2.y) + st.lo;
@@ -254,12 +277,14 @@ __device__ __forceinline__ bool warp_refine(const WarpFactor& f, const df* B, in
   return false;
 }
 
-// Factor and solve one right-hand side.
+// Factor and solve one right-hand side (packed df matrix A).
 __device__ __forceinline__ bool warp_solve(const df* A, const df* B, int N, int lane,
                                            const WarpScratch& W) {
+  auto at = [&](int e) { return A[e]; };
+  const auto row = shared_row(at, N, lane);
   WarpFactor f;
-  if (!warp_factor(A, N, lane, f, W)) return false;
-  return warp_refine(f, B, N, lane, W);
+  if (!warp_factor(row, N, lane, f, W)) return false;
+  return warp_refine(f, row, B, N, lane, W);
 }
 
 }  // namespace gs
