@@ -636,10 +636,7 @@ static int ensure_global_gemm(const gs_kriging* k) {
   if (k->gemm_state != 0) return GS_OK;
   const int N = k->lu_n;
   const size_t nn = (size_t)N * N;
-  if (dev_malloc((void**)&k->d_rh, nn * 4) != cudaSuccess ||
-      dev_malloc((void**)&k->d_rl, nn * 4) != cudaSuccess ||
-      dev_malloc((void**)&k->d_lambda, (size_t)N * 8) != cudaSuccess ||
-      dev_malloc((void**)&k->d_arow, (size_t)N * 8) != cudaSuccess) {
+  auto unavailable = [&]() {
     cudaGetLastError();  // clear the failed allocation
     cudaFree(k->d_rh);
     cudaFree(k->d_rl);
@@ -649,9 +646,16 @@ static int ensure_global_gemm(const gs_kriging* k) {
     k->d_lambda = k->d_arow = nullptr;
     k->gemm_state = 2;
     return GS_OK;
-  }
-  GS_TRY(global_gemm_prepare(base_args(k), N, k->d_lu, k->d_perm, k->d_rh, k->d_rl, k->d_lambda,
-                             k->d_arow, k->stream));
+  };
+  if (dev_malloc((void**)&k->d_rh, nn * 4) != cudaSuccess ||
+      dev_malloc((void**)&k->d_rl, nn * 4) != cudaSuccess ||
+      dev_malloc((void**)&k->d_lambda, (size_t)N * 8) != cudaSuccess ||
+      dev_malloc((void**)&k->d_arow, (size_t)N * 8) != cudaSuccess)
+    return unavailable();
+  const int rc = global_gemm_prepare(base_args(k), N, k->d_lu, k->d_perm, k->d_rh, k->d_rl,
+                                     k->d_lambda, k->d_arow, k->stream);
+  if (rc == GS_ERR_OUT_OF_MEMORY) return unavailable();  // its temporary buffers did not fit
+  if (rc) return rc;
   k->gemm_state = 1;
   return GS_OK;
 }

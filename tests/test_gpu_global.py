@@ -123,3 +123,43 @@ def test_global_matrix_form_over_several_target_chunks():
     assert_close(mixed.value[sample], ref["value"], vs, 1e-9, "value vs oracle")
     assert_close(mixed.variance[sample], ref["variance"], 1e-3 * m.total_sill(), 1e-9,
                  "variance vs oracle")
+
+
+def test_global_matrix_form_falls_back_without_room():
+    """When the matrix-product form's temporary buffers do not fit (the
+    library's next stream-ordered device allocation refused, a host-side fake
+    of an exhausted device), the mixed-precision call takes the per-target
+    solves with the factors -- the FP64 build's kernel, so the results are
+    identical -- and later calls keep doing so.  Device-resident targets, so
+    the first allocation of the call is the matrix form's."""
+    import torch
+    from geostat_rs import _abi
+    lib = _abi.load()
+    c = uniform_points(300, 2, 98, [1000.0, 1000.0])
+    v = smooth_values(c)
+    m = sph200_model()
+    k = G.Kriging.new(G.PointSet(c, v), m)
+    t = uniform_points(400, 2, 99, [1000.0, 1000.0])
+    dev = torch.device("cuda")
+    tx = torch.from_numpy(np.ascontiguousarray(t[:, 0])).to(dev)
+    ty = torch.from_numpy(np.ascontiguousarray(t[:, 1])).to(dev)
+
+    def run(prec):
+        val = torch.empty(len(t), dtype=torch.float64, device=dev)
+        var = torch.empty_like(val)
+        st = torch.empty(len(t), dtype=torch.uint8, device=dev)
+        k.predict_device(len(t), tx.data_ptr(), ty.data_ptr(), 0, val.data_ptr(), var.data_ptr(),
+                         st.data_ptr(), prec, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return val.cpu().numpy(), var.cpu().numpy(), st.cpu().numpy()
+
+    _abi.check(lib.gs_debug_refuse_allocations(1))
+    try:
+        mixed = run("mixed")
+    finally:
+        _abi.check(lib.gs_debug_refuse_allocations(0))
+    again = run("mixed")
+    f64 = run("fp64")
+    for out in (mixed, again):
+        assert (out[2] == f64[2]).all() and (f64[2] == 0).all()
+        assert np.array_equal(out[0], f64[0]) and np.array_equal(out[1], f64[1])
