@@ -281,22 +281,18 @@ __device__ __noinline__ void warp_sort(dkey* key, uint32_t* id, int n_valid, int
   }
 }
 
-template <int D, bool OCT, bool RANKED>
 // Blocks per SM the compiler plans registers for, measured on GB300: eight
 // for the single-buffer search (64 registers, a few values spilled: 9 %
 // faster than the 80-96 registers the compiler takes unbounded; ten and
 // twelve were slower again), four for the octant search (18 % faster than
 // unbounded, six slower).
-#ifndef GS_KNN_MINB
-#define GS_KNN_MINB 8
-#endif
-#ifndef GS_KNN_MINB_OCT
-#define GS_KNN_MINB_OCT 4
-#endif
-__global__ void __launch_bounds__(128, OCT ? GS_KNN_MINB_OCT : GS_KNN_MINB) knn_kernel(GridDev g, SearchFrame fr, SearchParams p,
-                                                  int64_t nt, int gs, const double* tx,
-                                                  const double* ty, const double* tz, int32_t* nb,
-                                                  int32_t* nbc) {
+constexpr int kKnnBlocksPerSm = 8;
+constexpr int kKnnOctantBlocksPerSm = 4;
+
+template <int D, bool OCT, bool RANKED>
+__global__ void __launch_bounds__(128, OCT ? kKnnOctantBlocksPerSm : kKnnBlocksPerSm)
+    knn_kernel(GridDev g, SearchFrame fr, SearchParams p, int64_t nt, int gs, const double* tx,
+               const double* ty, const double* tz, int32_t* nb, int32_t* nbc) {
   constexpr int NB = OCT ? (1 << D) : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;

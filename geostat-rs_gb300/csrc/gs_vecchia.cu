@@ -453,11 +453,9 @@ __device__ bool vecchia_refine_fp64(const VArgs& a, const DevModel& mdl, const E
 // register-row solver of gs_warp.cuh (no block barriers).  The likelihood
 // form is compiled for four blocks (16 warps) per SM (128 registers: the
 // matrix entries stay in shared memory); the REML form keeps the default.
-#ifndef GS_VECCHIA_MIN_BLOCKS
-#define GS_VECCHIA_MIN_BLOCKS 4
-#endif
+constexpr int kVWBlocksPerSm = 4;
 template <int D, bool REML>
-__global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : GS_VECCHIA_MIN_BLOCKS)
+__global__ void __launch_bounds__(32 * kVWarps, REML ? 1 : kVWBlocksPerSm)
     vecchia_warp_kernel(VArgs a, ExpTable tab_g, DfConsts kc, Exp64Table et_g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ExpTable tab;
