@@ -8,6 +8,8 @@
 #include <cstring>
 #include <atomic>
 #include <mutex>
+#include <map>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -574,6 +576,22 @@ constexpr int64_t kRouteSample = 16384;
 // smaller calls use the default.
 int size_class(int64_t nt) { return nt >= kTuneMinTargets ? 1 : 0; }
 
+// Shapes tuned by earlier predictors, keyed by what decides the best launch
+// shape: device, dimension, neighbour slots, drift terms, nested structures,
+// binning, cross-validation exclusion and size class.  A predictor whose
+// first call of a size class finds its key here starts from that shape
+// instead of timing the candidates again (repeated cross-validation or
+// tuning calls build a new predictor each time).
+struct TuneKey {
+  int device, dim, kout, p, ns, binnable, excl, cls;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(device, dim, kout, p, ns, binnable, excl, cls) <
+           std::tie(o.device, o.dim, o.kout, o.p, o.ns, o.binnable, o.excl, o.cls);
+  }
+};
+std::mutex g_tuned_mu;
+std::map<TuneKey, Tiles> g_tuned;
+
 // Launch shape without measurement: the longest run that still gives every
 // SM a few blocks.
 Tiles default_tiles(int64_t nt, bool binnable) {
@@ -776,12 +794,25 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
   // the first chunk (timed calls only), or the default
   Tiles tiles = default_tiles(nt, binnable);
   bool tune_now = false;
+  const TuneKey tkey{k->device, dim, kout, p, k->dm.ns, binnable ? 1 : 0, excl_labels ? 1 : 0,
+                     size_class(nt)};
   if (mixed) {
     std::lock_guard<std::mutex> lk(k->tiles_mu);
     auto it = k->tiles.find(size_class(nt));
-    if (k->pinned.run > 0) tiles = k->pinned;
-    else if (it != k->tiles.end()) tiles = it->second;
-    else tune_now = timed && nt >= kTuneMinTargets;
+    if (k->pinned.run > 0) {
+      tiles = k->pinned;
+    } else if (it != k->tiles.end()) {
+      tiles = it->second;
+    } else {
+      std::lock_guard<std::mutex> gl(g_tuned_mu);
+      auto g = g_tuned.find(tkey);
+      if (g != g_tuned.end()) {
+        tiles = g->second;
+        k->tiles[size_class(nt)] = tiles;
+      } else {
+        tune_now = timed && nt >= kTuneMinTargets;
+      }
+    }
   }
   const bool binned = binnable;
   DevBuf nb, nbc, flag, tlist, nsel, tmp, bins, counts;
@@ -949,6 +980,8 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
         if (!rc) {
           std::lock_guard<std::mutex> lk(k->tiles_mu);
           k->tiles[size_class(nt)] = tiles;
+          std::lock_guard<std::mutex> gl(g_tuned_mu);
+          g_tuned[tkey] = tiles;
         }
         if (rc) break;
       }

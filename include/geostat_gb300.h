@@ -203,13 +203,18 @@ int gs_kriging_block_cv(const gs_kriging* k, const int64_t* blocks_per_dim, doub
  * system on the two-warp solver); one or two systems per block -- on its
  * first 131,072 targets and keeps the fastest for every later call of at
  * least 65,536 targets; smaller and asynchronous calls before that use a
- * default.  Results of different shapes agree within the parity tolerance
- * (the order of roundings differs), and a predictor's results are
- * reproducible once its shapes are fixed.
+ * default.  A tuned shape is also kept for the process under the systems'
+ * shape (device, dimension, neighbour slots, drift terms, nested structures,
+ * binning, cross-validation or not): a later predictor of the same shape
+ * takes it on its first call instead of timing the candidates again.
+ * Results of different shapes agree within the parity tolerance (the order
+ * of roundings differs), and a predictor's results are reproducible once its
+ * shapes are fixed.
  * gs_kriging_set_tiles pins one shape for every call (run a power of two in
  * [1, 1024], bins 0/1, systems_per_block 1/2; run 0 unpins).
- * gs_kriging_tiles reports the shape a call with nt targets would use;
- * tuned = 0 default, 1 tuned, 2 pinned. */
+ * gs_kriging_tiles reports the shape this predictor has fixed for calls
+ * with nt targets: tuned = 0 none yet (its first call may still take one
+ * kept for the process), 1 tuned, 2 pinned. */
 int gs_kriging_set_tiles(gs_kriging* k, int run, int bins, int systems_per_block);
 int gs_kriging_tiles(const gs_kriging* k, int64_t nt, int* run, int* bins,
                      int* systems_per_block, int* tuned);
