@@ -646,9 +646,10 @@ struct BlockSpec {
 };
 
 // The factored global system's matrix-product form, prepared on first use by
-// a mixed-precision call (N solves with the factors: about 2 N^3 FP64 FMAs,
-// so a predictor used only at FP64 never pays for it).  Without device
-// memory for it, mixed-precision calls take the per-target solves.
+// a mixed-precision call of at least N / 4 targets (N solves with the
+// factors: about 2 N^3 FP64 FMAs, so a predictor used only at FP64, or only
+// for a few targets at a time, never pays for it).  Without device memory
+// for it, mixed-precision calls take the per-target solves.
 static int ensure_global_gemm(const gs_kriging* k) {
   std::lock_guard<std::mutex> lk(k->gemm_mu);
   if (k->gemm_state != 0) return GS_OK;
@@ -740,7 +741,11 @@ int predict_pass(const gs_kriging* k, int64_t nt, const double* tx, const double
     const int64_t warps = std::max<int64_t>(
         1, std::min<int64_t>((int64_t)sm_count() * 32, ((int64_t)512 << 20) / (16 * (int64_t)N)));
     DevBuf scratch;
-    if (precision != GS_PREC_FP64 && k->lu_state == 1) GS_TRY(ensure_global_gemm(k));
+    // the form is prepared by the first mixed call of at least N / 4 targets
+    // (its 2 N^3 FMAs are then at most four times the call's per-target
+    // solves, 2 N^2 each); smaller calls before it take the per-target solves
+    if (precision != GS_PREC_FP64 && k->lu_state == 1 && 4 * nt >= N)
+      GS_TRY(ensure_global_gemm(k));
     const bool gemm = precision != GS_PREC_FP64 && k->lu_state == 1 && k->gemm_state == 1;
     if (!gemm) GS_TRY(scratch.alloc((size_t)warps * 2 * N * 8, stream));
     KrigeArgs g = a;

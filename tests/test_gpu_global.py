@@ -163,3 +163,35 @@ def test_global_matrix_form_falls_back_without_room():
     for out in (mixed, again):
         assert (out[2] == f64[2]).all() and (f64[2] == 0).all()
         assert np.array_equal(out[0], f64[0]) and np.array_equal(out[1], f64[1])
+
+
+def test_global_small_calls_take_per_target_solves_until_a_large_one():
+    """A mixed-precision call of fewer than N / 4 targets does not prepare the
+    matrix-product form (its 2 N^3 FMAs would be more than four times the
+    call's per-target solves): it takes the per-target solves with the
+    factors, the FP64 build's kernel, so its results equal the FP64 call's.
+    A call of at least N / 4 targets prepares the form; later small calls
+    use it (within the mixed tolerance of the FP64 build)."""
+    c = uniform_points(300, 2, 100, [1000.0, 1000.0])
+    v = smooth_values(c)
+    m = sph200_model()
+    k = G.Kriging.new(G.PointSet(c, v), m)
+    small = uniform_points(50, 2, 101, [1000.0, 1000.0])
+    large = uniform_points(400, 2, 102, [1000.0, 1000.0])
+    first = k.predict_many(small, "mixed", full=True)
+    f64 = k.predict_many(small, "fp64", full=True)
+    assert (first.status == f64.status).all() and (f64.status == 0).all()
+    assert np.array_equal(first.value, f64.value)
+    assert np.array_equal(first.variance, f64.variance)
+    assert np.array_equal(first.lagrange, f64.lagrange)
+    big = k.predict_many(large, "mixed", full=True)
+    big64 = k.predict_many(large, "fp64", full=True)
+    vs = float(np.mean(np.abs(v)))
+    assert (big.status == big64.status).all()
+    assert_close(big.value, big64.value, vs, 1e-9, "value")
+    assert_close(big.variance, big64.variance, 1e-3 * m.total_sill(), 1e-9, "variance")
+    again = k.predict_many(small, "mixed", full=True)
+    assert (again.status == f64.status).all()
+    assert_close(again.value, f64.value, vs, 1e-9, "value")
+    assert_close(again.variance, f64.variance, 1e-3 * m.total_sill(), 1e-9, "variance")
+    assert_close(again.lagrange, f64.lagrange, 1.0, 1e-9, "lagrange")
