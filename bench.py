@@ -438,14 +438,9 @@ def cv_bench(args, coords, values, model, log):
             "max_rel_variance": rel(cv.variance[sample], np.array(ref_v), 1e-3)}
 
 
-def global_bench(args, log):
-    """Global-neighbourhood ordinary kriging (kriging.rs:396-406): the 2-D
-    workload's 2,000 points (uniform in 1000 x 1000 m, 10 + field, nugget 0.1 +
-    Sph(1, 200 m)) with no neighbour limit -- one 2,001-unknown system factored
-    at build -- predicted at the 100 x 100 grid: the mixed path (the system's
-    matrix-product form: FP64 dot products for estimates, a double-float GEMM
-    for variances) and the FP64 build (per-target solves with the LU
-    factors); the oracle (the same global LU path) on all host cores."""
+def global_setup():
+    """The global-neighbourhood workload: 2,000 points uniform in 1000 x 1000 m,
+    10 + field of nugget 0.1 + Sph(1, 200 m), targets the 100 x 100 grid."""
     import geostat_rs as G
     from geostat_rs.model import Structure, VariogramModel
     n = 2000
@@ -455,6 +450,19 @@ def global_bench(args, log):
     g = (np.arange(100) + 0.5) * 10.0
     yy, xx = np.meshgrid(g, g, indexing="ij")
     t = np.stack([xx.ravel(), yy.ravel()], 1)
+    return n, c, v, m, t
+
+
+def global_bench(args, log):
+    """Global-neighbourhood ordinary kriging (kriging.rs:396-406): the 2-D
+    workload's 2,000 points (uniform in 1000 x 1000 m, 10 + field, nugget 0.1 +
+    Sph(1, 200 m)) with no neighbour limit -- one 2,001-unknown system factored
+    at build -- predicted at the 100 x 100 grid: the mixed path (the system's
+    matrix-product form: FP64 dot products for estimates, a double-float GEMM
+    for variances) and the FP64 build (per-target solves with the LU
+    factors); the oracle (the same global LU path) on all host cores."""
+    import geostat_rs as G
+    n, c, v, m, t = global_setup()
     t0 = time.perf_counter()
     k = G.Kriging.new(G.PointSet(c, v), m)
     build = time.perf_counter() - t0
@@ -1065,6 +1073,16 @@ def profile_case(args):
             r = preds[0].predict_many(t, "mixed", full=True)
         torch.cuda.synchronize()
         print(f"profile clustered: {len(t)} targets, mean estimate {np.nanmean(r.value):.6f}")
+    if args.profile_global:
+        # the global-neighbourhood workload; the first call prepares the
+        # system's matrix-product form, the second is the steady state
+        n, c, v, m, t = global_setup()
+        t = t[:args.profile_global]
+        k = G.Kriging.new(G.PointSet(c, v), m)
+        for _ in range(2):
+            out = k.predict_many(t, full=True)
+        torch.cuda.synchronize()
+        print(f"profile global: {len(t)} targets, mean estimate {np.nanmean(out.value):.6f}")
     if args.profile_vecchia:
         from geostat_rs.model import Structure, VariogramModel
         n = args.profile_vecchia
@@ -1128,6 +1146,9 @@ def main():
     ap.add_argument("--profile-clustered", type=int, default=0,
                     help="run two ordinary-kriging passes of the clustered workload over N "
                          "grid targets and exit")
+    ap.add_argument("--profile-global", type=int, default=0,
+                    help="run two mixed-precision passes of the global-neighbourhood workload "
+                         "over its first N grid targets (at most 10,000) and exit")
     ap.add_argument("--profile-vecchia", type=int, default=0,
                     help="run one 16-candidate Vecchia batch on N points and exit")
     ap.add_argument("--profile-reml", type=int, default=0,
@@ -1140,7 +1161,8 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
-    if args.profile_case or args.profile_vecchia or args.profile_clustered or args.profile_reml:
+    if (args.profile_case or args.profile_vecchia or args.profile_clustered or args.profile_reml
+            or args.profile_global):
         profile_case(args)
         return
     if args.impl == "reference":

@@ -1411,14 +1411,18 @@ __global__ void global_rhs_kernel(KrigeArgs a, DevModel m, int N, int64_t T, flo
 // [64 by, 64 by + 64) of R with the targets [64 bx, 64 bx + 64) of B over
 // the columns from 64 by on, 16 columns per stage, each thread a 4 x 4 block of X in
 // double-float (two FP32x2 accumulator pairs per row, compensated), and
-// writes sum_i B_it X_it over its row tile to Q[by * T + t] (hi, lo).
+// writes sum_i B_it X_it over its row tile to Q[by * T + t] (hi, lo).  The
+// stages are double-buffered in shared memory: the next stage's entries are
+// loaded into registers while the current one is multiplied, so one barrier
+// per stage and no wait on the loads before the products.
 constexpr int kGT = 64;   // rows / targets per tile
 constexpr int kGK = 16;   // columns per stage
-__global__ void __launch_bounds__(256) global_quad_kernel(int N, int64_t T, const float* Rh,
-                                                         const float* Rl, const float* Bh,
-                                                         const float* Bl, df* Q) {
-  __shared__ __align__(16) float Ms[2][kGK][kGT + 4];
-  __shared__ __align__(16) float Bs[2][kGK][kGT + 4];
+constexpr int kGE = kGT * kGK / 256;  // entries of each tile a thread stages
+__global__ void __launch_bounds__(256, 2) global_quad_kernel(int N, int64_t T, const float* Rh,
+                                                            const float* Rl, const float* Bh,
+                                                            const float* Bl, df* Q) {
+  __shared__ __align__(16) float Ms[2][2][kGK][kGT + 4];  // [stage buffer][hi, lo]
+  __shared__ __align__(16) float Bs[2][2][kGK][kGT + 4];
   __shared__ df red[16][kGT];
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const int64_t i0 = (int64_t)blockIdx.y * kGT, t0 = (int64_t)blockIdx.x * kGT;
@@ -1434,42 +1438,53 @@ __global__ void __launch_bounds__(256) global_quad_kernel(int N, int64_t T, cons
   // 2 sum_(i<k) R_ik b_i b_k: columns from the diagonal tile on, with the
   // entries left of the diagonal weighted 0 and those right of it 2 (exact
   // scalings) -- half the products of the full form
+  float mh[kGE], ml[kGE], bh[kGE], bl[kGE];
+  // entries of stage k0 into registers: thread tid holds entries tid + 256 j
+  // of the row tile (row r = e / kGK, column kk = e % kGK) and of the target
+  // tile (column kk = e / kGT, target tt = e % kGT); zero outside R's upper
+  // triangle and outside the matrices
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int j = 0; j < kGE; ++j) {
+      const int e = tid + 256 * j;
+      const int64_t gi = i0 + e / kGK;
+      const int gk = k0 + e % kGK;
+      const bool in = gi < N && gk < N && gk >= gi;
+      mh[j] = in ? Rh[gi * N + gk] : 0.0f;
+      ml[j] = in ? Rl[gi * N + gk] : 0.0f;
+      const int gkb = k0 + e / kGT;
+      const int64_t gt = t0 + e % kGT;
+      const bool inb = gkb < N && gt < T;
+      bh[j] = inb ? Bh[(int64_t)gkb * T + gt] : 0.0f;
+      bl[j] = inb ? Bl[(int64_t)gkb * T + gt] : 0.0f;
+    }
+  };
+  fetch((int)i0);
+  int buf = 0;
   for (int k0 = (int)i0; k0 < N; k0 += kGK) {
-    for (int e = tid; e < kGT * kGK; e += 256) {
+#pragma unroll
+    for (int j = 0; j < kGE; ++j) {
+      const int e = tid + 256 * j;
       const int r = e / kGK, kk = e % kGK;
-      const int64_t gi = i0 + r;
-      const int gk = k0 + kk;
-      float h = 0.0f, l = 0.0f;
-      if (gi < N && gk < N && gk >= gi) {
-        const float w = gk == gi ? 1.0f : 2.0f;
-        h = w * Rh[gi * N + gk];
-        l = w * Rl[gi * N + gk];
-      }
-      Ms[0][kk][r] = h;
-      Ms[1][kk][r] = l;
+      const float w = k0 + kk == i0 + r ? 1.0f : 2.0f;
+      Ms[buf][0][kk][r] = w * mh[j];
+      Ms[buf][1][kk][r] = w * ml[j];
+      Bs[buf][0][e / kGT][e % kGT] = bh[j];
+      Bs[buf][1][e / kGT][e % kGT] = bl[j];
     }
-    for (int e = tid; e < kGK * kGT; e += 256) {
-      const int kk = e / kGT, tt = e % kGT;
-      const int gk = k0 + kk;
-      const int64_t gt = t0 + tt;
-      float h = 0.0f, l = 0.0f;
-      if (gk < N && gt < T) {
-        h = Bh[(int64_t)gk * T + gt];
-        l = Bl[(int64_t)gk * T + gt];
-      }
-      Bs[0][kk][tt] = h;
-      Bs[1][kk][tt] = l;
-    }
+    // a thread stores into this buffer again two stages later, after the
+    // next stage's barrier, which every thread reaches only once done here
     __syncthreads();
+    if (k0 + kGK < N) fetch(k0 + kGK);
 #pragma unroll 4
     for (int kk = 0; kk < kGK; ++kk) {
-      const float4 mh = *reinterpret_cast<const float4*>(&Ms[0][kk][ty * 4]);
-      const float4 ml = *reinterpret_cast<const float4*>(&Ms[1][kk][ty * 4]);
-      const float4 bh = *reinterpret_cast<const float4*>(&Bs[0][kk][tx * 4]);
-      const float4 bl = *reinterpret_cast<const float4*>(&Bs[1][kk][tx * 4]);
-      const float ah[4] = {mh.x, mh.y, mh.z, mh.w}, al[4] = {ml.x, ml.y, ml.z, ml.w};
-      const float2 bh2[2] = {make_float2(bh.x, bh.y), make_float2(bh.z, bh.w)};
-      const float2 bl2[2] = {make_float2(bl.x, bl.y), make_float2(bl.z, bl.w)};
+      const float4 mh4 = *reinterpret_cast<const float4*>(&Ms[buf][0][kk][ty * 4]);
+      const float4 ml4 = *reinterpret_cast<const float4*>(&Ms[buf][1][kk][ty * 4]);
+      const float4 bh4 = *reinterpret_cast<const float4*>(&Bs[buf][0][kk][tx * 4]);
+      const float4 bl4 = *reinterpret_cast<const float4*>(&Bs[buf][1][kk][tx * 4]);
+      const float ah[4] = {mh4.x, mh4.y, mh4.z, mh4.w}, al[4] = {ml4.x, ml4.y, ml4.z, ml4.w};
+      const float2 bh2[2] = {make_float2(bh4.x, bh4.y), make_float2(bh4.z, bh4.w)};
+      const float2 bl2[2] = {make_float2(bl4.x, bl4.y), make_float2(bl4.z, bl4.w)};
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const float2 a2 = make_float2(ah[r], ah[r]), l2 = make_float2(al[r], al[r]);
@@ -1485,7 +1500,7 @@ __global__ void __launch_bounds__(256) global_quad_kernel(int N, int64_t T, cons
         }
       }
     }
-    __syncthreads();
+    buf ^= 1;
   }
   // epilogue: this thread's rows' contribution sum_r B_(i0+4ty+r),t X_r,t
   df part[4];
