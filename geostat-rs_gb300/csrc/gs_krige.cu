@@ -1385,25 +1385,49 @@ __global__ void global_vectors_kernel(int N, int n, int p, int simple, double me
 }
 
 // Right-hand sides of a tile of targets, split: Bh/Bl[i * T + t] (i < N
-// system rows, t < T targets of this chunk).
+// system rows, t < T targets of this chunk), with lambda . b and a . b in
+// FP64 while b is at hand: a block takes 32 consecutive targets (one per
+// lane) and its 8 warps the rows i = w (mod 8); VL[t] = the warps' partial
+// sums added in warp order.
 template <int D>
-__global__ void global_rhs_kernel(KrigeArgs a, DevModel m, int N, int64_t T, float* Bh, float* Bl) {
+__global__ void __launch_bounds__(256) global_rhs_kernel(KrigeArgs a, DevModel m, int N, int64_t T,
+                                                        const double* lambda, const double* arow,
+                                                        float* Bh, float* Bl, double2* VL) {
+  __shared__ double2 part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n = (int)a.n;
-  const int64_t total = (int64_t)N * T;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / T, t = e - i * T;
-    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
-    double b;
-    if (i < n) {
-      const double h[3] = {a.x[i] - tp[0], a.y[i] - tp[1], D == 3 ? a.z[i] - tp[2] : 0.0};
-      b = cov_fp64<D>(m, h);
-    } else {
-      b = basis_at<D>(a, tp, a.tdrift ? a.tdrift + t * a.nv : nullptr, (int)(i - n));
+  for (int64_t t0 = (int64_t)blockIdx.x * 32; t0 < T; t0 += (int64_t)gridDim.x * 32) {
+    const int64_t t = t0 + lane;
+    double v = 0.0, lg = 0.0;
+    if (t < T) {
+      const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
+      const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
+      for (int i = w; i < N; i += 8) {
+        double b;
+        if (i < n) {
+          const double h[3] = {a.x[i] - tp[0], a.y[i] - tp[1], D == 3 ? a.z[i] - tp[2] : 0.0};
+          b = cov_fp64<D>(m, h);
+        } else {
+          b = basis_at<D>(a, tp, trow, i - n);
+        }
+        const float h = (float)b;
+        Bh[(int64_t)i * T + t] = h;
+        Bl[(int64_t)i * T + t] = (float)(b - (double)h);
+        v = fma(lambda[i], b, v);
+        lg = fma(arow[i], b, lg);
+      }
     }
-    const float h = (float)b;
-    Bh[e] = h;
-    Bl[e] = (float)(b - (double)h);
+    part[w][lane] = make_double2(v, lg);
+    __syncthreads();
+    if (w == 0 && t < T) {
+      double2 sum = part[0][lane];
+      for (int u = 1; u < 8; ++u) {
+        sum.x += part[u][lane].x;
+        sum.y += part[u][lane].y;
+      }
+      VL[t] = sum;
+    }
+    __syncthreads();
   }
 }
 
@@ -1534,57 +1558,32 @@ __global__ void __launch_bounds__(256, 2) global_quad_kernel(int N, int64_t T, c
   }
 }
 
-// Outputs of a tile of targets: one warp per target; FP64 right-hand side,
-// lambda . b and a . b in FP64, the quadratic form from the row tiles'
-// partial sums in tile order.
-template <int D>
-__global__ void global_finish_kernel(KrigeArgs a, DevModel m, int N, int64_t T, int ntiles,
-                                     const double* lambda, const double* arow, const df* Q) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+// Outputs of a tile of targets: one thread per target; the estimate and
+// Lagrange multiplier from VL (lambda . b, a . b), the quadratic form from
+// the row tiles' partial sums in tile order.
+__global__ void global_finish_kernel(KrigeArgs a, DevModel m, int64_t T, int ntiles,
+                                     const double2* VL, const df* Q) {
   const int n = (int)a.n, p = a.p;
   const double kNaN = __longlong_as_double(0x7ff8000000000000ll);
-  for (int64_t t = w0; t < T; t += nw) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T;
+       t += (int64_t)gridDim.x * blockDim.x) {
     uint8_t st = GS_ST_OK;
     if (n < a.min_nb) st = GS_ST_NO_NEIGHBORS;
     else if (n < p) st = GS_ST_INSUFFICIENT_DATA;
     if (st != GS_ST_OK) {
-      if (lane == 0) {
-        a.out_v[t] = kNaN;
-        a.out_var[t] = kNaN;
-        if (a.out_lag) a.out_lag[t] = kNaN;
-        a.out_st[t] = st;
-      }
+      a.out_v[t] = kNaN;
+      a.out_var[t] = kNaN;
+      if (a.out_lag) a.out_lag[t] = kNaN;
+      a.out_st[t] = st;
       continue;
     }
-    const double tp[3] = {a.tx[t], a.ty[t], D == 3 ? a.tz[t] : 0.0};
-    const double* trow = a.tdrift ? a.tdrift + t * a.nv : nullptr;
-    double v = 0.0, lg = 0.0;
-    for (int i = lane; i < N; i += 32) {
-      double b;
-      if (i < n) {
-        const double h[3] = {a.x[i] - tp[0], a.y[i] - tp[1], D == 3 ? a.z[i] - tp[2] : 0.0};
-        b = cov_fp64<D>(m, h);
-      } else {
-        b = basis_at<D>(a, tp, trow, i - n);
-      }
-      v = fma(lambda[i], b, v);
-      lg = fma(arow[i], b, lg);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      v += __shfl_xor_sync(0xffffffffu, v, o);
-      lg += __shfl_xor_sync(0xffffffffu, lg, o);
-    }
-    if (lane == 0) {
-      df q = Q[t];
-      for (int r = 1; r < ntiles; ++r) q = df_add(q, Q[(int64_t)r * T + t]);
-      a.out_v[t] = a.method == GS_SIMPLE ? a.sk_mean + v : v;
-      a.out_var[t] = fmax(m.c0 - df_to_double(q), 0.0);
-      if (a.out_lag) a.out_lag[t] = a.method == GS_SIMPLE ? kNaN : lg;
-      a.out_st[t] = GS_ST_OK;
-    }
+    const double2 vl = VL[t];
+    df q = Q[t];
+    for (int r = 1; r < ntiles; ++r) q = df_add(q, Q[(int64_t)r * T + t]);
+    a.out_v[t] = a.method == GS_SIMPLE ? a.sk_mean + vl.x : vl.x;
+    a.out_var[t] = fmax(m.c0 - df_to_double(q), 0.0);
+    if (a.out_lag) a.out_lag[t] = a.method == GS_SIMPLE ? kNaN : vl.y;
+    a.out_st[t] = GS_ST_OK;
   }
 }
 
@@ -1784,9 +1783,12 @@ int global_gemm_launch(const KrigeArgs& a, const DevModel& m, int N, const float
   const int ntiles = (N + kGT - 1) / kGT;
   DevBuf B, Q;
   GS_TRY(B.alloc((size_t)N * T * 8, stream));
-  GS_TRY(Q.alloc((size_t)ntiles * T * sizeof(df), stream));
+  // Q's row-tile sums, then VL (16-byte aligned)
+  const size_t vl_off = ((size_t)ntiles * T * sizeof(df) + 15) & ~(size_t)15;
+  GS_TRY(Q.alloc(vl_off + (size_t)T * sizeof(double2), stream));
   float* Bh = (float*)B.ptr;
   float* Bl = Bh + (size_t)N * T;
+  double2* VL = (double2*)((char*)Q.ptr + vl_off);
   for (int64_t c0 = 0; c0 < a.ntl; c0 += T) {
     const int64_t tc = std::min<int64_t>(T, a.ntl - c0);
     KrigeArgs ca = a;
@@ -1801,18 +1803,15 @@ int global_gemm_launch(const KrigeArgs& a, const DevModel& m, int N, const float
     // Bh / Bl laid out with this chunk's count as the row stride
     float* bh = Bh;
     float* bl = Bh + (size_t)N * tc;
-    const int rb = (int)std::min<int64_t>(((int64_t)N * tc + 255) / 256, (int64_t)sm_count() * 64);
-    if (a.dim == 2) global_rhs_kernel<2><<<rb, 256, 0, stream>>>(ca, m, N, tc, bh, bl);
-    else global_rhs_kernel<3><<<rb, 256, 0, stream>>>(ca, m, N, tc, bh, bl);
+    const int rb = (int)std::min<int64_t>((tc + 31) / 32, (int64_t)sm_count() * 8);
+    if (a.dim == 2)
+      global_rhs_kernel<2><<<rb, 256, 0, stream>>>(ca, m, N, tc, lambda, arow, bh, bl, VL);
+    else
+      global_rhs_kernel<3><<<rb, 256, 0, stream>>>(ca, m, N, tc, lambda, arow, bh, bl, VL);
     dim3 grid((unsigned)((tc + kGT - 1) / kGT), (unsigned)ntiles);
     global_quad_kernel<<<grid, 256, 0, stream>>>(N, tc, Rh, Rl, bh, bl, (df*)Q.ptr);
-    const int64_t fw = std::min<int64_t>(tc, (int64_t)sm_count() * 32);
-    if (a.dim == 2)
-      global_finish_kernel<2><<<(int)((fw * 32 + 127) / 128), 128, 0, stream>>>(
-          ca, m, N, tc, ntiles, lambda, arow, (const df*)Q.ptr);
-    else
-      global_finish_kernel<3><<<(int)((fw * 32 + 127) / 128), 128, 0, stream>>>(
-          ca, m, N, tc, ntiles, lambda, arow, (const df*)Q.ptr);
+    const int64_t fb = std::min<int64_t>((tc + 127) / 128, (int64_t)sm_count() * 16);
+    global_finish_kernel<<<(int)fb, 128, 0, stream>>>(ca, m, tc, ntiles, VL, (const df*)Q.ptr);
     GS_CUDA(cudaGetLastError());
     count_launch(3);
   }
