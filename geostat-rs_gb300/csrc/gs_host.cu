@@ -10,7 +10,6 @@
 #include <algorithm>
 #include <cstring>
 #include <limits>
-#include <queue>
 #include <vector>
 
 #include "gs_common.cuh"
@@ -244,168 +243,26 @@ double Xoshiro::normal() {
 }
 
 // ------------------------------------------------------- max-min order --
-// Farthest-point ordering with lazy key refresh (the algorithm of
-// vecchia.rs:144-215).  Keys only decrease as points are selected, so a
-// popped key that still dominates the heap after refreshing is exact.  The
-// refresh needs the exact nearest selected point; it comes from a uniform
-// grid over the selected points (any exact nearest-neighbour query yields
-// the same squared distance, which is all the ordering consumes).
+// Farthest-point ordering (vecchia.rs:144-215): the first point is the one
+// nearest the centroid; every later step takes the unselected point whose
+// squared distance to its nearest selected point is largest, ties going to
+// the larger index (the reference's heap order over (distance, index) under
+// f64::total_cmp).  The reference finds that point with lazily refreshed
+// heap keys; any exact search selects the same sequence.  Here every
+// unselected point keeps its exact key, lowered as soon as a newly selected
+// point lands closer, and a winner tree over the keys gives the maximum.  A
+// selected point can only lower points within its own key distance (it was
+// the maximum), so each step enumerates that ball.  The points are stored
+// (as slots) in a spatial order that makes the ball cheap to enumerate: a
+// uniform grid of about two points per cell when no cell is crowded, else a
+// balanced k-d tree whose leaves are runs of 16-31 slots.
 namespace {
 
-struct Key {
-  double d2;
-  int64_t idx;
-};
 inline int64_t tkey(double v) {
   int64_t b;
   std::memcpy(&b, &v, 8);
   return b ^ (int64_t)(((uint64_t)(b >> 63)) >> 1);
 }
-struct KeyLess {
-  bool operator()(const Key& a, const Key& b) const {
-    int64_t x = tkey(a.d2), y = tkey(b.d2);
-    if (x != y) return x < y;
-    return a.idx < b.idx;
-  }
-};
-
-// Multi-resolution grid over the selected points.  Level l has cells 2^l
-// times wider than level 0 (about one point per cell when all n points are
-// selected).  A query uses the finest level whose cells hold about one
-// selected point each, so the exact nearest neighbour is found within a
-// couple of rings whatever the current selected count.
-class SelectedGrid {
- public:
-  SelectedGrid(const std::vector<double>& pts, int dim, int64_t n) : dim_(dim) {
-    for (int d = 0; d < dim; ++d) {
-      lo_[d] = std::numeric_limits<double>::infinity();
-      hi_[d] = -lo_[d];
-    }
-    for (int64_t i = 0; i < n; ++i)
-      for (int d = 0; d < dim; ++d) {
-        lo_[d] = std::min(lo_[d], pts[i * dim + d]);
-        hi_[d] = std::max(hi_[d], pts[i * dim + d]);
-      }
-    double ext = 0.0;
-    for (int d = 0; d < dim; ++d) ext = std::max(ext, hi_[d] - lo_[d]);
-    if (!(ext > 0.0)) ext = 1.0;
-    double vol = 1.0;
-    int act = 0;
-    for (int d = 0; d < dim; ++d)
-      if (hi_[d] - lo_[d] > ext * 1e-9) {
-        vol *= hi_[d] - lo_[d];
-        ++act;
-      }
-    if (act == 0) act = 1;
-    double cell = pow(vol / (double)std::max<int64_t>(n, 1), 1.0 / act);
-    if (!(cell > 0.0)) cell = ext;
-    for (int guard = 0; guard < 64; ++guard) {
-      Level L;
-      L.cell = cell;
-      int64_t total = 1;
-      for (int d = 0; d < dim; ++d) {
-        double c = (hi_[d] - lo_[d] > ext * 1e-9) ? ceil((hi_[d] - lo_[d]) / cell) : 1.0;
-        L.n[d] = std::max<int64_t>(1, (int64_t)std::min(c, 1e9));
-        total *= L.n[d];
-      }
-      if (total <= 4 * std::max<int64_t>(n, 16) || levels_.size() > 0) {
-        L.head.assign(total, -1);
-        levels_.push_back(std::move(L));
-      }
-      if (total <= 4) break;
-      cell *= 2.0;
-    }
-    pts_.reserve(n * dim);
-  }
-  void insert(const double* p) {
-    const int64_t id = (int64_t)(pts_.size() / dim_);
-    for (int d = 0; d < dim_; ++d) pts_.push_back(p[d]);
-    for (auto& L : levels_) {
-      int64_t c = cell_of(L, p);
-      L.next.push_back(L.head[c]);
-      L.head[c] = id;
-    }
-  }
-  // Exact squared distance to the nearest inserted point.
-  double nearest_d2(const double* p) const {
-    const int64_t nsel = (int64_t)(pts_.size() / dim_);
-    size_t lv = 0;
-    while (lv + 1 < levels_.size() && (int64_t)levels_[lv].head.size() > 2 * nsel) ++lv;
-    const Level& L = levels_[lv];
-    int64_t tc[3] = {0, 0, 0};
-    cell_coords(L, p, tc);
-    double best = std::numeric_limits<double>::infinity();
-    int64_t maxring = 0;
-    for (int d = 0; d < dim_; ++d) maxring = std::max(maxring, L.n[d]);
-    for (int64_t ring = 0; ring <= maxring; ++ring) {
-      double rmin = std::max((double)ring - 1.0 - 1e-9, 0.0) * L.cell;
-      if (rmin * rmin > best) break;
-      visit_shell(L, tc, ring, [&](int64_t cell) {
-        for (int64_t q = L.head[cell]; q >= 0; q = L.next[q]) {
-          double s = 0.0;
-          for (int d = 0; d < dim_; ++d) {
-            double dd = pts_[q * dim_ + d] - p[d];
-            s += dd * dd;
-          }
-          if (s < best) best = s;
-        }
-      });
-    }
-    return best;
-  }
-
- private:
-  struct Level {
-    double cell = 1.0;
-    int64_t n[3] = {1, 1, 1};
-    std::vector<int64_t> head, next;
-  };
-  void cell_coords(const Level& L, const double* p, int64_t* c) const {
-    for (int d = 0; d < dim_; ++d) {
-      double q = floor((p[d] - lo_[d]) / L.cell);
-      c[d] = q < 0 ? 0 : (q >= (double)L.n[d] ? L.n[d] - 1 : (int64_t)q);
-    }
-  }
-  int64_t cell_of(const Level& L, const double* p) const {
-    int64_t c[3] = {0, 0, 0};
-    cell_coords(L, p, c);
-    int64_t id = 0, stride = 1;
-    for (int d = 0; d < dim_; ++d) {
-      id += c[d] * stride;
-      stride *= L.n[d];
-    }
-    return id;
-  }
-  template <class F>
-  void visit_shell(const Level& L, const int64_t* tc, int64_t r, F&& f) const {
-    int64_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int d = 0; d < dim_; ++d) {
-      lo[d] = tc[d] - r;
-      hi[d] = tc[d] + r;
-    }
-    const int64_t* n = L.n;
-    int64_t zlo = dim_ == 3 ? std::max<int64_t>(lo[2], 0) : 0;
-    int64_t zhi = dim_ == 3 ? std::min<int64_t>(hi[2], n[2] - 1) : 0;
-    int64_t ylo = std::max<int64_t>(lo[1], 0), yhi = std::min<int64_t>(hi[1], n[1] - 1);
-    int64_t xlo = std::max<int64_t>(lo[0], 0), xhi = std::min<int64_t>(hi[0], n[0] - 1);
-    for (int64_t z = zlo; z <= zhi; ++z) {
-      bool zface = dim_ == 3 && (z == lo[2] || z == hi[2]);
-      for (int64_t y = ylo; y <= yhi; ++y) {
-        bool yface = (y == lo[1] || y == hi[1]);
-        if (zface || yface || r == 0) {
-          for (int64_t x = xlo; x <= xhi; ++x) f(x + n[0] * (y + n[1] * z));
-        } else {
-          if (lo[0] >= 0) f(lo[0] + n[0] * (y + n[1] * z));
-          if (hi[0] < n[0] && hi[0] != lo[0]) f(hi[0] + n[0] * (y + n[1] * z));
-        }
-      }
-    }
-  }
-  int dim_;
-  double lo_[3], hi_[3];
-  std::vector<Level> levels_;
-  std::vector<double> pts_;
-};
 
 inline double dist2(const double* a, const double* b, int dim) {
   double s = 0.0;
@@ -415,6 +272,207 @@ inline double dist2(const double* a, const double* b, int dim) {
   }
   return s;
 }
+
+class MaxminLayout {
+ public:
+  MaxminLayout(const std::vector<double>& pts, int dim, int64_t n) : dim_(dim), n_(n) {
+    idx_.resize(n);
+    for (int64_t i = 0; i < n; ++i) idx_[i] = i;
+    if (!build_grid(pts)) build_tree(pts);
+    xs_.resize(n * dim);
+    for (int64_t j = 0; j < n; ++j)
+      for (int d = 0; d < dim; ++d) xs_[j * dim + d] = pts[idx_[j] * dim + d];
+    if (!grid_) tree_boxes();
+  }
+  int64_t point(int64_t j) const { return idx_[j]; }
+  const double* at(int64_t j) const { return &xs_[j * dim_]; }
+
+  // f(j) for every slot j whose point may lie closer than sqrt(R) to p:
+  // a superset of them, never missing one (see the bounds below)
+  template <class F>
+  void visit_ball(const double* p, double R, F&& f) const {
+    if (grid_) {
+      // a point q with dist2(q, p) < R has |q_d - p_d| < sqrt(R) (1 + 3u)
+      // per axis in exact terms (u = 2^-53); the slack (1e-9 relative, and
+      // 1e-12 of |p_d| + r absolute) exceeds that and the rounding of
+      // p_d -/+ r, and the cell index is monotone in its argument
+      const double r = sqrt(R);
+      int64_t clo[3] = {0, 0, 0}, chi[3] = {0, 0, 0};
+      for (int d = 0; d < dim_; ++d) {
+        const double rr = r + r * 1e-9 + 1e-12 * (fabs(p[d]) + r);
+        clo[d] = cell_coord(p[d] - rr, d);
+        chi[d] = cell_coord(p[d] + rr, d);
+      }
+      for (int64_t z = clo[2]; z <= chi[2]; ++z)
+        for (int64_t y = clo[1]; y <= chi[1]; ++y) {
+          const int64_t row = nc_[0] * (y + nc_[1] * z);
+          for (int64_t j = cstart_[row + clo[0]], je = cstart_[row + chi[0] + 1]; j < je; ++j) f(j);
+        }
+      return;
+    }
+    // k-d tree: a node is skipped when the squared gap between p and its
+    // box exceeds R; the gap per axis is computed from the box bound the
+    // way dist2 computes it from a coordinate inside the box, and rounding
+    // is monotone, so dist2 of every point inside is at least the gap
+    int64_t stack[130];
+    int sp = 0;
+    stack[sp++] = 1;
+    while (sp) {
+      const int64_t v = stack[--sp];
+      const double* lo = &blo_[v * 3];
+      const double* hi = &bhi_[v * 3];
+      double g2 = 0.0;
+      for (int d = 0; d < dim_; ++d) {
+        double g = 0.0;
+        if (p[d] < lo[d]) g = lo[d] - p[d];
+        else if (p[d] > hi[d]) g = p[d] - hi[d];
+        g2 += g * g;
+      }
+      if (g2 > R) continue;
+      if (v >= L_) {
+        for (int64_t j = leaf_begin(v - L_), je = leaf_begin(v - L_ + 1); j < je; ++j) f(j);
+      } else {
+        stack[sp++] = 2 * v + 1;
+        stack[sp++] = 2 * v;
+      }
+    }
+  }
+
+ private:
+  static constexpr int64_t kCrowded = 32;  // most points a grid cell may hold
+
+  // uniform grid of about two points per cell, slots sorted by cell; false
+  // when a coordinate is not finite or a cell holds more than kCrowded
+  bool build_grid(const std::vector<double>& pts) {
+    double hi[3];
+    for (int d = 0; d < dim_; ++d) {
+      lo_[d] = std::numeric_limits<double>::infinity();
+      hi[d] = -lo_[d];
+    }
+    for (int64_t i = 0; i < n_; ++i)
+      for (int d = 0; d < dim_; ++d) {
+        const double v = pts[i * dim_ + d];
+        if (!std::isfinite(v)) return false;
+        lo_[d] = std::min(lo_[d], v);
+        hi[d] = std::max(hi[d], v);
+      }
+    double ext = 0.0;
+    for (int d = 0; d < dim_; ++d) ext = std::max(ext, hi[d] - lo_[d]);
+    if (!(ext > 0.0) || !std::isfinite(ext)) return false;
+    double vol = 1.0;
+    int act = 0;
+    for (int d = 0; d < dim_; ++d)
+      if (hi[d] - lo_[d] > ext * 1e-9) {
+        vol *= hi[d] - lo_[d];
+        ++act;
+      }
+    cell_ = pow(vol * 2.0 / (double)n_, 1.0 / act);
+    if (!(cell_ > 0.0) || !std::isfinite(cell_)) return false;
+    double total = 1.0;
+    for (int d = 0; d < dim_; ++d) {
+      nc_[d] = 1;
+      if (hi[d] - lo_[d] > ext * 1e-9) {
+        const double c = ceil((hi[d] - lo_[d]) / cell_);
+        if (!(c < 1e12)) return false;
+        nc_[d] = std::max<int64_t>(1, (int64_t)c);
+      }
+      total *= (double)nc_[d];
+    }
+    if (total > 4.0 * (double)n_ + 64.0) return false;
+    const int64_t ncell = nc_[0] * nc_[1] * nc_[2];
+    std::vector<int64_t> cell_of(n_);
+    cstart_.assign(ncell + 1, 0);
+    for (int64_t i = 0; i < n_; ++i) {
+      int64_t id = 0, stride = 1;
+      for (int d = 0; d < dim_; ++d) {
+        id += cell_coord(pts[i * dim_ + d], d) * stride;
+        stride *= nc_[d];
+      }
+      cell_of[i] = id;
+      if (++cstart_[id + 1] > kCrowded) return false;
+    }
+    for (int64_t k = 0; k < ncell; ++k) cstart_[k + 1] += cstart_[k];
+    std::vector<int64_t> fill(cstart_.begin(), cstart_.end() - 1);
+    for (int64_t i = 0; i < n_; ++i) idx_[fill[cell_of[i]]++] = i;
+    grid_ = true;
+    return true;
+  }
+  int64_t cell_coord(double v, int d) const {
+    const double q = floor((v - lo_[d]) / cell_);
+    return q < 0.0 ? 0 : (q >= (double)nc_[d] ? nc_[d] - 1 : (int64_t)q);
+  }
+
+  // balanced k-d tree in heap layout: L_ leaves (a power of two), node v
+  // (1 <= v < 2 L_) covering leaves [k0, k1) holds slots
+  // [leaf_begin(k0), leaf_begin(k1)); each inner node splits its slots at
+  // its middle leaf boundary along its widest axis (coordinates compared in
+  // total order, so any input keeps the selection well defined)
+  void build_tree(const std::vector<double>& pts) {
+    L_ = 1;
+    while (L_ * 32 <= n_) L_ <<= 1;
+    for (int64_t v = 1; v < L_; ++v) {
+      int depth = 0;
+      while (((int64_t)2 << depth) <= v) ++depth;
+      const int64_t span = L_ >> depth, k0 = (v - ((int64_t)1 << depth)) * span;
+      const int64_t b = leaf_begin(k0), e = leaf_begin(k0 + span), mid = leaf_begin(k0 + span / 2);
+      double lo[3], hi[3];
+      for (int d = 0; d < dim_; ++d) {
+        lo[d] = std::numeric_limits<double>::infinity();
+        hi[d] = -lo[d];
+      }
+      for (int64_t k = b; k < e; ++k)
+        for (int d = 0; d < dim_; ++d) {
+          const double x = pts[idx_[k] * dim_ + d];
+          lo[d] = std::min(lo[d], x);
+          hi[d] = std::max(hi[d], x);
+        }
+      int ax = 0;
+      double w = -1.0;
+      for (int d = 0; d < dim_; ++d)
+        if (hi[d] - lo[d] > w) {
+          w = hi[d] - lo[d];
+          ax = d;
+        }
+      if (mid > b && mid < e)
+        std::nth_element(idx_.begin() + b, idx_.begin() + mid, idx_.begin() + e,
+                         [&](int64_t a, int64_t c) {
+                           return tkey(pts[a * dim_ + ax]) < tkey(pts[c * dim_ + ax]);
+                         });
+    }
+  }
+  // boxes of the leaves from their slots, of inner nodes from their children
+  void tree_boxes() {
+    blo_.assign(2 * L_ * 3, std::numeric_limits<double>::infinity());
+    bhi_.assign(2 * L_ * 3, -std::numeric_limits<double>::infinity());
+    for (int64_t k = 0; k < L_; ++k) {
+      double* lo = &blo_[(L_ + k) * 3];
+      double* hi = &bhi_[(L_ + k) * 3];
+      for (int64_t j = leaf_begin(k), je = leaf_begin(k + 1); j < je; ++j)
+        for (int d = 0; d < dim_; ++d) {
+          lo[d] = std::min(lo[d], xs_[j * dim_ + d]);
+          hi[d] = std::max(hi[d], xs_[j * dim_ + d]);
+        }
+    }
+    for (int64_t v = L_ - 1; v >= 1; --v)
+      for (int d = 0; d < 3; ++d) {
+        blo_[v * 3 + d] = std::min(blo_[2 * v * 3 + d], blo_[(2 * v + 1) * 3 + d]);
+        bhi_[v * 3 + d] = std::max(bhi_[2 * v * 3 + d], bhi_[(2 * v + 1) * 3 + d]);
+      }
+  }
+  // first slot of leaf k: floor(n k / L) without overflow
+  int64_t leaf_begin(int64_t k) const { return (n_ / L_) * k + (n_ % L_) * k / L_; }
+
+  int dim_;
+  int64_t n_;
+  std::vector<int64_t> idx_;  // slot -> point
+  std::vector<double> xs_;    // coordinates by slot
+  bool grid_ = false;
+  double lo_[3] = {0, 0, 0}, cell_ = 1.0;
+  int64_t nc_[3] = {1, 1, 1};
+  std::vector<int64_t> cstart_;  // grid: slots of cell c are [cstart_[c], cstart_[c + 1])
+  int64_t L_ = 1;
+  std::vector<double> blo_, bhi_;  // k-d tree: box of node v at [3 v, 3 v + 3)
+};
 
 }  // namespace
 
@@ -433,26 +491,53 @@ void maxmin_order(const std::vector<double>& pts, int dim, int64_t n, int64_t* o
       first = i;
     }
   }
-  SelectedGrid grid(pts, dim, n);
-  int64_t nsel = 0;
-  order[nsel++] = first;
-  grid.insert(&pts[first * dim]);
-  std::vector<Key> init;
-  init.reserve(n);
-  for (int64_t i = 0; i < n; ++i)
-    if (i != first) init.push_back({dist2(&pts[i * dim], &pts[first * dim], dim), i});
-  std::priority_queue<Key, std::vector<Key>, KeyLess> heap(KeyLess(), std::move(init));
-  KeyLess less;
-  while (!heap.empty()) {
-    Key top = heap.top();
-    heap.pop();
-    Key refreshed{grid.nearest_d2(&pts[top.idx * dim]), top.idx};
-    if (heap.empty() || !less(refreshed, heap.top())) {
-      order[nsel++] = top.idx;
-      grid.insert(&pts[top.idx * dim]);
-    } else {
-      heap.push(refreshed);
+  order[0] = first;
+  if (n == 1) return;
+  const MaxminLayout lay(pts, dim, n);
+  // keys by slot in total order (INT64_MIN once selected); win[v] is the
+  // slot of the largest (key, point index) below node v of a binary tree
+  // over the slots (leaves at size + j; slot n stands for padding)
+  std::vector<int64_t> key(n + 1), pid(n + 1);
+  int64_t sfirst = 0;
+  for (int64_t j = 0; j < n; ++j) {
+    pid[j] = lay.point(j);
+    key[j] = tkey(dist2(lay.at(j), &pts[first * dim], dim));
+    if (pid[j] == first) sfirst = j;
+  }
+  key[n] = std::numeric_limits<int64_t>::min();
+  pid[n] = -1;
+  int64_t size = 1;
+  while (size < n) size <<= 1;
+  std::vector<int64_t> win(2 * size);
+  auto better = [&](int64_t a, int64_t b) {
+    return (key[a] != key[b] ? key[a] > key[b] : pid[a] > pid[b]) ? a : b;
+  };
+  for (int64_t j = 0; j < size; ++j) win[size + j] = j < n ? j : n;
+  // slot j's key went down: a node changes only while j was its winner
+  auto lowered = [&](int64_t j) {
+    for (int64_t v = (size + j) >> 1; v >= 1; v >>= 1) {
+      const int64_t old = win[v];
+      win[v] = better(win[2 * v], win[2 * v + 1]);
+      if (old != j && win[v] == old) break;
     }
+  };
+  key[sfirst] = std::numeric_limits<int64_t>::min();
+  for (int64_t v = size - 1; v >= 1; --v) win[v] = better(win[2 * v], win[2 * v + 1]);
+  for (int64_t nsel = 1; nsel < n; ++nsel) {
+    const int64_t s = win[1];
+    order[nsel] = pid[s];
+    double R;
+    std::memcpy(&R, &key[s], 8);
+    key[s] = std::numeric_limits<int64_t>::min();
+    lowered(s);
+    const double* ps = lay.at(s);
+    lay.visit_ball(ps, R, [&](int64_t j) {
+      const int64_t e = tkey(dist2(lay.at(j), ps, dim));
+      if (e < key[j]) {
+        key[j] = e;
+        lowered(j);
+      }
+    });
   }
 }
 

@@ -107,6 +107,58 @@ def test_host_maxmin_degenerate_inputs():
     assert G.maxmin_order(one).tolist() == [0]
 
 
+def _maxmin_layout_cases():
+    """Inputs for both spatial layouts of the host ordering: spread-out sets
+    (the uniform grid, including exact distance ties on lattices and
+    coordinates far from the origin, where the grid's ball bounds must
+    absorb rounding) and crowded ones (the k-d tree)."""
+    rng = np.random.default_rng(17)
+    g2 = np.stack(np.meshgrid(np.arange(30.0), np.arange(30.0)), -1).reshape(-1, 2)
+    g3 = np.stack(np.meshgrid(np.arange(9.0), np.arange(9.0), np.arange(9.0)), -1).reshape(-1, 3)
+    blobs = rng.random((40, 2))[rng.integers(0, 40, 4000)] + 0.003 * rng.standard_normal((4000, 2))
+    crowd = rng.random((3000, 2))
+    crowd[1:2970] = 0.5 + 1e-6 * rng.random((2969, 2))
+    dup = rng.random((300, 3))
+    return {
+        "lattice 2-D": g2,
+        "lattice 3-D": g3,
+        "lattice, flat z": np.c_[g2, np.zeros(len(g2))],
+        "far from the origin 2-D": 1e6 + 1e3 * rng.random((5000, 2)),
+        "far from the origin 3-D": np.c_[5e5 + 1e4 * rng.random((3000, 2)), 100 * rng.random(3000)],
+        "rounded coordinates": np.round(rng.random((5000, 2)) * 50) / 50,
+        "blobs": blobs,
+        "one crowded cell": crowd,
+        "duplicates": np.r_[dup, dup[:120]],
+        "identical points": np.ones((40, 2)),
+        "tiny extent": 1e-300 * rng.random((500, 2)),
+    }
+
+
+@pytest.mark.parametrize("name", list(_maxmin_layout_cases()))
+def test_host_maxmin_layouts_match_oracle(name):
+    c = np.ascontiguousarray(_maxmin_layout_cases()[name], dtype=np.float64)
+    assert G.maxmin_order(c).tolist() == O.maxmin_order(c).tolist()
+
+
+def test_host_maxmin_matches_exact_traversal():
+    # the O(n^2) farthest-point traversal of the reference's test helper
+    # (vecchia.rs:2244-2275) on both layouts
+    rng = np.random.default_rng(23)
+    for c in (rng.random((700, 2)), rng.random((600, 3)),
+              np.r_[rng.random((10, 2)), 0.5 + 1e-7 * rng.random((590, 2))]):
+        assert G.maxmin_order(c).tolist() == O.maxmin_order_brute(c).tolist()
+
+
+def test_host_maxmin_non_finite_input_gives_a_permutation():
+    # point sets reject non-finite coordinates; the ordering itself still
+    # returns a permutation for them (no ordering is defined by the reference)
+    rng = np.random.default_rng(29)
+    c = rng.random((500, 2))
+    c[7, 0] = np.nan
+    c[100, 1] = np.inf
+    assert sorted(G.maxmin_order(c).tolist()) == list(range(500))
+
+
 def test_nelder_mead_state_machine_matches_reference_sequence():
     rosen = lambda x: (1 - x[0]) ** 2 + 100 * (x[1] - x[0] ** 2) ** 2
     for starts in ([[-1.2, 1.0]], [[-1.2, 1.0], [0.5, 0.5], [2.0, -1.0]]):
