@@ -264,7 +264,11 @@ int gs_kriging_neighbors(const gs_kriging* k, int64_t nt, const double* tx, cons
                          void* stream);
 
 /* vecchia::maxmin_order (crates/geostat-core/src/vecchia.rs:144-215), on
- * the host as in the reference. */
+ * the host as in the reference: the same order (first the point nearest the
+ * centroid, then the largest squared distance to the selected points, ties
+ * to the larger index), found by an exact eager search instead of the
+ * reference's lazily refreshed heap.  Non-finite coordinates (which point
+ * sets reject) still give a permutation. */
 int gs_maxmin_order(int dim, int64_t n, const double* x, const double* y, const double* z,
                     int64_t* order);
 /* vecchia_plan (vecchia.rs:232-282): order == NULL uses maxmin_order; the
